@@ -1,0 +1,1735 @@
+// Oracle test infrastructure -- not part of the product (see rv_oracle.h).
+//
+// A sequential CPU restatement of RabbitVar's per-region path, written to be
+// read beside the reference: every function names the reference lines it
+// restates.  Containers are ordered std::maps (the reference uses robin_hood
+// hash maps); where the reference's behaviour depends on its hash map's
+// iteration order this restatement uses an order measured from the
+// reference's map (noted at the use), or ascending position order.
+#include "rv_oracle.h"
+#include "fisher_oracle.h"
+
+#include <omp.h>
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <set>
+#include <string>
+#include <vector>
+
+namespace {
+
+using std::map;
+using std::string;
+using std::vector;
+
+const char kNt16[] = "=ACMGRSVTWYHKDBN";
+
+enum { OP_M = 0, OP_I = 1, OP_D = 2, OP_N = 3, OP_S = 4, OP_H = 5 };
+
+// Statistics of one allele key: include/Variation.h:12-82.
+struct Stat {
+    int cnt = 0, fwd = 0, rev = 0;
+    double pmean = 0, qmean = 0, mq = 0, nm = 0;
+    int lo = 0, hi = 0;
+    bool pstd = false, qstd = false;
+    int pp = 0;
+    double pq = 0;
+    int extracnt = 0;
+    void inc_dir(bool d) { d ? ++rev : ++fwd; }
+};
+
+// Soft-clip aggregate: include/Sclip.h:10-39.
+struct Clip : Stat {
+    map<int, map<char, int>> nt;
+    map<int, map<char, Stat>> seq;
+    string cons;  // cached consensus ("" = not computed yet)
+    bool used = false;
+};
+
+using KeyMap = map<string, Stat>;
+
+struct Maps {
+    map<int, KeyMap> nonins, ins;
+    map<int, int> cov;
+    map<int, Clip> sc5, sc3;
+    map<int, map<string, int>> inscnt, delcnt, mnp;
+    int max_read_len = 0;
+};
+
+// Reference window: RecordPreprocessor::makeReference
+// (src/recordPreprocessor.cpp:41-78) loads [lo, hi] where
+// hi = min(len, end + x + ext) - CONF_SEED_1 (17).  Lookups through the hash
+// map's operator[] insert a 0 for a missing position (robin_hood semantics);
+// those "phantom" entries then count as present with base 0.
+struct Ref {
+    const char *contig = nullptr;
+    int clen = 0, lo = 1, hi = 0;
+    std::set<int> phantom;
+    static char up(char c) { return (c >= 'a' && c <= 'z') ? (char)(c - 32) : c; }
+    bool has(int p) const { return (p >= lo && p <= hi) || phantom.count(p); }
+    char at(int p) const { return (p >= lo && p <= hi) ? up(contig[p - 1]) : 0; }
+    char idx(int p) {  // operator[]
+        if (p >= lo && p <= hi) return up(contig[p - 1]);
+        phantom.insert(p);
+        return 0;
+    }
+    bool has_eq(char c, int p) const { return has(p) && at(p) == c; }
+    bool has_ne(char c, int p) const { return has(p) && at(p) != c; }
+};
+
+struct ReadView {
+    int32_t pos, mpos, nm;
+    uint16_t flag;
+    uint8_t mapq;
+    int lseq;
+    vector<uint32_t> cig;      // CIGAR words followed by the bytes that follow them in a BAM record
+    int n_cigar;
+    vector<char> seq;          // decoded bases
+    vector<uint8_t> qual_buf;  // [byte preceding quals] + quals
+    const uint8_t *qual() const { return qual_buf.data() + 1; }
+};
+
+// ---------------------------------------------------------------------------
+// per-read walk: CigarParser (src/parseCigar.cpp)
+// ---------------------------------------------------------------------------
+struct Walker {
+    const rvo_params &P;
+    Maps &M;
+    Ref &R;
+    int rs, re;  // region start/end
+    int chr_len;
+    // CigarParser members
+    int start = 0, offset = 0, cel = 0, rpis = 0, rpes = 0, n_cigar = 0;
+    vector<uint32_t> *cigar = nullptr;
+    const ReadView *rv = nullptr;
+
+    Walker(const rvo_params &p, Maps &m, Ref &r, int s, int e, int cl) : P(p), M(m), R(r), rs(s), re(e), chr_len(cl) {}
+
+    static int op(uint32_t c) { return (int)(c & 15); }
+    static int oplen(uint32_t c) { return (int)(c >> 4); }
+    int cop(int i) const { return op((*cigar)[i]); }
+    int clen_(int i) const { return oplen((*cigar)[i]); }
+
+    Stat &getvar(map<int, KeyMap> &h, int p, const string &k) { return h[p][k]; }
+
+    // addCnt: src/parseCigar.cpp:318-343
+    void add_cnt(Stat &v, bool dir, int rp, double bq, int mq, int nm) {
+        v.cnt++;
+        dir ? v.rev++ : v.fwd++;
+        v.pmean += rp;
+        v.qmean += bq;
+        v.mq += mq;
+        v.nm += nm;
+        if (bq >= P.goodq) v.hi++; else v.lo++;
+    }
+
+    int tp_of(int rlen) const {  // src/parseCigar.cpp:896-898
+        return rpes < rlen - rpes ? rpes + 1 : rlen - rpes;
+    }
+
+    void pq_update(Stat &v, int tp, double q) {  // pstd/qstd rule, src/parseCigar.cpp:902-914
+        if (!v.pstd && v.pp != 0 && tp != v.pp) v.pstd = true;
+        if (!v.qstd && v.pq != 0 && q != v.pq) v.qstd = true;
+    }
+
+    // isTrimAtOptTBases: src/parseCigar.cpp:158-167
+    bool trim(bool dir, int tlen) const {
+        if (P.trim_bases_after != 0) {
+            if (!dir) return rpis > P.trim_bases_after;
+            return tlen - rpis > P.trim_bases_after;
+        }
+        return false;
+    }
+
+    // findOffset: src/parseCigar.cpp:208-256
+    int find_offset(int refp, int readp, int clen, string &sq, long &qsum, int &tnm) {
+        const vector<char> &s = rv->seq;
+        const uint8_t *q = rv->qual();
+        int off = 0, vsn = 0;
+        tnm = 0;
+        for (int vi = 0; vsn <= P.vext && vi < clen; vi++) {
+            if (s[readp + vi] == 'N') break;
+            if (q[readp + vi] < P.goodq) break;
+            if (R.has(refp + vi)) {
+                if (s[readp + vi] != R.at(refp + vi)) { off = vi + 1; tnm++; vsn = 0; }
+                else vsn++;
+            }
+        }
+        qsum = 0;
+        sq.clear();
+        if (off > 0) {
+            sq.assign(&s[readp], off);
+            for (int i = readp; i < readp + off; i++) qsum += q[i];
+            for (int i = 0; i < off; i++) M.cov[refp + i]++;
+        }
+        return off;
+    }
+
+    // isInsertionOrDeletionWithNextMatched: src/parseCigar.cpp:1817-1826
+    // (reads the CIGAR word at ci+3 even when it lies past the last op)
+    bool indel_next_matched(int ci) const {
+        return P.local_realign && n_cigar > ci + 2 && clen_(ci + 1) <= P.vext && cop(ci + 1) == OP_M &&
+               (cop(ci + 2) == OP_I || cop(ci + 2) == OP_D) && cop(ci + 3) != OP_I && cop(ci + 3) != OP_D;
+    }
+    bool next_matched(int ci) const { return P.local_realign && n_cigar > ci + 1 && cop(ci + 1) == OP_M; }
+    bool next_after_num_matched(int ci, int number) const {  // src/parseCigar.cpp:1084-1087
+        return n_cigar > ci + number && cop(ci + 1) == OP_M;
+    }
+
+    // appendSegments: src/parseCigar.cpp:1756-1815
+    void append_segments(int ci, string &desc, long &qsum, int &qcnt, int mlen, int indel_len, int begin, bool is_ins) {
+        const vector<char> &s = rv->seq;
+        const uint8_t *q = rv->qual();
+        desc += "#";
+        desc.append(&s[begin], mlen);
+        for (int i = begin; i < begin + mlen; i++) qsum += q[i];
+        desc += "^";
+        if (cop(ci + 2) == OP_I) desc.append(&s[begin + mlen], indel_len);
+        else desc += std::to_string(indel_len);
+        if (cop(ci + 2) == OP_I) {
+            for (int i = begin + mlen; i < begin + mlen + indel_len; i++) qsum += q[i];
+            qcnt += indel_len;
+        } else if (is_ins) {
+            qsum += q[begin + mlen];
+            qcnt += 1;
+        }
+    }
+
+    // process_softclip: src/parseCigar.cpp:1112-1301
+    void softclip(int ci, bool dir, int mapq, int nom, int position, int tlen) {
+        const vector<char> &s = rv->seq;
+        const uint8_t *q = rv->qual();
+        if (ci == 0) {
+            while (cel - 1 >= 0 && start - 1 > 0 && start - 1 <= chr_len && R.has_eq(s[cel - 1], start - 1) &&
+                   q[cel - 1] > 10) {
+                Stat &v = getvar(M.nonins, start - 1, string(1, R.idx(start - 1)));
+                add_cnt(v, dir, cel, q[cel - 1], mapq, nom);
+                M.cov[start - 1]++;
+                start--;
+                cel--;
+            }
+            if (cel > 0) {
+                int sumq = 0, nhq = 0, nlq = 0;
+                for (int si = cel - 1; si >= 0; si--) {
+                    if (s[si] == 'N') break;
+                    int bq = q[si];
+                    if (bq <= 12) nlq++;
+                    if (nlq > 1) break;
+                    sumq += bq;
+                    nhq++;
+                }
+                if (nhq >= 1 && nhq > nlq && start >= rs && start <= re) {
+                    Clip &sc = M.sc5[start];
+                    for (int si = cel - 1; cel - si <= nhq; si--) {
+                        char ch = s[si];
+                        int idx = cel - 1 - si;
+                        sc.nt[idx][ch]++;
+                        add_cnt(sc.seq[idx][ch], dir, si - (cel - nhq), q[si], mapq, nom);
+                    }
+                    add_cnt(sc, dir, cel, sumq / (double)nhq, mapq, nom);
+                }
+            }
+            cel = clen_(ci);
+        } else if (ci == n_cigar - 1) {
+            while (rpis < rv->lseq && R.has_eq(s[rpis], start) && q[rpis] > 10) {
+                Stat &v = getvar(M.nonins, start, string(1, R.at(start)));
+                add_cnt(v, dir, tlen - rpes, q[rpis], mapq, nom);
+                M.cov[start]++;
+                rpis++;
+                start++;
+                cel--;
+                rpes++;
+            }
+            if (rpis < rv->lseq) {
+                int sumq = 0, nhq = 0, nlq = 0;
+                for (int si = 0; si < cel; si++) {
+                    if (s[rpis + si] == 'N') break;
+                    int bq = q[rpis + si];
+                    if (bq <= 12) nlq++;
+                    if (nlq > 1) break;
+                    sumq += bq;
+                    nhq++;
+                }
+                if (nhq >= 1 && nhq > nlq && start >= rs && start <= re) {
+                    Clip &sc = M.sc3[start];
+                    for (int si = 0; si < nhq; si++) {
+                        char ch = s[rpis + si];
+                        sc.nt[si][ch]++;
+                        add_cnt(sc.seq[si][ch], dir, nhq - si, q[rpis + si], mapq, nom);
+                    }
+                    add_cnt(sc, dir, cel, sumq / (double)nhq, mapq, nom);
+                }
+            }
+        }
+        rpis += cel;
+        offset = 0;
+        start = position;
+    }
+
+    // adjInsPos: include/VariationUtils.h:99-113 (3' rotation of an
+    // all-ACGT insertion while the preceding reference base repeats it)
+    int adj_ins_pos(int bi, string &ins) {
+        int n = 1;
+        int len = (int)ins.size();
+        while (R.idx(bi) == ins[len - n]) {
+            n++;
+            if (n > len) n = 1;
+            bi--;
+        }
+        if (n > 1) ins = ins.substr(len - (n - 1)) + ins.substr(0, len - (n - 1));
+        return bi;
+    }
+
+    static bool all_acgt(const string &s) {
+        if (s.empty()) return false;
+        for (char c : s)
+            if (c != 'A' && c != 'C' && c != 'G' && c != 'T') return false;
+        return true;
+    }
+
+    // process_insertion: src/parseCigar.cpp:1303-1523
+    int insertion(int ci, bool dir, int mapq, int nom, int position, int rlen) {
+        const vector<char> &s = rv->seq;
+        const uint8_t *q = rv->qual();
+        if ((n_cigar > ci + 1 && cop(ci + 1) == OP_N) || (ci > 0 && cop(ci - 1) == OP_N)) {
+            rpis += cel;
+            return ci;
+        }
+        string desc(&s[rpis], cel);
+        long qsum = 0;
+        int qcnt = 0;
+        for (int i = rpis; i < rpis + cel; i++) qsum += q[i];
+        qcnt += cel;
+        string ss;
+        int multoffs = 0, multoffp = 0, nmoff = 0;
+        if (indel_next_matched(ci)) {
+            int mlen = clen_(ci + 1), indel_len = clen_(ci + 2);
+            int begin = rpis + cel;
+            append_segments(ci, desc, qsum, qcnt, mlen, indel_len, begin, true);
+            multoffs += mlen + (cop(ci + 2) == OP_D ? indel_len : 0);
+            multoffp += mlen + (cop(ci + 2) == OP_I ? indel_len : 0);
+            int ci6 = n_cigar > ci + 3 ? clen_(ci + 3) : 0;
+            if (ci6 != 0 && cop(ci + 3) == OP_M) {
+                long qs;
+                int tnm;
+                offset = find_offset(start + multoffs, rpis + cel + multoffp, ci6, ss, qs, tnm);
+                qsum += qs;
+                qcnt += offset;
+            }
+            ci += 2;
+        } else if (next_matched(ci)) {
+            int vsn = 0;
+            for (int vi = 0; vsn <= P.vext && vi < clen_(ci + 1); vi++) {
+                if (s[rpis + cel + vi] == 'N') break;
+                if (q[rpis + cel + vi] < P.goodq) break;
+                if (R.has(start + vi)) {
+                    if (s[rpis + cel + vi] != R.at(start + vi)) { offset = vi + 1; nmoff++; vsn = 0; }
+                    else vsn++;
+                }
+            }
+            if (offset != 0) {
+                ss.append(&s[rpis + cel], offset);
+                for (int i = rpis + cel; i < rpis + cel + offset; i++) qsum += q[i];
+                qcnt += offset;
+                for (int osi = 0; osi < offset; osi++) M.cov[start + osi]++;
+            }
+        }
+        if (offset > 0) desc += "&" + ss;
+        if (start - 1 >= rs && start - 1 <= re && desc.find('N') == string::npos) {
+            int inspos = start - 1;
+            if (all_acgt(desc)) {
+                string d2 = desc;
+                int bi = adj_ins_pos(start - 1, d2);
+                if (rpis - 1 - (start - 1 - bi) > 0) {
+                    inspos = bi;
+                    desc = d2;
+                }
+            }
+            string key = "+" + desc;
+            M.inscnt[inspos][key]++;
+            Stat &hv = getvar(M.ins, inspos, key);
+            hv.inc_dir(dir);
+            hv.cnt++;
+            int tp = tp_of(rlen);
+            double tmpq = (double)qsum / qcnt;
+            pq_update(hv, tp, tmpq);
+            hv.pmean += tp;
+            hv.qmean += tmpq;
+            hv.mq += mapq;
+            hv.pp = tp;
+            hv.pq = tmpq;
+            if (tmpq >= P.goodq) hv.hi++; else hv.lo++;
+            hv.nm += nom - nmoff;
+            int index = rpis - 1 - (start - 1 - inspos);
+            if (inspos > position && R.has_eq(s[index], inspos)) {
+                // getVariationMaybe: the subtraction applies only if the key exists now
+                auto it = M.nonins.find(inspos);
+                if (it != M.nonins.end()) {
+                    auto it2 = it->second.find(string(1, s[index]));
+                    if (it2 != it->second.end()) {
+                        Stat &tv = it2->second;
+                        tv.cnt--;
+                        dir ? tv.rev-- : tv.fwd--;
+                        tv.pmean -= tp;
+                        tv.qmean -= q[index];
+                        tv.mq -= mapq;
+                        tv.nm -= (nom - nmoff);
+                        if (q[index] >= P.goodq) tv.hi--; else tv.lo--;
+                    }
+                }
+            }
+            if (ci == 1 && (cop(0) == OP_S || cop(0) == OP_H)) {
+                Stat &tt = getvar(M.nonins, inspos, string(1, R.idx(inspos)));
+                tt.inc_dir(dir);
+                tt.cnt++;
+                tt.pstd = hv.pstd;
+                tt.qstd = hv.qstd;
+                tt.pmean += tp;
+                tt.qmean += tmpq;
+                tt.mq += mapq;
+                tt.pp = tp;
+                tt.pq = tmpq;
+                tt.nm += nom - nmoff;
+                M.cov[inspos]++;
+            }
+        }
+        rpis += cel + offset + multoffp;
+        rpes += cel + offset + multoffp;
+        start += offset + multoffs;
+        return ci;
+    }
+
+    // process_deletion + addVariationForDeletion: src/parseCigar.cpp:1525-1727, 1036-1082
+    int deletion(int ci, bool dir, int mapq, int nom, int rlen) {
+        const vector<char> &s = rv->seq;
+        const uint8_t *q = rv->qual();
+        if ((n_cigar > ci && cop(ci + 1) == OP_N) || (ci > 1 && cop(ci - 1) == OP_N)) {
+            rpis += cel;
+            return ci;
+        }
+        string desc = "-" + std::to_string(cel);
+        string app;
+        uint8_t qlast = q[rpis - 1];
+        long qsum = 0;
+        int qcnt = 0;
+        int multoffs = 0, multoffp = 0, nmoff = 0;
+        if (indel_next_matched(ci)) {
+            int mlen = clen_(ci + 1), indel_len = clen_(ci + 2);
+            append_segments(ci, desc, qsum, qcnt, mlen, indel_len, rpis, false);
+            multoffs += mlen + (cop(ci + 2) == OP_D ? indel_len : 0);
+            multoffp += mlen + (cop(ci + 2) == OP_I ? indel_len : 0);
+            if (next_after_num_matched(ci, 3)) {
+                int vsn = 0, tn = rpis + multoffp, ts = start + multoffs + cel;
+                for (int vi = 0; vsn <= P.vext && vi < clen_(ci + 3); vi++) {
+                    if (s[tn + vi] == 'N') break;
+                    if (q[tn + vi] < P.goodq) break;
+                    if (R.has_eq('N', ts + vi)) break;
+                    if (R.has(ts + vi)) {
+                        if (s[tn + vi] != R.at(ts + vi)) { offset = vi + 1; nmoff++; vsn = 0; }
+                        else vsn++;
+                    }
+                }
+                if (offset != 0) {
+                    app.append(&s[tn], offset);
+                    for (int i = tn; i < tn + offset; i++) qsum += q[i];
+                    qcnt += offset;
+                }
+            }
+            ci += 2;
+        } else if (P.local_realign && n_cigar > ci + 1 && cop(ci + 1) == OP_I) {
+            int ins_len = clen_(ci + 1);
+            desc += "^";
+            desc.append(&s[rpis], ins_len);
+            for (int i = rpis; i < rpis + ins_len; i++) qsum += q[i];
+            qcnt += ins_len;
+            multoffp += ins_len;
+            // the reference's follow-up scan here requires op(ci+1) == M, which
+            // cannot hold when op(ci+1) == I (src/parseCigar.cpp:1598-1626)
+            ci += 1;
+        } else if (next_matched(ci)) {
+            int mlen = clen_(ci + 1), vsn = 0;
+            for (int vi = 0; vsn <= P.vext && vi < mlen; vi++) {
+                char sc = s[rpis + vi];
+                if (sc == 'N') break;
+                if (q[rpis + vi] < P.goodq) break;
+                if (R.has(start + cel + vi)) {
+                    char rc = R.at(start + cel + vi);
+                    if (rc == 'N') break;
+                    if (sc != rc) { offset = vi + 1; nmoff++; vsn = 0; }
+                    else vsn++;
+                }
+            }
+            if (offset != 0) {
+                app.append(&s[rpis], offset);
+                for (int i = rpis; i < rpis + offset; i++) qsum += q[i];
+                qcnt += offset;
+            }
+        }
+        if (offset > 0) desc += "&" + app;
+        if (rpis + offset >= rv->lseq) {
+            qsum += qlast;
+            qcnt += 1;
+        } else {
+            uint8_t qo = q[rpis + offset];
+            qsum += qlast > qo ? qlast : qo;
+            qcnt += 1;
+        }
+        if (start >= rs && start <= re) {
+            Stat &hv = getvar(M.nonins, start, desc);
+            M.delcnt[start][desc]++;
+            hv.inc_dir(dir);
+            hv.cnt++;
+            int tp = tp_of(rlen);
+            double tmpq = (double)qsum / qcnt;
+            pq_update(hv, tp, tmpq);
+            hv.pmean += tp;
+            hv.qmean += tmpq;
+            hv.mq += mapq;
+            hv.pp = tp;
+            hv.pq = tmpq;
+            hv.nm += nom - nmoff;
+            if (tmpq >= P.goodq) hv.hi++; else hv.lo++;
+            for (int i = 0; i < cel; i++) M.cov[start + i]++;
+        }
+        start += cel + offset + multoffs;
+        rpis += offset + multoffp;
+        rpes += offset + multoffp;
+        return ci;
+    }
+
+    static bool is_mnv_key(const string &k) {  // isBEGIN_ATGC_AMP_ATGCs_END: src/parseCigar.cpp:476-495
+        if (k.size() <= 2 || k[1] != '&') return false;
+        auto acgt = [](char c) { return c == 'A' || c == 'C' || c == 'G' || c == 'T'; };
+        if (!acgt(k[0])) return false;
+        for (size_t i = 2; i < k.size(); i++)
+            if (!acgt(k[i])) return false;
+        return true;
+    }
+
+    // skipOverlappingReads / isReadsOverlap: src/parseCigar.cpp:180-206
+    bool skip_overlapping(int position, bool dir, int mate_start, int orig_ref_len, int endpos) const {
+        const ReadView &r = *rv;
+        bool paired_same = (r.flag & 1) && true;  // tid == mtid for single-contig inputs
+        if (P.unique_fwd && paired_same && !dir && start >= mate_start) return true;
+        if (P.unique_first && (r.flag & 1) && paired_same) {
+            bool ov;
+            if (position >= mate_start) ov = start >= mate_start && start <= mate_start + orig_ref_len - 1;
+            else ov = start >= mate_start && r.mpos + 1 <= endpos;
+            if (ov) return true;
+        }
+        return false;
+    }
+
+    // parseCigar: src/parseCigar.cpp:497-974
+    void parse(const ReadView &r) {
+        rv = &r;
+        vector<uint32_t> cg = r.cig;
+        cigar = &cg;
+        n_cigar = r.n_cigar;
+        if (n_cigar <= 0) return;
+        const vector<char> &s = r.seq;
+        const uint8_t *q = r.qual();
+        int idl = 0;
+        for (int i = 0; i < n_cigar; i++)
+            if (cop(i) == OP_I || cop(i) == OP_D) idl += clen_(i);
+        int nom = 0;
+        if (r.nm != INT32_MIN) {
+            nom = r.nm - idl;
+            if (nom > P.mismatch) return;
+        } else if (r.flag & 4) {
+            return;
+        }
+        bool dir = (r.flag & 16) != 0;
+        int mapq = r.mapq;
+        int position = r.pos + 1;
+        rpis = rpes = 0;
+        // (local realignment's CIGAR rewrite is not restated here)
+        // cleanupCigar: src/parseCigar.cpp:1858-1892
+        for (int pass = 0; pass < 2; pass++) {
+            bool none = true;
+            for (int k = 0; k < n_cigar && none; k++) {
+                int c = pass == 0 ? k : n_cigar - 1 - k;
+                int o = cop(c);
+                if (o == OP_I) cg[c] = (cg[c] & ~15u) | OP_S;
+                else if (o == 0 || o == 7 || o == 8) none = false;
+            }
+        }
+        start = position;
+        offset = 0;
+        if (cop(0) == OP_S && clen_(0) >= 10 && cop(n_cigar - 1) == OP_S && clen_(n_cigar - 1) >= 10) return;
+        int rlen = 0, tlen = 0;
+        for (int i = 0; i < n_cigar; i++) {
+            int o = cop(i);
+            if (o == OP_M || o == OP_I) rlen += clen_(i);
+            if (o == OP_M || o == OP_I || o == OP_S) tlen += clen_(i);
+        }
+        if (P.minmatch != 0 && rlen < P.minmatch) return;
+        if (tlen > M.max_read_len) M.max_read_len = tlen;
+        if (r.flag & 2048) return;
+        int mate_start = r.mpos + 1;
+        int orig_ref_len = 0;
+        for (int i = 0; i < r.n_cigar; i++) {
+            int o = op(cg[i]);
+            if (o == 0 || o == 2 || o == 3 || o == 7 || o == 8) orig_ref_len += oplen(cg[i]);
+        }
+        int endpos = orig_ref_len ? r.pos + orig_ref_len : r.pos + 1;
+        bool need_break = true;
+        for (int ci = 0; ci < n_cigar; ++ci) {
+            if (need_break && skip_overlapping(position, dir, mate_start, orig_ref_len, endpos)) break;
+            need_break = false;
+            int c_op = cop(ci);
+            cel = clen_(ci);
+            if ((ci == 0 || ci == n_cigar - 1) && c_op == OP_I) c_op = OP_S;
+            if (c_op == OP_N) {  // processNotMatched: src/parseCigar.cpp:1733-1753
+                start += cel;
+                offset = 0;
+                continue;
+            }
+            if (c_op == OP_S) { softclip(ci, dir, mapq, nom, position, tlen); continue; }
+            if (c_op == OP_H) { offset = 0; continue; }
+            if (c_op == OP_I) { offset = 0; ci = insertion(ci, dir, mapq, nom, position, rlen); continue; }
+            if (c_op == OP_D) { offset = 0; ci = deletion(ci, dir, mapq, nom, rlen); continue; }
+            int nmoff = 0, moffset = 0;
+            for (int i = offset; i < cel; i++) {
+                bool tr = trim(dir, tlen);
+                char ch1 = s[rpis];
+                string key(1, ch1);
+                bool swd = false;
+                if (ch1 == 'N') {
+                    start++;
+                    rpis++;
+                    rpes++;
+                    continue;
+                }
+                double qv = q[rpis];
+                int qbases = 1, qibases = 0;
+                string ss;
+                // MNV growth: src/parseCigar.cpp:711-767
+                while ((start + 1) >= rs && (start + 1) <= re && (i + 1) < cel && qv >= P.goodq &&
+                       R.has_ne(s[rpis], start) && R.idx(start) != 'N') {
+                    if (q[rpis + 1] < P.goodq + 5) break;
+                    char nuc = s[rpis + 1];
+                    if (nuc == 'N') break;
+                    if (R.has_eq('N', start + 1)) break;
+                    if (R.idx(start + 1) != nuc) {
+                        ss += nuc;
+                        qv += q[rpis + 1];
+                        qbases++;
+                        rpis++;
+                        rpes++;
+                        i++;
+                        start++;
+                        nmoff++;
+                    } else {
+                        int ssn = 0;
+                        for (int ssi = 1; ssi <= P.vext; ssi++) {
+                            if (i + 1 + ssi >= cel) break;
+                            if (rpis + 1 + ssi < r.lseq && R.has_ne(s[rpis + 1 + ssi], start + 1 + ssi)) {
+                                ssn = ssi + 1;
+                                break;
+                            }
+                        }
+                        if (ssn == 0) break;
+                        if (q[rpis + ssn] < P.goodq + 5) break;
+                        for (int ssi = 1; ssi <= ssn; ssi++) {
+                            ss += s[rpis + ssi];
+                            qv += q[rpis + ssi];
+                            qbases++;
+                        }
+                        rpis += ssn;
+                        rpes += ssn;
+                        i += ssn;
+                        start += ssn;
+                    }
+                }
+                if (!ss.empty()) key = key + "&" + ss;
+                int ddlen = 0;
+                // complex deletion / insertion tails: src/parseCigar.cpp:779-882
+                if (P.local_realign && cel - i <= P.vext && ci + 1 < n_cigar && cop(ci + 1) == OP_D && R.has(start) &&
+                    (!ss.empty() || s[rpis] != R.at(start)) && q[rpis] >= P.goodq) {
+                    while (i + 1 < cel) {
+                        key += s[rpis + 1];
+                        qv += q[rpis + 1];
+                        qbases++;
+                        i++;
+                        rpis++;
+                        rpes++;
+                        start++;
+                    }
+                    size_t amp = key.find('&');
+                    if (amp != string::npos) key.erase(amp, 1);
+                    key = "-" + std::to_string(clen_(ci + 1)) + "&" + key;
+                    swd = true;
+                    ddlen = clen_(ci + 1);
+                    ci += 1;
+                    if (n_cigar > ci + 1 && cop(ci + 1) == OP_I) {
+                        int nl = clen_(ci + 1);
+                        key += "^";
+                        key.append(&s[rpis + 1], nl);
+                        for (int qi = 1; qi <= nl; qi++) {
+                            qv += q[rpis + 1 + qi];
+                            qibases++;
+                        }
+                        rpis += nl;
+                        rpes += nl;
+                        ci += 1;
+                    }
+                    if (next_after_num_matched(ci, 1)) {
+                        string sq;
+                        long qs;
+                        int tnm;
+                        int to = find_offset(start + ddlen + 1, rpis + 1, clen_(ci + 1), sq, qs, tnm);
+                        if (to != 0) {
+                            moffset = to;
+                            nmoff += tnm;
+                            key += "&" + sq;
+                            // the reference adds an always-empty quality string here
+                        }
+                    }
+                } else if (P.local_realign && cel - i <= P.vext && ci + 1 < n_cigar && cop(ci + 1) == OP_I &&
+                           R.has(start) && (!ss.empty() || s[rpis] != R.at(start)) && q[rpis] >= P.goodq) {
+                    while (i + 1 < cel) {
+                        key += s[rpis + 1];
+                        qv += q[rpis + 1];
+                        qbases++;
+                        i++;
+                        rpis++;
+                        rpes++;
+                        start++;
+                    }
+                    size_t amp = key.find('&');
+                    if (amp != string::npos) key.erase(amp, 1);
+                    int nl = clen_(ci + 1);
+                    key.append(&s[rpis + 1], nl);
+                    key.insert((size_t)nl, "&");
+                    key = "+" + key;
+                    for (int qi = 1; qi <= nl; qi++) {
+                        qv += q[rpis + 1 + qi];
+                        qibases++;
+                    }
+                    rpis += nl;
+                    rpes += nl;
+                    ci += 1;
+                    qibases--;
+                    qbases++;
+                }
+                if (!tr) {
+                    int p = start - qbases + 1;
+                    if (p >= rs && p <= re) {
+                        Stat &hv = getvar(M.nonins, p, key);
+                        hv.inc_dir(dir);
+                        if (is_mnv_key(key)) M.mnp[p][key]++;
+                        hv.cnt++;
+                        int tp = tp_of(rlen);
+                        qv = qv / (qbases + qibases);
+                        pq_update(hv, tp, qv);
+                        hv.pmean += tp;
+                        hv.qmean += qv;
+                        hv.mq += mapq;
+                        hv.pp = tp;
+                        hv.pq = qv;
+                        hv.nm += nom - nmoff;
+                        if (qv >= P.goodq) hv.hi++; else hv.lo++;
+                        for (int qi = 1; qi <= qbases; qi++) M.cov[start - qi + 1]++;
+                        if (swd) {
+                            M.delcnt[p][key]++;
+                            for (int qi = 1; qi < ddlen; qi++) M.cov[start + qi]++;
+                        }
+                    }
+                }
+                if (swd) start += ddlen;
+                if (c_op != OP_I) start++;
+                if (c_op != OP_D) {
+                    rpis++;
+                    rpes++;
+                }
+            }
+            if (moffset != 0) {
+                offset = moffset;
+                rpis += moffset;
+                start += moffset;
+                rpes += moffset;
+            }
+            if (start > re) break;
+        }
+    }
+};
+
+// ---------------------------------------------------------------------------
+// local realigner, MNP part: VariationRealigner::adjustMNP
+// (src/VariationRealigner.cpp:334-465)
+// ---------------------------------------------------------------------------
+// The reference iterates the per-offset base counts of a soft clip in its
+// hash map's order; for the keys A,C,G,T,N that order was measured to be
+// N, A, T, G, C regardless of insertion order.
+int char_rank(char c) {
+    switch (c) {
+    case 'N': return 0;
+    case 'A': return 1;
+    case 'T': return 2;
+    case 'G': return 3;
+    case 'C': return 4;
+    default: return 5 + (unsigned char)c;
+    }
+}
+
+bool low_complexity(const string &seq) {  // islowcomplexseq: include/VariationUtils.h:366-395
+    int len = (int)seq.size();
+    if (len == 0) return true;
+    int ntcnt = 0;
+    for (char b : string("ATGC")) {
+        int c = (int)std::count(seq.begin(), seq.end(), b);
+        if (c > 0) ntcnt++;
+        if (c / (double)len > 0.75) return true;
+    }
+    return ntcnt < 3;
+}
+
+// findconseq: include/VariationUtils.h:403-509
+string consensus(Clip &sc) {
+    if (!sc.cons.empty()) return sc.cons;
+    int total = 0, match = 0;
+    string seqq;
+    bool flag = false;
+    for (auto &nve : sc.nt) {
+        int pos_in = nve.first;
+        vector<std::pair<char, int>> nv(nve.second.begin(), nve.second.end());
+        std::sort(nv.begin(), nv.end(), [](const std::pair<char, int> &a, const std::pair<char, int> &b) {
+            return char_rank(a.first) < char_rank(b.first);
+        });
+        int maxc = 0, tt = 0;
+        double maxq = 0;
+        char chosen = 0;
+        for (auto &e : nv) {
+            tt += e.second;
+            double sq = 0;
+            bool has = false;
+            auto it = sc.seq.find(pos_in);
+            if (it != sc.seq.end()) {
+                auto it2 = it->second.find(e.first);
+                if (it2 != it->second.end()) { has = true; sq = it2->second.qmean; }
+            }
+            if (e.second > maxc || (has && sq > maxq)) {
+                maxc = e.second;
+                chosen = e.first;
+                maxq = has ? sq : 0;  // operator[] creates an empty entry when absent
+            }
+        }
+        if (pos_in == 3 && sc.nt.size() >= 6 && tt / (double)sc.cnt < 0.2 && tt <= 2) break;
+        if ((tt - maxc > 2 || maxc <= tt - maxc) && maxc / (double)tt < 0.8) {
+            if (flag) break;
+            flag = true;
+        }
+        total += tt;
+        match += maxc;
+        if (chosen != 0) seqq += chosen;
+    }
+    string SEQ;
+    int nts = (int)sc.nt.size();
+    int sl = (int)seqq.size();
+    if (total != 0 && match / (double)total > 0.9 && sl / 1.5 > nts - sl &&
+        (sl / (double)nts > 0.8 || nts - sl < 10 || sl > 25))
+        SEQ = seqq;
+    else
+        SEQ = " ";
+    if (!SEQ.empty() && SEQ.size() > 12) {  // CONF_SEED_2
+        bool a7 = SEQ.size() >= 8 && SEQ.compare(1, 7, "AAAAAAA") == 0;
+        bool t7 = SEQ.size() >= 8 && SEQ.compare(1, 7, "TTTTTTT") == 0;
+        if (a7 || t7) sc.used = true;
+        if (low_complexity(SEQ)) sc.used = true;
+    }
+    sc.cons = SEQ;
+    return SEQ;
+}
+
+void adj_cnt(Stat &to, const Stat &v) {  // adjCnt: include/VariationUtils.h:338-352
+    to.cnt += v.cnt;
+    to.extracnt += v.cnt;
+    to.hi += v.hi;
+    to.lo += v.lo;
+    to.pmean += v.pmean;
+    to.qmean += v.qmean;
+    to.mq += v.mq;
+    to.nm += v.nm;
+    to.pstd = true;
+    to.qstd = true;
+    to.rev += v.rev;
+    to.fwd += v.fwd;
+}
+
+// ismatchref: src/VariationRealigner.cpp:2004-2024 (MM = 3)
+bool ismatchref(const string &sq, Ref &R, int position, int dir) {
+    int mm = 0;
+    int len = (int)sq.size();
+    for (int n = 0; n < len; n++) {
+        if (!R.has(position + dir * n)) return false;
+        char c = dir == 1 ? sq[n] : sq[len - n - 1];
+        if (c != R.idx(position + dir * n)) mm++;
+    }
+    return mm <= 3 && mm / (double)len < 0.15;
+}
+
+void adjust_mnp(Maps &M, Ref &R) {
+    struct T { int pos; string key; int cnt; };
+    vector<T> tmp;
+    for (auto &pe : M.mnp)
+        for (auto &ke : pe.second) tmp.push_back({pe.first, ke.first, ke.second});
+    // fillAndSortTmp / CMP_tmp: src/VariationRealigner.cpp:44-58, 1362-1386
+    std::sort(tmp.begin(), tmp.end(), [](const T &a, const T &b) {
+        if (a.cnt != b.cnt) return a.cnt > b.cnt;
+        if (a.pos != b.pos) return a.pos < b.pos;
+        return a.key.compare(b.key) > 0;
+    });
+    for (const T &t : tmp) {
+        int position = t.pos;
+        const string &vn = t.key;
+        auto pit = M.nonins.find(position);
+        if (pit == M.nonins.end()) continue;
+        std::set<string> local;  // keys of the by-value copy the reference iterates
+        for (auto &e : pit->second) local.insert(e.first);
+        if (!local.count(vn)) continue;
+        Stat &vref = pit->second.at(vn);
+        string mnt = vn;
+        size_t amp = mnt.find('&');
+        if (amp != string::npos) mnt.erase(amp, 1);
+        int ml = (int)mnt.size();
+        for (int i = 0; i < ml - 1; i++) {
+            string left = mnt.substr(0, i + 1);
+            if (left.size() > 1) left.insert(1, "&");
+            string right = mnt.substr(i + 1);
+            if (right.size() > 1) right.insert(1, "&");
+            if (local.count(left)) {
+                Stat &tref = pit->second.at(left);
+                if (tref.cnt <= 0) continue;
+                if (tref.cnt < vref.cnt && tref.pmean / tref.cnt <= i + 1) {
+                    adj_cnt(vref, tref);
+                    local.erase(left);
+                }
+            }
+            auto rit = M.nonins.find(position + i + 1);
+            if (rit != M.nonins.end()) {
+                auto kit = rit->second.find(right);
+                if (kit != rit->second.end()) {
+                    Stat &tref = kit->second;
+                    if (tref.cnt < 0) continue;
+                    if (tref.cnt < vref.cnt) {
+                        adj_cnt(vref, tref);
+                        M.cov[position] += tref.cnt;
+                        rit->second.erase(kit);
+                    }
+                }
+            }
+        }
+        auto s3 = M.sc3.find(position);
+        if (s3 != M.sc3.end() && !s3->second.used) {
+            string sq = consensus(s3->second);
+            if (sq.compare(0, ml, mnt) == 0 && (int)sq.size() >= ml) {
+                if ((int)sq.size() == ml || ismatchref(sq.substr(ml), R, position + ml, 1)) {
+                    adj_cnt(pit->second[vn], s3->second);
+                    M.cov[position] += s3->second.cnt;
+                    s3->second.used = true;
+                }
+            }
+        }
+        auto s5 = M.sc5.find(position + ml);
+        if (s5 != M.sc5.end() && !s5->second.used) {
+            string sq = consensus(s5->second);
+            if (sq != " " && (int)sq.size() >= ml) {
+                std::reverse(sq.begin(), sq.end());
+                if (sq.substr(sq.size() - ml, ml) == mnt) {
+                    if ((int)sq.size() == ml || ismatchref(sq.substr(0, sq.size() - ml), R, position - 1, -1)) {
+                        adj_cnt(pit->second[vn], s5->second);
+                        M.cov[position] += s5->second.cnt;
+                        s5->second.used = true;
+                    }
+                }
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// scoring: ToVarsBuilder (src/ToVarsBuilder.cpp) and Variant (include/Variant.h)
+// ---------------------------------------------------------------------------
+struct Var {
+    string desc;
+    int pc = 0, fwd = 0, rev = 0;
+    string sbf = "0";
+    double freq = 0, pmean = 0;
+    bool pstd = false;
+    double qual = 0;
+    bool qstd = false;
+    double mq = 0, qratio = 0, hifreq = 0, extrafreq = 0;
+    int shift3 = 0;
+    double msi = 0;
+    int msint = 0;
+    double nm = 0;
+    int hicnt = 0, hicov = 0;
+    string leftseq, rightseq;
+    int startp = 0, endp = 0, rfc = 0, rrc = 0, tpc = 0;
+    double duprate = 0;
+    string genotype, varallele, refallele, vartype;
+    bool filled = false;  // set when collectReferenceVariants completed for it
+};
+
+struct PosVars {
+    int ref_idx = -1;  // index into all
+    vector<int> vars;
+    vector<Var> all;
+};
+
+int strand_bias(int f, int r, const rvo_params &P) {  // include/VariationUtils.h:511-521
+    if (f + r <= 12) return f * r > 0 ? 2 : 0;
+    return (f / (double)(f + r) >= P.bias && r / (double)(f + r) >= P.bias && f >= P.min_bias_reads &&
+            r >= P.min_bias_reads) ? 2 : 1;
+}
+
+struct RefFail {};
+
+string join_ref(Ref &R, int from, int to) {  // joinRef: include/VariationUtils.h:356-362 (.at throws)
+    string s;
+    for (int i = from; i <= to; i++) {
+        if (!R.has(i)) throw RefFail();
+        s += R.at(i);
+    }
+    return s;
+}
+
+struct Msi { double msi; int shift3; string msint; };
+
+// findMSI with curmsi_from_end: src/ToVarsBuilder.cpp:614-678
+Msi find_msi(const string &t1, const string &t2, const string &left) {
+    int nmsi = 1, shift3 = 0;
+    string maxmsi;
+    double msicnt = 0;
+    while (nmsi <= (int)t1.size() && nmsi <= 6) {
+        string msint = t1.substr(t1.size() - nmsi, nmsi);
+        string mb = left + t1;
+        double cur = 1.0;
+        for (int i = (int)mb.size() - nmsi; i > 0; i -= nmsi) {
+            if (i > nmsi && mb.compare(i - nmsi, nmsi, msint) == 0) cur += 1;
+            else break;
+        }
+        for (int i = 0; i < (int)t2.size(); i += nmsi) {
+            if (i + nmsi < (int)t2.size() && t2.compare(i, nmsi, msint) == 0) cur += 1.0;
+            else break;
+        }
+        if (cur > msicnt) { maxmsi = msint; msicnt = cur; }
+        nmsi++;
+    }
+    string ts = t1 + t2;
+    while (shift3 < (int)t2.size() && ts[shift3] == t2[shift3]) shift3++;
+    return {msicnt, shift3, maxmsi};
+}
+
+void replace_first(string &s, const string &a, const string &b) {
+    size_t p = s.find(a);
+    if (p != string::npos) s.replace(p, a.size(), b);
+}
+
+bool starts_with(const string &s, const char *p) { return s.compare(0, strlen(p), p) == 0; }
+
+struct Scorer {
+    const rvo_params &P;
+    Maps &M;
+    Ref &R;
+    int chr_len;
+    int rs, re;
+    map<int, PosVars> aligned;
+
+    Scorer(const rvo_params &p, Maps &m, Ref &r, int cl, int s, int e) : P(p), M(m), R(r), chr_len(cl), rs(s), re(e) {}
+
+    Var make_var(const string &k, const Stat &c, int ttcov, int hicov) {
+        Var v;
+        v.desc = k;
+        v.pc = c.cnt;
+        v.fwd = c.fwd;
+        v.rev = c.rev;
+        v.sbf = std::to_string(strand_bias(c.fwd, c.rev, P));
+        v.freq = c.cnt / (double)ttcov;
+        v.pmean = c.pmean / (double)c.cnt;
+        v.pstd = c.pstd;
+        v.qual = c.qmean / c.cnt;
+        v.qstd = c.qstd;
+        v.mq = c.mq / (double)c.cnt;
+        v.qratio = c.hi / (c.lo != 0 ? (double)c.lo : 0.5);
+        v.hifreq = hicov > 0 ? c.hi / (double)hicov : 0;
+        v.extrafreq = c.extracnt != 0 ? c.extracnt / (double)ttcov : 0;
+        v.nm = c.nm / (double)c.cnt;
+        v.hicnt = c.hi;
+        v.hicov = hicov;
+        return v;
+    }
+
+    // ToVarsBuilder::process: src/ToVarsBuilder.cpp:97-205 (positions ascending)
+    void run() {
+        for (auto &pe : M.nonins) {
+            int position = pe.first;
+            KeyMap &vm = pe.second;
+            bool has_ins = M.ins.count(position) > 0;
+            if (vm.empty() && !has_ins) continue;
+            auto cit = M.cov.find(position);
+            if (cit == M.cov.end() || cit->second == 0) continue;
+            // isTheSameVariationOnRef: src/ToVarsBuilder.cpp:213-233
+            if (vm.size() == 1 && !has_ins && R.has(position) && vm.count(string(1, R.at(position))) && !P.do_pileup)
+                continue;
+            int tpc = cit->second;
+            int hicov = 0;  // calcHicov: src/ToVarsBuilder.cpp:570-587
+            for (auto &e : vm) hicov += e.second.hi;
+            if (has_ins)
+                for (auto &e : M.ins.at(position)) hicov += e.second.hi;
+            vector<Var> var;
+            // createVariant: src/ToVarsBuilder.cpp:466-536
+            for (auto &e : vm) {
+                const Stat &c = e.second;
+                if (c.cnt == 0) continue;
+                int ttcov = tpc;
+                if (c.cnt > tpc && c.extracnt > 0 && c.cnt - tpc < c.extracnt) ttcov = c.cnt;
+                var.push_back(make_var(e.first, c, ttcov, hicov));
+            }
+            // createInsertion: src/ToVarsBuilder.cpp:358-452
+            if (has_ins) {
+                int hic = hicov;
+                for (auto &e : M.ins.at(position)) {
+                    const Stat &c = e.second;
+                    int ttcov = tpc;
+                    if (c.cnt > tpc && c.extracnt != 0 && c.cnt - tpc < c.extracnt) ttcov = c.cnt;
+                    if (ttcov < c.cnt) {
+                        ttcov = c.cnt;
+                        auto nc = M.cov.find(position + 1);
+                        if (nc != M.cov.end() && R.has(position + 1) && ttcov < nc->second - c.cnt) {
+                            ttcov = nc->second;
+                            auto np = M.nonins.find(position + 1);
+                            if (np != M.nonins.end()) {
+                                auto nk = np->second.find(string(1, R.at(position + 1)));
+                                if (nk != np->second.end()) {
+                                    nk->second.fwd -= c.fwd;
+                                    nk->second.rev -= c.rev;
+                                }
+                            }
+                        }
+                        tpc = ttcov;
+                    }
+                    if (hic < c.hi) hic = c.hi;
+                    var.push_back(make_var(e.first, c, ttcov, hic));
+                }
+            }
+            // CMP_VARI: src/ToVarsBuilder.cpp:20-26
+            std::sort(var.begin(), var.end(), [](const Var &a, const Var &b) {
+                double r = a.qual * a.pc - b.qual * b.pc;
+                if (r < 0.00001 && r > -0.00001) return a.desc.compare(b.desc) < 0;
+                return r > 0;
+            });
+            // collectVarsAtPosition: src/ToVarsBuilder.cpp:327-346
+            PosVars pv;
+            double maxfreq = 0;
+            for (Var &v : var) {
+                pv.all.push_back(v);
+                int idx = (int)pv.all.size() - 1;
+                if (R.has(position) && v.desc == string(1, R.at(position))) pv.ref_idx = idx;
+                else {
+                    pv.vars.push_back(idx);
+                    if (v.freq > maxfreq) maxfreq = v.freq;
+                }
+            }
+            if (!P.do_pileup && maxfreq <= P.freq) continue;
+            try {
+                collect_reference(position, tpc, pv);
+            } catch (const RefFail &) {
+            }
+            aligned[position] = pv;
+        }
+    }
+
+    // proceedVrefIsDeletion / proceedVrefIsInsertion: src/ToVarsBuilder.cpp:242-317
+    Msi msi_deletion(int position, int dellen) {
+        string leftseq = join_ref(R, position - 70 > 1 ? position - 70 : 1, position - 1);
+        string tseq = join_ref(R, position, position + dellen + 70 > chr_len ? chr_len : position + dellen + 70);
+        string a = tseq.substr(0, std::min<size_t>(dellen, tseq.size()));
+        string b = (size_t)dellen <= tseq.size() ? tseq.substr(dellen) : string();
+        Msi m = find_msi(a, b, leftseq);
+        Msi t = find_msi(leftseq, b, "");
+        if (m.msi < t.msi) { m.msi = t.msi; m.msint = t.msint; }
+        if (m.msi <= m.shift3 / (double)dellen) m.msi = m.shift3 / (double)dellen;
+        return m;
+    }
+    Msi msi_insertion(int position, const string &vn) {
+        string t1 = vn.substr(1);
+        string leftseq = join_ref(R, position - 50 > 1 ? position - 50 : 1, position);
+        string t2 = join_ref(R, position + 1, position + 70 > chr_len ? chr_len : position + 70);
+        Msi m = find_msi(t1, t2, leftseq);
+        Msi t = find_msi(leftseq, t2, "");
+        if (m.msi < t.msi) { m.msi = t.msi; m.msint = t.msint; }
+        if (m.msi <= m.shift3 / (double)t1.size()) m.msi = m.shift3 / (double)t1.size();
+        return m;
+    }
+
+    // collectReferenceVariants: src/ToVarsBuilder.cpp:730-1098 (CRISPR mode not restated)
+    void collect_reference(int position, int tpc, PosVars &pv) {
+        int rfc = 0, rrc = 0;
+        string g1;
+        Var *refv = pv.ref_idx >= 0 ? &pv.all[pv.ref_idx] : nullptr;
+        if (refv && refv->freq >= P.freq) g1 = refv->desc;
+        else if (!pv.vars.empty()) g1 = pv.all[pv.vars[0]].desc;
+        else if (refv) g1 = refv->desc;
+        if (refv) { rfc = refv->fwd; rrc = refv->rev; }
+        if (starts_with(g1, "+")) g1 = "+" + std::to_string(g1.size() - 1);
+        if (tpc > M.cov[position] && M.nonins.count(position + 1) && R.has(position + 1)) {
+            KeyMap &n1 = M.nonins.at(position + 1);
+            auto it = n1.find(string(1, R.at(position + 1)));
+            if (it != n1.end()) { rfc = it->second.fwd; rrc = it->second.rev; }
+        }
+        if (!pv.vars.empty()) {
+            for (int vi : pv.vars) {
+                Var &v = pv.all[vi];
+                string g2 = v.desc;
+                if (starts_with(g2, "+")) g2 = "+" + std::to_string(g2.size() - 1);
+                const string &vn = v.desc;
+                int dellen = 0;
+                if (vn.size() > 1 && vn[0] == '-' && isdigit((unsigned char)vn[1])) dellen = atoi(vn.c_str() + 1);
+                int endp = position;
+                if (starts_with(vn, "-")) endp = position + dellen - 1;
+                string refa, vara, msint;
+                int shift3 = 0;
+                double msi = 0;
+                int startp = position;
+                if (starts_with(vn, "+")) {
+                    if (vn.find('&') == string::npos && vn.find('#') == string::npos && vn.find("<dup") == string::npos) {
+                        Msi m = msi_insertion(position, vn);
+                        msi = m.msi; shift3 = m.shift3; msint = m.msint;
+                    }
+                    if (P.move_indels_3) { startp += shift3; endp += shift3; }
+                    refa = R.has(position) ? string(1, R.at(position)) : "";
+                    vara = refa + vn.substr(1);
+                } else if (starts_with(vn, "-")) {
+                    if (dellen < P.svminlen) {
+                        vara = vn;
+                        size_t k = 1;
+                        while (k < vara.size() && isdigit((unsigned char)vara[k])) k++;
+                        if (k > 1) vara.erase(0, k);
+                        Msi m = msi_deletion(position, dellen);
+                        msi = m.msi; shift3 = m.shift3; msint = m.msint;
+                    }
+                    if (vn.find('&') == string::npos && vn.find('#') == string::npos && vn.find('^') == string::npos) {
+                        if (P.move_indels_3) startp += shift3;
+                        if (vara != "<DEL>") vara = R.has(position - 1) ? string(1, R.at(position - 1)) : "";
+                        refa = R.has(position - 1) ? string(1, R.at(position - 1)) : "";
+                        startp--;
+                    }
+                    if (dellen < P.svminlen) refa += join_ref(R, position, position + dellen - 1);
+                } else {
+                    string t1 = join_ref(R, position - 30 > 1 ? position - 30 : 1, position + 1);
+                    string t2 = join_ref(R, position + 2, position + 70 > chr_len ? chr_len : position + 70);
+                    Msi m = find_msi(t1, t2, "");
+                    msi = m.msi; shift3 = m.shift3; msint = m.msint;
+                    refa = R.has(position) ? string(1, R.at(position)) : "";
+                    vara = vn;
+                }
+                // AMP_ATGC ".*&([ATGC]+).*": the last '&' followed by a base run
+                auto amp_run = [](const string &s, string &run) {
+                    for (size_t k = s.size(); k-- > 0;) {
+                        if (s[k] == '&' && k + 1 < s.size() && strchr("ATGC", s[k + 1]) && s[k + 1]) {
+                            size_t e = k + 1;
+                            while (e < s.size() && s[e] && strchr("ATGC", s[e])) e++;
+                            run = s.substr(k + 1, e - k - 1);
+                            return true;
+                        }
+                    }
+                    return false;
+                };
+                string extra;
+                if (amp_run(vn, extra)) {
+                    replace_first(vara, "&", "");
+                    string tch = join_ref(R, endp + 1, endp + (int)extra.size());
+                    refa += tch;
+                    g1 += tch;
+                    endp += (int)extra.size();
+                    string vextra;
+                    if (amp_run(vara, vextra)) {
+                        replace_first(vara, "&", "");
+                        tch = join_ref(R, endp + 1, endp + (int)vextra.size());
+                        refa += tch;
+                        g1 += tch;
+                        endp += (int)vextra.size();
+                    }
+                    if (starts_with(vn, "+")) {
+                        refa = refa.substr(1);
+                        vara = vara.substr(1);
+                        startp++;
+                    }
+                }
+                // HASH_GROUP_CARET_GROUP "#(.+)\^(.+)"
+                size_t hp = vn.find('#');
+                size_t cp = vn.rfind('^');
+                if (hp != string::npos && cp != string::npos && cp > hp + 1 && cp + 1 < vn.size()) {
+                    string mseq = vn.substr(hp + 1, cp - hp - 1);
+                    string tail = vn.substr(cp + 1);
+                    endp += (int)mseq.size();
+                    refa += join_ref(R, endp - (int)mseq.size() + 1, endp);
+                    if (!tail.empty() && isdigit((unsigned char)tail[0])) {
+                        int d = atoi(tail.c_str());
+                        refa += join_ref(R, endp + 1, endp + d);
+                        endp += d;
+                    }
+                    replace_first(vara, "#", "");
+                    size_t c2 = vara.find('^');
+                    if (c2 != string::npos) {
+                        size_t e = c2 + 1;
+                        while (e < vara.size() && isdigit((unsigned char)vara[e])) e++;
+                        vara.erase(c2, e - c2);
+                    }
+                    replace_first(g1, "#", "m");
+                    replace_first(g1, "^", "i");
+                    replace_first(g2, "#", "m");
+                    replace_first(g2, "^", "i");
+                }
+                // CARET_ATGNC "\^([ATGNC]+)"
+                bool caret = false;
+                for (size_t k = 0; k + 1 < vn.size(); k++)
+                    if (vn[k] == '^' && strchr("ATGNC", vn[k + 1]) && vn[k + 1]) { caret = true; break; }
+                if (caret) {
+                    replace_first(vara, "^", "");
+                    replace_first(g1, "^", "i");
+                    replace_first(g2, "^", "i");
+                }
+                v.leftseq = join_ref(R, startp - 20 < 1 ? 1 : startp - 20, startp - 1);
+                v.rightseq = join_ref(R, endp + 1, endp + 20 > chr_len ? chr_len : endp + 20);
+                string gt = g1 + "/" + g2;
+                string gt2;
+                for (char c : gt) {
+                    if (c == '&' || c == '#') continue;
+                    gt2 += (c == '^') ? 'i' : c;
+                }
+                v.msi = msi;
+                v.msint = (int)msint.size();
+                v.shift3 = shift3;
+                v.startp = startp;
+                v.endp = endp;
+                v.refallele = refa;  // validateRefallele is the identity on A/C/G/T/N references
+                v.varallele = vara;
+                v.genotype = gt2;
+                v.tpc = tpc;
+                v.rfc = rfc;
+                v.rrc = rrc;
+                v.sbf = (refv ? refv->sbf : string("0")) + ";" + v.sbf;
+                if (v.rfc < 0) v.rfc = 0;
+                if (v.rrc < 0) v.rrc = 0;
+                if (v.fwd < 0) v.fwd = 0;
+                if (v.rev < 0) v.rev = 0;
+                v.filled = true;
+            }
+        } else if (refv) {
+            Var &v = *refv;
+            v.tpc = tpc;
+            v.pc = 0;
+            v.freq = 0;
+            v.rfc = rfc;
+            v.rrc = rrc;
+            v.fwd = v.rev = 0;
+            v.msi = 0;
+            v.msint = 0;
+            v.sbf += ";0";
+            v.shift3 = 0;
+            v.startp = v.endp = position;
+            string rb = R.has(position) ? string(1, R.at(position)) : "";
+            v.refallele = rb;
+            v.varallele = rb;
+            v.genotype = rb + "/" + rb;
+            v.leftseq = v.rightseq = "";
+            v.filled = true;
+        }
+    }
+};
+
+// Variant::varType / isGoodVar / adjComplex: include/Variant.h:99-248
+string var_type(const Var &v) {
+    const string &r = v.refallele, &a = v.varallele;
+    if (r.size() == 1 && a.size() == 1) return "SNV";
+    if (a.size() == 5 && a[0] == '<' && a[4] == '>') return a.substr(1, 3);
+    if (r.empty() || a.empty()) return "Complex";
+    if (r[0] != a[0]) return "Complex";
+    if (r.size() == 1 && a.size() > 1 && a.compare(0, 1, r) == 0) return "Insertion";
+    if (r.size() > 1 && a.size() == 1 && r.compare(0, 1, a) == 0) return "Deletion";
+    return "Complex";
+}
+
+bool good_var(const Var &v, const Var *refv, const string &type, const rvo_params &P) {
+    if (v.refallele.empty()) return false;
+    if (v.freq < P.freq || v.hicnt < P.minr || v.pmean < P.read_pos_filter || v.qual < P.goodq) return false;
+    if (refv && refv->hicnt > P.minr && v.freq < 0.25) {
+        double d = v.mq + v.refallele.size() + v.varallele.size();
+        double f = (1 + d) / (refv->mq + 1);
+        if ((d - 2 < 5 && refv->mq > 20) || f < 0.25) return false;
+    }
+    if (v.qratio < P.qratio) return false;
+    if (v.freq > 0.30) return true;
+    if (v.mq < P.mapq_filter) return false;
+    if (v.sbf == "2;1" && v.freq < 0.20) {
+        if (type.empty() || type == "SNV" || (v.refallele.size() < 3 && v.varallele.size() < 3)) return false;
+    }
+    return true;
+}
+
+void adj_complex(Var &v) {
+    string r = v.refallele, a = v.varallele;
+    if (!a.empty() && a[0] == '<') return;
+    size_t n = 0;
+    while (r.size() - n > 1 && a.size() - n > 1 && r[n] == a[n]) n++;
+    if (n > 0) {
+        v.startp += (int)n;
+        v.refallele = r.substr(n);
+        v.varallele = a.substr(n);
+        v.leftseq += r.substr(0, n);
+        v.leftseq = v.leftseq.substr(n);
+    }
+    r = v.refallele;
+    a = v.varallele;
+    size_t m = 1;
+    while (r.size() > m && a.size() > m && r[r.size() - m] == a[a.size() - m]) m++;
+    if (m > 1) {
+        v.endp -= (int)(m - 1);
+        v.refallele = r.substr(0, r.size() - (m - 1));
+        v.varallele = a.substr(0, a.size() - (m - 1));
+        long keep = (long)v.rightseq.size() - (long)(m - 1);
+        v.rightseq = r.substr(r.size() - (m - 1)) + (keep > 0 ? v.rightseq.substr(0, keep) : string());
+    }
+}
+
+string fstr(double d) { return std::to_string(d); }
+
+// print_output_variant_simple: src/modes/simpleMode.cpp:66-142
+void print_simple(string &out, const Var &v, const char *sample, const char *gene, const char *chr, int rs, int re,
+                  bool fisher) {
+    vector<string> c;
+    c.push_back(sample);
+    c.push_back(gene);
+    c.push_back(chr);
+    c.push_back(std::to_string(v.startp));
+    c.push_back(std::to_string(v.endp));
+    c.push_back(v.refallele);
+    c.push_back(v.varallele);
+    c.push_back(std::to_string(v.tpc));
+    c.push_back(std::to_string(v.pc));
+    c.push_back(std::to_string(v.rfc));
+    c.push_back(std::to_string(v.rrc));
+    c.push_back(std::to_string(v.fwd));
+    c.push_back(std::to_string(v.rev));
+    c.push_back(v.genotype.empty() ? "0" : v.genotype);
+    c.push_back(fstr(v.freq));
+    c.push_back(v.sbf);
+    c.push_back(fstr(v.pmean));
+    c.push_back(v.pstd ? "1" : "0");
+    c.push_back(fstr(v.qual));
+    c.push_back(v.qstd ? "1" : "0");
+    if (fisher) {
+        double l, r, t;
+        rv_oracle_fisher(v.rfc, v.rrc, v.fwd, v.rev, &l, &r, &t);
+        c.push_back(fstr(t));
+        double ad = (double)(v.rfc * v.rev), bc = (double)(v.rrc * v.fwd);
+        double ratio = 0.0;
+        if (bc != 0 && ad != 0) ratio = ad > bc ? ad / bc : bc / ad;
+        c.push_back(fstr(ratio));
+    }
+    c.push_back(fstr(v.mq));
+    c.push_back(fstr(v.qratio));
+    c.push_back(fstr(v.hifreq));
+    c.push_back(fstr(v.extrafreq));
+    c.push_back(std::to_string(v.shift3));
+    c.push_back(fstr(v.msi));
+    c.push_back(std::to_string(v.msint));
+    c.push_back(v.nm > 0 ? fstr(v.nm) : "0");
+    c.push_back(std::to_string(v.hicnt));
+    c.push_back(std::to_string(v.hicov));
+    c.push_back(v.leftseq.empty() ? "0" : v.leftseq);
+    c.push_back(v.rightseq.empty() ? "0" : v.rightseq);
+    c.push_back(string(chr) + ":" + std::to_string(rs) + "-" + std::to_string(re));
+    c.push_back(v.vartype);
+    c.push_back(fstr(v.duprate));
+    c.push_back("0");
+    for (size_t i = 0; i < c.size(); i++) {
+        out += c[i];
+        out += (i + 1 < c.size()) ? '\t' : '\n';
+    }
+}
+
+// SimpleMode::output: src/modes/simpleMode.cpp:144-208
+long emit_simple(string &out, Scorer &sc, const char *sample, const char *gene, const char *chr, const rvo_params &P) {
+    long n = 0;
+    for (auto &pe : sc.aligned) {
+        int position = pe.first;
+        if (position < sc.rs || position > sc.re) continue;
+        PosVars &pv = pe.second;
+        vector<Var *> vrefs;
+        Var *refv = pv.ref_idx >= 0 ? &pv.all[pv.ref_idx] : nullptr;
+        if (pv.vars.empty()) {
+            if (!P.do_pileup) continue;
+            if (!refv) continue;
+            refv->vartype = "";
+            vrefs.push_back(refv);
+        } else {
+            for (int vi : pv.vars) {
+                Var &v = pv.all[vi];
+                if (v.refallele.find('N') != string::npos) continue;
+                v.vartype = var_type(v);
+                if (!good_var(v, refv, v.vartype, P) && !P.do_pileup) continue;
+                vrefs.push_back(&v);
+            }
+        }
+        for (Var *v : vrefs) {
+            if (v->vartype == "Complex") adj_complex(*v);
+            print_simple(out, *v, sample, gene, chr, sc.rs, sc.re, P.fisher != 0);
+            n++;
+        }
+    }
+    return n;
+}
+
+// ---------------------------------------------------------------------------
+// record iteration: sam_itr_querys + RecordPreprocessor::next_record
+// (src/recordPreprocessor.cpp:101-180)
+// ---------------------------------------------------------------------------
+void load_read(const rvo_reads *rd, int64_t i, ReadView &r) {
+    r.pos = rd->pos[i];
+    r.mpos = rd->mpos[i];
+    r.nm = rd->nm[i];
+    r.flag = rd->flag[i];
+    r.mapq = rd->mapq[i];
+    r.lseq = rd->l_qseq[i];
+    r.n_cigar = rd->n_cigar[i];
+    const uint8_t *s4 = rd->seq4 + rd->base_off[i];
+    const uint8_t *q = rd->qual + rd->base_off[i];
+    r.seq.assign(r.lseq + 8, 0);
+    for (int k = 0; k < r.lseq; k++) r.seq[k] = kNt16[s4[k] & 15];
+    // the bytes that follow the CIGAR in a BAM record: packed bases, then quals
+    vector<uint8_t> tail;
+    for (int k = 0; k < r.lseq; k += 2)
+        tail.push_back((uint8_t)(((s4[k] & 15) << 4) | (k + 1 < r.lseq ? (s4[k + 1] & 15) : 0)));
+    uint8_t before_qual = tail.empty() ? 0 : tail.back();
+    for (int k = 0; k < r.lseq; k++) tail.push_back(q[k]);
+    while (tail.size() < 32) tail.push_back(0);
+    r.cig.assign(rd->cigar + rd->cig_off[i], rd->cigar + rd->cig_off[i] + r.n_cigar);
+    for (int w = 0; w < 4; w++) {
+        uint32_t v = 0;
+        memcpy(&v, &tail[4 * w], 4);
+        r.cig.push_back(v);
+    }
+    r.qual_buf.assign(r.lseq + 9, 0);
+    r.qual_buf[0] = before_qual;
+    memcpy(r.qual_buf.data() + 1, q, r.lseq);
+}
+
+int ref_span(const rvo_reads *rd, int64_t i) {
+    int len = 0;
+    const uint32_t *c = rd->cigar + rd->cig_off[i];
+    for (int k = 0; k < rd->n_cigar[i]; k++) {
+        int o = c[k] & 15;
+        if (o == 0 || o == 2 || o == 3 || o == 7 || o == 8) len += c[k] >> 4;
+    }
+    return len;
+}
+
+void run_pileup(const rvo_reads *rd, const rvo_params &P, int rs, int re, int chr_len, Maps &M, Ref &R) {
+    // reads overlapping [rs-1, re) in 0-based half-open coordinates, file order
+    int64_t lo = 0, hi = rd->n;
+    while (lo < hi) {  // first read with pos >= rs - 1 - max_span
+        int64_t mid = (lo + hi) / 2;
+        if (rd->pos[mid] < rs - 1 - 4096) lo = mid + 1; else hi = mid;
+    }
+    Walker W(P, M, R, rs, re, chr_len);
+    std::set<string> dups;
+    int first_match = 0;
+    ReadView r;
+    for (int64_t i = lo; i < rd->n && rd->pos[i] < re; i++) {
+        int span = ref_span(rd, i);
+        int endpos = ((rd->flag[i] & 4) || span == 0) ? rd->pos[i] + 1 : rd->pos[i] + span;
+        if (endpos <= rs - 1) continue;
+        uint16_t fl = rd->flag[i];
+        if (fl & P.samfilter) continue;
+        if (rd->mapq[i] < P.min_mapq) continue;
+        if (rd->l_qseq[i] == 1) continue;
+        if (P.dedup) {
+            int a = rd->pos[i] + 1, m = rd->mpos[i] + 1;
+            if (a != first_match) dups.clear();
+            string mref = (fl & 1) ? "=" : "*";
+            if (m < 10) {
+                string k = std::to_string(a) + "-" + mref + "-" + std::to_string(m);
+                if (dups.count(k)) continue;
+                dups.insert(k);
+                first_match = a;
+            } else if ((fl & 1) && (fl & 4)) {
+                string k = std::to_string(a) + "-";
+                const uint32_t *c = rd->cigar + rd->cig_off[i];
+                for (int q = 0; q < rd->n_cigar[i]; q++) k += std::to_string(c[q] >> 4) + "MIDNSHP=XB"[c[q] & 15];
+                if (dups.count(k)) continue;
+                dups.insert(k);
+                first_match = a;
+            }
+        }
+        load_read(rd, i, r);
+        W.parse(r);
+    }
+}
+
+void fmt_stat(string &o, const char *tag, int pos, const string &key, const Stat &v) {
+    char buf[512];
+    snprintf(buf, sizeof buf, "%s\t%d\t%s\t%d\t%d\t%d\t%.17g\t%.17g\t%.17g\t%.17g\t%d\t%d\t%d\t%d\t%d\t%.17g\t%d\n", tag,
+             pos, key.c_str(), v.cnt, v.fwd, v.rev, v.pmean, v.qmean, v.mq, v.nm, v.lo, v.hi, (int)v.pstd, (int)v.qstd,
+             v.pp, v.pq, v.extracnt);
+    o += buf;
+}
+
+void dump_maps(string &o, const char *pfx, Maps &M, bool full) {
+    string t;
+    char buf[64];
+    if (full) {
+        snprintf(buf, sizeof buf, "%s_ML\t%d\n", pfx, M.max_read_len);
+        o += buf;
+    }
+    for (auto &pe : M.nonins)
+        for (auto &ke : pe.second) fmt_stat(o, (string(pfx) + "N").c_str(), pe.first, ke.first, ke.second);
+    for (auto &pe : M.ins)
+        for (auto &ke : pe.second) fmt_stat(o, (string(pfx) + "I").c_str(), pe.first, ke.first, ke.second);
+    for (auto &ce : M.cov) {
+        snprintf(buf, sizeof buf, "%sC\t%d\t%d\n", pfx, ce.first, ce.second);
+        o += buf;
+    }
+    if (!full) return;
+    for (int side = 0; side < 2; side++) {
+        auto &mm = side == 0 ? M.sc5 : M.sc3;
+        string tag = string(pfx) + (side == 0 ? "S5" : "S3");
+        for (auto &se : mm) {
+            fmt_stat(o, tag.c_str(), se.first, "*", se.second);
+            for (auto &ne : se.second.nt) {
+                vector<char> cs;
+                for (auto &c : ne.second) cs.push_back(c.first);
+                std::sort(cs.begin(), cs.end());
+                for (char c : cs) {
+                    char key[64];
+                    snprintf(key, sizeof key, "%d:%c:%d", ne.first, c, ne.second.at(c));
+                    fmt_stat(o, tag.c_str(), se.first, key, se.second.seq.at(ne.first).at(c));
+                }
+            }
+        }
+    }
+    auto cnts = [&](const char *tg, map<int, map<string, int>> &mm) {
+        for (auto &pe : mm)
+            for (auto &ke : pe.second) {
+                o += string(pfx) + tg + "\t" + std::to_string(pe.first) + "\t" + ke.first + "\t" +
+                     std::to_string(ke.second) + "\n";
+            }
+    };
+    cnts("CI", M.inscnt);
+    cnts("CD", M.delcnt);
+    cnts("MN", M.mnp);
+}
+
+void dump_variants(string &o, Scorer &sc) {
+    char buf[2048];
+    for (auto &pe : sc.aligned) {
+        PosVars &pv = pe.second;
+        auto one = [&](const char *kind, const Var &v) {
+            snprintf(buf, sizeof buf,
+                     "V\t%d\t%s\t%s\t%d\t%d\t%d\t%s\t%.17g\t%.17g\t%d\t%.17g\t%d\t%.17g\t%.17g\t%.17g\t%.17g\t%d\t%.17g"
+                     "\t%d\t%.17g\t%d\t%d\t%s\t%s\t%d\t%d\t%d\t%d\t%d\t%s\t%s\t%s\n",
+                     pe.first, kind, v.desc.c_str(), v.pc, v.fwd, v.rev, v.sbf.c_str(), v.freq, v.pmean, (int)v.pstd,
+                     v.qual, (int)v.qstd, v.mq, v.qratio, v.hifreq, v.extrafreq, v.shift3, v.msi, v.msint, v.nm,
+                     v.hicnt, v.hicov, v.leftseq.c_str(), v.rightseq.c_str(), v.startp, v.endp, v.rfc, v.rrc, v.tpc,
+                     v.genotype.c_str(), v.refallele.c_str(), v.varallele.c_str());
+            o += buf;
+        };
+        if (pv.ref_idx >= 0) one("ref", pv.all[pv.ref_idx]);
+        for (int vi : pv.vars) one("var", pv.all[vi]);
+    }
+}
+
+void setup_ref(Ref &R, const char *ref, int clen, int rs, int re, const rvo_params &P) {
+    R.contig = ref;
+    R.clen = clen;
+    int ext = P.ref_extension, x = P.extend_nt;
+    R.lo = rs - x - ext < 1 ? 1 : rs - x - ext;
+    int seq_end = re + x + ext > clen ? clen : re + x + ext;
+    R.hi = seq_end - 17;
+}
+
+}  // namespace
+
+extern "C" {
+
+void rvo_default_params(rvo_params *p) {
+    memset(p, 0, sizeof *p);
+    p->goodq = 22.5;
+    p->vext = 2;
+    p->mismatch = 8;
+    p->local_realign = 1;
+    p->freq = 0.01;
+    p->minr = 2;
+    p->read_pos_filter = 5;
+    p->qratio = 1.5;
+    p->mapq_filter = 0;
+    p->min_mapq = 0;
+    p->lofreq = 0.05;
+    p->bias = 0.05;
+    p->min_bias_reads = 2;
+    p->samfilter = 0x504;
+    p->ref_extension = 1200;
+    p->svminlen = 1000;
+}
+
+int rvo_run_region(const rvo_reads *reads, const char *ref, int contig_len, const char *chr, int start, int end,
+                   const char *sample, const rvo_params *p, const char *stages, char **out, size_t *out_len) {
+    Maps M;
+    Ref R;
+    setup_ref(R, ref, contig_len, start, end, *p);
+    run_pileup(reads, *p, start, end, contig_len, M, R);
+    string o;
+    if (strchr(stages, 'P')) dump_maps(o, "P", M, true);
+    adjust_mnp(M, R);
+    if (strchr(stages, 'R')) dump_maps(o, "R", M, false);
+    Scorer sc(*p, M, R, contig_len, start, end);
+    sc.run();
+    if (strchr(stages, 'V')) dump_variants(o, sc);
+    if (strchr(stages, 'O')) emit_simple(o, sc, sample, chr, chr, *p);
+    *out = (char *)malloc(o.size() + 1);
+    memcpy(*out, o.data(), o.size());
+    (*out)[o.size()] = 0;
+    *out_len = o.size();
+    return 0;
+}
+
+long rvo_run_regions(const rvo_reads *reads, const char *ref, int contig_len, const char *chr, const int32_t *starts,
+                     const int32_t *ends, int n_regions, const char *sample, const rvo_params *p, int threads,
+                     char **out, size_t *out_len) {
+    vector<string> per(n_regions);
+    vector<long> cnt(n_regions, 0);
+#pragma omp parallel for schedule(dynamic) num_threads(threads > 0 ? threads : 1)
+    for (int i = 0; i < n_regions; i++) {
+        Maps M;
+        Ref R;
+        setup_ref(R, ref, contig_len, starts[i], ends[i], *p);
+        run_pileup(reads, *p, starts[i], ends[i], contig_len, M, R);
+        adjust_mnp(M, R);
+        Scorer sc(*p, M, R, contig_len, starts[i], ends[i]);
+        sc.run();
+        cnt[i] = emit_simple(per[i], sc, sample, chr, chr, *p);
+    }
+    string o;
+    long n = 0;
+    for (int i = 0; i < n_regions; i++) { o += per[i]; n += cnt[i]; }
+    *out = (char *)malloc(o.size() + 1);
+    memcpy(*out, o.data(), o.size());
+    (*out)[o.size()] = 0;
+    *out_len = o.size();
+    return n;
+}
+
+void rvo_free(char *p) { free(p); }
+
+double rvo_fisher(int n11, int n12, int n21, int n22, double *left, double *right, double *two) {
+    return rv_oracle_fisher(n11, n12, n21, n22, left, right, two);
+}
+}

@@ -1,0 +1,497 @@
+"""Seeded synthetic genomes and read sets with planted variants.
+
+The reference's own accuracy data (SEQC-II HCC1395 BAMs) is not available, so
+every workload here is generated from a seed: a random contig (uniform ACGT
+at a chosen GC fraction with homopolymer runs), planted SNVs / MNVs / indels
+with per-variant allele fractions, and 2x150 bp read pairs with Phred
+qualities, sequencing errors, N bases, soft clips, MAPQ and NM tags.
+
+A read set is held as a structure of arrays (`ReadSet`) in exactly the layout
+the GPU library consumes (BAM-native 4-bit bases, Phred quals, BAM CIGAR
+words).  `write_bam` serialises the same reads to a BGZF-compressed,
+coordinate-sorted BAM plus FASTA/.fai so the reference binary can read them.
+"""
+from __future__ import annotations
+
+import dataclasses
+import os
+import struct
+import zlib
+
+import numpy as np
+
+NT16 = "=ACMGRSVTWYHKDBN"
+# 2-bit genome alphabet A,C,G,T -> BAM 4-bit codes 1,2,4,8; N -> 15
+CODE_OF = np.array([1, 2, 4, 8], dtype=np.uint8)
+CODE_N = 15
+ASCII_OF_CODE = np.frombuffer(NT16.encode(), dtype=np.uint8)
+OP_M, OP_I, OP_D, OP_S = 0, 1, 2, 4
+
+
+@dataclasses.dataclass
+class Variant:
+    pos: int          # 0-based reference position of the first changed base
+    kind: str         # "snv", "mnv", "ins", "del"
+    ref: str
+    alt: str
+    vaf: float
+    strand_bias: float = 0.0   # fraction of carrying reads forced onto one strand (artifacts)
+    strand: int = 0            # strand the artifact prefers (0 fwd, 1 rev)
+
+
+@dataclasses.dataclass
+class ReadSet:
+    """Reads of one contig, coordinate-sorted, in the GPU batch layout.
+
+    pos:   int32  0-based leftmost aligned position (BAM POS)
+    flag:  uint16 SAM flag
+    mapq:  uint8
+    mpos:  int32  0-based mate position
+    isize: int32
+    nm:    int32  NM tag value
+    n_cigar, cig_off: uint16 / uint32 -> cigar (uint32 BAM words)
+    l_qseq, base_off: int32 / uint64 -> seq4 (one 4-bit code per base, unpacked)
+                       and qual (uint8 Phred); base_off is a multiple of 32
+    """
+    contig: str
+    contig_len: int
+    pos: np.ndarray
+    flag: np.ndarray
+    mapq: np.ndarray
+    mpos: np.ndarray
+    isize: np.ndarray
+    nm: np.ndarray
+    n_cigar: np.ndarray
+    cig_off: np.ndarray
+    cigar: np.ndarray
+    l_qseq: np.ndarray
+    base_off: np.ndarray
+    seq4: np.ndarray
+    qual: np.ndarray
+    name_id: np.ndarray
+
+    @property
+    def n(self) -> int:
+        return int(self.pos.shape[0])
+
+    def packed_seq(self) -> np.ndarray:
+        """BAM-packed 4-bit sequence (two bases per byte, high nibble first),
+        indexed by base_off // 2 for every read."""
+        s = self.seq4
+        if s.shape[0] % 2:
+            s = np.concatenate([s, np.zeros(1, np.uint8)])
+        return ((s[0::2] << 4) | s[1::2]).astype(np.uint8)
+
+
+def make_genome(length: int, rng: np.random.Generator, gc: float = 0.41,
+                homopolymer_rate: float = 0.01) -> np.ndarray:
+    """Uniform random contig (0..3 = A,C,G,T) with GC fraction `gc`; a
+    fraction `homopolymer_rate` of positions start a 5-20 bp homopolymer."""
+    p_at = (1.0 - gc) / 2
+    p_gc = gc / 2
+    g = rng.choice(4, size=length, p=[p_at, p_gc, p_gc, p_at]).astype(np.uint8)
+    starts = np.nonzero(rng.random(length) < homopolymer_rate)[0]
+    lens = rng.integers(5, 21, size=starts.shape[0])
+    for s, ln in zip(starts.tolist(), lens.tolist()):
+        g[s:s + ln] = g[s]
+    return g
+
+
+def genome_str(g: np.ndarray) -> str:
+    return np.frombuffer(b"ACGT", dtype=np.uint8)[g].tobytes().decode()
+
+
+def _rand_other(base: int, rng) -> int:
+    return int((base + rng.integers(1, 4)) % 4)
+
+
+def plant_variants(g: np.ndarray, rng: np.random.Generator, snv_rate: float,
+                   indel_rate: float, vaf_fn, mnv_frac: float = 0.0,
+                   max_indel: int = 10, margin: int = 200,
+                   spacing: int = 15, avoid=None) -> list[Variant]:
+    """Plant SNVs (and MNVs, a fraction `mnv_frac` of SNV sites) and 1..max_indel
+    bp insertions/deletions at the given per-bp rates, at least `spacing` bp
+    apart.  `vaf_fn(rng)` draws the allele fraction of each variant."""
+    L = g.shape[0]
+    out: list[Variant] = []
+    taken = np.zeros(L, dtype=bool)
+    if avoid is not None:
+        for v in avoid:
+            taken[max(0, v.pos - spacing):v.pos + spacing + 12] = True
+    n_snv = rng.binomial(L - 2 * margin, snv_rate)
+    n_ind = rng.binomial(L - 2 * margin, indel_rate)
+    cand = rng.integers(margin, L - margin, size=n_snv + n_ind)
+    for i, p in enumerate(cand.tolist()):
+        lo, hi = max(0, p - spacing), min(L, p + spacing + 12)
+        if taken[lo:hi].any():
+            continue
+        taken[lo:hi] = True
+        vaf = float(vaf_fn(rng))
+        if i < n_snv:
+            if rng.random() < mnv_frac:
+                k = int(rng.integers(2, 4))
+                ref = "".join("ACGT"[x] for x in g[p:p + k].tolist())
+                alt = "".join("ACGT"[_rand_other(int(x), rng)] for x in g[p:p + k].tolist())
+                out.append(Variant(p, "mnv", ref, alt, vaf))
+            else:
+                out.append(Variant(p, "snv", "ACGT"[g[p]], "ACGT"[_rand_other(int(g[p]), rng)], vaf))
+        else:
+            k = int(rng.integers(1, max_indel + 1))
+            if rng.random() < 0.5:
+                ins = "".join("ACGT"[x] for x in rng.integers(0, 4, size=k).tolist())
+                out.append(Variant(p, "ins", "", ins, vaf))
+            else:
+                ref = "".join("ACGT"[x] for x in g[p:p + k].tolist())
+                out.append(Variant(p, "del", ref, "", vaf))
+    out.sort(key=lambda v: v.pos)
+    return out
+
+
+def _qualities(n_reads: int, L: int, rng) -> np.ndarray:
+    """Phred mixture centred at 37 (range 2..41): most bases near 37 with a
+    mild decline along the read, a minority drawn from a low-quality tail."""
+    base = rng.normal(37.0, 2.0, size=(n_reads, L))
+    decline = np.linspace(0.0, 3.0, L)[None, :]
+    q = base - decline
+    low = rng.random((n_reads, L)) < 0.08
+    q = np.where(low, rng.uniform(2, 30, size=(n_reads, L)), q)
+    return np.clip(np.rint(q), 2, 41).astype(np.uint8)
+
+
+def simulate(genome: np.ndarray, variants: list[Variant], depth: float,
+             rng: np.random.Generator, contig: str = "ctg", read_len: int = 150,
+             insert_mean: float = 350.0, insert_sd: float = 50.0,
+             softclip_frac: float = 0.02, mapq0_frac: float = 0.05,
+             n_rate: float = 2e-4, span: tuple[int, int] | None = None,
+             name_base: int = 0, artifact_rate: float = 0.0,
+             artifact_q: int | None = None) -> ReadSet:
+    """Simulate coordinate-sorted 2x`read_len` pairs at `depth`x over
+    `span` (default: the whole contig).  Each read independently carries
+    each overlapping variant with probability vaf (strand-biased variants put
+    a `strand_bias` fraction of carriers on their preferred strand)."""
+    G = genome.shape[0]
+    L = read_len
+    lo, hi = span if span is not None else (0, G)
+    n_frag = int(round(depth * (hi - lo) / (2 * L)))
+    ins = np.clip(np.rint(rng.normal(insert_mean, insert_sd, n_frag)), L + 20, 3 * L).astype(np.int64)
+    fstart = rng.integers(max(0, lo - L // 2), np.maximum(max(0, lo - L // 2) + 1, hi - ins + L // 2))
+    fstart = np.clip(fstart, 0, G - ins)
+    r1_fwd = rng.random(n_frag) < 0.5
+    # read A = leftmost (forward strand), read B = rightmost (reverse strand)
+    startA = fstart
+    startB = fstart + ins - L
+    n = 2 * n_frag
+    start = np.concatenate([startA, startB])
+    rev = np.concatenate([np.zeros(n_frag, bool), np.ones(n_frag, bool)])
+    frag = np.concatenate([np.arange(n_frag), np.arange(n_frag)])
+    is_r1 = np.concatenate([r1_fwd, ~r1_fwd])
+    mate_start = np.concatenate([startB, startA])
+    isize = np.concatenate([ins, -ins])
+
+    seq = genome[start[:, None] + np.arange(L)[None, :]].copy()  # 0..3
+    qual = _qualities(n, L, rng)
+    # quality profile runs in sequencing direction: reverse it for reverse reads
+    qual[rev] = qual[rev][:, ::-1]
+
+    order_by_start = np.argsort(start, kind="stable")
+    s_sorted = start[order_by_start]
+
+    # per-read list of (variant index) for indels that the read carries
+    carried_indels: dict[int, list[int]] = {}
+    for vi, v in enumerate(variants):
+        vlen = max(len(v.ref), 1)
+        a = np.searchsorted(s_sorted, v.pos - L + 1, side="left")
+        b = np.searchsorted(s_sorted, v.pos + vlen, side="left")
+        idx = order_by_start[a:b]
+        if idx.size == 0:
+            continue
+        p_carry = np.full(idx.size, v.vaf)
+        if v.strand_bias > 0:
+            on = rev[idx] == bool(v.strand)
+            # a fraction strand_bias of carriers sit on the preferred strand
+            w_on = v.strand_bias / max(on.mean(), 1e-9)
+            w_off = (1 - v.strand_bias) / max(1 - on.mean(), 1e-9)
+            p_carry = np.clip(v.vaf * np.where(on, w_on, w_off), 0, 1)
+        carry = idx[rng.random(idx.size) < p_carry]
+        if v.kind in ("snv", "mnv"):
+            for k, ch in enumerate(v.alt):
+                col = v.pos + k - start[carry]
+                ok = (col >= 0) & (col < L)
+                seq[carry[ok], col[ok]] = "ACGT".index(ch)
+        else:
+            # indel carriers need at least 3 aligned bases on each side
+            off = v.pos - start[carry]
+            ok = (off >= 3) & (off + len(v.ref) <= L - 3)
+            for r in carry[ok].tolist():
+                carried_indels.setdefault(r, []).append(vi)
+
+    # sequencing errors: substitution with probability 10^(-q/10)
+    err = rng.random((n, L)) < np.power(10.0, -qual.astype(np.float64) / 10.0)
+    if artifact_rate > 0:
+        # oxidation-like C>A artifacts on C bases, at a skewed low quality
+        art = (seq == 1) & (rng.random((n, L)) < artifact_rate)
+        seq = np.where(art, 0, seq)
+        if artifact_q is not None:
+            qual = np.where(art, np.uint8(artifact_q), qual)
+    seq = np.where(err, (seq + rng.integers(1, 4, size=(n, L))) % 4, seq).astype(np.uint8)
+    codes = CODE_OF[seq]
+    nmask = rng.random((n, L)) < n_rate
+    codes[nmask] = CODE_N
+    qual[nmask] = 2
+
+    mapq = np.where(rng.random(n) < mapq0_frac, 0, 60).astype(np.uint8)
+    pos = start.astype(np.int64).copy()
+    cig_list: list[list[int] | None] = [None] * n
+    ref_codes = CODE_OF[genome]
+
+    # indel-carrying reads: rebuild sequence and CIGAR from the haplotype
+    for r, vis in carried_indels.items():
+        s0 = int(start[r])
+        bases: list[int] = []
+        ops: list[list[int]] = []
+
+        def push(op, ln):
+            if ln <= 0:
+                return
+            if ops and ops[-1][0] == op:
+                ops[-1][1] += ln
+            else:
+                ops.append([op, ln])
+        p = s0
+        vq = [variants[i] for i in sorted(vis, key=lambda i: variants[i].pos)]
+        j = 0
+        while len(bases) < L:
+            if j < len(vq) and p == vq[j].pos:
+                v = vq[j]
+                j += 1
+                if v.kind == "ins":
+                    k = min(len(v.alt), L - len(bases))
+                    bases.extend("ACGT".index(c) for c in v.alt[:k])
+                    push(OP_I, k)
+                    continue
+                else:
+                    push(OP_D, len(v.ref))
+                    p += len(v.ref)
+                    continue
+            bases.append(int(genome[p]))
+            push(OP_M, 1)
+            p += 1
+        # keep the simulated error/N pattern on the matched bases
+        b = np.array(bases[:L], dtype=np.uint8)
+        c = CODE_OF[b]
+        keep_err = err[r] | nmask[r]
+        c = np.where(nmask[r], CODE_N, np.where(err[r], CODE_OF[(b + 1) % 4], c))
+        codes[r] = c
+        if ops[-1][0] != OP_M:   # never end on an indel
+            ops[-1][0] = OP_S if ops[-1][0] == OP_I else ops[-1][0]
+        cig_list[r] = [(ln << 4) | op for op, ln in ops]
+        del keep_err
+
+    # soft clips on a fraction of the plain reads
+    clip = (rng.random(n) < softclip_frac)
+    clip_len = rng.integers(5, 31, size=n)
+    clip_5p = rng.random(n) < 0.5
+    junk = rng.random(n) < 0.5
+    for r in np.nonzero(clip)[0].tolist():
+        if cig_list[r] is not None:
+            continue
+        k = int(clip_len[r])
+        if junk[r]:
+            rnd = CODE_OF[rng.integers(0, 4, size=k)]
+            if clip_5p[r]:
+                codes[r, :k] = rnd
+            else:
+                codes[r, L - k:] = rnd
+        if clip_5p[r]:
+            cig_list[r] = [(k << 4) | OP_S, ((L - k) << 4) | OP_M]
+            pos[r] += k
+        else:
+            cig_list[r] = [((L - k) << 4) | OP_M, (k << 4) | OP_S]
+
+    # NM: mismatches (N included) over aligned bases plus inserted/deleted bases
+    ref_win = ref_codes[np.clip(start[:, None] + np.arange(L)[None, :], 0, G - 1)]
+    nm = (codes != ref_win).sum(axis=1).astype(np.int32)
+    for r in [i for i in range(n) if cig_list[i] is not None]:
+        cg = cig_list[r]
+        q = 0
+        rp = int(pos[r])
+        m = 0
+        for w in cg:
+            op, ln = w & 15, w >> 4
+            if op == OP_M:
+                m += int((codes[r, q:q + ln] != ref_codes[rp:rp + ln]).sum())
+                q += ln
+                rp += ln
+            elif op == OP_I:
+                m += ln
+                q += ln
+            elif op == OP_D:
+                m += ln
+                rp += ln
+            elif op == OP_S:
+                q += ln
+        nm[r] = m
+
+    # mate fields follow the (possibly clipped) alignment starts
+    mate_of = np.concatenate([np.arange(n_frag, n), np.arange(0, n_frag)])
+    mpos = pos[mate_of]
+    flag = (0x1 | 0x2 | np.where(rev, 0x10, 0) | np.where(rev[mate_of], 0x20, 0)
+            | np.where(is_r1, 0x40, 0x80)).astype(np.uint16)
+
+    order = np.lexsort((frag, pos))
+    return _pack(contig, G, order, pos, flag, mapq, mpos, isize, nm, cig_list, codes, qual,
+                 frag + name_base, L)
+
+
+def _pack(contig, G, order, pos, flag, mapq, mpos, isize, nm, cig_list, codes, qual, names, L):
+    n = order.shape[0]
+    n_cigar = np.ones(n, dtype=np.uint16)
+    cig_words = []
+    default = np.uint32((L << 4) | OP_M)
+    for i, r in enumerate(order.tolist()):
+        cg = cig_list[r]
+        if cg is None:
+            cig_words.append([int(default)])
+        else:
+            n_cigar[i] = len(cg)
+            cig_words.append(cg)
+    cig_off = np.zeros(n, dtype=np.uint32)
+    cig_off[1:] = np.cumsum(n_cigar[:-1].astype(np.uint32))
+    cigar = np.fromiter((w for cg in cig_words for w in cg), dtype=np.uint32)
+    stride = (L + 31) // 32 * 32
+    base_off = (np.arange(n, dtype=np.uint64) * stride)
+    seq4 = np.zeros(n * stride, dtype=np.uint8)
+    qv = np.zeros(n * stride, dtype=np.uint8)
+    seq4.reshape(n, stride)[:, :L] = codes[order]
+    qv.reshape(n, stride)[:, :L] = qual[order]
+    return ReadSet(contig=contig, contig_len=int(G), pos=pos[order].astype(np.int32),
+                   flag=flag[order], mapq=mapq[order], mpos=mpos[order].astype(np.int32),
+                   isize=isize[order].astype(np.int32), nm=nm[order],
+                   n_cigar=n_cigar, cig_off=cig_off, cigar=cigar,
+                   l_qseq=np.full(n, L, dtype=np.int32), base_off=base_off,
+                   seq4=seq4, qual=qv, name_id=names[order].astype(np.int64))
+
+
+# --------------------------------------------------------------------------
+# writers (BGZF/BAM per SAM spec 4.1-4.2, FASTA + .fai, BED)
+# --------------------------------------------------------------------------
+_BGZF_EOF = bytes.fromhex("1f8b08040000000000ff0600424302001b0003000000000000000000")
+
+
+def _bgzf_block(data: bytes, level: int) -> bytes:
+    co = zlib.compressobj(level, zlib.DEFLATED, -15)
+    cdata = co.compress(data) + co.flush()
+    bsize = len(cdata) + 25
+    hdr = struct.pack("<BBBBIBBHBBHH", 31, 139, 8, 4, 0, 0, 255, 6, 66, 67, 2, bsize)
+    return hdr + cdata + struct.pack("<II", zlib.crc32(data) & 0xFFFFFFFF, len(data))
+
+
+def write_bgzf(path: str, payload: bytes, level: int = 1) -> None:
+    with open(path, "wb") as f:
+        step = 0xFF00
+        for i in range(0, len(payload), step):
+            f.write(_bgzf_block(payload[i:i + step], level))
+        f.write(_BGZF_EOF)
+
+
+def _reg2bin(beg: int, end: int) -> int:
+    """UCSC binning scheme (SAM spec 5.3)."""
+    end -= 1
+    if beg >> 14 == end >> 14:
+        return ((1 << 15) - 1) // 7 + (beg >> 14)
+    if beg >> 17 == end >> 17:
+        return ((1 << 12) - 1) // 7 + (beg >> 17)
+    if beg >> 20 == end >> 20:
+        return ((1 << 9) - 1) // 7 + (beg >> 20)
+    if beg >> 23 == end >> 23:
+        return ((1 << 6) - 1) // 7 + (beg >> 23)
+    if beg >> 26 == end >> 26:
+        return ((1 << 3) - 1) // 7 + (beg >> 26)
+    return 0
+
+
+def bam_bytes(rs: ReadSet, sample: str = "S") -> bytes:
+    text = f"@HD\tVN:1.6\tSO:coordinate\n@SQ\tSN:{rs.contig}\tLN:{rs.contig_len}\n@RG\tID:{sample}\tSM:{sample}\n".encode()
+    out = [b"BAM\x01", struct.pack("<I", len(text)), text, struct.pack("<I", 1),
+           struct.pack("<I", len(rs.contig) + 1), rs.contig.encode() + b"\x00",
+           struct.pack("<I", rs.contig_len)]
+    packed = rs.packed_seq()
+    cig = rs.cigar
+    for i in range(rs.n):
+        name = b"r%d\x00" % int(rs.name_id[i])
+        nc = int(rs.n_cigar[i])
+        co = int(rs.cig_off[i])
+        words = cig[co:co + nc]
+        L = int(rs.l_qseq[i])
+        bo = int(rs.base_off[i])
+        ref_len = 0
+        for w in words.tolist():
+            if (w & 15) in (0, 2, 3, 7, 8):
+                ref_len += w >> 4
+        p = int(rs.pos[i])
+        b = _reg2bin(p, p + max(ref_len, 1))
+        seqb = packed[bo // 2: bo // 2 + (L + 1) // 2].tobytes()
+        qb = rs.qual[bo:bo + L].tobytes()
+        aux = b"NMi" + struct.pack("<i", int(rs.nm[i]))
+        body = struct.pack("<iiBBHHHiiii", 0, p, len(name), int(rs.mapq[i]), b, nc,
+                           int(rs.flag[i]), L, 0, int(rs.mpos[i]), int(rs.isize[i]))
+        rec = body + name + words.astype("<u4").tobytes() + seqb + qb + aux
+        out.append(struct.pack("<I", len(rec)))
+        out.append(rec)
+    return b"".join(out)
+
+
+def write_bam(path: str, rs: ReadSet, sample: str = "S") -> None:
+    write_bgzf(path, bam_bytes(rs, sample))
+    # the shim builds its own in-memory index; an empty .bai marks the file as indexed
+    open(path + ".bai", "wb").close()
+
+
+def write_fasta(path: str, name: str, genome: np.ndarray, width: int = 60) -> None:
+    s = genome_str(genome)
+    with open(path, "w") as f:
+        hdr = f">{name}\n"
+        f.write(hdr)
+        for i in range(0, len(s), width):
+            f.write(s[i:i + width] + "\n")
+    with open(path + ".fai", "w") as f:
+        f.write(f"{name}\t{len(s)}\t{len(hdr)}\t{width}\t{width + 1}\n")
+
+
+def write_bed(path: str, contig: str, regions: list[tuple[int, int]], name: str = "g") -> None:
+    """4-column BED (0-based start, end), the layout RabbitVar treats as
+    zero-based (src/RegionBuilder.cpp buildRegions)."""
+    with open(path, "w") as f:
+        for s, e in regions:
+            f.write(f"{contig}\t{s}\t{e}\t{name}\n")
+
+
+# --------------------------------------------------------------------------
+# workload presets (shapes of the reference's benchmark configurations)
+# --------------------------------------------------------------------------
+def germline_small(seed: int = 0x5EED0000, length: int = 100_000, depth: float = 30.0):
+    """100 kb contig, 30x 2x150 pairs, SNVs 1e-3/bp (VAF 0.5|1.0), indels
+    1-10 bp at 1e-4/bp: the single-sample germline shape."""
+    rng = np.random.default_rng(seed)
+    g = make_genome(length, rng)
+    vs = plant_variants(g, rng, 1e-3, 1e-4, lambda r: 0.5 if r.random() < 0.7 else 1.0)
+    rs = simulate(g, vs, depth, rng)
+    return g, vs, rs
+
+
+def somatic_pair(seed: int = 0x5EED0001, length: int = 1_000_000, tumor_depth: float = 200.0,
+                 normal_depth: float = 100.0):
+    """Tumor/normal pair: germline SNVs 1e-3/bp in both, somatic SNV/MNV
+    2e-5/bp with VAF ~U(0.01, 0.5) in the tumor, strand-biased artifacts
+    5e-6/bp with a 95% single-strand fraction."""
+    rng = np.random.default_rng(seed)
+    g = make_genome(length, rng)
+    germ = plant_variants(g, rng, 1e-3, 1e-4, lambda r: 0.5 if r.random() < 0.7 else 1.0)
+    som = plant_variants(g, rng, 2e-5, 0.0, lambda r: r.uniform(0.01, 0.5), mnv_frac=0.3, avoid=germ)
+    art = plant_variants(g, rng, 5e-6, 0.0, lambda r: r.uniform(0.05, 0.2), avoid=germ + som)
+    for v in art:
+        v.strand_bias = 0.95
+        v.strand = int(rng.integers(0, 2))
+    tumor = simulate(g, germ + som + art, tumor_depth, rng, name_base=0)
+    normal = simulate(g, germ, normal_depth, rng, name_base=10_000_000)
+    return g, (germ, som, art), tumor, normal
