@@ -1,0 +1,179 @@
+/* rvgpu.h -- C ABI of the GB300 pileup-and-scoring library.
+ *
+ * Replaces the per-region stage sequence RabbitVar runs in one_region_run
+ * (src/modes/simpleMode.cpp:18-64):
+ *     RecordPreprocessor(region, conf, bamReaders)       src/recordPreprocessor.cpp:10-32
+ *     CigarParser::process(Scope<InitialData>)           src/parseCigar.cpp:410-440
+ *     VariationRealigner::process(Scope<VariationData>)  src/VariationRealigner.cpp:135-161
+ *     ToVarsBuilder::process(Scope<RealignedVariationData>) src/ToVarsBuilder.cpp:97-205
+ *     SimpleMode::output / print_output_variant_simple   src/modes/simpleMode.cpp:66-208
+ * for a whole batch of regions at once.  All entry points are extern "C",
+ * take plain pointers and sizes, return rv_status (0 = OK, negative = error)
+ * and never exit the process.  One context per host thread; calls on one
+ * context are not thread-safe.  The context owns all device memory; the
+ * caller owns every host buffer it passes in.
+ */
+#ifndef RVGPU_H
+#define RVGPU_H
+#include <stddef.h>
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int rv_status;
+enum {
+    RV_OK = 0,
+    RV_ERR_ARG = -1,         /* bad argument or size */
+    RV_ERR_CUDA = -2,        /* a CUDA runtime call failed (rv_last_error has the text) */
+    RV_ERR_CAPACITY = -3,    /* a device table overflowed; retry with a larger budget */
+    RV_ERR_TIMEOUT = -4,     /* a bounded device wait gave up */
+    RV_ERR_UNSUPPORTED = -5, /* input uses a feature this build does not handle */
+    RV_ERR_STATE = -6,       /* call out of order (e.g. score before pileup) */
+    RV_ERR_COLLISION = -7,   /* allele-key fingerprint collision detected */
+    RV_ERR_FORMAT = -8       /* malformed BAM/BGZF input */
+};
+
+typedef struct rv_ctx rv_ctx;
+
+/* Mirrors the Configuration fields the path reads (include/Configuration.h:98-401).
+ * rv_default_params fills the reference's defaults. */
+typedef struct {
+    double goodq;          /* -q  22.5 */
+    int32_t vext;          /* -X  2 */
+    int32_t mismatch;      /* -m  8 */
+    int32_t local_realign; /* -k  1 (this build supports 0; 1 returns RV_ERR_UNSUPPORTED) */
+    double freq;           /* -f  0.01 */
+    int32_t minr;          /* -r  2 */
+    int32_t read_pos_filter; /* -P 5 */
+    double qratio;         /* -o  1.5 */
+    double mapq_filter;    /* -O  0 */
+    int32_t min_mapq;      /* -Q  0 */
+    double lofreq;         /* -V  0.05 */
+    double bias;           /* 0.05 */
+    int32_t min_bias_reads; /* -B 2 */
+    int32_t samfilter;     /* -F  0x504 */
+    int32_t ref_extension; /* -Y  1200 */
+    int32_t extend_nt;     /* -x  0 */
+    int32_t trim_bases_after; /* -T 0 */
+    int32_t minmatch;      /* -M  0 */
+    int32_t dedup;         /* -t */
+    int32_t unique_fwd;    /* -u */
+    int32_t unique_first;  /* --UN */
+    int32_t do_pileup;     /* -p (this build supports 0) */
+    int32_t fisher;        /* --fisher */
+    int32_t move_indels_3; /* -3 */
+    int32_t svminlen;      /* 1000 */
+} rv_params;
+
+/* Reads of one contig in coordinate (file) order, structure of arrays.
+ * seq is BAM-packed (4-bit codes, high nibble first) at byte base_off[i]/2;
+ * qual holds one Phred byte per base at base_off[i]; base_off[i] must be a
+ * multiple of 32 (so every read's bases start 16-byte aligned).
+ * nm[i] is the NM tag or INT32_MIN when the record has none. */
+typedef struct {
+    int64_t n_reads;
+    const int32_t *pos;      /* 0-based leftmost (BAM POS) */
+    const uint16_t *flag;
+    const uint8_t *mapq;
+    const int32_t *mpos;     /* 0-based mate position */
+    const int32_t *nm;
+    const uint16_t *n_cigar;
+    const uint32_t *cig_off; /* index of the first CIGAR word */
+    const uint32_t *cigar;   /* BAM CIGAR words (len << 4 | op) */
+    int64_t n_cigar_words;
+    const int32_t *l_qseq;
+    const uint64_t *base_off;
+    const uint8_t *seq;      /* n_bases / 2 bytes */
+    const uint8_t *qual;     /* n_bases bytes */
+    int64_t n_bases;
+} rv_read_batch;
+
+/* One region [start, end] (1-based inclusive, as Region in include/Region.h). */
+typedef struct {
+    int32_t start;
+    int32_t end;
+} rv_region;
+
+/* Per emitted record, the numeric part; the allele strings and flanks are in
+ * the text produced by rv_format_records. */
+typedef struct {
+    int32_t region;
+    int32_t position;
+    int32_t start, end;
+    int32_t total_cov, var_cov, ref_fwd, ref_rev, alt_fwd, alt_rev;
+    double freq, pmean, qual, mapq, qratio, hifreq, extrafreq, msi, nm;
+    int32_t pstd, qstd, shift3, msint, hicnt, hicov;
+    double fisher_p, fisher_ratio;
+} rv_site_record;
+
+void rv_default_params(rv_params *p);
+
+/* device: CUDA ordinal; hbm_budget: bytes of device memory the context may
+ * hold (0 = up to 90% of free memory). */
+rv_status rv_create(rv_ctx **out, const rv_params *p, int device, size_t hbm_budget);
+void rv_destroy(rv_ctx *ctx);
+const char *rv_last_error(const rv_ctx *ctx);
+
+/* Replaces RecordPreprocessor::makeReference (src/recordPreprocessor.cpp:41-78):
+ * uploads a whole contig (ASCII bases, any case); each region's window is
+ * derived from it exactly as the reference does. */
+rv_status rv_upload_reference(rv_ctx *ctx, const char *chr, const char *bases, int64_t n);
+
+/* Replaces the record iterator (sam_itr_querys + next_record,
+ * src/recordPreprocessor.cpp:101-180) for a batch of regions: copies the
+ * host batch to the device on `stream` (cudaStream_t, NULL = default). */
+rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *reads, const rv_region *regions, int n_regions,
+                          void *stream);
+
+/* Replaces CigarParser::process (src/parseCigar.cpp:410-974): record filters,
+ * CIGAR walk and allele-count maps for every region of the batch. */
+rv_status rv_pileup(rv_ctx *ctx, void *stream);
+
+/* Replaces VariationRealigner::process for -k 0
+ * (adjustMNP, src/VariationRealigner.cpp:334-465): host realigner over the
+ * device-built maps; reads the MNP keys and their neighbours from the
+ * device, applies the merges on the host and writes the changes back. */
+rv_status rv_realign(rv_ctx *ctx, void *stream);
+
+/* Replaces ToVarsBuilder::process (src/ToVarsBuilder.cpp:97-205), the hard
+ * filter (Variant::isGoodVar, include/Variant.h:197-248) and the --fisher
+ * test: per-site statistics and candidate selection on the device. */
+rv_status rv_score(rv_ctx *ctx, void *stream);
+
+/* Replaces SimpleMode::output (src/modes/simpleMode.cpp:144-208): builds the
+ * tab-delimited records (allele strings, MSI, flanks on the host) into a
+ * context-owned buffer valid until the next call on ctx.  `sample` is the -N
+ * name, `gene` the region label (the contig name for -R). */
+rv_status rv_format_records(rv_ctx *ctx, const char *sample, const char *gene, const char **text,
+                            size_t *text_len, int64_t *n_records);
+
+/* Copies up to `cap` numeric records; *n receives the total available. */
+rv_status rv_fetch_records(rv_ctx *ctx, rv_site_record *out, size_t cap, size_t *n);
+
+/* Convenience: submit + pileup + realign + score + format in one call. */
+rv_status rv_call_regions(rv_ctx *ctx, const rv_read_batch *reads, const rv_region *regions, int n_regions,
+                          const char *sample, const char *gene, const char **text, size_t *text_len,
+                          int64_t *n_records);
+
+/* Pileup-boundary map export for parity checks and for host consumers of the
+ * maps (the realigner's input, VariationData in
+ * include/scopedata/VariationData.h:14-56): writes a text dump of region
+ * `region` in the same line format as the oracle dump (P* lines).  Valid
+ * until the next call on ctx. */
+rv_status rv_export_maps(rv_ctx *ctx, int region, const char *stages, const char **text, size_t *text_len);
+
+/* Timing of the last rv_pileup/rv_score call (device time, ms, CUDA events on
+ * the launch stream) and the number of device kernels those calls launched. */
+rv_status rv_last_timings(const rv_ctx *ctx, double *pileup_ms, double *score_ms, double *total_ms,
+                          int64_t *kernels);
+
+/* Fisher exact test on the device for n tables (a,b,c,d) stored as 4*n int32;
+ * writes two-sided p and the simple-mode ratio. Replaces the kt_fisher_exact
+ * call sites (src/modes/simpleMode.cpp:96-108). */
+rv_status rv_fisher_batch(rv_ctx *ctx, const int32_t *tables, int64_t n, double *two_sided, double *ratio);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,44 @@
+/* rvgpu_io.h -- host input helpers of librvgpu (C ABI).
+ *
+ * Replace the htslib calls RabbitVar makes to obtain records and reference
+ * bases (RecordPreprocessor, src/recordPreprocessor.cpp:10-78): BGZF/BAM
+ * decode into pinned structure-of-arrays read batches, FASTA loading, and
+ * pinned host allocations for callers that build batches themselves.
+ */
+#ifndef RVGPU_IO_H
+#define RVGPU_IO_H
+#include "rvgpu.h"
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct rv_bam rv_bam;
+
+/* Inflates a whole BGZF-compressed BAM file (members decoded on `threads`
+ * host threads, 0 = all cores) and indexes its records.  Replaces sam_open +
+ * sam_hdr_read + the record iterator (src/recordPreprocessor.cpp:10-32). */
+rv_status rv_bam_read(const char *path, int threads, rv_bam **out);
+
+/* Reference sequences named in the BAM header (bam_hdr_t target_name/len). */
+rv_status rv_bam_contigs(const rv_bam *bam, int *n, const char *const **names, const int32_t **lens);
+
+/* Structure-of-arrays batch of every record on contig `tid`, in file order,
+ * in pinned host memory owned by `bam` (valid until rv_bam_free). */
+rv_status rv_bam_batch(rv_bam *bam, int tid, rv_read_batch *out);
+
+void rv_bam_free(rv_bam *bam);
+
+/* Reads sequence `name` (NULL = first) of a FASTA file; *seq is malloc'd,
+ * free it with rv_free.  Replaces fai_load/fai_fetch
+ * (src/recordPreprocessor.cpp:56-72). */
+rv_status rv_fasta_read(const char *path, const char *name, char **seq, int64_t *len);
+void rv_free(void *p);
+
+/* Pinned (page-locked) host memory for batch buffers the caller fills. */
+void *rv_alloc_pinned(size_t bytes);
+void rv_free_pinned(void *p);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

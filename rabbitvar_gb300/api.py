@@ -1,0 +1,310 @@
+"""Python front end of librvgpu (ctypes over the C ABI in include/rvgpu.h).
+
+The call sequence mirrors the reference's per-region stages
+(src/modes/simpleMode.cpp:18-64): submit a batch of reads and regions, pile
+them up (CigarParser), realign MNPs (VariationRealigner), score sites
+(ToVarsBuilder + isGoodVar + Fisher) and format the tab-delimited records
+(SimpleMode::output).  Every error status raises RvError; nothing here
+falls back to a CPU implementation.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "librvgpu.so")
+
+STATUS = {0: "OK", -1: "ERR_ARG", -2: "ERR_CUDA", -3: "ERR_CAPACITY", -4: "ERR_TIMEOUT", -5: "ERR_UNSUPPORTED",
+          -6: "ERR_STATE", -7: "ERR_COLLISION", -8: "ERR_FORMAT"}
+
+
+class RvError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class Params(C.Structure):
+    _fields_ = [("goodq", C.c_double), ("vext", C.c_int32), ("mismatch", C.c_int32), ("local_realign", C.c_int32),
+                ("freq", C.c_double), ("minr", C.c_int32), ("read_pos_filter", C.c_int32), ("qratio", C.c_double),
+                ("mapq_filter", C.c_double), ("min_mapq", C.c_int32), ("lofreq", C.c_double), ("bias", C.c_double),
+                ("min_bias_reads", C.c_int32), ("samfilter", C.c_int32), ("ref_extension", C.c_int32),
+                ("extend_nt", C.c_int32), ("trim_bases_after", C.c_int32), ("minmatch", C.c_int32),
+                ("dedup", C.c_int32), ("unique_fwd", C.c_int32), ("unique_first", C.c_int32),
+                ("do_pileup", C.c_int32), ("fisher", C.c_int32), ("move_indels_3", C.c_int32),
+                ("svminlen", C.c_int32)]
+
+
+class ReadBatch(C.Structure):
+    _fields_ = [("n_reads", C.c_int64), ("pos", C.c_void_p), ("flag", C.c_void_p), ("mapq", C.c_void_p),
+                ("mpos", C.c_void_p), ("nm", C.c_void_p), ("n_cigar", C.c_void_p), ("cig_off", C.c_void_p),
+                ("cigar", C.c_void_p), ("n_cigar_words", C.c_int64), ("l_qseq", C.c_void_p),
+                ("base_off", C.c_void_p), ("seq", C.c_void_p), ("qual", C.c_void_p), ("n_bases", C.c_int64)]
+
+
+class Region(C.Structure):
+    _fields_ = [("start", C.c_int32), ("end", C.c_int32)]
+
+
+class SiteRecord(C.Structure):
+    _fields_ = ([(n, C.c_int32) for n in ("region", "position", "start", "end", "total_cov", "var_cov", "ref_fwd",
+                                          "ref_rev", "alt_fwd", "alt_rev")] +
+                [(n, C.c_double) for n in ("freq", "pmean", "qual", "mapq", "qratio", "hifreq", "extrafreq", "msi",
+                                           "nm")] +
+                [(n, C.c_int32) for n in ("pstd", "qstd", "shift3", "msint", "hicnt", "hicov")] +
+                [("fisher_p", C.c_double), ("fisher_ratio", C.c_double)])
+
+
+EXPORTS = ["rv_default_params", "rv_create", "rv_destroy", "rv_last_error", "rv_upload_reference",
+           "rv_submit_batch", "rv_pileup", "rv_realign", "rv_score", "rv_format_records", "rv_fetch_records",
+           "rv_call_regions", "rv_export_maps", "rv_last_timings", "rv_fisher_batch", "rv_bam_read",
+           "rv_bam_contigs", "rv_bam_batch", "rv_bam_free", "rv_fasta_read", "rv_free", "rv_alloc_pinned",
+           "rv_free_pinned"]
+
+_lib = None
+
+
+def lib():
+    """Load librvgpu.so (building it first when it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        from . import build as _b
+        _b.build()
+    L = C.CDLL(LIB_PATH)
+    vp, i32, i64, sz = C.c_void_p, C.c_int32, C.c_int64, C.c_size_t
+    L.rv_default_params.argtypes = [C.POINTER(Params)]
+    L.rv_create.argtypes = [C.POINTER(vp), C.POINTER(Params), C.c_int, sz]
+    L.rv_destroy.argtypes = [vp]
+    L.rv_last_error.argtypes = [vp]
+    L.rv_last_error.restype = C.c_char_p
+    L.rv_upload_reference.argtypes = [vp, C.c_char_p, C.c_char_p, i64]
+    L.rv_submit_batch.argtypes = [vp, C.POINTER(ReadBatch), C.POINTER(Region), C.c_int, vp]
+    L.rv_pileup.argtypes = [vp, vp]
+    L.rv_realign.argtypes = [vp, vp]
+    L.rv_score.argtypes = [vp, vp]
+    L.rv_format_records.argtypes = [vp, C.c_char_p, C.c_char_p, C.POINTER(C.c_char_p), C.POINTER(sz),
+                                    C.POINTER(i64)]
+    L.rv_fetch_records.argtypes = [vp, C.POINTER(SiteRecord), sz, C.POINTER(sz)]
+    L.rv_export_maps.argtypes = [vp, C.c_int, C.c_char_p, C.POINTER(vp), C.POINTER(sz)]
+    L.rv_last_timings.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                  C.POINTER(i64)]
+    L.rv_fisher_batch.argtypes = [vp, vp, i64, vp, vp]
+    L.rv_bam_read.argtypes = [C.c_char_p, C.c_int, C.POINTER(vp)]
+    L.rv_bam_contigs.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(vp), C.POINTER(vp)]
+    L.rv_bam_batch.argtypes = [vp, C.c_int, C.POINTER(ReadBatch)]
+    L.rv_bam_free.argtypes = [vp]
+    L.rv_fasta_read.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(vp), C.POINTER(i64)]
+    L.rv_free.argtypes = [vp]
+    L.rv_alloc_pinned.argtypes = [sz]
+    L.rv_alloc_pinned.restype = vp
+    L.rv_free_pinned.argtypes = [vp]
+    _lib = L
+    return L
+
+
+def default_params(**kw) -> Params:
+    p = Params()
+    lib().rv_default_params(C.byref(p))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+class Batch:
+    """Host structure-of-arrays read batch (keeps its arrays alive).
+
+    With pinned=True the arrays are allocated in page-locked memory."""
+
+    FIELDS = [("pos", np.int32), ("flag", np.uint16), ("mapq", np.uint8), ("mpos", np.int32), ("nm", np.int32),
+              ("n_cigar", np.uint16), ("cig_off", np.uint32), ("cigar", np.uint32), ("l_qseq", np.int32),
+              ("base_off", np.uint64), ("seq", np.uint8), ("qual", np.uint8)]
+
+    def __init__(self, arrays: dict, pinned: bool = False):
+        self._pinned = []
+        self.arrays = {}
+        for name, dt in self.FIELDS:
+            a = np.ascontiguousarray(arrays[name], dtype=dt)
+            if pinned:
+                ptr = lib().rv_alloc_pinned(max(a.nbytes, 1))
+                if not ptr:
+                    raise RvError(-2, "pinned allocation failed")
+                self._pinned.append(ptr)
+                buf = (C.c_uint8 * max(a.nbytes, 1)).from_address(ptr)
+                b = np.frombuffer(buf, dtype=dt, count=a.size)
+                b[...] = a
+                a = b
+            self.arrays[name] = a
+        self.n_reads = int(self.arrays["pos"].size)
+        self.n_bases = int(arrays.get("n_bases", self.arrays["qual"].size))
+        self.nbytes = sum(a.nbytes for a in self.arrays.values())
+
+    @classmethod
+    def from_readset(cls, rs, pinned: bool = False) -> "Batch":
+        arrs = dict(pos=rs.pos, flag=rs.flag, mapq=rs.mapq, mpos=rs.mpos, nm=rs.nm, n_cigar=rs.n_cigar,
+                    cig_off=rs.cig_off, cigar=rs.cigar, l_qseq=rs.l_qseq, base_off=rs.base_off,
+                    seq=rs.packed_seq(), qual=rs.qual, n_bases=rs.qual.size)
+        return cls(arrs, pinned=pinned)
+
+    def struct(self) -> ReadBatch:
+        b = ReadBatch()
+        b.n_reads = self.n_reads
+        for name, _ in self.FIELDS:
+            setattr(b, name, self.arrays[name].ctypes.data)
+        b.n_cigar_words = int(self.arrays["cigar"].size)
+        b.n_bases = self.n_bases
+        return b
+
+    def close(self):
+        for p in self._pinned:
+            lib().rv_free_pinned(p)
+        self._pinned = []
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Context:
+    """One GPU context (rv_ctx): device memory, stream, and the last results."""
+
+    def __init__(self, params: Params | None = None, device: int = 0, budget: int = 0):
+        self.L = lib()
+        self.params = params or default_params(local_realign=0)
+        self.h = C.c_void_p()
+        st = self.L.rv_create(C.byref(self.h), C.byref(self.params), device, budget)
+        self._check(st)
+
+    def _check(self, st: int):
+        if st != 0:
+            msg = self.L.rv_last_error(self.h).decode() if self.h else ""
+            raise RvError(st, msg)
+
+    def close(self):
+        if self.h:
+            self.L.rv_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload_reference(self, chr_name: str, bases: bytes):
+        self._check(self.L.rv_upload_reference(self.h, chr_name.encode(), bases, len(bases)))
+
+    def submit(self, batch: Batch, regions: list[tuple[int, int]]):
+        self._batch_struct = batch.struct()
+        self._regions = (Region * max(len(regions), 1))(*[Region(a, b) for a, b in regions])
+        self._check(self.L.rv_submit_batch(self.h, C.byref(self._batch_struct), self._regions, len(regions), None))
+
+    def pileup(self):
+        self._check(self.L.rv_pileup(self.h, None))
+
+    def realign(self):
+        self._check(self.L.rv_realign(self.h, None))
+
+    def score(self):
+        self._check(self.L.rv_score(self.h, None))
+
+    def format_records(self, sample: str = "S", gene: str | None = None) -> tuple[str, int]:
+        t = C.c_char_p()
+        n = C.c_size_t()
+        nrec = C.c_int64()
+        self._check(self.L.rv_format_records(self.h, sample.encode(), gene.encode() if gene else None,
+                                             C.byref(t), C.byref(n), C.byref(nrec)))
+        return C.string_at(t, n.value).decode(), nrec.value
+
+    def records(self) -> list[SiteRecord]:
+        n = C.c_size_t()
+        self._check(self.L.rv_fetch_records(self.h, None, 0, C.byref(n)))
+        arr = (SiteRecord * max(n.value, 1))()
+        self._check(self.L.rv_fetch_records(self.h, arr, n.value, C.byref(n)))
+        return list(arr[:n.value])
+
+    def call(self, batch: Batch, regions, sample: str = "S", gene: str | None = None) -> str:
+        self.submit(batch, regions)
+        self.pileup()
+        self.realign()
+        self.score()
+        return self.format_records(sample, gene)[0]
+
+    def export_maps(self, region: int = 0, stages: str = "P") -> str:
+        t = C.c_void_p()
+        n = C.c_size_t()
+        self._check(self.L.rv_export_maps(self.h, region, stages.encode(), C.byref(t), C.byref(n)))
+        return C.string_at(t, n.value).decode()
+
+    def timings(self) -> dict:
+        a, b, c = C.c_double(), C.c_double(), C.c_double()
+        k = C.c_int64()
+        self._check(self.L.rv_last_timings(self.h, C.byref(a), C.byref(b), C.byref(c), C.byref(k)))
+        return dict(pileup_ms=a.value, score_ms=b.value, total_ms=c.value, kernels=k.value)
+
+    def fisher(self, tables: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+        t = np.ascontiguousarray(tables, dtype=np.int32).reshape(-1, 4)
+        p = np.zeros(t.shape[0])
+        r = np.zeros(t.shape[0])
+        self._check(self.L.rv_fisher_batch(self.h, t.ctypes.data, t.shape[0], p.ctypes.data, r.ctypes.data))
+        return p, r
+
+
+def read_bam(path: str, threads: int = 0):
+    """Decode a BAM file with the library's host decoder; returns
+    (contig names, lengths, {tid: Batch}) with copies of the arrays."""
+    L = lib()
+    h = C.c_void_p()
+    st = L.rv_bam_read(path.encode(), threads, C.byref(h))
+    if st != 0:
+        raise RvError(st, f"cannot decode {path}")
+    try:
+        n = C.c_int()
+        names = C.c_void_p()
+        lens = C.c_void_p()
+        L.rv_bam_contigs(h, C.byref(n), C.byref(names), C.byref(lens))
+        nm = [C.cast(names, C.POINTER(C.c_char_p))[i].decode() for i in range(n.value)]
+        ln = [C.cast(lens, C.POINTER(C.c_int32))[i] for i in range(n.value)]
+        out = {}
+        for tid in range(n.value):
+            rb = ReadBatch()
+            st = L.rv_bam_batch(h, tid, C.byref(rb))
+            if st != 0:
+                raise RvError(st, "rv_bam_batch")
+            nr = rb.n_reads
+
+            def arr(ptr, dt, count):
+                if count == 0:
+                    return np.zeros(0, dt)
+                return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(np.ctypeslib.as_ctypes_type(dt))),
+                                             shape=(count,)).copy()
+            arrays = dict(pos=arr(rb.pos, np.int32, nr), flag=arr(rb.flag, np.uint16, nr),
+                          mapq=arr(rb.mapq, np.uint8, nr), mpos=arr(rb.mpos, np.int32, nr),
+                          nm=arr(rb.nm, np.int32, nr), n_cigar=arr(rb.n_cigar, np.uint16, nr),
+                          cig_off=arr(rb.cig_off, np.uint32, nr), cigar=arr(rb.cigar, np.uint32, rb.n_cigar_words),
+                          l_qseq=arr(rb.l_qseq, np.int32, nr), base_off=arr(rb.base_off, np.uint64, nr),
+                          seq=arr(rb.seq, np.uint8, (rb.n_bases + 1) // 2), qual=arr(rb.qual, np.uint8, rb.n_bases),
+                          n_bases=rb.n_bases)
+            out[tid] = Batch(arrays)
+        return nm, ln, out
+    finally:
+        L.rv_bam_free(h)
+
+
+def read_fasta(path: str, name: str | None = None) -> bytes:
+    L = lib()
+    p = C.c_void_p()
+    n = C.c_int64()
+    st = L.rv_fasta_read(path.encode(), name.encode() if name else None, C.byref(p), C.byref(n))
+    if st != 0:
+        raise RvError(st, f"cannot read {path}")
+    try:
+        return C.string_at(p, n.value)
+    finally:
+        L.rv_free(p)

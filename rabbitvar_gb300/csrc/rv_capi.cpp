@@ -1,0 +1,553 @@
+// C ABI of librvgpu (include/rvgpu.h): context, device memory, batch upload,
+// and the stage sequence pileup -> realign -> score -> format.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "rv_ctx.h"
+
+namespace rv {
+rv_status host_realign_mnp(rv_ctx *ctx);
+rv_status host_format_records(rv_ctx *ctx, const char *sample, const char *gene);
+rv_status host_export_maps(rv_ctx *ctx, int region, const char *stages);
+}  // namespace rv
+
+using namespace rv;
+
+#define RV_CUDA(call)                                                              \
+    do {                                                                           \
+        cudaError_t e_ = (call);                                                   \
+        if (e_ != cudaSuccess) {                                                   \
+            ctx->err = std::string(#call) + ": " + cudaGetErrorString(e_);         \
+            return RV_ERR_CUDA;                                                    \
+        }                                                                          \
+    } while (0)
+
+namespace {
+
+template <class T>
+rv_status grow(rv_ctx *ctx, T *&p, size_t &cap, size_t need) {
+    if (need <= cap && p) return RV_OK;
+    if (p) cudaFree(p);
+    p = nullptr;
+    size_t n = std::max<size_t>(need + need / 4, 1024);
+    RV_CUDA(cudaMalloc((void **)&p, n * sizeof(T)));
+    cap = n;
+    return RV_OK;
+}
+
+unsigned long long next_pow2(unsigned long long x) {
+    unsigned long long p = 1;
+    while (p < x) p <<= 1;
+    return p;
+}
+
+enum { CNT_TILE = 0, CNT_DEFER = 1, CNT_USED = 2, CNT_ERR = 3, CNT_CAND = 4, CNT_AUX = 5 };
+
+}  // namespace
+
+DevState rv_ctx::state() const {
+    DevState s;
+    s.batch.n_reads = n_reads;
+    s.batch.pos = d_pos;
+    s.batch.mpos = d_mpos;
+    s.batch.nm = d_nm;
+    s.batch.l_qseq = d_lq;
+    s.batch.flag = d_flag;
+    s.batch.n_cigar = d_ncig;
+    s.batch.mapq = d_mapq;
+    s.batch.cig_off = d_cigoff;
+    s.batch.cigar = d_cigar;
+    s.batch.base_off = d_boff;
+    s.batch.seq = d_seq;
+    s.batch.qual = d_qual;
+    s.regions = d_regions;
+    s.n_regions = (int32_t)regions.size();
+    s.tiles = d_tiles;
+    s.n_tiles = (int32_t)tiles.size();
+    s.tile_counter = d_counters + CNT_TILE;
+    s.cells = cells;
+    s.hash.slots = d_slots;
+    s.hash.mask = hash_cap ? hash_cap - 1 : 0;
+    s.hash.arena = d_arena;
+    s.hash.arena_cap = arena_cap;
+    s.hash.arena_used = (unsigned long long *)(d_counters + 8);
+    s.hash.n_used = d_counters + CNT_USED;
+    s.deferred = d_deferred;
+    s.n_deferred = d_counters + CNT_DEFER;
+    s.deferred_cap = deferred_cap;
+    s.ref = d_ref;
+    s.ref_len = ref_len;
+    s.err = d_counters + CNT_ERR;
+    s.head = d_head;
+    s.score_base = d_score_base;
+    s.n_score = n_score;
+    s.cand = d_cand;
+    s.n_cand = d_counters + CNT_CAND;
+    s.cand_cap = cand_cap;
+    return s;
+}
+
+extern "C" {
+
+void rv_default_params(rv_params *p) {
+    memset(p, 0, sizeof *p);
+    p->goodq = 22.5;
+    p->vext = 2;
+    p->mismatch = 8;
+    p->local_realign = 1;
+    p->freq = 0.01;
+    p->minr = 2;
+    p->read_pos_filter = 5;
+    p->qratio = 1.5;
+    p->mapq_filter = 0;
+    p->min_mapq = 0;
+    p->lofreq = 0.05;
+    p->bias = 0.05;
+    p->min_bias_reads = 2;
+    p->samfilter = 0x504;
+    p->ref_extension = 1200;
+    p->svminlen = 1000;
+}
+
+const char *rv_last_error(const rv_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+rv_status rv_create(rv_ctx **out, const rv_params *p, int device, size_t hbm_budget) {
+    if (!out || !p) return RV_ERR_ARG;
+    *out = nullptr;
+    rv_ctx *ctx = new rv_ctx();
+    ctx->device = device;
+    ctx->params = *p;
+    ctx->budget = hbm_budget;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+    for (int i = 0; e == cudaSuccess && i < 6; i++) e = cudaEventCreate(&ctx->ev[i]);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&ctx->d_counters, 64 * sizeof(unsigned int));
+    if (e != cudaSuccess) {
+        ctx->err = cudaGetErrorString(e);
+        *out = ctx;
+        return RV_ERR_CUDA;
+    }
+    DevParams &d = ctx->dp;
+    memset(&d, 0, sizeof d);
+    d.goodq = p->goodq;
+    d.freq = p->freq;
+    d.qratio = p->qratio;
+    d.mapq_filter = p->mapq_filter;
+    d.lofreq = p->lofreq;
+    d.bias = p->bias;
+    d.vext = p->vext;
+    d.mismatch = p->mismatch;
+    d.local_realign = p->local_realign;
+    d.minr = p->minr;
+    d.read_pos_filter = p->read_pos_filter;
+    d.min_mapq = p->min_mapq;
+    d.min_bias_reads = p->min_bias_reads;
+    d.samfilter = p->samfilter;
+    d.trim_bases_after = p->trim_bases_after;
+    d.minmatch = p->minmatch;
+    d.dedup = p->dedup;
+    d.unique_fwd = p->unique_fwd;
+    d.unique_first = p->unique_first;
+    d.do_pileup = p->do_pileup;
+    d.fisher = p->fisher;
+    d.move_indels_3 = p->move_indels_3;
+    d.svminlen = p->svminlen;
+    *out = ctx;
+    if (p->local_realign) {
+        ctx->err = "local realignment (-k 1) is not supported by this build; use local_realign = 0";
+        return RV_ERR_UNSUPPORTED;
+    }
+    if (p->do_pileup) {
+        ctx->err = "pileup mode (-p) is not supported by this build";
+        return RV_ERR_UNSUPPORTED;
+    }
+    return RV_OK;
+}
+
+void rv_destroy(rv_ctx *ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    void *ptrs[] = {ctx->d_ref, ctx->d_pos, ctx->d_mpos, ctx->d_nm, ctx->d_lq, ctx->d_flag, ctx->d_ncig,
+                    ctx->d_mapq, ctx->d_cigoff, ctx->d_cigar, ctx->d_boff, ctx->d_seq, ctx->d_qual,
+                    ctx->d_regions, ctx->d_tiles, ctx->d_score_base, ctx->d_cellmem, ctx->d_head, ctx->d_slots,
+                    ctx->d_arena, ctx->d_deferred, ctx->d_cand, ctx->d_counters};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    for (int i = 0; i < 6; i++)
+        if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+rv_status rv_upload_reference(rv_ctx *ctx, const char *chr, const char *bases, int64_t n) {
+    if (!ctx || !bases || n <= 0 || n > INT32_MAX) return RV_ERR_ARG;
+    RV_CUDA(cudaSetDevice(ctx->device));
+    ctx->chr = chr ? chr : "";
+    ctx->ref_host.assign(bases, bases + n);
+    for (char &c : ctx->ref_host)
+        if (c >= 'a' && c <= 'z') c = (char)(c - 32);
+    if (ctx->d_ref) cudaFree(ctx->d_ref);
+    ctx->d_ref = nullptr;
+    RV_CUDA(cudaMalloc((void **)&ctx->d_ref, (size_t)n));
+    RV_CUDA(cudaMemcpy(ctx->d_ref, ctx->ref_host.data(), (size_t)n, cudaMemcpyHostToDevice));
+    ctx->ref_len = (int32_t)n;
+    return RV_OK;
+}
+
+rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *regs, int n_regions,
+                          void *stream) {
+    if (!ctx || !b || (!regs && n_regions > 0) || n_regions < 0) return RV_ERR_ARG;
+    if (!ctx->d_ref) { ctx->err = "reference not uploaded"; return RV_ERR_STATE; }
+    RV_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+    const int64_t n = b->n_reads;
+    if (n < 0 || b->n_cigar_words < 0 || b->n_bases < 0) return RV_ERR_ARG;
+    for (int64_t i = 0; i < n; i++)
+        if (b->base_off[i] & 31) { ctx->err = "base_off must be a multiple of 32"; return RV_ERR_ARG; }
+    ctx->n_reads = n;
+    ctx->n_cigar_words = b->n_cigar_words;
+    ctx->n_bases = b->n_bases;
+    size_t cr = ctx->cap_reads, cr2 = cr, cr3 = cr, cr4 = cr, cr5 = cr, cr6 = cr, cr7 = cr, cr8 = cr, cr9 = cr;
+    rv_status st;
+    size_t need = (size_t)std::max<int64_t>(n, 1);
+    if ((st = grow(ctx, ctx->d_pos, cr, need)) || (st = grow(ctx, ctx->d_mpos, cr2, need)) ||
+        (st = grow(ctx, ctx->d_nm, cr3, need)) || (st = grow(ctx, ctx->d_lq, cr4, need)) ||
+        (st = grow(ctx, ctx->d_flag, cr5, need)) || (st = grow(ctx, ctx->d_ncig, cr6, need)) ||
+        (st = grow(ctx, ctx->d_mapq, cr7, need)) || (st = grow(ctx, ctx->d_cigoff, cr8, need)) ||
+        (st = grow(ctx, ctx->d_boff, cr9, need)))
+        return st;
+    ctx->cap_reads = cr;
+    size_t cc = ctx->cap_cigar;
+    if ((st = grow(ctx, ctx->d_cigar, cc, (size_t)std::max<int64_t>(b->n_cigar_words, 1)))) return st;
+    ctx->cap_cigar = cc;
+    size_t cb = ctx->cap_bases, cb2 = cb;
+    if ((st = grow(ctx, ctx->d_qual, cb, (size_t)std::max<int64_t>(b->n_bases, 32) + 64)) ||
+        (st = grow(ctx, ctx->d_seq, cb2, (size_t)std::max<int64_t>(b->n_bases, 32) / 2 + 64)))
+        return st;
+    ctx->cap_bases = cb;
+    if (n > 0) {
+        RV_CUDA(cudaMemcpyAsync(ctx->d_pos, b->pos, n * 4, cudaMemcpyHostToDevice, s));
+        RV_CUDA(cudaMemcpyAsync(ctx->d_mpos, b->mpos, n * 4, cudaMemcpyHostToDevice, s));
+        RV_CUDA(cudaMemcpyAsync(ctx->d_nm, b->nm, n * 4, cudaMemcpyHostToDevice, s));
+        RV_CUDA(cudaMemcpyAsync(ctx->d_lq, b->l_qseq, n * 4, cudaMemcpyHostToDevice, s));
+        RV_CUDA(cudaMemcpyAsync(ctx->d_flag, b->flag, n * 2, cudaMemcpyHostToDevice, s));
+        RV_CUDA(cudaMemcpyAsync(ctx->d_ncig, b->n_cigar, n * 2, cudaMemcpyHostToDevice, s));
+        RV_CUDA(cudaMemcpyAsync(ctx->d_mapq, b->mapq, n, cudaMemcpyHostToDevice, s));
+        RV_CUDA(cudaMemcpyAsync(ctx->d_cigoff, b->cig_off, n * 4, cudaMemcpyHostToDevice, s));
+        RV_CUDA(cudaMemcpyAsync(ctx->d_boff, b->base_off, n * 8, cudaMemcpyHostToDevice, s));
+        RV_CUDA(cudaMemcpyAsync(ctx->d_cigar, b->cigar, b->n_cigar_words * 4, cudaMemcpyHostToDevice, s));
+        RV_CUDA(cudaMemcpyAsync(ctx->d_seq, b->seq, (size_t)(b->n_bases + 1) / 2, cudaMemcpyHostToDevice, s));
+        RV_CUDA(cudaMemcpyAsync(ctx->d_qual, b->qual, (size_t)b->n_bases, cudaMemcpyHostToDevice, s));
+    }
+    // batch-wide bounds used to size the per-region cell ranges
+    int max_span = 1, max_lq = 1;
+    for (int64_t i = 0; i < n; i++) {
+        const uint32_t *c = b->cigar + b->cig_off[i];
+        int sp = 0;
+        for (int k = 0; k < b->n_cigar[i]; k++) {
+            int o = c[k] & 15;
+            if (o == 0 || o == 2 || o == 3 || o == 7 || o == 8) sp += (int)(c[k] >> 4);
+        }
+        max_span = std::max(max_span, sp);
+        max_lq = std::max(max_lq, (int)b->l_qseq[i]);
+    }
+    const int pad = max_span + max_lq + 4;
+    const rv_params &P = ctx->params;
+    ctx->regions.clear();
+    ctx->tiles.clear();
+    ctx->score_base.clear();
+    int64_t cell_base = 0, score = 0;
+    for (int r = 0; r < n_regions; r++) {
+        Region R;
+        memset(&R, 0, sizeof R);
+        R.start = regs[r].start;
+        R.end = regs[r].end;
+        if (R.start < 1 || R.end < R.start) { ctx->err = "bad region"; return RV_ERR_ARG; }
+        int ext = P.ref_extension, x = P.extend_nt;
+        R.ws = R.start - x - ext < 1 ? 1 : R.start - x - ext;
+        int seq_end = R.end + x + ext > ctx->ref_len ? ctx->ref_len : R.end + x + ext;
+        R.we = seq_end - 17;  // CONF_SEED_1
+        R.clo = std::max(1, R.start - pad);
+        R.chi = R.end + pad;
+        // align the cell base so that a region's kflags words are not shared
+        cell_base = (cell_base + 3) & ~3LL;
+        R.cell_base = cell_base;
+        cell_base += (R.chi - R.clo + 1);
+        // reads overlapping [start-1, end): pos < end and pos + span > start-1
+        int lo_pos = R.start - 1 - max_span;
+        R.r0 = std::lower_bound(b->pos, b->pos + n, lo_pos) - b->pos;
+        R.r1 = std::lower_bound(b->pos, b->pos + n, R.end) - b->pos;
+        ctx->regions.push_back(R);
+        ctx->score_base.push_back(score);
+        score += R.end - R.start + 1;
+        // tiles of consecutive reads sized so a tile's window fits kTileW positions
+        int64_t nr = R.r1 - R.r0;
+        if (nr > 0) {
+            double dens = nr / (double)(R.end - R.start + 1 + 2 * max_lq);
+            double usable = (double)kTileW - max_span - 2.0 * max_lq - 16.0;
+            int64_t tr = (int64_t)std::max(32.0, std::min(1024.0, usable * dens));
+            for (int64_t a = R.r0; a < R.r1; a += tr) {
+                Tile t;
+                t.region = r;
+                t.pad = 0;
+                t.r0 = a;
+                t.r1 = std::min(R.r1, a + tr);
+                ctx->tiles.push_back(t);
+            }
+        }
+    }
+    ctx->n_score = score;
+    ctx->n_cells = cell_base + 4;
+    size_t creg = ctx->cap_regions, ct = ctx->cap_tiles, creg2 = ctx->cap_regions;
+    if ((st = grow(ctx, ctx->d_regions, creg, ctx->regions.size() + 1)) ||
+        (st = grow(ctx, ctx->d_score_base, creg2, ctx->regions.size() + 1)) ||
+        (st = grow(ctx, ctx->d_tiles, ct, ctx->tiles.size() + 1)))
+        return st;
+    ctx->cap_regions = creg;
+    ctx->cap_tiles = ct;
+    if (!ctx->regions.empty()) {
+        RV_CUDA(cudaMemcpyAsync(ctx->d_regions, ctx->regions.data(), ctx->regions.size() * sizeof(Region),
+                                cudaMemcpyHostToDevice, s));
+        RV_CUDA(cudaMemcpyAsync(ctx->d_score_base, ctx->score_base.data(), ctx->score_base.size() * 8,
+                                cudaMemcpyHostToDevice, s));
+    }
+    if (!ctx->tiles.empty())
+        RV_CUDA(cudaMemcpyAsync(ctx->d_tiles, ctx->tiles.data(), ctx->tiles.size() * sizeof(Tile),
+                                cudaMemcpyHostToDevice, s));
+    // cells: 7 x 4 words + first (4 words) per position, plus cov, kflags, head
+    size_t need_cells = (size_t)ctx->n_cells;
+    if (need_cells > ctx->cap_cells || !ctx->d_cellmem) {
+        if (ctx->d_cellmem) cudaFree(ctx->d_cellmem);
+        if (ctx->d_head) cudaFree(ctx->d_head);
+        ctx->d_cellmem = nullptr;
+        ctx->d_head = nullptr;
+        size_t cap = need_cells + need_cells / 4 + 1024;
+        cap = (cap + 63) & ~(size_t)63;
+        RV_CUDA(cudaMalloc(&ctx->d_cellmem, cap * (8 * 16 + 4 + 1)));
+        RV_CUDA(cudaMalloc((void **)&ctx->d_head, cap * 4));
+        ctx->cap_cells = cap;
+    }
+    {
+        size_t cap = ctx->cap_cells;
+        char *m = (char *)ctx->d_cellmem;
+        Cells &C = ctx->cells;
+        C.fwd = (uint32_t *)m; m += cap * 16;
+        C.rev = (uint32_t *)m; m += cap * 16;
+        C.hi = (uint32_t *)m; m += cap * 16;
+        C.tp = (uint32_t *)m; m += cap * 16;
+        C.q = (uint32_t *)m; m += cap * 16;
+        C.mq = (uint32_t *)m; m += cap * 16;
+        C.nm = (int32_t *)m; m += cap * 16;
+        C.first = (uint32_t *)m; m += cap * 16;
+        C.cov = (uint32_t *)m; m += cap * 4;
+        C.kflags = (uint8_t *)m;
+        C.n_cells = ctx->n_cells;
+    }
+    // hash table / arena / deferred / candidates sized from the batch
+    unsigned long long want_hash = next_pow2(std::max<unsigned long long>(1ULL << 16, (unsigned long long)n));
+    if (want_hash > ctx->hash_cap || !ctx->d_slots) {
+        if (ctx->d_slots) cudaFree(ctx->d_slots);
+        ctx->d_slots = nullptr;
+        RV_CUDA(cudaMalloc((void **)&ctx->d_slots, want_hash * sizeof(Slot)));
+        ctx->hash_cap = want_hash;
+    }
+    unsigned long long want_arena = std::max<unsigned long long>(1ULL << 20, (unsigned long long)n * 16);
+    if (want_arena > ctx->arena_cap || !ctx->d_arena) {
+        if (ctx->d_arena) cudaFree(ctx->d_arena);
+        ctx->d_arena = nullptr;
+        RV_CUDA(cudaMalloc((void **)&ctx->d_arena, want_arena));
+        ctx->arena_cap = want_arena;
+    }
+    unsigned int want_def = (unsigned int)std::min<int64_t>(INT32_MAX, n / 8 + 4096);
+    if (want_def > ctx->deferred_cap || !ctx->d_deferred) {
+        if (ctx->d_deferred) cudaFree(ctx->d_deferred);
+        ctx->d_deferred = nullptr;
+        RV_CUDA(cudaMalloc((void **)&ctx->d_deferred, (size_t)want_def * sizeof(Deferred)));
+        ctx->deferred_cap = want_def;
+    }
+    unsigned int want_cand = (unsigned int)std::min<int64_t>(INT32_MAX, std::max<int64_t>(1 << 16, score / 4 + 1024));
+    if (want_cand > ctx->cand_cap || !ctx->d_cand) {
+        if (ctx->d_cand) cudaFree(ctx->d_cand);
+        ctx->d_cand = nullptr;
+        RV_CUDA(cudaMalloc((void **)&ctx->d_cand, (size_t)want_cand * sizeof(CandVar)));
+        ctx->cand_cap = want_cand;
+    }
+    ctx->stage = 1;
+    return RV_OK;
+}
+
+rv_status rv_pileup(rv_ctx *ctx, void *stream) {
+    if (!ctx) return RV_ERR_ARG;
+    if (ctx->stage < 1) { ctx->err = "rv_pileup before rv_submit_batch"; return RV_ERR_STATE; }
+    RV_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+    size_t cap = ctx->cap_cells;
+    RV_CUDA(cudaEventRecord(ctx->ev[0], s));
+    RV_CUDA(cudaMemsetAsync(ctx->d_cellmem, 0, cap * (8 * 16 + 4 + 1), s));
+    RV_CUDA(cudaMemsetAsync(ctx->d_head, 0xFF, cap * 4, s));
+    RV_CUDA(cudaMemsetAsync(ctx->d_counters, 0, 64 * sizeof(unsigned int), s));
+    RV_CUDA(cudaMemsetAsync(ctx->d_arena, 0, 16, s));
+    launch_init_slots(ctx->d_slots, ctx->hash_cap, s);
+    DevState st = ctx->state();
+    launch_region_spans(st, s);
+    int per_sm = std::max(1, pileup_blocks_per_sm());
+    int grid = std::max(1, std::min<int>((int)ctx->tiles.size(), per_sm * ctx->sm_count));
+    RV_CUDA(launch_pileup(st, ctx->dp, grid, s));
+    launch_serial(st, ctx->dp, s);
+    launch_resolve(st, ctx->dp, s);
+    launch_link(st, s);
+    launch_collisions(st, s);
+    RV_CUDA(cudaGetLastError());
+    RV_CUDA(cudaEventRecord(ctx->ev[1], s));
+    ctx->kernels = 7;
+    unsigned int err = 0;
+    RV_CUDA(cudaMemcpyAsync(&err, ctx->d_counters + CNT_ERR, 4, cudaMemcpyDeviceToHost, s));
+    RV_CUDA(cudaStreamSynchronize(s));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
+    ctx->pileup_ms = ms;
+    if (err) {
+        char buf[160];
+        snprintf(buf, sizeof buf, "pileup device error bits 0x%x", err);
+        ctx->err = buf;
+        if (err & (ERR_HASH_FULL | ERR_ARENA_FULL | ERR_DEFER_FULL)) return RV_ERR_CAPACITY;
+        if (err & ERR_COLLISION) return RV_ERR_COLLISION;
+        return RV_ERR_UNSUPPORTED;
+    }
+    ctx->stage = 2;
+    return RV_OK;
+}
+
+rv_status rv_realign(rv_ctx *ctx, void *stream) {
+    if (!ctx) return RV_ERR_ARG;
+    if (ctx->stage < 2) { ctx->err = "rv_realign before rv_pileup"; return RV_ERR_STATE; }
+    (void)stream;
+    RV_CUDA(cudaSetDevice(ctx->device));
+    rv_status st = host_realign_mnp(ctx);
+    if (st) return st;
+    ctx->stage = 3;
+    return RV_OK;
+}
+
+rv_status rv_score(rv_ctx *ctx, void *stream) {
+    if (!ctx) return RV_ERR_ARG;
+    if (ctx->stage < 2) { ctx->err = "rv_score before rv_pileup"; return RV_ERR_STATE; }
+    RV_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+    DevState st = ctx->state();
+    RV_CUDA(cudaEventRecord(ctx->ev[2], s));
+    RV_CUDA(cudaMemsetAsync(ctx->d_counters + CNT_CAND, 0, 4, s));
+    launch_ins_adjust(st, s);
+    launch_score(st, ctx->dp, s);
+    RV_CUDA(cudaGetLastError());
+    RV_CUDA(cudaEventRecord(ctx->ev[3], s));
+    unsigned int hdr[8];
+    RV_CUDA(cudaMemcpyAsync(hdr, ctx->d_counters, sizeof hdr, cudaMemcpyDeviceToHost, s));
+    RV_CUDA(cudaStreamSynchronize(s));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]);
+    ctx->score_ms = ms;
+    ctx->kernels += 2;
+    unsigned int n = hdr[CNT_CAND];
+    if (n > ctx->cand_cap) {
+        ctx->err = "candidate buffer overflow";
+        return RV_ERR_CAPACITY;
+    }
+    if (hdr[CNT_ERR] & (ERR_UNSUPPORTED | ERR_CELL_RANGE)) {
+        char buf[96];
+        snprintf(buf, sizeof buf, "score device error bits 0x%x", hdr[CNT_ERR]);
+        ctx->err = buf;
+        return RV_ERR_UNSUPPORTED;
+    }
+    ctx->h_cand.resize(n);
+    if (n) RV_CUDA(cudaMemcpy(ctx->h_cand.data(), ctx->d_cand, (size_t)n * sizeof(CandVar), cudaMemcpyDeviceToHost));
+    unsigned long long used = 0;
+    RV_CUDA(cudaMemcpy(&used, ctx->d_counters + 8, 8, cudaMemcpyDeviceToHost));
+    used = std::min<unsigned long long>(used, ctx->arena_cap);
+    ctx->h_arena.resize(used);
+    if (used) RV_CUDA(cudaMemcpy(ctx->h_arena.data(), ctx->d_arena, used, cudaMemcpyDeviceToHost));
+    ctx->stage = 4;
+    return RV_OK;
+}
+
+rv_status rv_format_records(rv_ctx *ctx, const char *sample, const char *gene, const char **text,
+                            size_t *text_len, int64_t *n_records) {
+    if (!ctx) return RV_ERR_ARG;
+    if (ctx->stage < 4) { ctx->err = "rv_format_records before rv_score"; return RV_ERR_STATE; }
+    rv_status st = host_format_records(ctx, sample ? sample : "", gene ? gene : ctx->chr.c_str());
+    if (st) return st;
+    if (text) *text = ctx->text.c_str();
+    if (text_len) *text_len = ctx->text.size();
+    if (n_records) *n_records = ctx->n_records;
+    return RV_OK;
+}
+
+rv_status rv_fetch_records(rv_ctx *ctx, rv_site_record *out, size_t cap, size_t *n) {
+    if (!ctx || !n) return RV_ERR_ARG;
+    *n = ctx->h_records.size();
+    if (out) memcpy(out, ctx->h_records.data(), std::min(cap, ctx->h_records.size()) * sizeof(rv_site_record));
+    return RV_OK;
+}
+
+rv_status rv_call_regions(rv_ctx *ctx, const rv_read_batch *reads, const rv_region *regions, int n_regions,
+                          const char *sample, const char *gene, const char **text, size_t *text_len,
+                          int64_t *n_records) {
+    rv_status s;
+    if ((s = rv_submit_batch(ctx, reads, regions, n_regions, nullptr))) return s;
+    if ((s = rv_pileup(ctx, nullptr))) return s;
+    if ((s = rv_realign(ctx, nullptr))) return s;
+    if ((s = rv_score(ctx, nullptr))) return s;
+    return rv_format_records(ctx, sample, gene, text, text_len, n_records);
+}
+
+rv_status rv_export_maps(rv_ctx *ctx, int region, const char *stages, const char **text, size_t *text_len) {
+    if (!ctx || region < 0 || region >= (int)ctx->regions.size()) return RV_ERR_ARG;
+    if (ctx->stage < 2) { ctx->err = "rv_export_maps before rv_pileup"; return RV_ERR_STATE; }
+    RV_CUDA(cudaSetDevice(ctx->device));
+    rv_status st = host_export_maps(ctx, region, stages ? stages : "P");
+    if (st) return st;
+    if (text) *text = ctx->dump.c_str();
+    if (text_len) *text_len = ctx->dump.size();
+    return RV_OK;
+}
+
+rv_status rv_last_timings(const rv_ctx *ctx, double *pileup_ms, double *score_ms, double *total_ms,
+                          int64_t *kernels) {
+    if (!ctx) return RV_ERR_ARG;
+    if (pileup_ms) *pileup_ms = ctx->pileup_ms;
+    if (score_ms) *score_ms = ctx->score_ms;
+    if (total_ms) *total_ms = ctx->pileup_ms + ctx->score_ms;
+    if (kernels) *kernels = ctx->kernels;
+    return RV_OK;
+}
+
+rv_status rv_fisher_batch(rv_ctx *ctx, const int32_t *tables, int64_t n, double *two_sided, double *ratio) {
+    if (!ctx || n < 0 || (n > 0 && (!tables || !two_sided || !ratio))) return RV_ERR_ARG;
+    if (n == 0) return RV_OK;
+    RV_CUDA(cudaSetDevice(ctx->device));
+    int32_t *dt = nullptr;
+    double *dp = nullptr;
+    RV_CUDA(cudaMalloc((void **)&dt, (size_t)n * 16));
+    cudaError_t e = cudaMalloc((void **)&dp, (size_t)n * 16);
+    if (e != cudaSuccess) { cudaFree(dt); ctx->err = cudaGetErrorString(e); return RV_ERR_CUDA; }
+    e = cudaMemcpy(dt, tables, (size_t)n * 16, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        launch_fisher(dt, n, dp, dp + n, ctx->stream);
+        e = cudaStreamSynchronize(ctx->stream);
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(two_sided, dp, (size_t)n * 8, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(ratio, dp + n, (size_t)n * 8, cudaMemcpyDeviceToHost);
+    cudaFree(dt);
+    cudaFree(dp);
+    if (e != cudaSuccess) { ctx->err = cudaGetErrorString(e); return RV_ERR_CUDA; }
+    return RV_OK;
+}
+
+}  // extern "C"

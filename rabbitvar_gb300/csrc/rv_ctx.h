@@ -1,0 +1,131 @@
+// Host-side context of librvgpu (not part of the public ABI).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "rv_internal.h"
+
+namespace rv {
+
+// kernel launchers (rv_pileup.cu, rv_score.cu)
+void launch_init_slots(Slot *slots, unsigned long long n, cudaStream_t s);
+void launch_region_spans(const DevState &st, cudaStream_t s);
+cudaError_t launch_pileup(const DevState &st, const DevParams &P, int grid, cudaStream_t s);
+void launch_serial(const DevState &st, const DevParams &P, cudaStream_t s);
+void launch_resolve(const DevState &st, const DevParams &P, cudaStream_t s);
+int pileup_blocks_per_sm();
+size_t pileup_smem_bytes();
+void launch_link(const DevState &st, cudaStream_t s);
+void launch_collisions(const DevState &st, cudaStream_t s);
+void launch_ins_adjust(const DevState &st, cudaStream_t s);
+void launch_score(const DevState &st, const DevParams &P, cudaStream_t s);
+void launch_fisher(const int32_t *tab, int64_t n, double *p2, double *ratio, cudaStream_t s);
+void launch_compact_slots(const DevState &st, uint32_t *out, unsigned int *n_out, cudaStream_t s);
+void launch_gather_slots(const Slot *slots, const uint32_t *idx, int64_t n, Slot *out, cudaStream_t s);
+
+// one cell (position) as seen by the host realigner
+struct CellView {
+    uint32_t fwd[4], rev[4], hi[4], tp[4], q[4], mq[4];
+    int32_t nm[4];
+    uint32_t first[4];
+    uint32_t cov;
+    uint32_t kflags;
+};
+void launch_gather_cells(const DevState &st, const int64_t *cells, int64_t n, CellView *out, cudaStream_t s);
+
+// patch written back by the host realigner
+struct Patch {
+    int32_t type;       // 0 overwrite slot stats, 1 erase slot, 2 erase single cell key, 3 add coverage
+    int32_t base;
+    int64_t target;     // slot index or cell index
+    int32_t fwd, rev, hi, lo, extracnt, flags_or;
+    long long tp_sum, mq_sum, nm_sum;
+    double q_sum;
+    int32_t cov_add, pad;
+};
+void launch_apply_patches(const DevState &st, const Patch *p, int64_t n, cudaStream_t s);
+
+template <class T>
+struct DevBuf {
+    T *p = nullptr;
+    size_t n = 0;
+};
+
+}  // namespace rv
+
+struct rv_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    rv_params params;
+    rv::DevParams dp;
+    std::string err;
+    size_t budget = 0;
+    int sm_count = 0;
+
+    // reference contig
+    std::string chr;
+    std::string ref_host;   // uppercase
+    char *d_ref = nullptr;
+    int32_t ref_len = 0;
+
+    // batch (device copies)
+    int64_t n_reads = 0, n_cigar_words = 0, n_bases = 0;
+    size_t cap_reads = 0, cap_cigar = 0, cap_bases = 0;
+    int32_t *d_pos = nullptr, *d_mpos = nullptr, *d_nm = nullptr, *d_lq = nullptr;
+    uint16_t *d_flag = nullptr, *d_ncig = nullptr;
+    uint8_t *d_mapq = nullptr;
+    uint32_t *d_cigoff = nullptr, *d_cigar = nullptr;
+    uint64_t *d_boff = nullptr;
+    uint8_t *d_seq = nullptr, *d_qual = nullptr;
+    std::vector<int32_t> h_pos;  // positions kept for region lookup
+
+    // regions / tiles
+    std::vector<rv::Region> regions;
+    std::vector<rv::Tile> tiles;
+    std::vector<int64_t> score_base;
+    rv::Region *d_regions = nullptr;
+    rv::Tile *d_tiles = nullptr;
+    int64_t *d_score_base = nullptr;
+    size_t cap_regions = 0, cap_tiles = 0;
+    int64_t n_score = 0;
+
+    // cells
+    int64_t n_cells = 0;
+    size_t cap_cells = 0;
+    void *d_cellmem = nullptr;
+    rv::Cells cells{};
+    uint32_t *d_head = nullptr;
+
+    // hash
+    unsigned long long hash_cap = 0;
+    rv::Slot *d_slots = nullptr;
+    uint8_t *d_arena = nullptr;
+    unsigned long long arena_cap = 0;
+
+    // deferred, candidates
+    rv::Deferred *d_deferred = nullptr;
+    unsigned int deferred_cap = 0;
+    rv::CandVar *d_cand = nullptr;
+    unsigned int cand_cap = 0;
+
+    // small counters: tile_counter, n_deferred, n_used, err, n_cand, pad, arena_used(64)
+    unsigned int *d_counters = nullptr;
+
+    // host mirrors
+    std::vector<rv::CandVar> h_cand;
+    std::vector<uint8_t> h_arena;
+    std::vector<rv_site_record> h_records;
+    std::string text;
+    std::string dump;
+    int64_t n_records = 0;
+
+    // stage
+    int stage = 0;  // 0 none, 1 submitted, 2 piled up, 3 realigned, 4 scored
+    cudaEvent_t ev[6] = {};
+    double pileup_ms = 0, score_ms = 0, total_ms = 0;
+    int64_t kernels = 0;
+
+    rv::DevState state() const;
+};

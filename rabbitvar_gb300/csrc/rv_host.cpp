@@ -1,0 +1,940 @@
+// Host side of librvgpu that works on strings and on the few keys the local
+// realigner touches:
+//   * host_realign_mnp: VariationRealigner::adjustMNP
+//     (src/VariationRealigner.cpp:334-465) over the device-built maps;
+//   * host_format_records: the allele-string part of
+//     ToVarsBuilder::collectReferenceVariants (src/ToVarsBuilder.cpp:730-1098,
+//     findMSI :614-678, proceedVrefIs* :242-317), Variant::varType /
+//     isGoodVar / adjComplex (include/Variant.h:99-248) and
+//     print_output_variant_simple (src/modes/simpleMode.cpp:66-142);
+//   * host_export_maps: the pileup-boundary maps as text.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <set>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "rv_ctx.h"
+
+namespace rv {
+
+namespace {
+
+#define HCUDA(call)                                                        \
+    do {                                                                   \
+        cudaError_t e_ = (call);                                           \
+        if (e_ != cudaSuccess) {                                           \
+            ctx->err = std::string(#call) + ": " + cudaGetErrorString(e_); \
+            return RV_ERR_CUDA;                                            \
+        }                                                                  \
+    } while (0)
+
+constexpr uint32_t FC_PDIFF = 1u << 30, FC_QDIFF = 1u << 31;
+const char kBases[4] = {'A', 'C', 'G', 'T'};
+
+// Statistics of one allele key as the host realigner sees it.
+struct HVar {
+    int cnt = 0, fwd = 0, rev = 0, hi = 0, lo = 0, extracnt = 0;
+    double tp = 0, q = 0, mq = 0, nm = 0;
+    bool pstd = false, qstd = false;
+    int64_t slot = -1;   // hash slot, or -1 for a cell key
+    int64_t cell = -1;
+    int base = -1;
+    bool dirty = false, erased = false, force_std = false;
+};
+
+struct HClip {
+    HVar agg;
+    std::map<int, std::map<char, std::pair<int, double>>> nt;  // idx -> ch -> (count, quality sum)
+    std::string cons;
+    bool used = false;
+};
+
+// Measured iteration order of the reference's hash map over soft-clip
+// bases (N, A, T, G, C), which decides ties in the consensus.
+int clip_rank(char c) {
+    switch (c) {
+    case 'N': return 0;
+    case 'A': return 1;
+    case 'T': return 2;
+    case 'G': return 3;
+    case 'C': return 4;
+    default: return 5 + (unsigned char)c;
+    }
+}
+
+bool is_mnv(const std::string &k) {
+    if (k.size() <= 2 || k[1] != '&') return false;
+    auto b = [](char c) { return c == 'A' || c == 'C' || c == 'G' || c == 'T'; };
+    if (!b(k[0])) return false;
+    for (size_t i = 2; i < k.size(); i++)
+        if (!b(k[i])) return false;
+    return true;
+}
+
+struct RefWin {
+    const std::string *ref;
+    int ws, we, len;
+    bool has(int p) const { return p >= ws && p <= we; }
+    char at(int p) const { return has(p) ? (*ref)[p - 1] : 0; }
+};
+
+// findconseq: include/VariationUtils.h:403-509
+std::string clip_consensus(HClip &sc) {
+    if (!sc.cons.empty()) return sc.cons;
+    int total = 0, match = 0;
+    std::string seqq;
+    bool flag = false;
+    for (auto &nve : sc.nt) {
+        std::vector<std::pair<char, std::pair<int, double>>> nv(nve.second.begin(), nve.second.end());
+        std::sort(nv.begin(), nv.end(), [](const auto &a, const auto &b) { return clip_rank(a.first) < clip_rank(b.first); });
+        int maxc = 0, tt = 0;
+        double maxq = 0;
+        char chosen = 0;
+        for (auto &e : nv) {
+            tt += e.second.first;
+            if (e.second.first > maxc || e.second.second > maxq) {
+                maxc = e.second.first;
+                chosen = e.first;
+                maxq = e.second.second;
+            }
+        }
+        if (nve.first == 3 && sc.nt.size() >= 6 && tt / (double)sc.agg.cnt < 0.2 && tt <= 2) break;
+        if ((tt - maxc > 2 || maxc <= tt - maxc) && maxc / (double)tt < 0.8) {
+            if (flag) break;
+            flag = true;
+        }
+        total += tt;
+        match += maxc;
+        if (chosen != 0) seqq += chosen;
+    }
+    int nts = (int)sc.nt.size(), sl = (int)seqq.size();
+    std::string out;
+    if (total != 0 && match / (double)total > 0.9 && sl / 1.5 > nts - sl &&
+        (sl / (double)nts > 0.8 || nts - sl < 10 || sl > 25))
+        out = seqq;
+    else
+        out = " ";
+    if (out.size() > 12) {
+        bool a7 = out.compare(1, 7, "AAAAAAA") == 0, t7 = out.compare(1, 7, "TTTTTTT") == 0;
+        if (a7 || t7) sc.used = true;
+        int len = (int)out.size(), kinds = 0;
+        bool low = false;
+        for (char b : std::string("ATGC")) {
+            int c = (int)std::count(out.begin(), out.end(), b);
+            if (c > 0) kinds++;
+            if (c / (double)len > 0.75) low = true;
+        }
+        if (low || kinds < 3) sc.used = true;
+    }
+    sc.cons = out;
+    return out;
+}
+
+void add_into(HVar &to, const HVar &v) {  // adjCnt: include/VariationUtils.h:338-352
+    to.cnt += v.cnt;
+    to.extracnt += v.cnt;
+    to.hi += v.hi;
+    to.lo += v.lo;
+    to.tp += v.tp;
+    to.q += v.q;
+    to.mq += v.mq;
+    to.nm += v.nm;
+    to.fwd += v.fwd;
+    to.rev += v.rev;
+    to.pstd = to.qstd = true;
+    to.force_std = true;
+    to.dirty = true;
+}
+
+bool matches_ref(const std::string &s, const RefWin &R, int position, int dir) {  // ismatchref, MM = 3
+    int mm = 0, n = (int)s.size();
+    for (int k = 0; k < n; k++) {
+        int p = position + dir * k;
+        if (!R.has(p)) return false;
+        char c = dir == 1 ? s[k] : s[n - k - 1];
+        if (c != R.at(p)) mm++;
+    }
+    return mm <= 3 && mm / (double)n < 0.15;
+}
+
+std::string slot_key(const rv_ctx *ctx, const Slot &s) {
+    if (s.klen == 0 || (size_t)s.koff + s.klen > ctx->h_arena.size()) return std::string();
+    return std::string((const char *)ctx->h_arena.data() + s.koff, s.klen);
+}
+
+rv_status fetch_slots(rv_ctx *ctx, std::vector<Slot> &slots, std::vector<uint32_t> &idx) {
+    DevState st = ctx->state();
+    unsigned int *d_n = nullptr;
+    uint32_t *d_idx = nullptr;
+    Slot *d_out = nullptr;
+    HCUDA(cudaMalloc((void **)&d_n, 4));
+    HCUDA(cudaMemset(d_n, 0, 4));
+    HCUDA(cudaMalloc((void **)&d_idx, ctx->hash_cap * 4));
+    launch_compact_slots(st, d_idx, d_n, ctx->stream);
+    unsigned int n = 0;
+    HCUDA(cudaMemcpyAsync(&n, d_n, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    HCUDA(cudaStreamSynchronize(ctx->stream));
+    idx.resize(n);
+    slots.resize(n);
+    if (n) {
+        HCUDA(cudaMalloc((void **)&d_out, (size_t)n * sizeof(Slot)));
+        launch_gather_slots(ctx->d_slots, d_idx, n, d_out, ctx->stream);
+        HCUDA(cudaMemcpyAsync(slots.data(), d_out, (size_t)n * sizeof(Slot), cudaMemcpyDeviceToHost, ctx->stream));
+        HCUDA(cudaMemcpyAsync(idx.data(), d_idx, (size_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    unsigned long long used = 0;
+    HCUDA(cudaMemcpyAsync(&used, ctx->d_counters + 8, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    HCUDA(cudaStreamSynchronize(ctx->stream));
+    used = std::min<unsigned long long>(used, ctx->arena_cap);
+    ctx->h_arena.resize(used);
+    if (used) HCUDA(cudaMemcpy(ctx->h_arena.data(), ctx->d_arena, used, cudaMemcpyDeviceToHost));
+    cudaFree(d_n);
+    cudaFree(d_idx);
+    if (d_out) cudaFree(d_out);
+    return RV_OK;
+}
+
+rv_status fetch_cells(rv_ctx *ctx, const std::vector<int64_t> &cells, std::vector<CellView> &out) {
+    out.resize(cells.size());
+    if (cells.empty()) return RV_OK;
+    int64_t *d_c = nullptr;
+    CellView *d_v = nullptr;
+    HCUDA(cudaMalloc((void **)&d_c, cells.size() * 8));
+    HCUDA(cudaMalloc((void **)&d_v, cells.size() * sizeof(CellView)));
+    HCUDA(cudaMemcpyAsync(d_c, cells.data(), cells.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
+    launch_gather_cells(ctx->state(), d_c, (int64_t)cells.size(), d_v, ctx->stream);
+    HCUDA(cudaMemcpyAsync(out.data(), d_v, cells.size() * sizeof(CellView), cudaMemcpyDeviceToHost, ctx->stream));
+    HCUDA(cudaStreamSynchronize(ctx->stream));
+    cudaFree(d_c);
+    cudaFree(d_v);
+    return RV_OK;
+}
+
+HVar from_cell(const CellView &v, int b, int64_t cell) {
+    HVar h;
+    h.fwd = (int)v.fwd[b];
+    h.rev = (int)v.rev[b];
+    h.cnt = h.fwd + h.rev;
+    h.hi = (int)v.hi[b];
+    h.lo = h.cnt - h.hi;
+    h.tp = (double)(int)v.tp[b];
+    h.q = (double)(int)v.q[b];
+    h.mq = (double)(int)v.mq[b];
+    h.nm = (double)v.nm[b];
+    h.pstd = (v.first[b] & FC_PDIFF) != 0;
+    h.qstd = (v.first[b] & FC_QDIFF) != 0;
+    h.cell = cell;
+    h.base = b;
+    return h;
+}
+
+HVar from_slot(const Slot &s, int64_t slot) {
+    HVar h;
+    h.fwd = s.fwd;
+    h.rev = s.rev;
+    h.cnt = s.fwd + s.rev;
+    h.hi = s.hi;
+    h.lo = s.lo;
+    h.extracnt = s.extracnt;
+    h.tp = (double)s.tp_sum;
+    h.q = s.q_sum;
+    h.mq = (double)s.mq_sum;
+    h.nm = (double)s.nm_sum;
+    h.pstd = (s.flags & (SF_PDIFF | SF_FORCE_STD)) != 0;
+    h.qstd = (s.flags & (SF_QDIFF | SF_FORCE_STD)) != 0;
+    h.erased = (s.flags & SF_ERASED) != 0;
+    h.slot = slot;
+    return h;
+}
+
+}  // namespace
+
+rv_status host_realign_mnp(rv_ctx *ctx) {
+    std::vector<Slot> slots;
+    std::vector<uint32_t> sidx;
+    rv_status st = fetch_slots(ctx, slots, sidx);
+    if (st) return st;
+    struct Mnp { int region, pos; std::string key; int cnt; };
+    std::vector<Mnp> mnps;
+    for (size_t i = 0; i < slots.size(); i++) {
+        const Slot &s = slots[i];
+        if (s.kind != KIND_NONINS || (s.flags & SF_ERASED) || s.obs <= 0) continue;
+        std::string k = slot_key(ctx, s);
+        if (is_mnv(k)) mnps.push_back({s.region, s.pos, k, s.obs});
+    }
+    if (mnps.empty()) return RV_OK;
+    // positions whose keys the MNP merge may read or change
+    std::set<std::pair<int, int>> need;
+    std::set<std::tuple<int, int, int>> need_clip;  // region, pos, side (5 or 3)
+    for (const Mnp &m : mnps) {
+        int len = (int)m.key.size() - 1;
+        for (int k = 0; k < len; k++) need.insert({m.region, m.pos + k});
+        need_clip.insert({m.region, m.pos, 3});
+        need_clip.insert({m.region, m.pos + len, 5});
+    }
+    std::vector<int64_t> cells;
+    std::vector<std::pair<int, int>> cell_pos;
+    for (auto &np : need) {
+        const Region &R = ctx->regions[np.first];
+        if (np.second < R.clo || np.second > R.chi) continue;
+        cells.push_back(R.cell_base + (np.second - R.clo));
+        cell_pos.push_back(np);
+    }
+    std::vector<CellView> cv;
+    if ((st = fetch_cells(ctx, cells, cv))) return st;
+    // mirror of the touched part of the maps
+    std::map<std::pair<int, int>, std::map<std::string, HVar>> vars;
+    std::map<std::pair<int, int>, int64_t> cell_of_pos;
+    for (size_t i = 0; i < cells.size(); i++) {
+        auto &m = vars[cell_pos[i]];
+        cell_of_pos[cell_pos[i]] = cells[i];
+        for (int b = 0; b < 4; b++) {
+            bool exist = (cv[i].kflags >> b) & 1, erased = (cv[i].kflags >> (4 + b)) & 1;
+            if (exist && !erased) m[std::string(1, kBases[b])] = from_cell(cv[i], b, cells[i]);
+        }
+    }
+    std::map<std::tuple<int, int, int>, HClip> clips;
+    for (size_t i = 0; i < slots.size(); i++) {
+        const Slot &s = slots[i];
+        if (s.kind == KIND_NONINS && need.count({s.region, s.pos}) && !(s.flags & SF_ERASED)) {
+            vars[{s.region, s.pos}][slot_key(ctx, s)] = from_slot(s, sidx[i]);
+        } else if (s.kind == KIND_SC3 || s.kind == KIND_SC5) {
+            auto key = std::make_tuple((int)s.region, (int)s.pos, s.kind == KIND_SC3 ? 3 : 5);
+            if (need_clip.count(key)) clips[key].agg = from_slot(s, sidx[i]);
+        } else if (s.kind == KIND_SC3_SEQ || s.kind == KIND_SC5_SEQ) {
+            auto key = std::make_tuple((int)s.region, (int)s.pos, s.kind == KIND_SC3_SEQ ? 3 : 5);
+            if (!need_clip.count(key)) continue;
+            std::string k = slot_key(ctx, s);
+            if (k.size() != 3) continue;
+            int idx = (uint8_t)k[0] | ((uint8_t)k[1] << 8);
+            clips[key].nt[idx][k[2]] = {s.obs, s.q_sum};
+        }
+    }
+    // fillAndSortTmp / CMP_tmp (src/VariationRealigner.cpp:44-58, 1362-1386), per region
+    std::sort(mnps.begin(), mnps.end(), [](const Mnp &a, const Mnp &b) {
+        if (a.region != b.region) return a.region < b.region;
+        if (a.cnt != b.cnt) return a.cnt > b.cnt;
+        if (a.pos != b.pos) return a.pos < b.pos;
+        return a.key.compare(b.key) > 0;
+    });
+    std::vector<Patch> patches;
+    auto add_cov = [&](int region, int pos, int n) {
+        auto it = cell_of_pos.find({region, pos});
+        if (it == cell_of_pos.end()) return;
+        Patch p;
+        memset(&p, 0, sizeof p);
+        p.type = 3;
+        p.target = it->second;
+        p.cov_add = n;
+        patches.push_back(p);
+    };
+    for (const Mnp &m : mnps) {
+        const Region &Rg = ctx->regions[m.region];
+        RefWin R{&ctx->ref_host, Rg.ws, Rg.we, ctx->ref_len};
+        auto pit = vars.find({m.region, m.pos});
+        if (pit == vars.end() || !pit->second.count(m.key)) continue;
+        std::set<std::string> local;
+        for (auto &e : pit->second) local.insert(e.first);
+        HVar &vref = pit->second.at(m.key);
+        std::string mnt = m.key;
+        mnt.erase(mnt.find('&'), 1);
+        int ml = (int)mnt.size();
+        for (int i = 0; i < ml - 1; i++) {
+            std::string left = mnt.substr(0, i + 1), right = mnt.substr(i + 1);
+            if (left.size() > 1) left.insert(1, "&");
+            if (right.size() > 1) right.insert(1, "&");
+            if (local.count(left)) {
+                HVar &tref = pit->second.at(left);
+                if (tref.cnt <= 0) continue;
+                if (tref.cnt < vref.cnt && tref.tp / tref.cnt <= i + 1) {
+                    add_into(vref, tref);
+                    local.erase(left);
+                }
+            }
+            auto rit = vars.find({m.region, m.pos + i + 1});
+            if (rit != vars.end()) {
+                auto kit = rit->second.find(right);
+                if (kit != rit->second.end()) {
+                    HVar &tref = kit->second;
+                    if (tref.cnt < 0) continue;
+                    if (tref.cnt < vref.cnt) {
+                        add_into(vref, tref);
+                        add_cov(m.region, m.pos, tref.cnt);
+                        Patch p;
+                        memset(&p, 0, sizeof p);
+                        if (tref.slot >= 0) { p.type = 1; p.target = tref.slot; }
+                        else { p.type = 2; p.target = tref.cell; p.base = tref.base; }
+                        patches.push_back(p);
+                        rit->second.erase(kit);
+                    }
+                }
+            }
+        }
+        auto s3 = clips.find(std::make_tuple(m.region, m.pos, 3));
+        if (s3 != clips.end() && !s3->second.used) {
+            std::string sq = clip_consensus(s3->second);
+            if ((int)sq.size() >= ml && sq.compare(0, ml, mnt) == 0 &&
+                ((int)sq.size() == ml || matches_ref(sq.substr(ml), R, m.pos + ml, 1))) {
+                add_into(vref, s3->second.agg);
+                add_cov(m.region, m.pos, s3->second.agg.cnt);
+                s3->second.used = true;
+            }
+        }
+        auto s5 = clips.find(std::make_tuple(m.region, m.pos + ml, 5));
+        if (s5 != clips.end() && !s5->second.used) {
+            std::string sq = clip_consensus(s5->second);
+            if (sq != " " && (int)sq.size() >= ml) {
+                std::reverse(sq.begin(), sq.end());
+                if (sq.compare(sq.size() - ml, ml, mnt) == 0 &&
+                    ((int)sq.size() == ml || matches_ref(sq.substr(0, sq.size() - ml), R, m.pos - 1, -1))) {
+                    add_into(vref, s5->second.agg);
+                    add_cov(m.region, m.pos, s5->second.agg.cnt);
+                    s5->second.used = true;
+                }
+            }
+        }
+    }
+    for (auto &pe : vars)
+        for (auto &ke : pe.second) {
+            const HVar &h = ke.second;
+            if (!h.dirty || h.slot < 0) continue;
+            Patch p;
+            memset(&p, 0, sizeof p);
+            p.type = 0;
+            p.target = h.slot;
+            p.fwd = h.fwd;
+            p.rev = h.rev;
+            p.hi = h.hi;
+            p.lo = h.lo;
+            p.extracnt = h.extracnt;
+            p.tp_sum = (long long)llround(h.tp);
+            p.mq_sum = (long long)llround(h.mq);
+            p.nm_sum = (long long)llround(h.nm);
+            p.q_sum = h.q;
+            p.flags_or = h.force_std ? (int)SF_FORCE_STD : 0;
+            patches.push_back(p);
+        }
+    if (patches.empty()) return RV_OK;
+    Patch *d_p = nullptr;
+    HCUDA(cudaMalloc((void **)&d_p, patches.size() * sizeof(Patch)));
+    HCUDA(cudaMemcpyAsync(d_p, patches.data(), patches.size() * sizeof(Patch), cudaMemcpyHostToDevice, ctx->stream));
+    launch_apply_patches(ctx->state(), d_p, (int64_t)patches.size(), ctx->stream);
+    HCUDA(cudaStreamSynchronize(ctx->stream));
+    cudaFree(d_p);
+    return RV_OK;
+}
+
+// ---------------------------------------------------------------------------
+// records
+// ---------------------------------------------------------------------------
+namespace {
+
+struct Msi { double msi; int shift3; std::string unit; };
+
+// findMSI with curmsi_from_end (src/ToVarsBuilder.cpp:614-678)
+Msi find_msi(const std::string &t1, const std::string &t2, const std::string &left) {
+    int nmsi = 1, shift3 = 0;
+    std::string best;
+    double best_cnt = 0;
+    std::string both = left + t1;
+    while (nmsi <= (int)t1.size() && nmsi <= 6) {
+        std::string unit = t1.substr(t1.size() - nmsi, nmsi);
+        double cur = 1.0;
+        for (int i = (int)both.size() - nmsi; i > 0; i -= nmsi) {
+            if (i > nmsi && both.compare(i - nmsi, nmsi, unit) == 0) cur += 1;
+            else break;
+        }
+        for (int i = 0; i < (int)t2.size(); i += nmsi) {
+            if (i + nmsi < (int)t2.size() && t2.compare(i, nmsi, unit) == 0) cur += 1.0;
+            else break;
+        }
+        if (cur > best_cnt) { best = unit; best_cnt = cur; }
+        nmsi++;
+    }
+    std::string ts = t1 + t2;
+    while (shift3 < (int)t2.size() && ts[shift3] == t2[shift3]) shift3++;
+    return {best_cnt, shift3, best};
+}
+
+struct NoRef {};
+
+struct RecVar {
+    const CandVar *c;
+    std::string desc;
+    std::string sbf;
+    int startp = 0, endp = 0, shift3 = 0, msint = 0;
+    double msi = 0;
+    std::string leftseq, rightseq, genotype, refallele, varallele, vartype;
+    bool filled = false;
+};
+
+std::string join(const RefWin &R, int from, int to) {
+    std::string s;
+    for (int i = from; i <= to; i++) {
+        if (!R.has(i)) throw NoRef();
+        s += R.at(i);
+    }
+    return s;
+}
+
+void repl_first(std::string &s, const std::string &a, const std::string &b) {
+    size_t p = s.find(a);
+    if (p != std::string::npos) s.replace(p, a.size(), b);
+}
+
+bool starts(const std::string &s, char c) { return !s.empty() && s[0] == c; }
+
+// last '&' followed by an A/C/G/T run (the ".*&([ATGC]+).*" search)
+bool amp_tail(const std::string &s, std::string &run) {
+    for (size_t k = s.size(); k-- > 0;) {
+        if (s[k] == '&' && k + 1 < s.size() && strchr("ATGC", s[k + 1]) && s[k + 1]) {
+            size_t e = k + 1;
+            while (e < s.size() && s[e] && strchr("ATGC", s[e])) e++;
+            run = s.substr(k + 1, e - k - 1);
+            return true;
+        }
+    }
+    return false;
+}
+
+void describe(RecVar &v, std::string &g1, int position, const RefWin &R, const rv_params &P) {
+    std::string g2 = v.desc;
+    if (starts(g2, '+')) g2 = "+" + std::to_string(g2.size() - 1);
+    const std::string &vn = v.desc;
+    int dellen = 0;
+    if (vn.size() > 1 && vn[0] == '-' && isdigit((unsigned char)vn[1])) dellen = atoi(vn.c_str() + 1);
+    int endp = position, startp = position, shift3 = 0;
+    if (starts(vn, '-')) endp = position + dellen - 1;
+    std::string refa, vara, unit;
+    double msi = 0;
+    int L = R.len;
+    if (starts(vn, '+')) {
+        if (vn.find('&') == std::string::npos && vn.find('#') == std::string::npos && vn.find("<dup") == std::string::npos) {
+            std::string t1 = vn.substr(1);
+            std::string left = join(R, position - 50 > 1 ? position - 50 : 1, position);
+            std::string t2 = join(R, position + 1, position + 70 > L ? L : position + 70);
+            Msi a = find_msi(t1, t2, left), b = find_msi(left, t2, "");
+            if (a.msi < b.msi) { a.msi = b.msi; a.unit = b.unit; }
+            if (a.msi <= a.shift3 / (double)t1.size()) a.msi = a.shift3 / (double)t1.size();
+            msi = a.msi; shift3 = a.shift3; unit = a.unit;
+        }
+        if (P.move_indels_3) { startp += shift3; endp += shift3; }
+        refa = R.has(position) ? std::string(1, R.at(position)) : "";
+        vara = refa + vn.substr(1);
+    } else if (starts(vn, '-')) {
+        if (dellen < P.svminlen) {
+            vara = vn;
+            size_t k = 1;
+            while (k < vara.size() && isdigit((unsigned char)vara[k])) k++;
+            if (k > 1) vara.erase(0, k);
+            std::string left = join(R, position - 70 > 1 ? position - 70 : 1, position - 1);
+            std::string ts = join(R, position, position + dellen + 70 > L ? L : position + dellen + 70);
+            std::string a1 = ts.substr(0, std::min<size_t>(dellen, ts.size()));
+            std::string a2 = (size_t)dellen <= ts.size() ? ts.substr(dellen) : std::string();
+            Msi a = find_msi(a1, a2, left), b = find_msi(left, a2, "");
+            if (a.msi < b.msi) { a.msi = b.msi; a.unit = b.unit; }
+            if (a.msi <= a.shift3 / (double)dellen) a.msi = a.shift3 / (double)dellen;
+            msi = a.msi; shift3 = a.shift3; unit = a.unit;
+        }
+        if (vn.find('&') == std::string::npos && vn.find('#') == std::string::npos && vn.find('^') == std::string::npos) {
+            if (P.move_indels_3) startp += shift3;
+            if (vara != "<DEL>") vara = R.has(position - 1) ? std::string(1, R.at(position - 1)) : "";
+            refa = R.has(position - 1) ? std::string(1, R.at(position - 1)) : "";
+            startp--;
+        }
+        if (dellen < P.svminlen) refa += join(R, position, position + dellen - 1);
+    } else {
+        std::string t1 = join(R, position - 30 > 1 ? position - 30 : 1, position + 1);
+        std::string t2 = join(R, position + 2, position + 70 > L ? L : position + 70);
+        Msi a = find_msi(t1, t2, "");
+        msi = a.msi; shift3 = a.shift3; unit = a.unit;
+        refa = R.has(position) ? std::string(1, R.at(position)) : "";
+        vara = vn;
+    }
+    std::string extra;
+    if (amp_tail(vn, extra)) {
+        repl_first(vara, "&", "");
+        std::string tch = join(R, endp + 1, endp + (int)extra.size());
+        refa += tch;
+        g1 += tch;
+        endp += (int)extra.size();
+        std::string vextra;
+        if (amp_tail(vara, vextra)) {
+            repl_first(vara, "&", "");
+            tch = join(R, endp + 1, endp + (int)vextra.size());
+            refa += tch;
+            g1 += tch;
+            endp += (int)vextra.size();
+        }
+        if (starts(vn, '+')) {
+            refa = refa.substr(1);
+            vara = vara.substr(1);
+            startp++;
+        }
+    }
+    size_t hp = vn.find('#'), cp = vn.rfind('^');
+    if (hp != std::string::npos && cp != std::string::npos && cp > hp + 1 && cp + 1 < vn.size()) {
+        std::string mseq = vn.substr(hp + 1, cp - hp - 1), tail = vn.substr(cp + 1);
+        endp += (int)mseq.size();
+        refa += join(R, endp - (int)mseq.size() + 1, endp);
+        if (!tail.empty() && isdigit((unsigned char)tail[0])) {
+            int d = atoi(tail.c_str());
+            refa += join(R, endp + 1, endp + d);
+            endp += d;
+        }
+        repl_first(vara, "#", "");
+        size_t c2 = vara.find('^');
+        if (c2 != std::string::npos) {
+            size_t e = c2 + 1;
+            while (e < vara.size() && isdigit((unsigned char)vara[e])) e++;
+            vara.erase(c2, e - c2);
+        }
+        repl_first(g1, "#", "m");
+        repl_first(g1, "^", "i");
+        repl_first(g2, "#", "m");
+        repl_first(g2, "^", "i");
+    }
+    for (size_t k = 0; k + 1 < vn.size(); k++) {
+        if (vn[k] == '^' && vn[k + 1] && strchr("ATGNC", vn[k + 1])) {
+            repl_first(vara, "^", "");
+            repl_first(g1, "^", "i");
+            repl_first(g2, "^", "i");
+            break;
+        }
+    }
+    v.leftseq = join(R, startp - 20 < 1 ? 1 : startp - 20, startp - 1);
+    v.rightseq = join(R, endp + 1, endp + 20 > L ? L : endp + 20);
+    std::string gt;
+    for (char c : g1 + "/" + g2) {
+        if (c == '&' || c == '#') continue;
+        gt += c == '^' ? 'i' : c;
+    }
+    v.msi = msi;
+    v.msint = (int)unit.size();
+    v.shift3 = shift3;
+    v.startp = startp;
+    v.endp = endp;
+    v.refallele = refa;
+    v.varallele = vara;
+    v.genotype = gt;
+    v.filled = true;
+}
+
+std::string var_type(const RecVar &v) {
+    const std::string &r = v.refallele, &a = v.varallele;
+    if (r.size() == 1 && a.size() == 1) return "SNV";
+    if (a.size() == 5 && a[0] == '<' && a[4] == '>') return a.substr(1, 3);
+    if (r.empty() || a.empty()) return "Complex";
+    if (r[0] != a[0]) return "Complex";
+    if (r.size() == 1 && a.size() > 1 && a[0] == r[0]) return "Insertion";
+    if (r.size() > 1 && a.size() == 1 && r[0] == a[0]) return "Deletion";
+    return "Complex";
+}
+
+bool good_var(const RecVar &v, const CandVar *ref, const rv_params &P) {
+    const CandVar &c = *v.c;
+    if (v.refallele.empty()) return false;
+    if (c.freq < P.freq || c.hicnt < P.minr || c.pmean < P.read_pos_filter || c.qual < P.goodq) return false;
+    if (ref && ref->hicnt > P.minr && c.freq < 0.25) {
+        double d = c.mq + v.refallele.size() + v.varallele.size();
+        double f = (1 + d) / (ref->mq + 1);
+        if ((d - 2 < 5 && ref->mq > 20) || f < 0.25) return false;
+    }
+    if (c.qratio < P.qratio) return false;
+    if (c.freq > 0.30) return true;
+    if (c.mq < P.mapq_filter) return false;
+    if (v.sbf == "2;1" && c.freq < 0.20) {
+        if (v.vartype.empty() || v.vartype == "SNV" || (v.refallele.size() < 3 && v.varallele.size() < 3)) return false;
+    }
+    return true;
+}
+
+void adj_complex(RecVar &v) {
+    std::string r = v.refallele, a = v.varallele;
+    if (!a.empty() && a[0] == '<') return;
+    size_t n = 0;
+    while (r.size() - n > 1 && a.size() - n > 1 && r[n] == a[n]) n++;
+    if (n > 0) {
+        v.startp += (int)n;
+        v.refallele = r.substr(n);
+        v.varallele = a.substr(n);
+        v.leftseq += r.substr(0, n);
+        v.leftseq = v.leftseq.substr(n);
+    }
+    r = v.refallele;
+    a = v.varallele;
+    size_t m = 1;
+    while (r.size() > m && a.size() > m && r[r.size() - m] == a[a.size() - m]) m++;
+    if (m > 1) {
+        v.endp -= (int)(m - 1);
+        v.refallele = r.substr(0, r.size() - (m - 1));
+        v.varallele = a.substr(0, a.size() - (m - 1));
+        long keep = (long)v.rightseq.size() - (long)(m - 1);
+        v.rightseq = r.substr(r.size() - (m - 1)) + (keep > 0 ? v.rightseq.substr(0, keep) : std::string());
+    }
+}
+
+std::string f6(double d) {
+    char b[64];
+    snprintf(b, sizeof b, "%f", d);
+    return b;
+}
+
+}  // namespace
+
+rv_status host_format_records(rv_ctx *ctx, const char *sample, const char *gene) {
+    const rv_params &P = ctx->params;
+    std::vector<const CandVar *> order(ctx->h_cand.size());
+    for (size_t i = 0; i < order.size(); i++) order[i] = &ctx->h_cand[i];
+    std::sort(order.begin(), order.end(), [](const CandVar *a, const CandVar *b) {
+        if (a->region != b->region) return a->region < b->region;
+        if (a->pos != b->pos) return a->pos < b->pos;
+        return a->rank < b->rank;
+    });
+    ctx->text.clear();
+    ctx->h_records.clear();
+    ctx->n_records = 0;
+    const std::string &chr = ctx->chr;
+    size_t i = 0;
+    while (i < order.size()) {
+        size_t j = i;
+        while (j < order.size() && order[j]->region == order[i]->region && order[j]->pos == order[i]->pos) j++;
+        const Region &Rg = ctx->regions[order[i]->region];
+        RefWin R{&ctx->ref_host, Rg.ws, Rg.we, ctx->ref_len};
+        int position = order[i]->pos;
+        const CandVar *ref = nullptr;
+        std::vector<RecVar> vs;
+        for (size_t k = i; k < j; k++) {
+            const CandVar *c = order[k];
+            if (c->kind == 0) { ref = c; continue; }
+            RecVar v;
+            v.c = c;
+            if (c->key_len < 0) v.desc = std::string(1, kBases[c->key_off & 3]);
+            else v.desc.assign((const char *)ctx->h_arena.data() + c->key_off, c->key_len);
+            vs.push_back(v);
+        }
+        std::string refdesc = ref ? std::string(1, R.at(position)) : "";
+        std::string g1;
+        if (ref && ref->freq >= P.freq) g1 = refdesc;
+        else if (!vs.empty()) g1 = vs[0].desc;
+        else g1 = refdesc;
+        if (starts(g1, '+')) g1 = "+" + std::to_string(g1.size() - 1);
+        try {
+            for (RecVar &v : vs) {
+                describe(v, g1, position, R, P);
+                v.sbf = std::string(ref ? std::to_string(ref->bias) : std::string("0")) + ";" + std::to_string(v.c->bias);
+            }
+        } catch (const NoRef &) {
+            // the reference's joinRef throws here; the position keeps the
+            // variants described so far (src/ToVarsBuilder.cpp:183-186)
+        }
+        std::string reg = chr + ":" + std::to_string(Rg.start) + "-" + std::to_string(Rg.end);
+        for (RecVar &v : vs) {
+            if (!v.filled) continue;
+            if (v.refallele.find('N') != std::string::npos) continue;
+            v.vartype = var_type(v);
+            if (!good_var(v, ref, P)) continue;
+            if (v.vartype == "Complex") adj_complex(v);
+            const CandVar &c = *v.c;
+            std::vector<std::string> f;
+            f.push_back(sample);
+            f.push_back(gene);
+            f.push_back(chr);
+            f.push_back(std::to_string(v.startp));
+            f.push_back(std::to_string(v.endp));
+            f.push_back(v.refallele);
+            f.push_back(v.varallele);
+            f.push_back(std::to_string(c.tpc));
+            f.push_back(std::to_string(c.pc));
+            f.push_back(std::to_string(c.rfc));
+            f.push_back(std::to_string(c.rrc));
+            f.push_back(std::to_string(c.fwd));
+            f.push_back(std::to_string(c.rev));
+            f.push_back(v.genotype.empty() ? "0" : v.genotype);
+            f.push_back(f6(c.freq));
+            f.push_back(v.sbf);
+            f.push_back(f6(c.pmean));
+            f.push_back(c.pstd ? "1" : "0");
+            f.push_back(f6(c.qual));
+            f.push_back(c.qstd ? "1" : "0");
+            if (P.fisher) {
+                f.push_back(f6(c.fisher_p));
+                f.push_back(f6(c.fisher_ratio));
+            }
+            f.push_back(f6(c.mq));
+            f.push_back(f6(c.qratio));
+            f.push_back(f6(c.hifreq));
+            f.push_back(f6(c.extrafreq));
+            f.push_back(std::to_string(v.shift3));
+            f.push_back(f6(v.msi));
+            f.push_back(std::to_string(v.msint));
+            f.push_back(c.nm > 0 ? f6(c.nm) : "0");
+            f.push_back(std::to_string(c.hicnt));
+            f.push_back(std::to_string(c.hicov));
+            f.push_back(v.leftseq.empty() ? "0" : v.leftseq);
+            f.push_back(v.rightseq.empty() ? "0" : v.rightseq);
+            f.push_back(reg);
+            f.push_back(v.vartype);
+            f.push_back(f6(0.0));
+            f.push_back("0");
+            for (size_t k = 0; k < f.size(); k++) {
+                ctx->text += f[k];
+                ctx->text += k + 1 < f.size() ? '\t' : '\n';
+            }
+            rv_site_record r;
+            memset(&r, 0, sizeof r);
+            r.region = c.region;
+            r.position = position;
+            r.start = v.startp;
+            r.end = v.endp;
+            r.total_cov = c.tpc;
+            r.var_cov = c.pc;
+            r.ref_fwd = c.rfc;
+            r.ref_rev = c.rrc;
+            r.alt_fwd = c.fwd;
+            r.alt_rev = c.rev;
+            r.freq = c.freq;
+            r.pmean = c.pmean;
+            r.qual = c.qual;
+            r.mapq = c.mq;
+            r.qratio = c.qratio;
+            r.hifreq = c.hifreq;
+            r.extrafreq = c.extrafreq;
+            r.msi = v.msi;
+            r.nm = c.nm;
+            r.pstd = c.pstd;
+            r.qstd = c.qstd;
+            r.shift3 = v.shift3;
+            r.msint = v.msint;
+            r.hicnt = c.hicnt;
+            r.hicov = c.hicov;
+            r.fisher_p = c.fisher_p;
+            r.fisher_ratio = c.fisher_ratio;
+            ctx->h_records.push_back(r);
+            ctx->n_records++;
+        }
+        i = j;
+    }
+    return RV_OK;
+}
+
+// ---------------------------------------------------------------------------
+// map export (pileup boundary) in the oracle's line format
+// ---------------------------------------------------------------------------
+rv_status host_export_maps(rv_ctx *ctx, int region, const char *stages) {
+    const Region &Rg = ctx->regions[region];
+    std::vector<Slot> slots;
+    std::vector<uint32_t> sidx;
+    rv_status st = fetch_slots(ctx, slots, sidx);
+    if (st) return st;
+    std::vector<int64_t> cells;
+    for (int p = Rg.clo; p <= Rg.chi; p++) cells.push_back(Rg.cell_base + (p - Rg.clo));
+    std::vector<CellView> cv;
+    if ((st = fetch_cells(ctx, cells, cv))) return st;
+    // max read length of the region
+    Region Rd;
+    HCUDA(cudaMemcpy(&Rd, ctx->d_regions + region, sizeof(Region), cudaMemcpyDeviceToHost));
+    bool realigned = strchr(stages, 'R') != nullptr;
+    const char *pfx = realigned ? "R" : "P";
+    char buf[640];
+    std::string &o = ctx->dump;
+    o.clear();
+    if (!realigned) {
+        snprintf(buf, sizeof buf, "P_ML\t%d\n", Rd.max_read_len);
+        o += buf;
+    }
+    auto line = [&](const char *tag, int pos, const std::string &key, const HVar &v) {
+        snprintf(buf, sizeof buf, "%s\t%d\t%s\t%d\t%d\t%d\t%.17g\t%.17g\t%.17g\t%.17g\t%d\t%d\t%d\t%d\t%d\t%.17g\t%d\n", tag,
+                 pos, key.c_str(), v.cnt, v.fwd, v.rev, v.tp, v.q, v.mq, v.nm, v.lo, v.hi, (int)v.pstd, (int)v.qstd, 0,
+                 0.0, v.extracnt);
+        o += buf;
+    };
+    std::map<int, std::map<std::string, HVar>> nonins, ins;
+    std::map<int, std::pair<HVar, std::map<int, std::map<char, HVar>>>> sc[2];
+    std::map<int, std::map<std::string, int>> cnt_i, cnt_d, cnt_m;
+    std::map<int, int> cov;
+    for (size_t i = 0; i < cells.size(); i++) {
+        int p = Rg.clo + (int)i;
+        for (int b = 0; b < 4; b++) {
+            bool exist = (cv[i].kflags >> b) & 1, erased = (cv[i].kflags >> (4 + b)) & 1;
+            if (exist && !(realigned && erased)) nonins[p][std::string(1, kBases[b])] = from_cell(cv[i], b, cells[i]);
+        }
+        if (cv[i].cov) cov[p] = (int)cv[i].cov;
+    }
+    for (size_t i = 0; i < slots.size(); i++) {
+        const Slot &s = slots[i];
+        if (s.region != region) continue;
+        std::string k = slot_key(ctx, s);
+        HVar h = from_slot(s, sidx[i]);
+        if (realigned && h.erased) continue;
+        switch (s.kind) {
+        case KIND_NONINS:
+            nonins[s.pos][k] = h;
+            if (is_mnv(k)) cnt_m[s.pos][k] = s.obs;
+            if (starts(k, '-')) cnt_d[s.pos][k] = s.obs;
+            break;
+        case KIND_INS:
+            ins[s.pos][k] = h;
+            cnt_i[s.pos][k] = s.obs;
+            break;
+        case KIND_SC5: case KIND_SC3:
+            sc[s.kind == KIND_SC3][s.pos].first = h;
+            break;
+        case KIND_SC5_SEQ: case KIND_SC3_SEQ: {
+            if (k.size() != 3) break;
+            int idx = (uint8_t)k[0] | ((uint8_t)k[1] << 8);
+            HVar hv = h;
+            hv.extracnt = s.obs;  // nt count rides along
+            sc[s.kind == KIND_SC3_SEQ][s.pos].second[idx][k[2]] = hv;
+            break;
+        }
+        default: break;
+        }
+    }
+    std::string tN = std::string(pfx) + "N", tI = std::string(pfx) + "I";
+    for (auto &pe : nonins)
+        for (auto &ke : pe.second) line(tN.c_str(), pe.first, ke.first, ke.second);
+    for (auto &pe : ins)
+        for (auto &ke : pe.second) line(tI.c_str(), pe.first, ke.first, ke.second);
+    for (auto &ce : cov) {
+        snprintf(buf, sizeof buf, "%sC\t%d\t%d\n", pfx, ce.first, ce.second);
+        o += buf;
+    }
+    if (!realigned) {
+        for (int side = 0; side < 2; side++) {
+            const char *tag = side == 0 ? "PS5" : "PS3";
+            for (auto &se : sc[side]) {
+                line(tag, se.first, "*", se.second.first);
+                for (auto &ie : se.second.second)
+                    for (auto &che : ie.second) {
+                        HVar v = che.second;
+                        int ntc = v.extracnt;
+                        v.extracnt = 0;
+                        char key[64];
+                        snprintf(key, sizeof key, "%d:%c:%d", ie.first, che.first, ntc);
+                        line(tag, se.first, key, v);
+                    }
+            }
+        }
+        auto cnts = [&](const char *tg, std::map<int, std::map<std::string, int>> &m) {
+            for (auto &pe : m)
+                for (auto &ke : pe.second) {
+                    snprintf(buf, sizeof buf, "%s\t%d\t%s\t%d\n", tg, pe.first, ke.first.c_str(), ke.second);
+                    o += buf;
+                }
+        };
+        cnts("PCI", cnt_i);
+        cnts("PCD", cnt_d);
+        cnts("PMN", cnt_m);
+    }
+    return RV_OK;
+}
+
+}  // namespace rv

@@ -1,0 +1,172 @@
+// Internal declarations shared by the device kernels and the host side of
+// librvgpu.  Not part of the public C ABI (include/rvgpu.h).
+#pragma once
+#include <cstddef>
+#include <cstdint>
+
+#include "rvgpu.h"
+
+namespace rv {
+
+// Hard limits of this build.
+constexpr int kMaxKey = 640;        // longest allele key a walk may build
+constexpr int kTileW = 1024;        // positions per shared-memory tile window
+constexpr int kPileupThreads = 256; // threads per pileup block (one read per thread at a time)
+
+// Allele-key kinds stored in the device hash table (the maps of
+// include/scopedata/VariationData.h:14-56).
+enum KeyKind : uint16_t {
+    KIND_NONINS = 0,   // nonInsertionVariants, string keys (MNV, deletion, complex, non-ACGT bases)
+    KIND_INS = 1,      // insertionVariants
+    KIND_SC5 = 2,      // softClips5End aggregate Variation
+    KIND_SC3 = 3,      // softClips3End aggregate Variation
+    KIND_SC5_SEQ = 4,  // softClips5End seq[idx][ch] (key = idx, ch)
+    KIND_SC3_SEQ = 5,
+    KIND_SPLICE = 6,   // spliceCount (key "a-b")
+};
+
+// Entry flags
+enum : uint32_t {
+    SF_PDIFF = 1u,      // two pstd-relevant observations with different read positions
+    SF_QDIFF = 2u,      // ... with different mean qualities
+    SF_ZERO = 4u,       // an observation with read position 0 or quality 0 (order-sensitive)
+    SF_ERASED = 8u,     // removed by the realigner
+    SF_FIRST = 16u,     // first_tp / first_q hold a value
+    SF_FORCE_STD = 32u, // pstd and qstd forced true (adjCnt)
+};
+
+// One allele key of the device hash table.
+struct alignas(16) Slot {
+    unsigned long long fp;   // fingerprint of (region, kind, pos, key); 0 = empty
+    unsigned long long h2x;  // XOR of a second hash over all inserters (collision check)
+    int32_t region, pos;
+    uint16_t kind, klen;
+    uint32_t koff;           // key bytes in the arena
+    int32_t fwd, rev, hi, lo, obs, extracnt;
+    long long tp_sum, mq_sum, nm_sum;
+    double q_sum;
+    unsigned long long first_q;  // double bits of the first pstd-relevant quality
+    int32_t first_tp;
+    uint32_t flags;
+    uint32_t min_stamp;      // first read (batch index) that created the key
+    uint32_t next;           // next slot at the same position (per-position list), ~0u = end
+};
+
+// Per-region record on the device.
+struct Region {
+    int32_t start, end;      // region, 1-based inclusive
+    int32_t ws, we;          // reference window [ws, we] (RecordPreprocessor::makeReference)
+    int32_t clo, chi;        // cell range (positions with a cell)
+    int64_t cell_base;       // index of position clo in the cell arrays
+    int64_t r0, r1;          // candidate read range in the batch
+    int32_t span_lo, span_hi; // min/max position any read of the region may touch
+    int32_t serial;          // 1: processed by the in-order exact walker
+    int32_t max_read_len;    // maxReadLength of the region
+    int32_t err;             // error bits
+    int32_t pad;
+};
+
+struct Tile {
+    int32_t region;
+    int32_t pad;
+    int64_t r0, r1;          // reads [r0, r1) of the batch
+};
+
+// Device copy of rv_params plus derived values.
+struct DevParams {
+    double goodq, freq, qratio, mapq_filter, lofreq, bias;
+    int32_t vext, mismatch, local_realign, minr, read_pos_filter, min_mapq, min_bias_reads, samfilter;
+    int32_t trim_bases_after, minmatch, dedup, unique_fwd, unique_first, do_pileup, fisher, move_indels_3;
+    int32_t svminlen, pad;
+};
+
+// Cell arrays: one cell per (position, base A/C/G/T); index = 4 * cell + b.
+struct Cells {
+    uint32_t *fwd, *rev, *hi, *tp, *q, *mq;
+    int32_t *nm;
+    uint32_t *first;     // packed first (tp, q) of pstd-relevant observations | flag bits
+    uint32_t *cov;       // per position: refCoverage
+    uint8_t *kflags;     // per position: bit b = key b exists, bit 4+b = key b erased
+    int64_t n_cells;     // positions
+};
+
+struct Batch {
+    int64_t n_reads;
+    const int32_t *pos, *mpos, *nm, *l_qseq;
+    const uint16_t *flag, *n_cigar;
+    const uint8_t *mapq;
+    const uint32_t *cig_off, *cigar;
+    const uint64_t *base_off;
+    const uint8_t *seq, *qual;
+};
+
+struct Hash {
+    Slot *slots;
+    unsigned long long mask;   // capacity - 1 (power of two)
+    uint8_t *arena;
+    unsigned long long arena_cap;
+    unsigned long long *arena_used;
+    unsigned int *n_used;
+};
+
+// Deferred subtraction of a reference-base observation after an insertion
+// (src/parseCigar.cpp:1471-1490): applied only if the key existed when the
+// insertion was seen, which a later kernel decides.
+struct Deferred {
+    int32_t region, pos;
+    int64_t read;            // batch index of the read that saw the insertion
+    int32_t ci;              // CIGAR op index of the insertion
+    int32_t base;            // 0..3
+    int32_t dir, tp, q, mapq, nm;
+    int32_t pad;
+};
+
+// Error word bits (per context)
+enum : uint32_t {
+    ERR_HASH_FULL = 1u,
+    ERR_ARENA_FULL = 2u,
+    ERR_KEY_TOO_LONG = 4u,
+    ERR_DEFER_FULL = 8u,
+    ERR_CELL_RANGE = 16u,
+    ERR_UNSUPPORTED = 32u,
+    ERR_PROBE_LIMIT = 64u,
+    ERR_COLLISION = 128u,
+};
+
+// One scored allele at a candidate position, handed to the host for the
+// string part of collectReferenceVariants and the record text.
+struct CandVar {
+    int32_t region, pos;
+    int32_t kind;            // 0 reference allele, 1 variant allele
+    int32_t rank;            // order after the CMP_VARI sort (src/ToVarsBuilder.cpp:20-26)
+    int32_t key_off, key_len;  // key bytes in the arena; key_len < 0: single base, key_off = 0..3
+    int32_t pc, fwd, rev, hicnt, hicov, tpc, rfc, rrc;
+    int32_t bias, ref_bias, pstd, qstd, pass, nvars;
+    double freq, pmean, qual, mq, qratio, hifreq, extrafreq, nm;
+    double fisher_p, fisher_ratio;
+};
+
+struct DevState {
+    Batch batch;
+    Region *regions;
+    int32_t n_regions;
+    Tile *tiles;
+    int32_t n_tiles;
+    unsigned int *tile_counter;
+    Cells cells;
+    Hash hash;
+    Deferred *deferred;
+    unsigned int *n_deferred;
+    unsigned int deferred_cap;
+    const char *ref;        // whole contig, uppercase, 0-based
+    int32_t ref_len;
+    unsigned int *err;
+    uint32_t *head;          // per cell: first hash slot at that position
+    int64_t *score_base;     // per region: first scoring thread (prefix sum of region lengths)
+    int64_t n_score;
+    CandVar *cand;
+    unsigned int *n_cand;
+    unsigned int cand_cap;
+};
+
+}  // namespace rv

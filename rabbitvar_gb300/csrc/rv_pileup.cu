@@ -1,0 +1,538 @@
+// Pileup kernels: the record filter, the per-read CIGAR walk and the
+// allele-count maps (CigarParser::process, src/parseCigar.cpp:410-974).
+//
+//  * k_pileup_tiles: persistent blocks pull tiles (a region's consecutive
+//    reads) from a device work queue; each thread walks one read; A/C/G/T
+//    observations go into a shared-memory histogram covering the tile's
+//    window (kTileW positions), flushed to the per-position global cells once
+//    per tile; string-keyed alleles (MNV, indels, soft clips) go to a global
+//    open-addressing hash table.
+//  * k_pileup_serial: regions whose reads reach outside the reference window
+//    are walked in file order by one thread, reproducing the reference map's
+//    insert-on-lookup behaviour exactly.
+//  * k_resolve_deferred: decides, for every reference-base subtraction after
+//    an insertion, whether that key existed when the insertion was seen (the
+//    getVariationMaybe lookup of src/parseCigar.cpp:1475) by re-walking the
+//    same and earlier reads, then applies it.
+#include <cuda_runtime.h>
+
+#include "rv_walk.cuh"
+
+namespace rv {
+
+__device__ __forceinline__ void set_err(unsigned int *err, unsigned int bits) { atomicOr(err, bits); }
+
+// ---------------------------------------------------------------------------
+// device hash table of string-keyed alleles
+// ---------------------------------------------------------------------------
+__device__ void key_hashes(int region, int kind, int pos, const char *k, int n, unsigned long long &h1,
+                           unsigned long long &h2) {
+    unsigned long long a = fmix64(((unsigned long long)(uint32_t)region << 32) ^ (uint32_t)pos ^
+                                  ((unsigned long long)kind << 58) ^ ((unsigned long long)n << 44));
+    unsigned long long b = fmix64(a ^ 0x9e3779b97f4a7c15ULL);
+    int i = 0;
+    while (i < n) {
+        unsigned long long w = 0;
+        int m = n - i < 8 ? n - i : 8;
+        for (int j = 0; j < m; j++) w |= (unsigned long long)(uint8_t)k[i + j] << (8 * j);
+        a = fmix64(a ^ w) + 0x632be59bd9b4e019ULL;
+        b = fmix64(b + w * 0x94d049bb133111ebULL);
+        i += m;
+    }
+    h1 = a ? a : 1;
+    h2 = b;
+}
+
+__device__ Slot *hash_get(const Hash &H, unsigned int *err, int region, int kind, int pos, const char *k, int n) {
+    unsigned long long h1, h2;
+    key_hashes(region, kind, pos, k, n, h1, h2);
+    unsigned long long i = h1 & H.mask;
+    for (int step = 0; step <= 4096; step++) {
+        Slot *s = &H.slots[i];
+        unsigned long long old = atomicCAS(&s->fp, 0ULL, h1);
+        if (old == 0ULL) {
+            s->region = region;
+            s->pos = pos;
+            s->kind = (uint16_t)kind;
+            s->klen = (uint16_t)n;
+            unsigned long long off = n ? atomicAdd(H.arena_used, (unsigned long long)n) : 0ULL;
+            if (off + n > H.arena_cap) {
+                set_err(err, ERR_ARENA_FULL);
+                s->koff = 0;
+                s->klen = 0;
+            } else {
+                s->koff = (uint32_t)off;
+                for (int j = 0; j < n; j++) H.arena[off + j] = (uint8_t)k[j];
+            }
+            atomicAdd(H.n_used, 1u);
+            atomicXor(&s->h2x, h2);
+            return s;
+        }
+        if (old == h1) {
+            atomicXor(&s->h2x, h2);
+            return s;
+        }
+        i = (i + 1) & H.mask;
+    }
+    set_err(err, ERR_HASH_FULL);
+    return nullptr;
+}
+
+__device__ void slot_obs(Slot *s, const Obs &o, double goodq, uint32_t stamp) {
+    if (o.dir) atomicAdd(&s->rev, 1); else atomicAdd(&s->fwd, 1);
+    if (o.q >= goodq) atomicAdd(&s->hi, 1); else atomicAdd(&s->lo, 1);
+    atomicAdd((unsigned long long *)&s->tp_sum, (unsigned long long)(long long)o.tp);
+    atomicAdd(&s->q_sum, o.q);
+    atomicAdd((unsigned long long *)&s->mq_sum, (unsigned long long)(long long)o.mapq);
+    atomicAdd((unsigned long long *)&s->nm_sum, (unsigned long long)(long long)o.nm);
+    if (o.creates) atomicAdd(&s->obs, 1);
+    atomicMin(&s->min_stamp, stamp);
+    if (o.std_rel) {
+        // pstd/qstd (src/parseCigar.cpp:902-914): "not all values equal", tested
+        // against whichever observation claimed the first slot
+        int old_tp = atomicCAS(&s->first_tp, INT32_MIN, o.tp);
+        if (old_tp != INT32_MIN && old_tp != o.tp) atomicOr(&s->flags, SF_PDIFF);
+        unsigned long long qb = (unsigned long long)__double_as_longlong(o.q);
+        unsigned long long old_q = atomicCAS(&s->first_q, 0xFFF8DEADBEEF0001ULL, qb);
+        if (old_q != 0xFFF8DEADBEEF0001ULL && old_q != qb) atomicOr(&s->flags, SF_QDIFF);
+        if (o.tp == 0 || o.q == 0.0) atomicOr(&s->flags, SF_ZERO);
+    }
+}
+
+__global__ void k_init_slots(Slot *slots, unsigned long long n) {
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        Slot &s = slots[i];
+        s.fp = 0;
+        s.h2x = 0;
+        s.region = 0;
+        s.pos = 0;
+        s.kind = 0;
+        s.klen = 0;
+        s.koff = 0;
+        s.fwd = s.rev = s.hi = s.lo = s.obs = s.extracnt = 0;
+        s.tp_sum = s.mq_sum = s.nm_sum = 0;
+        s.q_sum = 0.0;
+        s.first_q = 0xFFF8DEADBEEF0001ULL;
+        s.first_tp = INT32_MIN;
+        s.flags = 0;
+        s.min_stamp = 0xFFFFFFFFu;
+        s.next = 0xFFFFFFFFu;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// per-position cells
+// ---------------------------------------------------------------------------
+// packed first (tp, q) of pstd-relevant observations: tp in bits 0-11,
+// q in bits 12-21, bit 29 zero-seen, bit 30 pdiff, bit 31 qdiff
+constexpr uint32_t FC_ZERO = 1u << 29, FC_PDIFF = 1u << 30, FC_QDIFF = 1u << 31;
+constexpr uint32_t FC_VAL = (1u << 22) - 1;
+
+__device__ __forceinline__ void first_merge(uint32_t *w, uint32_t v, uint32_t flags) {
+    // v: packed value (nonzero); merge into word *w.  Flag bits may change
+    // concurrently, so retry the claim while the value field is still empty
+    // (bounded: each retry means another thread changed the word).
+    uint32_t cur = *((volatile uint32_t *)w);
+    for (int it = 0; it < 64 && (cur & FC_VAL) == 0; it++) {
+        uint32_t old = atomicCAS(w, cur, cur | v);
+        if (old == cur) { cur |= v; break; }
+        cur = old;
+    }
+    uint32_t f = flags;
+    uint32_t cv = cur & FC_VAL;
+    if (cv != 0 && cv != v) {
+        if ((cv & 0xFFFu) != (v & 0xFFFu)) f |= FC_PDIFF;
+        if ((cv >> 12) != (v >> 12)) f |= FC_QDIFF;
+    }
+    if (f & ~cur) atomicOr(w, f);
+}
+
+__device__ __forceinline__ int64_t cell_of(const Region &R, int p) { return R.cell_base + (p - R.clo); }
+
+// Direct global update of one A/C/G/T observation (outside a tile window, or
+// the in-order walker).
+__device__ void cell_obs_global(const Cells &C, const Region &R, unsigned int *err, int p, int b, const Obs &o,
+                                double goodq) {
+    if (p < R.clo || p > R.chi) { set_err(err, ERR_CELL_RANGE); return; }
+    int64_t c = cell_of(R, p);
+    int64_t g = 4 * c + b;
+    int qi = (int)o.q;
+    if (o.dir) atomicAdd(&C.rev[g], 1u); else atomicAdd(&C.fwd[g], 1u);
+    if (o.q >= goodq) atomicAdd(&C.hi[g], 1u);
+    atomicAdd(&C.tp[g], (uint32_t)o.tp);
+    atomicAdd(&C.q[g], (uint32_t)qi);
+    atomicAdd(&C.mq[g], (uint32_t)o.mapq);
+    atomicAdd(&C.nm[g], o.nm);
+    atomicAdd(&C.cov[c], 1u);
+    atomicOr((unsigned int *)&C.kflags[c & ~3LL], 1u << (b + 8 * (c & 3)));
+    if (o.std_rel) {
+        if (o.tp <= 0 || o.tp > 4095 || qi <= 0 || qi > 1023) {
+            set_err(err, o.tp > 4095 ? ERR_UNSUPPORTED : 0u);
+            atomicOr(&C.first[g], FC_ZERO);
+        } else {
+            first_merge(&C.first[g], (uint32_t)o.tp | ((uint32_t)qi << 12), 0u);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// sinks
+// ---------------------------------------------------------------------------
+struct SinkBase {
+    const DevState *st;
+    const DevParams *P;
+    const Region *R;
+    int region_idx;
+    __device__ void error(unsigned int bits) { set_err(st->err, bits); }
+    __device__ void cov(int p, int n) {
+        if (p < R->clo || p > R->chi) { error(ERR_CELL_RANGE); return; }
+        atomicAdd(&st->cells.cov[cell_of(*R, p)], (uint32_t)n);
+    }
+    __device__ void event(int kind, int pos, const char *k, int n, const Obs &o, int64_t read) {
+        Slot *s = hash_get(st->hash, st->err, region_idx, kind, pos, k, n);
+        if (s) slot_obs(s, o, P->goodq, (uint32_t)read);
+    }
+    __device__ void max_len(int tlen) { atomicMax((int *)&R->max_read_len, tlen); }
+};
+
+// Tile sink: A/C/G/T observations inside [wlo, wlo + kTileW) accumulate in
+// shared memory; subtractions are deferred.
+struct TileSink : SinkBase {
+    unsigned long long *cnt;   // fwd (21) | rev (21) | hi (22)
+    unsigned long long *sums;  // tp (21) | q (21) | mapq (22)
+    int *nmv;
+    uint32_t *first;
+    int wlo;
+    __device__ bool phantom(int) const { return false; }
+    __device__ void touch_phantom(int) { error(ERR_UNSUPPORTED); }
+    __device__ void single(int p, int b, const Obs &o, int64_t) {
+        int d = p - wlo;
+        int qi = (int)o.q;
+        if (d >= 0 && d < kTileW && o.tp >= 1 && o.tp < 1024 && qi >= 1 && qi < 1024 && o.mapq < 256) {
+            int ix = 4 * d + b;
+            unsigned long long cv = (o.dir ? (1ULL << 21) : 1ULL) + (o.q >= P->goodq ? (1ULL << 42) : 0ULL);
+            atomicAdd(&cnt[ix], cv);
+            atomicAdd(&sums[ix], (unsigned long long)o.tp | ((unsigned long long)qi << 21) |
+                                     ((unsigned long long)o.mapq << 42));
+            atomicAdd(&nmv[ix], o.nm);
+            if (o.std_rel) first_merge(&first[ix], (uint32_t)o.tp | ((uint32_t)qi << 12), 0u);
+        } else {
+            cell_obs_global(st->cells, *R, st->err, p, b, o, P->goodq);
+        }
+    }
+    __device__ void subtract(int p, int b, int dir, int tp, int q, int mapq, int nm, int64_t read, int ci) {
+        unsigned int k = atomicAdd(st->n_deferred, 1u);
+        if (k >= st->deferred_cap) { error(ERR_DEFER_FULL); return; }
+        Deferred &d = st->deferred[k];
+        d.region = region_idx; d.pos = p; d.read = read; d.ci = ci; d.base = b;
+        d.dir = dir; d.tp = tp; d.q = q; d.mapq = mapq; d.nm = nm; d.pad = 0;
+    }
+};
+
+__device__ void apply_subtract(const Cells &C, const Region &R, unsigned int *err, int p, int b, int dir, int tp,
+                               int q, int mapq, int nm, double goodq) {
+    if (p < R.clo || p > R.chi) { set_err(err, ERR_CELL_RANGE); return; }
+    int64_t g = 4 * cell_of(R, p) + b;
+    if (dir) atomicSub(&C.rev[g], 1u); else atomicSub(&C.fwd[g], 1u);
+    if (q >= goodq) atomicSub(&C.hi[g], 1u);
+    atomicSub(&C.tp[g], (uint32_t)tp);
+    atomicSub(&C.q[g], (uint32_t)q);
+    atomicSub(&C.mq[g], (uint32_t)mapq);
+    atomicSub(&C.nm[g], nm);
+}
+
+// In-order sink for the exact serial walker.
+struct SerialSink : SinkBase {
+    uint32_t *ph_hi;   // bitmap of inserted positions above the window
+    uint32_t *ph_lo;   // bitmap of inserted positions below the window
+    static constexpr int kPh = 4096;
+    __device__ bool phantom(int p) const {
+        if (p > R->we) { int d = p - R->we - 1; return d < kPh && ((ph_hi[d >> 5] >> (d & 31)) & 1u); }
+        if (p < R->ws) { int d = R->ws - 1 - p; return d < kPh && ((ph_lo[d >> 5] >> (d & 31)) & 1u); }
+        return false;
+    }
+    __device__ void touch_phantom(int p) {
+        if (p > R->we) {
+            int d = p - R->we - 1;
+            if (d < kPh) ph_hi[d >> 5] |= 1u << (d & 31); else error(ERR_UNSUPPORTED);
+        } else if (p < R->ws) {
+            int d = R->ws - 1 - p;
+            if (d < kPh) ph_lo[d >> 5] |= 1u << (d & 31); else error(ERR_UNSUPPORTED);
+        }
+    }
+    __device__ void single(int p, int b, const Obs &o, int64_t) {
+        cell_obs_global(st->cells, *R, st->err, p, b, o, P->goodq);
+    }
+    __device__ void subtract(int p, int b, int dir, int tp, int q, int mapq, int nm, int64_t, int) {
+        if (p < R->clo || p > R->chi) return;
+        int64_t c = cell_of(*R, p);
+        uint32_t kf = st->cells.kflags[c];
+        if (kf & (1u << b)) apply_subtract(st->cells, *R, st->err, p, b, dir, tp, q, mapq, nm, P->goodq);
+    }
+};
+
+// Probe sink: reports whether the walked read creates key (pos, base) before
+// it reaches the insertion (read, ci) that asked.
+struct ProbeSink {
+    const Region *R;
+    int pos, base;
+    int64_t stop_read;
+    int stop_ci;
+    bool stopped, found;
+    __device__ bool phantom(int) const { return false; }
+    __device__ void touch_phantom(int) {}
+    __device__ void error(unsigned int) {}
+    __device__ void cov(int, int) {}
+    __device__ void event(int, int, const char *, int, const Obs &, int64_t) {}
+    __device__ void max_len(int) {}
+    __device__ void single(int p, int b, const Obs &, int64_t) {
+        if (!stopped && p == pos && b == base) found = true;
+    }
+    __device__ void subtract(int, int, int, int, int, int, int, int64_t read, int ci) {
+        if (read == stop_read && ci == stop_ci) stopped = true;
+    }
+};
+
+// Record filters of next_record (src/recordPreprocessor.cpp:101-180) plus the
+// region-overlap test of sam_itr_querys.
+__device__ bool read_passes(const Batch &B, const DevParams &P, const Region &R, int64_t r) {
+    int pos = B.pos[r];
+    if (pos >= R.end) return false;
+    const uint32_t *c = B.cigar + B.cig_off[r];
+    int n = B.n_cigar[r], span = 0;
+    for (int k = 0; k < n; k++) {
+        int o = cig_op(__ldg(c + k));
+        if (o == 0 || o == 2 || o == 3 || o == 7 || o == 8) span += cig_len(__ldg(c + k));
+    }
+    int flag = B.flag[r];
+    int endpos = ((flag & 4) || span == 0) ? pos + 1 : pos + span;
+    if (endpos <= R.start - 1) return false;
+    if (flag & P.samfilter) return false;
+    if ((int)B.mapq[r] < P.min_mapq) return false;
+    if (B.l_qseq[r] == 1) return false;
+    return true;
+}
+
+// read span incl. soft clips, used for tile windows
+__device__ void read_span(const Batch &B, int64_t r, int &lo, int &hi) {
+    const uint32_t *c = B.cigar + B.cig_off[r];
+    int n = B.n_cigar[r], span = 0;
+    int clip5 = 0, clip3 = 0;
+    for (int k = 0; k < n; k++) {
+        uint32_t w = __ldg(c + k);
+        int o = cig_op(w);
+        if (o == 0 || o == 2 || o == 3 || o == 7 || o == 8) span += cig_len(w);
+    }
+    if (n > 0) {
+        uint32_t w0 = __ldg(c), w1 = __ldg(c + n - 1);
+        if (cig_op(w0) == 4 || cig_op(w0) == 1) clip5 = cig_len(w0);
+        if (cig_op(w1) == 4 || cig_op(w1) == 1) clip3 = cig_len(w1);
+    }
+    int pos1 = B.pos[r] + 1;
+    lo = pos1 - clip5 - 1;
+    hi = pos1 + span + clip3;
+}
+
+// ---------------------------------------------------------------------------
+// kernels
+// ---------------------------------------------------------------------------
+__global__ void k_region_spans(DevState st) {
+    int reg = blockIdx.x;
+    if (reg >= st.n_regions) return;
+    Region &R = st.regions[reg];
+    __shared__ int lo, hi;
+    if (threadIdx.x == 0) { lo = INT32_MAX; hi = INT32_MIN; }
+    __syncthreads();
+    int mylo = INT32_MAX, myhi = INT32_MIN;
+    for (int64_t r = R.r0 + threadIdx.x; r < R.r1; r += blockDim.x) {
+        int a, b;
+        read_span(st.batch, r, a, b);
+        mylo = min(mylo, a);
+        myhi = max(myhi, b);
+    }
+    atomicMin(&lo, mylo);
+    atomicMax(&hi, myhi);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        R.span_lo = lo;
+        R.span_hi = hi;
+        // reads that can reach outside the reference window take the in-order path
+        R.serial = (R.r1 > R.r0) && (hi + 2 > R.we || lo - 2 < R.ws) ? 1 : 0;
+        if (R.r1 > R.r0 && (lo < R.clo || hi > R.chi)) set_err(st.err, ERR_CELL_RANGE);
+    }
+}
+
+template <int TW>
+__global__ void __launch_bounds__(kPileupThreads) k_pileup_tiles(DevState st, DevParams P) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    unsigned long long *cnt = (unsigned long long *)smem;
+    unsigned long long *sums = cnt + 4 * TW;
+    int *nmv = (int *)(sums + 4 * TW);
+    uint32_t *first = (uint32_t *)(nmv + 4 * TW);
+    __shared__ int s_tile, s_wlo;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            s_tile = (int)atomicAdd(st.tile_counter, 1u);
+            s_wlo = INT32_MAX;
+        }
+        __syncthreads();
+        int t = s_tile;
+        if (t >= st.n_tiles) return;
+        const Tile tile = st.tiles[t];
+        const Region &R = st.regions[tile.region];
+        if (R.serial) { __syncthreads(); continue; }
+        for (int64_t r = tile.r0 + threadIdx.x; r < tile.r1; r += blockDim.x) {
+            int a, b;
+            read_span(st.batch, r, a, b);
+            atomicMin(&s_wlo, a);
+        }
+        for (int i = threadIdx.x; i < 4 * TW; i += blockDim.x) {
+            cnt[i] = 0ULL;
+            sums[i] = 0ULL;
+            nmv[i] = 0;
+            first[i] = 0u;
+        }
+        __syncthreads();
+        int wlo = max(s_wlo, R.clo);
+        TileSink sink;
+        sink.st = &st;
+        sink.P = &P;
+        sink.R = &R;
+        sink.region_idx = tile.region;
+        sink.cnt = cnt;
+        sink.sums = sums;
+        sink.nmv = nmv;
+        sink.first = first;
+        sink.wlo = wlo;
+        {
+            Walker<TileSink> w(P, sink, R, st.ref, st.ref_len);
+            for (int64_t r = tile.r0 + threadIdx.x; r < tile.r1; r += blockDim.x) {
+                if (!read_passes(st.batch, P, R, r)) continue;
+                w.walk(st.batch, r);
+            }
+        }
+        __syncthreads();
+        // flush the tile histogram into the global cells
+        const Cells &C = st.cells;
+        for (int i = threadIdx.x; i < 4 * TW; i += blockDim.x) {
+            unsigned long long c = cnt[i];
+            if (c == 0ULL) continue;
+            int p = wlo + (i >> 2);
+            int b = i & 3;
+            if (p > R.chi) { set_err(st.err, ERR_CELL_RANGE); continue; }
+            int64_t cell = cell_of(R, p);
+            int64_t g = 4 * cell + b;
+            uint32_t f = (uint32_t)(c & 0x1FFFFFULL), rv_ = (uint32_t)((c >> 21) & 0x1FFFFFULL);
+            uint32_t h = (uint32_t)(c >> 42);
+            unsigned long long s = sums[i];
+            if (f) atomicAdd(&C.fwd[g], f);
+            if (rv_) atomicAdd(&C.rev[g], rv_);
+            if (h) atomicAdd(&C.hi[g], h);
+            atomicAdd(&C.tp[g], (uint32_t)(s & 0x1FFFFFULL));
+            atomicAdd(&C.q[g], (uint32_t)((s >> 21) & 0x1FFFFFULL));
+            atomicAdd(&C.mq[g], (uint32_t)(s >> 42));
+            if (nmv[i]) atomicAdd(&C.nm[g], nmv[i]);
+            atomicAdd(&C.cov[cell], f + rv_);
+            atomicOr((unsigned int *)&C.kflags[cell & ~3LL], 1u << (b + 8 * (cell & 3)));
+            uint32_t fw = first[i];
+            if (fw) first_merge(&C.first[g], fw & FC_VAL, fw & ~FC_VAL);
+        }
+        __syncthreads();
+    }
+}
+
+// One block per region; thread 0 walks the serial regions' reads in order.
+__global__ void k_pileup_serial(DevState st, DevParams P) {
+    int reg = blockIdx.x;
+    if (reg >= st.n_regions) return;
+    const Region &R = st.regions[reg];
+    if (!R.serial) return;
+    __shared__ uint32_t ph_hi[SerialSink::kPh / 32], ph_lo[SerialSink::kPh / 32];
+    for (int i = threadIdx.x; i < SerialSink::kPh / 32; i += blockDim.x) { ph_hi[i] = 0; ph_lo[i] = 0; }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    SerialSink sink;
+    sink.st = &st;
+    sink.P = &P;
+    sink.R = &R;
+    sink.region_idx = reg;
+    sink.ph_hi = ph_hi;
+    sink.ph_lo = ph_lo;
+    Walker<SerialSink> w(P, sink, R, st.ref, st.ref_len);
+    for (int64_t r = R.r0; r < R.r1; r++) {
+        if (!read_passes(st.batch, P, R, r)) continue;
+        w.walk(st.batch, r);
+    }
+}
+
+// One thread per deferred subtraction.
+__global__ void k_resolve_deferred(DevState st, DevParams P, int max_probe_reads) {
+    unsigned int n = *st.n_deferred;
+    if (n > st.deferred_cap) n = st.deferred_cap;
+    for (unsigned int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const Deferred d = st.deferred[k];
+        const Region &R = st.regions[d.region];
+        ProbeSink ps;
+        ps.R = &R;
+        ps.pos = d.pos;
+        ps.base = d.base;
+        ps.stop_read = d.read;
+        ps.stop_ci = d.ci;
+        ps.stopped = false;
+        ps.found = false;
+        Walker<ProbeSink> w(P, ps, R, st.ref, st.ref_len);
+        w.walk(st.batch, d.read);
+        int probes = 0;
+        for (int64_t r = d.read - 1; !ps.found && r >= R.r0; r--) {
+            int a, b;
+            read_span(st.batch, r, a, b);
+            // reads are coordinate-sorted: stop once no earlier read can reach pos
+            if (st.batch.pos[r] + 1 + 4 * 1024 < d.pos) break;
+            if (a > d.pos || b < d.pos) continue;
+            if (!read_passes(st.batch, P, R, r)) continue;
+            if (++probes > max_probe_reads) { set_err(st.err, ERR_PROBE_LIMIT); break; }
+            ps.stopped = false;
+            ps.stop_read = -1;
+            w.walk(st.batch, r);
+        }
+        if (ps.found) apply_subtract(st.cells, R, st.err, d.pos, d.base, d.dir, d.tp, d.q, d.mapq, d.nm, P.goodq);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host-side launchers
+// ---------------------------------------------------------------------------
+void launch_init_slots(Slot *slots, unsigned long long n, cudaStream_t s) {
+    k_init_slots<<<592, 256, 0, s>>>(slots, n);
+}
+
+void launch_region_spans(const DevState &st, cudaStream_t s) {
+    if (st.n_regions > 0) k_region_spans<<<st.n_regions, 256, 0, s>>>(st);
+}
+
+size_t pileup_smem_bytes() { return (size_t)kTileW * 4 * (8 + 8 + 4 + 4); }
+
+cudaError_t launch_pileup(const DevState &st, const DevParams &P, int grid, cudaStream_t s) {
+    size_t smem = pileup_smem_bytes();
+    cudaError_t e = cudaFuncSetAttribute(k_pileup_tiles<kTileW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_pileup_tiles<kTileW><<<grid, kPileupThreads, smem, s>>>(st, P);
+    return cudaGetLastError();
+}
+
+void launch_serial(const DevState &st, const DevParams &P, cudaStream_t s) {
+    if (st.n_regions > 0) k_pileup_serial<<<st.n_regions, 128, 0, s>>>(st, P);
+}
+
+void launch_resolve(const DevState &st, const DevParams &P, cudaStream_t s) {
+    k_resolve_deferred<<<152, 128, 0, s>>>(st, P, 1 << 16);
+}
+
+int pileup_blocks_per_sm() {
+    int n = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_pileup_tiles<kTileW>, kPileupThreads, pileup_smem_bytes());
+    return n;
+}
+
+}  // namespace rv

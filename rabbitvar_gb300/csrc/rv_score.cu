@@ -1,0 +1,478 @@
+// Scoring kernels: per-site statistics of ToVarsBuilder::process
+// (src/ToVarsBuilder.cpp:97-205, createVariant :466-536, createInsertion
+// :358-452, calcHicov :570-587, CMP_VARI :20-26, collectVarsAtPosition
+// :327-346, the numeric part of collectReferenceVariants :730-1098), the
+// numeric pre-screen of Variant::isGoodVar (include/Variant.h:197-248) and
+// the two-sided Fisher exact test of the --fisher output
+// (src/modes/simpleMode.cpp:96-108) in FP64.
+#include <cuda_runtime.h>
+
+#include "rv_walk.cuh"
+
+namespace rv {
+
+constexpr int kMaxVars = 32;
+constexpr uint32_t kNone = 0xFFFFFFFFu;
+constexpr uint32_t FCS_PDIFF = 1u << 30, FCS_QDIFF = 1u << 31;
+
+__device__ __forceinline__ int64_t cell_index(const Region &R, int p) { return R.cell_base + (p - R.clo); }
+
+// Link every string-keyed allele into the list of its position.
+__global__ void k_link_slots(DevState st) {
+    unsigned long long n = st.hash.mask + 1ULL;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        Slot &s = st.hash.slots[i];
+        if (s.fp == 0ULL || (s.kind != KIND_NONINS && s.kind != KIND_INS)) continue;
+        const Region &R = st.regions[s.region];
+        if (s.pos < R.clo || s.pos > R.chi) continue;
+        int64_t c = cell_index(R, s.pos);
+        s.next = atomicExch(&st.head[c], (uint32_t)i);
+    }
+}
+
+__global__ void k_check_collisions(DevState st) {
+    // every inserter XORs h2 of its key into the slot: for an odd number of
+    // inserters of one key the result is h2, for an even number it is 0
+    unsigned long long n = st.hash.mask + 1ULL;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        const Slot &s = st.hash.slots[i];
+        if (s.fp == 0ULL) continue;
+        unsigned long long h1, h2;
+        unsigned long long a = fmix64(((unsigned long long)(uint32_t)s.region << 32) ^ (uint32_t)s.pos ^
+                                      ((unsigned long long)s.kind << 58) ^ ((unsigned long long)s.klen << 44));
+        unsigned long long b = fmix64(a ^ 0x9e3779b97f4a7c15ULL);
+        const uint8_t *k = st.hash.arena + s.koff;
+        int n_ = s.klen;
+        for (int ii = 0; ii < n_;) {
+            unsigned long long w = 0;
+            int m = n_ - ii < 8 ? n_ - ii : 8;
+            for (int j = 0; j < m; j++) w |= (unsigned long long)k[ii + j] << (8 * j);
+            a = fmix64(a ^ w) + 0x632be59bd9b4e019ULL;
+            b = fmix64(b + w * 0x94d049bb133111ebULL);
+            ii += m;
+        }
+        h1 = a ? a : 1;
+        h2 = b;
+        int inserters = s.fwd + s.rev;  // every observation re-inserts the key
+        (void)inserters;
+        if (h1 != s.fp || (s.h2x != 0ULL && s.h2x != h2)) atomicOr(st.err, ERR_COLLISION);
+    }
+}
+
+struct V {
+    int kind;       // 0 single (key_off = base), 1 hash slot (key_off = slot index)
+    int key;        // base 0..3 or slot index
+    int cnt, fwd, rev, hi, lo, extracnt;
+    double tp, q, mq, nm;
+    bool pstd, qstd;
+    // derived Variant fields
+    int ttcov, hicov;
+    double freq, pmean, qual, mqv, qratio, hifreq, extrafreq, nmv;
+    int bias;
+};
+
+__device__ int strand_bias(int f, int r, const DevParams &P) {  // include/VariationUtils.h:511-521
+    if (f + r <= 12) return f * r > 0 ? 2 : 0;
+    return (f / (double)(f + r) >= P.bias && r / (double)(f + r) >= P.bias && f >= P.min_bias_reads &&
+            r >= P.min_bias_reads) ? 2 : 1;
+}
+
+__device__ void finish_var(V &v, int ttcov, int hicov, const DevParams &P) {
+    v.ttcov = ttcov;
+    v.hicov = hicov;
+    v.bias = strand_bias(v.fwd, v.rev, P);
+    v.freq = v.cnt / (double)ttcov;
+    v.pmean = v.tp / (double)v.cnt;
+    v.qual = v.q / v.cnt;
+    v.mqv = v.mq / (double)v.cnt;
+    v.qratio = v.hi / (v.lo != 0 ? (double)v.lo : 0.5);
+    v.hifreq = hicov > 0 ? v.hi / (double)hicov : 0;
+    v.extrafreq = v.extracnt != 0 ? v.extracnt / (double)ttcov : 0;
+    v.nmv = v.nm / (double)v.cnt;
+}
+
+// lexicographic compare of two keys (std::string::compare order)
+__device__ int key_cmp(const DevState &st, const V &a, const V &b) {
+    const char bases[4] = {'A', 'C', 'G', 'T'};
+    char ca[1], cb[1];
+    const char *pa, *pb;
+    int na, nb;
+    if (a.kind == 0) { ca[0] = bases[a.key]; pa = ca; na = 1; }
+    else { const Slot &s = st.hash.slots[a.key]; pa = (const char *)st.hash.arena + s.koff; na = s.klen; }
+    if (b.kind == 0) { cb[0] = bases[b.key]; pb = cb; nb = 1; }
+    else { const Slot &s = st.hash.slots[b.key]; pb = (const char *)st.hash.arena + s.koff; nb = s.klen; }
+    int m = na < nb ? na : nb;
+    for (int i = 0; i < m; i++) {
+        unsigned char x = (unsigned char)pa[i], y = (unsigned char)pb[i];
+        if (x != y) return x < y ? -1 : 1;
+    }
+    return na == nb ? 0 : (na < nb ? -1 : 1);
+}
+
+__device__ bool cmp_vari(const DevState &st, const V &a, const V &b) {  // CMP_VARI
+    double r = a.qual * a.cnt - b.qual * b.cnt;
+    if (r < 0.00001 && r > -0.00001) return key_cmp(st, a, b) < 0;
+    return r > 0;
+}
+
+__device__ void load_slot(const Slot &s, int idx, V &v) {
+    v.kind = 1;
+    v.key = idx;
+    v.cnt = s.fwd + s.rev;
+    v.fwd = s.fwd;
+    v.rev = s.rev;
+    v.hi = s.hi;
+    v.lo = s.lo;
+    v.extracnt = s.extracnt;
+    v.tp = (double)s.tp_sum;
+    v.q = s.q_sum;
+    v.mq = (double)s.mq_sum;
+    v.nm = (double)s.nm_sum;
+    v.pstd = (s.flags & (SF_PDIFF | SF_FORCE_STD)) != 0;
+    v.qstd = (s.flags & (SF_QDIFF | SF_FORCE_STD)) != 0;
+}
+
+struct PosKeys {
+    uint32_t ins[kMaxVars];
+    int n_ins;
+    int n_nonins;        // keys present in the position's nonInsertionVariants map
+    bool in_map;         // the position has an entry in nonInsertionVariants
+    int single_mask;     // present A/C/G/T keys
+};
+
+__device__ void gather_keys(const DevState &st, const Region &R, int p, PosKeys &k) {
+    int64_t c = cell_index(R, p);
+    uint8_t kf = st.cells.kflags[c];
+    int exist = kf & 15, erased = (kf >> 4) & 15;
+    k.single_mask = exist & ~erased;
+    k.n_nonins = __popc(k.single_mask);
+    k.in_map = exist != 0;
+    k.n_ins = 0;
+    for (uint32_t s = st.head[c]; s != kNone; s = st.hash.slots[s].next) {
+        const Slot &sl = st.hash.slots[s];
+        if (sl.kind == KIND_NONINS) {
+            k.in_map = true;
+            if (!(sl.flags & SF_ERASED)) k.n_nonins++;
+        } else if (sl.kind == KIND_INS && !(sl.flags & SF_ERASED)) {
+            if (k.n_ins < kMaxVars) k.ins[k.n_ins++] = s;
+            else atomicOr(st.err, ERR_UNSUPPORTED);
+        }
+    }
+}
+
+// sort the insertion keys of a position by key string (createInsertion sorts them)
+__device__ void sort_ins(const DevState &st, PosKeys &k) {
+    for (int i = 1; i < k.n_ins; i++) {
+        uint32_t x = k.ins[i];
+        V vx; vx.kind = 1; vx.key = (int)x;
+        int j = i - 1;
+        while (j >= 0) {
+            V vy; vy.kind = 1; vy.key = (int)k.ins[j];
+            if (key_cmp(st, vy, vx) <= 0) break;
+            k.ins[j + 1] = k.ins[j];
+            j--;
+        }
+        k.ins[j + 1] = x;
+    }
+}
+
+__device__ char ref_at(const DevState &st, const Region &R, int p) {
+    return (p >= R.ws && p <= R.we) ? st.ref[p - 1] : (char)0;
+}
+
+// createInsertion's coverage bookkeeping for position p; when `apply` the
+// reference counts at p+1 are adjusted (src/ToVarsBuilder.cpp:403-417).
+// Returns the updated total coverage.
+__device__ int insertion_pass(const DevState &st, const Region &R, int p, int tpc, const PosKeys &k, bool apply) {
+    for (int i = 0; i < k.n_ins; i++) {
+        const Slot &s = st.hash.slots[k.ins[i]];
+        int cnt = s.fwd + s.rev;
+        int ttcov = tpc;
+        if (cnt > tpc && s.extracnt != 0 && cnt - tpc < s.extracnt) ttcov = cnt;
+        if (ttcov < cnt) {
+            ttcov = cnt;
+            int p1 = p + 1;
+            if (p1 <= R.chi) {
+                int64_t c1 = cell_index(R, p1);
+                uint32_t cov1 = st.cells.cov[c1];
+                bool has1 = (p1 >= R.ws && p1 <= R.we);
+                if (cov1 != 0 && has1 && ttcov < (int)cov1 - cnt) {
+                    ttcov = (int)cov1;
+                    if (apply) {
+                        int b = base_index(ref_at(st, R, p1));
+                        uint8_t kf = st.cells.kflags[c1];
+                        if (b >= 0 && ((kf >> b) & 1) && !((kf >> (4 + b)) & 1)) {
+                            atomicSub(&st.cells.fwd[4 * c1 + b], (uint32_t)s.fwd);
+                            atomicSub(&st.cells.rev[4 * c1 + b], (uint32_t)s.rev);
+                        }
+                    }
+                }
+            }
+            tpc = ttcov;
+        }
+    }
+    return tpc;
+}
+
+// ToVarsBuilder visits a position when it has a nonInsertionVariants entry
+// with at least one key or an insertion, and nonzero coverage.
+__device__ bool visited(const DevState &st, const Region &R, int p, PosKeys &k) {
+    gather_keys(st, R, p, k);
+    if (!k.in_map) return false;
+    if (k.n_nonins == 0 && k.n_ins == 0) return false;
+    return st.cells.cov[cell_index(R, p)] != 0;
+}
+
+// Apply the insertion adjustments of every visited position (in ascending
+// position order semantics: a position's adjustment of p+1 is visible when
+// p+1 is scored).
+__global__ void k_ins_adjust(DevState st) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < st.cells.n_cells;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        if (st.head[t] == kNone) continue;
+        // region of cell t
+        int lo = 0, hi = st.n_regions - 1;
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (st.regions[mid].cell_base <= t) lo = mid; else hi = mid - 1;
+        }
+        const Region &R = st.regions[lo];
+        int p = R.clo + (int)(t - R.cell_base);
+        PosKeys k;
+        if (!visited(st, R, p, k) || k.n_ins == 0) continue;
+        sort_ins(st, k);
+        insertion_pass(st, R, p, (int)st.cells.cov[t], k, true);
+    }
+}
+
+__device__ double log_choose(int n, int k) {
+    return lgamma((double)n + 1.0) - lgamma((double)k + 1.0) - lgamma((double)(n - k) + 1.0);
+}
+
+// Two-sided Fisher exact test on (n11 n12; n21 n22) from the hypergeometric
+// definition: sum of table probabilities not above the observed one
+// (relative slack 1e-7 for ties).
+__device__ double fisher_two_sided(int n11, int n12, int n21, int n22) {
+    int r1 = n11 + n12, c1 = n11 + n21, n = n11 + n12 + n21 + n22;
+    int lo = r1 + c1 - n > 0 ? r1 + c1 - n : 0;
+    int hi = r1 < c1 ? r1 : c1;
+    if (n11 < 0 || n12 < 0 || n21 < 0 || n22 < 0 || lo >= hi) return 1.0;
+    double base = log_choose(n, c1);
+    double p_obs = exp(log_choose(r1, n11) + log_choose(n - r1, c1 - n11) - base);
+    double thr = p_obs * (1.0 + 1e-7);
+    double st = 0.0;
+    for (int x = lo; x <= hi; ++x) {
+        double p = exp(log_choose(r1, x) + log_choose(n - r1, c1 - x) - base);
+        if (p <= thr) st += p;
+    }
+    return st > 1.0 ? 1.0 : st;
+}
+
+__global__ void k_score(DevState st, DevParams P) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < st.n_score;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        int lo = 0, hi = st.n_regions - 1;
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (st.score_base[mid] <= t) lo = mid; else hi = mid - 1;
+        }
+        const Region &R = st.regions[lo];
+        int p = R.start + (int)(t - st.score_base[lo]);
+        if (p < R.clo || p > R.chi) continue;
+        PosKeys k;
+        if (!visited(st, R, p, k)) continue;
+        int64_t c = cell_index(R, p);
+        char rb = ref_at(st, R, p);
+        int rbi = base_index(rb);
+        bool hasp = p >= R.ws && p <= R.we;
+        // isTheSameVariationOnRef (src/ToVarsBuilder.cpp:213-233)
+        if (!P.do_pileup && k.n_nonins == 1 && k.n_ins == 0 && hasp && rbi >= 0 && k.single_mask == (1 << rbi))
+            continue;
+        int tpc = (int)st.cells.cov[c];
+        // calcHicov
+        int hicov = 0;
+        V vs[kMaxVars];
+        int nv = 0;
+        for (int b = 0; b < 4; b++) {
+            if (!((k.single_mask >> b) & 1)) continue;
+            int64_t g = 4 * c + b;
+            hicov += (int)st.cells.hi[g];
+        }
+        for (uint32_t s = st.head[c]; s != kNone; s = st.hash.slots[s].next) {
+            const Slot &sl = st.hash.slots[s];
+            if (!(sl.flags & SF_ERASED) && (sl.kind == KIND_NONINS || sl.kind == KIND_INS)) hicov += sl.hi;
+        }
+        // createVariant (non-insertion keys with a count)
+        for (int b = 0; b < 4; b++) {
+            if (!((k.single_mask >> b) & 1)) continue;
+            int64_t g = 4 * c + b;
+            V v;
+            v.kind = 0;
+            v.key = b;
+            v.fwd = (int)st.cells.fwd[g];
+            v.rev = (int)st.cells.rev[g];
+            v.cnt = v.fwd + v.rev;
+            if (v.cnt == 0) continue;
+            v.hi = (int)st.cells.hi[g];
+            v.lo = v.cnt - v.hi;
+            v.extracnt = 0;
+            v.tp = (double)(int)st.cells.tp[g];
+            v.q = (double)(int)st.cells.q[g];
+            v.mq = (double)(int)st.cells.mq[g];
+            v.nm = (double)st.cells.nm[g];
+            uint32_t f = st.cells.first[g];
+            v.pstd = (f & FCS_PDIFF) != 0;
+            v.qstd = (f & FCS_QDIFF) != 0;
+            finish_var(v, tpc, hicov, P);
+            if (nv < kMaxVars) vs[nv++] = v;
+        }
+        for (uint32_t s = st.head[c]; s != kNone; s = st.hash.slots[s].next) {
+            const Slot &sl = st.hash.slots[s];
+            if (sl.kind != KIND_NONINS || (sl.flags & SF_ERASED)) continue;
+            V v;
+            load_slot(sl, (int)s, v);
+            if (v.cnt == 0) continue;
+            int ttcov = tpc;
+            if (v.cnt > tpc && v.extracnt > 0 && v.cnt - tpc < v.extracnt) ttcov = v.cnt;
+            finish_var(v, ttcov, hicov, P);
+            if (nv < kMaxVars) vs[nv++] = v; else atomicOr(st.err, ERR_UNSUPPORTED);
+        }
+        // createInsertion
+        if (k.n_ins > 0) {
+            sort_ins(st, k);
+            int hic = hicov;
+            for (int i = 0; i < k.n_ins; i++) {
+                const Slot &sl = st.hash.slots[k.ins[i]];
+                V v;
+                load_slot(sl, (int)k.ins[i], v);
+                int ttcov = tpc;
+                if (v.cnt > tpc && v.extracnt != 0 && v.cnt - tpc < v.extracnt) ttcov = v.cnt;
+                if (ttcov < v.cnt) {
+                    ttcov = v.cnt;
+                    int p1 = p + 1;
+                    if (p1 <= R.chi) {
+                        uint32_t cov1 = st.cells.cov[cell_index(R, p1)];
+                        if (cov1 != 0 && p1 >= R.ws && p1 <= R.we && ttcov < (int)cov1 - v.cnt) ttcov = (int)cov1;
+                    }
+                    tpc = ttcov;
+                }
+                if (hic < v.hi) hic = v.hi;
+                finish_var(v, ttcov, hic, P);
+                if (nv < kMaxVars) vs[nv++] = v; else atomicOr(st.err, ERR_UNSUPPORTED);
+            }
+        }
+        // sort by CMP_VARI (insertion sort; few alleles per position)
+        for (int i = 1; i < nv; i++) {
+            V x = vs[i];
+            int j = i - 1;
+            while (j >= 0 && cmp_vari(st, x, vs[j])) { vs[j + 1] = vs[j]; j--; }
+            vs[j + 1] = x;
+        }
+        // collectVarsAtPosition: the reference allele is the single key equal to the reference base
+        int ref_i = -1;
+        double maxfreq = 0;
+        int n_var = 0;
+        for (int i = 0; i < nv; i++) {
+            if (hasp && vs[i].kind == 0 && vs[i].key == rbi) ref_i = i;
+            else { n_var++; if (vs[i].freq > maxfreq) maxfreq = vs[i].freq; }
+        }
+        if (!P.do_pileup && maxfreq <= P.freq) continue;
+        if (n_var == 0) continue;
+        // numeric pre-screen of isGoodVar: a necessary condition for emission
+        bool any = false;
+        for (int i = 0; i < nv; i++) {
+            if (i == ref_i) continue;
+            const V &v = vs[i];
+            if (v.freq >= P.freq && v.hi >= P.minr && v.pmean >= P.read_pos_filter && v.qual >= P.goodq &&
+                v.qratio >= P.qratio)
+                any = true;
+        }
+        if (!any && !P.do_pileup) continue;
+        // reference strand counts (collectReferenceVariants :730-760)
+        int rfc = 0, rrc = 0;
+        if (ref_i >= 0) { rfc = vs[ref_i].fwd; rrc = vs[ref_i].rev; }
+        if (tpc > (int)st.cells.cov[c] && p + 1 <= R.chi) {
+            int p1 = p + 1;
+            int64_t c1 = cell_index(R, p1);
+            char rb1 = ref_at(st, R, p1);
+            int b1 = base_index(rb1);
+            uint8_t kf1 = st.cells.kflags[c1];
+            if (p1 >= R.ws && p1 <= R.we && b1 >= 0 && ((kf1 >> b1) & 1) && !((kf1 >> (4 + b1)) & 1)) {
+                rfc = (int)st.cells.fwd[4 * c1 + b1];
+                rrc = (int)st.cells.rev[4 * c1 + b1];
+            }
+        }
+        unsigned int base = atomicAdd(st.n_cand, (unsigned int)nv);
+        if (base + nv > st.cand_cap) { atomicOr(st.err, ERR_HASH_FULL); continue; }
+        int rank = 0;
+        for (int i = 0; i < nv; i++) {
+            const V &v = vs[i];
+            CandVar &o = st.cand[base + i];
+            o.region = lo;
+            o.pos = p;
+            o.kind = (i == ref_i) ? 0 : 1;
+            o.rank = (i == ref_i) ? -1 : rank++;
+            if (v.kind == 0) { o.key_off = v.key; o.key_len = -1; }
+            else { const Slot &sl = st.hash.slots[v.key]; o.key_off = (int)sl.koff; o.key_len = sl.klen; }
+            int fwd = v.fwd < 0 ? 0 : v.fwd, rev = v.rev < 0 ? 0 : v.rev;
+            int rf = rfc < 0 ? 0 : rfc, rr = rrc < 0 ? 0 : rrc;
+            o.pc = v.cnt;
+            o.fwd = fwd;
+            o.rev = rev;
+            o.hicnt = v.hi;
+            o.hicov = v.hicov;
+            o.tpc = tpc;
+            o.rfc = rf;
+            o.rrc = rr;
+            o.bias = v.bias;
+            o.ref_bias = ref_i >= 0 ? vs[ref_i].bias : -1;
+            o.pstd = v.pstd;
+            o.qstd = v.qstd;
+            o.pass = (v.freq >= P.freq && v.hi >= P.minr && v.pmean >= P.read_pos_filter && v.qual >= P.goodq &&
+                      v.qratio >= P.qratio) ? 1 : 0;
+            o.nvars = nv;
+            o.freq = v.freq;
+            o.pmean = v.pmean;
+            o.qual = v.qual;
+            o.mq = v.mqv;
+            o.qratio = v.qratio;
+            o.hifreq = v.hifreq;
+            o.extrafreq = v.extrafreq;
+            o.nm = v.nmv;
+            if (P.fisher && o.kind == 1 && o.pass) {
+                o.fisher_p = fisher_two_sided(rf, rr, fwd, rev);
+                double ad = (double)(rf * rev), bc = (double)(rr * fwd);
+                o.fisher_ratio = (bc != 0 && ad != 0) ? (ad > bc ? ad / bc : bc / ad) : 0.0;
+            } else {
+                o.fisher_p = 0;
+                o.fisher_ratio = 0;
+            }
+        }
+    }
+}
+
+// Batched Fisher tests (rv_fisher_batch)
+__global__ void k_fisher(const int32_t *tab, int64_t n, double *p2, double *ratio) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int a = tab[4 * i], b = tab[4 * i + 1], c = tab[4 * i + 2], d = tab[4 * i + 3];
+        p2[i] = fisher_two_sided(a, b, c, d);
+        double ad = (double)a * d, bc = (double)b * c;
+        ratio[i] = (bc != 0 && ad != 0) ? (ad > bc ? ad / bc : bc / ad) : 0.0;
+    }
+}
+
+void launch_link(const DevState &st, cudaStream_t s) { k_link_slots<<<592, 256, 0, s>>>(st); }
+void launch_collisions(const DevState &st, cudaStream_t s) { k_check_collisions<<<592, 256, 0, s>>>(st); }
+void launch_ins_adjust(const DevState &st, cudaStream_t s) {
+    if (st.cells.n_cells > 0) k_ins_adjust<<<1216, 256, 0, s>>>(st);
+}
+void launch_score(const DevState &st, const DevParams &P, cudaStream_t s) {
+    if (st.n_score > 0) k_score<<<1216, 128, 0, s>>>(st, P);
+}
+void launch_fisher(const int32_t *tab, int64_t n, double *p2, double *ratio, cudaStream_t s) {
+    if (n > 0) k_fisher<<<(int)((n + 127) / 128 < 4096 ? (n + 127) / 128 : 4096), 128, 0, s>>>(tab, n, p2, ratio);
+}
+
+}  // namespace rv

@@ -1,0 +1,84 @@
+// Small data-movement kernels at the realigner boundary: compact the used
+// hash slots, gather cells for the host realigner, apply its patches.
+#include <cuda_runtime.h>
+
+#include "rv_ctx.h"
+
+namespace rv {
+
+__global__ void k_compact_slots(DevState st, uint32_t *out, unsigned int *n_out) {
+    unsigned long long n = st.hash.mask + 1ULL;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        if (st.hash.slots[i].fp != 0ULL) out[atomicAdd(n_out, 1u)] = (uint32_t)i;
+    }
+}
+
+__global__ void k_gather_slots(const Slot *slots, const uint32_t *idx, int64_t n, Slot *out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = slots[idx[i]];
+}
+
+__global__ void k_gather_cells(DevState st, const int64_t *cells, int64_t n, CellView *out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int64_t c = cells[i];
+        CellView v;
+        for (int b = 0; b < 4; b++) {
+            int64_t g = 4 * c + b;
+            v.fwd[b] = st.cells.fwd[g];
+            v.rev[b] = st.cells.rev[g];
+            v.hi[b] = st.cells.hi[g];
+            v.tp[b] = st.cells.tp[g];
+            v.q[b] = st.cells.q[g];
+            v.mq[b] = st.cells.mq[g];
+            v.nm[b] = st.cells.nm[g];
+            v.first[b] = st.cells.first[g];
+        }
+        v.cov = st.cells.cov[c];
+        v.kflags = st.cells.kflags[c];
+        out[i] = v;
+    }
+}
+
+// Patches are applied by one thread each; a slot or cell key is named by at
+// most one overwrite patch, and coverage additions use atomics.
+__global__ void k_apply_patches(DevState st, const Patch *p, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const Patch &q = p[i];
+        if (q.type == 0) {
+            Slot &s = st.hash.slots[q.target];
+            s.fwd = q.fwd;
+            s.rev = q.rev;
+            s.hi = q.hi;
+            s.lo = q.lo;
+            s.extracnt = q.extracnt;
+            s.tp_sum = q.tp_sum;
+            s.mq_sum = q.mq_sum;
+            s.nm_sum = q.nm_sum;
+            s.q_sum = q.q_sum;
+            s.flags |= (uint32_t)q.flags_or;
+        } else if (q.type == 1) {
+            atomicOr(&st.hash.slots[q.target].flags, SF_ERASED);
+        } else if (q.type == 2) {
+            int64_t c = q.target;
+            atomicOr((unsigned int *)&st.cells.kflags[c & ~3LL], 1u << (4 + q.base + 8 * (c & 3)));
+        } else if (q.type == 3) {
+            atomicAdd(&st.cells.cov[q.target], (uint32_t)q.cov_add);
+        }
+    }
+}
+
+void launch_compact_slots(const DevState &st, uint32_t *out, unsigned int *n_out, cudaStream_t s) {
+    k_compact_slots<<<592, 256, 0, s>>>(st, out, n_out);
+}
+void launch_gather_slots(const Slot *slots, const uint32_t *idx, int64_t n, Slot *out, cudaStream_t s) {
+    if (n > 0) k_gather_slots<<<(int)((n + 255) / 256 < 2048 ? (n + 255) / 256 : 2048), 256, 0, s>>>(slots, idx, n, out);
+}
+void launch_gather_cells(const DevState &st, const int64_t *cells, int64_t n, CellView *out, cudaStream_t s) {
+    if (n > 0) k_gather_cells<<<(int)((n + 127) / 128 < 2048 ? (n + 127) / 128 : 2048), 128, 0, s>>>(st, cells, n, out);
+}
+void launch_apply_patches(const DevState &st, const Patch *p, int64_t n, cudaStream_t s) {
+    if (n > 0) k_apply_patches<<<(int)((n + 127) / 128 < 2048 ? (n + 127) / 128 : 2048), 128, 0, s>>>(st, p, n);
+}
+
+}  // namespace rv

@@ -164,7 +164,7 @@ def simulate(genome: np.ndarray, variants: list[Variant], depth: float,
              softclip_frac: float = 0.02, mapq0_frac: float = 0.05,
              n_rate: float = 2e-4, span: tuple[int, int] | None = None,
              name_base: int = 0, artifact_rate: float = 0.0,
-             artifact_q: int | None = None) -> ReadSet:
+             artifact_q: int | None = None, tail_margin: int = 0) -> ReadSet:
     """Simulate coordinate-sorted 2x`read_len` pairs at `depth`x over
     `span` (default: the whole contig).  Each read independently carries
     each overlapping variant with probability vaf (strand-biased variants put
@@ -175,7 +175,7 @@ def simulate(genome: np.ndarray, variants: list[Variant], depth: float,
     n_frag = int(round(depth * (hi - lo) / (2 * L)))
     ins = np.clip(np.rint(rng.normal(insert_mean, insert_sd, n_frag)), L + 20, 3 * L).astype(np.int64)
     fstart = rng.integers(max(0, lo - L // 2), np.maximum(max(0, lo - L // 2) + 1, hi - ins + L // 2))
-    fstart = np.clip(fstart, 0, G - ins)
+    fstart = np.clip(fstart, 0, G - tail_margin - ins)
     r1_fwd = rng.random(n_frag) < 0.5
     # read A = leftmost (forward strand), read B = rightmost (reverse strand)
     startA = fstart
@@ -221,7 +221,7 @@ def simulate(genome: np.ndarray, variants: list[Variant], depth: float,
         else:
             # indel carriers need at least 3 aligned bases on each side
             off = v.pos - start[carry]
-            ok = (off >= 3) & (off + len(v.ref) <= L - 3)
+            ok = (off >= 3) & (off + len(v.ref) <= L - 3) & (start[carry] + L + len(v.ref) + 4 < G)
             for r in carry[ok].tolist():
                 carried_indels.setdefault(r, []).append(vi)
 
@@ -495,3 +495,13 @@ def somatic_pair(seed: int = 0x5EED0001, length: int = 1_000_000, tumor_depth: f
     tumor = simulate(g, germ + som + art, tumor_depth, rng, name_base=0)
     normal = simulate(g, germ, normal_depth, rng, name_base=10_000_000)
     return g, (germ, som, art), tumor, normal
+
+
+def dense_multi(seed: int = 0x5EED00D0, length: int = 60_000, depth: float = 60.0):
+    """A small contig with dense SNV/MNV/indel planting, more soft clips and
+    reads kept away from the contig end, for exercising every pileup path."""
+    rng = np.random.default_rng(seed)
+    g = make_genome(length, rng, homopolymer_rate=0.02)
+    vs = plant_variants(g, rng, 4e-3, 1e-3, lambda r: r.choice([0.2, 0.5, 1.0]), mnv_frac=0.2, spacing=12)
+    rs = simulate(g, vs, depth, rng, softclip_frac=0.06, n_rate=1e-3, tail_margin=300)
+    return g, vs, rs

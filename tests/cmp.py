@@ -1,0 +1,78 @@
+"""Comparison helpers for map dumps and records (shared by the tests)."""
+from __future__ import annotations
+
+# column index (0-based, tag first) of pp and pq in stat lines: the last-seen
+# read position / quality the reference keeps only to derive pstd/qstd
+STAT_SKIP = (14, 15)
+
+
+def parse(text: str) -> dict:
+    d: dict = {}
+    for ln in text.splitlines():
+        f = ln.split("\t")
+        d.setdefault(f[0], []).append(f)
+    return d
+
+
+def diff_dump(a_text: str, b_text: str, tags, skip=STAT_SKIP, rel=1e-6, key_cols=2):
+    """Compares two dumps tag by tag.  Integer fields must match exactly;
+    fields with a decimal point match within `rel` relative tolerance.
+    Returns a list of human-readable problems (empty = equal)."""
+    A, B = parse(a_text), parse(b_text)
+    problems = []
+    for t in tags:
+        a, b = A.get(t, []), B.get(t, [])
+        kk = (lambda x: tuple(x[1:1 + key_cols]))
+        ka = {kk(x): x for x in a}
+        kb = {kk(x): x for x in b}
+        miss = sorted(set(ka) - set(kb))[:5]
+        extra = sorted(set(kb) - set(ka))[:5]
+        if miss:
+            problems.append(f"{t}: {len(set(ka) - set(kb))} missing, e.g. {miss}")
+        if extra:
+            problems.append(f"{t}: {len(set(kb) - set(ka))} extra, e.g. {extra}")
+        nbad = 0
+        for k in set(ka) & set(kb):
+            x, y = ka[k], kb[k]
+            for i, (u, v) in enumerate(zip(x, y)):
+                if i in skip or u == v:
+                    continue
+                try:
+                    fu, fv = float(u), float(v)
+                    if ("." in u or "." in v or "e" in u or "e" in v) and abs(fu - fv) <= rel * max(1.0, abs(fu)):
+                        continue
+                except ValueError:
+                    pass
+                nbad += 1
+                if nbad <= 5:
+                    problems.append(f"{t} {k} col {i}: {u} != {v}")
+                break
+        if nbad > 5:
+            problems.append(f"{t}: {nbad} differing entries")
+    return problems
+
+
+def diff_records(ra: list[str], rb: list[str], rel=2e-6):
+    """Emitted record sets: same (start, ref, alt) keys, integer and string
+    columns equal, %f-formatted columns within rel (plus one unit in the
+    sixth decimal)."""
+    def key(f):
+        return (f[2], int(f[3]), f[5], f[6])
+    A = {key(l.split("\t")): l.split("\t") for l in ra if l}
+    B = {key(l.split("\t")): l.split("\t") for l in rb if l}
+    problems = []
+    if set(A) != set(B):
+        problems.append(f"record keys differ: missing {sorted(set(A) - set(B))[:5]} extra {sorted(set(B) - set(A))[:5]}")
+    for k in set(A) & set(B):
+        for i, (u, v) in enumerate(zip(A[k], B[k])):
+            if u == v:
+                continue
+            try:
+                fu, fv = float(u), float(v)
+                if "." in u and abs(fu - fv) <= rel * max(1.0, abs(fu)) + 1.5e-6:
+                    continue
+            except ValueError:
+                pass
+            problems.append(f"record {k} col {i}: {u} != {v}")
+            break
+    return problems
