@@ -1,0 +1,289 @@
+"""Benchmark: reads/s of pileup + variant scoring on one GB300.
+
+Workload (the somatic-pair shape the reference's metric is quoted on): a
+seeded synthetic 1 Mb contig, tumor 200x + normal 100x 2x150 bp pairs
+(~2.0 M reads), germline SNVs 1e-3/bp and indels 1e-4/bp in both samples,
+somatic SNV/MNV 2e-5/bp (VAF U(0.01, 0.5)) and strand-biased artifacts
+5e-6/bp in the tumor, called over 100 BED tiles of 10 kb with --fisher and
+-k 0, every sample through the full per-region path (record filters, CIGAR
+walk, allele maps, MNP realignment, site statistics, hard filter, Fisher
+test, record text).  One step = both samples, all regions.
+
+    value : reads/s with the read batches already resident in HBM
+    e2e   : reads/s through the C ABI from pinned host batches, including
+            the host->device copy of the reads and the device->host copy of
+            the scored candidates every step
+Inputs (~0.5 GB of reads) exceed the 129 MB L2, so no flush is needed
+between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+TILE = 10_000
+CONTIG = 1_000_000
+# algorithmic bytes per unit (the scope table's figures): per read
+# 4 pos + 4 n_cigar words + L/4 bases + L/8 N mask + L quals + 1 mapq + 2 flag
+# + 4 mpos + 1 NM; per covered site 256 B of count record; per string-keyed
+# allele 64 B; plus 1 B per reference base
+BYTES_PER_READ_FIXED = 4 + 1 + 2 + 4 + 1
+
+
+def read_alg_bytes(rs) -> float:
+    L = rs.l_qseq.astype(float)
+    return float((BYTES_PER_READ_FIXED + 4 * rs.n_cigar.astype(float) + L / 4 + L / 8 + L).sum())
+
+
+def make_workload(seed_offset: int = 0):
+    from rabbitvar_gb300 import synth
+    g, _, tumor, normal = synth.somatic_pair(seed=0x5EED0001 + seed_offset, length=CONTIG)
+    regions = [(1 + TILE * i, TILE * (i + 1)) for i in range(CONTIG // TILE)]
+    return g, tumor, normal, regions
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index: int = 0):
+        self.p = None
+        self.path = f"/tmp/rv_clocks_{os.getpid()}.csv"
+        try:
+            self.p = subprocess.Popen(
+                ["nvidia-smi", f"--id={index}",
+                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.p = None
+
+    def stop(self) -> dict:
+        if not self.p:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for ln in f:
+                c = [x.strip() for x in ln.split(",")]
+                if len(c) < 8:
+                    continue
+                try:
+                    sm.append(float(c[0]))
+                    mx.append(float(c[1]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, c[4:8]):
+                    if v.lower() == "active":
+                        reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def dist_init():
+    n = int(os.environ.get("WORLD_SIZE", "1"))
+    if n <= 1:
+        return 0, 1, None
+    import torch.distributed as dist
+    backend = "nccl"
+    try:
+        import torch
+        if not torch.cuda.is_available():
+            backend = "gloo"
+    except ImportError:
+        backend = "gloo"
+    dist.init_process_group(backend)
+    return dist.get_rank(), dist.get_world_size(), dist
+
+
+def barrier_max(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    if dist.get_backend() == "nccl":
+        t = t.cuda()
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_baseline_run(g, samples, regions, threads: int, n_regions: int):
+    """The oracle's CPU restatement of the path (OpenMP over regions) on a
+    bounded sample of the workload's regions; returns reads/s."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    import numpy as np
+    p = O.default_params(local_realign=0, fisher=1)
+    sub = regions[:n_regions]
+    lo, hi = sub[0][0], sub[-1][1]
+    reads = 0
+    t0 = time.perf_counter()
+    for rs in samples:
+        O.run_regions(rs, g, sub, params=p, threads=threads)
+        reads += int(((rs.pos >= lo - 1) & (rs.pos < hi)).sum())
+    dt = time.perf_counter() - t0
+    return reads / dt, dt, reads
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    g, tumor, normal, regions = make_workload()
+    threads = os.cpu_count() or 1
+    n_reg = 8
+    vals = []
+    for _ in range(args.warmup):
+        cpu_baseline_run(g, [tumor, normal], regions, threads, n_reg)
+    for _ in range(args.steps):
+        v, dt, nr = cpu_baseline_run(g, [tumor, normal], regions, threads, n_reg)
+        vals.append(v)
+    v = statistics.median(vals)
+    out = {"impl": "reference", "metric": "reads/s pileup+var scoring (somatic pair 1 Mb, T200x+N100x)",
+           "value": v, "unit": "reads/s", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+           "higher_is_better": True, "data": "synthetic",
+           "config": {"workload": "somatic pair 1 Mb contig, tumor 200x + normal 100x 2x150, 100 x 10 kb BED tiles, --fisher, -k 0",
+                      "sample": f"first {n_reg} of 100 tiles, both samples"},
+           "cpu_baseline": {"value": v, "unit": "reads/s", "cores": threads, "kind": "port",
+                            "sample": f"first {n_reg} of 100 10-kb tiles, tumor+normal, per step"},
+           "e2e": {"value": v, "unit": "reads/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank, world, dist = dist_init()
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+    import numpy as np
+    from rabbitvar_gb300 import api, synth
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    g, tumor, normal, regions = make_workload(seed_offset=rank)
+    samples = [("T", tumor), ("N", normal)]
+    params = api.default_params(local_realign=0, fisher=1)
+    ctxs, batches = [], []
+    for name, rs in samples:
+        c = api.Context(params, device=local)
+        c.upload_reference(rs.contig, synth.genome_str(g).encode())
+        ctxs.append(c)
+        batches.append(api.Batch.from_readset(rs, pinned=True))
+    n_reads = sum(rs.n for _, rs in samples)
+    alg_read_bytes = sum(read_alg_bytes(rs) for _, rs in samples)
+
+    def device_step(collect=None):
+        kernels = 0
+        recs = 0
+        for c in ctxs:
+            c.pileup()
+            c.realign()
+            c.score()
+            text, n = c.format_records("S", "ctg")
+            recs += n
+            kernels += c.timings()["kernels"]
+            if collect is not None:
+                collect.append(c.stage_times())
+        return kernels, recs
+
+    def e2e_step():
+        kernels = 0
+        recs = 0
+        for c, b in zip(ctxs, batches):
+            c.submit(b, regions)
+            c.pileup()
+            c.realign()
+            c.score()
+            text, n = c.format_records("S", "ctg")
+            recs += n
+            kernels += c.timings()["kernels"]
+        return kernels, recs
+
+    # e2e: pinned host batch -> device every step
+    for _ in range(args.warmup):
+        e2e_step()
+    clocks = Clocks(local)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    e2e_dt = barrier_max(dist, time.perf_counter() - t0)
+    # value: reads resident on the device (submitted once above), device-side steps
+    for _ in range(args.warmup):
+        device_step()
+    stages = []
+    t0 = time.perf_counter()
+    kernels = 0
+    recs = 0
+    for _ in range(args.steps):
+        k, recs = device_step(stages)
+        kernels += k
+    dev_dt = barrier_max(dist, time.perf_counter() - t0)
+    clk = clocks.stop()
+    ms_per_step = dev_dt / args.steps * 1e3
+    value = n_reads * world * args.steps / dev_dt
+    e2e = n_reads * world * args.steps / e2e_dt
+    # roofline of the dominant kernel (pileup tiles), event-timed per launch
+    tile_ms = statistics.mean(s["pileup_tiles"] for s in stages)  # per sample launch
+    per_launch_bytes = alg_read_bytes / len(samples)
+    cells = sum(r[1] - r[0] + 1 for r in regions)
+    per_launch_bytes += cells * 256 + CONTIG  # site records + reference window
+    achieved = per_launch_bytes / (tile_ms * 1e-3) / 1e9
+    peak, peak_kind = measured_peak_hbm()
+    h2d = sum(b.nbytes for b in batches)
+    out = {
+        "metric": "reads/s pileup+var scoring (somatic pair 1 Mb, T200x+N100x)",
+        "value": value, "unit": "reads/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "int32/fp64", "data": "synthetic (seeded)",
+        "config": {"workload": "somatic pair 1 Mb contig, tumor 200x + normal 100x 2x150, 100 x 10 kb BED tiles, --fisher, -k 0",
+                   "reads_per_step": n_reads * world, "l2": "inputs (~0.5 GB) larger than L2, no flush",
+                   "records_per_step": recs},
+        "e2e": {"value": e2e, "unit": "reads/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": None},
+        "gpu_launches": kernels,
+        "stage_ms": {k: statistics.mean(s[k] for s in stages) for k in stages[0]},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+                     "kernel": "k_pileup_tiles", "alg_bytes_per_launch": per_launch_bytes},
+        "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        v, dt, nr = cpu_baseline_run(g, [tumor, normal], regions, 1, 2)
+        out["cpu_baseline"] = {"value": v, "unit": "reads/s", "cores": 1, "kind": "port",
+                               "sample": f"first 2 of 100 10-kb tiles, tumor+normal ({nr} reads, {dt:.1f} s)"}
+    if rank == 0:
+        print(json.dumps(out))
+    for c in ctxs:
+        c.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -168,6 +168,13 @@ rv_status rv_export_maps(rv_ctx *ctx, int region, const char *stages, const char
 rv_status rv_last_timings(const rv_ctx *ctx, double *pileup_ms, double *score_ms, double *total_ms,
                           int64_t *kernels);
 
+/* Device time (ms, CUDA events on the launch stream) of the last rv_pileup /
+ * rv_score calls by stage:
+ * stages: [0] cell/table reset, [1] region spans, [2] pileup tiles,
+ * [3] in-order edge walk, [4] deferred subtraction + list linking +
+ * collision check, [5] insertion coverage adjustment, [6] site scoring. */
+rv_status rv_stage_times(const rv_ctx *ctx, double *ms, int n);
+
 /* Fisher exact test on the device for n tables (a,b,c,d) stored as 4*n int32;
  * writes two-sided p and the simple-mode ratio. Replaces the kt_fisher_exact
  * call sites (src/modes/simpleMode.cpp:96-108). */

@@ -60,7 +60,7 @@ class SiteRecord(C.Structure):
 
 EXPORTS = ["rv_default_params", "rv_create", "rv_destroy", "rv_last_error", "rv_upload_reference",
            "rv_submit_batch", "rv_pileup", "rv_realign", "rv_score", "rv_format_records", "rv_fetch_records",
-           "rv_call_regions", "rv_export_maps", "rv_last_timings", "rv_fisher_batch", "rv_bam_read",
+           "rv_call_regions", "rv_export_maps", "rv_last_timings", "rv_stage_times", "rv_fisher_batch", "rv_bam_read",
            "rv_bam_contigs", "rv_bam_batch", "rv_bam_free", "rv_fasta_read", "rv_free", "rv_alloc_pinned",
            "rv_free_pinned"]
 
@@ -94,6 +94,7 @@ def lib():
     L.rv_last_timings.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double),
                                   C.POINTER(i64)]
     L.rv_fisher_batch.argtypes = [vp, vp, i64, vp, vp]
+    L.rv_stage_times.argtypes = [vp, vp, C.c_int]
     L.rv_bam_read.argtypes = [C.c_char_p, C.c_int, C.POINTER(vp)]
     L.rv_bam_contigs.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(vp), C.POINTER(vp)]
     L.rv_bam_batch.argtypes = [vp, C.c_int, C.POINTER(ReadBatch)]
@@ -247,6 +248,13 @@ class Context:
         k = C.c_int64()
         self._check(self.L.rv_last_timings(self.h, C.byref(a), C.byref(b), C.byref(c), C.byref(k)))
         return dict(pileup_ms=a.value, score_ms=b.value, total_ms=c.value, kernels=k.value)
+
+    STAGES = ["reset", "region_spans", "pileup_tiles", "edge_walk", "deferred_link_check", "ins_adjust", "score"]
+
+    def stage_times(self) -> dict:
+        ms = np.zeros(8)
+        self._check(self.L.rv_stage_times(self.h, ms.ctypes.data, 8))
+        return {k: float(ms[i]) for i, k in enumerate(self.STAGES)}
 
     def fisher(self, tables: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
         t = np.ascontiguousarray(tables, dtype=np.int32).reshape(-1, 4)

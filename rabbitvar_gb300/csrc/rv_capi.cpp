@@ -127,7 +127,7 @@ rv_status rv_create(rv_ctx **out, const rv_params *p, int device, size_t hbm_bud
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
-    for (int i = 0; e == cudaSuccess && i < 6; i++) e = cudaEventCreate(&ctx->ev[i]);
+    for (int i = 0; e == cudaSuccess && i < 12; i++) e = cudaEventCreate(&ctx->ev[i]);
     if (e == cudaSuccess) e = cudaMalloc((void **)&ctx->d_counters, 64 * sizeof(unsigned int));
     if (e != cudaSuccess) {
         ctx->err = cudaGetErrorString(e);
@@ -180,7 +180,7 @@ void rv_destroy(rv_ctx *ctx) {
                     ctx->d_arena, ctx->d_deferred, ctx->d_cand, ctx->d_counters};
     for (void *p : ptrs)
         if (p) cudaFree(p);
-    for (int i = 0; i < 6; i++)
+    for (int i = 0; i < 12; i++)
         if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -396,11 +396,15 @@ rv_status rv_pileup(rv_ctx *ctx, void *stream) {
     RV_CUDA(cudaMemsetAsync(ctx->d_arena, 0, 16, s));
     launch_init_slots(ctx->d_slots, ctx->hash_cap, s);
     DevState st = ctx->state();
+    RV_CUDA(cudaEventRecord(ctx->ev[4], s));
     launch_region_spans(st, s);
+    RV_CUDA(cudaEventRecord(ctx->ev[5], s));
     int per_sm = std::max(1, pileup_blocks_per_sm());
     int grid = std::max(1, std::min<int>((int)ctx->tiles.size(), per_sm * ctx->sm_count));
     RV_CUDA(launch_pileup(st, ctx->dp, grid, s));
+    RV_CUDA(cudaEventRecord(ctx->ev[6], s));
     launch_serial(st, ctx->dp, s);
+    RV_CUDA(cudaEventRecord(ctx->ev[7], s));
     launch_resolve(st, ctx->dp, s);
     launch_link(st, s);
     launch_collisions(st, s);
@@ -413,6 +417,14 @@ rv_status rv_pileup(rv_ctx *ctx, void *stream) {
     float ms = 0;
     cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
     ctx->pileup_ms = ms;
+    const int marks[5] = {0, 4, 5, 6, 7};
+    for (int k = 0; k < 4; k++) {
+        float m = 0;
+        cudaEventElapsedTime(&m, ctx->ev[marks[k]], ctx->ev[marks[k + 1]]);
+        ctx->stage_ms[k] = m;
+    }
+    cudaEventElapsedTime(&ms, ctx->ev[7], ctx->ev[1]);
+    ctx->stage_ms[4] = ms;
     if (err) {
         char buf[160];
         snprintf(buf, sizeof buf, "pileup device error bits 0x%x", err);
@@ -445,6 +457,7 @@ rv_status rv_score(rv_ctx *ctx, void *stream) {
     RV_CUDA(cudaEventRecord(ctx->ev[2], s));
     RV_CUDA(cudaMemsetAsync(ctx->d_counters + CNT_CAND, 0, 4, s));
     launch_ins_adjust(st, s);
+    RV_CUDA(cudaEventRecord(ctx->ev[8], s));
     launch_score(st, ctx->dp, s);
     RV_CUDA(cudaGetLastError());
     RV_CUDA(cudaEventRecord(ctx->ev[3], s));
@@ -454,6 +467,10 @@ rv_status rv_score(rv_ctx *ctx, void *stream) {
     float ms = 0;
     cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]);
     ctx->score_ms = ms;
+    cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[8]);
+    ctx->stage_ms[5] = ms;
+    cudaEventElapsedTime(&ms, ctx->ev[8], ctx->ev[3]);
+    ctx->stage_ms[6] = ms;
     ctx->kernels += 2;
     unsigned int n = hdr[CNT_CAND];
     if (n > ctx->cand_cap) {
@@ -525,6 +542,12 @@ rv_status rv_last_timings(const rv_ctx *ctx, double *pileup_ms, double *score_ms
     if (score_ms) *score_ms = ctx->score_ms;
     if (total_ms) *total_ms = ctx->pileup_ms + ctx->score_ms;
     if (kernels) *kernels = ctx->kernels;
+    return RV_OK;
+}
+
+rv_status rv_stage_times(const rv_ctx *ctx, double *ms, int n) {
+    if (!ctx || !ms || n < 0) return RV_ERR_ARG;
+    for (int i = 0; i < n && i < 8; i++) ms[i] = ctx->stage_ms[i];
     return RV_OK;
 }
 

@@ -123,8 +123,9 @@ struct rv_ctx {
 
     // stage
     int stage = 0;  // 0 none, 1 submitted, 2 piled up, 3 realigned, 4 scored
-    cudaEvent_t ev[6] = {};
+    cudaEvent_t ev[12] = {};
     double pileup_ms = 0, score_ms = 0, total_ms = 0;
+    double stage_ms[8] = {};
     int64_t kernels = 0;
 
     rv::DevState state() const;

@@ -205,7 +205,11 @@ struct TileSink : SinkBase {
     uint32_t *first;
     int wlo;
     __device__ bool phantom(int) const { return false; }
-    __device__ void touch_phantom(int) { error(ERR_UNSUPPORTED); }
+    // Positions below 1 never get queried by the walk; above the window only
+    // edge reads (handled in order by k_pileup_edge) can reach.
+    __device__ void touch_phantom(int p) {
+        if (p >= 1) error(ERR_UNSUPPORTED);
+    }
     __device__ void single(int p, int b, const Obs &o, int64_t) {
         int d = p - wlo;
         int qi = (int)o.q;
@@ -264,13 +268,21 @@ struct SerialSink : SinkBase {
     __device__ void single(int p, int b, const Obs &o, int64_t) {
         cell_obs_global(st->cells, *R, st->err, p, b, o, P->goodq);
     }
-    __device__ void subtract(int p, int b, int dir, int tp, int q, int mapq, int nm, int64_t, int) {
-        if (p < R->clo || p > R->chi) return;
-        int64_t c = cell_of(*R, p);
-        uint32_t kf = st->cells.kflags[c];
-        if (kf & (1u << b)) apply_subtract(st->cells, *R, st->err, p, b, dir, tp, q, mapq, nm, P->goodq);
+    // existence of the key is decided in read order by k_resolve_deferred
+    __device__ void subtract(int p, int b, int dir, int tp, int q, int mapq, int nm, int64_t read, int ci) {
+        unsigned int k = atomicAdd(st->n_deferred, 1u);
+        if (k >= st->deferred_cap) { error(ERR_DEFER_FULL); return; }
+        Deferred &d = st->deferred[k];
+        d.region = region_idx; d.pos = p; d.read = read; d.ci = ci; d.base = b;
+        d.dir = dir; d.tp = tp; d.q = q; d.mapq = mapq; d.nm = nm; d.pad = 0;
     }
 };
+
+// A read is an edge read when its walk may look up reference positions past
+// the loaded window (the reference's map then inserts 0 entries that later
+// lookups see); edge reads of a region are walked in file order by one thread.
+constexpr int kEdgeMargin = 8;
+__device__ __forceinline__ bool is_edge(const Region &R, int span_hi) { return span_hi + kEdgeMargin > R.we; }
 
 // Probe sink: reports whether the walked read creates key (pos, base) before
 // it reaches the insertion (read, ci) that asked.
@@ -358,7 +370,7 @@ __global__ void k_region_spans(DevState st) {
         R.span_lo = lo;
         R.span_hi = hi;
         // reads that can reach outside the reference window take the in-order path
-        R.serial = (R.r1 > R.r0) && (hi + 2 > R.we || lo - 2 < R.ws) ? 1 : 0;
+        R.serial = (R.r1 > R.r0) && is_edge(R, hi) ? 1 : 0;
         if (R.r1 > R.r0 && (lo < R.clo || hi > R.chi)) set_err(st.err, ERR_CELL_RANGE);
     }
 }
@@ -381,11 +393,10 @@ __global__ void __launch_bounds__(kPileupThreads) k_pileup_tiles(DevState st, De
         if (t >= st.n_tiles) return;
         const Tile tile = st.tiles[t];
         const Region &R = st.regions[tile.region];
-        if (R.serial) { __syncthreads(); continue; }
         for (int64_t r = tile.r0 + threadIdx.x; r < tile.r1; r += blockDim.x) {
             int a, b;
             read_span(st.batch, r, a, b);
-            atomicMin(&s_wlo, a);
+            if (!is_edge(R, b)) atomicMin(&s_wlo, a);
         }
         for (int i = threadIdx.x; i < 4 * TW; i += blockDim.x) {
             cnt[i] = 0ULL;
@@ -409,6 +420,11 @@ __global__ void __launch_bounds__(kPileupThreads) k_pileup_tiles(DevState st, De
             Walker<TileSink> w(P, sink, R, st.ref, st.ref_len);
             for (int64_t r = tile.r0 + threadIdx.x; r < tile.r1; r += blockDim.x) {
                 if (!read_passes(st.batch, P, R, r)) continue;
+                if (R.serial) {
+                    int a, b;
+                    read_span(st.batch, r, a, b);
+                    if (is_edge(R, b)) continue;
+                }
                 w.walk(st.batch, r);
             }
         }
@@ -442,7 +458,7 @@ __global__ void __launch_bounds__(kPileupThreads) k_pileup_tiles(DevState st, De
     }
 }
 
-// One block per region; thread 0 walks the serial regions' reads in order.
+// One block per region with edge reads; thread 0 walks them in file order.
 __global__ void k_pileup_serial(DevState st, DevParams P) {
     int reg = blockIdx.x;
     if (reg >= st.n_regions) return;
@@ -460,8 +476,20 @@ __global__ void k_pileup_serial(DevState st, DevParams P) {
     sink.ph_hi = ph_hi;
     sink.ph_lo = ph_lo;
     Walker<SerialSink> w(P, sink, R, st.ref, st.ref_len);
-    for (int64_t r = R.r0; r < R.r1; r++) {
+    // edge reads start within kEdgeGuard of the window end (reads are
+    // coordinate sorted); find the first candidate by binary search
+    const int kEdgeGuard = 4096;
+    int64_t lo = R.r0, hi = R.r1;
+    while (lo < hi) {
+        int64_t mid = (lo + hi) / 2;
+        if (st.batch.pos[mid] + 1 + kEdgeGuard < R.we) lo = mid + 1; else hi = mid;
+    }
+    for (int64_t r = lo; r < R.r1; r++) {
         if (!read_passes(st.batch, P, R, r)) continue;
+        int a, b;
+        read_span(st.batch, r, a, b);
+        if (!is_edge(R, b)) continue;
+        if (b - (st.batch.pos[r] + 1) > kEdgeGuard) { sink.error(ERR_UNSUPPORTED); continue; }
         w.walk(st.batch, r);
     }
 }

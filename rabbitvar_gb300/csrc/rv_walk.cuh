@@ -231,7 +231,9 @@ struct Walker {
                         char kb[3];
                         int idx_ = cel - 1 - si;
                         kb[0] = (char)(idx_ & 0xff); kb[1] = (char)(idx_ >> 8); kb[2] = rv.base(si);
-                        S.event(KIND_SC5_SEQ, start, kb, 3, plain_obs(dir, si - (cel - nhq), rv.q(si), mapq, nom), read_idx);
+                        Obs so = plain_obs(dir, si - (cel - nhq), rv.q(si), mapq, nom);
+                        so.creates = true;  // Sclip.nt[idx][ch] counts every observation
+                        S.event(KIND_SC5_SEQ, start, kb, 3, so, read_idx);
                     }
                     Obs a = plain_obs(dir, cel, 0, mapq, nom);
                     a.q = sumq / (double)nhq;
@@ -261,7 +263,9 @@ struct Walker {
                     for (int si = 0; si < nhq; si++) {
                         char kb[3];
                         kb[0] = (char)(si & 0xff); kb[1] = (char)(si >> 8); kb[2] = rv.base(rpis + si);
-                        S.event(KIND_SC3_SEQ, start, kb, 3, plain_obs(dir, nhq - si, rv.q(rpis + si), mapq, nom), read_idx);
+                        Obs so = plain_obs(dir, nhq - si, rv.q(rpis + si), mapq, nom);
+                        so.creates = true;
+                        S.event(KIND_SC3_SEQ, start, kb, 3, so, read_idx);
                     }
                     Obs a = plain_obs(dir, cel, 0, mapq, nom);
                     a.q = sumq / (double)nhq;
