@@ -292,7 +292,7 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
         if (nr > 0) {
             double dens = nr / (double)(R.end - R.start + 1 + 2 * max_lq);
             double usable = (double)kTileW - max_span - 2.0 * max_lq - 16.0;
-            int64_t tr = (int64_t)std::max(32.0, std::min(1024.0, usable * dens));
+            int64_t tr = (int64_t)std::max(32.0, std::min((double)kTileReads, usable * dens));
             for (int64_t a = R.r0; a < R.r1; a += tr) {
                 Tile t;
                 t.region = r;
@@ -398,6 +398,7 @@ rv_status rv_pileup(rv_ctx *ctx, void *stream) {
     DevState st = ctx->state();
     RV_CUDA(cudaEventRecord(ctx->ev[4], s));
     launch_region_spans(st, s);
+    launch_edge_detect(st, ctx->dp, s);
     RV_CUDA(cudaEventRecord(ctx->ev[5], s));
     int per_sm = std::max(1, pileup_blocks_per_sm());
     int grid = std::max(1, std::min<int>((int)ctx->tiles.size(), per_sm * ctx->sm_count));

@@ -14,6 +14,7 @@ void launch_init_slots(Slot *slots, unsigned long long n, cudaStream_t s);
 void launch_region_spans(const DevState &st, cudaStream_t s);
 cudaError_t launch_pileup(const DevState &st, const DevParams &P, int grid, cudaStream_t s);
 void launch_serial(const DevState &st, const DevParams &P, cudaStream_t s);
+void launch_edge_detect(const DevState &st, const DevParams &P, cudaStream_t s);
 void launch_resolve(const DevState &st, const DevParams &P, cudaStream_t s);
 int pileup_blocks_per_sm();
 size_t pileup_smem_bytes();

@@ -196,34 +196,63 @@ struct SinkBase {
     __device__ void max_len(int tlen) { atomicMax((int *)&R->max_read_len, tlen); }
 };
 
+// Tile-histogram packing of one (position, base) cell in shared memory:
+//   cnt : fwd (bits 0-11) | rev (12-23) | hi (24-35) | nm + 128 (36-63)
+//   sums: tp (0-20) | q (21-41) | mapq (42-63)
+// valid for tiles of at most kTileReads reads (one observation per read and
+// position), tp and q in 1..1023, mapq <= 255, nm in -128..127; anything else
+// goes straight to the global cells.
+
+struct TileFast {
+    unsigned long long *cnt, *sums;
+    uint32_t *first;
+    int wlo;
+    double goodq;
+    __device__ __forceinline__ bool emit(int p, int b, int dir, int tp, int q, int mapq, int nm) const {
+        return emit_any(p, b, dir, tp, q, mapq, nm, true);
+    }
+    // std_rel: the observation takes part in pstd/qstd (M-op bases do, the
+    // soft-clip re-alignment counts do not)
+    __device__ __forceinline__ bool emit_any(int p, int b, int dir, int tp, int q, int mapq, int nm, bool std_rel) const {
+        unsigned d = (unsigned)(p - wlo);
+        if (d >= (unsigned)kTileW || (unsigned)(tp - 1) > 1022u || (unsigned)(q - 1) > 1022u || (unsigned)mapq > 255u ||
+            (unsigned)(nm + 128) > 255u)
+            return false;
+        int ix = 4 * (int)d + b;
+        atomicAdd(&cnt[ix], (dir ? (1ULL << 12) : 1ULL) + (q >= goodq ? (1ULL << 24) : 0ULL) +
+                                ((unsigned long long)(nm + 128) << 36));
+        atomicAdd(&sums[ix], (unsigned long long)tp | ((unsigned long long)q << 21) | ((unsigned long long)mapq << 42));
+        if (!std_rel) return true;
+        const uint32_t v = (uint32_t)tp | ((uint32_t)q << 12);
+        const uint32_t f = first[ix];
+        const uint32_t fv = f & FC_VAL;
+        if (fv == 0u) {
+            first_merge(&first[ix], v, 0u);
+        } else {
+            uint32_t need = 0u;
+            if (!(f & FC_PDIFF) && (fv & 0xFFFu) != (v & 0xFFFu)) need |= FC_PDIFF;
+            if (!(f & FC_QDIFF) && (fv >> 12) != (v >> 12)) need |= FC_QDIFF;
+            if (need) atomicOr(&first[ix], need);
+        }
+        return true;
+    }
+};
+
 // Tile sink: A/C/G/T observations inside [wlo, wlo + kTileW) accumulate in
 // shared memory; subtractions are deferred.
 struct TileSink : SinkBase {
-    unsigned long long *cnt;   // fwd (21) | rev (21) | hi (22)
-    unsigned long long *sums;  // tp (21) | q (21) | mapq (22)
-    int *nmv;
-    uint32_t *first;
-    int wlo;
+    TileFast f;
+    using Fast = TileFast;
+    __device__ Fast fast() const { return f; }
     __device__ bool phantom(int) const { return false; }
     // Positions below 1 never get queried by the walk; above the window only
-    // edge reads (handled in order by k_pileup_edge) can reach.
+    // edge reads of regions marked for the in-order walk can reach.
     __device__ void touch_phantom(int p) {
         if (p >= 1) error(ERR_UNSUPPORTED);
     }
     __device__ void single(int p, int b, const Obs &o, int64_t) {
-        int d = p - wlo;
-        int qi = (int)o.q;
-        if (d >= 0 && d < kTileW && o.tp >= 1 && o.tp < 1024 && qi >= 1 && qi < 1024 && o.mapq < 256) {
-            int ix = 4 * d + b;
-            unsigned long long cv = (o.dir ? (1ULL << 21) : 1ULL) + (o.q >= P->goodq ? (1ULL << 42) : 0ULL);
-            atomicAdd(&cnt[ix], cv);
-            atomicAdd(&sums[ix], (unsigned long long)o.tp | ((unsigned long long)qi << 21) |
-                                     ((unsigned long long)o.mapq << 42));
-            atomicAdd(&nmv[ix], o.nm);
-            if (o.std_rel) first_merge(&first[ix], (uint32_t)o.tp | ((uint32_t)qi << 12), 0u);
-        } else {
-            cell_obs_global(st->cells, *R, st->err, p, b, o, P->goodq);
-        }
+        if (f.emit_any(p, b, o.dir, o.tp, (int)o.q, o.mapq, o.nm, o.std_rel)) return;
+        cell_obs_global(st->cells, *R, st->err, p, b, o, P->goodq);
     }
     __device__ void subtract(int p, int b, int dir, int tp, int q, int mapq, int nm, int64_t read, int ci) {
         unsigned int k = atomicAdd(st->n_deferred, 1u);
@@ -248,6 +277,8 @@ __device__ void apply_subtract(const Cells &C, const Region &R, unsigned int *er
 
 // In-order sink for the exact serial walker.
 struct SerialSink : SinkBase {
+    using Fast = NoFast;
+    __device__ Fast fast() const { return Fast(); }
     uint32_t *ph_hi;   // bitmap of inserted positions above the window
     uint32_t *ph_lo;   // bitmap of inserted positions below the window
     static constexpr int kPh = 4096;
@@ -287,6 +318,8 @@ __device__ __forceinline__ bool is_edge(const Region &R, int span_hi) { return s
 // Probe sink: reports whether the walked read creates key (pos, base) before
 // it reaches the insertion (read, ci) that asked.
 struct ProbeSink {
+    using Fast = NoFast;
+    __device__ Fast fast() const { return Fast(); }
     const Region *R;
     int pos, base;
     int64_t stop_read;
@@ -304,6 +337,26 @@ struct ProbeSink {
     __device__ void subtract(int, int, int, int, int, int, int, int64_t read, int ci) {
         if (read == stop_read && ci == stop_ci) stopped = true;
     }
+};
+
+// Detection sink for edge reads: records whether the walk would insert a
+// 0 entry past the reference window (the only way the in-order semantics can
+// differ from a parallel walk); produces nothing else.
+struct DetectSink {
+    using Fast = NoFast;
+    __device__ Fast fast() const { return Fast(); }
+    const Region *R;
+    int *hit;
+    __device__ bool phantom(int) const { return false; }
+    __device__ void touch_phantom(int p) {
+        if (p > R->we) atomicExch(hit, 1);
+    }
+    __device__ void error(unsigned int) {}
+    __device__ void cov(int, int) {}
+    __device__ void event(int, int, const char *, int, const Obs &, int64_t) {}
+    __device__ void max_len(int) {}
+    __device__ void single(int, int, const Obs &, int64_t) {}
+    __device__ void subtract(int, int, int, int, int, int, int, int64_t, int) {}
 };
 
 // Record filters of next_record (src/recordPreprocessor.cpp:101-180) plus the
@@ -380,8 +433,7 @@ __global__ void __launch_bounds__(kPileupThreads) k_pileup_tiles(DevState st, De
     extern __shared__ __align__(16) unsigned char smem[];
     unsigned long long *cnt = (unsigned long long *)smem;
     unsigned long long *sums = cnt + 4 * TW;
-    int *nmv = (int *)(sums + 4 * TW);
-    uint32_t *first = (uint32_t *)(nmv + 4 * TW);
+    uint32_t *first = (uint32_t *)(sums + 4 * TW);
     __shared__ int s_tile, s_wlo;
     for (;;) {
         if (threadIdx.x == 0) {
@@ -401,7 +453,6 @@ __global__ void __launch_bounds__(kPileupThreads) k_pileup_tiles(DevState st, De
         for (int i = threadIdx.x; i < 4 * TW; i += blockDim.x) {
             cnt[i] = 0ULL;
             sums[i] = 0ULL;
-            nmv[i] = 0;
             first[i] = 0u;
         }
         __syncthreads();
@@ -411,11 +462,11 @@ __global__ void __launch_bounds__(kPileupThreads) k_pileup_tiles(DevState st, De
         sink.P = &P;
         sink.R = &R;
         sink.region_idx = tile.region;
-        sink.cnt = cnt;
-        sink.sums = sums;
-        sink.nmv = nmv;
-        sink.first = first;
-        sink.wlo = wlo;
+        sink.f.cnt = cnt;
+        sink.f.sums = sums;
+        sink.f.first = first;
+        sink.f.wlo = wlo;
+        sink.f.goodq = P.goodq;
         {
             Walker<TileSink> w(P, sink, R, st.ref, st.ref_len);
             for (int64_t r = tile.r0 + threadIdx.x; r < tile.r1; r += blockDim.x) {
@@ -439,8 +490,9 @@ __global__ void __launch_bounds__(kPileupThreads) k_pileup_tiles(DevState st, De
             if (p > R.chi) { set_err(st.err, ERR_CELL_RANGE); continue; }
             int64_t cell = cell_of(R, p);
             int64_t g = 4 * cell + b;
-            uint32_t f = (uint32_t)(c & 0x1FFFFFULL), rv_ = (uint32_t)((c >> 21) & 0x1FFFFFULL);
-            uint32_t h = (uint32_t)(c >> 42);
+            uint32_t f = (uint32_t)(c & 0xFFFULL), rv_ = (uint32_t)((c >> 12) & 0xFFFULL);
+            uint32_t h = (uint32_t)((c >> 24) & 0xFFFULL);
+            int nmsum = (int)(c >> 36) - 128 * (int)(f + rv_);
             unsigned long long s = sums[i];
             if (f) atomicAdd(&C.fwd[g], f);
             if (rv_) atomicAdd(&C.rev[g], rv_);
@@ -448,7 +500,7 @@ __global__ void __launch_bounds__(kPileupThreads) k_pileup_tiles(DevState st, De
             atomicAdd(&C.tp[g], (uint32_t)(s & 0x1FFFFFULL));
             atomicAdd(&C.q[g], (uint32_t)((s >> 21) & 0x1FFFFFULL));
             atomicAdd(&C.mq[g], (uint32_t)(s >> 42));
-            if (nmv[i]) atomicAdd(&C.nm[g], nmv[i]);
+            if (nmsum) atomicAdd(&C.nm[g], nmsum);
             atomicAdd(&C.cov[cell], f + rv_);
             atomicOr((unsigned int *)&C.kflags[cell & ~3LL], 1u << (b + 8 * (cell & 3)));
             uint32_t fw = first[i];
@@ -456,6 +508,38 @@ __global__ void __launch_bounds__(kPileupThreads) k_pileup_tiles(DevState st, De
         }
         __syncthreads();
     }
+}
+
+// For regions with edge reads: walk the edge reads in parallel with the
+// detection sink; if none would touch a position past the window, the
+// parallel walk is exact and the region leaves the in-order path.
+__global__ void k_edge_detect(DevState st, DevParams P) {
+    int reg = blockIdx.x;
+    if (reg >= st.n_regions) return;
+    Region &R = st.regions[reg];
+    if (!R.serial) return;
+    __shared__ int hit;
+    if (threadIdx.x == 0) hit = 0;
+    __syncthreads();
+    const int kEdgeGuard = 4096;
+    int64_t lo = R.r0, hi = R.r1;
+    while (lo < hi) {
+        int64_t mid = (lo + hi) / 2;
+        if (st.batch.pos[mid] + 1 + kEdgeGuard < R.we) lo = mid + 1; else hi = mid;
+    }
+    DetectSink sink;
+    sink.R = &R;
+    sink.hit = &hit;
+    Walker<DetectSink> w(P, sink, R, st.ref, st.ref_len);
+    for (int64_t r = lo + threadIdx.x; r < R.r1; r += blockDim.x) {
+        if (!read_passes(st.batch, P, R, r)) continue;
+        int a, b;
+        read_span(st.batch, r, a, b);
+        if (!is_edge(R, b)) continue;
+        w.walk(st.batch, r);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && hit == 0) R.serial = 0;
 }
 
 // One block per region with edge reads; thread 0 walks them in file order.
@@ -539,7 +623,7 @@ void launch_region_spans(const DevState &st, cudaStream_t s) {
     if (st.n_regions > 0) k_region_spans<<<st.n_regions, 256, 0, s>>>(st);
 }
 
-size_t pileup_smem_bytes() { return (size_t)kTileW * 4 * (8 + 8 + 4 + 4); }
+size_t pileup_smem_bytes() { return (size_t)kTileW * 4 * (8 + 8 + 4); }
 
 cudaError_t launch_pileup(const DevState &st, const DevParams &P, int grid, cudaStream_t s) {
     size_t smem = pileup_smem_bytes();
@@ -547,6 +631,10 @@ cudaError_t launch_pileup(const DevState &st, const DevParams &P, int grid, cuda
     if (e != cudaSuccess) return e;
     k_pileup_tiles<kTileW><<<grid, kPileupThreads, smem, s>>>(st, P);
     return cudaGetLastError();
+}
+
+void launch_edge_detect(const DevState &st, const DevParams &P, cudaStream_t s) {
+    if (st.n_regions > 0) k_edge_detect<<<st.n_regions, 128, 0, s>>>(st, P);
 }
 
 void launch_serial(const DevState &st, const DevParams &P, cudaStream_t s) {

@@ -84,6 +84,20 @@ struct ReadView {
     }
 };
 
+__device__ __forceinline__ uint32_t pick_word(const uint4 &v, int k) {
+    return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w));
+}
+
+// BAM 4-bit code -> 0..3 for A/C/G/T, -1 otherwise
+__device__ __forceinline__ int code_base(int code) {
+    return code == 1 ? 0 : (code == 2 ? 1 : (code == 4 ? 2 : (code == 8 ? 3 : -1)));
+}
+
+// Sinks without an inline fast path for single-base observations.
+struct NoFast {
+    __device__ __forceinline__ bool emit(int, int, int, int, int, int, int) const { return false; }
+};
+
 // Observation destined for an allele key.
 struct Obs {
     int dir;
@@ -106,14 +120,24 @@ struct Walker {
     int64_t read_idx;
     // CigarParser state
     int start, offset, cel, rpis, rpes, n_cigar;
-    uint32_t cg[64];   // CIGAR after cleanupCigar (first 64 ops + 4 trailing words)
-    int ncg_store;
+    // cleanupCigar (src/parseCigar.cpp:1858-1892) turns the insertions before
+    // the first and after the last M/=/X op into soft clips; applied on read
+    int lead_end, trail_start;
+    // M-loop iteration state shared with the out-of-line slow iteration
+    int m_i, m_ci, m_nmoff, m_moffset, m_cop;
+    bool m_dir;
+    int m_mapq, m_nom, m_rlen, m_tlen;
     KeyBuf key;
 
     __device__ Walker(const DevParams &p, Sink &s, const Region &r, const char *rf, int rl)
         : P(p), S(s), R(r), ref(rf), ref_len(rl) {}
 
-    __device__ uint32_t W(int k) const { return k < ncg_store ? cg[k] : rv.word(k); }
+    __device__ uint32_t W(int k) const {
+        if (k >= n_cigar) return rv.word(k);
+        uint32_t w = __ldg(rv.cig + k);
+        if ((w & 15u) == 1u && (k < lead_end || k > trail_start)) w = (w & ~15u) | 4u;
+        return w;
+    }
     __device__ int cop(int k) const { return cig_op(W(k)); }
     __device__ int clen(int k) const { return cig_len(W(k)); }
 
@@ -208,7 +232,7 @@ struct Walker {
     }
 
     // process_softclip: src/parseCigar.cpp:1112-1301
-    __device__ void softclip(int ci, bool dir, int mapq, int nom, int position, int tlen) {
+    __device__ __noinline__ void softclip(int ci, bool dir, int mapq, int nom, int position, int tlen) {
         if (ci == 0) {
             while (cel - 1 >= 0 && start - 1 > 0 && start - 1 <= ref_len && has_eq(rv.base(cel - 1), start - 1) &&
                    rv.q(cel - 1) > 10) {
@@ -297,7 +321,7 @@ struct Walker {
     }
 
     // process_insertion: src/parseCigar.cpp:1303-1523
-    __device__ int insertion(int ci, bool dir, int mapq, int nom, int position, int rlen) {
+    __device__ __noinline__ int insertion(int ci, bool dir, int mapq, int nom, int position, int rlen) {
         if ((n_cigar > ci + 1 && cop(ci + 1) == 3) || (ci > 0 && cop(ci - 1) == 3)) {
             rpis += cel;
             return ci;
@@ -390,7 +414,7 @@ struct Walker {
     }
 
     // process_deletion + addVariationForDeletion: src/parseCigar.cpp:1525-1727, 1036-1082
-    __device__ int deletion(int ci, bool dir, int mapq, int nom, int rlen) {
+    __device__ __noinline__ int deletion(int ci, bool dir, int mapq, int nom, int rlen) {
         if ((n_cigar > ci && cop(ci + 1) == 3) || (ci > 1 && cop(ci - 1) == 3)) {
             rpis += cel;
             return ci;
@@ -479,6 +503,168 @@ struct Walker {
         return ci;
     }
 
+    // One iteration of the M-op base loop for a base that may start an MNV
+    // or a complex indel tail (src/parseCigar.cpp:678-959); the common
+    // single-base case is handled inline by walk().
+    __device__ __noinline__ void m_iteration() {
+            const bool dir = m_dir;
+            const int mapq = m_mapq, nom = m_nom, rlen = m_rlen, tlen = m_tlen, c_op = m_cop;
+            int &i = m_i, &ci = m_ci, &nmoff = m_nmoff, &moffset = m_moffset;
+            bool tr = trim(dir, tlen);
+            char ch1 = rv.base(rpis);
+            if (ch1 == 'N') {
+                start++;
+                rpis++;
+                rpes++;
+                return;
+            }
+            int q0 = rv.q(rpis);
+            long long qv = q0;
+            int qbases = 1, qibases = 0;
+            bool swd = false;
+            int ddlen = 0;
+            bool simple = true;   // key is the single base ch1
+            // MNV growth: src/parseCigar.cpp:711-767
+            if ((start + 1) >= R.start && (start + 1) <= R.end && (i + 1) < cel && qv >= P.goodq &&
+                has_ne(ch1, start) && idx(start) != 'N') {
+                key.clear();
+                key.push(ch1);
+                int sslen = 0;
+                while ((start + 1) >= R.start && (start + 1) <= R.end && (i + 1) < cel && qv >= P.goodq &&
+                       has_ne(rv.base(rpis), start) && idx(start) != 'N') {
+                    if (rv.q(rpis + 1) < P.goodq + 5) break;
+                    char nuc = rv.base(rpis + 1);
+                    if (nuc == 'N') break;
+                    if (has_eq('N', start + 1)) break;
+                    if (idx(start + 1) != nuc) {
+                        if (sslen == 0) key.push('&');
+                        key.push(nuc);
+                        sslen++;
+                        qv += rv.q(rpis + 1);
+                        qbases++;
+                        rpis++; rpes++; i++; start++; nmoff++;
+                    } else {
+                        int ssn = 0;
+                        for (int ssi = 1; ssi <= P.vext; ssi++) {
+                            if (i + 1 + ssi >= cel) break;
+                            if (rpis + 1 + ssi < rv.lseq && has_ne(rv.base(rpis + 1 + ssi), start + 1 + ssi)) {
+                                ssn = ssi + 1;
+                                break;
+                            }
+                        }
+                        if (ssn == 0) break;
+                        if (rv.q(rpis + ssn) < P.goodq + 5) break;
+                        for (int ssi = 1; ssi <= ssn; ssi++) {
+                            if (sslen == 0) key.push('&');
+                            key.push(rv.base(rpis + ssi));
+                            sslen++;
+                            qv += rv.q(rpis + ssi);
+                            qbases++;
+                        }
+                        rpis += ssn; rpes += ssn; i += ssn; start += ssn;
+                    }
+                }
+                simple = sslen == 0;
+            }
+            // complex tails next to a deletion / insertion: src/parseCigar.cpp:779-882
+            bool ss_nonempty = !simple;
+            if (P.local_realign && cel - i <= P.vext && ci + 1 < n_cigar &&
+                (cop(ci + 1) == 2 || cop(ci + 1) == 1) && has(start) &&
+                (ss_nonempty || rv.base(rpis) != at(start)) && rv.q(rpis) >= P.goodq) {
+                if (simple) { key.clear(); key.push(ch1); }
+                simple = false;
+                if (cop(ci + 1) == 2) {
+                    while (i + 1 < cel) {
+                        key.push(rv.base(rpis + 1));
+                        qv += rv.q(rpis + 1);
+                        qbases++; i++; rpis++; rpes++; start++;
+                    }
+                    // "-" dellen "&" + key without its first '&'
+                    char tmp[kMaxKey];
+                    int tn = 0;
+                    bool dropped = false;
+                    for (int k = 0; k < key.n; k++) {
+                        if (!dropped && key.b[k] == '&') { dropped = true; continue; }
+                        tmp[tn++] = key.b[k];
+                    }
+                    ddlen = clen(ci + 1);
+                    key.clear();
+                    key.push('-');
+                    key.push_int(ddlen);
+                    key.push('&');
+                    for (int k = 0; k < tn; k++) key.push(tmp[k]);
+                    swd = true;
+                    ci += 1;
+                    if (n_cigar > ci + 1 && cop(ci + 1) == 1) {
+                        int nl = clen(ci + 1);
+                        key.push('^');
+                        append_read(rpis + 1, nl);
+                        for (int qi = 1; qi <= nl; qi++) { qv += rv.q(rpis + 1 + qi); qibases++; }
+                        rpis += nl; rpes += nl; ci += 1;
+                    }
+                    if (next_after_num_matched(ci, 1)) {
+                        int tnm, qs;
+                        int to = find_offset(start + ddlen + 1, rpis + 1, clen(ci + 1), tnm, qs);
+                        if (to != 0) {
+                            moffset = to;
+                            nmoff += tnm;
+                            key.push('&');
+                            append_read(rpis + 1, to);
+                        }
+                    }
+                } else {
+                    while (i + 1 < cel) {
+                        key.push(rv.base(rpis + 1));
+                        qv += rv.q(rpis + 1);
+                        qbases++; i++; rpis++; rpes++; start++;
+                    }
+                    char tmp[kMaxKey];
+                    int tn = 0;
+                    bool dropped = false;
+                    for (int k = 0; k < key.n; k++) {
+                        if (!dropped && key.b[k] == '&') { dropped = true; continue; }
+                        tmp[tn++] = key.b[k];
+                    }
+                    int nl = clen(ci + 1);
+                    for (int k = 0; k < nl; k++) tmp[tn++] = rv.base(rpis + 1 + k);
+                    // s.insert(nl, "&") then "+" prefix
+                    key.clear();
+                    key.push('+');
+                    for (int k = 0; k < tn; k++) {
+                        if (k == nl) key.push('&');
+                        key.push(tmp[k]);
+                    }
+                    if (nl == tn) key.push('&');
+                    for (int qi = 1; qi <= nl; qi++) { qv += rv.q(rpis + 1 + qi); qibases++; }
+                    rpis += nl; rpes += nl; ci += 1;
+                    qibases--;
+                    qbases++;
+                }
+            }
+            if (!tr) {
+                int p = start - qbases + 1;
+                if (p >= R.start && p <= R.end) {
+                    int tp = tp_of(rlen);
+                    Obs o;
+                    o.dir = dir; o.tp = tp; o.mapq = mapq; o.nm = nom - nmoff; o.std_rel = true; o.creates = true;
+                    if (simple) {
+                        o.q = (double)q0;
+                        single(p, ch1, o);
+                    } else {
+                        o.q = (double)qv / (qbases + qibases);
+                        if (key.overflow) S.error(ERR_KEY_TOO_LONG);
+                        S.event(KIND_NONINS, p, key.b, key.n, o, read_idx);
+                        for (int qi = 1; qi <= qbases; qi++) S.cov(start - qi + 1, 1);
+                        if (swd)
+                            for (int qi = 1; qi < ddlen; qi++) S.cov(start + qi, 1);
+                    }
+                }
+            }
+            if (swd) start += ddlen;
+            if (c_op != 1) start++;
+            if (c_op != 2) { rpis++; rpes++; }
+            }
+
     // parseCigar: src/parseCigar.cpp:497-974
     __device__ void walk(const Batch &B, int64_t r) {
         read_idx = r;
@@ -489,13 +675,21 @@ struct Walker {
         rv.n_cigar = B.n_cigar[r];
         n_cigar = rv.n_cigar;
         if (n_cigar <= 0) return;
-        if (n_cigar > 60) { S.error(ERR_UNSUPPORTED); return; }
-        ncg_store = n_cigar + 4;
-        for (int k = 0; k < ncg_store; k++) cg[k] = rv.word(k);
+        lead_end = n_cigar;
+        trail_start = -1;
+        for (int k = 0; k < n_cigar; k++) {
+            int o = cig_op(__ldg(rv.cig + k));
+            if (o == 0 || o == 7 || o == 8) {
+                if (lead_end == n_cigar) lead_end = k;
+                trail_start = k;
+            }
+        }
         int flag = B.flag[r];
         int idl = 0;
-        for (int i = 0; i < n_cigar; i++)
-            if (cop(i) == 1 || cop(i) == 2) idl += clen(i);
+        for (int i = 0; i < n_cigar; i++) {
+            int o = cig_op(__ldg(rv.cig + i));  // original ops (before cleanup)
+            if (o == 1 || o == 2) idl += clen(i);
+        }
         int nmtag = B.nm[r];
         int nom = 0;
         if (nmtag != INT32_MIN) {
@@ -508,16 +702,6 @@ struct Walker {
         int mapq = B.mapq[r];
         int position = B.pos[r] + 1;
         rpis = rpes = 0;
-        // cleanupCigar: src/parseCigar.cpp:1858-1892
-        for (int pass = 0; pass < 2; pass++) {
-            bool none = true;
-            for (int k = 0; k < n_cigar && none; k++) {
-                int c = pass == 0 ? k : n_cigar - 1 - k;
-                int o = cig_op(cg[c]);
-                if (o == 1) cg[c] = (cg[c] & ~15u) | 4u;
-                else if (o == 0 || o == 7 || o == 8) none = false;
-            }
-        }
         start = position;
         offset = 0;
         if (cop(0) == 4 && clen(0) >= 10 && cop(n_cigar - 1) == 4 && clen(n_cigar - 1) >= 10) return;
@@ -541,6 +725,15 @@ struct Walker {
             else ov = start >= mate_start && mate_start <= endpos;
             if (ov) return;
         }
+        m_dir = dir;
+        m_mapq = mapq;
+        m_nom = nom;
+        m_rlen = rlen;
+        m_tlen = tlen;
+        typename Sink::Fast fe = S.fast();
+        const int rs = R.start, re = R.end, ws = R.ws, we = R.we;
+        const double goodq = P.goodq;
+        const int ttr = P.trim_bases_after;
         for (int ci = 0; ci < n_cigar; ++ci) {
             int c_op = cop(ci);
             cel = clen(ci);
@@ -563,161 +756,51 @@ struct Walker {
             if (c_op == 1) { offset = 0; ci = insertion(ci, dir, mapq, nom, position, rlen); continue; }
             if (c_op == 2) { offset = 0; ci = deletion(ci, dir, mapq, nom, rlen); continue; }
             int nmoff = 0, moffset = 0;
+            // with local realignment, bases within vext of a following indel
+            // may build complex keys: take the out-of-line iteration for them
+            const int tail_from = (P.local_realign && ci + 1 < n_cigar && (cop(ci + 1) == 1 || cop(ci + 1) == 2))
+                                      ? cel - P.vext : INT32_MAX;
+            // hot loop: state in registers, bases and quals through 16-byte windows
+            int st = start, rp = rpis, rq = rpes;
+            uint4 qw = make_uint4(0, 0, 0, 0), sw = make_uint4(0, 0, 0, 0);
+            int qblk = -1, sblk = -1;
             for (int i = offset; i < cel; i++) {
-                bool tr = trim(dir, tlen);
-                char ch1 = rv.base(rpis);
-                if (ch1 == 'N') {
-                    start++;
-                    rpis++;
-                    rpes++;
+                if ((rp >> 5) != sblk) { sblk = rp >> 5; sw = __ldg(reinterpret_cast<const uint4 *>(rv.seq) + sblk); }
+                const uint32_t swd_ = pick_word(sw, (rp & 31) >> 3);
+                const int code = (int)((swd_ >> (((rp & 7) ^ 1) * 4)) & 15u);
+                if (code == 15) {  // 'N': skipped (src/parseCigar.cpp:686-692)
+                    st++; rp++; rq++;
                     continue;
                 }
-                int q0 = rv.q(rpis);
-                long long qv = q0;
-                int qbases = 1, qibases = 0;
-                bool swd = false;
-                int ddlen = 0;
-                bool simple = true;   // key is the single base ch1
-                // MNV growth: src/parseCigar.cpp:711-767
-                if ((start + 1) >= R.start && (start + 1) <= R.end && (i + 1) < cel && qv >= P.goodq &&
-                    has_ne(ch1, start) && idx(start) != 'N') {
-                    key.clear();
-                    key.push(ch1);
-                    int sslen = 0;
-                    while ((start + 1) >= R.start && (start + 1) <= R.end && (i + 1) < cel && qv >= P.goodq &&
-                           has_ne(rv.base(rpis), start) && idx(start) != 'N') {
-                        if (rv.q(rpis + 1) < P.goodq + 5) break;
-                        char nuc = rv.base(rpis + 1);
-                        if (nuc == 'N') break;
-                        if (has_eq('N', start + 1)) break;
-                        if (idx(start + 1) != nuc) {
-                            if (sslen == 0) key.push('&');
-                            key.push(nuc);
-                            sslen++;
-                            qv += rv.q(rpis + 1);
-                            qbases++;
-                            rpis++; rpes++; i++; start++; nmoff++;
-                        } else {
-                            int ssn = 0;
-                            for (int ssi = 1; ssi <= P.vext; ssi++) {
-                                if (i + 1 + ssi >= cel) break;
-                                if (rpis + 1 + ssi < rv.lseq && has_ne(rv.base(rpis + 1 + ssi), start + 1 + ssi)) {
-                                    ssn = ssi + 1;
-                                    break;
-                                }
-                            }
-                            if (ssn == 0) break;
-                            if (rv.q(rpis + ssn) < P.goodq + 5) break;
-                            for (int ssi = 1; ssi <= ssn; ssi++) {
-                                if (sslen == 0) key.push('&');
-                                key.push(rv.base(rpis + ssi));
-                                sslen++;
-                                qv += rv.q(rpis + ssi);
-                                qbases++;
-                            }
-                            rpis += ssn; rpes += ssn; i += ssn; start += ssn;
+                if ((rp >> 4) != qblk) { qblk = rp >> 4; qw = __ldg(reinterpret_cast<const uint4 *>(rv.qual) + qblk); }
+                const int q0 = (int)((pick_word(qw, (rp & 15) >> 2) >> ((rp & 3) * 8)) & 255u);
+                const int b = code_base(code);
+                const bool hs = st >= ws && st <= we;
+                const char rc = hs ? ref[st - 1] : (char)0;
+                const bool mm = hs && base_index(rc) != b;
+                const bool slow = b < 0 || i >= tail_from ||
+                                  (mm && q0 >= goodq && st + 1 >= rs && st + 1 <= re && i + 1 < cel && rc != 'N');
+                if (!slow) {
+                    const bool tr = ttr != 0 && (dir ? tlen - rp > ttr : rp > ttr);
+                    if (!tr && st >= rs && st <= re) {
+                        const int tp = rq < rlen - rq ? rq + 1 : rlen - rq;
+                        if (!fe.emit(st, b, dir, tp, q0, mapq, nom - nmoff)) {
+                            Obs o;
+                            o.dir = dir; o.tp = tp; o.q = (double)q0; o.mapq = mapq; o.nm = nom - nmoff;
+                            o.std_rel = true; o.creates = true;
+                            S.single(st, b, o, read_idx);
                         }
                     }
-                    simple = sslen == 0;
+                    st++; rp++; rq++;
+                    continue;
                 }
-                // complex tails next to a deletion / insertion: src/parseCigar.cpp:779-882
-                bool ss_nonempty = !simple;
-                if (P.local_realign && cel - i <= P.vext && ci + 1 < n_cigar &&
-                    (cop(ci + 1) == 2 || cop(ci + 1) == 1) && has(start) &&
-                    (ss_nonempty || rv.base(rpis) != at(start)) && rv.q(rpis) >= P.goodq) {
-                    if (simple) { key.clear(); key.push(ch1); }
-                    simple = false;
-                    if (cop(ci + 1) == 2) {
-                        while (i + 1 < cel) {
-                            key.push(rv.base(rpis + 1));
-                            qv += rv.q(rpis + 1);
-                            qbases++; i++; rpis++; rpes++; start++;
-                        }
-                        // "-" dellen "&" + key without its first '&'
-                        char tmp[kMaxKey];
-                        int tn = 0;
-                        bool dropped = false;
-                        for (int k = 0; k < key.n; k++) {
-                            if (!dropped && key.b[k] == '&') { dropped = true; continue; }
-                            tmp[tn++] = key.b[k];
-                        }
-                        ddlen = clen(ci + 1);
-                        key.clear();
-                        key.push('-');
-                        key.push_int(ddlen);
-                        key.push('&');
-                        for (int k = 0; k < tn; k++) key.push(tmp[k]);
-                        swd = true;
-                        ci += 1;
-                        if (n_cigar > ci + 1 && cop(ci + 1) == 1) {
-                            int nl = clen(ci + 1);
-                            key.push('^');
-                            append_read(rpis + 1, nl);
-                            for (int qi = 1; qi <= nl; qi++) { qv += rv.q(rpis + 1 + qi); qibases++; }
-                            rpis += nl; rpes += nl; ci += 1;
-                        }
-                        if (next_after_num_matched(ci, 1)) {
-                            int tnm, qs;
-                            int to = find_offset(start + ddlen + 1, rpis + 1, clen(ci + 1), tnm, qs);
-                            if (to != 0) {
-                                moffset = to;
-                                nmoff += tnm;
-                                key.push('&');
-                                append_read(rpis + 1, to);
-                            }
-                        }
-                    } else {
-                        while (i + 1 < cel) {
-                            key.push(rv.base(rpis + 1));
-                            qv += rv.q(rpis + 1);
-                            qbases++; i++; rpis++; rpes++; start++;
-                        }
-                        char tmp[kMaxKey];
-                        int tn = 0;
-                        bool dropped = false;
-                        for (int k = 0; k < key.n; k++) {
-                            if (!dropped && key.b[k] == '&') { dropped = true; continue; }
-                            tmp[tn++] = key.b[k];
-                        }
-                        int nl = clen(ci + 1);
-                        for (int k = 0; k < nl; k++) tmp[tn++] = rv.base(rpis + 1 + k);
-                        // s.insert(nl, "&") then "+" prefix
-                        key.clear();
-                        key.push('+');
-                        for (int k = 0; k < tn; k++) {
-                            if (k == nl) key.push('&');
-                            key.push(tmp[k]);
-                        }
-                        if (nl == tn) key.push('&');
-                        for (int qi = 1; qi <= nl; qi++) { qv += rv.q(rpis + 1 + qi); qibases++; }
-                        rpis += nl; rpes += nl; ci += 1;
-                        qibases--;
-                        qbases++;
-                    }
-                }
-                if (!tr) {
-                    int p = start - qbases + 1;
-                    if (p >= R.start && p <= R.end) {
-                        int tp = tp_of(rlen);
-                        Obs o;
-                        o.dir = dir; o.tp = tp; o.mapq = mapq; o.nm = nom - nmoff; o.std_rel = true; o.creates = true;
-                        if (simple) {
-                            o.q = (double)q0;
-                            single(p, ch1, o);
-                        } else {
-                            o.q = (double)qv / (qbases + qibases);
-                            if (key.overflow) S.error(ERR_KEY_TOO_LONG);
-                            S.event(KIND_NONINS, p, key.b, key.n, o, read_idx);
-                            for (int qi = 1; qi <= qbases; qi++) S.cov(start - qi + 1, 1);
-                            if (swd)
-                                for (int qi = 1; qi < ddlen; qi++) S.cov(start + qi, 1);
-                        }
-                    }
-                }
-                if (swd) start += ddlen;
-                if (c_op != 1) start++;
-                if (c_op != 2) { rpis++; rpes++; }
+                start = st; rpis = rp; rpes = rq;
+                m_i = i; m_ci = ci; m_nmoff = nmoff; m_moffset = moffset; m_cop = c_op;
+                m_iteration();
+                st = start; rp = rpis; rq = rpes;
+                i = m_i; ci = m_ci; nmoff = m_nmoff; moffset = m_moffset;
             }
+            start = st; rpis = rp; rpes = rq;
             if (moffset != 0) {
                 offset = moffset;
                 rpis += moffset;
