@@ -177,7 +177,8 @@ void rv_destroy(rv_ctx *ctx) {
     void *ptrs[] = {ctx->d_ref, ctx->d_pos, ctx->d_mpos, ctx->d_nm, ctx->d_lq, ctx->d_flag, ctx->d_ncig,
                     ctx->d_mapq, ctx->d_cigoff, ctx->d_cigar, ctx->d_boff, ctx->d_seq, ctx->d_qual,
                     ctx->d_regions, ctx->d_tiles, ctx->d_score_base, ctx->d_cellmem, ctx->d_head, ctx->d_slots,
-                    ctx->d_arena, ctx->d_deferred, ctx->d_cand, ctx->d_counters};
+                    ctx->d_arena, ctx->d_deferred, ctx->d_cand, ctx->d_counters, ctx->d_tmp_idx,
+                    ctx->d_tmp_slots, ctx->d_tmp_cells, ctx->d_tmp_views, ctx->d_tmp_n};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (int i = 0; i < 12; i++)

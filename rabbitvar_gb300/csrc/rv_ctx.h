@@ -34,6 +34,9 @@ struct CellView {
     uint32_t cov;
     uint32_t kflags;
 };
+void launch_select_mnv(const DevState &st, uint32_t *out, unsigned int *n_out, cudaStream_t s);
+void launch_gather_lists(const DevState &st, const int64_t *cells, int64_t n, uint32_t *out, unsigned int *n_out,
+                         unsigned int cap, cudaStream_t s);
 void launch_gather_cells(const DevState &st, const int64_t *cells, int64_t n, CellView *out, cudaStream_t s);
 
 // patch written back by the host realigner
@@ -113,6 +116,17 @@ struct rv_ctx {
 
     // small counters: tile_counter, n_deferred, n_used, err, n_cand, pad, arena_used(64)
     unsigned int *d_counters = nullptr;
+
+    // scratch for the realigner boundary (grown on demand, owned by the context)
+    uint32_t *d_tmp_idx = nullptr;
+    size_t cap_tmp_idx = 0;
+    rv::Slot *d_tmp_slots = nullptr;
+    size_t cap_tmp_slots = 0;
+    int64_t *d_tmp_cells = nullptr;
+    size_t cap_tmp_cells = 0;
+    void *d_tmp_views = nullptr;
+    size_t cap_tmp_views = 0;
+    unsigned int *d_tmp_n = nullptr;
 
     // host mirrors
     std::vector<rv::CandVar> h_cand;

@@ -256,20 +256,61 @@ HVar from_slot(const Slot &s, int64_t slot) {
 
 }  // namespace
 
-rv_status host_realign_mnp(rv_ctx *ctx) {
-    std::vector<Slot> slots;
-    std::vector<uint32_t> sidx;
-    rv_status st = fetch_slots(ctx, slots, sidx);
+template <class T>
+rv_status ensure(rv_ctx *ctx, T *&p, size_t &cap, size_t need) {
+    if (p && need <= cap) return RV_OK;
+    if (p) cudaFree(p);
+    p = nullptr;
+    size_t n = std::max<size_t>(need + need / 2, 256);
+    HCUDA(cudaMalloc((void **)&p, n * sizeof(T)));
+    cap = n;
+    return RV_OK;
+}
+
+// Slots named by a device index list, copied to the host.
+rv_status pull_slots(rv_ctx *ctx, unsigned int n, std::vector<Slot> &slots, std::vector<uint32_t> &idx) {
+    slots.resize(n);
+    idx.resize(n);
+    if (!n) return RV_OK;
+    rv_status st = ensure(ctx, ctx->d_tmp_slots, ctx->cap_tmp_slots, n);
     if (st) return st;
+    launch_gather_slots(ctx->d_slots, ctx->d_tmp_idx, n, ctx->d_tmp_slots, ctx->stream);
+    HCUDA(cudaMemcpyAsync(slots.data(), ctx->d_tmp_slots, (size_t)n * sizeof(Slot), cudaMemcpyDeviceToHost, ctx->stream));
+    HCUDA(cudaMemcpyAsync(idx.data(), ctx->d_tmp_idx, (size_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    HCUDA(cudaStreamSynchronize(ctx->stream));
+    return RV_OK;
+}
+
+rv_status pull_arena(rv_ctx *ctx) {
+    unsigned long long used = 0;
+    HCUDA(cudaMemcpyAsync(&used, ctx->d_counters + 8, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    HCUDA(cudaStreamSynchronize(ctx->stream));
+    used = std::min<unsigned long long>(used, ctx->arena_cap);
+    ctx->h_arena.resize(used);
+    if (used) HCUDA(cudaMemcpy(ctx->h_arena.data(), ctx->d_arena, used, cudaMemcpyDeviceToHost));
+    return RV_OK;
+}
+
+rv_status host_realign_mnp(rv_ctx *ctx) {
+    rv_status st;
+    if ((st = ensure(ctx, ctx->d_tmp_idx, ctx->cap_tmp_idx, (size_t)ctx->hash_cap))) return st;
+    size_t one = 0;
+    if (!ctx->d_tmp_n) HCUDA(cudaMalloc((void **)&ctx->d_tmp_n, 16));
+    (void)one;
+    HCUDA(cudaMemsetAsync(ctx->d_tmp_n, 0, 4, ctx->stream));
+    DevState ds = ctx->state();
+    launch_select_mnv(ds, ctx->d_tmp_idx, ctx->d_tmp_n, ctx->stream);
+    unsigned int n_mnv = 0;
+    HCUDA(cudaMemcpyAsync(&n_mnv, ctx->d_tmp_n, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    HCUDA(cudaStreamSynchronize(ctx->stream));
+    if (n_mnv == 0) return RV_OK;
+    std::vector<Slot> mslots;
+    std::vector<uint32_t> midx;
+    if ((st = pull_slots(ctx, n_mnv, mslots, midx))) return st;
+    if ((st = pull_arena(ctx))) return st;
     struct Mnp { int region, pos; std::string key; int cnt; };
     std::vector<Mnp> mnps;
-    for (size_t i = 0; i < slots.size(); i++) {
-        const Slot &s = slots[i];
-        if (s.kind != KIND_NONINS || (s.flags & SF_ERASED) || s.obs <= 0) continue;
-        std::string k = slot_key(ctx, s);
-        if (is_mnv(k)) mnps.push_back({s.region, s.pos, k, s.obs});
-    }
-    if (mnps.empty()) return RV_OK;
+    for (const Slot &s : mslots) mnps.push_back({s.region, s.pos, slot_key(ctx, s), s.obs});
     // positions whose keys the MNP merge may read or change
     std::set<std::pair<int, int>> need;
     std::set<std::tuple<int, int, int>> need_clip;  // region, pos, side (5 or 3)
@@ -279,22 +320,45 @@ rv_status host_realign_mnp(rv_ctx *ctx) {
         need_clip.insert({m.region, m.pos, 3});
         need_clip.insert({m.region, m.pos + len, 5});
     }
+    std::set<std::pair<int, int>> all_pos(need.begin(), need.end());
+    for (auto &c : need_clip) all_pos.insert({std::get<0>(c), std::get<1>(c)});
     std::vector<int64_t> cells;
     std::vector<std::pair<int, int>> cell_pos;
-    for (auto &np : need) {
+    for (auto &np : all_pos) {
         const Region &R = ctx->regions[np.first];
         if (np.second < R.clo || np.second > R.chi) continue;
         cells.push_back(R.cell_base + (np.second - R.clo));
         cell_pos.push_back(np);
     }
-    std::vector<CellView> cv;
-    if ((st = fetch_cells(ctx, cells, cv))) return st;
+    std::vector<CellView> cv(cells.size());
+    std::vector<Slot> slots;
+    std::vector<uint32_t> sidx;
+    if (!cells.empty()) {
+        if ((st = ensure(ctx, ctx->d_tmp_cells, ctx->cap_tmp_cells, cells.size()))) return st;
+        CellView *dv = (CellView *)ctx->d_tmp_views;
+        size_t capv = ctx->cap_tmp_views;
+        if ((st = ensure(ctx, dv, capv, cells.size()))) return st;
+        ctx->d_tmp_views = dv;
+        ctx->cap_tmp_views = capv;
+        HCUDA(cudaMemcpyAsync(ctx->d_tmp_cells, cells.data(), cells.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
+        launch_gather_cells(ds, ctx->d_tmp_cells, (int64_t)cells.size(), dv, ctx->stream);
+        HCUDA(cudaMemcpyAsync(cv.data(), dv, cells.size() * sizeof(CellView), cudaMemcpyDeviceToHost, ctx->stream));
+        HCUDA(cudaMemsetAsync(ctx->d_tmp_n, 0, 4, ctx->stream));
+        launch_gather_lists(ds, ctx->d_tmp_cells, (int64_t)cells.size(), ctx->d_tmp_idx, ctx->d_tmp_n,
+                            (unsigned int)ctx->cap_tmp_idx, ctx->stream);
+        unsigned int nl = 0;
+        HCUDA(cudaMemcpyAsync(&nl, ctx->d_tmp_n, 4, cudaMemcpyDeviceToHost, ctx->stream));
+        HCUDA(cudaStreamSynchronize(ctx->stream));
+        if (nl > ctx->cap_tmp_idx) { ctx->err = "realigner gather overflow"; return RV_ERR_CAPACITY; }
+        if ((st = pull_slots(ctx, nl, slots, sidx))) return st;
+    }
     // mirror of the touched part of the maps
     std::map<std::pair<int, int>, std::map<std::string, HVar>> vars;
     std::map<std::pair<int, int>, int64_t> cell_of_pos;
     for (size_t i = 0; i < cells.size(); i++) {
-        auto &m = vars[cell_pos[i]];
         cell_of_pos[cell_pos[i]] = cells[i];
+        if (!need.count(cell_pos[i])) continue;
+        auto &m = vars[cell_pos[i]];
         for (int b = 0; b < 4; b++) {
             bool exist = (cv[i].kflags >> b) & 1, erased = (cv[i].kflags >> (4 + b)) & 1;
             if (exist && !erased) m[std::string(1, kBases[b])] = from_cell(cv[i], b, cells[i]);
@@ -422,12 +486,19 @@ rv_status host_realign_mnp(rv_ctx *ctx) {
             patches.push_back(p);
         }
     if (patches.empty()) return RV_OK;
-    Patch *d_p = nullptr;
-    HCUDA(cudaMalloc((void **)&d_p, patches.size() * sizeof(Patch)));
+    Patch *d_p = (Patch *)ctx->d_tmp_views;
+    size_t capp = ctx->cap_tmp_views * sizeof(CellView) / sizeof(Patch);
+    if (!d_p || capp < patches.size()) {
+        if (ctx->d_tmp_views) cudaFree(ctx->d_tmp_views);
+        ctx->d_tmp_views = nullptr;
+        size_t nv = (patches.size() * sizeof(Patch) + sizeof(CellView) - 1) / sizeof(CellView) + 64;
+        HCUDA(cudaMalloc(&ctx->d_tmp_views, nv * sizeof(CellView)));
+        ctx->cap_tmp_views = nv;
+        d_p = (Patch *)ctx->d_tmp_views;
+    }
     HCUDA(cudaMemcpyAsync(d_p, patches.data(), patches.size() * sizeof(Patch), cudaMemcpyHostToDevice, ctx->stream));
     launch_apply_patches(ctx->state(), d_p, (int64_t)patches.size(), ctx->stream);
     HCUDA(cudaStreamSynchronize(ctx->stream));
-    cudaFree(d_p);
     return RV_OK;
 }
 

@@ -203,9 +203,27 @@ struct SinkBase {
 // position), tp and q in 1..1023, mapq <= 255, nm in -128..127; anything else
 // goes straight to the global cells.
 
+// shared-state-space atomics on 32-bit shared addresses (the generic forms
+// cannot be proven not to alias the walker's local-memory object)
+__device__ __forceinline__ void shared_add_u64(uint32_t addr, unsigned long long v) {
+    asm volatile("red.shared.add.u64 [%0], %1;" ::"r"(addr), "l"(v) : "memory");
+}
+__device__ __forceinline__ uint32_t shared_ld_u32(uint32_t addr) {
+    uint32_t v;
+    asm volatile("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(addr) : "memory");
+    return v;
+}
+__device__ __forceinline__ void shared_or_u32(uint32_t addr, uint32_t v) {
+    asm volatile("red.shared.or.b32 [%0], %1;" ::"r"(addr), "r"(v) : "memory");
+}
+__device__ __forceinline__ uint32_t shared_cas_u32(uint32_t addr, uint32_t cmp, uint32_t v) {
+    uint32_t old;
+    asm volatile("atom.shared.cas.b32 %0, [%1], %2, %3;" : "=r"(old) : "r"(addr), "r"(cmp), "r"(v) : "memory");
+    return old;
+}
+
 struct TileFast {
-    unsigned long long *cnt, *sums;
-    uint32_t *first;
+    uint32_t cnt_s, sums_s, first_s;   // shared-space addresses of the three arrays
     int wlo;
     double goodq;
     __device__ __forceinline__ bool emit(int p, int b, int dir, int tp, int q, int mapq, int nm) const {
@@ -218,22 +236,26 @@ struct TileFast {
         if (d >= (unsigned)kTileW || (unsigned)(tp - 1) > 1022u || (unsigned)(q - 1) > 1022u || (unsigned)mapq > 255u ||
             (unsigned)(nm + 128) > 255u)
             return false;
-        int ix = 4 * (int)d + b;
-        atomicAdd(&cnt[ix], (dir ? (1ULL << 12) : 1ULL) + (q >= goodq ? (1ULL << 24) : 0ULL) +
-                                ((unsigned long long)(nm + 128) << 36));
-        atomicAdd(&sums[ix], (unsigned long long)tp | ((unsigned long long)q << 21) | ((unsigned long long)mapq << 42));
+        const uint32_t ix = 4u * d + (uint32_t)b;
+        shared_add_u64(cnt_s + 8u * ix, (dir ? (1ULL << 12) : 1ULL) + (q >= goodq ? (1ULL << 24) : 0ULL) +
+                                            ((unsigned long long)(nm + 128) << 36));
+        shared_add_u64(sums_s + 8u * ix,
+                       (unsigned long long)tp | ((unsigned long long)q << 21) | ((unsigned long long)mapq << 42));
         if (!std_rel) return true;
         const uint32_t v = (uint32_t)tp | ((uint32_t)q << 12);
-        const uint32_t f = first[ix];
-        const uint32_t fv = f & FC_VAL;
-        if (fv == 0u) {
-            first_merge(&first[ix], v, 0u);
-        } else {
-            uint32_t need = 0u;
-            if (!(f & FC_PDIFF) && (fv & 0xFFFu) != (v & 0xFFFu)) need |= FC_PDIFF;
-            if (!(f & FC_QDIFF) && (fv >> 12) != (v >> 12)) need |= FC_QDIFF;
-            if (need) atomicOr(&first[ix], need);
+        const uint32_t fa = first_s + 4u * ix;
+        uint32_t f = shared_ld_u32(fa);
+        // claim the value slot if empty (bounded retries: flag bits may change)
+        for (int it = 0; it < 64 && (f & FC_VAL) == 0u; it++) {
+            uint32_t old = shared_cas_u32(fa, f, f | v);
+            if (old == f) return true;
+            f = old;
         }
+        const uint32_t fv = f & FC_VAL;
+        uint32_t need = 0u;
+        if (!(f & FC_PDIFF) && (fv & 0xFFFu) != (v & 0xFFFu)) need |= FC_PDIFF;
+        if (!(f & FC_QDIFF) && (fv >> 12) != (v >> 12)) need |= FC_QDIFF;
+        if (need) shared_or_u32(fa, need);
         return true;
     }
 };
@@ -462,9 +484,9 @@ __global__ void __launch_bounds__(kPileupThreads) k_pileup_tiles(DevState st, De
         sink.P = &P;
         sink.R = &R;
         sink.region_idx = tile.region;
-        sink.f.cnt = cnt;
-        sink.f.sums = sums;
-        sink.f.first = first;
+        sink.f.cnt_s = (uint32_t)__cvta_generic_to_shared(cnt);
+        sink.f.sums_s = (uint32_t)__cvta_generic_to_shared(sums);
+        sink.f.first_s = (uint32_t)__cvta_generic_to_shared(first);
         sink.f.wlo = wlo;
         sink.f.goodq = P.goodq;
         {

@@ -23,7 +23,7 @@ __global__ void k_link_slots(DevState st) {
     for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
          i += (unsigned long long)gridDim.x * blockDim.x) {
         Slot &s = st.hash.slots[i];
-        if (s.fp == 0ULL || (s.kind != KIND_NONINS && s.kind != KIND_INS)) continue;
+        if (s.fp == 0ULL || s.kind == KIND_SPLICE) continue;
         const Region &R = st.regions[s.region];
         if (s.pos < R.clo || s.pos > R.chi) continue;
         int64_t c = cell_index(R, s.pos);
@@ -281,12 +281,36 @@ __global__ void k_score(DevState st, DevParams P) {
         const Region &R = st.regions[lo];
         int p = R.start + (int)(t - st.score_base[lo]);
         if (p < R.clo || p > R.chi) continue;
-        PosKeys k;
-        if (!visited(st, R, p, k)) continue;
         int64_t c = cell_index(R, p);
         char rb = ref_at(st, R, p);
         int rbi = base_index(rb);
         bool hasp = p >= R.ws && p <= R.we;
+        // quick screen for positions holding only A/C/G/T keys: skip when only
+        // the reference base was seen, or when no other base could pass the
+        // -f gate and the numeric part of isGoodVar
+        if (st.head[c] == kNone && !P.do_pileup) {
+            uint8_t kf0 = st.cells.kflags[c];
+            int ex = kf0 & 15 & ~(kf0 >> 4);
+            if (ex == 0) continue;
+            uint32_t cov0 = st.cells.cov[c];
+            if (cov0 == 0) continue;
+            if (hasp && rbi >= 0 && ex == (1 << rbi)) continue;
+            const uint4 f4 = *reinterpret_cast<const uint4 *>(st.cells.fwd + 4 * c);
+            const uint4 r4 = *reinterpret_cast<const uint4 *>(st.cells.rev + 4 * c);
+            const uint4 h4 = *reinterpret_cast<const uint4 *>(st.cells.hi + 4 * c);
+            const uint32_t fa[4] = {f4.x, f4.y, f4.z, f4.w}, ra[4] = {r4.x, r4.y, r4.z, r4.w};
+            const uint32_t ha[4] = {h4.x, h4.y, h4.z, h4.w};
+            bool maybe = false;
+            for (int b = 0; b < 4; b++) {
+                if (!((ex >> b) & 1) || (hasp && b == rbi)) continue;
+                int cnt = (int)(fa[b] + ra[b]);
+                if (cnt > 0 && cnt / (double)cov0 > P.freq && (int)ha[b] >= P.minr && cnt / (double)cov0 >= P.freq)
+                    maybe = true;
+            }
+            if (!maybe) continue;
+        }
+        PosKeys k;
+        if (!visited(st, R, p, k)) continue;
         // isTheSameVariationOnRef (src/ToVarsBuilder.cpp:213-233)
         if (!P.do_pileup && k.n_nonins == 1 && k.n_ins == 0 && hasp && rbi >= 0 && k.single_mask == (1 << rbi))
             continue;

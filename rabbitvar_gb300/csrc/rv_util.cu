@@ -68,6 +68,41 @@ __global__ void k_apply_patches(DevState st, const Patch *p, int64_t n) {
     }
 }
 
+// MNP keys (A/C/G/T '&' A/C/G/T...) that the realigner's adjustMNP visits.
+__global__ void k_select_mnv(DevState st, uint32_t *out, unsigned int *n_out) {
+    unsigned long long n = st.hash.mask + 1ULL;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        const Slot &s = st.hash.slots[i];
+        if (s.fp == 0ULL || s.kind != KIND_NONINS || (s.flags & SF_ERASED) || s.obs <= 0 || s.klen < 3) continue;
+        const uint8_t *k = st.hash.arena + s.koff;
+        auto acgt = [](uint8_t c) { return c == 'A' || c == 'C' || c == 'G' || c == 'T'; };
+        bool ok = k[1] == '&' && acgt(k[0]);
+        for (int j = 2; ok && j < s.klen; j++) ok = acgt(k[j]);
+        if (ok) out[atomicAdd(n_out, 1u)] = (uint32_t)i;
+    }
+}
+
+// All keys linked at the requested cells (their per-position lists).
+__global__ void k_gather_lists(DevState st, const int64_t *cells, int64_t n, uint32_t *out, unsigned int *n_out,
+                               unsigned int cap) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int steps = 0;
+        for (uint32_t s = st.head[cells[i]]; s != 0xFFFFFFFFu && steps < (1 << 20); s = st.hash.slots[s].next, steps++) {
+            unsigned int k = atomicAdd(n_out, 1u);
+            if (k < cap) out[k] = s;
+        }
+    }
+}
+
+void launch_select_mnv(const DevState &st, uint32_t *out, unsigned int *n_out, cudaStream_t s) {
+    k_select_mnv<<<592, 256, 0, s>>>(st, out, n_out);
+}
+void launch_gather_lists(const DevState &st, const int64_t *cells, int64_t n, uint32_t *out, unsigned int *n_out,
+                         unsigned int cap, cudaStream_t s) {
+    if (n > 0) k_gather_lists<<<(int)((n + 127) / 128 < 1024 ? (n + 127) / 128 : 1024), 128, 0, s>>>(st, cells, n, out, n_out, cap);
+}
+
 void launch_compact_slots(const DevState &st, uint32_t *out, unsigned int *n_out, cudaStream_t s) {
     k_compact_slots<<<592, 256, 0, s>>>(st, out, n_out);
 }

@@ -760,26 +760,31 @@ struct Walker {
             // may build complex keys: take the out-of-line iteration for them
             const int tail_from = (P.local_realign && ci + 1 < n_cigar && (cop(ci + 1) == 1 || cop(ci + 1) == 2))
                                       ? cel - P.vext : INT32_MAX;
-            // hot loop: state in registers, bases and quals through 16-byte windows
+            // hot loop: every value it touches lives in registers (the walker
+            // object itself is in local memory for the out-of-line paths)
             int st = start, rp = rpis, rq = rpes;
+            int celr = cel;
+            const uint4 *seq16 = reinterpret_cast<const uint4 *>(rv.seq);
+            const uint4 *qual16 = reinterpret_cast<const uint4 *>(rv.qual);
+            const char *refp = ref;
             uint4 qw = make_uint4(0, 0, 0, 0), sw = make_uint4(0, 0, 0, 0);
             int qblk = -1, sblk = -1;
-            for (int i = offset; i < cel; i++) {
-                if ((rp >> 5) != sblk) { sblk = rp >> 5; sw = __ldg(reinterpret_cast<const uint4 *>(rv.seq) + sblk); }
+            for (int i = offset; i < celr; i++) {
+                if ((rp >> 5) != sblk) { sblk = rp >> 5; sw = __ldg(seq16 + sblk); }
                 const uint32_t swd_ = pick_word(sw, (rp & 31) >> 3);
                 const int code = (int)((swd_ >> (((rp & 7) ^ 1) * 4)) & 15u);
                 if (code == 15) {  // 'N': skipped (src/parseCigar.cpp:686-692)
                     st++; rp++; rq++;
                     continue;
                 }
-                if ((rp >> 4) != qblk) { qblk = rp >> 4; qw = __ldg(reinterpret_cast<const uint4 *>(rv.qual) + qblk); }
+                if ((rp >> 4) != qblk) { qblk = rp >> 4; qw = __ldg(qual16 + qblk); }
                 const int q0 = (int)((pick_word(qw, (rp & 15) >> 2) >> ((rp & 3) * 8)) & 255u);
                 const int b = code_base(code);
                 const bool hs = st >= ws && st <= we;
-                const char rc = hs ? ref[st - 1] : (char)0;
+                const char rc = hs ? __ldg(refp + st - 1) : (char)0;
                 const bool mm = hs && base_index(rc) != b;
                 const bool slow = b < 0 || i >= tail_from ||
-                                  (mm && q0 >= goodq && st + 1 >= rs && st + 1 <= re && i + 1 < cel && rc != 'N');
+                                  (mm && q0 >= goodq && st + 1 >= rs && st + 1 <= re && i + 1 < celr && rc != 'N');
                 if (!slow) {
                     const bool tr = ttr != 0 && (dir ? tlen - rp > ttr : rp > ttr);
                     if (!tr && st >= rs && st <= re) {
@@ -799,6 +804,7 @@ struct Walker {
                 m_iteration();
                 st = start; rp = rpis; rq = rpes;
                 i = m_i; ci = m_ci; nmoff = m_nmoff; moffset = m_moffset;
+                celr = cel;
             }
             start = st; rpis = rp; rpes = rq;
             if (moffset != 0) {
