@@ -292,7 +292,7 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
         int64_t nr = R.r1 - R.r0;
         if (nr > 0) {
             double dens = nr / (double)(R.end - R.start + 1 + 2 * max_lq);
-            double usable = (double)kTileW - max_span - 2.0 * max_lq - 16.0;
+            double usable = (double)kTileW - max_span - max_lq - 16.0;  // window = start span + read extent
             int64_t tr = (int64_t)std::max(32.0, std::min((double)kTileReads, usable * dens));
             for (int64_t a = R.r0; a < R.r1; a += tr) {
                 Tile t;

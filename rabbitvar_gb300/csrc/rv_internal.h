@@ -10,9 +10,9 @@ namespace rv {
 
 // Hard limits of this build.
 constexpr int kMaxKey = 640;        // longest allele key a walk may build
-constexpr int kTileW = 896;         // positions per shared-memory tile window
+constexpr int kTileW = 640;         // positions per shared-memory tile window
 constexpr int kPileupThreads = 256; // threads per pileup block (one read per thread at a time)
-constexpr int kTileReads = 512;     // reads per tile at most (bounds the packed shared-memory counters)
+constexpr int kTileReads = 256;     // reads per tile at most (bounds the packed shared-memory counters)
 
 // Allele-key kinds stored in the device hash table (the maps of
 // include/scopedata/VariationData.h:14-56).

@@ -196,17 +196,18 @@ struct SinkBase {
     __device__ void max_len(int tlen) { atomicMax((int *)&R->max_read_len, tlen); }
 };
 
-// Tile-histogram packing of one (position, base) cell in shared memory:
-//   cnt : fwd (bits 0-11) | rev (12-23) | hi (24-35) | nm + 128 (36-63)
-//   sums: tp (0-20) | q (21-41) | mapq (42-63)
-// valid for tiles of at most kTileReads reads (one observation per read and
-// position), tp and q in 1..1023, mapq <= 255, nm in -128..127; anything else
-// goes straight to the global cells.
-
-// shared-state-space atomics on 32-bit shared addresses (the generic forms
-// cannot be proven not to alias the walker's local-memory object)
-__device__ __forceinline__ void shared_add_u64(uint32_t addr, unsigned long long v) {
-    asm volatile("red.shared.add.u64 [%0], %1;" ::"r"(addr), "l"(v) : "memory");
+// Tile-histogram packing of one (position, base) cell in shared memory,
+// three 32-bit words (32-bit shared atomics are native; 64-bit ones are not):
+//   w0: fwd (bits 0-9) | rev (10-19) | hi (20-29)
+//   w1: tp (bits 0-16) | q (17-31)
+//   w2: mapq (bits 0-15) | nm + 128 (16-31)
+// valid for tiles of at most kTileReads (256) reads, one observation per read
+// and position, tp in 1..511, q in 1..127, mapq <= 255, nm in -128..127;
+// anything else goes straight to the global cells.  The word arrays are
+// addressed in the shared state space (the generic forms cannot be proven not
+// to alias the walker's local-memory object).
+__device__ __forceinline__ void shared_add_u32(uint32_t addr, uint32_t v) {
+    asm volatile("red.shared.add.u32 [%0], %1;" ::"r"(addr), "r"(v) : "memory");
 }
 __device__ __forceinline__ uint32_t shared_ld_u32(uint32_t addr) {
     uint32_t v;
@@ -223,7 +224,7 @@ __device__ __forceinline__ uint32_t shared_cas_u32(uint32_t addr, uint32_t cmp, 
 }
 
 struct TileFast {
-    uint32_t cnt_s, sums_s, first_s;   // shared-space addresses of the three arrays
+    uint32_t w_s;       // shared-space address of the word arrays (w0 | w1 | w2 | first, 4*kTileW words each)
     int wlo;
     double goodq;
     __device__ __forceinline__ bool emit(int p, int b, int dir, int tp, int q, int mapq, int nm) const {
@@ -233,17 +234,18 @@ struct TileFast {
     // soft-clip re-alignment counts do not)
     __device__ __forceinline__ bool emit_any(int p, int b, int dir, int tp, int q, int mapq, int nm, bool std_rel) const {
         unsigned d = (unsigned)(p - wlo);
-        if (d >= (unsigned)kTileW || (unsigned)(tp - 1) > 1022u || (unsigned)(q - 1) > 1022u || (unsigned)mapq > 255u ||
+        if (d >= (unsigned)kTileW || (unsigned)(tp - 1) > 510u || (unsigned)(q - 1) > 126u || (unsigned)mapq > 255u ||
             (unsigned)(nm + 128) > 255u)
             return false;
         const uint32_t ix = 4u * d + (uint32_t)b;
-        shared_add_u64(cnt_s + 8u * ix, (dir ? (1ULL << 12) : 1ULL) + (q >= goodq ? (1ULL << 24) : 0ULL) +
-                                            ((unsigned long long)(nm + 128) << 36));
-        shared_add_u64(sums_s + 8u * ix,
-                       (unsigned long long)tp | ((unsigned long long)q << 21) | ((unsigned long long)mapq << 42));
+        const uint32_t a0 = w_s + 4u * ix;
+        constexpr uint32_t kArr = 4u * 4u * kTileW;  // bytes per word array
+        shared_add_u32(a0, (dir ? (1u << 10) : 1u) + (q >= goodq ? (1u << 20) : 0u));
+        shared_add_u32(a0 + kArr, (uint32_t)tp | ((uint32_t)q << 17));
+        shared_add_u32(a0 + 2u * kArr, (uint32_t)mapq | ((uint32_t)(nm + 128) << 16));
         if (!std_rel) return true;
         const uint32_t v = (uint32_t)tp | ((uint32_t)q << 12);
-        const uint32_t fa = first_s + 4u * ix;
+        const uint32_t fa = a0 + 3u * kArr;
         uint32_t f = shared_ld_u32(fa);
         // claim the value slot if empty (bounded retries: flag bits may change)
         for (int it = 0; it < 64 && (f & FC_VAL) == 0u; it++) {
@@ -453,9 +455,10 @@ __global__ void k_region_spans(DevState st) {
 template <int TW>
 __global__ void __launch_bounds__(kPileupThreads) k_pileup_tiles(DevState st, DevParams P) {
     extern __shared__ __align__(16) unsigned char smem[];
-    unsigned long long *cnt = (unsigned long long *)smem;
-    unsigned long long *sums = cnt + 4 * TW;
-    uint32_t *first = (uint32_t *)(sums + 4 * TW);
+    uint32_t *w0 = (uint32_t *)smem;
+    uint32_t *w1 = w0 + 4 * TW;
+    uint32_t *w2 = w1 + 4 * TW;
+    uint32_t *first = w2 + 4 * TW;
     __shared__ int s_tile, s_wlo;
     for (;;) {
         if (threadIdx.x == 0) {
@@ -472,11 +475,7 @@ __global__ void __launch_bounds__(kPileupThreads) k_pileup_tiles(DevState st, De
             read_span(st.batch, r, a, b);
             if (!is_edge(R, b)) atomicMin(&s_wlo, a);
         }
-        for (int i = threadIdx.x; i < 4 * TW; i += blockDim.x) {
-            cnt[i] = 0ULL;
-            sums[i] = 0ULL;
-            first[i] = 0u;
-        }
+        for (int i = threadIdx.x; i < 4 * 4 * TW; i += blockDim.x) w0[i] = 0u;
         __syncthreads();
         int wlo = max(s_wlo, R.clo);
         TileSink sink;
@@ -484,9 +483,7 @@ __global__ void __launch_bounds__(kPileupThreads) k_pileup_tiles(DevState st, De
         sink.P = &P;
         sink.R = &R;
         sink.region_idx = tile.region;
-        sink.f.cnt_s = (uint32_t)__cvta_generic_to_shared(cnt);
-        sink.f.sums_s = (uint32_t)__cvta_generic_to_shared(sums);
-        sink.f.first_s = (uint32_t)__cvta_generic_to_shared(first);
+        sink.f.w_s = (uint32_t)__cvta_generic_to_shared(w0);
         sink.f.wlo = wlo;
         sink.f.goodq = P.goodq;
         {
@@ -505,23 +502,22 @@ __global__ void __launch_bounds__(kPileupThreads) k_pileup_tiles(DevState st, De
         // flush the tile histogram into the global cells
         const Cells &C = st.cells;
         for (int i = threadIdx.x; i < 4 * TW; i += blockDim.x) {
-            unsigned long long c = cnt[i];
-            if (c == 0ULL) continue;
+            uint32_t c = w0[i];
+            if (c == 0u) continue;
             int p = wlo + (i >> 2);
             int b = i & 3;
             if (p > R.chi) { set_err(st.err, ERR_CELL_RANGE); continue; }
             int64_t cell = cell_of(R, p);
             int64_t g = 4 * cell + b;
-            uint32_t f = (uint32_t)(c & 0xFFFULL), rv_ = (uint32_t)((c >> 12) & 0xFFFULL);
-            uint32_t h = (uint32_t)((c >> 24) & 0xFFFULL);
-            int nmsum = (int)(c >> 36) - 128 * (int)(f + rv_);
-            unsigned long long s = sums[i];
+            uint32_t f = c & 0x3FFu, rv_ = (c >> 10) & 0x3FFu, h = (c >> 20) & 0x3FFu;
+            uint32_t s1 = w1[i], s2 = w2[i];
+            int nmsum = (int)(s2 >> 16) - 128 * (int)(f + rv_);
             if (f) atomicAdd(&C.fwd[g], f);
             if (rv_) atomicAdd(&C.rev[g], rv_);
             if (h) atomicAdd(&C.hi[g], h);
-            atomicAdd(&C.tp[g], (uint32_t)(s & 0x1FFFFFULL));
-            atomicAdd(&C.q[g], (uint32_t)((s >> 21) & 0x1FFFFFULL));
-            atomicAdd(&C.mq[g], (uint32_t)(s >> 42));
+            atomicAdd(&C.tp[g], s1 & 0x1FFFFu);
+            atomicAdd(&C.q[g], s1 >> 17);
+            atomicAdd(&C.mq[g], s2 & 0xFFFFu);
             if (nmsum) atomicAdd(&C.nm[g], nmsum);
             atomicAdd(&C.cov[cell], f + rv_);
             atomicOr((unsigned int *)&C.kflags[cell & ~3LL], 1u << (b + 8 * (cell & 3)));
@@ -645,7 +641,7 @@ void launch_region_spans(const DevState &st, cudaStream_t s) {
     if (st.n_regions > 0) k_region_spans<<<st.n_regions, 256, 0, s>>>(st);
 }
 
-size_t pileup_smem_bytes() { return (size_t)kTileW * 4 * (8 + 8 + 4); }
+size_t pileup_smem_bytes() { return (size_t)kTileW * 4 * 4 * 4; }
 
 cudaError_t launch_pileup(const DevState &st, const DevParams &P, int grid, cudaStream_t s) {
     size_t smem = pileup_smem_bytes();

@@ -300,14 +300,19 @@ __global__ void k_score(DevState st, DevParams P) {
             const uint4 h4 = *reinterpret_cast<const uint4 *>(st.cells.hi + 4 * c);
             const uint32_t fa[4] = {f4.x, f4.y, f4.z, f4.w}, ra[4] = {r4.x, r4.y, r4.z, r4.w};
             const uint32_t ha[4] = {h4.x, h4.y, h4.z, h4.w};
-            bool maybe = false;
+            // the -f gate needs some non-reference allele with freq > -f; an
+            // emitted record needs one with freq >= -f and hicnt >= -r (they
+            // may be different alleles, e.g. at freq exactly -f)
+            bool gate = false, pass = false;
             for (int b = 0; b < 4; b++) {
                 if (!((ex >> b) & 1) || (hasp && b == rbi)) continue;
                 int cnt = (int)(fa[b] + ra[b]);
-                if (cnt > 0 && cnt / (double)cov0 > P.freq && (int)ha[b] >= P.minr && cnt / (double)cov0 >= P.freq)
-                    maybe = true;
+                if (cnt <= 0) continue;
+                double fr = cnt / (double)cov0;
+                if (fr > P.freq) gate = true;
+                if (fr >= P.freq && (int)ha[b] >= P.minr) pass = true;
             }
-            if (!maybe) continue;
+            if (!(gate && pass)) continue;
         }
         PosKeys k;
         if (!visited(st, R, p, k)) continue;

@@ -109,3 +109,20 @@ def test_fisher_batch_matches_oracle():
     for i, (a, b, c, d) in enumerate(tabs.tolist()):
         _, _, two = O.fisher(a, b, c, d)
         assert abs(p[i] - two) <= 1e-9 * max(abs(two), 1e-300), (i, a, b, c, d, p[i], two)
+
+
+def test_somatic_depth_tiles():
+    """Tumor-depth (200x) reads over BED-style 10 kb tiles: the bench shape."""
+    import oracle as O
+    from rabbitvar_gb300 import synth
+    rng = np.random.default_rng(0x5EED0002)
+    g = synth.make_genome(40_000, rng)
+    germ = synth.plant_variants(g, rng, 1e-3, 1e-4, lambda r: 0.5 if r.random() < 0.7 else 1.0)
+    som = synth.plant_variants(g, rng, 4e-4, 0.0, lambda r: r.uniform(0.01, 0.5), mnv_frac=0.3, avoid=germ)
+    rs = synth.simulate(g, germ + som, 200.0, rng, tail_margin=300)
+    regions = [(1 + 10_000 * i, 10_000 * (i + 1)) for i in range(4)]
+    api, ctx = _gpu_ctx(fisher=1)
+    _, _, text = _run_gpu(ctx, api, rs, g, regions)
+    n, ora_text = O.run_regions(rs, g, regions, params=O.default_params(local_realign=0, fisher=1), threads=4)
+    assert n > 30
+    assert diff_records(ora_text.splitlines(), text.splitlines(), rel=1e-9) == []
