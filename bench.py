@@ -198,14 +198,26 @@ def main():
     n_reads = sum(rs.n for _, rs in samples)
     alg_read_bytes = sum(read_alg_bytes(rs) for _, rs in samples)
 
+    host_ms = {"pileup": 0.0, "realign": 0.0, "score": 0.0, "format": 0.0}
+
     def device_step(collect=None):
         kernels = 0
         recs = 0
         for c in ctxs:
+            t0 = time.perf_counter()
             c.pileup()
+            t1 = time.perf_counter()
             c.realign()
+            t2 = time.perf_counter()
             c.score()
+            t3 = time.perf_counter()
             text, n = c.format_records("S", "ctg")
+            t4 = time.perf_counter()
+            if collect is not None:
+                host_ms["pileup"] += (t1 - t0) * 1e3
+                host_ms["realign"] += (t2 - t1) * 1e3
+                host_ms["score"] += (t3 - t2) * 1e3
+                host_ms["format"] += (t4 - t3) * 1e3
             recs += n
             kernels += c.timings()["kernels"]
             if collect is not None:
@@ -268,6 +280,7 @@ def main():
                 "d2h_bytes_per_step": None},
         "gpu_launches": kernels,
         "stage_ms": {k: statistics.mean(s[k] for s in stages) for k in stages[0]},
+        "host_call_ms_per_step": {k: v / args.steps for k, v in host_ms.items()},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
                      "kernel": "k_pileup_tiles", "alg_bytes_per_launch": per_launch_bytes},

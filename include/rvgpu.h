@@ -172,7 +172,8 @@ rv_status rv_last_timings(const rv_ctx *ctx, double *pileup_ms, double *score_ms
  * rv_score calls by stage:
  * stages: [0] cell/table reset, [1] region spans, [2] pileup tiles,
  * [3] in-order edge walk, [4] deferred subtraction + list linking +
- * collision check, [5] insertion coverage adjustment, [6] site scoring. */
+ * collision check, [5] insertion coverage adjustment, [6] site scoring;
+ * [7] the pileup kernel variant the autotuner used (not a time). */
 rv_status rv_stage_times(const rv_ctx *ctx, double *ms, int n);
 
 /* Fisher exact test on the device for n tables (a,b,c,d) stored as 4*n int32;

@@ -249,7 +249,8 @@ class Context:
         self._check(self.L.rv_last_timings(self.h, C.byref(a), C.byref(b), C.byref(c), C.byref(k)))
         return dict(pileup_ms=a.value, score_ms=b.value, total_ms=c.value, kernels=k.value)
 
-    STAGES = ["reset", "region_spans", "pileup_tiles", "edge_walk", "deferred_link_check", "ins_adjust", "score"]
+    STAGES = ["reset", "region_spans", "pileup_tiles", "edge_walk", "deferred_link_check", "ins_adjust", "score",
+              "pileup_variant"]
 
     def stage_times(self) -> dict:
         ms = np.zeros(8)

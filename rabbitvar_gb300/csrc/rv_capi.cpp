@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <climits>
 #include <cstdio>
 #include <cstring>
@@ -401,9 +402,22 @@ rv_status rv_pileup(rv_ctx *ctx, void *stream) {
     launch_region_spans(st, s);
     launch_edge_detect(st, ctx->dp, s);
     RV_CUDA(cudaEventRecord(ctx->ev[5], s));
-    int per_sm = std::max(1, pileup_blocks_per_sm());
+    // autotuner: unless RV_PILEUP_VARIANT pins one, the first batches try each
+    // kernel variant once and later batches use the fastest seen
+    int nvar = pileup_variants();
+    int variant;
+    const char *pin = getenv("RV_PILEUP_VARIANT");
+    if (pin && *pin) variant = std::max(0, std::min(nvar - 1, atoi(pin)));
+    else if (ctx->variant_runs < nvar) variant = ctx->variant_runs;
+    else {
+        variant = 0;
+        for (int v = 1; v < nvar; v++)
+            if (ctx->variant_ms[v] < ctx->variant_ms[variant]) variant = v;
+    }
+    ctx->variant = variant;
+    int per_sm = std::max(1, pileup_blocks_per_sm(variant));
     int grid = std::max(1, std::min<int>((int)ctx->tiles.size(), per_sm * ctx->sm_count));
-    RV_CUDA(launch_pileup(st, ctx->dp, grid, s));
+    RV_CUDA(launch_pileup(st, ctx->dp, grid, s, variant));
     RV_CUDA(cudaEventRecord(ctx->ev[6], s));
     launch_serial(st, ctx->dp, s);
     RV_CUDA(cudaEventRecord(ctx->ev[7], s));
@@ -427,6 +441,10 @@ rv_status rv_pileup(rv_ctx *ctx, void *stream) {
     }
     cudaEventElapsedTime(&ms, ctx->ev[7], ctx->ev[1]);
     ctx->stage_ms[4] = ms;
+    if (!(pin && *pin) && ctx->variant_runs < nvar) {
+        ctx->variant_ms[variant] = ctx->stage_ms[2];
+        ctx->variant_runs++;
+    }
     if (err) {
         char buf[160];
         snprintf(buf, sizeof buf, "pileup device error bits 0x%x", err);
@@ -550,6 +568,7 @@ rv_status rv_last_timings(const rv_ctx *ctx, double *pileup_ms, double *score_ms
 rv_status rv_stage_times(const rv_ctx *ctx, double *ms, int n) {
     if (!ctx || !ms || n < 0) return RV_ERR_ARG;
     for (int i = 0; i < n && i < 8; i++) ms[i] = ctx->stage_ms[i];
+    if (n > 7) ms[7] = ctx->variant;
     return RV_OK;
 }
 

@@ -12,11 +12,12 @@ namespace rv {
 // kernel launchers (rv_pileup.cu, rv_score.cu)
 void launch_init_slots(Slot *slots, unsigned long long n, cudaStream_t s);
 void launch_region_spans(const DevState &st, cudaStream_t s);
-cudaError_t launch_pileup(const DevState &st, const DevParams &P, int grid, cudaStream_t s);
+cudaError_t launch_pileup(const DevState &st, const DevParams &P, int grid, cudaStream_t s, int variant);
+int pileup_variants();
 void launch_serial(const DevState &st, const DevParams &P, cudaStream_t s);
 void launch_edge_detect(const DevState &st, const DevParams &P, cudaStream_t s);
 void launch_resolve(const DevState &st, const DevParams &P, cudaStream_t s);
-int pileup_blocks_per_sm();
+int pileup_blocks_per_sm(int variant);
 size_t pileup_smem_bytes();
 void launch_link(const DevState &st, cudaStream_t s);
 void launch_collisions(const DevState &st, cudaStream_t s);
@@ -141,6 +142,10 @@ struct rv_ctx {
     cudaEvent_t ev[12] = {};
     double pileup_ms = 0, score_ms = 0, total_ms = 0;
     double stage_ms[8] = {};
+    // pileup kernel autotuning: variant in use, per-variant best time seen
+    int variant = -1;
+    double variant_ms[8] = {};
+    int variant_runs = 0;
     int64_t kernels = 0;
 
     rv::DevState state() const;

@@ -452,8 +452,8 @@ __global__ void k_region_spans(DevState st) {
     }
 }
 
-template <int TW>
-__global__ void __launch_bounds__(kPileupThreads) k_pileup_tiles(DevState st, DevParams P) {
+template <int TW, int MINB>
+__global__ void __launch_bounds__(kPileupThreads, MINB) k_pileup_tiles(DevState st, DevParams P) {
     extern __shared__ __align__(16) unsigned char smem[];
     uint32_t *w0 = (uint32_t *)smem;
     uint32_t *w1 = w0 + 4 * TW;
@@ -643,12 +643,32 @@ void launch_region_spans(const DevState &st, cudaStream_t s) {
 
 size_t pileup_smem_bytes() { return (size_t)kTileW * 4 * 4 * 4; }
 
-cudaError_t launch_pileup(const DevState &st, const DevParams &P, int grid, cudaStream_t s) {
+// Instantiations differing in the minimum resident blocks per SM (and so in
+// the register budget per thread); the autotuner times them on the first
+// batch and keeps the fastest (RV_PILEUP_VARIANT pins one: 0, 1 or 2).
+using PileupKernel = void (*)(DevState, DevParams);
+static PileupKernel pileup_variant(int v) {
+    switch (v) {
+    case 0: return k_pileup_tiles<kTileW, 2>;
+    case 1: return k_pileup_tiles<kTileW, 3>;
+    default: return k_pileup_tiles<kTileW, 4>;
+    }
+}
+int pileup_variants() { return 3; }
+
+cudaError_t launch_pileup(const DevState &st, const DevParams &P, int grid, cudaStream_t s, int variant) {
     size_t smem = pileup_smem_bytes();
-    cudaError_t e = cudaFuncSetAttribute(k_pileup_tiles<kTileW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    PileupKernel k = pileup_variant(variant);
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k_pileup_tiles<kTileW><<<grid, kPileupThreads, smem, s>>>(st, P);
+    k<<<grid, kPileupThreads, smem, s>>>(st, P);
     return cudaGetLastError();
+}
+
+int pileup_blocks_per_sm(int variant) {
+    int n = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pileup_variant(variant), kPileupThreads, pileup_smem_bytes());
+    return n;
 }
 
 void launch_edge_detect(const DevState &st, const DevParams &P, cudaStream_t s) {
@@ -663,10 +683,5 @@ void launch_resolve(const DevState &st, const DevParams &P, cudaStream_t s) {
     k_resolve_deferred<<<152, 128, 0, s>>>(st, P, 1 << 16);
 }
 
-int pileup_blocks_per_sm() {
-    int n = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_pileup_tiles<kTileW>, kPileupThreads, pileup_smem_bytes());
-    return n;
-}
 
 }  // namespace rv

@@ -7,6 +7,8 @@
 // (src/modes/simpleMode.cpp:96-108) in FP64.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "rv_walk.cuh"
 
 namespace rv {
@@ -270,14 +272,27 @@ __device__ double fisher_two_sided(int n11, int n12, int n21, int n22) {
     return st > 1.0 ? 1.0 : st;
 }
 
+// Each block scores a contiguous chunk of positions; the region of the
+// chunk start is found once and threads advance from it.
+constexpr int kScoreChunk = 2048;
+
 __global__ void k_score(DevState st, DevParams P) {
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < st.n_score;
-         t += (int64_t)gridDim.x * blockDim.x) {
-        int lo = 0, hi = st.n_regions - 1;
-        while (lo < hi) {
-            int mid = (lo + hi + 1) >> 1;
-            if (st.score_base[mid] <= t) lo = mid; else hi = mid - 1;
+    __shared__ int s_lo;
+    for (int64_t c0 = (int64_t)blockIdx.x * kScoreChunk; c0 < st.n_score; c0 += (int64_t)gridDim.x * kScoreChunk) {
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int a = 0, b = st.n_regions - 1;
+            while (a < b) {
+                int mid = (a + b + 1) >> 1;
+                if (st.score_base[mid] <= c0) a = mid; else b = mid - 1;
+            }
+            s_lo = a;
         }
+        __syncthreads();
+        const int lo0 = s_lo;
+    for (int64_t t = c0 + threadIdx.x; t < c0 + kScoreChunk && t < st.n_score; t += blockDim.x) {
+        int lo = lo0;
+        while (lo + 1 < st.n_regions && st.score_base[lo + 1] <= t) lo++;
         const Region &R = st.regions[lo];
         int p = R.start + (int)(t - st.score_base[lo]);
         if (p < R.clo || p > R.chi) continue;
@@ -480,6 +495,7 @@ __global__ void k_score(DevState st, DevParams P) {
             }
         }
     }
+    }
 }
 
 // Batched Fisher tests (rv_fisher_batch)
@@ -498,7 +514,10 @@ void launch_ins_adjust(const DevState &st, cudaStream_t s) {
     if (st.cells.n_cells > 0) k_ins_adjust<<<1216, 256, 0, s>>>(st);
 }
 void launch_score(const DevState &st, const DevParams &P, cudaStream_t s) {
-    if (st.n_score > 0) k_score<<<1216, 128, 0, s>>>(st, P);
+    if (st.n_score > 0) {
+        int64_t chunks = (st.n_score + kScoreChunk - 1) / kScoreChunk;
+        k_score<<<(int)std::min<int64_t>(chunks, 4864), 256, 0, s>>>(st, P);
+    }
 }
 void launch_fisher(const int32_t *tab, int64_t n, double *p2, double *ratio, cudaStream_t s) {
     if (n > 0) k_fisher<<<(int)((n + 127) / 128 < 4096 ? (n + 127) / 128 : 4096), 128, 0, s>>>(tab, n, p2, ratio);
