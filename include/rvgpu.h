@@ -176,6 +176,10 @@ rv_status rv_last_timings(const rv_ctx *ctx, double *pileup_ms, double *score_ms
  * [7] the pileup kernel variant the autotuner used (not a time). */
 rv_status rv_stage_times(const rv_ctx *ctx, double *ms, int n);
 
+/* Bytes copied host->device by the last rv_submit_batch and device->host
+ * by the calls since then (realigner boundary, scored candidates). */
+rv_status rv_io_bytes(const rv_ctx *ctx, int64_t *h2d, int64_t *d2h);
+
 /* Fisher exact test on the device for n tables (a,b,c,d) stored as 4*n int32;
  * writes two-sided p and the simple-mode ratio. Replaces the kt_fisher_exact
  * call sites (src/modes/simpleMode.cpp:96-108). */

@@ -60,7 +60,7 @@ class SiteRecord(C.Structure):
 
 EXPORTS = ["rv_default_params", "rv_create", "rv_destroy", "rv_last_error", "rv_upload_reference",
            "rv_submit_batch", "rv_pileup", "rv_realign", "rv_score", "rv_format_records", "rv_fetch_records",
-           "rv_call_regions", "rv_export_maps", "rv_last_timings", "rv_stage_times", "rv_fisher_batch", "rv_bam_read",
+           "rv_call_regions", "rv_export_maps", "rv_last_timings", "rv_stage_times", "rv_io_bytes", "rv_fisher_batch", "rv_bam_read",
            "rv_bam_contigs", "rv_bam_batch", "rv_bam_free", "rv_fasta_read", "rv_free", "rv_alloc_pinned",
            "rv_free_pinned"]
 
@@ -95,6 +95,7 @@ def lib():
                                   C.POINTER(i64)]
     L.rv_fisher_batch.argtypes = [vp, vp, i64, vp, vp]
     L.rv_stage_times.argtypes = [vp, vp, C.c_int]
+    L.rv_io_bytes.argtypes = [vp, C.POINTER(i64), C.POINTER(i64)]
     L.rv_bam_read.argtypes = [C.c_char_p, C.c_int, C.POINTER(vp)]
     L.rv_bam_contigs.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(vp), C.POINTER(vp)]
     L.rv_bam_batch.argtypes = [vp, C.c_int, C.POINTER(ReadBatch)]
@@ -248,6 +249,11 @@ class Context:
         k = C.c_int64()
         self._check(self.L.rv_last_timings(self.h, C.byref(a), C.byref(b), C.byref(c), C.byref(k)))
         return dict(pileup_ms=a.value, score_ms=b.value, total_ms=c.value, kernels=k.value)
+
+    def io_bytes(self) -> tuple[int, int]:
+        a, b = C.c_int64(), C.c_int64()
+        self._check(self.L.rv_io_bytes(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
 
     STAGES = ["reset", "region_spans", "pileup_tiles", "edge_walk", "deferred_link_check", "ins_adjust", "score",
               "pileup_variant"]

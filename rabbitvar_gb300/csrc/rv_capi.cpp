@@ -86,6 +86,7 @@ DevState rv_ctx::state() const {
     s.ref_len = ref_len;
     s.err = d_counters + CNT_ERR;
     s.head = d_head;
+    s.head_sc = d_head ? d_head + cap_cells : nullptr;
     s.score_base = d_score_base;
     s.n_score = n_score;
     s.cand = d_cand;
@@ -234,6 +235,8 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
         (st = grow(ctx, ctx->d_seq, cb2, (size_t)std::max<int64_t>(b->n_bases, 32) / 2 + 64)))
         return st;
     ctx->cap_bases = cb;
+    ctx->io_h2d = n * (4 + 4 + 4 + 4 + 2 + 2 + 1 + 4 + 8) + b->n_cigar_words * 4 + (b->n_bases + 1) / 2 + b->n_bases;
+    ctx->io_d2h = 0;
     if (n > 0) {
         RV_CUDA(cudaMemcpyAsync(ctx->d_pos, b->pos, n * 4, cudaMemcpyHostToDevice, s));
         RV_CUDA(cudaMemcpyAsync(ctx->d_mpos, b->mpos, n * 4, cudaMemcpyHostToDevice, s));
@@ -333,7 +336,7 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
         size_t cap = need_cells + need_cells / 4 + 1024;
         cap = (cap + 63) & ~(size_t)63;
         RV_CUDA(cudaMalloc(&ctx->d_cellmem, cap * (8 * 16 + 4 + 1)));
-        RV_CUDA(cudaMalloc((void **)&ctx->d_head, cap * 4));
+        RV_CUDA(cudaMalloc((void **)&ctx->d_head, cap * 8));
         ctx->cap_cells = cap;
     }
     {
@@ -393,7 +396,7 @@ rv_status rv_pileup(rv_ctx *ctx, void *stream) {
     size_t cap = ctx->cap_cells;
     RV_CUDA(cudaEventRecord(ctx->ev[0], s));
     RV_CUDA(cudaMemsetAsync(ctx->d_cellmem, 0, cap * (8 * 16 + 4 + 1), s));
-    RV_CUDA(cudaMemsetAsync(ctx->d_head, 0xFF, cap * 4, s));
+    RV_CUDA(cudaMemsetAsync(ctx->d_head, 0xFF, cap * 8, s));
     RV_CUDA(cudaMemsetAsync(ctx->d_counters, 0, 64 * sizeof(unsigned int), s));
     RV_CUDA(cudaMemsetAsync(ctx->d_arena, 0, 16, s));
     launch_init_slots(ctx->d_slots, ctx->hash_cap, s);
@@ -510,6 +513,7 @@ rv_status rv_score(rv_ctx *ctx, void *stream) {
     used = std::min<unsigned long long>(used, ctx->arena_cap);
     ctx->h_arena.resize(used);
     if (used) RV_CUDA(cudaMemcpy(ctx->h_arena.data(), ctx->d_arena, used, cudaMemcpyDeviceToHost));
+    ctx->io_d2h += (int64_t)sizeof hdr + (int64_t)n * (int64_t)sizeof(CandVar) + 8 + (int64_t)used;
     ctx->stage = 4;
     return RV_OK;
 }
@@ -562,6 +566,13 @@ rv_status rv_last_timings(const rv_ctx *ctx, double *pileup_ms, double *score_ms
     if (score_ms) *score_ms = ctx->score_ms;
     if (total_ms) *total_ms = ctx->pileup_ms + ctx->score_ms;
     if (kernels) *kernels = ctx->kernels;
+    return RV_OK;
+}
+
+rv_status rv_io_bytes(const rv_ctx *ctx, int64_t *h2d, int64_t *d2h) {
+    if (!ctx) return RV_ERR_ARG;
+    if (h2d) *h2d = ctx->io_h2d;
+    if (d2h) *d2h = ctx->io_d2h;
     return RV_OK;
 }
 

@@ -147,6 +147,8 @@ struct rv_ctx {
     double variant_ms[8] = {};
     int variant_runs = 0;
     int64_t kernels = 0;
+    // bytes moved host<->device since the last rv_submit_batch
+    int64_t io_h2d = 0, io_d2h = 0;
 
     rv::DevState state() const;
 };

@@ -17,6 +17,7 @@
 #include <map>
 #include <set>
 #include <string>
+#include <thread>
 #include <tuple>
 #include <vector>
 
@@ -278,6 +279,7 @@ rv_status pull_slots(rv_ctx *ctx, unsigned int n, std::vector<Slot> &slots, std:
     HCUDA(cudaMemcpyAsync(slots.data(), ctx->d_tmp_slots, (size_t)n * sizeof(Slot), cudaMemcpyDeviceToHost, ctx->stream));
     HCUDA(cudaMemcpyAsync(idx.data(), ctx->d_tmp_idx, (size_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
     HCUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->io_d2h += (int64_t)n * (int64_t)(sizeof(Slot) + 4);
     return RV_OK;
 }
 
@@ -547,12 +549,14 @@ struct RecVar {
 };
 
 std::string join(const RefWin &R, int from, int to) {
-    std::string s;
-    for (int i = from; i <= to; i++) {
-        if (!R.has(i)) throw NoRef();
-        s += R.at(i);
-    }
-    return s;
+    if (from > to) return std::string();
+    if (!R.has(from) || !R.has(to)) throw NoRef();  // the window is one contiguous range
+    return std::string(R.ref->data() + (from - 1), (size_t)(to - from + 1));
+}
+
+// joinRef's failure condition without building the string
+void join_check(const RefWin &R, int from, int to) {
+    if (from <= to && (!R.has(from) || !R.has(to))) throw NoRef();
 }
 
 void repl_first(std::string &s, const std::string &a, const std::string &b) {
@@ -575,7 +579,11 @@ bool amp_tail(const std::string &s, std::string &run) {
     return false;
 }
 
-void describe(RecVar &v, std::string &g1, int position, const RefWin &R, const rv_params &P) {
+// collectReferenceVariants for one variant.  With full == false (a variant
+// the device pre-screen rules out of the output) only what can affect later
+// variants of the position is done: the genotype-1 edits and the
+// reference-window checks whose failure ends the position.
+void describe(RecVar &v, std::string &g1, int position, const RefWin &R, const rv_params &P, bool full) {
     std::string g2 = v.desc;
     if (starts(g2, '+')) g2 = "+" + std::to_string(g2.size() - 1);
     const std::string &vn = v.desc;
@@ -588,6 +596,10 @@ void describe(RecVar &v, std::string &g1, int position, const RefWin &R, const r
     int L = R.len;
     if (starts(vn, '+')) {
         if (vn.find('&') == std::string::npos && vn.find('#') == std::string::npos && vn.find("<dup") == std::string::npos) {
+            if (!full) {
+                join_check(R, position - 50 > 1 ? position - 50 : 1, position);
+                join_check(R, position + 1, position + 70 > L ? L : position + 70);
+            } else {
             std::string t1 = vn.substr(1);
             std::string left = join(R, position - 50 > 1 ? position - 50 : 1, position);
             std::string t2 = join(R, position + 1, position + 70 > L ? L : position + 70);
@@ -595,6 +607,7 @@ void describe(RecVar &v, std::string &g1, int position, const RefWin &R, const r
             if (a.msi < b.msi) { a.msi = b.msi; a.unit = b.unit; }
             if (a.msi <= a.shift3 / (double)t1.size()) a.msi = a.shift3 / (double)t1.size();
             msi = a.msi; shift3 = a.shift3; unit = a.unit;
+            }
         }
         if (P.move_indels_3) { startp += shift3; endp += shift3; }
         refa = R.has(position) ? std::string(1, R.at(position)) : "";
@@ -605,6 +618,10 @@ void describe(RecVar &v, std::string &g1, int position, const RefWin &R, const r
             size_t k = 1;
             while (k < vara.size() && isdigit((unsigned char)vara[k])) k++;
             if (k > 1) vara.erase(0, k);
+            if (!full) {
+                join_check(R, position - 70 > 1 ? position - 70 : 1, position - 1);
+                join_check(R, position, position + dellen + 70 > L ? L : position + dellen + 70);
+            } else {
             std::string left = join(R, position - 70 > 1 ? position - 70 : 1, position - 1);
             std::string ts = join(R, position, position + dellen + 70 > L ? L : position + dellen + 70);
             std::string a1 = ts.substr(0, std::min<size_t>(dellen, ts.size()));
@@ -613,6 +630,7 @@ void describe(RecVar &v, std::string &g1, int position, const RefWin &R, const r
             if (a.msi < b.msi) { a.msi = b.msi; a.unit = b.unit; }
             if (a.msi <= a.shift3 / (double)dellen) a.msi = a.shift3 / (double)dellen;
             msi = a.msi; shift3 = a.shift3; unit = a.unit;
+            }
         }
         if (vn.find('&') == std::string::npos && vn.find('#') == std::string::npos && vn.find('^') == std::string::npos) {
             if (P.move_indels_3) startp += shift3;
@@ -622,10 +640,15 @@ void describe(RecVar &v, std::string &g1, int position, const RefWin &R, const r
         }
         if (dellen < P.svminlen) refa += join(R, position, position + dellen - 1);
     } else {
-        std::string t1 = join(R, position - 30 > 1 ? position - 30 : 1, position + 1);
-        std::string t2 = join(R, position + 2, position + 70 > L ? L : position + 70);
-        Msi a = find_msi(t1, t2, "");
-        msi = a.msi; shift3 = a.shift3; unit = a.unit;
+        if (!full) {
+            join_check(R, position - 30 > 1 ? position - 30 : 1, position + 1);
+            join_check(R, position + 2, position + 70 > L ? L : position + 70);
+        } else {
+            std::string t1 = join(R, position - 30 > 1 ? position - 30 : 1, position + 1);
+            std::string t2 = join(R, position + 2, position + 70 > L ? L : position + 70);
+            Msi a = find_msi(t1, t2, "");
+            msi = a.msi; shift3 = a.shift3; unit = a.unit;
+        }
         refa = R.has(position) ? std::string(1, R.at(position)) : "";
         vara = vn;
     }
@@ -679,6 +702,11 @@ void describe(RecVar &v, std::string &g1, int position, const RefWin &R, const r
             repl_first(g2, "^", "i");
             break;
         }
+    }
+    if (!full) {
+        join_check(R, startp - 20 < 1 ? 1 : startp - 20, startp - 1);
+        join_check(R, endp + 1, endp + 20 > L ? L : endp + 20);
+        return;  // not emitted: no record fields needed
     }
     v.leftseq = join(R, startp - 20 < 1 ? 1 : startp - 20, startp - 1);
     v.rightseq = join(R, endp + 1, endp + 20 > L ? L : endp + 20);
@@ -760,28 +788,21 @@ std::string f6(double d) {
 
 }  // namespace
 
-rv_status host_format_records(rv_ctx *ctx, const char *sample, const char *gene) {
+// Text and numeric records of the candidate positions [g0, g1) of `groups`.
+static void format_groups(const rv_ctx *ctx, const std::vector<const CandVar *> &order,
+                          const std::vector<std::pair<size_t, size_t>> &groups, size_t g0, size_t g1,
+                          const char *sample, const char *gene, std::string &text,
+                          std::vector<rv_site_record> &recs) {
     const rv_params &P = ctx->params;
-    std::vector<const CandVar *> order(ctx->h_cand.size());
-    for (size_t i = 0; i < order.size(); i++) order[i] = &ctx->h_cand[i];
-    std::sort(order.begin(), order.end(), [](const CandVar *a, const CandVar *b) {
-        if (a->region != b->region) return a->region < b->region;
-        if (a->pos != b->pos) return a->pos < b->pos;
-        return a->rank < b->rank;
-    });
-    ctx->text.clear();
-    ctx->h_records.clear();
-    ctx->n_records = 0;
     const std::string &chr = ctx->chr;
-    size_t i = 0;
-    while (i < order.size()) {
-        size_t j = i;
-        while (j < order.size() && order[j]->region == order[i]->region && order[j]->pos == order[i]->pos) j++;
+    for (size_t gi = g0; gi < g1; gi++) {
+        size_t i = groups[gi].first, j = groups[gi].second;
         const Region &Rg = ctx->regions[order[i]->region];
         RefWin R{&ctx->ref_host, Rg.ws, Rg.we, ctx->ref_len};
         int position = order[i]->pos;
         const CandVar *ref = nullptr;
         std::vector<RecVar> vs;
+        vs.reserve(j - i);
         for (size_t k = i; k < j; k++) {
             const CandVar *c = order[k];
             if (c->kind == 0) { ref = c; continue; }
@@ -789,17 +810,17 @@ rv_status host_format_records(rv_ctx *ctx, const char *sample, const char *gene)
             v.c = c;
             if (c->key_len < 0) v.desc = std::string(1, kBases[c->key_off & 3]);
             else v.desc.assign((const char *)ctx->h_arena.data() + c->key_off, c->key_len);
-            vs.push_back(v);
+            vs.push_back(std::move(v));
         }
         std::string refdesc = ref ? std::string(1, R.at(position)) : "";
-        std::string g1;
-        if (ref && ref->freq >= P.freq) g1 = refdesc;
-        else if (!vs.empty()) g1 = vs[0].desc;
-        else g1 = refdesc;
-        if (starts(g1, '+')) g1 = "+" + std::to_string(g1.size() - 1);
+        std::string g1s;
+        if (ref && ref->freq >= P.freq) g1s = refdesc;
+        else if (!vs.empty()) g1s = vs[0].desc;
+        else g1s = refdesc;
+        if (starts(g1s, '+')) g1s = "+" + std::to_string(g1s.size() - 1);
         try {
             for (RecVar &v : vs) {
-                describe(v, g1, position, R, P);
+                describe(v, g1s, position, R, P, v.c->pass != 0);
                 v.sbf = std::string(ref ? std::to_string(ref->bias) : std::string("0")) + ";" + std::to_string(v.c->bias);
             }
         } catch (const NoRef &) {
@@ -808,57 +829,59 @@ rv_status host_format_records(rv_ctx *ctx, const char *sample, const char *gene)
         }
         std::string reg = chr + ":" + std::to_string(Rg.start) + "-" + std::to_string(Rg.end);
         for (RecVar &v : vs) {
-            if (!v.filled) continue;
+            if (!v.filled || !v.c->pass) continue;
             if (v.refallele.find('N') != std::string::npos) continue;
             v.vartype = var_type(v);
             if (!good_var(v, ref, P)) continue;
             if (v.vartype == "Complex") adj_complex(v);
             const CandVar &c = *v.c;
-            std::vector<std::string> f;
-            f.push_back(sample);
-            f.push_back(gene);
-            f.push_back(chr);
-            f.push_back(std::to_string(v.startp));
-            f.push_back(std::to_string(v.endp));
-            f.push_back(v.refallele);
-            f.push_back(v.varallele);
-            f.push_back(std::to_string(c.tpc));
-            f.push_back(std::to_string(c.pc));
-            f.push_back(std::to_string(c.rfc));
-            f.push_back(std::to_string(c.rrc));
-            f.push_back(std::to_string(c.fwd));
-            f.push_back(std::to_string(c.rev));
-            f.push_back(v.genotype.empty() ? "0" : v.genotype);
-            f.push_back(f6(c.freq));
-            f.push_back(v.sbf);
-            f.push_back(f6(c.pmean));
-            f.push_back(c.pstd ? "1" : "0");
-            f.push_back(f6(c.qual));
-            f.push_back(c.qstd ? "1" : "0");
+            char num[64];
+            auto add = [&](const std::string &x, bool last = false) {
+                text += x;
+                text += last ? '\n' : '\t';
+            };
+            auto addi = [&](long long x) { snprintf(num, sizeof num, "%lld", x); add(num); };
+            auto addf = [&](double x) { snprintf(num, sizeof num, "%f", x); add(num); };
+            add(sample);
+            add(gene);
+            add(chr);
+            addi(v.startp);
+            addi(v.endp);
+            add(v.refallele);
+            add(v.varallele);
+            addi(c.tpc);
+            addi(c.pc);
+            addi(c.rfc);
+            addi(c.rrc);
+            addi(c.fwd);
+            addi(c.rev);
+            add(v.genotype.empty() ? "0" : v.genotype);
+            addf(c.freq);
+            add(v.sbf);
+            addf(c.pmean);
+            add(c.pstd ? "1" : "0");
+            addf(c.qual);
+            add(c.qstd ? "1" : "0");
             if (P.fisher) {
-                f.push_back(f6(c.fisher_p));
-                f.push_back(f6(c.fisher_ratio));
+                addf(c.fisher_p);
+                addf(c.fisher_ratio);
             }
-            f.push_back(f6(c.mq));
-            f.push_back(f6(c.qratio));
-            f.push_back(f6(c.hifreq));
-            f.push_back(f6(c.extrafreq));
-            f.push_back(std::to_string(v.shift3));
-            f.push_back(f6(v.msi));
-            f.push_back(std::to_string(v.msint));
-            f.push_back(c.nm > 0 ? f6(c.nm) : "0");
-            f.push_back(std::to_string(c.hicnt));
-            f.push_back(std::to_string(c.hicov));
-            f.push_back(v.leftseq.empty() ? "0" : v.leftseq);
-            f.push_back(v.rightseq.empty() ? "0" : v.rightseq);
-            f.push_back(reg);
-            f.push_back(v.vartype);
-            f.push_back(f6(0.0));
-            f.push_back("0");
-            for (size_t k = 0; k < f.size(); k++) {
-                ctx->text += f[k];
-                ctx->text += k + 1 < f.size() ? '\t' : '\n';
-            }
+            addf(c.mq);
+            addf(c.qratio);
+            addf(c.hifreq);
+            addf(c.extrafreq);
+            addi(v.shift3);
+            addf(v.msi);
+            addi(v.msint);
+            if (c.nm > 0) addf(c.nm); else add("0");
+            addi(c.hicnt);
+            addi(c.hicov);
+            add(v.leftseq.empty() ? "0" : v.leftseq);
+            add(v.rightseq.empty() ? "0" : v.rightseq);
+            add(reg);
+            add(v.vartype);
+            addf(0.0);
+            add("0", true);
             rv_site_record r;
             memset(&r, 0, sizeof r);
             r.region = c.region;
@@ -888,11 +911,47 @@ rv_status host_format_records(rv_ctx *ctx, const char *sample, const char *gene)
             r.hicov = c.hicov;
             r.fisher_p = c.fisher_p;
             r.fisher_ratio = c.fisher_ratio;
-            ctx->h_records.push_back(r);
-            ctx->n_records++;
+            recs.push_back(r);
         }
+    }
+}
+
+rv_status host_format_records(rv_ctx *ctx, const char *sample, const char *gene) {
+    std::vector<const CandVar *> order(ctx->h_cand.size());
+    for (size_t i = 0; i < order.size(); i++) order[i] = &ctx->h_cand[i];
+    std::sort(order.begin(), order.end(), [](const CandVar *a, const CandVar *b) {
+        if (a->region != b->region) return a->region < b->region;
+        if (a->pos != b->pos) return a->pos < b->pos;
+        return a->rank < b->rank;
+    });
+    std::vector<std::pair<size_t, size_t>> groups;
+    for (size_t i = 0; i < order.size();) {
+        size_t j = i;
+        while (j < order.size() && order[j]->region == order[i]->region && order[j]->pos == order[i]->pos) j++;
+        groups.push_back({i, j});
         i = j;
     }
+    // candidate positions are independent: split them over host threads
+    int nt = (int)std::min<size_t>(std::max(1u, std::thread::hardware_concurrency()), 32);
+    nt = (int)std::min<size_t>((size_t)nt, std::max<size_t>(1, groups.size() / 64));
+    std::vector<std::string> texts(nt);
+    std::vector<std::vector<rv_site_record>> recs(nt);
+    std::vector<std::thread> pool;
+    size_t per = (groups.size() + nt - 1) / std::max(1, nt);
+    for (int t = 0; t < nt; t++) {
+        size_t a = std::min(groups.size(), t * per), b = std::min(groups.size(), (t + 1) * per);
+        auto job = [&, t, a, b]() { format_groups(ctx, order, groups, a, b, sample, gene, texts[t], recs[t]); };
+        if (t + 1 < nt) pool.emplace_back(job);
+        else job();
+    }
+    for (auto &th : pool) th.join();
+    ctx->text.clear();
+    ctx->h_records.clear();
+    for (int t = 0; t < nt; t++) {
+        ctx->text += texts[t];
+        ctx->h_records.insert(ctx->h_records.end(), recs[t].begin(), recs[t].end());
+    }
+    ctx->n_records = (int64_t)ctx->h_records.size();
     return RV_OK;
 }
 

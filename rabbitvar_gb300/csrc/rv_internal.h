@@ -162,7 +162,8 @@ struct DevState {
     const char *ref;        // whole contig, uppercase, 0-based
     int32_t ref_len;
     unsigned int *err;
-    uint32_t *head;          // per cell: first hash slot at that position
+    uint32_t *head;          // per cell: first NONINS/INS hash slot at that position
+    uint32_t *head_sc;       // per cell: first soft-clip slot at that position
     int64_t *score_base;     // per region: first scoring thread (prefix sum of region lengths)
     int64_t n_score;
     CandVar *cand;

@@ -29,7 +29,8 @@ __global__ void k_link_slots(DevState st) {
         const Region &R = st.regions[s.region];
         if (s.pos < R.clo || s.pos > R.chi) continue;
         int64_t c = cell_index(R, s.pos);
-        s.next = atomicExch(&st.head[c], (uint32_t)i);
+        bool clip = s.kind != KIND_NONINS && s.kind != KIND_INS;
+        s.next = atomicExch(clip ? &st.head_sc[c] : &st.head[c], (uint32_t)i);
     }
 }
 

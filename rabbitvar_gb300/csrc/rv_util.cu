@@ -87,10 +87,13 @@ __global__ void k_select_mnv(DevState st, uint32_t *out, unsigned int *n_out) {
 __global__ void k_gather_lists(DevState st, const int64_t *cells, int64_t n, uint32_t *out, unsigned int *n_out,
                                unsigned int cap) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        int steps = 0;
-        for (uint32_t s = st.head[cells[i]]; s != 0xFFFFFFFFu && steps < (1 << 20); s = st.hash.slots[s].next, steps++) {
-            unsigned int k = atomicAdd(n_out, 1u);
-            if (k < cap) out[k] = s;
+        for (int list = 0; list < 2; list++) {
+            int steps = 0;
+            uint32_t h = list == 0 ? st.head[cells[i]] : st.head_sc[cells[i]];
+            for (uint32_t s = h; s != 0xFFFFFFFFu && steps < (1 << 20); s = st.hash.slots[s].next, steps++) {
+                unsigned int k = atomicAdd(n_out, 1u);
+                if (k < cap) out[k] = s;
+            }
         }
     }
 }
