@@ -1,0 +1,72 @@
+"""The oracle (CPU restatement) against golden outputs of the reference.
+
+The golden files under tests/golden/ were produced by the reference itself
+(its unmodified sources built here against the project's htslib-API shim;
+tests/golden/make_golden.py).  The oracle must reproduce every map entry
+after the CIGAR walk (P), after the realigner (R), every per-site variant (V)
+and every emitted record, exactly (doubles to 1e-12 relative).
+"""
+import gzip
+import json
+import os
+
+import pytest
+
+from cmp import diff_dump, diff_records
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLD = os.path.join(HERE, "golden")
+META = json.load(open(os.path.join(GOLD, "golden.json")))
+
+P_TAGS = ["P_ML", "PN", "PI", "PC", "PS5", "PS3", "PCI", "PCD", "PMN"]
+R_TAGS = ["RN", "RI", "RC"]
+
+
+def _params(flags):
+    import oracle as O
+    kw = {"local_realign": 0}
+    if "-u" in flags:
+        kw["unique_fwd"] = 1
+    if "--fisher" in flags:
+        kw["fisher"] = 1
+    return O.default_params(**kw)
+
+
+@pytest.mark.parametrize("name", sorted(META))
+def test_oracle_matches_reference_golden(name):
+    import oracle as O
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(GOLD, "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    g, rs, (a, b), flags = mg.CASES[name]()
+    assert mg.readset_fingerprint(rs) == META[name]["fingerprint"], "synthetic generator drifted: rerun make_golden.py"
+    gold = gzip.open(os.path.join(GOLD, f"{name}.dump.txt.gz"), "rt").read()
+    ora = O.run_region(rs, g, a, b, stages="PRVO", params=_params(flags))
+    # pp/pq (last-seen read position/quality) are compared too: the oracle is sequential
+    assert diff_dump(gold, ora, P_TAGS, skip=(), rel=1e-12) == []
+    assert diff_dump(gold, ora, R_TAGS, skip=(), rel=1e-12) == []
+    assert diff_dump(gold, ora, ["V"], skip=(), rel=1e-12, key_cols=3) == []
+    recs = open(os.path.join(GOLD, f"{name}.records.txt")).read().splitlines()
+    mine = [l for l in ora.splitlines() if l.startswith("S\t")]
+    assert len(recs) == META[name]["records"] > 5
+    assert diff_records(recs, mine, rel=0) == []
+
+
+def test_oracle_matches_reference_binary_config0(tmp_path):
+    """Against the reference binary itself when it was built here (the
+    reference tree is not present on GPU hosts)."""
+    import oracle as O
+    if not O.have_reference():
+        pytest.skip("reference binaries not built (reference tree absent)")
+    from rabbitvar_gb300 import synth
+    g, vs, rs = synth.germline_small()
+    bam, fa = str(tmp_path / "s.bam"), str(tmp_path / "ref.fa")
+    synth.write_bam(bam, rs)
+    synth.write_fasta(fa, rs.contig, g)
+    ref = O.reference_dump(fa, bam, "ctg:1-100000", ["-k", "0"], stages="PV")
+    ora = O.run_region(rs, g, 1, 100000, stages="PVO", params=O.default_params(local_realign=0))
+    assert diff_dump(ref, ora, P_TAGS, skip=(), rel=1e-12) == []
+    assert diff_dump(ref, ora, ["V"], skip=(), rel=1e-12, key_cols=3) == []
+    recs = O.reference_records(fa, bam, "ctg:1-100000", str(tmp_path / "o.txt"), ["-k", "0"])
+    assert diff_records(recs, [l for l in ora.splitlines() if l.startswith("S\t")], rel=0) == []
