@@ -64,6 +64,13 @@ def lib():
                                       C.c_int, C.c_char_p, C.POINTER(Params), C.c_int, C.POINTER(C.c_void_p),
                                       C.POINTER(C.c_size_t)]
         L.rvo_run_regions.restype = C.c_long
+        L.rvo_run_somatic.argtypes = [C.POINTER(Reads), C.POINTER(Reads), C.c_char_p, C.c_int, C.c_char_p, C.c_int,
+                                      C.c_int, C.c_char_p, C.POINTER(Params), C.c_char_p, C.POINTER(C.c_void_p),
+                                      C.POINTER(C.c_size_t)]
+        L.rvo_run_somatic_regions.argtypes = [C.POINTER(Reads), C.POINTER(Reads), C.c_char_p, C.c_int, C.c_char_p,
+                                              C.c_void_p, C.c_void_p, C.c_int, C.c_char_p, C.POINTER(Params),
+                                              C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_size_t)]
+        L.rvo_run_somatic_regions.restype = C.c_long
         L.rvo_free.argtypes = [C.c_void_p]
         L.rvo_fisher.argtypes = [C.c_int] * 4 + [C.POINTER(C.c_double)] * 3
         L.rvo_fisher.restype = C.c_double
@@ -132,6 +139,42 @@ def run_regions(rs, genome, regions, sample: str = "S", params: Params | None = 
     return cnt, s
 
 
+def run_somatic(tumor, normal, genome, start: int, end: int, stages: str = "O", sample: str = "T",
+                params: Params | None = None) -> str:
+    """Somatic mode on region [start, end] (1-based) of a tumor/normal pair."""
+    keep: list = []
+    rt = _reads_struct(tumor, keep)
+    rn = _reads_struct(normal, keep)
+    g = _genome_bytes(genome)
+    p = params or default_params()
+    out = C.c_void_p()
+    n = C.c_size_t()
+    lib().rvo_run_somatic(C.byref(rt), C.byref(rn), g, len(g), tumor.contig.encode(), start, end, sample.encode(),
+                          C.byref(p), stages.encode(), C.byref(out), C.byref(n))
+    s = C.string_at(out, n.value).decode()
+    lib().rvo_free(out)
+    return s
+
+
+def run_somatic_regions(tumor, normal, genome, regions, sample: str = "T", params: Params | None = None,
+                        threads: int = 1):
+    keep: list = []
+    rt = _reads_struct(tumor, keep)
+    rn = _reads_struct(normal, keep)
+    g = _genome_bytes(genome)
+    p = params or default_params()
+    st = np.ascontiguousarray([a for a, _ in regions], np.int32)
+    en = np.ascontiguousarray([b for _, b in regions], np.int32)
+    out = C.c_void_p()
+    n = C.c_size_t()
+    cnt = lib().rvo_run_somatic_regions(C.byref(rt), C.byref(rn), g, len(g), tumor.contig.encode(), st.ctypes.data,
+                                        en.ctypes.data, len(regions), sample.encode(), C.byref(p), threads,
+                                        C.byref(out), C.byref(n))
+    s = C.string_at(out, n.value).decode()
+    lib().rvo_free(out)
+    return cnt, s
+
+
 def fisher(a: int, b: int, c: int, d: int):
     l, r, t = C.c_double(), C.c_double(), C.c_double()
     lib().rvo_fisher(a, b, c, d, C.byref(l), C.byref(r), C.byref(t))
@@ -149,6 +192,8 @@ def reference_dump(fasta: str, bam: str, region: str, extra: list[str] | None = 
 
 def reference_records(fasta: str, bam: str, region: str, out_path: str, extra: list[str] | None = None,
                       sample: str = "S") -> list[str]:
+    """Records of the reference binary; `bam` may be a 'T.bam|N.bam' pair with
+    `sample` 'T|N' (somatic mode)."""
     cmd = [REF_BIN, "-G", fasta, "-b", bam, "-N", sample, "-R", region, "--out", out_path] + (extra or [])
     subprocess.run(cmd, check=True, capture_output=True, text=True)
     with open(out_path) as f:

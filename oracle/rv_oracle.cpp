@@ -1040,9 +1040,11 @@ struct Scorer {
     Ref &R;
     int chr_len;
     int rs, re;
+    bool somatic;  // a second BAM is configured (conf->bam.hasBam2())
     map<int, PosVars> aligned;
 
-    Scorer(const rvo_params &p, Maps &m, Ref &r, int cl, int s, int e) : P(p), M(m), R(r), chr_len(cl), rs(s), re(e) {}
+    Scorer(const rvo_params &p, Maps &m, Ref &r, int cl, int s, int e, bool som = false)
+        : P(p), M(m), R(r), chr_len(cl), rs(s), re(e), somatic(som) {}
 
     Var make_var(const string &k, const Stat &c, int ttcov, int hicov) {
         Var v;
@@ -1076,7 +1078,8 @@ struct Scorer {
             auto cit = M.cov.find(position);
             if (cit == M.cov.end() || cit->second == 0) continue;
             // isTheSameVariationOnRef: src/ToVarsBuilder.cpp:213-233
-            if (vm.size() == 1 && !has_ins && R.has(position) && vm.count(string(1, R.at(position))) && !P.do_pileup)
+            if (vm.size() == 1 && !has_ins && R.has(position) && vm.count(string(1, R.at(position))) && !P.do_pileup &&
+                !somatic)
                 continue;
             int tpc = cit->second;
             int hicov = 0;  // calcHicov: src/ToVarsBuilder.cpp:570-587
@@ -1137,7 +1140,11 @@ struct Scorer {
                     if (v.freq > maxfreq) maxfreq = v.freq;
                 }
             }
-            if (!P.do_pileup && maxfreq <= P.freq) continue;
+            if (!P.do_pileup && maxfreq <= P.freq && !somatic) continue;
+            // only zero-count keys (and no insertion): the reference dereferences
+            // a null reference variant in collectReferenceVariants
+            // (src/ToVarsBuilder.cpp:737-743); such positions are left out
+            if (pv.all.empty()) continue;
             try {
                 collect_reference(position, tpc, pv);
             } catch (const RefFail &) {
@@ -1358,8 +1365,9 @@ string var_type(const Var &v) {
     return "Complex";
 }
 
-bool good_var(const Var &v, const Var *refv, const string &type, const rvo_params &P) {
+bool good_var(const Var &v, const Var *refv, const string &type_in, const rvo_params &P) {
     if (v.refallele.empty()) return false;
+    const string type = type_in.empty() ? var_type(v) : type_in;
     if (v.freq < P.freq || v.hicnt < P.minr || v.pmean < P.read_pos_filter || v.qual < P.goodq) return false;
     if (refv && refv->hicnt > P.minr && v.freq < 0.25) {
         double d = v.mq + v.refallele.size() + v.varallele.size();
@@ -1488,6 +1496,234 @@ long emit_simple(string &out, Scorer &sc, const char *sample, const char *gene, 
     }
     return n;
 }
+
+// ---------------------------------------------------------------------------
+// somatic mode: src/modes/somaticMode.cpp
+// ---------------------------------------------------------------------------
+struct Somatic {
+    const rvo_params &P;
+    const char *sample, *gene, *chr;
+    int rs, re;
+    string &o;
+    long n = 0;
+
+    // put_fisher_ext_and_odds (:130-149): two-sided p, then a float32 log ratio
+    // with +0.5 pseudocounts
+    void fisher_odds(int rf, int rr, int af, int ar) {
+        double l, r, t;
+        rv_oracle_fisher(rf, rr, af, ar, &l, &r, &t);
+        o += std::to_string(t) + "\t";
+        const float a = rf + 0.5, b = rr + 0.5, c = af + 0.5, d = ar + 0.5;
+        const float ad = a * d, bc = b * c;
+        const float ratio = std::log(ad / bc + bc / ad);
+        o += std::to_string(ratio) + "\t";
+    }
+
+    void stats(const Var *v, const Var *tv) {
+        if (!v) {
+            for (int i = 0; i < 18; i++) o += "0\t";
+            return;
+        }
+        auto put = [&](const string &x) { o += x; o += '\t'; };
+        put(std::to_string(v->tpc));
+        put(std::to_string(v->pc));
+        put(std::to_string(v->rfc));
+        put(std::to_string(v->rrc));
+        put(std::to_string(v->fwd));
+        put(std::to_string(v->rev));
+        // the normal column prints the tumor genotype (:218)
+        put(v->genotype.empty() ? "0" : tv->genotype);
+        put(fstr(v->freq));
+        put(v->sbf);
+        put(fstr(v->pmean));
+        put(v->pstd ? "1" : "0");
+        put(fstr(v->qual));
+        put(v->qstd ? "1" : "0");
+        put(fstr(v->mq));
+        put(fstr(v->qratio));
+        put(fstr(v->hifreq));
+        put(fstr(v->extrafreq));
+        put(fstr(v->nm));
+    }
+
+    // print_output_variant_simple (:151-309)
+    void print(const Var *beg, const Var *end, const Var *tv, const Var *nv, const string &label) {
+        o += string(sample) + "\t" + gene + "\t" + chr + "\t";
+        if (beg)
+            o += std::to_string(beg->startp) + "\t" + std::to_string(beg->endp) + "\t" + beg->refallele + "\t" +
+                 beg->varallele + "\t";
+        else
+            o += "0\t0\t0\t0\t";
+        stats(tv, tv);
+        if (P.fisher) {
+            if (tv) fisher_odds(tv->rfc, tv->rrc, tv->fwd, tv->rev);
+            else o += "0\t0\t";
+        }
+        stats(nv, tv);
+        if (P.fisher) {
+            if (nv) fisher_odds(nv->rfc, nv->rrc, nv->fwd, nv->rev);
+            else o += "0\t0\t";
+        }
+        if (end)
+            o += std::to_string(end->shift3) + "\t" + fstr(end->msi) + "\t" + std::to_string(end->msint) + "\t" +
+                 (end->leftseq.empty() ? string("0") : end->leftseq) + "\t" +
+                 (end->rightseq.empty() ? string("0") : end->rightseq) + "\t";
+        else
+            o += "\t\t\t\t\t";
+        o += string(chr) + ":" + std::to_string(rs) + "-" + std::to_string(re) + "\t";
+        o += label + "\t";
+        o += (beg ? beg->vartype : string()) + "\t";
+        o += (tv ? fstr(tv->duprate) : string("0")) + "\t0\t";
+        o += (nv ? fstr(nv->duprate) : string("0")) + "\t0\t";
+        if (P.fisher) {
+            int t_tot = tv ? tv->tpc : 0, t_var = tv ? tv->pc : 0;
+            int n_tot = nv ? nv->tpc : 0, n_var = nv ? nv->pc : 0;
+            int tref = t_tot - t_var, rref = n_tot - n_var;
+            if (tref < 0) tref = 0;
+            if (rref < 0) rref = 0;
+            fisher_odds(t_var, tref, n_var, rref);
+            double tvaf = tv ? tv->freq : 0, nvaf = nv ? nv->freq : 0;
+            o += std::to_string(std::log(std::max(tvaf, 0.0001) / std::max(nvaf, 0.0001))) + "\t";
+            o += std::to_string(std::log((static_cast<float>(t_var) + 0.5) / (static_cast<float>(n_var) + 0.5))) +
+                 "\t";
+        }
+        o += "\n";
+        n++;
+    }
+
+    static Var *find(PosVars &pv, const string &desc) {
+        for (int vi : pv.vars)
+            if (pv.all[vi].desc == desc) return &pv.all[vi];
+        return nullptr;
+    }
+    static Var *refv(PosVars &pv) { return pv.ref_idx >= 0 ? &pv.all[pv.ref_idx] : nullptr; }
+
+    // Variant::isNoise (include/Variant.h:75-94): zeroes the counts of a noise variant
+    bool is_noise(Var &v) {
+        const double q = v.qual;
+        if (((q < 4.5 || (q < 12 && !v.qstd)) && v.pc <= 3) || (q < P.goodq && v.freq < 2 * P.lofreq && v.pc <= 1)) {
+            v.tpc -= v.pc;
+            v.pc = 0;
+            v.fwd = v.rev = 0;
+            v.freq = 0;
+            v.hifreq = 0;
+            return true;
+        }
+        return false;
+    }
+
+    // determinateType (:608-633)
+    string determinate(PosVars &v2, Var &std_v, Var &cmp) {
+        string type;
+        if (good_var(cmp, refv(v2), std_v.vartype, P)) {
+            if (std_v.freq > 1 - P.lofreq && cmp.freq < 0.8 && cmp.freq > 0.2) type = "LikelyLOH";
+            else if (cmp.freq < P.lofreq || cmp.pc <= 1) type = "LikelySomatic";
+            else type = "Germline";
+        } else {
+            if (cmp.freq < P.lofreq || cmp.pc <= 1) type = "LikelySomatic";
+            else type = "AFDiff";
+        }
+        if (is_noise(cmp) && std_v.vartype == "SNV") type = "StrongSomatic";
+        return type;
+    }
+
+    // callingForOneSample (:360-380), tumor only
+    void one_sample(PosVars &v1, const string &label) {
+        for (int vi : v1.vars) {
+            Var &v = v1.all[vi];
+            v.vartype = var_type(v);
+            if (!good_var(v, refv(v1), v.vartype, P)) continue;
+            if (v.vartype == "Complex") adj_complex(v);
+            print(&v, &v, &v, nullptr, label);
+        }
+    }
+
+    // printVariationsFromFirstSample (:405-530)
+    void first_sample(PosVars &v1, PosVars &v2) {
+        size_t k = 0;
+        while (k < v1.vars.size() && good_var(v1.all[v1.vars[k]], refv(v1), v1.all[v1.vars[k]].vartype, P)) {
+            Var &vref = v1.all[v1.vars[k]];
+            vref.vartype = var_type(vref);
+            if (vref.vartype == "Complex") adj_complex(vref);
+            Var *v2nt = find(v2, vref.desc);
+            if (v2nt) {
+                string type = determinate(v2, vref, *v2nt);
+                print(&vref, v2nt, &vref, v2nt, type);
+            } else {
+                // sample 1 only; combineAnalysis (:639-735) needs a '<' in the
+                // description, which no key of this pipeline has
+                Var shown;
+                const Var *vfp;
+                if (!v2.vars.empty()) {
+                    const Var &v2r = v2.all[v2.vars[0]];
+                    shown.tpc = v2r.tpc;
+                    shown.rfc = v2r.rfc;
+                    shown.rrc = v2r.rrc;
+                    vfp = &shown;
+                } else {
+                    vfp = refv(v2);
+                }
+                print(&vref, &vref, &vref, vfp, "StrongSomatic");
+            }
+            k++;
+        }
+        if (k > 0 || v2.vars.empty()) return;
+        for (int vi : v2.vars) {
+            Var &v2var = v2.all[vi];
+            v2var.vartype = var_type(v2var);
+            if (!good_var(v2var, refv(v2), v2var.vartype, P)) continue;
+            Var *v1nt = find(v1, v2var.desc);
+            if (v1nt) {
+                string type = v1nt->freq < P.lofreq ? "LikelyLOH" : "Germline";
+                if (v2var.vartype == "Complex") adj_complex(*v1nt);
+                v1nt->vartype = var_type(*v1nt);
+                print(v1nt, &v2var, v1nt, &v2var, type);
+            } else {
+                const Var *v1var = v1.vars.empty() ? nullptr : &v1.all[v1.vars[0]];
+                const Var *v1ref = refv(v1);
+                Var shown;
+                shown.tpc = v1var ? v1var->tpc : 0;
+                shown.rfc = v1ref ? v1ref->fwd : 0;
+                shown.rrc = v1ref ? v1ref->rev : 0;
+                shown.genotype = v1var ? v1var->genotype : (v1ref ? v1ref->desc + "/" + v1ref->desc : "N/N");
+                if (v2var.vartype == "Complex") adj_complex(v2var);
+                print(&v2var, &v2var, &shown, &v2var, "StrongLOH");
+            }
+        }
+    }
+
+    // printVariationsFromSecondSample (:537-600)
+    void second_sample(PosVars &v1, PosVars &v2) {
+        for (int vi : v2.vars) {
+            Var &v2var = v2.all[vi];
+            v2var.vartype = var_type(v2var);
+            if (!good_var(v2var, refv(v2), v2var.vartype, P)) continue;
+            Var *v1nt = find(v1, v2var.desc);
+            if (v1nt) v1nt->pc = 0;
+            const Var *vfp = refv(v1);
+            if (v2var.vartype == "Complex") adj_complex(v2var);
+            print(&v2var, &v2var, vfp, &v2var, "StrongLOH");
+        }
+    }
+
+    // SomaticMode::output (:311-353): positions of the first BAM only
+    void run(Scorer &t, Scorer &nrm) {
+        for (auto &pe : t.aligned) {
+            int position = pe.first;
+            if (position < rs || position > re) continue;
+            PosVars &v1 = pe.second;
+            auto it = nrm.aligned.find(position);
+            if (it == nrm.aligned.end()) {
+                if (!v1.vars.empty()) one_sample(v1, "SampleSpecific");
+                continue;
+            }
+            PosVars &v2 = it->second;
+            if (v1.vars.empty() && v2.vars.empty()) continue;
+            if (!v1.vars.empty()) first_sample(v1, v2);
+            else second_sample(v1, v2);
+        }
+    }
+};
 
 // ---------------------------------------------------------------------------
 // record iteration: sam_itr_querys + RecordPreprocessor::next_record
@@ -1717,6 +1953,66 @@ long rvo_run_regions(const rvo_reads *reads, const char *ref, int contig_len, co
         sc.run();
         cnt[i] = emit_simple(per[i], sc, sample, chr, chr, *p);
     }
+    string o;
+    long n = 0;
+    for (int i = 0; i < n_regions; i++) { o += per[i]; n += cnt[i]; }
+    *out = (char *)malloc(o.size() + 1);
+    memcpy(*out, o.data(), o.size());
+    (*out)[o.size()] = 0;
+    *out_len = o.size();
+    return n;
+}
+
+// SomaticMode::process / one_region_run_somt (src/modes/somaticMode.cpp:83-127):
+// the tumor (first BAM) and the normal run the same per-region pipeline on a
+// shared reference window, then the two variant sets are classified.
+static long somatic_region(const rvo_reads *tumor, const rvo_reads *normal, const char *ref, int contig_len,
+                           const char *chr, int start, int end, const char *sample, const rvo_params &P,
+                           const char *stages, string &o) {
+    Maps MT, MN;
+    Ref R;
+    setup_ref(R, ref, contig_len, start, end, P);
+    run_pileup(tumor, P, start, end, contig_len, MT, R);
+    adjust_mnp(MT, R);
+    Scorer st(P, MT, R, contig_len, start, end, true);
+    st.run();
+    run_pileup(normal, P, start, end, contig_len, MN, R);
+    adjust_mnp(MN, R);
+    Scorer sn(P, MN, R, contig_len, start, end, true);
+    sn.run();
+    if (strchr(stages, 'V')) {
+        string a, b;
+        dump_variants(a, st);
+        dump_variants(b, sn);
+        for (size_t i = 0; i < a.size(); i++) o += (i == 0 || a[i - 1] == '\n') && a[i] == 'V' ? "VT" : string(1, a[i]);
+        for (size_t i = 0; i < b.size(); i++) o += (i == 0 || b[i - 1] == '\n') && b[i] == 'V' ? "VN" : string(1, b[i]);
+    }
+    if (!strchr(stages, 'O')) return 0;
+    Somatic so{P, sample, chr, chr, start, end, o};
+    so.run(st, sn);
+    return so.n;
+}
+
+int rvo_run_somatic(const rvo_reads *tumor, const rvo_reads *normal, const char *ref, int contig_len, const char *chr,
+                    int start, int end, const char *sample, const rvo_params *p, const char *stages, char **out,
+                    size_t *out_len) {
+    string o;
+    somatic_region(tumor, normal, ref, contig_len, chr, start, end, sample, *p, stages, o);
+    *out = (char *)malloc(o.size() + 1);
+    memcpy(*out, o.data(), o.size());
+    (*out)[o.size()] = 0;
+    *out_len = o.size();
+    return 0;
+}
+
+long rvo_run_somatic_regions(const rvo_reads *tumor, const rvo_reads *normal, const char *ref, int contig_len,
+                             const char *chr, const int32_t *starts, const int32_t *ends, int n_regions,
+                             const char *sample, const rvo_params *p, int threads, char **out, size_t *out_len) {
+    vector<string> per(n_regions);
+    vector<long> cnt(n_regions, 0);
+#pragma omp parallel for schedule(dynamic) num_threads(threads > 0 ? threads : 1)
+    for (int i = 0; i < n_regions; i++)
+        cnt[i] = somatic_region(tumor, normal, ref, contig_len, chr, starts[i], ends[i], sample, *p, "O", per[i]);
     string o;
     long n = 0;
     for (int i = 0; i < n_regions; i++) { o += per[i]; n += cnt[i]; }

@@ -82,6 +82,20 @@ long rvo_run_regions(const rvo_reads *reads, const char *ref, int contig_len, co
                      const char *sample, const rvo_params *p, int threads,
                      char **out, size_t *out_len);
 
+/* Somatic mode (a tumor/normal pair, `-b 'T.bam|N.bam'`): both samples run
+ * the per-region pipeline on the same reference window; the tumor's
+ * positions are classified against the normal's variants and written as
+ * 63-column records (64 with the trailing tab).  Stage V dumps the per-site
+ * variants of both samples (VT / VN lines). */
+int rvo_run_somatic(const rvo_reads *tumor, const rvo_reads *normal, const char *ref, int contig_len,
+                    const char *chr, int start, int end, const char *sample,
+                    const rvo_params *p, const char *stages, char **out, size_t *out_len);
+
+long rvo_run_somatic_regions(const rvo_reads *tumor, const rvo_reads *normal, const char *ref,
+                             int contig_len, const char *chr, const int32_t *starts,
+                             const int32_t *ends, int n_regions, const char *sample,
+                             const rvo_params *p, int threads, char **out, size_t *out_len);
+
 void rvo_free(char *p);
 
 double rvo_fisher(int n11, int n12, int n21, int n22, double *left, double *right, double *two);

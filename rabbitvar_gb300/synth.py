@@ -37,6 +37,7 @@ class Variant:
     vaf: float
     strand_bias: float = 0.0   # fraction of carrying reads forced onto one strand (artifacts)
     strand: int = 0            # strand the artifact prefers (0 fwd, 1 rev)
+    vq: int | None = None      # base quality forced on the changed bases of carrying reads (SNV/MNV)
 
 
 @dataclasses.dataclass
@@ -81,6 +82,30 @@ class ReadSet:
         if s.shape[0] % 2:
             s = np.concatenate([s, np.zeros(1, np.uint8)])
         return ((s[0::2] << 4) | s[1::2]).astype(np.uint8)
+
+
+def subset(rs: ReadSet, keep: np.ndarray) -> ReadSet:
+    """The reads of `rs` where `keep` is true, in the same order and layout."""
+    idx = np.nonzero(keep)[0]
+    n = idx.shape[0]
+    n_cigar = rs.n_cigar[idx]
+    cig_off = np.zeros(n, dtype=np.uint32)
+    if n:
+        cig_off[1:] = np.cumsum(n_cigar[:-1].astype(np.uint32))
+    cigar = np.concatenate([rs.cigar[int(rs.cig_off[i]):int(rs.cig_off[i]) + int(rs.n_cigar[i])] for i in idx]
+                           ) if n else np.zeros(0, np.uint32)
+    stride = int(rs.base_off[1] - rs.base_off[0]) if rs.n > 1 else 160
+    base_off = np.arange(n, dtype=np.uint64) * stride
+    seq4 = np.zeros(n * stride, dtype=np.uint8)
+    qv = np.zeros(n * stride, dtype=np.uint8)
+    for j, i in enumerate(idx.tolist()):
+        a = int(rs.base_off[i])
+        seq4[j * stride:(j + 1) * stride] = rs.seq4[a:a + stride]
+        qv[j * stride:(j + 1) * stride] = rs.qual[a:a + stride]
+    return ReadSet(contig=rs.contig, contig_len=rs.contig_len, pos=rs.pos[idx], flag=rs.flag[idx],
+                   mapq=rs.mapq[idx], mpos=rs.mpos[idx], isize=rs.isize[idx], nm=rs.nm[idx],
+                   n_cigar=n_cigar, cig_off=cig_off, cigar=cigar.astype(np.uint32), l_qseq=rs.l_qseq[idx],
+                   base_off=base_off, seq4=seq4, qual=qv, name_id=rs.name_id[idx])
 
 
 def make_genome(length: int, rng: np.random.Generator, gc: float = 0.41,
@@ -218,6 +243,8 @@ def simulate(genome: np.ndarray, variants: list[Variant], depth: float,
                 col = v.pos + k - start[carry]
                 ok = (col >= 0) & (col < L)
                 seq[carry[ok], col[ok]] = "ACGT".index(ch)
+                if v.vq is not None:
+                    qual[carry[ok], col[ok]] = v.vq
         else:
             # indel carriers need at least 3 aligned bases on each side
             off = v.pos - start[carry]
@@ -495,6 +522,40 @@ def somatic_pair(seed: int = 0x5EED0001, length: int = 1_000_000, tumor_depth: f
     tumor = simulate(g, germ + som + art, tumor_depth, rng, name_base=0)
     normal = simulate(g, germ, normal_depth, rng, name_base=10_000_000)
     return g, (germ, som, art), tumor, normal
+
+
+def somatic_mix(seed: int = 0x5EED0051, length: int = 30_000, tumor_depth: float = 80.0,
+                normal_depth: float = 40.0, gap: tuple[int, int] | None = (12_000, 12_400),
+                tail_margin: int = 0):
+    """Small tumor/normal pair that reaches every somatic label: shared
+    germline variants, tumor-only somatic SNV/MNV/indels, heterozygous normal
+    variants lost (VAF 0.02) or made homozygous (VAF 1.0) in the tumor,
+    strand-biased artifacts in both samples, shared SNVs with low-quality
+    normal reads, and a window `gap` (0-based,
+    half-open) where the normal has no reads."""
+    rng = np.random.default_rng(seed)
+    g = make_genome(length, rng)
+    germ = plant_variants(g, rng, 2e-3, 4e-4, lambda r: 0.5 if r.random() < 0.7 else 1.0)
+    som = plant_variants(g, rng, 1e-3, 3e-4, lambda r: r.uniform(0.01, 0.5), mnv_frac=0.3, avoid=germ)
+    loh = plant_variants(g, rng, 1e-3, 2e-4, lambda r: 0.5, mnv_frac=0.2, avoid=germ + som)
+    art = plant_variants(g, rng, 6e-4, 0.0, lambda r: r.uniform(0.05, 0.3), avoid=germ + som + loh)
+    for v in art:
+        v.strand_bias = 0.95
+        v.strand = int(rng.integers(0, 2))
+    # shared SNVs whose normal reads carry low base quality (called in the
+    # tumor, present but failing the quality filter in the normal)
+    lowq = plant_variants(g, rng, 4e-4, 0.0, lambda r: 0.35, avoid=germ + som + loh + art)
+    lowq_n = [dataclasses.replace(v, vaf=0.3, vq=12) for v in lowq]
+    loh_t = [dataclasses.replace(v, vaf=0.02 if i % 2 == 0 else 1.0) for i, v in enumerate(loh)]
+    art_t, art_n = art[0::2], art[1::2]
+    tumor = simulate(g, germ + som + loh_t + art_t + lowq, tumor_depth, rng, name_base=0, softclip_frac=0.04,
+                     tail_margin=tail_margin)
+    normal = simulate(g, germ + loh + art_n + lowq_n, normal_depth, rng, name_base=10_000_000,
+                      softclip_frac=0.04, tail_margin=tail_margin)
+    if gap is not None:
+        end = normal.pos + 150
+        normal = subset(normal, (end <= gap[0]) | (normal.pos >= gap[1]))
+    return g, (germ, som, loh, art, lowq), tumor, normal
 
 
 def dense_multi(seed: int = 0x5EED00D0, length: int = 60_000, depth: float = 60.0):

@@ -7,7 +7,8 @@ the reference's per-region dump (rvref_dump: maps after CigarParser and
 VariationRealigner, variants after ToVarsBuilder) and its emitted records
 (the RabbitVar binary) -> gzipped text files next to this script, plus a
 fingerprint of the generated reads so a change of the generator is reported
-as such rather than as a parity failure.
+as such rather than as a parity failure.  The somatic cases (a tumor/normal
+pair run in the reference's somatic mode) keep the emitted records only.
 
     python tests/golden/make_golden.py
 """
@@ -58,6 +59,20 @@ def case_unique_fisher():
 CASES = {"germline_dense": case_germline_dense, "contig_end": case_contig_end, "unique_fisher": case_unique_fisher}
 
 
+# somatic mode (`-b 'T.bam|N.bam' -N 'T|N'`): records only
+def case_somatic_mix():
+    g, _, t, n = synth.somatic_mix(0x5EED0051)
+    return g, t, n, (1, g.shape[0]), ["-k", "0", "--fisher"]
+
+
+def case_somatic_sub():
+    g, _, t, n = synth.somatic_mix(0x5EED0052)
+    return g, t, n, (8_001, 20_000), ["-k", "0"]
+
+
+SOMATIC = {"somatic_mix": case_somatic_mix, "somatic_sub": case_somatic_sub}
+
+
 def readset_fingerprint(rs) -> str:
     h = hashlib.sha256()
     for a in (rs.pos, rs.flag, rs.mapq, rs.mpos, rs.nm, rs.n_cigar, rs.cigar, rs.l_qseq, rs.seq4, rs.qual):
@@ -81,13 +96,28 @@ def main():
             dump_flags = [f for f in flags if f != "--fisher"]
             dump = O.reference_dump(fa, bam, region, dump_flags, stages="PRV")
             recs = O.reference_records(fa, bam, region, os.path.join(td, "out.txt"), flags)
-        with gzip.open(os.path.join(HERE, f"{name}.dump.txt.gz"), "wt") as f:
-            f.write(dump)
+        # mtime 0: the same dump gives the same bytes
+        with gzip.GzipFile(os.path.join(HERE, f"{name}.dump.txt.gz"), "wb", mtime=0) as f:
+            f.write(dump.encode())
         with open(os.path.join(HERE, f"{name}.records.txt"), "w") as f:
             f.write("\n".join(sorted(recs)) + "\n")
         meta[name] = {"region": [a, b], "flags": flags, "reads": rs.n, "fingerprint": readset_fingerprint(rs),
                       "records": len(recs)}
         print(name, rs.n, "reads", len(recs), "records")
+    for name, fn in SOMATIC.items():
+        g, t, n, (a, b), flags = fn()
+        with tempfile.TemporaryDirectory() as td:
+            tb, nb, fa = (os.path.join(td, x) for x in ("T.bam", "N.bam", "ref.fa"))
+            synth.write_bam(tb, t)
+            synth.write_bam(nb, n)
+            synth.write_fasta(fa, t.contig, g)
+            recs = O.reference_records(fa, f"{tb}|{nb}", f"{t.contig}:{a}-{b}", os.path.join(td, "out.txt"), flags,
+                                       sample="T|N")
+        with open(os.path.join(HERE, f"{name}.records.txt"), "w") as f:
+            f.write("\n".join(sorted(recs)) + "\n")
+        meta[name] = {"somatic": True, "region": [a, b], "flags": flags, "reads": [t.n, n.n],
+                      "fingerprint": [readset_fingerprint(t), readset_fingerprint(n)], "records": len(recs)}
+        print(name, t.n, n.n, "reads", len(recs), "records")
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump(meta, f, indent=1)
 

@@ -17,6 +17,8 @@ from cmp import diff_dump, diff_records
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLD = os.path.join(HERE, "golden")
 META = json.load(open(os.path.join(GOLD, "golden.json")))
+SINGLE = sorted(k for k, v in META.items() if not v.get("somatic"))
+SOMATIC = sorted(k for k, v in META.items() if v.get("somatic"))
 
 P_TAGS = ["P_ML", "PN", "PI", "PC", "PS5", "PS3", "PCI", "PCD", "PMN"]
 R_TAGS = ["RN", "RI", "RC"]
@@ -32,13 +34,18 @@ def _params(flags):
     return O.default_params(**kw)
 
 
-@pytest.mark.parametrize("name", sorted(META))
-def test_oracle_matches_reference_golden(name):
-    import oracle as O
+def _make_golden():
     import importlib.util
     spec = importlib.util.spec_from_file_location("make_golden", os.path.join(GOLD, "make_golden.py"))
     mg = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(mg)
+    return mg
+
+
+@pytest.mark.parametrize("name", SINGLE)
+def test_oracle_matches_reference_golden(name):
+    import oracle as O
+    mg = _make_golden()
     g, rs, (a, b), flags = mg.CASES[name]()
     assert mg.readset_fingerprint(rs) == META[name]["fingerprint"], "synthetic generator drifted: rerun make_golden.py"
     gold = gzip.open(os.path.join(GOLD, f"{name}.dump.txt.gz"), "rt").read()
@@ -70,3 +77,23 @@ def test_oracle_matches_reference_binary_config0(tmp_path):
     assert diff_dump(ref, ora, ["V"], skip=(), rel=1e-12, key_cols=3) == []
     recs = O.reference_records(fa, bam, "ctg:1-100000", str(tmp_path / "o.txt"), ["-k", "0"])
     assert diff_records(recs, [l for l in ora.splitlines() if l.startswith("S\t")], rel=0) == []
+
+
+@pytest.mark.parametrize("name", SOMATIC)
+def test_oracle_somatic_matches_reference_golden(name):
+    """Somatic mode: every one of the 63-column records (labels StrongSomatic,
+    LikelySomatic, Germline, AFDiff, LikelyLOH, StrongLOH, SampleSpecific),
+    byte for byte."""
+    import oracle as O
+    mg = _make_golden()
+    g, t, n, (a, b), flags = mg.SOMATIC[name]()
+    assert [mg.readset_fingerprint(t), mg.readset_fingerprint(n)] == META[name]["fingerprint"], \
+        "synthetic generator drifted: rerun make_golden.py"
+    recs = open(os.path.join(GOLD, f"{name}.records.txt")).read().splitlines()
+    mine = O.run_somatic(t, n, g, a, b, "O", "T", _params(flags)).splitlines()
+    assert len(recs) == META[name]["records"] > 50
+    assert sorted(mine) == sorted(recs)
+    if name == "somatic_mix":
+        labels = {r.split("\t")[53] for r in recs}
+        assert labels >= {"StrongSomatic", "LikelySomatic", "Germline", "AFDiff", "LikelyLOH", "StrongLOH",
+                          "SampleSpecific"}
