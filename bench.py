@@ -4,10 +4,12 @@ Workload (the somatic-pair shape the reference's metric is quoted on): a
 seeded synthetic 1 Mb contig, tumor 200x + normal 100x 2x150 bp pairs
 (~2.0 M reads), germline SNVs 1e-3/bp and indels 1e-4/bp in both samples,
 somatic SNV/MNV 2e-5/bp (VAF U(0.01, 0.5)) and strand-biased artifacts
-5e-6/bp in the tumor, called over 100 BED tiles of 10 kb with --fisher and
--k 0, every sample through the full per-region path (record filters, CIGAR
-walk, allele maps, MNP realignment, site statistics, hard filter, Fisher
-test, record text).  One step = both samples, all regions.
+5e-6/bp in the tumor, called in somatic mode (the reference's
+`-b 'T.bam|N.bam' -N 'T|N' --fisher`) over 100 BED tiles of 10 kb with -k 0:
+both samples through the full per-region path (record filters, CIGAR walk,
+allele maps, MNP realignment, site statistics), then the tumor/normal
+classification, the hard filter, three Fisher tests per record and the
+63-column record text.  One step = both samples, all regions.
 
     value : reads/s with the read batches already resident in HBM
     e2e   : reads/s through the C ABI from pinned host batches, including
@@ -129,20 +131,24 @@ def barrier_max(dist, x: float) -> float:
     return float(t.item())
 
 
-def cpu_baseline_run(g, samples, regions, threads: int, n_regions: int):
-    """The oracle's CPU restatement of the path (OpenMP over regions) on a
-    bounded sample of the workload's regions; returns reads/s."""
+WORKLOAD = ("somatic mode (-b 'T|N' -N 'T|N' --fisher -f 0.01 -k 0): synthetic 1 Mb contig, "
+            "tumor 200x + normal 100x 2x150, 100 x 10 kb BED tiles")
+METRIC = "reads/s pileup+var scoring (somatic pair 1 Mb, T200x+N100x)"
+CPU_TILES = 40   # CPU sample: 40 of the 100 tiles (~0.8 M reads, ~10 s on one core)
+
+
+def cpu_baseline_run(g, tumor, normal, regions, threads: int, n_regions: int):
+    """The oracle's CPU restatement of the path in somatic mode (OpenMP over
+    regions, as the reference's BED mode) on a bounded sample of the
+    workload's regions; returns reads/s."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
-    import numpy as np
     p = O.default_params(local_realign=0, fisher=1)
     sub = regions[:n_regions]
     lo, hi = sub[0][0], sub[-1][1]
-    reads = 0
+    reads = sum(int(((rs.pos >= lo - 1) & (rs.pos < hi)).sum()) for rs in (tumor, normal))
     t0 = time.perf_counter()
-    for rs in samples:
-        O.run_regions(rs, g, sub, params=p, threads=threads)
-        reads += int(((rs.pos >= lo - 1) & (rs.pos < hi)).sum())
+    O.run_somatic_regions(tumor, normal, g, sub, "T", p, threads=threads)
     dt = time.perf_counter() - t0
     return reads / dt, dt, reads
 
@@ -152,21 +158,20 @@ def run_reference(args, rank):
         return
     g, tumor, normal, regions = make_workload()
     threads = os.cpu_count() or 1
-    n_reg = 8
+    n_reg = CPU_TILES
     vals = []
     for _ in range(args.warmup):
-        cpu_baseline_run(g, [tumor, normal], regions, threads, n_reg)
+        cpu_baseline_run(g, tumor, normal, regions, threads, n_reg)
     for _ in range(args.steps):
-        v, dt, nr = cpu_baseline_run(g, [tumor, normal], regions, threads, n_reg)
+        v, dt, nr = cpu_baseline_run(g, tumor, normal, regions, threads, n_reg)
         vals.append(v)
     v = statistics.median(vals)
-    out = {"impl": "reference", "metric": "reads/s pileup+var scoring (somatic pair 1 Mb, T200x+N100x)",
+    out = {"impl": "reference", "metric": METRIC,
            "value": v, "unit": "reads/s", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
            "higher_is_better": True, "data": "synthetic",
-           "config": {"workload": "somatic pair 1 Mb contig, tumor 200x + normal 100x 2x150, 100 x 10 kb BED tiles, --fisher, -k 0",
-                      "sample": f"first {n_reg} of 100 tiles, both samples"},
+           "config": {"workload": WORKLOAD, "sample": f"first {n_reg} of 100 tiles, both samples"},
            "cpu_baseline": {"value": v, "unit": "reads/s", "cores": threads, "kind": "port",
-                            "sample": f"first {n_reg} of 100 10-kb tiles, tumor+normal, per step"},
+                            "sample": f"first {n_reg} of 100 10-kb tiles, tumor+normal ({nr} reads), per step"},
            "e2e": {"value": v, "unit": "reads/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
 
@@ -189,63 +194,49 @@ def main():
     g, tumor, normal, regions = make_workload(seed_offset=rank)
     samples = [("T", tumor), ("N", normal)]
     params = api.default_params(local_realign=0, fisher=1)
-    ctxs, batches = [], []
-    for name, rs in samples:
-        c = api.Context(params, device=local)
-        c.upload_reference(rs.contig, synth.genome_str(g).encode())
-        ctxs.append(c)
-        batches.append(api.Batch.from_readset(rs, pinned=True))
+    pair = api.SomaticPair(params, device=local)
+    pair.upload_reference(tumor.contig, synth.genome_str(g).encode())
+    ctxs = [pair.tumor, pair.normal]
+    batches = [api.Batch.from_readset(rs, pinned=True) for _, rs in samples]
     n_reads = sum(rs.n for _, rs in samples)
     alg_read_bytes = sum(read_alg_bytes(rs) for _, rs in samples)
 
     host_ms = {"pileup": 0.0, "realign": 0.0, "score": 0.0, "format": 0.0}
 
+    def kernels_of():
+        return sum(c.timings()["kernels"] for c in ctxs)
+
     def device_step(collect=None):
-        kernels = 0
-        recs = 0
-        for c in ctxs:
-            t0 = time.perf_counter()
-            c.pileup()
-            t1 = time.perf_counter()
-            c.realign()
-            t2 = time.perf_counter()
-            c.score()
-            t3 = time.perf_counter()
-            text, n = c.format_records("S", "ctg")
-            t4 = time.perf_counter()
-            if collect is not None:
-                host_ms["pileup"] += (t1 - t0) * 1e3
-                host_ms["realign"] += (t2 - t1) * 1e3
-                host_ms["score"] += (t3 - t2) * 1e3
-                host_ms["format"] += (t4 - t3) * 1e3
-            recs += n
-            kernels += c.timings()["kernels"]
-            if collect is not None:
-                collect.append(c.stage_times())
-        return kernels, recs
+        t0 = time.perf_counter()
+        pair.pileup()
+        t1 = time.perf_counter()
+        pair.realign()
+        t2 = time.perf_counter()
+        pair.score()
+        t3 = time.perf_counter()
+        text, n = pair.format_records("T", "ctg")
+        t4 = time.perf_counter()
+        if collect is not None:
+            host_ms["pileup"] += (t1 - t0) * 1e3
+            host_ms["realign"] += (t2 - t1) * 1e3
+            host_ms["score"] += (t3 - t2) * 1e3
+            host_ms["format"] += (t4 - t3) * 1e3
+            collect.extend(c.stage_times() for c in ctxs)
+        return kernels_of(), n
 
     io = {"h2d": 0, "d2h": 0}
 
     def e2e_step():
-        kernels = 0
-        recs = 0
         # both uploads are queued first (each context has its own stream), so
         # the second sample's copy overlaps the first sample's kernels
-        for c, b in zip(ctxs, batches):
-            c.submit(b, regions)
-        h2d = d2h = 0
-        for c in ctxs:
-            c.pileup()
-            c.realign()
-            c.score()
-            text, n = c.format_records("S", "ctg")
-            recs += n
-            kernels += c.timings()["kernels"]
-            a, b_ = c.io_bytes()
-            h2d += a
-            d2h += b_
-        io["h2d"], io["d2h"] = h2d, d2h
-        return kernels, recs
+        pair.submit(batches[0], batches[1], regions)
+        pair.pileup()
+        pair.realign()
+        pair.score()
+        text, n = pair.format_records("T", "ctg")
+        io["h2d"] = sum(c.io_bytes()[0] for c in ctxs)
+        io["d2h"] = sum(c.io_bytes()[1] for c in ctxs)
+        return kernels_of(), n
 
     # e2e: pinned host batch -> device every step
     for _ in range(args.warmup):
@@ -279,12 +270,11 @@ def main():
     peak, peak_kind = measured_peak_hbm()
     h2d = sum(b.nbytes for b in batches)
     out = {
-        "metric": "reads/s pileup+var scoring (somatic pair 1 Mb, T200x+N100x)",
+        "metric": METRIC,
         "value": value, "unit": "reads/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "int32/fp64", "data": "synthetic (seeded)",
-        "config": {"workload": "somatic pair 1 Mb contig, tumor 200x + normal 100x 2x150, 100 x 10 kb BED tiles, --fisher, -k 0",
-                   "reads_per_step": n_reads * world, "l2": "inputs (~0.5 GB) larger than L2, no flush",
+        "config": {"workload": WORKLOAD, "reads_per_step": n_reads * world, "l2": "inputs (~0.5 GB) larger than L2, no flush",
                    "records_per_step": recs},
         "e2e": {"value": e2e, "unit": "reads/s", "h2d_bytes_per_step": io["h2d"],
                 "d2h_bytes_per_step": io["d2h"]},
@@ -297,13 +287,12 @@ def main():
         "clocks": clk,
     }
     if rank == 0 and not args.no_cpu_baseline:
-        v, dt, nr = cpu_baseline_run(g, [tumor, normal], regions, 1, 2)
+        v, dt, nr = cpu_baseline_run(g, tumor, normal, regions, 1, CPU_TILES)
         out["cpu_baseline"] = {"value": v, "unit": "reads/s", "cores": 1, "kind": "port",
-                               "sample": f"first 2 of 100 10-kb tiles, tumor+normal ({nr} reads, {dt:.1f} s)"}
+                               "sample": f"first {CPU_TILES} of 100 10-kb tiles, tumor+normal ({nr} reads, {dt:.1f} s)"}
     if rank == 0:
         print(json.dumps(out))
-    for c in ctxs:
-        c.close()
+    pair.close()
     if dist is not None:
         dist.destroy_process_group()
 

@@ -64,6 +64,8 @@ typedef struct {
     int32_t fisher;        /* --fisher */
     int32_t move_indels_3; /* -3 */
     int32_t svminlen;      /* 1000 */
+    int32_t somatic;       /* a second BAM is configured (conf->bam.hasBam2()): the context is
+                              one sample of a tumor/normal pair, see rv_score_pair */
 } rv_params;
 
 /* Reads of one contig in coordinate (file) order, structure of arrays.
@@ -161,6 +163,30 @@ rv_status rv_call_regions(rv_ctx *ctx, const rv_read_batch *reads, const rv_regi
  * include/scopedata/VariationData.h:14-56): writes a text dump of region
  * `region` in the same line format as the oracle dump (P* lines).  Valid
  * until the next call on ctx. */
+/* Somatic mode: the tumor/normal pair of `-b 'T.bam|N.bam'` (SomaticMode::process,
+ * src/modes/somaticMode.cpp:83-127 one_region_run_somt, :311-353 output).  `tumor`
+ * and `normal` are two contexts created with params.somatic = 1, given the same
+ * contig (rv_upload_reference) and the same region list (rv_submit_batch with each
+ * sample's reads), and each taken through rv_pileup and rv_realign.
+ *
+ * rv_score_pair replaces the two ToVarsBuilder::process calls: it scores both
+ * samples and then, in each sample, the positions where only the other one has a
+ * candidate, so every position that can produce a record is complete in both.
+ * rv_format_somatic replaces SomaticMode::output + print_output_variant_simple
+ * (:151-309): the labels StrongSomatic, LikelySomatic, Germline, AFDiff,
+ * LikelyLOH, StrongLOH, SampleSpecific and the 63-column records (64 fields with
+ * the trailing tab; 55 without --fisher), the three Fisher tests of each record
+ * run on the device.  As in the reference, positions come from the tumor only.
+ * The text belongs to `tumor` until its next call.  rv_call_somatic runs the
+ * whole sequence. */
+rv_status rv_score_pair(rv_ctx *tumor, rv_ctx *normal);
+rv_status rv_format_somatic(rv_ctx *tumor, rv_ctx *normal, const char *sample, const char *gene,
+                            const char **text, size_t *text_len, int64_t *n_records);
+rv_status rv_call_somatic(rv_ctx *tumor, rv_ctx *normal, const rv_read_batch *tumor_reads,
+                          const rv_read_batch *normal_reads, const rv_region *regions, int n_regions,
+                          const char *sample, const char *gene, const char **text, size_t *text_len,
+                          int64_t *n_records);
+
 rv_status rv_export_maps(rv_ctx *ctx, int region, const char *stages, const char **text, size_t *text_len);
 
 /* Timing of the last rv_pileup/rv_score call (device time, ms, CUDA events on

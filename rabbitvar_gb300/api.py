@@ -35,7 +35,7 @@ class Params(C.Structure):
                 ("extend_nt", C.c_int32), ("trim_bases_after", C.c_int32), ("minmatch", C.c_int32),
                 ("dedup", C.c_int32), ("unique_fwd", C.c_int32), ("unique_first", C.c_int32),
                 ("do_pileup", C.c_int32), ("fisher", C.c_int32), ("move_indels_3", C.c_int32),
-                ("svminlen", C.c_int32)]
+                ("svminlen", C.c_int32), ("somatic", C.c_int32)]
 
 
 class ReadBatch(C.Structure):
@@ -60,7 +60,7 @@ class SiteRecord(C.Structure):
 
 EXPORTS = ["rv_default_params", "rv_create", "rv_destroy", "rv_last_error", "rv_upload_reference",
            "rv_submit_batch", "rv_pileup", "rv_realign", "rv_score", "rv_format_records", "rv_fetch_records",
-           "rv_call_regions", "rv_export_maps", "rv_last_timings", "rv_stage_times", "rv_io_bytes", "rv_fisher_batch", "rv_bam_read",
+           "rv_call_regions", "rv_score_pair", "rv_format_somatic", "rv_call_somatic", "rv_export_maps", "rv_last_timings", "rv_stage_times", "rv_io_bytes", "rv_fisher_batch", "rv_bam_read",
            "rv_bam_contigs", "rv_bam_batch", "rv_bam_free", "rv_fasta_read", "rv_free", "rv_alloc_pinned",
            "rv_free_pinned"]
 
@@ -90,6 +90,9 @@ def lib():
     L.rv_format_records.argtypes = [vp, C.c_char_p, C.c_char_p, C.POINTER(C.c_char_p), C.POINTER(sz),
                                     C.POINTER(i64)]
     L.rv_fetch_records.argtypes = [vp, C.POINTER(SiteRecord), sz, C.POINTER(sz)]
+    L.rv_score_pair.argtypes = [vp, vp]
+    L.rv_format_somatic.argtypes = [vp, vp, C.c_char_p, C.c_char_p, C.POINTER(C.c_char_p), C.POINTER(sz),
+                                    C.POINTER(i64)]
     L.rv_export_maps.argtypes = [vp, C.c_int, C.c_char_p, C.POINTER(vp), C.POINTER(sz)]
     L.rv_last_timings.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double),
                                   C.POINTER(i64)]
@@ -269,6 +272,57 @@ class Context:
         r = np.zeros(t.shape[0])
         self._check(self.L.rv_fisher_batch(self.h, t.ctypes.data, t.shape[0], p.ctypes.data, r.ctypes.data))
         return p, r
+
+
+class SomaticPair:
+    """Somatic mode (a tumor/normal pair, the reference's `-b 'T.bam|N.bam'`):
+    one context per sample, created with somatic = 1, sharing the contig and
+    the region list."""
+
+    def __init__(self, params: Params | None = None, device: int = 0, budget: int = 0):
+        p = params or default_params(local_realign=0)
+        p.somatic = 1
+        self.tumor = Context(p, device, budget)
+        self.normal = Context(p, device, budget)
+
+    def close(self):
+        self.tumor.close()
+        self.normal.close()
+
+    def upload_reference(self, chr_name: str, bases: bytes):
+        self.tumor.upload_reference(chr_name, bases)
+        self.normal.upload_reference(chr_name, bases)
+
+    def submit(self, tumor: Batch, normal: Batch, regions):
+        self.tumor.submit(tumor, regions)
+        self.normal.submit(normal, regions)
+
+    def pileup(self):
+        self.tumor.pileup()
+        self.normal.pileup()
+
+    def realign(self):
+        self.tumor.realign()
+        self.normal.realign()
+
+    def score(self):
+        self.tumor._check(self.tumor.L.rv_score_pair(self.tumor.h, self.normal.h))
+
+    def format_records(self, sample: str = "T", gene: str | None = None) -> tuple[str, int]:
+        t = C.c_char_p()
+        n = C.c_size_t()
+        nrec = C.c_int64()
+        self.tumor._check(self.tumor.L.rv_format_somatic(self.tumor.h, self.normal.h, sample.encode(),
+                                                         gene.encode() if gene else None, C.byref(t), C.byref(n),
+                                                         C.byref(nrec)))
+        return C.string_at(t, n.value).decode(), nrec.value
+
+    def call(self, tumor: Batch, normal: Batch, regions, sample: str = "T", gene: str | None = None) -> str:
+        self.submit(tumor, normal, regions)
+        self.pileup()
+        self.realign()
+        self.score()
+        return self.format_records(sample, gene)[0]
 
 
 def read_bam(path: str, threads: int = 0):

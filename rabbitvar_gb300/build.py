@@ -17,7 +17,7 @@ OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "librvgpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU = ["rv_pileup.cu", "rv_score.cu", "rv_util.cu", "rv_noalloc.cu"]
-CPP = ["rv_capi.cpp", "rv_host.cpp", "rv_bam.cpp"]
+CPP = ["rv_capi.cpp", "rv_host.cpp", "rv_records.cpp", "rv_somatic.cpp", "rv_bam.cpp"]
 
 
 def _nvcc() -> str:
@@ -59,7 +59,7 @@ def build(verbose: bool = False) -> str:
         obj = os.path.join(OUT_DIR, f + ".o")
         objs.append(obj)
         if _needs(obj, [src] + headers):
-            jobs.append(["g++", "-O2", "-g", "-std=c++17", "-fPIC", "-I" + os.path.join(cuda, "include")] + inc +
+            jobs.append(["g++", "-O2", "-g", "-std=c++17", "-fPIC", "-ffp-contract=off", "-I" + os.path.join(cuda, "include")] + inc +
                         ["-c", src, "-o", obj])
 
     def run(cmd):

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <iterator>
 #include <cstdlib>
 #include <climits>
 #include <cstdio>
@@ -95,6 +96,104 @@ DevState rv_ctx::state() const {
     return s;
 }
 
+namespace rv {
+
+rv_status device_fisher(rv_ctx *ctx, const int32_t *tables, int64_t n, double *p2) {
+    if (n <= 0) return RV_OK;
+    RV_CUDA(cudaSetDevice(ctx->device));
+    // tables (16 B each) followed by the p-values and ratios (16 B per table)
+    size_t need = (size_t)n * 2;
+    if (need > ctx->cap_ftab || !ctx->d_ftab) {
+        if (ctx->d_ftab) cudaFree(ctx->d_ftab);
+        ctx->d_ftab = nullptr;
+        size_t cap = std::max<size_t>(need + need / 4, 4096);
+        RV_CUDA(cudaMalloc((void **)&ctx->d_ftab, cap * 16));
+        ctx->cap_ftab = cap;
+    }
+    double *dp = (double *)(ctx->d_ftab + 4 * n);
+    RV_CUDA(cudaMemcpyAsync(ctx->d_ftab, tables, (size_t)n * 16, cudaMemcpyHostToDevice, ctx->stream));
+    launch_fisher(ctx->d_ftab, n, dp, dp + n, ctx->stream);
+    RV_CUDA(cudaGetLastError());
+    RV_CUDA(cudaMemcpyAsync(p2, dp, (size_t)n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    RV_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->io_h2d += n * 16;
+    ctx->io_d2h += n * 8;
+    ctx->kernels += 1;
+    return RV_OK;
+}
+
+}  // namespace rv
+
+namespace {
+
+// Scores the listed (region, position) pairs of `ctx` without screens and
+// appends their CandVars to the host copy.
+rv_status score_list(rv_ctx *ctx, const std::vector<int2> &list) {
+    if (list.empty()) return RV_OK;
+    if (list.size() > ctx->cap_list || !ctx->d_list) {
+        if (ctx->d_list) cudaFree(ctx->d_list);
+        ctx->d_list = nullptr;
+        size_t cap = std::max<size_t>(list.size() + list.size() / 4, 4096);
+        RV_CUDA(cudaMalloc((void **)&ctx->d_list, cap * sizeof(int2)));
+        ctx->cap_list = cap;
+    }
+    cudaStream_t s = ctx->stream;
+    RV_CUDA(cudaMemcpyAsync(ctx->d_list, list.data(), list.size() * sizeof(int2), cudaMemcpyHostToDevice, s));
+    DevState st = ctx->state();
+    launch_score_list(st, ctx->dp, ctx->d_list, (int)list.size(), s);
+    RV_CUDA(cudaGetLastError());
+    unsigned int hdr[8];
+    RV_CUDA(cudaMemcpyAsync(hdr, ctx->d_counters, sizeof hdr, cudaMemcpyDeviceToHost, s));
+    RV_CUDA(cudaStreamSynchronize(s));
+    unsigned int n0 = (unsigned int)ctx->h_cand.size(), n = hdr[CNT_CAND];
+    if (n > ctx->cand_cap || (hdr[CNT_ERR] & ERR_HASH_FULL)) {
+        ctx->err = "candidate buffer overflow";
+        return RV_ERR_CAPACITY;
+    }
+    if (hdr[CNT_ERR] & (ERR_UNSUPPORTED | ERR_CELL_RANGE)) {
+        char buf[96];
+        snprintf(buf, sizeof buf, "score device error bits 0x%x", hdr[CNT_ERR]);
+        ctx->err = buf;
+        return RV_ERR_UNSUPPORTED;
+    }
+    ctx->h_cand.resize(n);
+    if (n > n0)
+        RV_CUDA(cudaMemcpy(ctx->h_cand.data() + n0, ctx->d_cand + n0, (size_t)(n - n0) * sizeof(CandVar),
+                           cudaMemcpyDeviceToHost));
+    ctx->io_h2d += (int64_t)(list.size() * sizeof(int2));
+    ctx->io_d2h += (int64_t)sizeof hdr + (int64_t)(n - n0) * (int64_t)sizeof(CandVar);
+    ctx->kernels += 1;
+    return RV_OK;
+}
+
+std::vector<int2> positions_of(const rv_ctx *ctx) {
+    std::vector<int2> v;
+    v.reserve(ctx->h_cand.size());
+    for (const CandVar &c : ctx->h_cand) v.push_back(make_int2(c.region, c.pos));
+    auto lt = [](const int2 &a, const int2 &b) { return a.x != b.x ? a.x < b.x : a.y < b.y; };
+    std::sort(v.begin(), v.end(), lt);
+    v.erase(std::unique(v.begin(), v.end(), [](const int2 &a, const int2 &b) { return a.x == b.x && a.y == b.y; }),
+            v.end());
+    return v;
+}
+
+// the positions of `a` missing from `b` (both sorted and unique)
+std::vector<int2> missing(const std::vector<int2> &a, const std::vector<int2> &b) {
+    std::vector<int2> out;
+    auto lt = [](const int2 &x, const int2 &y) { return x.x != y.x ? x.x < y.x : x.y < y.y; };
+    std::set_difference(a.begin(), a.end(), b.begin(), b.end(), std::back_inserter(out), lt);
+    return out;
+}
+
+bool same_regions(const rv_ctx *a, const rv_ctx *b) {
+    if (a->regions.size() != b->regions.size()) return false;
+    for (size_t i = 0; i < a->regions.size(); i++)
+        if (a->regions[i].start != b->regions[i].start || a->regions[i].end != b->regions[i].end) return false;
+    return a->chr == b->chr && a->ref_len == b->ref_len;
+}
+
+}  // namespace
+
 extern "C" {
 
 void rv_default_params(rv_params *p) {
@@ -161,6 +260,7 @@ rv_status rv_create(rv_ctx **out, const rv_params *p, int device, size_t hbm_bud
     d.fisher = p->fisher;
     d.move_indels_3 = p->move_indels_3;
     d.svminlen = p->svminlen;
+    d.somatic = p->somatic;
     *out = ctx;
     if (p->local_realign) {
         ctx->err = "local realignment (-k 1) is not supported by this build; use local_realign = 0";
@@ -180,7 +280,8 @@ void rv_destroy(rv_ctx *ctx) {
                     ctx->d_mapq, ctx->d_cigoff, ctx->d_cigar, ctx->d_boff, ctx->d_seq, ctx->d_qual,
                     ctx->d_regions, ctx->d_tiles, ctx->d_score_base, ctx->d_cellmem, ctx->d_head, ctx->d_slots,
                     ctx->d_arena, ctx->d_deferred, ctx->d_cand, ctx->d_counters, ctx->d_tmp_idx,
-                    ctx->d_tmp_slots, ctx->d_tmp_cells, ctx->d_tmp_views, ctx->d_tmp_n};
+                    ctx->d_tmp_slots, ctx->d_tmp_cells, ctx->d_tmp_views, ctx->d_tmp_n, ctx->d_list,
+                    ctx->d_ftab};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (int i = 0; i < 12; i++)
@@ -429,7 +530,7 @@ rv_status rv_pileup(rv_ctx *ctx, void *stream) {
     launch_collisions(st, s);
     RV_CUDA(cudaGetLastError());
     RV_CUDA(cudaEventRecord(ctx->ev[1], s));
-    ctx->kernels = 7;
+    ctx->kernels = 8;  // init_slots, region_spans, edge_detect, pileup_tiles, serial, resolve, link, collisions
     unsigned int err = 0;
     RV_CUDA(cudaMemcpyAsync(&err, ctx->d_counters + CNT_ERR, 4, cudaMemcpyDeviceToHost, s));
     RV_CUDA(cudaStreamSynchronize(s));
@@ -546,6 +647,57 @@ rv_status rv_call_regions(rv_ctx *ctx, const rv_read_batch *reads, const rv_regi
     if ((s = rv_realign(ctx, nullptr))) return s;
     if ((s = rv_score(ctx, nullptr))) return s;
     return rv_format_records(ctx, sample, gene, text, text_len, n_records);
+}
+
+rv_status rv_score_pair(rv_ctx *tumor, rv_ctx *normal) {
+    if (!tumor || !normal || tumor == normal) return RV_ERR_ARG;
+    if (!tumor->params.somatic || !normal->params.somatic) {
+        tumor->err = "rv_score_pair needs two contexts created with somatic = 1";
+        return RV_ERR_ARG;
+    }
+    if (!same_regions(tumor, normal) || tumor->device != normal->device) {
+        tumor->err = "rv_score_pair: the two samples must share the contig, the region list and the device";
+        return RV_ERR_ARG;
+    }
+    rv_status s;
+    if ((s = rv_score(tumor, nullptr))) return s;
+    if ((s = rv_score(normal, nullptr))) { tumor->err = normal->err; return s; }
+    // every position where one sample has a candidate is needed in both
+    std::vector<int2> pt = positions_of(tumor), pn = positions_of(normal);
+    if ((s = score_list(tumor, missing(pn, pt)))) return s;
+    if ((s = score_list(normal, missing(pt, pn)))) { tumor->err = normal->err; return s; }
+    return RV_OK;
+}
+
+rv_status rv_format_somatic(rv_ctx *tumor, rv_ctx *normal, const char *sample, const char *gene, const char **text,
+                            size_t *text_len, int64_t *n_records) {
+    if (!tumor || !normal) return RV_ERR_ARG;
+    if (tumor->stage < 4 || normal->stage < 4) {
+        tumor->err = "rv_format_somatic before rv_score_pair";
+        return RV_ERR_STATE;
+    }
+    rv_status st = host_format_somatic(tumor, normal, sample ? sample : "", gene ? gene : tumor->chr.c_str());
+    if (st) return st;
+    if (text) *text = tumor->text.c_str();
+    if (text_len) *text_len = tumor->text.size();
+    if (n_records) *n_records = tumor->n_records;
+    return RV_OK;
+}
+
+rv_status rv_call_somatic(rv_ctx *tumor, rv_ctx *normal, const rv_read_batch *tumor_reads,
+                          const rv_read_batch *normal_reads, const rv_region *regions, int n_regions,
+                          const char *sample, const char *gene, const char **text, size_t *text_len,
+                          int64_t *n_records) {
+    if (!tumor || !normal) return RV_ERR_ARG;
+    rv_status s;
+    if ((s = rv_submit_batch(tumor, tumor_reads, regions, n_regions, nullptr))) return s;
+    if ((s = rv_submit_batch(normal, normal_reads, regions, n_regions, nullptr))) { tumor->err = normal->err; return s; }
+    if ((s = rv_pileup(tumor, nullptr))) return s;
+    if ((s = rv_pileup(normal, nullptr))) { tumor->err = normal->err; return s; }
+    if ((s = rv_realign(tumor, nullptr))) return s;
+    if ((s = rv_realign(normal, nullptr))) { tumor->err = normal->err; return s; }
+    if ((s = rv_score_pair(tumor, normal))) return s;
+    return rv_format_somatic(tumor, normal, sample, gene, text, text_len, n_records);
 }
 
 rv_status rv_export_maps(rv_ctx *ctx, int region, const char *stages, const char **text, size_t *text_len) {

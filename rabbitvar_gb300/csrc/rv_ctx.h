@@ -24,6 +24,7 @@ void launch_collisions(const DevState &st, cudaStream_t s);
 void launch_ins_adjust(const DevState &st, cudaStream_t s);
 void launch_score(const DevState &st, const DevParams &P, cudaStream_t s);
 void launch_fisher(const int32_t *tab, int64_t n, double *p2, double *ratio, cudaStream_t s);
+void launch_score_list(const DevState &st, const DevParams &P, const int2 *list, int n, cudaStream_t s);
 void launch_compact_slots(const DevState &st, uint32_t *out, unsigned int *n_out, cudaStream_t s);
 void launch_gather_slots(const Slot *slots, const uint32_t *idx, int64_t n, Slot *out, cudaStream_t s);
 
@@ -128,6 +129,11 @@ struct rv_ctx {
     void *d_tmp_views = nullptr;
     size_t cap_tmp_views = 0;
     unsigned int *d_tmp_n = nullptr;
+    // somatic mode: positions to score without screens; Fisher tables and results
+    int2 *d_list = nullptr;
+    size_t cap_list = 0;
+    int32_t *d_ftab = nullptr;
+    size_t cap_ftab = 0;  // tables
 
     // host mirrors
     std::vector<rv::CandVar> h_cand;
@@ -152,3 +158,9 @@ struct rv_ctx {
 
     rv::DevState state() const;
 };
+
+namespace rv {
+// two-sided Fisher p-values of n (a, b, c, d) tables on the context's device
+rv_status device_fisher(rv_ctx *ctx, const int32_t *tables, int64_t n, double *p2);
+rv_status host_format_somatic(rv_ctx *tumor, rv_ctx *normal, const char *sample, const char *gene);
+}  // namespace rv

@@ -78,7 +78,7 @@ struct DevParams {
     double goodq, freq, qratio, mapq_filter, lofreq, bias;
     int32_t vext, mismatch, local_realign, minr, read_pos_filter, min_mapq, min_bias_reads, samfilter;
     int32_t trim_bases_after, minmatch, dedup, unique_fwd, unique_first, do_pileup, fisher, move_indels_3;
-    int32_t svminlen, pad;
+    int32_t svminlen, somatic;
 };
 
 // Cell arrays: one cell per (position, base A/C/G/T); index = 4 * cell + b.

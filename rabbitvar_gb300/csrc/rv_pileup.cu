@@ -437,7 +437,9 @@ __global__ void k_region_spans(DevState st) {
     for (int64_t r = R.r0 + threadIdx.x; r < R.r1; r += blockDim.x) {
         int a, b;
         read_span(st.batch, r, a, b);
-        mylo = min(mylo, a);
+        // a 5' clip of a read at the contig start reaches below position 1,
+        // where there is no reference base and so no cell is touched
+        mylo = min(mylo, max(a, 1));
         myhi = max(myhi, b);
     }
     atomicMin(&lo, mylo);

@@ -273,6 +273,221 @@ __device__ double fisher_two_sided(int n11, int n12, int n21, int n22) {
     return st > 1.0 ? 1.0 : st;
 }
 
+// Scores position p of region `lo`: ToVarsBuilder::process for one position
+// (src/ToVarsBuilder.cpp:97-205).  Positions that pass the screens (or every
+// position with variants when `forced`) write all their alleles as CandVars.
+__device__ void score_position(const DevState &st, const DevParams &P, int lo, int p, bool forced) {
+    const Region &R = st.regions[lo];
+    if (p < R.clo || p > R.chi) return;
+    int64_t c = cell_index(R, p);
+    char rb = ref_at(st, R, p);
+    int rbi = base_index(rb);
+    bool hasp = p >= R.ws && p <= R.we;
+    // quick screen for positions holding only A/C/G/T keys: skip when only
+    // the reference base was seen, or when no other base could pass the
+    // -f gate and the numeric part of isGoodVar
+    if (!forced && st.head[c] == kNone && !P.do_pileup) {
+        uint8_t kf0 = st.cells.kflags[c];
+        int ex = kf0 & 15 & ~(kf0 >> 4);
+        if (ex == 0) return;
+        uint32_t cov0 = st.cells.cov[c];
+        if (cov0 == 0) return;
+        if (hasp && rbi >= 0 && ex == (1 << rbi)) return;
+        const uint4 f4 = *reinterpret_cast<const uint4 *>(st.cells.fwd + 4 * c);
+        const uint4 r4 = *reinterpret_cast<const uint4 *>(st.cells.rev + 4 * c);
+        const uint4 h4 = *reinterpret_cast<const uint4 *>(st.cells.hi + 4 * c);
+        const uint32_t fa[4] = {f4.x, f4.y, f4.z, f4.w}, ra[4] = {r4.x, r4.y, r4.z, r4.w};
+        const uint32_t ha[4] = {h4.x, h4.y, h4.z, h4.w};
+        // the -f gate needs some non-reference allele with freq > -f; an
+        // emitted record needs one with freq >= -f and hicnt >= -r (they
+        // may be different alleles, e.g. at freq exactly -f)
+        bool gate = false, pass = false;
+        for (int b = 0; b < 4; b++) {
+            if (!((ex >> b) & 1) || (hasp && b == rbi)) continue;
+            int cnt = (int)(fa[b] + ra[b]);
+            if (cnt <= 0) continue;
+            double fr = cnt / (double)cov0;
+            if (fr > P.freq) gate = true;
+            if (fr >= P.freq && (int)ha[b] >= P.minr) pass = true;
+        }
+        // somatic mode keeps every covered position (no -f gate), so only
+        // the emission condition screens
+        if (!pass || !(gate || P.somatic)) return;
+    }
+    PosKeys k;
+    if (!visited(st, R, p, k)) return;
+    // isTheSameVariationOnRef (src/ToVarsBuilder.cpp:213-233)
+    if (!forced && !P.do_pileup && !P.somatic && k.n_nonins == 1 && k.n_ins == 0 && hasp && rbi >= 0 &&
+        k.single_mask == (1 << rbi))
+        return;
+    int tpc = (int)st.cells.cov[c];
+    // calcHicov
+    int hicov = 0;
+    V vs[kMaxVars];
+    int nv = 0;
+    for (int b = 0; b < 4; b++) {
+        if (!((k.single_mask >> b) & 1)) continue;
+        int64_t g = 4 * c + b;
+        hicov += (int)st.cells.hi[g];
+    }
+    for (uint32_t s = st.head[c]; s != kNone; s = st.hash.slots[s].next) {
+        const Slot &sl = st.hash.slots[s];
+        if (!(sl.flags & SF_ERASED) && (sl.kind == KIND_NONINS || sl.kind == KIND_INS)) hicov += sl.hi;
+    }
+    // createVariant (non-insertion keys with a count)
+    for (int b = 0; b < 4; b++) {
+        if (!((k.single_mask >> b) & 1)) continue;
+        int64_t g = 4 * c + b;
+        V v;
+        v.kind = 0;
+        v.key = b;
+        v.fwd = (int)st.cells.fwd[g];
+        v.rev = (int)st.cells.rev[g];
+        v.cnt = v.fwd + v.rev;
+        if (v.cnt == 0) continue;
+        v.hi = (int)st.cells.hi[g];
+        v.lo = v.cnt - v.hi;
+        v.extracnt = 0;
+        v.tp = (double)(int)st.cells.tp[g];
+        v.q = (double)(int)st.cells.q[g];
+        v.mq = (double)(int)st.cells.mq[g];
+        v.nm = (double)st.cells.nm[g];
+        uint32_t f = st.cells.first[g];
+        v.pstd = (f & FCS_PDIFF) != 0;
+        v.qstd = (f & FCS_QDIFF) != 0;
+        finish_var(v, tpc, hicov, P);
+        if (nv < kMaxVars) vs[nv++] = v;
+    }
+    for (uint32_t s = st.head[c]; s != kNone; s = st.hash.slots[s].next) {
+        const Slot &sl = st.hash.slots[s];
+        if (sl.kind != KIND_NONINS || (sl.flags & SF_ERASED)) continue;
+        V v;
+        load_slot(sl, (int)s, v);
+        if (v.cnt == 0) continue;
+        int ttcov = tpc;
+        if (v.cnt > tpc && v.extracnt > 0 && v.cnt - tpc < v.extracnt) ttcov = v.cnt;
+        finish_var(v, ttcov, hicov, P);
+        if (nv < kMaxVars) vs[nv++] = v; else atomicOr(st.err, ERR_UNSUPPORTED);
+    }
+    // createInsertion
+    if (k.n_ins > 0) {
+        sort_ins(st, k);
+        int hic = hicov;
+        for (int i = 0; i < k.n_ins; i++) {
+            const Slot &sl = st.hash.slots[k.ins[i]];
+            V v;
+            load_slot(sl, (int)k.ins[i], v);
+            int ttcov = tpc;
+            if (v.cnt > tpc && v.extracnt != 0 && v.cnt - tpc < v.extracnt) ttcov = v.cnt;
+            if (ttcov < v.cnt) {
+                ttcov = v.cnt;
+                int p1 = p + 1;
+                if (p1 <= R.chi) {
+                    uint32_t cov1 = st.cells.cov[cell_index(R, p1)];
+                    if (cov1 != 0 && p1 >= R.ws && p1 <= R.we && ttcov < (int)cov1 - v.cnt) ttcov = (int)cov1;
+                }
+                tpc = ttcov;
+            }
+            if (hic < v.hi) hic = v.hi;
+            finish_var(v, ttcov, hic, P);
+            if (nv < kMaxVars) vs[nv++] = v; else atomicOr(st.err, ERR_UNSUPPORTED);
+        }
+    }
+    // sort by CMP_VARI (insertion sort; few alleles per position)
+    for (int i = 1; i < nv; i++) {
+        V x = vs[i];
+        int j = i - 1;
+        while (j >= 0 && cmp_vari(st, x, vs[j])) { vs[j + 1] = vs[j]; j--; }
+        vs[j + 1] = x;
+    }
+    // collectVarsAtPosition: the reference allele is the single key equal to the reference base
+    int ref_i = -1;
+    double maxfreq = 0;
+    int n_var = 0;
+    for (int i = 0; i < nv; i++) {
+        if (hasp && vs[i].kind == 0 && vs[i].key == rbi) ref_i = i;
+        else { n_var++; if (vs[i].freq > maxfreq) maxfreq = vs[i].freq; }
+    }
+    // only zero-count keys: the reference dereferences a null reference
+    // variant there (src/ToVarsBuilder.cpp:737-743); nothing is emitted
+    if (nv == 0) return;
+    if (!forced) {
+        if (!P.do_pileup && !P.somatic && maxfreq <= P.freq) return;
+        if (n_var == 0) return;
+    }
+    // numeric pre-screen of isGoodVar: a necessary condition for emission
+    bool any = false;
+    for (int i = 0; i < nv; i++) {
+        if (i == ref_i) continue;
+        const V &v = vs[i];
+        if (v.freq >= P.freq && v.hi >= P.minr && v.pmean >= P.read_pos_filter && v.qual >= P.goodq &&
+            v.qratio >= P.qratio)
+            any = true;
+    }
+    if (!any && !P.do_pileup && !forced) return;
+    // reference strand counts (collectReferenceVariants :730-760)
+    int rfc = 0, rrc = 0;
+    if (ref_i >= 0) { rfc = vs[ref_i].fwd; rrc = vs[ref_i].rev; }
+    if (tpc > (int)st.cells.cov[c] && p + 1 <= R.chi) {
+        int p1 = p + 1;
+        int64_t c1 = cell_index(R, p1);
+        char rb1 = ref_at(st, R, p1);
+        int b1 = base_index(rb1);
+        uint8_t kf1 = st.cells.kflags[c1];
+        if (p1 >= R.ws && p1 <= R.we && b1 >= 0 && ((kf1 >> b1) & 1) && !((kf1 >> (4 + b1)) & 1)) {
+            rfc = (int)st.cells.fwd[4 * c1 + b1];
+            rrc = (int)st.cells.rev[4 * c1 + b1];
+        }
+    }
+    unsigned int base = atomicAdd(st.n_cand, (unsigned int)nv);
+    if (base + nv > st.cand_cap) { atomicOr(st.err, ERR_HASH_FULL); return; }
+    int rank = 0;
+    for (int i = 0; i < nv; i++) {
+        const V &v = vs[i];
+        CandVar &o = st.cand[base + i];
+        o.region = lo;
+        o.pos = p;
+        o.kind = (i == ref_i) ? 0 : 1;
+        o.rank = (i == ref_i) ? -1 : rank++;
+        if (v.kind == 0) { o.key_off = v.key; o.key_len = -1; }
+        else { const Slot &sl = st.hash.slots[v.key]; o.key_off = (int)sl.koff; o.key_len = sl.klen; }
+        // raw counts (the record writers clamp negatives where the reference does)
+        int fwd = v.fwd < 0 ? 0 : v.fwd, rev = v.rev < 0 ? 0 : v.rev;
+        int rf = rfc < 0 ? 0 : rfc, rr = rrc < 0 ? 0 : rrc;
+        o.pc = v.cnt;
+        o.fwd = v.fwd;
+        o.rev = v.rev;
+        o.hicnt = v.hi;
+        o.hicov = v.hicov;
+        o.tpc = tpc;
+        o.rfc = rfc;
+        o.rrc = rrc;
+        o.bias = v.bias;
+        o.ref_bias = ref_i >= 0 ? vs[ref_i].bias : -1;
+        o.pstd = v.pstd;
+        o.qstd = v.qstd;
+        o.pass = (v.freq >= P.freq && v.hi >= P.minr && v.pmean >= P.read_pos_filter && v.qual >= P.goodq &&
+                  v.qratio >= P.qratio) ? 1 : 0;
+        o.nvars = nv;
+        o.freq = v.freq;
+        o.pmean = v.pmean;
+        o.qual = v.qual;
+        o.mq = v.mqv;
+        o.qratio = v.qratio;
+        o.hifreq = v.hifreq;
+        o.extrafreq = v.extrafreq;
+        o.nm = v.nmv;
+        if (P.fisher && !P.somatic && o.kind == 1 && o.pass) {
+            o.fisher_p = fisher_two_sided(rf, rr, fwd, rev);
+            double ad = (double)(rf * rev), bc = (double)(rr * fwd);
+            o.fisher_ratio = (bc != 0 && ad != 0) ? (ad > bc ? ad / bc : bc / ad) : 0.0;
+        } else {
+            o.fisher_p = 0;
+            o.fisher_ratio = 0;
+        }
+    }
+}
+
 // Each block scores a contiguous chunk of positions; the region of the
 // chunk start is found once and threads advance from it.
 constexpr int kScoreChunk = 2048;
@@ -291,211 +506,23 @@ __global__ void k_score(DevState st, DevParams P) {
         }
         __syncthreads();
         const int lo0 = s_lo;
-    for (int64_t t = c0 + threadIdx.x; t < c0 + kScoreChunk && t < st.n_score; t += blockDim.x) {
-        int lo = lo0;
-        while (lo + 1 < st.n_regions && st.score_base[lo + 1] <= t) lo++;
-        const Region &R = st.regions[lo];
-        int p = R.start + (int)(t - st.score_base[lo]);
-        if (p < R.clo || p > R.chi) continue;
-        int64_t c = cell_index(R, p);
-        char rb = ref_at(st, R, p);
-        int rbi = base_index(rb);
-        bool hasp = p >= R.ws && p <= R.we;
-        // quick screen for positions holding only A/C/G/T keys: skip when only
-        // the reference base was seen, or when no other base could pass the
-        // -f gate and the numeric part of isGoodVar
-        if (st.head[c] == kNone && !P.do_pileup) {
-            uint8_t kf0 = st.cells.kflags[c];
-            int ex = kf0 & 15 & ~(kf0 >> 4);
-            if (ex == 0) continue;
-            uint32_t cov0 = st.cells.cov[c];
-            if (cov0 == 0) continue;
-            if (hasp && rbi >= 0 && ex == (1 << rbi)) continue;
-            const uint4 f4 = *reinterpret_cast<const uint4 *>(st.cells.fwd + 4 * c);
-            const uint4 r4 = *reinterpret_cast<const uint4 *>(st.cells.rev + 4 * c);
-            const uint4 h4 = *reinterpret_cast<const uint4 *>(st.cells.hi + 4 * c);
-            const uint32_t fa[4] = {f4.x, f4.y, f4.z, f4.w}, ra[4] = {r4.x, r4.y, r4.z, r4.w};
-            const uint32_t ha[4] = {h4.x, h4.y, h4.z, h4.w};
-            // the -f gate needs some non-reference allele with freq > -f; an
-            // emitted record needs one with freq >= -f and hicnt >= -r (they
-            // may be different alleles, e.g. at freq exactly -f)
-            bool gate = false, pass = false;
-            for (int b = 0; b < 4; b++) {
-                if (!((ex >> b) & 1) || (hasp && b == rbi)) continue;
-                int cnt = (int)(fa[b] + ra[b]);
-                if (cnt <= 0) continue;
-                double fr = cnt / (double)cov0;
-                if (fr > P.freq) gate = true;
-                if (fr >= P.freq && (int)ha[b] >= P.minr) pass = true;
-            }
-            if (!(gate && pass)) continue;
-        }
-        PosKeys k;
-        if (!visited(st, R, p, k)) continue;
-        // isTheSameVariationOnRef (src/ToVarsBuilder.cpp:213-233)
-        if (!P.do_pileup && k.n_nonins == 1 && k.n_ins == 0 && hasp && rbi >= 0 && k.single_mask == (1 << rbi))
-            continue;
-        int tpc = (int)st.cells.cov[c];
-        // calcHicov
-        int hicov = 0;
-        V vs[kMaxVars];
-        int nv = 0;
-        for (int b = 0; b < 4; b++) {
-            if (!((k.single_mask >> b) & 1)) continue;
-            int64_t g = 4 * c + b;
-            hicov += (int)st.cells.hi[g];
-        }
-        for (uint32_t s = st.head[c]; s != kNone; s = st.hash.slots[s].next) {
-            const Slot &sl = st.hash.slots[s];
-            if (!(sl.flags & SF_ERASED) && (sl.kind == KIND_NONINS || sl.kind == KIND_INS)) hicov += sl.hi;
-        }
-        // createVariant (non-insertion keys with a count)
-        for (int b = 0; b < 4; b++) {
-            if (!((k.single_mask >> b) & 1)) continue;
-            int64_t g = 4 * c + b;
-            V v;
-            v.kind = 0;
-            v.key = b;
-            v.fwd = (int)st.cells.fwd[g];
-            v.rev = (int)st.cells.rev[g];
-            v.cnt = v.fwd + v.rev;
-            if (v.cnt == 0) continue;
-            v.hi = (int)st.cells.hi[g];
-            v.lo = v.cnt - v.hi;
-            v.extracnt = 0;
-            v.tp = (double)(int)st.cells.tp[g];
-            v.q = (double)(int)st.cells.q[g];
-            v.mq = (double)(int)st.cells.mq[g];
-            v.nm = (double)st.cells.nm[g];
-            uint32_t f = st.cells.first[g];
-            v.pstd = (f & FCS_PDIFF) != 0;
-            v.qstd = (f & FCS_QDIFF) != 0;
-            finish_var(v, tpc, hicov, P);
-            if (nv < kMaxVars) vs[nv++] = v;
-        }
-        for (uint32_t s = st.head[c]; s != kNone; s = st.hash.slots[s].next) {
-            const Slot &sl = st.hash.slots[s];
-            if (sl.kind != KIND_NONINS || (sl.flags & SF_ERASED)) continue;
-            V v;
-            load_slot(sl, (int)s, v);
-            if (v.cnt == 0) continue;
-            int ttcov = tpc;
-            if (v.cnt > tpc && v.extracnt > 0 && v.cnt - tpc < v.extracnt) ttcov = v.cnt;
-            finish_var(v, ttcov, hicov, P);
-            if (nv < kMaxVars) vs[nv++] = v; else atomicOr(st.err, ERR_UNSUPPORTED);
-        }
-        // createInsertion
-        if (k.n_ins > 0) {
-            sort_ins(st, k);
-            int hic = hicov;
-            for (int i = 0; i < k.n_ins; i++) {
-                const Slot &sl = st.hash.slots[k.ins[i]];
-                V v;
-                load_slot(sl, (int)k.ins[i], v);
-                int ttcov = tpc;
-                if (v.cnt > tpc && v.extracnt != 0 && v.cnt - tpc < v.extracnt) ttcov = v.cnt;
-                if (ttcov < v.cnt) {
-                    ttcov = v.cnt;
-                    int p1 = p + 1;
-                    if (p1 <= R.chi) {
-                        uint32_t cov1 = st.cells.cov[cell_index(R, p1)];
-                        if (cov1 != 0 && p1 >= R.ws && p1 <= R.we && ttcov < (int)cov1 - v.cnt) ttcov = (int)cov1;
-                    }
-                    tpc = ttcov;
-                }
-                if (hic < v.hi) hic = v.hi;
-                finish_var(v, ttcov, hic, P);
-                if (nv < kMaxVars) vs[nv++] = v; else atomicOr(st.err, ERR_UNSUPPORTED);
-            }
-        }
-        // sort by CMP_VARI (insertion sort; few alleles per position)
-        for (int i = 1; i < nv; i++) {
-            V x = vs[i];
-            int j = i - 1;
-            while (j >= 0 && cmp_vari(st, x, vs[j])) { vs[j + 1] = vs[j]; j--; }
-            vs[j + 1] = x;
-        }
-        // collectVarsAtPosition: the reference allele is the single key equal to the reference base
-        int ref_i = -1;
-        double maxfreq = 0;
-        int n_var = 0;
-        for (int i = 0; i < nv; i++) {
-            if (hasp && vs[i].kind == 0 && vs[i].key == rbi) ref_i = i;
-            else { n_var++; if (vs[i].freq > maxfreq) maxfreq = vs[i].freq; }
-        }
-        if (!P.do_pileup && maxfreq <= P.freq) continue;
-        if (n_var == 0) continue;
-        // numeric pre-screen of isGoodVar: a necessary condition for emission
-        bool any = false;
-        for (int i = 0; i < nv; i++) {
-            if (i == ref_i) continue;
-            const V &v = vs[i];
-            if (v.freq >= P.freq && v.hi >= P.minr && v.pmean >= P.read_pos_filter && v.qual >= P.goodq &&
-                v.qratio >= P.qratio)
-                any = true;
-        }
-        if (!any && !P.do_pileup) continue;
-        // reference strand counts (collectReferenceVariants :730-760)
-        int rfc = 0, rrc = 0;
-        if (ref_i >= 0) { rfc = vs[ref_i].fwd; rrc = vs[ref_i].rev; }
-        if (tpc > (int)st.cells.cov[c] && p + 1 <= R.chi) {
-            int p1 = p + 1;
-            int64_t c1 = cell_index(R, p1);
-            char rb1 = ref_at(st, R, p1);
-            int b1 = base_index(rb1);
-            uint8_t kf1 = st.cells.kflags[c1];
-            if (p1 >= R.ws && p1 <= R.we && b1 >= 0 && ((kf1 >> b1) & 1) && !((kf1 >> (4 + b1)) & 1)) {
-                rfc = (int)st.cells.fwd[4 * c1 + b1];
-                rrc = (int)st.cells.rev[4 * c1 + b1];
-            }
-        }
-        unsigned int base = atomicAdd(st.n_cand, (unsigned int)nv);
-        if (base + nv > st.cand_cap) { atomicOr(st.err, ERR_HASH_FULL); continue; }
-        int rank = 0;
-        for (int i = 0; i < nv; i++) {
-            const V &v = vs[i];
-            CandVar &o = st.cand[base + i];
-            o.region = lo;
-            o.pos = p;
-            o.kind = (i == ref_i) ? 0 : 1;
-            o.rank = (i == ref_i) ? -1 : rank++;
-            if (v.kind == 0) { o.key_off = v.key; o.key_len = -1; }
-            else { const Slot &sl = st.hash.slots[v.key]; o.key_off = (int)sl.koff; o.key_len = sl.klen; }
-            int fwd = v.fwd < 0 ? 0 : v.fwd, rev = v.rev < 0 ? 0 : v.rev;
-            int rf = rfc < 0 ? 0 : rfc, rr = rrc < 0 ? 0 : rrc;
-            o.pc = v.cnt;
-            o.fwd = fwd;
-            o.rev = rev;
-            o.hicnt = v.hi;
-            o.hicov = v.hicov;
-            o.tpc = tpc;
-            o.rfc = rf;
-            o.rrc = rr;
-            o.bias = v.bias;
-            o.ref_bias = ref_i >= 0 ? vs[ref_i].bias : -1;
-            o.pstd = v.pstd;
-            o.qstd = v.qstd;
-            o.pass = (v.freq >= P.freq && v.hi >= P.minr && v.pmean >= P.read_pos_filter && v.qual >= P.goodq &&
-                      v.qratio >= P.qratio) ? 1 : 0;
-            o.nvars = nv;
-            o.freq = v.freq;
-            o.pmean = v.pmean;
-            o.qual = v.qual;
-            o.mq = v.mqv;
-            o.qratio = v.qratio;
-            o.hifreq = v.hifreq;
-            o.extrafreq = v.extrafreq;
-            o.nm = v.nmv;
-            if (P.fisher && o.kind == 1 && o.pass) {
-                o.fisher_p = fisher_two_sided(rf, rr, fwd, rev);
-                double ad = (double)(rf * rev), bc = (double)(rr * fwd);
-                o.fisher_ratio = (bc != 0 && ad != 0) ? (ad > bc ? ad / bc : bc / ad) : 0.0;
-            } else {
-                o.fisher_p = 0;
-                o.fisher_ratio = 0;
-            }
+        for (int64_t t = c0 + threadIdx.x; t < c0 + kScoreChunk && t < st.n_score; t += blockDim.x) {
+            int lo = lo0;
+            while (lo + 1 < st.n_regions && st.score_base[lo + 1] <= t) lo++;
+            score_position(st, P, lo, st.regions[lo].start + (int)(t - st.score_base[lo]), false);
         }
     }
+}
+
+// Listed (region, position) pairs, scored without screens: in somatic mode
+// the positions where the other sample has a candidate.
+__global__ void k_score_list(DevState st, DevParams P, const int2 *list, int n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int2 e = list[i];
+        if (e.x < 0 || e.x >= st.n_regions) continue;
+        const Region &R = st.regions[e.x];
+        if (e.y < R.start || e.y > R.end) continue;
+        score_position(st, P, e.x, e.y, true);
     }
 }
 
@@ -519,6 +546,9 @@ void launch_score(const DevState &st, const DevParams &P, cudaStream_t s) {
         int64_t chunks = (st.n_score + kScoreChunk - 1) / kScoreChunk;
         k_score<<<(int)std::min<int64_t>(chunks, 4864), 256, 0, s>>>(st, P);
     }
+}
+void launch_score_list(const DevState &st, const DevParams &P, const int2 *list, int n, cudaStream_t s) {
+    if (n > 0) k_score_list<<<(n + 127) / 128 < 1216 ? (n + 127) / 128 : 1216, 128, 0, s>>>(st, P, list, n);
 }
 void launch_fisher(const int32_t *tab, int64_t n, double *p2, double *ratio, cudaStream_t s) {
     if (n > 0) k_fisher<<<(int)((n + 127) / 128 < 4096 ? (n + 127) / 128 : 4096), 128, 0, s>>>(tab, n, p2, ratio);

@@ -52,15 +52,18 @@ def diff_dump(a_text: str, b_text: str, tags, skip=STAT_SKIP, rel=1e-6, key_cols
     return problems
 
 
-def diff_records(ra: list[str], rb: list[str], rel=2e-6):
-    """Emitted record sets: same (start, ref, alt) keys, integer and string
-    columns equal, %f-formatted columns within rel (plus one unit in the
-    sixth decimal)."""
+def diff_records(ra: list[str], rb: list[str], rel=2e-6, somatic: bool = False):
+    """Emitted record sets: same (start, ref, alt) keys (plus the label column
+    for somatic records), integer and string columns equal, %f-formatted
+    columns within rel (plus one unit in the sixth decimal)."""
     def key(f):
-        return (f[2], int(f[3]), f[5], f[6])
+        k = (f[2], int(f[3]), f[5], f[6])
+        return k + (f[-11] if len(f) > 60 else f[-7],) if somatic else k
     A = {key(l.split("\t")): l.split("\t") for l in ra if l}
     B = {key(l.split("\t")): l.split("\t") for l in rb if l}
     problems = []
+    if somatic and (len(A) != len([l for l in ra if l]) or len(B) != len([l for l in rb if l])):
+        problems.append("duplicate record keys")
     if set(A) != set(B):
         problems.append(f"record keys differ: missing {sorted(set(A) - set(B))[:5]} extra {sorted(set(B) - set(A))[:5]}")
     for k in set(A) & set(B):
