@@ -187,6 +187,26 @@ rv_status rv_call_somatic(rv_ctx *tumor, rv_ctx *normal, const rv_read_batch *tu
                           const char *sample, const char *gene, const char **text, size_t *text_len,
                           int64_t *n_records);
 
+/* Candidate set of the learned filter (include/rvgpu_mlp.h); no counterpart in
+ * the reference.  rv_score_candidates replaces rv_score after rv_realign: every
+ * position with a non-reference allele seen at least `min_count` times keeps all
+ * its alleles (the -f gate and the isGoodVar pre-screen are not applied).
+ * rv_candidates then returns, for every candidate allele (reference alleles
+ * excluded) in one order, RV_FEATURES floats (features[n][RV_FEATURES], computed
+ * on the device from the allele's site statistics, its key and the reference
+ * around it) and an rv_candidate with its position, key and whether simple mode
+ * (rv_format_records, i.e. the hard filter) emits it.  With both pointers NULL
+ * only *n is set. */
+#define RV_FEATURES 40
+typedef struct {
+    int32_t region, position;  /* region index, 1-based position */
+    int32_t hard_pass;         /* 1: emitted by the hard filter */
+    int32_t key_len;           /* length of the allele key */
+    char key[48];              /* allele key, truncated to 47 bytes, NUL-terminated */
+} rv_candidate;
+rv_status rv_score_candidates(rv_ctx *ctx, int min_count);
+rv_status rv_candidates(rv_ctx *ctx, float *features, rv_candidate *cands, int64_t cap, int64_t *n);
+
 rv_status rv_export_maps(rv_ctx *ctx, int region, const char *stages, const char **text, size_t *text_len);
 
 /* Timing of the last rv_pileup/rv_score call (device time, ms, CUDA events on

@@ -49,6 +49,11 @@ class Region(C.Structure):
     _fields_ = [("start", C.c_int32), ("end", C.c_int32)]
 
 
+class Candidate(C.Structure):
+    _fields_ = [("region", C.c_int32), ("position", C.c_int32), ("hard_pass", C.c_int32), ("key_len", C.c_int32),
+                ("key", C.c_char * 48)]
+
+
 class SiteRecord(C.Structure):
     _fields_ = ([(n, C.c_int32) for n in ("region", "position", "start", "end", "total_cov", "var_cov", "ref_fwd",
                                           "ref_rev", "alt_fwd", "alt_rev")] +
@@ -60,9 +65,10 @@ class SiteRecord(C.Structure):
 
 EXPORTS = ["rv_default_params", "rv_create", "rv_destroy", "rv_last_error", "rv_upload_reference",
            "rv_submit_batch", "rv_pileup", "rv_realign", "rv_score", "rv_format_records", "rv_fetch_records",
-           "rv_call_regions", "rv_score_pair", "rv_format_somatic", "rv_call_somatic", "rv_export_maps", "rv_last_timings", "rv_stage_times", "rv_io_bytes", "rv_fisher_batch", "rv_bam_read",
+           "rv_call_regions", "rv_score_candidates", "rv_candidates", "rv_score_pair", "rv_format_somatic", "rv_call_somatic", "rv_export_maps", "rv_last_timings", "rv_stage_times", "rv_io_bytes", "rv_fisher_batch", "rv_bam_read",
            "rv_bam_contigs", "rv_bam_batch", "rv_bam_free", "rv_fasta_read", "rv_free", "rv_alloc_pinned",
-           "rv_free_pinned"]
+           "rv_free_pinned", "rv_mlp_create", "rv_mlp_destroy", "rv_mlp_last_error", "rv_mlp_set_params",
+           "rv_mlp_get_params", "rv_mlp_train", "rv_mlp_gradients", "rv_mlp_predict"]
 
 _lib = None
 
@@ -91,6 +97,8 @@ def lib():
                                     C.POINTER(i64)]
     L.rv_fetch_records.argtypes = [vp, C.POINTER(SiteRecord), sz, C.POINTER(sz)]
     L.rv_score_pair.argtypes = [vp, vp]
+    L.rv_score_candidates.argtypes = [vp, C.c_int]
+    L.rv_candidates.argtypes = [vp, vp, vp, i64, C.POINTER(i64)]
     L.rv_format_somatic.argtypes = [vp, vp, C.c_char_p, C.c_char_p, C.POINTER(C.c_char_p), C.POINTER(sz),
                                     C.POINTER(i64)]
     L.rv_export_maps.argtypes = [vp, C.c_int, C.c_char_p, C.POINTER(vp), C.POINTER(sz)]
@@ -265,6 +273,20 @@ class Context:
         ms = np.zeros(8)
         self._check(self.L.rv_stage_times(self.h, ms.ctypes.data, 8))
         return {k: float(ms[i]) for i, k in enumerate(self.STAGES)}
+
+    def score_candidates(self, min_count: int = 2):
+        self._check(self.L.rv_score_candidates(self.h, min_count))
+
+    def candidates(self):
+        """Features [n][40] (float32) and the candidate table of the last
+        scoring call: list of (region, position, key, hard_pass)."""
+        n = C.c_int64()
+        self._check(self.L.rv_candidates(self.h, None, None, 0, C.byref(n)))
+        feats = np.zeros((max(n.value, 1), 40), np.float32)
+        arr = (Candidate * max(n.value, 1))()
+        self._check(self.L.rv_candidates(self.h, feats.ctypes.data, arr, n.value, C.byref(n)))
+        table = [(c.region, c.position, c.key.decode(), c.hard_pass) for c in arr[:n.value]]
+        return feats[:n.value], table
 
     def fisher(self, tables: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
         t = np.ascontiguousarray(tables, dtype=np.int32).reshape(-1, 4)

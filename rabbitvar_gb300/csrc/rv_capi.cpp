@@ -15,7 +15,7 @@
 
 namespace rv {
 rv_status host_realign_mnp(rv_ctx *ctx);
-rv_status host_format_records(rv_ctx *ctx, const char *sample, const char *gene);
+rv_status host_format_records(rv_ctx *ctx, const char *sample, const char *gene, uint8_t *emitted = nullptr);
 rv_status host_export_maps(rv_ctx *ctx, int region, const char *stages);
 }  // namespace rv
 
@@ -93,6 +93,7 @@ DevState rv_ctx::state() const {
     s.cand = d_cand;
     s.n_cand = d_counters + CNT_CAND;
     s.cand_cap = cand_cap;
+    s.logfact = d_logfact;
     return s;
 }
 
@@ -112,7 +113,7 @@ rv_status device_fisher(rv_ctx *ctx, const int32_t *tables, int64_t n, double *p
     }
     double *dp = (double *)(ctx->d_ftab + 4 * n);
     RV_CUDA(cudaMemcpyAsync(ctx->d_ftab, tables, (size_t)n * 16, cudaMemcpyHostToDevice, ctx->stream));
-    launch_fisher(ctx->d_ftab, n, dp, dp + n, ctx->stream);
+    launch_fisher(ctx->d_ftab, n, dp, dp + n, ctx->stream, ctx->d_logfact);
     RV_CUDA(cudaGetLastError());
     RV_CUDA(cudaMemcpyAsync(p2, dp, (size_t)n * 8, cudaMemcpyDeviceToHost, ctx->stream));
     RV_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -230,6 +231,11 @@ rv_status rv_create(rv_ctx **out, const rv_params *p, int device, size_t hbm_bud
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
     for (int i = 0; e == cudaSuccess && i < 12; i++) e = cudaEventCreate(&ctx->ev[i]);
     if (e == cudaSuccess) e = cudaMalloc((void **)&ctx->d_counters, 64 * sizeof(unsigned int));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&ctx->d_logfact, (size_t)kLogFact * sizeof(double));
+    if (e == cudaSuccess) {
+        launch_fill_logfact(ctx->d_logfact, ctx->stream);
+        e = cudaGetLastError();
+    }
     if (e != cudaSuccess) {
         ctx->err = cudaGetErrorString(e);
         *out = ctx;
@@ -281,7 +287,7 @@ void rv_destroy(rv_ctx *ctx) {
                     ctx->d_regions, ctx->d_tiles, ctx->d_score_base, ctx->d_cellmem, ctx->d_head, ctx->d_slots,
                     ctx->d_arena, ctx->d_deferred, ctx->d_cand, ctx->d_counters, ctx->d_tmp_idx,
                     ctx->d_tmp_slots, ctx->d_tmp_cells, ctx->d_tmp_views, ctx->d_tmp_n, ctx->d_list,
-                    ctx->d_ftab};
+                    ctx->d_ftab, ctx->d_logfact};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (int i = 0; i < 12; i++)
@@ -572,9 +578,10 @@ rv_status rv_realign(rv_ctx *ctx, void *stream) {
     return RV_OK;
 }
 
-rv_status rv_score(rv_ctx *ctx, void *stream) {
+static rv_status score_impl(rv_ctx *ctx, void *stream, const DevParams &dp) {
     if (!ctx) return RV_ERR_ARG;
     if (ctx->stage < 2) { ctx->err = "rv_score before rv_pileup"; return RV_ERR_STATE; }
+    if (ctx->stage >= 4) { ctx->err = "this batch was already scored (submit it again)"; return RV_ERR_STATE; }
     RV_CUDA(cudaSetDevice(ctx->device));
     cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
     DevState st = ctx->state();
@@ -582,7 +589,7 @@ rv_status rv_score(rv_ctx *ctx, void *stream) {
     RV_CUDA(cudaMemsetAsync(ctx->d_counters + CNT_CAND, 0, 4, s));
     launch_ins_adjust(st, s);
     RV_CUDA(cudaEventRecord(ctx->ev[8], s));
-    launch_score(st, ctx->dp, s);
+    launch_score(st, dp, s);
     RV_CUDA(cudaGetLastError());
     RV_CUDA(cudaEventRecord(ctx->ev[3], s));
     unsigned int hdr[8];
@@ -619,11 +626,80 @@ rv_status rv_score(rv_ctx *ctx, void *stream) {
     return RV_OK;
 }
 
+rv_status rv_score(rv_ctx *ctx, void *stream) {
+    if (!ctx) return RV_ERR_ARG;
+    ctx->dp.dataset_min = 0;
+    return score_impl(ctx, stream, ctx->dp);
+}
+
+rv_status rv_score_candidates(rv_ctx *ctx, int min_count) {
+    if (!ctx || min_count < 1) return RV_ERR_ARG;
+    if (ctx->params.somatic) { ctx->err = "rv_score_candidates scores one sample (somatic = 0)"; return RV_ERR_ARG; }
+    ctx->dp.dataset_min = min_count;
+    rv_status s = score_impl(ctx, nullptr, ctx->dp);
+    return s;
+}
+
+rv_status rv_candidates(rv_ctx *ctx, float *features, rv_candidate *cands, int64_t cap, int64_t *n) {
+    if (!ctx || !n) return RV_ERR_ARG;
+    if (ctx->stage < 4) { ctx->err = "rv_candidates before a scoring call"; return RV_ERR_STATE; }
+    int64_t nv = 0;
+    for (const CandVar &c : ctx->h_cand) nv += c.kind == 1;
+    *n = nv;
+    if (!features && !cands) return RV_OK;
+    if (cap < nv) { ctx->err = "rv_candidates: buffers too small"; return RV_ERR_CAPACITY; }
+    RV_CUDA(cudaSetDevice(ctx->device));
+    const int64_t all = (int64_t)ctx->h_cand.size();
+    std::vector<float> f((size_t)std::max<int64_t>(all, 1) * RV_FEATURES);
+    if (features && all > 0) {
+        float *df = nullptr;
+        RV_CUDA(cudaMalloc((void **)&df, (size_t)all * RV_FEATURES * sizeof(float)));
+        DevState st = ctx->state();
+        launch_features(st, ctx->dp, ctx->d_cand, all, df, ctx->stream);
+        cudaError_t e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaMemcpyAsync(f.data(), df, (size_t)all * RV_FEATURES * sizeof(float),
+                                                  cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        cudaFree(df);
+        if (e != cudaSuccess) { ctx->err = cudaGetErrorString(e); return RV_ERR_CUDA; }
+        ctx->kernels += 1;
+    }
+    std::vector<uint8_t> emitted((size_t)std::max<int64_t>(all, 1), 0);
+    if (cands) {
+        std::string keep = ctx->text;
+        rv_status s = host_format_records(ctx, "", "", emitted.data());
+        ctx->text.swap(keep);
+        if (s) return s;
+    }
+    int64_t j = 0;
+    for (int64_t i = 0; i < all; i++) {
+        const CandVar &c = ctx->h_cand[i];
+        if (c.kind != 1) continue;
+        if (features) memcpy(features + j * RV_FEATURES, f.data() + i * RV_FEATURES, RV_FEATURES * sizeof(float));
+        if (cands) {
+            rv_candidate &o = cands[j];
+            memset(&o, 0, sizeof o);
+            o.region = c.region;
+            o.position = c.pos;
+            o.hard_pass = emitted[i];
+            if (c.key_len < 0) {
+                o.key_len = 1;
+                o.key[0] = "ACGT"[c.key_off & 3];
+            } else {
+                o.key_len = c.key_len;
+                memcpy(o.key, ctx->h_arena.data() + c.key_off, std::min<int>(c.key_len, (int)sizeof o.key - 1));
+            }
+        }
+        j++;
+    }
+    return RV_OK;
+}
+
 rv_status rv_format_records(rv_ctx *ctx, const char *sample, const char *gene, const char **text,
                             size_t *text_len, int64_t *n_records) {
     if (!ctx) return RV_ERR_ARG;
     if (ctx->stage < 4) { ctx->err = "rv_format_records before rv_score"; return RV_ERR_STATE; }
-    rv_status st = host_format_records(ctx, sample ? sample : "", gene ? gene : ctx->chr.c_str());
+    rv_status st = host_format_records(ctx, sample ? sample : "", gene ? gene : ctx->chr.c_str(), nullptr);
     if (st) return st;
     if (text) *text = ctx->text.c_str();
     if (text_len) *text_len = ctx->text.size();
@@ -746,7 +822,7 @@ rv_status rv_fisher_batch(rv_ctx *ctx, const int32_t *tables, int64_t n, double 
     if (e != cudaSuccess) { cudaFree(dt); ctx->err = cudaGetErrorString(e); return RV_ERR_CUDA; }
     e = cudaMemcpy(dt, tables, (size_t)n * 16, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) {
-        launch_fisher(dt, n, dp, dp + n, ctx->stream);
+        launch_fisher(dt, n, dp, dp + n, ctx->stream, ctx->d_logfact);
         e = cudaStreamSynchronize(ctx->stream);
     }
     if (e == cudaSuccess) e = cudaMemcpy(two_sided, dp, (size_t)n * 8, cudaMemcpyDeviceToHost);

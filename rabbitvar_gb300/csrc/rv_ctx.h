@@ -23,7 +23,11 @@ void launch_link(const DevState &st, cudaStream_t s);
 void launch_collisions(const DevState &st, cudaStream_t s);
 void launch_ins_adjust(const DevState &st, cudaStream_t s);
 void launch_score(const DevState &st, const DevParams &P, cudaStream_t s);
-void launch_fisher(const int32_t *tab, int64_t n, double *p2, double *ratio, cudaStream_t s);
+void launch_fisher(const int32_t *tab, int64_t n, double *p2, double *ratio, cudaStream_t s,
+                   const double *lf = nullptr);
+void launch_fill_logfact(double *lf, cudaStream_t s);
+void launch_features(const DevState &st, const DevParams &P, const CandVar *cand, int64_t n, float *out,
+                     cudaStream_t s);
 void launch_score_list(const DevState &st, const DevParams &P, const int2 *list, int n, cudaStream_t s);
 void launch_compact_slots(const DevState &st, uint32_t *out, unsigned int *n_out, cudaStream_t s);
 void launch_gather_slots(const Slot *slots, const uint32_t *idx, int64_t n, Slot *out, cudaStream_t s);
@@ -130,6 +134,7 @@ struct rv_ctx {
     size_t cap_tmp_views = 0;
     unsigned int *d_tmp_n = nullptr;
     // somatic mode: positions to score without screens; Fisher tables and results
+    double *d_logfact = nullptr;  // log(k!) table for the Fisher tests
     int2 *d_list = nullptr;
     size_t cap_list = 0;
     int32_t *d_ftab = nullptr;

@@ -513,7 +513,7 @@ rv_status host_realign_mnp(rv_ctx *ctx) {
 static void format_groups(const rv_ctx *ctx, const std::vector<const CandVar *> &order,
                           const std::vector<std::pair<size_t, size_t>> &groups, size_t g0, size_t g1,
                           const char *sample, const char *gene, std::string &text,
-                          std::vector<rv_site_record> &recs) {
+                          std::vector<rv_site_record> &recs, uint8_t *emitted) {
     const rv_params &P = ctx->params;
     const std::string &chr = ctx->chr;
     for (size_t gi = g0; gi < g1; gi++) {
@@ -549,6 +549,13 @@ static void format_groups(const rv_ctx *ctx, const std::vector<const CandVar *> 
             // variants described so far (src/ToVarsBuilder.cpp:183-186)
         }
         std::string reg = chr + ":" + std::to_string(Rg.start) + "-" + std::to_string(Rg.end);
+        if (ctx->dp.dataset_min > 0) {
+            // candidate-set scoring keeps positions the -f gate drops
+            // (src/ToVarsBuilder.cpp:170-175): apply it here
+            double maxfreq = 0;
+            for (RecVar &v : vs) maxfreq = std::max(maxfreq, v.c->freq);
+            if (maxfreq <= P.freq) continue;
+        }
         for (RecVar &v : vs) {
             if (!v.filled || !v.c->pass) continue;
             if (v.refallele.find('N') != std::string::npos) continue;
@@ -636,11 +643,12 @@ static void format_groups(const rv_ctx *ctx, const std::vector<const CandVar *> 
             r.fisher_p = c.fisher_p;
             r.fisher_ratio = c.fisher_ratio;
             recs.push_back(r);
+            if (emitted) emitted[v.c - ctx->h_cand.data()] = 1;
         }
     }
 }
 
-rv_status host_format_records(rv_ctx *ctx, const char *sample, const char *gene) {
+rv_status host_format_records(rv_ctx *ctx, const char *sample, const char *gene, uint8_t *emitted) {
     std::vector<const CandVar *> order(ctx->h_cand.size());
     for (size_t i = 0; i < order.size(); i++) order[i] = &ctx->h_cand[i];
     std::sort(order.begin(), order.end(), [](const CandVar *a, const CandVar *b) {
@@ -664,7 +672,9 @@ rv_status host_format_records(rv_ctx *ctx, const char *sample, const char *gene)
     size_t per = (groups.size() + nt - 1) / std::max(1, nt);
     for (int t = 0; t < nt; t++) {
         size_t a = std::min(groups.size(), t * per), b = std::min(groups.size(), (t + 1) * per);
-        auto job = [&, t, a, b]() { format_groups(ctx, order, groups, a, b, sample, gene, texts[t], recs[t]); };
+        auto job = [&, t, a, b]() {
+            format_groups(ctx, order, groups, a, b, sample, gene, texts[t], recs[t], emitted);
+        };
         if (t + 1 < nt) pool.emplace_back(job);
         else job();
     }

@@ -79,6 +79,8 @@ struct DevParams {
     int32_t vext, mismatch, local_realign, minr, read_pos_filter, min_mapq, min_bias_reads, samfilter;
     int32_t trim_bases_after, minmatch, dedup, unique_fwd, unique_first, do_pileup, fisher, move_indels_3;
     int32_t svminlen, somatic;
+    int32_t dataset_min;  // > 0: candidate-set scoring (every allele seen this many times)
+    int32_t pad;
 };
 
 // Cell arrays: one cell per (position, base A/C/G/T); index = 4 * cell + b.
@@ -169,6 +171,9 @@ struct DevState {
     CandVar *cand;
     unsigned int *n_cand;
     unsigned int cand_cap;
+    const double *logfact;   // log(k!) for k < kLogFact (Fisher tests)
 };
+
+constexpr int kLogFact = 1 << 16;
 
 }  // namespace rv

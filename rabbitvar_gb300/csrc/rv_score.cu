@@ -254,14 +254,33 @@ __device__ double log_choose(int n, int k) {
     return lgamma((double)n + 1.0) - lgamma((double)k + 1.0) - lgamma((double)(n - k) + 1.0);
 }
 
+// log(k!) from the context's table (the same lgamma values, computed once)
+__device__ __forceinline__ double log_choose_t(const double *lf, int n, int k) { return lf[n] - lf[k] - lf[n - k]; }
+
+__global__ void k_fill_logfact(double *lf, int n) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+        lf[k] = lgamma((double)k + 1.0);
+}
+
 // Two-sided Fisher exact test on (n11 n12; n21 n22) from the hypergeometric
 // definition: sum of table probabilities not above the observed one
 // (relative slack 1e-7 for ties).
-__device__ double fisher_two_sided(int n11, int n12, int n21, int n22) {
+__device__ double fisher_two_sided(int n11, int n12, int n21, int n22, const double *lf = nullptr) {
     int r1 = n11 + n12, c1 = n11 + n21, n = n11 + n12 + n21 + n22;
     int lo = r1 + c1 - n > 0 ? r1 + c1 - n : 0;
     int hi = r1 < c1 ? r1 : c1;
     if (n11 < 0 || n12 < 0 || n21 < 0 || n22 < 0 || lo >= hi) return 1.0;
+    if (lf && n < kLogFact) {
+        double base = log_choose_t(lf, n, c1);
+        double p_obs = exp(log_choose_t(lf, r1, n11) + log_choose_t(lf, n - r1, c1 - n11) - base);
+        double thr = p_obs * (1.0 + 1e-7);
+        double st = 0.0;
+        for (int x = lo; x <= hi; ++x) {
+            double p = exp(log_choose_t(lf, r1, x) + log_choose_t(lf, n - r1, c1 - x) - base);
+            if (p <= thr) st += p;
+        }
+        return st > 1.0 ? 1.0 : st;
+    }
     double base = log_choose(n, c1);
     double p_obs = exp(log_choose(r1, n11) + log_choose(n - r1, c1 - n11) - base);
     double thr = p_obs * (1.0 + 1e-7);
@@ -309,6 +328,7 @@ __device__ void score_position(const DevState &st, const DevParams &P, int lo, i
             double fr = cnt / (double)cov0;
             if (fr > P.freq) gate = true;
             if (fr >= P.freq && (int)ha[b] >= P.minr) pass = true;
+            if (P.dataset_min > 0 && cnt >= P.dataset_min) pass = gate = true;
         }
         // somatic mode keeps every covered position (no -f gate), so only
         // the emission condition screens
@@ -412,7 +432,7 @@ __device__ void score_position(const DevState &st, const DevParams &P, int lo, i
     // variant there (src/ToVarsBuilder.cpp:737-743); nothing is emitted
     if (nv == 0) return;
     if (!forced) {
-        if (!P.do_pileup && !P.somatic && maxfreq <= P.freq) return;
+        if (!P.do_pileup && !P.somatic && !P.dataset_min && maxfreq <= P.freq) return;
         if (n_var == 0) return;
     }
     // numeric pre-screen of isGoodVar: a necessary condition for emission
@@ -423,6 +443,7 @@ __device__ void score_position(const DevState &st, const DevParams &P, int lo, i
         if (v.freq >= P.freq && v.hi >= P.minr && v.pmean >= P.read_pos_filter && v.qual >= P.goodq &&
             v.qratio >= P.qratio)
             any = true;
+        if (P.dataset_min > 0 && v.cnt >= P.dataset_min) any = true;
     }
     if (!any && !P.do_pileup && !forced) return;
     // reference strand counts (collectReferenceVariants :730-760)
@@ -477,8 +498,8 @@ __device__ void score_position(const DevState &st, const DevParams &P, int lo, i
         o.hifreq = v.hifreq;
         o.extrafreq = v.extrafreq;
         o.nm = v.nmv;
-        if (P.fisher && !P.somatic && o.kind == 1 && o.pass) {
-            o.fisher_p = fisher_two_sided(rf, rr, fwd, rev);
+        if (P.fisher && !P.somatic && !P.dataset_min && o.kind == 1 && o.pass) {
+            o.fisher_p = fisher_two_sided(rf, rr, fwd, rev, st.logfact);
             double ad = (double)(rf * rev), bc = (double)(rr * fwd);
             o.fisher_ratio = (bc != 0 && ad != 0) ? (ad > bc ? ad / bc : bc / ad) : 0.0;
         } else {
@@ -526,11 +547,93 @@ __global__ void k_score_list(DevState st, DevParams P, const int2 *list, int n) 
     }
 }
 
+// Features of the learned filter: 40 floats per candidate allele, from its
+// site statistics, its key and the reference around it.
+__device__ int run_len(const DevState &st, const Region &R, int p, int dir) {
+    char b = ref_at(st, R, p);
+    if (!b) return 0;
+    int n = 0;
+    for (int q = p + dir; n < 20 && q >= R.ws && q <= R.we && st.ref[q - 1] == b; q += dir) n++;
+    return n;
+}
+
+__global__ void k_features(DevState st, DevParams P, const CandVar *cand, int64_t n, float *out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const CandVar c = cand[i];
+        float *f = out + i * 40;
+        const Region &R = st.regions[c.region];
+        const int fwd = max(c.fwd, 0), rev = max(c.rev, 0), rf = max(c.rfc, 0), rr = max(c.rrc, 0);
+        const float pc = (float)max(c.pc, 0), tpc = (float)max(c.tpc, 1);
+        f[0] = log1pf((float)c.tpc) / 8.f;
+        f[1] = log1pf(pc) / 8.f;
+        f[2] = (float)c.freq;
+        f[3] = log1pf((float)c.hicnt) / 8.f;
+        f[4] = log1pf((float)c.hicov) / 8.f;
+        f[5] = (float)c.hifreq;
+        f[6] = pc > 0 ? fwd / pc : 0.5f;
+        f[7] = rf + rr > 0 ? rf / (float)(rf + rr) : 0.5f;
+        f[8] = c.bias * 0.5f;
+        f[9] = c.ref_bias * 0.5f;
+        f[10] = (float)c.pstd;
+        f[11] = (float)c.qstd;
+        f[12] = (float)c.pmean / 75.f;
+        f[13] = (float)c.qual / 40.f;
+        f[14] = (float)c.mq / 60.f;
+        f[15] = log1pf((float)c.qratio) / 4.f;
+        f[16] = (float)c.extrafreq;
+        f[17] = (float)c.nm / 10.f;
+        const double fp = fisher_two_sided(rf, rr, fwd, rev, st.logfact);
+        f[18] = fminf(-log10f(fmaxf((float)fp, 1e-30f)), 30.f) / 10.f;
+        const double ad = (double)rf * rev, bc = (double)rr * fwd;
+        const double ratio = (bc != 0 && ad != 0) ? (ad > bc ? ad / bc : bc / ad) : 0.0;
+        f[19] = log1pf((float)ratio) / 4.f;
+        int kind = 0;  // 0 SNV, 1 MNV, 2 insertion, 3 deletion, 4 other
+        int klen = 1;
+        if (c.key_len >= 0) {
+            const uint8_t *k = st.hash.arena + c.key_off;
+            klen = c.key_len;
+            if (k[0] == '+') kind = 2;
+            else if (k[0] == '-') kind = 3;
+            else if (klen > 2 && k[1] == '&') kind = 1;
+            else kind = 4;
+        }
+        for (int j = 0; j < 5; j++) f[20 + j] = kind == j ? 1.f : 0.f;
+        f[25] = klen / 20.f;
+        f[26] = c.nvars / 8.f;
+        f[27] = c.rank / 8.f;
+        f[28] = c.rank == 0 ? 1.f : 0.f;
+        f[29] = run_len(st, R, c.pos, -1) / 20.f;
+        f[30] = run_len(st, R, c.pos, 1) / 20.f;
+        int gc = 0, tot = 0, rep = 0;
+        for (int q = c.pos - 20; q <= c.pos + 20; q++) {
+            char b = ref_at(st, R, q);
+            if (!b) continue;
+            tot++;
+            if (b == 'G' || b == 'C') gc++;
+            if (q + 2 <= c.pos + 20 && b == ref_at(st, R, q + 2)) rep++;
+        }
+        f[31] = tot ? gc / (float)tot : 0.f;
+        f[32] = rep / 40.f;
+        f[33] = c.hicov / tpc;
+        f[34] = pc > 0 ? c.hicnt / pc : 0.f;
+        f[35] = (rf + rr) / tpc;
+        f[36] = c.pc >= P.minr ? 1.f : 0.f;
+        f[37] = c.freq >= P.freq ? 1.f : 0.f;
+        f[38] = (float)c.pass;
+        f[39] = log1pf((float)abs(fwd - rev)) / 8.f;
+    }
+}
+
+void launch_features(const DevState &st, const DevParams &P, const CandVar *cand, int64_t n, float *out,
+                     cudaStream_t s) {
+    if (n > 0) k_features<<<(int)std::min<int64_t>((n + 127) / 128, 4096), 128, 0, s>>>(st, P, cand, n, out);
+}
+
 // Batched Fisher tests (rv_fisher_batch)
-__global__ void k_fisher(const int32_t *tab, int64_t n, double *p2, double *ratio) {
+__global__ void k_fisher(const int32_t *tab, int64_t n, double *p2, double *ratio, const double *lf) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         int a = tab[4 * i], b = tab[4 * i + 1], c = tab[4 * i + 2], d = tab[4 * i + 3];
-        p2[i] = fisher_two_sided(a, b, c, d);
+        p2[i] = fisher_two_sided(a, b, c, d, lf);
         double ad = (double)a * d, bc = (double)b * c;
         ratio[i] = (bc != 0 && ad != 0) ? (ad > bc ? ad / bc : bc / ad) : 0.0;
     }
@@ -550,8 +653,10 @@ void launch_score(const DevState &st, const DevParams &P, cudaStream_t s) {
 void launch_score_list(const DevState &st, const DevParams &P, const int2 *list, int n, cudaStream_t s) {
     if (n > 0) k_score_list<<<(n + 127) / 128 < 1216 ? (n + 127) / 128 : 1216, 128, 0, s>>>(st, P, list, n);
 }
-void launch_fisher(const int32_t *tab, int64_t n, double *p2, double *ratio, cudaStream_t s) {
-    if (n > 0) k_fisher<<<(int)((n + 127) / 128 < 4096 ? (n + 127) / 128 : 4096), 128, 0, s>>>(tab, n, p2, ratio);
+void launch_fisher(const int32_t *tab, int64_t n, double *p2, double *ratio, cudaStream_t s, const double *lf) {
+    if (n > 0)
+        k_fisher<<<(int)((n + 127) / 128 < 4096 ? (n + 127) / 128 : 4096), 128, 0, s>>>(tab, n, p2, ratio, lf);
 }
+void launch_fill_logfact(double *lf, cudaStream_t s) { k_fill_logfact<<<256, 256, 0, s>>>(lf, kLogFact); }
 
 }  // namespace rv

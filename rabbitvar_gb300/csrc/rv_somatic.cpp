@@ -16,6 +16,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "rv_ctx.h"
@@ -329,6 +330,27 @@ void put_fisher(std::string &o, double p, const int32_t *t) {
     o += b;
 }
 
+// Runs fn(thread, begin, end) over [0, n) split into contiguous chunks on
+// up to `max_threads` host threads (the calling thread takes the last chunk).
+template <class F>
+void parallel_chunks(size_t n, size_t min_per_thread, F fn) {
+    size_t nt = std::min<size_t>(std::max(1u, std::thread::hardware_concurrency()), 32);
+    nt = std::max<size_t>(1, std::min(nt, n / std::max<size_t>(1, min_per_thread)));
+    size_t per = (n + nt - 1) / nt;
+    std::vector<std::thread> pool;
+    for (size_t k = 0; k < nt; k++) {
+        size_t a = std::min(n, k * per), b = std::min(n, (k + 1) * per);
+        if (k + 1 < nt) pool.emplace_back(fn, k, a, b);
+        else fn(k, a, b);
+    }
+    for (auto &th : pool) th.join();
+}
+
+size_t threads_for(size_t n, size_t min_per_thread) {
+    size_t nt = std::min<size_t>(std::max(1u, std::thread::hardware_concurrency()), 32);
+    return std::max<size_t>(1, std::min(nt, n / std::max<size_t>(1, min_per_thread)));
+}
+
 }  // namespace
 
 rv_status host_format_somatic(rv_ctx *t, rv_ctx *n, const char *sample, const char *gene) {
@@ -337,26 +359,34 @@ rv_status host_format_somatic(rv_ctx *t, rv_ctx *n, const char *sample, const ch
     std::vector<std::pair<size_t, size_t>> tg, ng;
     group(t, to, tg);
     group(n, no, ng);
-    std::vector<Rec> recs;
-    Classifier C{P, recs};
-    size_t j = 0;
-    for (const auto &gi : tg) {
-        SPos v1;
-        build_position(t, &to[gi.first], gi.second - gi.first, v1);
-        while (j < ng.size() && std::make_pair(no[ng[j].first]->region, no[ng[j].first]->pos) <
-                                    std::make_pair(v1.region, v1.pos))
-            j++;
-        bool has2 = j < ng.size() && no[ng[j].first]->region == v1.region && no[ng[j].first]->pos == v1.pos;
-        if (!has2) {
-            if (!v1.vars.empty()) C.one_sample(v1);
-            continue;
+    // positions are independent: classify them on host threads, keeping order
+    const size_t kMinPos = 64;
+    std::vector<std::vector<Rec>> part(threads_for(tg.size(), kMinPos));
+    parallel_chunks(tg.size(), kMinPos, [&](size_t k, size_t a, size_t b) {
+        Classifier C{P, part[k]};
+        for (size_t gi = a; gi < b; gi++) {
+            SPos v1;
+            build_position(t, &to[tg[gi].first], tg[gi].second - tg[gi].first, v1);
+            auto key = std::make_pair(v1.region, v1.pos);
+            auto it = std::lower_bound(ng.begin(), ng.end(), key, [&](const std::pair<size_t, size_t> &g,
+                                                                      const std::pair<int, int> &k2) {
+                return std::make_pair(no[g.first]->region, no[g.first]->pos) < k2;
+            });
+            bool has2 = it != ng.end() && no[it->first]->region == v1.region && no[it->first]->pos == v1.pos;
+            if (!has2) {
+                if (!v1.vars.empty()) C.one_sample(v1);
+                continue;
+            }
+            SPos v2;
+            build_position(n, &no[it->first], it->second - it->first, v2);
+            if (v1.vars.empty() && v2.vars.empty()) continue;
+            if (!v1.vars.empty()) C.first_sample(v1, v2);
+            else C.second_sample(v1, v2);
         }
-        SPos v2;
-        build_position(n, &no[ng[j].first], ng[j].second - ng[j].first, v2);
-        if (v1.vars.empty() && v2.vars.empty()) continue;
-        if (!v1.vars.empty()) C.first_sample(v1, v2);
-        else C.second_sample(v1, v2);
-    }
+    });
+    std::vector<Rec> recs;
+    for (auto &pv : part)
+        for (auto &r : pv) recs.push_back(std::move(r));
     // the three Fisher tables of every record, tested on the device
     std::vector<int32_t> tab;
     std::vector<double> p2;
@@ -380,10 +410,11 @@ rv_status host_format_somatic(rv_ctx *t, rv_ctx *n, const char *sample, const ch
         if (s) return s;
     }
     const Region *regs = t->regions.data();
-    std::string &o = t->text;
-    o.clear();
+    std::vector<std::string> texts(threads_for(recs.size(), 256));
+    parallel_chunks(recs.size(), 256, [&](size_t k, size_t i0, size_t i1) {
+    std::string &o = texts[k];
     char b[96];
-    for (size_t i = 0; i < recs.size(); i++) {
+    for (size_t i = i0; i < i1; i++) {
         const Rec &r = recs[i];
         o += sample;
         o += '\t';
@@ -434,6 +465,9 @@ rv_status host_format_somatic(rv_ctx *t, rv_ctx *n, const char *sample, const ch
         }
         o += '\n';
     }
+    });
+    t->text.clear();
+    for (auto &x : texts) t->text += x;
     t->n_records = (int64_t)recs.size();
     t->h_records.clear();
     return RV_OK;

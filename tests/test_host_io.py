@@ -53,7 +53,7 @@ def test_library_exports_every_declared_symbol():
     from rabbitvar_gb300 import api
     L = api.lib()
     declared = set()
-    for h in ("rvgpu.h", "rvgpu_io.h"):
+    for h in ("rvgpu.h", "rvgpu_io.h", "rvgpu_mlp.h"):
         src = open(os.path.join(ROOT, "include", h)).read()
         declared |= set(re.findall(r"^(?:rv_status|void|const char|void \*|const char \*)\s*\**\s*(rv_[a-z_0-9]+)\s*\(",
                                    src, flags=re.M))
