@@ -153,6 +153,31 @@ def cpu_baseline_run(g, tumor, normal, regions, threads: int, n_regions: int):
     return reads / dt, dt, reads
 
 
+def learned_filter_leg():
+    """The learned filter against the hard filter on the deep-panel shape:
+    trained on 4 seeded panels, evaluated on 2 held-out ones (planted truth),
+    F1 and precision at the hard filter's recall, plus the training step
+    time and the inference rate (candidates/s, features already built)."""
+    from rabbitvar_gb300 import learn, mlp
+    xtr, ytr, _ = learn.dataset([101, 102, 103, 104], n_regions=6)
+    xte, yte, hte = learn.dataset([201, 202], n_regions=6)
+    m = mlp.Mlp(batch=4096, seed=3)
+    t0 = time.perf_counter()
+    m.train(xtr, ytr, epochs=20, lr=1e-3)
+    train_s = time.perf_counter() - t0
+    m.predict(xte)
+    t0 = time.perf_counter()
+    scores = m.predict(xte)
+    pred_s = time.perf_counter() - t0
+    res = learn.compare(scores, yte, hte)
+    res.update({"train_candidates": int(len(ytr)), "epochs": 20, "train_s": train_s,
+                "train_step_ms": m.step_ms(), "predict_candidates_per_s": len(yte) / pred_s,
+                "network": "40-128-128-128-1 GELU, BF16 tcgen05 GEMMs, FP32 accumulate, Adam",
+                "data": "synthetic deep panels (6 x 5 kb at 1500x, C>A artifacts 1e-4/base at Q20, planted truth)"})
+    m.close()
+    return res
+
+
 def run_reference(args, rank):
     if rank != 0:
         return
@@ -183,6 +208,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-learned", action="store_true")
     args = ap.parse_args()
     rank, world, dist = dist_init()
     if args.impl == "reference":
@@ -286,6 +312,11 @@ def main():
                      "kernel": "k_pileup_tiles", "alg_bytes_per_launch": per_launch_bytes},
         "clocks": clk,
     }
+    # sites/s: region positions of both samples scored per second of k_score
+    score_ms = statistics.mean(s["score"] for s in stages)
+    out["sites_per_s"] = (sum(r[1] - r[0] + 1 for r in regions)) / (score_ms * 1e-3)
+    if rank == 0 and not args.no_learned:
+        out["learned_filter"] = learned_filter_leg()
     if rank == 0 and not args.no_cpu_baseline:
         v, dt, nr = cpu_baseline_run(g, tumor, normal, regions, 1, CPU_TILES)
         out["cpu_baseline"] = {"value": v, "unit": "reads/s", "cores": 1, "kind": "port",

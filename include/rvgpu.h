@@ -42,7 +42,8 @@ typedef struct {
     double goodq;          /* -q  22.5 */
     int32_t vext;          /* -X  2 */
     int32_t mismatch;      /* -m  8 */
-    int32_t local_realign; /* -k  1 (this build supports 0; 1 returns RV_ERR_UNSUPPORTED) */
+    int32_t local_realign; /* -k  1: the CIGAR rewrite runs in rv_pileup; rv_realign's indel passes
+                              are not in this build (RV_ERR_UNSUPPORTED) */
     double freq;           /* -f  0.01 */
     int32_t minr;          /* -r  2 */
     int32_t read_pos_filter; /* -P 5 */

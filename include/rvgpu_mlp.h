@@ -47,6 +47,10 @@ rv_status rv_mlp_get_params(rv_mlp *m, float *params);
 rv_status rv_mlp_train(rv_mlp *m, const float *features, const float *labels, int64_t n, int epochs, float lr,
                        float pos_weight, uint64_t seed, float *epoch_loss);
 
+/* Mean device time of one training step in the last rv_mlp_train call (a
+ * step is one captured CUDA graph: gather, forward, backward, Adam). */
+rv_status rv_mlp_step_ms(const rv_mlp *m, double *ms);
+
 /* One forward and backward pass over n <= batch rows without an update:
  * the FP32 gradients (RV_MLP_PARAMS floats) and the mean loss. */
 rv_status rv_mlp_gradients(rv_mlp *m, const float *features, const float *labels, int64_t n, float pos_weight,

@@ -17,6 +17,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <regex>
 #include <set>
 #include <string>
 #include <vector>
@@ -82,6 +83,8 @@ struct Ref {
     bool has_ne(char c, int p) const { return has(p) && at(p) != c; }
 };
 
+struct UnsupportedRead {};
+
 struct ReadView {
     int32_t pos, mpos, nm;
     uint16_t flag;
@@ -93,6 +96,396 @@ struct ReadView {
     vector<uint8_t> qual_buf;  // [byte preceding quals] + quals
     const uint8_t *qual() const { return qual_buf.data() + 1; }
 };
+
+// ---------------------------------------------------------------------------
+// -k 1 CIGAR rewrite: CigarModifier (src/cigarModifier.cpp), on the CIGAR
+// string with the reference's own pattern grammar (include/patterns.h:52-153)
+// ---------------------------------------------------------------------------
+struct CigarMod {
+    Ref &R;
+    const vector<char> &seq;
+    const uint8_t *qual;
+    int lseq;
+    int position;
+    string cs;
+
+    static const std::regex &re(int i) {
+        static const std::regex tab[] = {
+            std::regex("^(\\d+)S(\\d+)([ID])"),                                           // 0
+            std::regex("(\\d+)([ID])(\\d+)S$"),                                           // 1
+            std::regex("^(\\d+)S(\\d+)M(\\d+)([ID])"),                                    // 2
+            std::regex("(\\d+)([ID])(\\d+)M(\\d+)S$"),                                    // 3
+            std::regex("^(\\d)M(\\d+)([ID])(\\d+)M"),                                     // 4
+            std::regex("^\\dM\\d+[ID]\\d+M"),                                             // 5
+            std::regex("(\\d+)([ID])(\\d)M$"),                                            // 6
+            std::regex("^(.*?)(\\d+)M(\\d+)D(\\d+)M(\\d+)I(\\d+)M(\\d+)D(\\d+)M"),        // 7
+            std::regex("(\\d+)M(\\d+)D(\\d+)M(\\d+)I(\\d+)M(\\d+)D(\\d+)M"),              // 8
+            std::regex("^(.*?)(\\d+)M(\\d+)D(\\d+)M(\\d+)D(\\d+)M(\\d+)D(\\d+)M"),        // 9
+            std::regex("^(.*?)(\\d+)M(\\d+)([DI])(\\d+)M(\\d+)([DI])(\\d+)M(\\d+)([DI])(\\d+)M"),  // 10
+            std::regex("\\d+M\\d+[DI]\\d+M\\d+[DI]\\d+M\\d+[DI]\\d+M"),                   // 11
+            std::regex("\\d+M\\d+D\\d+M\\d+D\\d+M\\d+D\\d+M"),                            // 12
+            std::regex("(\\d+)D(\\d+)M(\\d+)([DI])(\\d+I)?"),                             // 13
+            std::regex("(\\d+)I(\\d+)M(\\d+)([DI])(\\d+I)?"),                             // 14
+            std::regex("(\\D)(\\d+)I(\\d+)M(\\d+)([DI])(\\d+I)?"),                        // 15
+            std::regex("(\\d+)D(\\d+)D"),                                                 // 16
+            std::regex("(\\d+)I(\\d+)I"),                                                 // 17
+            std::regex("^(.*?)(\\d+)M$"),                                                 // 18
+            std::regex("\\d+M$"),                                                         // 19
+            std::regex("^(\\d+)M"),                                                       // 20
+            std::regex("^(\\d+)S(\\d+)M"),                                                // 21
+            std::regex("\\d+M\\d+S$"),                                                    // 22
+            std::regex("^(.*?)(\\d+)M(\\d+)S$"),                                          // 23
+            std::regex("(\\d+)[MND]"),                                                    // 24
+            std::regex("(\\d+)[MIS]"),                                                    // 25
+        };
+        return tab[i];
+    }
+    static int I(const std::smatch &m, int k) { return std::stoi(m.str(k)); }
+    static int sum_of(int rx, const string &s) {  // globalFindAndSum (include/util.h:186-199)
+        int r = 0;
+        for (std::sregex_iterator it(s.begin(), s.end(), re(rx)), e; it != e; ++it) r += std::stoi((*it)[1].str());
+        return r;
+    }
+    void rep_first(int rx, const string &to) {
+        cs = std::regex_replace(cs, re(rx), to, std::regex_constants::format_first_only);
+    }
+    void rep_all(int rx, const string &to) { cs = std::regex_replace(cs, re(rx), to); }
+    bool eq(int p, int i) const { return R.has(p) && R.at(p) == seq[i]; }    // isHasAndEquals(ref, p, seq, i)
+    bool ne(int p, int i) const { return R.has(p) && R.at(p) != seq[i]; }    // isHasAndNotEquals(ref, p, seq, i)
+
+    // combineBeginDigM (:412-439)
+    void begin_dig_m(const std::smatch &m) {
+        int mch = I(m, 1), rn = 0, rrn = 0, rmch = 0;
+        while (rrn < mch && rn < mch) {
+            if (!R.has(position + rrn)) break;
+            if (ne(position + rrn, rrn)) { rn = rrn + 1; rmch = 0; }
+            else if (eq(position + rrn, rrn)) rmch++;
+            rrn++;
+            if (rmch >= 3) break;
+        }
+        if (rn > 0 && rn <= 3) {
+            mch -= rn;
+            rep_first(20, std::to_string(rn) + "S" + std::to_string(mch) + "M");
+            position += rn;
+        }
+    }
+    // combineDigSDigM (:445-525)
+    void dig_s_dig_m(const std::smatch &m) {
+        int mch = I(m, 2), soft = I(m, 1), rn = 0;
+        std::set<char> RN;
+        while (rn < soft && eq(position - rn - 1, soft - rn - 1) && qual[soft - rn - 1] > 10) rn++;
+        if (rn > 0) {
+            mch += rn;
+            soft -= rn;
+            rep_first(21, soft > 0 ? std::to_string(soft) + "S" + std::to_string(mch) + "M" : std::to_string(mch) + "M");
+            position -= rn;
+            rn = 0;
+        }
+        if (soft > 0) {
+            while (rn + 1 < soft && eq(position - rn - 2, soft - rn - 2) && qual[soft - rn - 2] > 10) {
+                rn++;
+                if (R.has(position - rn - 2)) RN.insert(R.at(position - rn - 2));
+            }
+            int rn_nt = (int)RN.size();
+            if ((rn > 4 && rn_nt > 1) || eq(position - 1, soft - 1)) {
+                mch += rn + 1;
+                soft -= rn + 1;
+                rep_first(21, soft > 0 ? std::to_string(soft) + "S" + std::to_string(mch) + "M"
+                                       : std::to_string(mch) + "M");
+                position -= rn + 1;
+            }
+            if (rn == 0) {
+                int rrn = 0, rmch = 0;
+                while (rrn < mch && rn < mch) {
+                    if (!R.has(position + rrn)) break;
+                    if (ne(position + rrn, soft + rrn)) { rn = rrn + 1; rmch = 0; }
+                    else if (eq(position + rrn, soft + rrn)) rmch++;
+                    rrn++;
+                    if (rmch >= 3) break;
+                }
+                if (rn > 0 && rn < mch) {
+                    soft += rn;
+                    mch -= rn;
+                    rep_first(21, std::to_string(soft) + "S" + std::to_string(mch) + "M");
+                    position += rn;
+                }
+            }
+        }
+    }
+    // captureMisSoftly3Mismatches (:531-566)
+    void mis3(const std::smatch &m) {
+        string ov5 = m.str(1);
+        int mch = I(m, 2), refoff = position + mch, rdoff = mch;
+        if (!ov5.empty()) { refoff += sum_of(24, ov5); rdoff += sum_of(25, ov5); }
+        int rn = 0, rrn = 0, rmch = 0;
+        while (rrn < mch && rn < mch) {
+            if (!R.has(refoff - rrn - 1)) break;
+            if (rrn < rdoff && R.at(refoff - rrn - 1) != seq[rdoff - rrn - 1]) { rn = rrn + 1; rmch = 0; }
+            else if (rrn < rdoff && R.at(refoff - rrn - 1) == seq[rdoff - rrn - 1]) rmch++;
+            rrn++;
+            if (rmch >= 3) break;
+        }
+        mch -= rn;
+        if (rn > 0 && rn <= 3) rep_first(19, std::to_string(mch) + "M" + std::to_string(rn) + "S");
+    }
+    // captureMisSoftlyMS (:572-653)
+    void mis_ms(const std::smatch &m) {
+        string ov5 = m.str(1);
+        int mch = I(m, 2), soft = I(m, 3), refoff = position + mch, rdoff = mch;
+        if (!ov5.empty()) { refoff += sum_of(24, ov5); rdoff += sum_of(25, ov5); }
+        int rn = 0;
+        std::set<char> RN;
+        while (rn < soft && eq(refoff + rn, rdoff + rn) && qual[rdoff + rn] > 10) rn++;
+        if (rn > 0) {
+            mch += rn;
+            soft -= rn;
+            rep_first(22, soft > 0 ? std::to_string(mch) + "M" + std::to_string(soft) + "S" : std::to_string(mch) + "M");
+            rn = 0;
+        }
+        if (soft > 0) {
+            while (rn + 1 < soft && eq(refoff + rn + 1, rdoff + rn + 1) && qual[rdoff + rn + 1] > 10) {
+                rn++;
+                if (R.has(refoff + rn + 1)) RN.insert(R.at(refoff + rn + 1));
+            }
+            int rn_nt = (int)RN.size();
+            if (rn > 4 && rn_nt > 1) {
+                mch += rn + 1;
+                soft -= rn + 1;
+                rep_first(22, soft > 0 ? std::to_string(mch) + "M" + std::to_string(soft) + "S"
+                                       : std::to_string(mch) + "M");
+            }
+            if (rn == 0) {
+                int rrn = 0, rmch = 0;
+                while (rrn < mch && rn < mch) {
+                    if (!R.has(refoff - rrn - 1)) break;
+                    if (rrn < rdoff && R.at(refoff - rrn - 1) != seq[rdoff - rrn - 1]) { rn = rrn + 1; rmch = 0; }
+                    else if (rrn < rdoff && R.at(refoff - rrn - 1) == seq[rdoff - rrn - 1]) rmch++;
+                    rrn++;
+                    if (rmch >= 3) break;
+                }
+                if (rn > 0 && rn < mch) {
+                    soft += rn;
+                    mch -= rn;
+                    rep_first(22, std::to_string(mch) + "M" + std::to_string(soft) + "S");
+                }
+            }
+        }
+    }
+    // combineToCloseToOne (:662-707)
+    bool close_to_one(const std::smatch &m, bool flag) {
+        string op = m.str(5);
+        int g2 = I(m, 2), g3 = I(m, 3), g4 = I(m, 4);
+        if (g3 <= 15) {
+            int dlen = g3, ilen = g2 + g3;
+            if (op == "I") ilen += g4;
+            else if (op == "D") {
+                dlen += g4;
+                string istr = m.str(6);
+                if (!istr.empty()) ilen += std::stoi(istr.substr(0, istr.size() - 1));
+            }
+            rep_first(14, std::to_string(dlen) + "D" + std::to_string(ilen) + "I");
+            flag = true;
+        }
+        return flag;
+    }
+    // combineToCloseToCorrect (:717-745)
+    bool close_to_correct(const std::smatch &m, bool flag) {
+        int g1 = I(m, 1), g2 = I(m, 2), g3 = I(m, 3);
+        if (g2 <= 15) {
+            string op = m.str(4);
+            int dlen = g1 + g2, ilen = g2;
+            if (op == "I") ilen += g3;
+            else if (op == "D") {
+                dlen += g3;
+                string istr = m.str(5);
+                if (!istr.empty()) ilen += std::stoi(istr.substr(0, istr.size() - 1));
+            }
+            rep_first(13, std::to_string(dlen) + "D" + std::to_string(ilen) + "I");
+            flag = true;
+        }
+        return flag;
+    }
+    // the matched-bases scan shared by the three-event rules
+    int run_match(int rdoff, int refoff) const {
+        int rn = 0;
+        while (rdoff + rn < lseq && R.has(refoff + rn) && R.at(refoff + rn) == seq[rdoff + rn]) rn++;
+        return rn;
+    }
+    // threeIndels (:755-846)
+    bool three_indels(const std::smatch &m, bool flag) {
+        int mid = I(m, 5) + I(m, 8), tslen = mid, dlen = mid;
+        for (int k : {4, 7, 10}) {
+            if (m.str(k) == "I") tslen += I(m, k - 1);
+            if (m.str(k) == "D") dlen += I(m, k - 1);
+        }
+        string ov5 = m.str(1);
+        int refoff = position + I(m, 2), rdoff = I(m, 2), RDOFF = I(m, 2), rm = I(m, 11);
+        if (!ov5.empty()) { refoff += sum_of(24, ov5); rdoff += sum_of(25, ov5); }
+        int rn = run_match(rdoff, refoff);
+        RDOFF += rn;
+        dlen -= rn;
+        tslen -= rn;
+        string nc = std::to_string(RDOFF) + "M";
+        if (tslen <= 0) {
+            dlen -= tslen;
+            rm += tslen;
+            if (dlen == 0) {
+                RDOFF += rm;
+                nc = std::to_string(RDOFF) + "M";
+            } else if (dlen < 0) {
+                tslen = -dlen;
+                rm += dlen;
+                if (rm < 0) {
+                    RDOFF += rm;
+                    nc = std::to_string(RDOFF) + "M" + std::to_string(tslen) + "I";
+                } else {
+                    nc += std::to_string(tslen) + "I" + std::to_string(rm) + "M";
+                }
+            } else {
+                nc += std::to_string(dlen) + "D" + std::to_string(rm) + "M";
+            }
+        } else {
+            if (dlen == 0) nc += std::to_string(tslen) + "I" + std::to_string(rm) + "M";
+            else if (dlen < 0) { rm += dlen; nc += std::to_string(tslen) + "I" + std::to_string(rm) + "M"; }
+            else nc += std::to_string(dlen) + "D" + std::to_string(tslen) + "I" + std::to_string(rm) + "M";
+        }
+        if (mid <= 15) { rep_first(11, nc); flag = true; }
+        return flag;
+    }
+    // threeDeletions (:856-910)
+    bool three_deletions(const std::smatch &m, bool flag) {
+        int tslen = I(m, 4) + I(m, 6), dlen = I(m, 3) + I(m, 4) + I(m, 5) + I(m, 6) + I(m, 7);
+        int mid = I(m, 4) + I(m, 6);
+        string ov5 = m.str(1);
+        int refoff = position + I(m, 2), rdoff = I(m, 2), RDOFF = I(m, 2), rm = I(m, 8);
+        if (!ov5.empty()) { refoff += sum_of(24, ov5); rdoff += sum_of(25, ov5); }
+        int rn = run_match(rdoff, refoff);
+        RDOFF += rn;
+        dlen -= rn;
+        tslen -= rn;
+        string nc = std::to_string(RDOFF) + "M";
+        if (tslen <= 0) { dlen -= tslen; rm += tslen; nc += std::to_string(dlen) + "D" + std::to_string(rm) + "M"; }
+        else nc += std::to_string(dlen) + "D" + std::to_string(tslen) + "I" + std::to_string(rm) + "M";
+        if (mid <= 15) { rep_first(12, nc); flag = true; }
+        return flag;
+    }
+    // twoDeletionsInsertionToComplex (:920-972)
+    bool two_del_ins(const std::smatch &m, bool flag) {
+        int tslen = I(m, 4) + I(m, 5) + I(m, 6), dlen = I(m, 3) + I(m, 4) + I(m, 6) + I(m, 7);
+        int mid = I(m, 4) + I(m, 6);
+        string ov5 = m.str(1);
+        int mch = I(m, 2), refoff = position + mch, rdoff = mch, RDOFF = mch, rm = I(m, 8);
+        if (!ov5.empty()) { refoff += sum_of(24, ov5); rdoff += sum_of(25, ov5); }
+        int rn = run_match(rdoff, refoff);
+        RDOFF += rn;
+        dlen -= rn;
+        tslen -= rn;
+        string nc = std::to_string(RDOFF) + "M";
+        if (tslen <= 0) { dlen -= tslen; rm += tslen; nc += std::to_string(dlen) + "D" + std::to_string(rm) + "M"; }
+        else nc += std::to_string(dlen) + "D" + std::to_string(tslen) + "I" + std::to_string(rm) + "M";
+        if (mid <= 15) { rep_first(8, nc); flag = true; }
+        return flag;
+    }
+    // beginDigitMNumberIorDNumberM (:982-1000)
+    bool begin_digit_m(const std::smatch &m) {
+        int tmid = I(m, 1), mlen = I(m, 4), tn = 0;
+        int tslen = tmid + (m.str(3) == "I" ? I(m, 2) : 0);
+        position += tmid + (m.str(3) == "D" ? I(m, 2) : 0);
+        while (tn < mlen && R.has(position + tn) && R.at(position + tn) != seq[tslen + tn]) tn++;
+        tslen += tn;
+        mlen -= tn;
+        position += tn;
+        rep_first(5, std::to_string(tslen) + "S" + std::to_string(mlen) + "M");
+        return true;
+    }
+
+    // modifyCigar (:219-390) after the leading/trailing D and I handling,
+    // which returns before reaching here for the CIGARs this restatement takes
+    void rules(int indel) {
+        std::smatch m;
+        bool flag = true;
+        while (flag && indel > 0) {
+            flag = false;
+            if (std::regex_search(cs, m, re(0))) {
+                string t = std::to_string(I(m, 1) + (m.str(3) == "I" ? I(m, 2) : 0)) + "S";
+                position += m.str(3) == "D" ? I(m, 2) : 0;
+                rep_all(0, t);
+                flag = true;
+            }
+            if (std::regex_search(cs, m, re(1))) {
+                string t = std::to_string(I(m, 3) + (m.str(2) == "I" ? I(m, 1) : 0)) + "S";
+                rep_all(1, t);
+                flag = true;
+            }
+            if (std::regex_search(cs, m, re(2))) {
+                int tmid = I(m, 2);
+                if (tmid <= 10) {
+                    string t = std::to_string(I(m, 1) + tmid + (m.str(4) == "I" ? I(m, 3) : 0)) + "S";
+                    position += tmid + (m.str(4) == "D" ? I(m, 3) : 0);
+                    rep_all(2, t);
+                    flag = true;
+                }
+            }
+            if (std::regex_search(cs, m, re(3))) {
+                int tmid = I(m, 3);
+                if (tmid <= 10) {
+                    string t = std::to_string(I(m, 4) + tmid + (m.str(2) == "I" ? I(m, 1) : 0)) + "S";
+                    rep_all(3, t);
+                    flag = true;
+                }
+            }
+            if (std::regex_search(cs, m, re(4))) flag = begin_digit_m(m);
+            if (std::regex_search(cs, m, re(6))) {
+                string t = std::to_string(I(m, 3) + (m.str(2) == "I" ? I(m, 1) : 0)) + "S";
+                rep_all(6, t);
+                flag = true;
+            }
+            std::smatch mt, md;
+            bool m7 = std::regex_search(cs, m, re(7));
+            bool m10 = std::regex_search(cs, mt, re(10));
+            bool m9 = std::regex_search(cs, md, re(9));
+            if (m7) flag = two_del_ins(m, flag);
+            else if (m9) flag = three_deletions(md, flag);
+            else if (m10) flag = three_indels(mt, flag);
+            if (std::regex_search(cs, m, re(13))) flag = close_to_correct(m, flag);
+            if (std::regex_search(cs, m, re(15)) && m.str(1) != "D" && m.str(1) != "H") flag = close_to_one(m, flag);
+            if (std::regex_search(cs, m, re(16))) {
+                rep_first(16, std::to_string(I(m, 1) + I(m, 2)) + "D");
+                flag = true;
+            }
+            if (std::regex_search(cs, m, re(17))) {
+                rep_first(17, std::to_string(I(m, 1) + I(m, 2)) + "I");
+                flag = true;
+            }
+        }
+        if (std::regex_search(cs, m, re(23))) mis_ms(m);
+        else if (std::regex_search(cs, m, re(18))) mis3(m);
+        if (std::regex_search(cs, m, re(21))) dig_s_dig_m(m);
+        else if (std::regex_search(cs, m, re(20))) begin_dig_m(m);
+    }
+};
+
+string cigar_string(const vector<uint32_t> &c, int n) {  // get_cigar_string (include/VariationUtils.h:563-570)
+    string s;
+    for (int i = 0; i < n; i++) s += std::to_string(c[i] >> 4) + "MIDNSHP=XB??????"[c[i] & 15];
+    return s;
+}
+
+// cigarstr_2cigar (include/VariationUtils.h:608-629); false on a negative length
+bool parse_cigar_string(string s, vector<uint32_t> &out) {
+    out.clear();
+    while (!s.empty()) {
+        size_t po = 0;
+        int num = std::stoi(s, &po);
+        if (num < 0) return false;
+        const char *ops = "MIDNSHP=XB";
+        const char *q = strchr(ops, s[po]);
+        int op = (q && s[po]) ? (int)(q - ops) : 0;
+        out.push_back(((uint32_t)num << 4) | (uint32_t)op);
+        s = s.substr(po + 1);
+    }
+    return true;
+}
 
 // ---------------------------------------------------------------------------
 // per-read walk: CigarParser (src/parseCigar.cpp)
@@ -548,7 +941,30 @@ struct Walker {
         int mapq = r.mapq;
         int position = r.pos + 1;
         rpis = rpes = 0;
-        // (local realignment's CIGAR rewrite is not restated here)
+        if (P.local_realign) {
+            // CigarModifier (src/parseCigar.cpp:547-571): the rewritten CIGAR is
+            // written over the record's CIGAR words (and the bytes after them when
+            // it is longer); the walk reads the new count from the same address
+            if (op(cg[0]) == OP_D) throw UnsupportedRead();  // the :249 pointer shift is not restated
+            int nm_ = n_cigar;
+            if (cg[nm_ - 1] == OP_D) nm_--;                       // whole-word compare (:251)
+            if (op(cg[0]) == OP_I) cg[0] = (cg[0] & ~15u) | OP_D;  // a leading I becomes D (:253-255)
+            if (cg[nm_ - 1] == OP_I) cg[nm_ - 1] = OP_D;          // whole-word compare (:256-258)
+            CigarMod cm{R, s, q, r.lseq, position, cigar_string(cg, nm_)};
+            const string orig = cigar_string(r.cig, r.n_cigar);
+            cm.rules(idl);
+            if (cm.cs != orig) {
+                vector<uint32_t> nc;
+                bool ok = parse_cigar_string(cm.cs, nc);
+                if (!ok) parse_cigar_string(orig, nc);  // a negative length: the original CIGAR is written back
+                if (nc.size() > (size_t)r.n_cigar + 3) throw UnsupportedRead();
+                for (size_t k = 0; k < nc.size(); k++) cg[k] = nc[k];
+                if (ok) {
+                    n_cigar = (int)nc.size();
+                    position = cm.position;
+                }
+            }
+        }
         // cleanupCigar: src/parseCigar.cpp:1858-1892
         for (int pass = 0; pass < 2; pass++) {
             bool none = true;
@@ -1921,7 +2337,14 @@ int rvo_run_region(const rvo_reads *reads, const char *ref, int contig_len, cons
     Maps M;
     Ref R;
     setup_ref(R, ref, contig_len, start, end, *p);
-    run_pileup(reads, *p, start, end, contig_len, M, R);
+    try {
+        run_pileup(reads, *p, start, end, contig_len, M, R);
+    } catch (const UnsupportedRead &) {
+        const char *msg = "ERROR unsupported read (leading D or a CIGAR rewrite longer than the record allows)\n";
+        *out = strdup(msg);
+        *out_len = strlen(msg);
+        return -5;
+    }
     string o;
     if (strchr(stages, 'P')) dump_maps(o, "P", M, true);
     adjust_mnp(M, R);

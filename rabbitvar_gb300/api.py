@@ -68,7 +68,7 @@ EXPORTS = ["rv_default_params", "rv_create", "rv_destroy", "rv_last_error", "rv_
            "rv_call_regions", "rv_score_candidates", "rv_candidates", "rv_score_pair", "rv_format_somatic", "rv_call_somatic", "rv_export_maps", "rv_last_timings", "rv_stage_times", "rv_io_bytes", "rv_fisher_batch", "rv_bam_read",
            "rv_bam_contigs", "rv_bam_batch", "rv_bam_free", "rv_fasta_read", "rv_free", "rv_alloc_pinned",
            "rv_free_pinned", "rv_mlp_create", "rv_mlp_destroy", "rv_mlp_last_error", "rv_mlp_set_params",
-           "rv_mlp_get_params", "rv_mlp_train", "rv_mlp_gradients", "rv_mlp_predict"]
+           "rv_mlp_get_params", "rv_mlp_train", "rv_mlp_gradients", "rv_mlp_predict", "rv_mlp_step_ms"]
 
 _lib = None
 

@@ -8,6 +8,7 @@
 #include <climits>
 #include <cstdio>
 #include <cstring>
+#include <set>
 #include <string>
 #include <vector>
 
@@ -68,6 +69,7 @@ DevState rv_ctx::state() const {
     s.batch.base_off = d_boff;
     s.batch.seq = d_seq;
     s.batch.qual = d_qual;
+    s.batch.skip = use_skip ? d_skip : nullptr;
     s.regions = d_regions;
     s.n_regions = (int32_t)regions.size();
     s.tiles = d_tiles;
@@ -268,10 +270,6 @@ rv_status rv_create(rv_ctx **out, const rv_params *p, int device, size_t hbm_bud
     d.svminlen = p->svminlen;
     d.somatic = p->somatic;
     *out = ctx;
-    if (p->local_realign) {
-        ctx->err = "local realignment (-k 1) is not supported by this build; use local_realign = 0";
-        return RV_ERR_UNSUPPORTED;
-    }
     if (p->do_pileup) {
         ctx->err = "pileup mode (-p) is not supported by this build";
         return RV_ERR_UNSUPPORTED;
@@ -287,7 +285,7 @@ void rv_destroy(rv_ctx *ctx) {
                     ctx->d_regions, ctx->d_tiles, ctx->d_score_base, ctx->d_cellmem, ctx->d_head, ctx->d_slots,
                     ctx->d_arena, ctx->d_deferred, ctx->d_cand, ctx->d_counters, ctx->d_tmp_idx,
                     ctx->d_tmp_slots, ctx->d_tmp_cells, ctx->d_tmp_views, ctx->d_tmp_n, ctx->d_list,
-                    ctx->d_ftab, ctx->d_logfact};
+                    ctx->d_ftab, ctx->d_logfact, ctx->d_skip};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (int i = 0; i < 12; i++)
@@ -417,6 +415,56 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
     }
     ctx->n_score = score;
     ctx->n_cells = cell_base + 4;
+    // -t: RecordPreprocessor::next_record's duplicate filter
+    // (src/recordPreprocessor.cpp:152-176), in each region's read order
+    ctx->use_skip = false;
+    if (P.dedup && n > 0) {
+        std::vector<uint8_t> skip((size_t)n, 0), seen((size_t)n, 0);
+        for (const Region &R : ctx->regions) {
+            std::set<std::string> dups;
+            int first_match = 0;
+            for (int64_t r = R.r0; r < R.r1; r++) {
+                const uint32_t *c = b->cigar + b->cig_off[r];
+                int span = 0;
+                for (int k = 0; k < b->n_cigar[r]; k++) {
+                    int o = c[k] & 15;
+                    if (o == 0 || o == 2 || o == 3 || o == 7 || o == 8) span += (int)(c[k] >> 4);
+                }
+                int endpos = ((b->flag[r] & 4) || span == 0) ? b->pos[r] + 1 : b->pos[r] + span;
+                if (endpos <= R.start - 1 || b->pos[r] >= R.end) continue;
+                if ((b->flag[r] & P.samfilter) || (int)b->mapq[r] < P.min_mapq || b->l_qseq[r] == 1) continue;
+                const int a = b->pos[r] + 1, m = b->mpos[r] + 1;
+                if (a != first_match) dups.clear();
+                std::string key;
+                if (m < 10) {
+                    key = std::to_string(a) + ((b->flag[r] & 1) ? "-=-" : "-*-") + std::to_string(m);
+                } else if ((b->flag[r] & 1) && (b->flag[r] & 4)) {
+                    key = std::to_string(a) + "-";
+                    for (int k = 0; k < b->n_cigar[r]; k++) key += std::to_string(c[k] >> 4) + "MIDNSHP=XB"[c[k] & 15];
+                } else {
+                    continue;
+                }
+                uint8_t d = dups.count(key) ? 1 : 0;
+                if (!d) {
+                    dups.insert(key);
+                    first_match = a;
+                }
+                if (seen[r] && skip[r] != d) {
+                    ctx->err = "-t: a read is a duplicate in one region and not in an overlapping one";
+                    return RV_ERR_UNSUPPORTED;
+                }
+                seen[r] = 1;
+                skip[r] = d;
+            }
+        }
+        size_t cs = ctx->cap_skip;
+        if ((st = grow(ctx, ctx->d_skip, cs, (size_t)n))) return st;
+        ctx->cap_skip = cs;
+        RV_CUDA(cudaMemcpyAsync(ctx->d_skip, skip.data(), (size_t)n, cudaMemcpyHostToDevice, s));
+        RV_CUDA(cudaStreamSynchronize(s));
+        ctx->io_h2d += n;
+        ctx->use_skip = true;
+    }
     size_t creg = ctx->cap_regions, ct = ctx->cap_tiles, creg2 = ctx->cap_regions;
     if ((st = grow(ctx, ctx->d_regions, creg, ctx->regions.size() + 1)) ||
         (st = grow(ctx, ctx->d_score_base, creg2, ctx->regions.size() + 1)) ||
@@ -509,7 +557,7 @@ rv_status rv_pileup(rv_ctx *ctx, void *stream) {
     launch_init_slots(ctx->d_slots, ctx->hash_cap, s);
     DevState st = ctx->state();
     RV_CUDA(cudaEventRecord(ctx->ev[4], s));
-    launch_region_spans(st, s);
+    launch_region_spans(st, ctx->dp, s);
     launch_edge_detect(st, ctx->dp, s);
     RV_CUDA(cudaEventRecord(ctx->ev[5], s));
     // autotuner: unless RV_PILEUP_VARIANT pins one, the first batches try each
@@ -570,6 +618,11 @@ rv_status rv_pileup(rv_ctx *ctx, void *stream) {
 rv_status rv_realign(rv_ctx *ctx, void *stream) {
     if (!ctx) return RV_ERR_ARG;
     if (ctx->stage < 2) { ctx->err = "rv_realign before rv_pileup"; return RV_ERR_STATE; }
+    if (ctx->params.local_realign) {
+        ctx->err = "-k 1: the realigner's indel passes (realignIndels) are not in this build; "
+                   "rv_pileup and rv_export_maps support -k 1";
+        return RV_ERR_UNSUPPORTED;
+    }
     (void)stream;
     RV_CUDA(cudaSetDevice(ctx->device));
     rv_status st = host_realign_mnp(ctx);
@@ -636,6 +689,14 @@ rv_status rv_score_candidates(rv_ctx *ctx, int min_count) {
     if (!ctx || min_count < 1) return RV_ERR_ARG;
     if (ctx->params.somatic) { ctx->err = "rv_score_candidates scores one sample (somatic = 0)"; return RV_ERR_ARG; }
     ctx->dp.dataset_min = min_count;
+    // every covered position may keep all its alleles
+    const unsigned int want = (unsigned int)std::min<int64_t>(INT32_MAX, ctx->n_score * 6 + 1024);
+    if (want > ctx->cand_cap) {
+        if (ctx->d_cand) cudaFree(ctx->d_cand);
+        ctx->d_cand = nullptr;
+        RV_CUDA(cudaMalloc((void **)&ctx->d_cand, (size_t)want * sizeof(CandVar)));
+        ctx->cand_cap = want;
+    }
     rv_status s = score_impl(ctx, nullptr, ctx->dp);
     return s;
 }

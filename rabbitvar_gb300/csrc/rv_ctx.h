@@ -11,7 +11,7 @@ namespace rv {
 
 // kernel launchers (rv_pileup.cu, rv_score.cu)
 void launch_init_slots(Slot *slots, unsigned long long n, cudaStream_t s);
-void launch_region_spans(const DevState &st, cudaStream_t s);
+void launch_region_spans(const DevState &st, const DevParams &P, cudaStream_t s);
 cudaError_t launch_pileup(const DevState &st, const DevParams &P, int grid, cudaStream_t s, int variant);
 int pileup_variants();
 void launch_serial(const DevState &st, const DevParams &P, cudaStream_t s);
@@ -89,6 +89,9 @@ struct rv_ctx {
     uint32_t *d_cigoff = nullptr, *d_cigar = nullptr;
     uint64_t *d_boff = nullptr;
     uint8_t *d_seq = nullptr, *d_qual = nullptr;
+    uint8_t *d_skip = nullptr;  // -t duplicate flags
+    size_t cap_skip = 0;
+    bool use_skip = false;
     std::vector<int32_t> h_pos;  // positions kept for region lookup
 
     // regions / tiles

@@ -101,6 +101,7 @@ struct Batch {
     const uint32_t *cig_off, *cigar;
     const uint64_t *base_off;
     const uint8_t *seq, *qual;
+    const uint8_t *skip;    // -t: 1 = duplicate read (null when -t is off)
 };
 
 struct Hash {

@@ -218,10 +218,20 @@ __global__ void __launch_bounds__(128, 1) k_umma(const bf16 *A, int lda, const b
     }
 }
 
+// Per-step scalars of a training run, in device memory so that one captured
+// step replays for every batch: the batch index within the epoch and the
+// Adam step count.
+struct StepState {
+    int64_t batch;
+    int64_t t;
+};
+
 // Batch rows -> BF16 layer-1 input (zero padded to 64 columns) and its
-// transpose; rows past `n` are zero (their loss weight is zero).
+// transpose; rows past `n` are zero (their loss weight is zero).  The first
+// row is `b0`, or batch * B when `ss` is given.
 __global__ void k_gather(const float *feat, const int32_t *idx, int64_t n, int64_t b0, int B, bf16 *h0, bf16 *h0t,
-                         float *y_out, const float *y) {
+                         float *y_out, const float *y, const StepState *ss) {
+    if (ss) b0 = ss->batch * B;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < B * KIN; i += gridDim.x * blockDim.x) {
         const int r = i / KIN, c = i % KIN;
         const int64_t g = b0 + r;
@@ -238,7 +248,9 @@ __global__ void k_gather(const float *feat, const int32_t *idx, int64_t n, int64
 // gradient of the last hidden layer (dz3 = dlogit * w4 * GELU'(z3)) and the
 // output-layer gradients.  One thread per row.
 __global__ void k_head(const bf16 *h3, const float *z3, const float *params, int B, const float *y, float pos_weight,
-                       float inv_n, float *logit_out, bf16 *dz3, bf16 *dz3t, float *grad, float *loss) {
+                       float inv_n, float *logit_out, bf16 *dz3, bf16 *dz3t, float *grad, float *loss,
+                       const StepState *ss = nullptr, int64_t n_total = 0) {
+    if (ss) inv_n = 1.f / (float)min((int64_t)B, n_total - ss->batch * B);  // rows of this batch
     __shared__ float s_db3[H], s_dw4[H];
     for (int i = threadIdx.x; i < H; i += blockDim.x) { s_db3[i] = 0.f; s_dw4[i] = 0.f; }
     __syncthreads();
@@ -309,7 +321,12 @@ __global__ void k_cast(const float *p, bf16 *w1, bf16 *w2, bf16 *w3, bf16 *w2t, 
 
 // Adam on the FP32 master parameters; the padded input columns of W1 stay 0.
 __global__ void k_adam(float *p, const float *g, float *mo, float *ve, float lr, float b1, float b2, float eps,
-                       float c1, float c2) {
+                       float c1, float c2, const StepState *ss) {
+    if (ss) {  // bias corrections of step t (1-based)
+        const double t = (double)(ss->t + 1);
+        c1 = (float)(1.0 - pow((double)b1, t));
+        c2 = (float)(1.0 - pow((double)b2, t));
+    }
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N_PARAM; i += gridDim.x * blockDim.x) {
         if (i < OFF_B1 && (i % KIN) >= NF) continue;
         const float gi = g[i];
@@ -319,6 +336,11 @@ __global__ void k_adam(float *p, const float *g, float *mo, float *ve, float lr,
         ve[i] = v;
         p[i] -= lr * (m / c1) / (sqrtf(v / c2) + eps);
     }
+}
+
+__global__ void k_advance(StepState *ss) {
+    ss->batch += 1;
+    ss->t += 1;
 }
 
 }  // namespace
@@ -337,6 +359,11 @@ struct rv_mlp {
     int32_t *perm = nullptr;
     int64_t cap_n = 0;
     int64_t steps = 0;
+    StepState *ss = nullptr;        // device
+    cudaGraphExec_t step_graph = nullptr;
+    int64_t graph_n = -1;           // training-set size the graph was captured for
+    float graph_lr = 0, graph_pw = 0;
+    double step_ms = 0;             // mean time of a training step (last train call)
     std::string msg;
 };
 
@@ -354,12 +381,6 @@ namespace {
 template <int N, int EPI>
 cudaError_t gemm(rv_mlp *m, const bf16 *A, int lda, const bf16 *Bm, int ldb, int mtiles, int ksplit, int kper,
                  const Epi &e) {
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t x = cudaFuncSetAttribute(k_umma<N, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGemmSmem);
-        if (x != cudaSuccess) return x;
-        attr = true;
-    }
     k_umma<N, EPI><<<dim3(mtiles, ksplit), 128, kGemmSmem, m->stream>>>(A, lda, Bm, ldb, kper, e);
     return cudaGetLastError();
 }
@@ -386,13 +407,16 @@ cudaError_t forward(rv_mlp *m, int B) {
     return cudaSuccess;
 }
 
-// one training step on the gathered batch (labels in m->y, -1 = padding row)
-cudaError_t train_step(rv_mlp *m, int B, float inv_n, float pos_weight, float lr, int64_t t) {
+// one training step: gather batch `ss->batch` of the shuffled training set,
+// forward, backward, Adam; every per-step scalar is read from `ss`, so the
+// launch sequence is the same for every step (it is captured once)
+cudaError_t train_step(rv_mlp *m, int B, int64_t n, float pos_weight, float lr) {
+    k_gather<<<256, 256, 0, m->stream>>>(m->feat, m->perm, n, 0, B, m->h0, m->h0t, m->y, m->labels, m->ss);
     cudaError_t x = forward(m, B);
     if (x != cudaSuccess) return x;
     cudaMemsetAsync(m->grad, 0, N_PARAM * sizeof(float), m->stream);
-    k_head<<<B / 128, 128, 0, m->stream>>>(m->h[2], m->z[2], m->params, B, m->y, pos_weight, inv_n, m->logit,
-                                           m->dz[2], m->dzt[2], m->grad, m->loss);
+    k_head<<<B / 128, 128, 0, m->stream>>>(m->h[2], m->z[2], m->params, B, m->y, pos_weight, 1.f, m->logit,
+                                           m->dz[2], m->dzt[2], m->grad, m->loss, m->ss, n);
     // weight gradients: dW_l = dz_l^T * h_{l-1}, K = batch, split in chunks of 512 rows
     const int kper = std::min(B, 512), ks = B / kper;
     const bf16 *hprev_t[3] = {m->h0t, m->ht[0], m->ht[1]};
@@ -419,10 +443,23 @@ cudaError_t train_step(rv_mlp *m, int B, float inv_n, float pos_weight, float lr
         if (x != cudaSuccess) return x;
     }
     const float b1 = 0.9f, b2 = 0.999f;
-    const float c1 = 1.f - (float)std::pow((double)b1, (double)t), c2 = 1.f - (float)std::pow((double)b2, (double)t);
-    k_adam<<<(N_PARAM + 255) / 256, 256, 0, m->stream>>>(m->params, m->grad, m->mo, m->ve, lr, b1, b2, 1e-8f, c1, c2);
+    k_adam<<<(N_PARAM + 255) / 256, 256, 0, m->stream>>>(m->params, m->grad, m->mo, m->ve, lr, b1, b2, 1e-8f, 1.f,
+                                                         1.f, m->ss);
     k_cast<<<64, 256, 0, m->stream>>>(m->params, m->w1, m->w2, m->w3, m->w2t, m->w3t);
+    k_advance<<<1, 1, 0, m->stream>>>(m->ss);
     return cudaGetLastError();
+}
+
+// the GEMM kernels' shared-memory size is set once, outside any capture
+cudaError_t gemm_attrs() {
+    cudaError_t x = cudaFuncSetAttribute(k_umma<H, EPI_FWD>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGemmSmem);
+    if (x == cudaSuccess)
+        x = cudaFuncSetAttribute(k_umma<H, EPI_DH>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGemmSmem);
+    if (x == cudaSuccess)
+        x = cudaFuncSetAttribute(k_umma<H, EPI_DW>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGemmSmem);
+    if (x == cudaSuccess)
+        x = cudaFuncSetAttribute(k_umma<KIN, EPI_DW>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGemmSmem);
+    return x;
 }
 
 rv_status check_err(rv_mlp *m) {
@@ -488,6 +525,9 @@ rv_status rv_mlp_create(rv_mlp **out, int device, int batch, uint64_t seed) {
     MCUDA(cudaMalloc((void **)&m->loss, sizeof(float)));
     MCUDA(cudaMalloc((void **)&m->err, sizeof(unsigned int)));
     MCUDA(cudaMemset(m->err, 0, sizeof(unsigned int)));
+    MCUDA(cudaMalloc((void **)&m->ss, sizeof(StepState)));
+    MCUDA(cudaMemset(m->ss, 0, sizeof(StepState)));
+    MCUDA(gemm_attrs());
     // He-normal hidden weights, zero biases (host generator, fixed seed)
     std::vector<float> p(N_PARAM, 0.f);
     std::mt19937_64 rng(seed);
@@ -511,9 +551,10 @@ void rv_mlp_destroy(rv_mlp *m) {
     void *ptrs[] = {m->params, m->grad, m->mo, m->ve, m->w1, m->w2, m->w3, m->w2t, m->w3t, m->h0, m->h0t,
                     m->h[0], m->h[1], m->h[2], m->ht[0], m->ht[1], m->ht[2], m->dz[0], m->dz[1], m->dz[2],
                     m->dzt[0], m->dzt[1], m->dzt[2], m->z[0], m->z[1], m->z[2], m->y, m->logit, m->loss,
-                    m->err, m->feat, m->labels, m->perm};
+                    m->err, m->feat, m->labels, m->perm, m->ss};
     for (void *p : ptrs)
         if (p) cudaFree(p);
+    if (m->step_graph) cudaGraphExecDestroy(m->step_graph);
     if (m->stream) cudaStreamDestroy(m->stream);
     delete m;
 }
@@ -550,7 +591,7 @@ rv_status rv_mlp_gradients(rv_mlp *m, const float *features, const float *labels
     MCUDA(cudaMemcpyAsync(m->labels, labels, (size_t)n * sizeof(float), cudaMemcpyHostToDevice, m->stream));
     MCUDA(cudaMemsetAsync(m->loss, 0, sizeof(float), m->stream));
     const int B = m->B;
-    k_gather<<<256, 256, 0, m->stream>>>(m->feat, nullptr, n, 0, B, m->h0, m->h0t, m->y, m->labels);
+    k_gather<<<256, 256, 0, m->stream>>>(m->feat, nullptr, n, 0, B, m->h0, m->h0t, m->y, m->labels, nullptr);
     MCUDA(forward(m, B));
     MCUDA(cudaMemsetAsync(m->grad, 0, N_PARAM * sizeof(float), m->stream));
     // the same sequence as a training step, without the optimizer
@@ -592,26 +633,65 @@ rv_status rv_mlp_train(rv_mlp *m, const float *features, const float *labels, in
     MCUDA(cudaMemcpyAsync(m->feat, features, (size_t)n * NF * sizeof(float), cudaMemcpyHostToDevice, m->stream));
     MCUDA(cudaMemcpyAsync(m->labels, labels, (size_t)n * sizeof(float), cudaMemcpyHostToDevice, m->stream));
     const int B = m->B;
+    // one step captured as a graph (re-captured when the set size or the
+    // hyper-parameters change), replayed once per batch
+    if (!m->step_graph || m->graph_n != n || m->graph_lr != lr || m->graph_pw != pos_weight) {
+        if (m->step_graph) cudaGraphExecDestroy(m->step_graph);
+        m->step_graph = nullptr;
+        cudaGraph_t g = nullptr;
+        MCUDA(cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal));
+        cudaError_t x = train_step(m, B, n, pos_weight, lr);
+        cudaError_t y = cudaStreamEndCapture(m->stream, &g);
+        if (x != cudaSuccess || y != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            m->msg = std::string("step capture: ") + cudaGetErrorString(x != cudaSuccess ? x : y);
+            return RV_ERR_CUDA;
+        }
+        x = cudaGraphInstantiate(&m->step_graph, g, 0);
+        cudaGraphDestroy(g);
+        if (x != cudaSuccess) { m->msg = cudaGetErrorString(x); return RV_ERR_CUDA; }
+        m->graph_n = n;
+        m->graph_lr = lr;
+        m->graph_pw = pos_weight;
+    }
     std::vector<int32_t> perm((size_t)n);
     std::mt19937_64 rng(seed);
+    cudaEvent_t e0, e1;
+    MCUDA(cudaEventCreate(&e0));
+    MCUDA(cudaEventCreate(&e1));
+    int64_t total_steps = 0;
+    float total_ms = 0;
     for (int ep = 0; ep < epochs; ep++) {
         for (int64_t i = 0; i < n; i++) perm[i] = (int32_t)i;
         for (int64_t i = n - 1; i > 0; i--) std::swap(perm[i], perm[rng() % (uint64_t)(i + 1)]);
         MCUDA(cudaMemcpyAsync(m->perm, perm.data(), (size_t)n * sizeof(int32_t), cudaMemcpyHostToDevice,
                               m->stream));
         MCUDA(cudaMemsetAsync(m->loss, 0, sizeof(float), m->stream));
+        // batch index back to 0; the Adam step count carries on
+        MCUDA(cudaMemsetAsync(&m->ss->batch, 0, sizeof(int64_t), m->stream));
         int64_t nb = (n + B - 1) / B;
-        for (int64_t b = 0; b < nb; b++) {
-            const int64_t rows = std::min<int64_t>(B, n - b * B);
-            k_gather<<<256, 256, 0, m->stream>>>(m->feat, m->perm, n, b * B, B, m->h0, m->h0t, m->y, m->labels);
-            m->steps++;
-            MCUDA(train_step(m, B, 1.f / (float)rows, pos_weight, lr, m->steps));
-        }
+        MCUDA(cudaEventRecord(e0, m->stream));
+        for (int64_t b = 0; b < nb; b++) MCUDA(cudaGraphLaunch(m->step_graph, m->stream));
+        MCUDA(cudaEventRecord(e1, m->stream));
+        m->steps += nb;
         if ((s = check_err(m))) return s;
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        total_ms += ms;
+        total_steps += nb;
         float l = 0;
         MCUDA(cudaMemcpy(&l, m->loss, sizeof(float), cudaMemcpyDeviceToHost));
         if (epoch_loss) epoch_loss[ep] = l / (float)nb;
     }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    m->step_ms = total_steps ? total_ms / total_steps : 0;
+    return RV_OK;
+}
+
+rv_status rv_mlp_step_ms(const rv_mlp *m, double *ms) {
+    if (!m || !ms) return RV_ERR_ARG;
+    *ms = m->step_ms;
     return RV_OK;
 }
 
@@ -626,7 +706,7 @@ rv_status rv_mlp_predict(rv_mlp *m, const float *features, int64_t n, float *sco
     std::vector<float> out((size_t)B);
     for (int64_t b0 = 0; b0 < n; b0 += B) {
         const int64_t rows = std::min<int64_t>(B, n - b0);
-        k_gather<<<256, 256, 0, m->stream>>>(m->feat, nullptr, n, b0, B, m->h0, m->h0t, nullptr, nullptr);
+        k_gather<<<256, 256, 0, m->stream>>>(m->feat, nullptr, n, b0, B, m->h0, m->h0t, nullptr, nullptr, nullptr);
         MCUDA(forward(m, B));
         k_head<<<B / 128, 128, 0, m->stream>>>(m->h[2], m->z[2], m->params, B, nullptr, 1.f, 0.f, m->logit, nullptr,
                                                nullptr, nullptr, nullptr);

@@ -400,33 +400,38 @@ __device__ bool read_passes(const Batch &B, const DevParams &P, const Region &R,
     if (flag & P.samfilter) return false;
     if ((int)B.mapq[r] < P.min_mapq) return false;
     if (B.l_qseq[r] == 1) return false;
+    if (B.skip && B.skip[r]) return false;
     return true;
 }
 
 // read span incl. soft clips, used for tile windows
-__device__ void read_span(const Batch &B, int64_t r, int &lo, int &hi) {
+// With -k 1 (`widen`) the CIGAR rewrite can turn insertions into soft clips
+// that reach further out: the span grows by the read's inserted bases.
+__device__ void read_span(const Batch &B, int64_t r, int &lo, int &hi, bool widen = false) {
     const uint32_t *c = B.cigar + B.cig_off[r];
-    int n = B.n_cigar[r], span = 0;
+    int n = B.n_cigar[r], span = 0, ins = 0;
     int clip5 = 0, clip3 = 0;
     for (int k = 0; k < n; k++) {
         uint32_t w = __ldg(c + k);
         int o = cig_op(w);
         if (o == 0 || o == 2 || o == 3 || o == 7 || o == 8) span += cig_len(w);
+        if (o == 1) ins += cig_len(w);
     }
+    if (!widen) ins = 0;
     if (n > 0) {
         uint32_t w0 = __ldg(c), w1 = __ldg(c + n - 1);
         if (cig_op(w0) == 4 || cig_op(w0) == 1) clip5 = cig_len(w0);
         if (cig_op(w1) == 4 || cig_op(w1) == 1) clip3 = cig_len(w1);
     }
     int pos1 = B.pos[r] + 1;
-    lo = pos1 - clip5 - 1;
-    hi = pos1 + span + clip3;
+    lo = pos1 - clip5 - 1 - ins;
+    hi = pos1 + span + clip3 + ins;
 }
 
 // ---------------------------------------------------------------------------
 // kernels
 // ---------------------------------------------------------------------------
-__global__ void k_region_spans(DevState st) {
+__global__ void k_region_spans(DevState st, DevParams P) {
     int reg = blockIdx.x;
     if (reg >= st.n_regions) return;
     Region &R = st.regions[reg];
@@ -436,7 +441,7 @@ __global__ void k_region_spans(DevState st) {
     int mylo = INT32_MAX, myhi = INT32_MIN;
     for (int64_t r = R.r0 + threadIdx.x; r < R.r1; r += blockDim.x) {
         int a, b;
-        read_span(st.batch, r, a, b);
+        read_span(st.batch, r, a, b, P.local_realign != 0);
         // a 5' clip of a read at the contig start reaches below position 1,
         // where there is no reference base and so no cell is touched
         mylo = min(mylo, max(a, 1));
@@ -474,7 +479,7 @@ __global__ void __launch_bounds__(kPileupThreads, MINB) k_pileup_tiles(DevState 
         const Region &R = st.regions[tile.region];
         for (int64_t r = tile.r0 + threadIdx.x; r < tile.r1; r += blockDim.x) {
             int a, b;
-            read_span(st.batch, r, a, b);
+            read_span(st.batch, r, a, b, P.local_realign != 0);
             if (!is_edge(R, b)) atomicMin(&s_wlo, a);
         }
         for (int i = threadIdx.x; i < 4 * 4 * TW; i += blockDim.x) w0[i] = 0u;
@@ -494,7 +499,7 @@ __global__ void __launch_bounds__(kPileupThreads, MINB) k_pileup_tiles(DevState 
                 if (!read_passes(st.batch, P, R, r)) continue;
                 if (R.serial) {
                     int a, b;
-                    read_span(st.batch, r, a, b);
+                    read_span(st.batch, r, a, b, P.local_realign != 0);
                     if (is_edge(R, b)) continue;
                 }
                 w.walk(st.batch, r);
@@ -554,7 +559,7 @@ __global__ void k_edge_detect(DevState st, DevParams P) {
     for (int64_t r = lo + threadIdx.x; r < R.r1; r += blockDim.x) {
         if (!read_passes(st.batch, P, R, r)) continue;
         int a, b;
-        read_span(st.batch, r, a, b);
+        read_span(st.batch, r, a, b, P.local_realign != 0);
         if (!is_edge(R, b)) continue;
         w.walk(st.batch, r);
     }
@@ -591,7 +596,7 @@ __global__ void k_pileup_serial(DevState st, DevParams P) {
     for (int64_t r = lo; r < R.r1; r++) {
         if (!read_passes(st.batch, P, R, r)) continue;
         int a, b;
-        read_span(st.batch, r, a, b);
+        read_span(st.batch, r, a, b, P.local_realign != 0);
         if (!is_edge(R, b)) continue;
         if (b - (st.batch.pos[r] + 1) > kEdgeGuard) { sink.error(ERR_UNSUPPORTED); continue; }
         w.walk(st.batch, r);
@@ -618,7 +623,7 @@ __global__ void k_resolve_deferred(DevState st, DevParams P, int max_probe_reads
         int probes = 0;
         for (int64_t r = d.read - 1; !ps.found && r >= R.r0; r--) {
             int a, b;
-            read_span(st.batch, r, a, b);
+            read_span(st.batch, r, a, b, P.local_realign != 0);
             // reads are coordinate-sorted: stop once no earlier read can reach pos
             if (st.batch.pos[r] + 1 + 4 * 1024 < d.pos) break;
             if (a > d.pos || b < d.pos) continue;
@@ -639,8 +644,8 @@ void launch_init_slots(Slot *slots, unsigned long long n, cudaStream_t s) {
     k_init_slots<<<592, 256, 0, s>>>(slots, n);
 }
 
-void launch_region_spans(const DevState &st, cudaStream_t s) {
-    if (st.n_regions > 0) k_region_spans<<<st.n_regions, 256, 0, s>>>(st);
+void launch_region_spans(const DevState &st, const DevParams &P, cudaStream_t s) {
+    if (st.n_regions > 0) k_region_spans<<<st.n_regions, 256, 0, s>>>(st, P);
 }
 
 size_t pileup_smem_bytes() { return (size_t)kTileW * 4 * 4 * 4; }

@@ -5,6 +5,7 @@
 // key).  One thread walks one read.
 #pragma once
 #include "rv_internal.h"
+#include "rv_cigar.cuh"
 
 namespace rv {
 
@@ -128,15 +129,71 @@ struct Walker {
     bool m_dir;
     int m_mapq, m_nom, m_rlen, m_tlen;
     KeyBuf key;
+    // -k 1: the rewritten CIGAR (written over the record's first words), and
+    // the record's own word count
+    uint32_t mod_w[kCigTok];
+    int mod_n;
 
     __device__ Walker(const DevParams &p, Sink &s, const Region &r, const char *rf, int rl)
         : P(p), S(s), R(r), ref(rf), ref_len(rl) {}
 
+    // record memory word k: the rewritten words first, then the record's own
+    // words and the bytes after them
+    __device__ uint32_t mem(int k) const {
+        if (k < mod_n) return mod_w[k];
+        return k < rv.n_cigar ? __ldg(rv.cig + k) : rv.word(k);
+    }
     __device__ uint32_t W(int k) const {
-        if (k >= n_cigar) return rv.word(k);
-        uint32_t w = __ldg(rv.cig + k);
+        if (k >= n_cigar) return mem(k);
+        uint32_t w = mem(k);
         if ((w & 15u) == 1u && (k < lead_end || k > trail_start)) w = (w & ~15u) | 4u;
         return w;
+    }
+    // reference, bases and qualities as CigarEdit reads them
+    struct EditAcc {
+        const Walker *w;
+        __device__ bool has(int p) const { return w->has(p); }
+        __device__ char at(int p) const { return w->at(p); }
+        __device__ char base(int i) const { return i >= 0 && i < w->rv.lseq ? w->rv.base(i) : (char)0; }
+        __device__ int q(int i) const { return w->rv.q(i); }
+        __device__ int lseq() const { return w->rv.lseq; }
+    };
+    // CigarModifier (src/parseCigar.cpp:547-571); false when the read is not supported
+    __device__ __noinline__ bool rewrite_cigar(int idl, int &position) {
+        const int n0 = rv.n_cigar;
+        if (n0 > kCigTok || cig_op(__ldg(rv.cig)) == 2) return false;  // the leading-D pointer shift (:249)
+        EditAcc acc{this};
+        CigarEdit<EditAcc> ce{acc, CigTok(), position};
+        CigTok orig;
+        orig.n = 0;
+        orig.bad = false;
+        int nm = n0;
+        if (__ldg(rv.cig + n0 - 1) == 2u) nm--;  // whole-word compare (:251)
+        ce.t.n = 0;
+        ce.t.bad = false;
+        for (int k = 0; k < n0; k++) {
+            const uint32_t w = __ldg(rv.cig + k);
+            orig.len[k] = cig_len(w);
+            orig.op[k] = op_char(w);
+            if (orig.op[k] == '?') return false;
+        }
+        orig.n = n0;
+        for (int k = 0; k < nm; k++) {
+            uint32_t w = __ldg(rv.cig + k);
+            if (k == 0 && cig_op(w) == 1) w = (w & ~15u) | 2u;  // a leading I becomes D (:253-255)
+            if (k == nm - 1 && w == 1u) w = 2u;                 // whole-word compare (:256-258)
+            ce.t.len[k] = cig_len(w);
+            ce.t.op[k] = op_char(w);
+        }
+        ce.t.n = nm;
+        ce.run(idl);
+        if (ce.t.bad) return false;
+        if (ce.t.eq(orig)) return true;
+        for (int k = 0; k < ce.t.n; k++) mod_w[k] = ((uint32_t)ce.t.len[k] << 4) | op_code(ce.t.op[k]);
+        mod_n = ce.t.n;
+        n_cigar = ce.t.n;
+        position = ce.position;
+        return true;
     }
     __device__ int cop(int k) const { return cig_op(W(k)); }
     __device__ int clen(int k) const { return cig_len(W(k)); }
@@ -674,21 +731,13 @@ struct Walker {
         rv.lseq = B.l_qseq[r];
         rv.n_cigar = B.n_cigar[r];
         n_cigar = rv.n_cigar;
+        mod_n = 0;
         if (n_cigar <= 0) return;
-        lead_end = n_cigar;
-        trail_start = -1;
-        for (int k = 0; k < n_cigar; k++) {
-            int o = cig_op(__ldg(rv.cig + k));
-            if (o == 0 || o == 7 || o == 8) {
-                if (lead_end == n_cigar) lead_end = k;
-                trail_start = k;
-            }
-        }
         int flag = B.flag[r];
         int idl = 0;
         for (int i = 0; i < n_cigar; i++) {
-            int o = cig_op(__ldg(rv.cig + i));  // original ops (before cleanup)
-            if (o == 1 || o == 2) idl += clen(i);
+            const uint32_t w = __ldg(rv.cig + i);  // original ops (before cleanup)
+            if (cig_op(w) == 1 || cig_op(w) == 2) idl += cig_len(w);
         }
         int nmtag = B.nm[r];
         int nom = 0;
@@ -702,6 +751,20 @@ struct Walker {
         int mapq = B.mapq[r];
         int position = B.pos[r] + 1;
         rpis = rpes = 0;
+        if (P.local_realign && !rewrite_cigar(idl, position)) {
+            S.error(ERR_UNSUPPORTED);
+            return;
+        }
+        // cleanupCigar (src/parseCigar.cpp:1858-1892), applied on read by W()
+        lead_end = n_cigar;
+        trail_start = -1;
+        for (int k = 0; k < n_cigar; k++) {
+            int o = cig_op(mem(k));
+            if (o == 0 || o == 7 || o == 8) {
+                if (lead_end == n_cigar) lead_end = k;
+                trail_start = k;
+            }
+        }
         start = position;
         offset = 0;
         if (cop(0) == 4 && clen(0) >= 10 && cop(n_cigar - 1) == 4 && clen(n_cigar - 1) >= 10) return;
@@ -710,7 +773,11 @@ struct Walker {
             int o = cop(i);
             if (o == 0 || o == 1) rlen += clen(i);
             if (o == 0 || o == 1 || o == 4) tlen += clen(i);
-            if (o == 0 || o == 2 || o == 3 || o == 7 || o == 8) orig_ref_len += clen(i);
+        }
+        // the record's end (bam_endpos): its own word count over the words now in memory
+        for (int i = 0; i < rv.n_cigar; i++) {
+            int o = cig_op(mem(i));
+            if (o == 0 || o == 2 || o == 3 || o == 7 || o == 8) orig_ref_len += cig_len(mem(i));
         }
         if (P.minmatch != 0 && rlen < P.minmatch) return;
         S.max_len(tlen);

@@ -33,6 +33,7 @@ def _lib():
         L.rv_mlp_train.argtypes = [vp, vp, vp, i64, C.c_int, C.c_float, C.c_float, C.c_uint64, vp]
         L.rv_mlp_gradients.argtypes = [vp, vp, vp, i64, C.c_float, vp, f32p]
         L.rv_mlp_predict.argtypes = [vp, vp, i64, vp]
+        L.rv_mlp_step_ms.argtypes = [vp, C.POINTER(C.c_double)]
         _bound = True
     return L
 
@@ -98,6 +99,11 @@ class Mlp:
         self._check(self.L.rv_mlp_train(self.h, x.ctypes.data, y.ctypes.data, x.shape[0], epochs, lr, pos_weight,
                                         seed, losses.ctypes.data))
         return losses
+
+    def step_ms(self) -> float:
+        v = C.c_double()
+        self._check(self.L.rv_mlp_step_ms(self.h, C.byref(v)))
+        return v.value
 
     def predict(self, x: np.ndarray) -> np.ndarray:
         x = np.ascontiguousarray(x, np.float32)

@@ -86,7 +86,13 @@ class ReadSet:
 
 def subset(rs: ReadSet, keep: np.ndarray) -> ReadSet:
     """The reads of `rs` where `keep` is true, in the same order and layout."""
-    idx = np.nonzero(keep)[0]
+    return take(rs, np.nonzero(keep)[0])
+
+
+def take(rs: ReadSet, idx: np.ndarray) -> ReadSet:
+    """The reads rs[idx] (indices may repeat: exact duplicate records), in
+    the order of `idx`, in the same layout."""
+    idx = np.asarray(idx, dtype=np.int64)
     n = idx.shape[0]
     n_cigar = rs.n_cigar[idx]
     cig_off = np.zeros(n, dtype=np.uint32)

@@ -56,7 +56,22 @@ def case_unique_fisher():
     return g, rs, (1_501, 4_500), ["-k", "0", "-u", "--fisher"]
 
 
-CASES = {"germline_dense": case_germline_dense, "contig_end": case_contig_end, "unique_fisher": case_unique_fisher}
+def case_dedup():
+    # reads starting in 2000..4000 get mate position 4 (so -t considers them)
+    # and two exact copies each
+    g, _, rs = synth.dense_multi(seed=0x5EED00D2, length=8_000)
+    idx = []
+    for i in range(rs.n):
+        idx.append(i)
+        if 2000 <= rs.pos[i] < 4000:
+            idx += [i, i]
+    rs2 = synth.take(rs, np.array(idx))
+    rs2.mpos[(rs2.pos >= 2000) & (rs2.pos < 4000)] = 4
+    return g, rs2, (1_801, 4_200), ["-k", "0", "-t"]
+
+
+CASES = {"germline_dense": case_germline_dense, "contig_end": case_contig_end, "unique_fisher": case_unique_fisher,
+         "dedup": case_dedup}
 
 
 # somatic mode (`-b 'T.bam|N.bam' -N 'T|N'`): records only

@@ -126,3 +126,59 @@ def test_somatic_depth_tiles():
     n, ora_text = O.run_regions(rs, g, regions, params=O.default_params(local_realign=0, fisher=1), threads=4)
     assert n > 30
     assert diff_records(ora_text.splitlines(), text.splitlines(), rel=1e-9) == []
+
+
+def test_dedup_duplicate_reads():
+    """-t: reads whose mate starts within the first 9 bases are deduplicated
+    by (start, mate contig, mate start), in each region's read order
+    (RecordPreprocessor::next_record).  Here every read starting in
+    2000..4000 gets mate position 4 and two exact copies."""
+    import numpy as np
+    import oracle as O
+    from rabbitvar_gb300 import synth
+    g, vs, rs = synth.dense_multi(seed=0x5EED00D2, length=8_000)
+    idx = []
+    for i in range(rs.n):
+        idx.append(i)
+        if 2000 <= rs.pos[i] < 4000:
+            idx += [i, i]
+    rs2 = synth.take(rs, np.array(idx))
+    sel = (rs2.pos >= 2000) & (rs2.pos < 4000)
+    rs2.mpos[sel] = 4
+    regions = [(1, 2000), (2001, 4000), (4001, 8000)]
+    api, ctx = _gpu_ctx(dedup=1)
+    _, _, text = _run_gpu(ctx, api, rs2, g, regions)
+    n, ora_text = O.run_regions(rs2, g, regions, params=O.default_params(local_realign=0, dedup=1))
+    assert n > 10
+    assert diff_records(ora_text.splitlines(), text.splitlines()) == []
+    # without -t the copies count three times
+    n2, ora2 = O.run_regions(rs2, g, regions, params=O.default_params(local_realign=0))
+    assert ora2 != ora_text
+    api2, ctx2 = _gpu_ctx()
+    _, _, text2 = _run_gpu(ctx2, api2, rs2, g, regions)
+    assert diff_records(ora2.splitlines(), text2.splitlines()) == []
+
+
+@pytest.mark.parametrize("case", ["germline", "dense"])
+def test_local_realign_cigar_rewrite_maps(case, germline_small):
+    """-k 1: the device CIGAR rewrite (CigarModifier) and the -k 1 branches of
+    the walk give the same maps after the pileup (P) as the oracle, which
+    matches the reference's own -k 1 maps."""
+    import oracle as O
+    from rabbitvar_gb300 import synth
+    if case == "germline":
+        g, vs, rs = germline_small
+        regions = [(1, 100000)]
+    else:
+        g, vs, rs = synth.dense_multi()
+        regions = [(1 + 6000 * i, 6000 * (i + 1)) for i in range(10)]
+    api, ctx = _gpu_ctx(local_realign=1)
+    ctx.upload_reference(rs.contig, _genome_bytes(g))
+    ctx.submit(api.Batch.from_readset(rs), regions)
+    ctx.pileup()
+    prm = O.default_params(local_realign=1)
+    for i in range(len(regions)) if len(regions) < 4 else (0, 4, 9):
+        ora = O.run_region(rs, g, regions[i][0], regions[i][1], stages="P", params=prm)
+        assert diff_dump(ora, ctx.export_maps(i, "P"), P_TAGS, rel=1e-9) == [], f"region {i}"
+    with pytest.raises(api.RvError):
+        ctx.realign()

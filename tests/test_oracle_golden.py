@@ -29,6 +29,8 @@ def _params(flags):
     kw = {"local_realign": 0}
     if "-u" in flags:
         kw["unique_fwd"] = 1
+    if "-t" in flags:
+        kw["dedup"] = 1
     if "--fisher" in flags:
         kw["fisher"] = 1
     return O.default_params(**kw)
