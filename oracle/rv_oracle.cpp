@@ -1370,6 +1370,712 @@ void adjust_mnp(Maps &M, Ref &R) {
 }
 
 // ---------------------------------------------------------------------------
+// -k 1 indel realignment: VariationRealigner::realignIndels
+// (src/VariationRealigner.cpp:467-1360) with its helpers (:1396-1990)
+// ---------------------------------------------------------------------------
+struct RefFail {};
+
+string join_ref(Ref &R, int from, int to) {  // joinRef: include/VariationUtils.h:356-362 (.at throws)
+    string s;
+    for (int i = from; i <= to; i++) {
+        if (!R.has(i)) throw RefFail();
+        s += R.at(i);
+    }
+    return s;
+}
+
+void replace_first(string &s, const string &a, const string &b) {
+    size_t p = s.find(a);
+    if (p != string::npos) s.replace(p, a.size(), b);
+}
+
+struct OutOfRange {};  // std::out_of_range from string::substr (caught per candidate)
+
+string vsub(const string &s, int idx) {  // vc_substr(str, idx): include/util.h:27-34
+    // `str.length() + idx < 0` is an unsigned comparison there: too negative
+    // an index wraps and substr throws
+    size_t b = idx >= 0 ? (size_t)idx : s.size() + (size_t)(long long)idx;
+    if (b > s.size()) throw OutOfRange();
+    return s.substr(b);
+}
+string vsub(const string &s, int begin, int len) {  // vc_substr(str, begin, len): include/util.h:44-57
+    if (begin < 0) begin = (int)(s.size() + (size_t)(long long)begin);
+    if (len > 0) {
+        if ((size_t)(long long)begin > s.size()) throw OutOfRange();
+        return s.substr((size_t)(long long)begin, (size_t)len);
+    }
+    if (len == 0) return string();
+    len = (int)(s.size() + (size_t)(long long)len - (size_t)(long long)begin);
+    if (len < 0) return string();
+    if ((size_t)(long long)begin > s.size()) throw OutOfRange();
+    return s.substr((size_t)(long long)begin, (size_t)len);
+}
+char char_at(const string &s, int i) {  // charAt: include/util.h:171-179
+    if (i < 0) {
+        int k = (int)s.size() + i;
+        return k < 0 ? (char)-1 : s[k];
+    }
+    return s[i];
+}
+string strip_hash_caret(const string &s) {  // regex_replace(s, "#|\\^", "")
+    string o;
+    for (char c : s)
+        if (c != '#' && c != '^') o += c;
+    return o;
+}
+
+void adj_cnt3(Stat &to, Stat &v, Stat *ref) {  // adjCnt(varToAdd, variant, referenceVar): include/VariationUtils.h:291-317
+    adj_cnt(to, v);
+    if (!ref) return;
+    ref->cnt -= v.cnt;
+    ref->hi -= v.hi;
+    ref->lo -= v.lo;
+    ref->pmean -= v.pmean;
+    ref->qmean -= v.qmean;
+    ref->mq -= v.mq;
+    ref->nm -= v.nm;
+    ref->rev -= v.rev;
+    ref->fwd -= v.fwd;
+    // correctCnt: include/VariationUtils.h:263-280
+    if (ref->cnt < 0) ref->cnt = 0;
+    if (ref->hi < 0) ref->hi = 0;
+    if (ref->lo < 0) ref->lo = 0;
+    if (ref->pmean < 0) ref->pmean = 0;
+    if (ref->qmean < 0) ref->qmean = 0;
+    if (ref->mq < 0) ref->mq = 0;
+    if (ref->rev < 0) ref->rev = 0;
+    if (ref->fwd < 0) ref->fwd = 0;
+}
+void correct_cnt(Stat &r) {
+    if (r.cnt < 0) r.cnt = 0;
+    if (r.hi < 0) r.hi = 0;
+    if (r.lo < 0) r.lo = 0;
+    if (r.pmean < 0) r.pmean = 0;
+    if (r.qmean < 0) r.qmean = 0;
+    if (r.mq < 0) r.mq = 0;
+    if (r.rev < 0) r.rev = 0;
+    if (r.fwd < 0) r.fwd = 0;
+}
+
+struct Mism { string seq; int pos; int end; };
+struct MmResult { vector<Mism> mm; vector<int> scp; int nm = 0, misp = 0; string misnt; };
+
+struct Realigner {
+    Maps &M;
+    Ref &R;
+    const rvo_params &P;
+    const rvo_reads *rd;
+    int rs, re, chr_len;
+    int max_rl;
+
+    static Stat *maybe(map<int, KeyMap> &h, int p, char base) {  // getVariationMaybe: include/VariationUtils.h:218-239
+        if (base == 0) return nullptr;
+        auto it = h.find(p);
+        if (it == h.end()) return nullptr;
+        auto j = it->second.find(string(1, base));
+        return j == it->second.end() ? nullptr : &j->second;
+    }
+    bool has_key(int p, const string &k) {
+        auto it = M.nonins.find(p);
+        return it != M.nonins.end() && it->second.count(k);
+    }
+
+    // findMM5 (:1857-1916)
+    MmResult find_mm5(Ref &RR, int position, const string &wupseq) {
+        string seq = strip_hash_caret(wupseq);
+        MmResult r;
+        int n = 0, mcnt = 0;
+        string str;
+        while (RR.has_ne(char_at(seq, -1 - n), position - n) && mcnt < 3) {
+            str.insert(0, 1, char_at(seq, -1 - n));
+            r.mm.push_back({str, position - n, 5});
+            n++;
+            mcnt++;
+        }
+        r.scp.push_back(position + 1);
+        if (str.size() == 1) {
+            while (RR.has_eq(char_at(seq, -1 - n), position - n)) {
+                n++;
+                if (n != 0) r.nm++;
+            }
+            if (r.nm > 1) {
+                // the second scan's condition (-1 - n - 1 - n2 >= 0) never holds
+                r.scp.push_back(position - n);
+                auto it = M.sc5.find(position - n);
+                if (it != M.sc5.end()) it->second.used = true;
+            }
+        }
+        return r;
+    }
+    // findMM3 (:1919-1984)
+    MmResult find_mm3(Ref &RR, int p, const string &sanpseq) {
+        string seq = strip_hash_caret(sanpseq);
+        MmResult r;
+        int n = 0, mcnt = 0, len = (int)seq.size();
+        string str;
+        while (n < len && RR.has(p + n) && RR.at(p + n) == seq[n]) n++;
+        r.scp.push_back(p + n);
+        const int Tbp = p + n;
+        while (mcnt <= 3 && n < len && RR.idx(p + n) != seq[n]) {
+            str += seq[n];
+            r.mm.push_back({str, Tbp, 3});
+            n++;
+            mcnt++;
+        }
+        if (str.size() == 1) {
+            while (n < len && RR.has_eq(seq[n], p + n)) {
+                n++;
+                if (n != 0) r.nm++;
+            }
+            if (r.nm > 1) {
+                int n2 = 0;
+                while (n + n2 + 1 < len && RR.has_eq(seq[n + n2 + 1], p + n + 1 + n2)) n2++;
+                if (n2 > 2 && n + n2 + 1 < len) {
+                    r.scp.push_back(p + n + n2);
+                    r.misp = p + n;
+                    r.misnt = string(1, seq[n]);
+                    auto it = M.sc3.find(p + n + n2);
+                    if (it != M.sc3.end()) it->second.used = true;
+                    r.nm += n2;
+                } else {
+                    r.scp.push_back(p + n);
+                    auto it = M.sc3.find(p + n);
+                    if (it != M.sc3.end()) it->second.used = true;
+                }
+            }
+        }
+        return r;
+    }
+    // ismatch (:1507-1546), MM = 3
+    static bool ismatch(const string &seq1, const string &seq2_in, int dir) {
+        string seq2 = strip_hash_caret(seq2_in);
+        int mm = 0;
+        for (int n = 0; n < (int)seq1.size() && n < (int)seq2.size(); n++)
+            if (seq1[n] != vsub(seq2, dir * n - (dir == -1 ? 1 : 0), 1)[0]) mm++;
+        return mm <= 3 && mm / (double)seq1.size() < 0.15;
+    }
+    // adjRefCnt (:1753-1787)
+    static void adj_ref_cnt(Stat &tv, Stat *ref, int len) {
+        if (!ref) return;
+        double f = tv.pmean != 0 ? (tv.pmean / (double)tv.cnt - len + 1) / (tv.pmean / (double)tv.cnt) : 0;
+        if (f < 0) return;
+        if (f > 1) f = 1;
+        ref->cnt -= (int)(f * tv.cnt);
+        ref->hi -= (int)(f * tv.hi);
+        ref->lo -= (int)(f * tv.lo);
+        ref->pmean -= f * tv.pmean;
+        ref->qmean -= f * tv.qmean;
+        ref->mq -= f * tv.mq;
+        ref->nm -= f * tv.nm;
+        ref->rev -= (int)(f * tv.rev);
+        ref->fwd -= (int)(f * tv.fwd);
+        correct_cnt(*ref);
+    }
+    // adjRefFactor (:1794-1822)
+    static void adj_ref_factor(Stat *ref, double f) {
+        if (!ref) return;
+        if (f > 1) f = 1;
+        if (f < -1) return;
+        int old = ref->cnt;
+        ref->cnt -= (int)(f * ref->cnt);
+        ref->hi -= (int)(f * ref->hi);
+        ref->lo -= (int)(f * ref->lo);
+        double fc = old != 0 ? std::abs(ref->cnt - old) / (double)old : 1;
+        ref->pmean -= ref->pmean * f * fc;
+        ref->qmean -= ref->qmean * f * fc;
+        ref->mq -= ref->mq * f * fc;
+        ref->nm -= f * ref->nm;
+        ref->fwd -= (int)(f * ref->fwd);
+        ref->rev -= (int)(f * ref->rev);
+        correct_cnt(*ref);
+    }
+    // noPassingReads (:1447-1505): raw records over chr:start-end, no filters
+    bool no_passing_reads(int start, int end) {
+        int cnt = 0;
+        const uint32_t dlenqr = ((uint32_t)(end - start) << 4) | 2u;
+        int64_t lo = 0, hi = rd->n;
+        while (lo < hi) {
+            int64_t mid = (lo + hi) / 2;
+            if (rd->pos[mid] < start - 1 - 4096) lo = mid + 1; else hi = mid;
+        }
+        for (int64_t i = lo; i < rd->n && rd->pos[i] < end; i++) {
+            const uint32_t *c = rd->cigar + rd->cig_off[i];
+            int span = 0, aligned = 0;
+            bool has_d = false;
+            for (int k = 0; k < rd->n_cigar[i]; k++) {
+                int o = c[k] & 15;
+                if (o == 0 || o == 2 || o == 3 || o == 7 || o == 8) span += c[k] >> 4;
+                if (o == 0 || o == 2) aligned += c[k] >> 4;
+                if (c[k] == dlenqr) has_d = true;
+            }
+            int endpos = ((rd->flag[i] & 4) || span == 0) ? rd->pos[i] + 1 : rd->pos[i] + span;
+            if (endpos <= start - 1) continue;
+            if (has_d) continue;
+            int rs0 = rd->pos[i] + 1, reE = rs0 + aligned;
+            if (reE > end + 2 && rs0 < start - 2) cnt++;
+        }
+        return cnt <= 0;
+    }
+
+    struct Cand { int pos; string key; int cnt; };
+    static vector<Cand> sorted(const map<int, map<string, int>> &ch) {  // fillAndSortTmp + CMP_tmp (:44-58, :1362-1386)
+        vector<Cand> t;
+        for (auto &pe : ch)
+            for (auto &ke : pe.second) t.push_back({pe.first, ke.first, ke.second});
+        std::sort(t.begin(), t.end(), [](const Cand &a, const Cand &b) {
+            if (a.cnt != b.cnt) return a.cnt > b.cnt;
+            if (a.pos != b.pos) return a.pos < b.pos;
+            return a.key.compare(b.key) > 0;
+        });
+        return t;
+    }
+    static bool rx(const string &s, const char *pat, std::smatch &m) {
+        return std::regex_search(s, m, std::regex(pat));
+    }
+
+    // realigndel (:489-775)
+    void realigndel(bool with_bams, map<int, map<string, int>> dcnt_map) {
+        vector<Cand> tmp = sorted(dcnt_map);
+        for (const Cand &tpl : tmp) {
+            try {
+                const int p = tpl.pos;
+                const string &vn = tpl.key;
+                const int dcnt = tpl.cnt;
+                Stat &vref = M.nonins[p][vn];
+                int dellen = 0;
+                std::smatch m;
+                if (rx(vn, "^-(\\d+).*", m)) dellen = atoi(m.str(1).c_str());
+                if (rx(vn, "\\^(\\d+)$", m)) dellen += atoi(m.str(1).c_str());
+                string extrains, extra, inv5, inv3;
+                if (rx(vn, "^-\\d+\\^([ATGNC]+)<...\\d+>([ATGNC]+)$", m)) {
+                    inv5 = m.str(1);
+                    inv3 = m.str(2);
+                } else if (rx(vn, "^-\\d+(.*)", m)) {
+                    for (char c : m.str(1))
+                        if (c != '^' && c != '&' && c != '#') extra += c;
+                    if (rx(vn, "\\^([ATGNC]+)", m)) extrains = m.str(1);
+                }
+                const int wustart = p - 200 > 1 ? p - 200 : 1;
+                string wupseq = join_ref(R, wustart, p - 1) + extra;
+                if (!inv3.empty()) wupseq = inv3;
+                const int sanend = p + 200 > chr_len ? chr_len : p + 200;
+                const int off = dellen + (int)extra.size() - (int)extrains.size();
+                string sanpseq = extra + join_ref(R, p + off, sanend);
+                if (!inv5.empty()) sanpseq = inv5;
+                MmResult r3 = find_mm3(R, p, sanpseq);
+                MmResult r5 = find_mm5(R, p + off - 1, wupseq);
+                vector<Mism> mmm = r3.mm;
+                mmm.insert(mmm.end(), r5.mm.begin(), r5.mm.end());
+                for (Mism &mi : mmm) {
+                    string mm = mi.seq;
+                    if (mm.size() > 1) mm.insert(1, 1, '&');
+                    const int mp = mi.pos, me = mi.end;
+                    if (!has_key(mp, mm)) continue;
+                    Stat &tv = M.nonins[mp][mm];
+                    if (tv.cnt == 0) continue;
+                    if (tv.qmean / tv.cnt < P.goodq) continue;
+                    if (tv.pmean / tv.cnt > (me == 3 ? r3.nm + 4 : r5.nm + 4)) continue;
+                    if (tv.cnt >= dcnt + dellen || tv.cnt / dcnt >= 8) continue;
+                    if (mp > p && me == 5) {
+                        double f = tv.pmean != 0 ? (mp - p) / (tv.pmean / (double)tv.cnt) : 1;
+                        if (f > 1) f = 1;
+                        M.cov[p] += (int)(tv.cnt * f);
+                        adj_ref_cnt(tv, maybe(M.nonins, p, R.idx(p)), dellen);
+                    }
+                    if (mp > p && me == 3 && M.nonins.count(p) && M.nonins[p].count(string(1, R.idx(p)))) {
+                        Stat *lref = &M.nonins[p][string(1, R.idx(p))];
+                        adj_cnt3(vref, tv, lref);
+                    } else {
+                        adj_cnt(vref, tv);
+                    }
+                    M.nonins[mp].erase(mm);
+                    if (M.nonins[mp].empty()) M.nonins.erase(mp);
+                }
+                if (r3.misp != 0 && r3.mm.size() == 1 && has_key(r3.misp, r3.misnt) &&
+                    M.nonins[r3.misp][r3.misnt].cnt < dcnt)
+                    M.nonins[r3.misp].erase(r3.misnt);
+                if (r5.misp != 0 && r5.mm.size() == 1 && has_key(r5.misp, r5.misnt) &&
+                    M.nonins[r5.misp][r5.misnt].cnt < dcnt)
+                    M.nonins[r5.misp].erase(r5.misnt);
+                for (int sc5pp : r5.scp) {
+                    auto it = M.sc5.find(sc5pp);
+                    if (it == M.sc5.end() || it->second.used) continue;
+                    Clip &tv = it->second;
+                    string seq = consensus(tv);
+                    if (dcnt <= 2 && tv.cnt / dcnt > 5) continue;
+                    if (seq != " " && ismatch(seq, wupseq, -1)) {
+                        if (sc5pp > p) M.cov[p] += tv.cnt;
+                        adj_cnt(vref, tv);
+                        tv.used = true;
+                    }
+                }
+                for (int sc3pp : r3.scp) {
+                    auto it = M.sc3.find(sc3pp);
+                    if (it == M.sc3.end() || it->second.used) continue;
+                    Clip &tv = it->second;
+                    string seq = consensus(tv);
+                    if (dcnt <= 2 && tv.cnt / dcnt > 5) continue;
+                    if (seq != " " && ismatch(seq, vsub(sanpseq, sc3pp - p), 1)) {
+                        if (sc3pp <= p) M.cov[p] += tv.cnt;
+                        Stat *lref = sc3pp <= p ? nullptr : maybe(M.nonins, p, R.idx(p));
+                        adj_cnt3(vref, tv, lref);
+                        tv.used = true;
+                    }
+                }
+                const int pe = p + off;
+                Stat *h = maybe(M.nonins, p, R.idx(p));
+                if (with_bams && pe - p >= 5 && pe - p < max_rl - 10 && h && h->cnt != 0 &&
+                    vref.cnt > 2 * h->cnt * (1 - (pe - p) / (double)max_rl) && no_passing_reads(p, pe))
+                    adj_cnt3(vref, *h, h);
+            } catch (const RefFail &) {
+            } catch (const OutOfRange &) {
+            }
+        }
+        for (int i = (int)tmp.size() - 1; i > 0; i--) {
+            const int p = tmp[i].pos;
+            const string &vn = tmp[i].key;
+            if (!has_key(p, vn)) continue;
+            Stat &vref = M.nonins[p][vn];
+            std::smatch m;
+            if (rx(vn, "(-\\d+)&[ATGC]+$", m)) {
+                string tn = m.str(1);
+                if (M.nonins[p].count(tn)) {
+                    Stat &tref = M.nonins[p][tn];
+                    if (vref.cnt < tref.cnt) {
+                        adj_cnt(tref, vref);
+                        M.nonins[p].erase(vn);
+                    }
+                }
+            }
+        }
+    }
+
+    // realignins (:785-1114)
+    void realignins(map<int, map<string, int>> &icnt_map) {
+        vector<Cand> tmp = sorted(icnt_map);
+        for (const Cand &tpl : tmp) {
+            try {
+                const int position = tpl.pos;
+                const string &vn = tpl.key;
+                const int icnt = tpl.cnt;
+                std::smatch m;
+                string insert1;
+                if (rx(vn, "^\\+([ATGC]+).*", m)) insert1 = m.str(1);
+                else continue;
+                string ins3;
+                int inslen = (int)insert1.size();
+                if (rx(vn, "<dup(\\d+)>([ATGC]+)$", m)) {
+                    ins3 = m.str(2);
+                    inslen += atoi(m.str(1).c_str()) + (int)ins3.size();
+                }
+                string extra, compm;
+                if (rx(vn, ".*&([ATGC]+).*", m)) extra = m.str(1);
+                if (rx(vn, "#([ATGC]+).*", m)) compm = m.str(1);
+                int newdel = 0;
+                if (rx(vn, "\\^(\\d+)$", m)) newdel = atoi(m.str(1).c_str());
+                string tn = vn;
+                if (!tn.empty() && tn[0] == '+') tn.erase(0, 1);
+                replace_first(tn, "&", "");
+                replace_first(tn, "#", "");
+                tn = std::regex_replace(tn, std::regex("\\^\\d+$"), "", std::regex_constants::format_first_only);
+                tn = std::regex_replace(tn, std::regex("\\^"), "", std::regex_constants::format_first_only);
+                const int wustart = position - 150 > 1 ? position - 150 : 1;
+                string wupseq = join_ref(R, wustart, position) + tn;
+                int sanend = position + (int)vn.size() + 100;
+                if (chr_len < sanend) sanend = chr_len;
+                string sanpseq;
+                MmResult r3;
+                if (!ins3.empty()) {
+                    int p3 = position + inslen - (int)ins3.size() + 50;
+                    if ((int)ins3.size() > 50) sanpseq = vsub(ins3, 50 - (int)ins3.size());
+                    sanpseq += join_ref(R, position + 1, position + 101);
+                    r3 = find_mm3(R, p3 + 1, sanpseq);
+                } else {
+                    sanpseq = tn + join_ref(R, position + (int)extra.size() + 1 + (int)compm.size() + newdel, sanend);
+                    r3 = find_mm3(R, position + 1, sanpseq);
+                }
+                MmResult r5 = find_mm5(R, position + (int)extra.size() + (int)compm.size() + newdel, wupseq);
+                vector<Mism> mmm = r3.mm;
+                mmm.insert(mmm.end(), r5.mm.begin(), r5.mm.end());
+                Stat &vref = M.ins[position][vn];
+                for (Mism &mi : mmm) {
+                    string mb = mi.seq;
+                    if (mb.size() > 1) mb = string(1, mb[0]) + "&" + mb.substr(1);
+                    const int mp = mi.pos, me = mi.end;
+                    if (!has_key(mp, mb)) continue;
+                    Stat &var = M.nonins[mp][mb];
+                    if (var.cnt == 0) continue;
+                    if (var.qmean / var.cnt < P.goodq) continue;
+                    if (var.pmean / var.cnt > (me == 3 ? r3.nm + 4 : r5.nm + 4)) continue;
+                    if (var.cnt >= icnt + (int)insert1.size() || var.cnt / icnt >= 8) continue;
+                    if (mp > position && me == 5) M.cov[position] += var.cnt;
+                    if (mp > position && me == 3 && M.nonins.count(position) && R.has(position) &&
+                        M.nonins[position].count(string(1, R.idx(position)))) {
+                        Stat *lref = &M.nonins[position][string(1, R.idx(position))];
+                        adj_cnt3(vref, var, lref);
+                    } else {
+                        adj_cnt(vref, var);
+                    }
+                    M.nonins[mp].erase(mb);
+                    if (M.nonins[mp].empty()) M.nonins.erase(mp);
+                }
+                if (r3.misp != 0 && r3.mm.size() == 1 && has_key(r3.misp, r3.misnt) &&
+                    M.nonins[r3.misp][r3.misnt].cnt < icnt)
+                    M.nonins[r3.misp].erase(r3.misnt);
+                if (r5.misp != 0 && r5.mm.size() == 1 && has_key(r5.misp, r5.misnt) &&
+                    M.nonins[r5.misp][r5.misnt].cnt < icnt)
+                    M.nonins[r5.misp].erase(r5.misnt);
+                for (int sc5pp : r5.scp) {
+                    auto it = M.sc5.find(sc5pp);
+                    if (it == M.sc5.end()) continue;
+                    Clip &tv = it->second;
+                    if (tv.used) continue;
+                    string seq = consensus(tv);
+                    if (seq != " " && ismatch(seq, wupseq, -1)) {
+                        if (sc5pp > position) M.cov[position] += tv.cnt;
+                        adj_cnt(vref, tv);
+                        tv.used = true;
+                    }
+                }
+                for (int sc3pp : r3.scp) {
+                    auto it = M.sc3.find(sc3pp);
+                    if (it == M.sc3.end()) continue;
+                    Clip &tv = it->second;
+                    if (tv.used) continue;
+                    string seq = consensus(tv);
+                    string mseq = !ins3.empty() ? sanpseq : vsub(sanpseq, sc3pp - position - 1);
+                    if (seq != " " && ismatch(seq, mseq, 1)) {
+                        if (sc3pp <= position || (int)insert1.size() > tv.pmean / tv.cnt) M.cov[position] += tv.cnt;
+                        Stat *lref = nullptr;
+                        if (sc3pp > position && M.nonins.count(position) && R.has(position) &&
+                            M.nonins[position].count(string(1, R.idx(position))))
+                            lref = &M.nonins[position][string(1, R.idx(position))];
+                        if ((int)insert1.size() > tv.pmean / tv.cnt) lref = nullptr;
+                        adj_cnt3(vref, tv, lref);
+                        tv.used = true;
+                        if (insert1.size() + 1 == vn.size() && (int)insert1.size() > max_rl &&
+                            sc3pp >= position + 1 + (int)insert1.size()) {
+                            int flag = 0;
+                            int offset = (sc3pp - position - 1) % (int)insert1.size();
+                            string tvn = vn;
+                            for (int si = 0; si < (int)seq.size() && si + offset < (int)insert1.size(); si++) {
+                                if (vsub(seq, si, 1) != vsub(insert1, si + offset, 1)) {
+                                    flag++;
+                                    int shift = si + offset + 1;
+                                    tvn = tvn.substr(0, shift) + vsub(seq, si, 1) + tvn.substr(shift + 1);
+                                }
+                            }
+                            if (flag > 0) {
+                                Stat moved = M.ins[position][vn];
+                                M.ins[position][tvn] = moved;
+                                M.ins[position].erase(vn);
+                            }
+                        }
+                    }
+                }
+                if (!r3.scp.empty() && !r5.scp.empty()) {
+                    int first3 = r3.scp[0], first5 = r5.scp[0];
+                    if (first3 > first5 + 3 && first3 - first5 < max_rl * 0.75) {
+                        if (R.has(position) && M.nonins.count(position) &&
+                            M.nonins[position].count(string(1, R.idx(position))))
+                            adj_ref_factor(&M.nonins[position].at(string(1, R.idx(position))),
+                                           (first3 - first5 - 1) / (double)max_rl);
+                        adj_ref_factor(&vref, -(first3 - first5 - 1) / (double)max_rl);
+                    }
+                }
+            } catch (const RefFail &) {
+            } catch (const OutOfRange &) {
+            }
+        }
+        for (int i = (int)tmp.size() - 1; i > 0; i--) {
+            const int p = tmp[i].pos;
+            const string &vn = tmp[i].key;
+            auto it = M.ins.find(p);
+            if (it == M.ins.end() || !it->second.count(vn)) continue;
+            Stat &vref = it->second.at(vn);
+            std::smatch m;
+            if (rx(vn, "(\\+[ATGC]+)&[ATGC]+$", m)) {
+                string tn = m.str(1);
+                if (it->second.count(tn)) {
+                    Stat &tref = it->second.at(tn);
+                    if (vref.cnt < tref.cnt) {
+                        adj_cnt3(tref, vref, maybe(M.nonins, p, R.idx(p)));
+                        it->second.erase(vn);
+                    }
+                }
+            }
+        }
+    }
+
+    // find35match (:1396-1428)
+    static void find35(const string &s5, const string &s3, int &b5, int &b3, int &score) {
+        b5 = b3 = score = 0;
+        for (int i = 0; i < (int)s5.size() - 8; i++) {
+            for (int j = 1; j < (int)s3.size() - 8; j++) {
+                int nm = 0, n = 0;
+                while (n + j <= (int)s3.size() && i + n <= (int)s5.size()) {
+                    if (vsub(s3, -j - n, 1) != vsub(s5, i + n, 1)) nm++;
+                    if (nm > 2) break;
+                    n++;
+                }
+                if (n - nm > score && n - nm > 8 && nm / (double)n < 0.1 &&
+                    (n + j >= (int)s3.size() || i + n >= (int)s5.size())) {
+                    b5 = i;
+                    b3 = j;
+                    score = n - nm;
+                    return;
+                }
+            }
+        }
+    }
+
+    // realignlgins30 (:1119-1350); its reference map is a copy (operator[]
+    // entries stay local), the nested realignins/realigndel use the shared one
+    void realignlgins30() {
+        Ref RL = R;
+        struct T { int pos; Clip *c; int cnt; };
+        vector<T> t5, t3;
+        for (auto &e : M.sc5)
+            if (!(e.first < rs - 5000 || e.first > re + 5000)) t5.push_back({e.first, &e.second, e.second.cnt});
+        for (auto &e : M.sc3)
+            if (!(e.first < rs - 5000 || e.first > re + 5000)) t3.push_back({e.first, &e.second, e.second.cnt});
+        auto cmp3 = [](const T &a, const T &b) { return a.cnt != b.cnt ? a.cnt > b.cnt : a.pos < b.pos; };
+        std::sort(t5.begin(), t5.end(), cmp3);
+        std::sort(t3.begin(), t3.end(), cmp3);
+        for (T &a : t5) {
+            const int p5 = a.pos;
+            Clip &sc5v = *a.c;
+            const int cnt5 = a.cnt;
+            if (sc5v.used) continue;
+            string seq5 = consensus(sc5v);
+            if (seq5.size() <= 10) continue;
+            for (T &b : t3) {
+                try {
+                    const int p3 = b.pos;
+                    Clip &sc3v = *b.c;
+                    const int cnt3 = b.cnt;
+                    if (sc5v.used) break;
+                    if (sc3v.used) continue;
+                    if (p5 - p3 > max_rl * 2.5) continue;
+                    if (p3 - p5 > max_rl - 10) continue;
+                    string seq3 = consensus(sc3v);
+                    if (seq3.size() <= 10) continue;
+                    if (!(cnt5 / (double)cnt3 >= 0.08 && cnt5 / (double)cnt3 <= 12)) continue;
+                    int bp5, bp3, score;
+                    find35(seq5, seq3, bp5, bp3, score);
+                    if (score == 0) continue;
+                    const int sm = score / 2;
+                    string ins = bp3 + sm > 1 ? vsub(seq3, 0, -(bp3 + sm) + 1) : seq3;
+                    if (bp5 + sm > 0) {
+                        string tt = seq5.substr(0, bp5 + sm);
+                        std::reverse(tt.begin(), tt.end());
+                        ins += tt;
+                    }
+                    if (low_complexity(ins)) continue;
+                    int bi = 0;
+                    Stat *vref;
+                    const int il = (int)ins.size();
+                    if ((int)seq3.size() > il &&
+                        !ismatch(seq3.substr(il), join_ref(RL, p5, p5 + (int)seq3.size() - il + 2), 1))
+                        continue;
+                    if ((int)seq5.size() > il &&
+                        !ismatch(seq5.substr(il), join_ref(RL, p3 - ((int)seq5.size() - il) - 2, p3 - 1), -1))
+                        continue;
+                    if (p5 > p3) {
+                        string tmp = join_ref(RL, p3, p5 - 1);
+                        if (tmp.size() > ins.size()) {
+                            ins = std::to_string(p3 - p5) + "^" + ins;
+                            bi = p3;
+                            vref = &M.nonins[p3][ins];
+                        } else if (tmp.size() < ins.size()) {
+                            ins = vsub(ins, 0, (int)ins.size() - (int)tmp.size()) + "&" + vsub(ins, p3 - p5);
+                            ins = "+" + ins;
+                            bi = p3 - 1;
+                            vref = &M.ins[bi][ins];
+                        } else {
+                            ins = "-" + std::to_string(ins.size()) + "^" + ins;
+                            bi = p3;
+                            vref = &M.nonins[p3][ins];
+                        }
+                    } else {
+                        string tmp;
+                        if ((int)ins.size() <= p3 - p5) {
+                            int rpt = 2, tnr = 3;
+                            const int tot = p3 - p5 + (int)ins.size();
+                            while ((tot / (double)tnr) / (double)ins.size() > 1) {
+                                if (tot % tnr == 0) rpt++;
+                                tnr++;
+                            }
+                            const double to = p5 + tot / (double)rpt - ins.size();
+                            for (int i = p5; i < to; i++) {  // joinRef_double: include/VariationUtils.h:343-349
+                                if (!RL.has(i)) throw RefFail();
+                                tmp += RL.at(i);
+                            }
+                            ins = "+" + tmp + ins;
+                        } else {
+                            tmp += join_ref(RL, p5, p3 - 1);
+                            if ((ins.size() - tmp.size()) % 2 == 0) {
+                                int tex = (int)(ins.size() - tmp.size()) / 2;
+                                ins = (tmp + vsub(ins, 0, tex)) == vsub(ins, tex) ? "+" + vsub(ins, tex) : "+" + tmp + ins;
+                            } else {
+                                ins = "+" + tmp + ins;
+                            }
+                        }
+                        bi = p5 - 1;
+                        vref = &M.ins[bi][ins];
+                    }
+                    sc3v.used = true;
+                    sc5v.used = true;
+                    vref->pstd = true;
+                    vref->qstd = true;
+                    M.cov[bi] += sc5v.cnt;
+                    if (ins[0] == '+') {
+                        Stat *mvref = maybe(M.nonins, bi, RL.idx(bi));
+                        adj_cnt3(*vref, sc3v, mvref);
+                        adj_cnt(*vref, sc5v);
+                        if (p3 - p5 >= 5 && p3 - p5 < max_rl - 10 && mvref && mvref->cnt != 0 &&
+                            vref->cnt > 2 * mvref->cnt && no_passing_reads(p5, p3))
+                            adj_cnt3(*vref, *mvref, mvref);
+                        map<int, map<string, int>> tins;
+                        tins[bi][ins] = vref->cnt;
+                        realignins(tins);
+                    } else if (ins[0] == '-') {
+                        adj_cnt3(*vref, sc3v, maybe(M.nonins, bi, RL.idx(bi)));
+                        adj_cnt(*vref, sc5v);
+                        map<int, map<string, int>> tdel;
+                        tdel[bi][ins] = vref->cnt;
+                        realigndel(false, tdel);
+                    } else {
+                        adj_cnt(*vref, sc3v);
+                        adj_cnt(*vref, sc5v);
+                    }
+                    break;
+                } catch (const RefFail &) {
+                } catch (const OutOfRange &) {
+                }
+            }
+        }
+    }
+
+    // realignIndels (:467-482)
+    void run() {
+        realigndel(true, M.delcnt);
+        realignins(M.inscnt);
+        realignlgins30();
+    }
+};
+
+// VariationRealigner::process (src/VariationRealigner.cpp:135-161): adjustMNP
+// always, the indel passes with -k 1
+void realign(Maps &M, Ref &R, const rvo_params &P, const rvo_reads *rd, int rs, int re, int chr_len) {
+    adjust_mnp(M, R);
+    if (P.local_realign) {
+        Realigner rl{M, R, P, rd, rs, re, chr_len, M.max_read_len};
+        rl.run();
+    }
+}
+
+// ---------------------------------------------------------------------------
 // scoring: ToVarsBuilder (src/ToVarsBuilder.cpp) and Variant (include/Variant.h)
 // ---------------------------------------------------------------------------
 struct Var {
@@ -1405,16 +2111,6 @@ int strand_bias(int f, int r, const rvo_params &P) {  // include/VariationUtils.
             r >= P.min_bias_reads) ? 2 : 1;
 }
 
-struct RefFail {};
-
-string join_ref(Ref &R, int from, int to) {  // joinRef: include/VariationUtils.h:356-362 (.at throws)
-    string s;
-    for (int i = from; i <= to; i++) {
-        if (!R.has(i)) throw RefFail();
-        s += R.at(i);
-    }
-    return s;
-}
 
 struct Msi { double msi; int shift3; string msint; };
 
@@ -1443,10 +2139,6 @@ Msi find_msi(const string &t1, const string &t2, const string &left) {
     return {msicnt, shift3, maxmsi};
 }
 
-void replace_first(string &s, const string &a, const string &b) {
-    size_t p = s.find(a);
-    if (p != string::npos) s.replace(p, a.size(), b);
-}
 
 bool starts_with(const string &s, const char *p) { return s.compare(0, strlen(p), p) == 0; }
 
@@ -2347,7 +3039,7 @@ int rvo_run_region(const rvo_reads *reads, const char *ref, int contig_len, cons
     }
     string o;
     if (strchr(stages, 'P')) dump_maps(o, "P", M, true);
-    adjust_mnp(M, R);
+    realign(M, R, *p, reads, start, end, contig_len);
     if (strchr(stages, 'R')) dump_maps(o, "R", M, false);
     Scorer sc(*p, M, R, contig_len, start, end);
     sc.run();
@@ -2371,7 +3063,7 @@ long rvo_run_regions(const rvo_reads *reads, const char *ref, int contig_len, co
         Ref R;
         setup_ref(R, ref, contig_len, starts[i], ends[i], *p);
         run_pileup(reads, *p, starts[i], ends[i], contig_len, M, R);
-        adjust_mnp(M, R);
+        realign(M, R, *p, reads, starts[i], ends[i], contig_len);
         Scorer sc(*p, M, R, contig_len, starts[i], ends[i]);
         sc.run();
         cnt[i] = emit_simple(per[i], sc, sample, chr, chr, *p);
@@ -2396,11 +3088,11 @@ static long somatic_region(const rvo_reads *tumor, const rvo_reads *normal, cons
     Ref R;
     setup_ref(R, ref, contig_len, start, end, P);
     run_pileup(tumor, P, start, end, contig_len, MT, R);
-    adjust_mnp(MT, R);
+    realign(MT, R, P, tumor, start, end, contig_len);
     Scorer st(P, MT, R, contig_len, start, end, true);
     st.run();
     run_pileup(normal, P, start, end, contig_len, MN, R);
-    adjust_mnp(MN, R);
+    realign(MN, R, P, normal, start, end, contig_len);
     Scorer sn(P, MN, R, contig_len, start, end, true);
     sn.run();
     if (strchr(stages, 'V')) {

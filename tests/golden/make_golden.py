@@ -70,8 +70,28 @@ def case_dedup():
     return g, rs2, (1_801, 4_200), ["-k", "0", "-t"]
 
 
+def case_germline_dense_k1():
+    # local realignment (-k 1, the reference's default): CIGAR rewrite and indel realigner
+    g, rs, region, _ = case_germline_dense()
+    return g, rs, region, ["-k", "1"]
+
+
 CASES = {"germline_dense": case_germline_dense, "contig_end": case_contig_end, "unique_fisher": case_unique_fisher,
-         "dedup": case_dedup}
+         "dedup": case_dedup, "germline_dense_k1": case_germline_dense_k1}
+
+
+# records only
+def case_contig_end_k1():
+    g, rs, region, _ = case_contig_end()
+    return g, rs, region, ["-k", "1"]
+
+
+def case_dense_multi_k1():
+    g, _, rs = synth.dense_multi()
+    return g, rs, (1, 30_000), ["-k", "1", "--fisher"]
+
+
+RECORDS_ONLY = {"contig_end_k1": case_contig_end_k1, "dense_multi_k1": case_dense_multi_k1}
 
 
 # somatic mode (`-b 'T.bam|N.bam' -N 'T|N'`): records only
@@ -85,7 +105,12 @@ def case_somatic_sub():
     return g, t, n, (8_001, 20_000), ["-k", "0"]
 
 
-SOMATIC = {"somatic_mix": case_somatic_mix, "somatic_sub": case_somatic_sub}
+def case_somatic_mix_k1():
+    g, _, t, n = synth.somatic_mix(0x5EED0051)
+    return g, t, n, (1, g.shape[0]), ["-k", "1", "--fisher"]
+
+
+SOMATIC = {"somatic_mix": case_somatic_mix, "somatic_sub": case_somatic_sub, "somatic_mix_k1": case_somatic_mix_k1}
 
 
 def readset_fingerprint(rs) -> str:
@@ -118,6 +143,19 @@ def main():
             f.write("\n".join(sorted(recs)) + "\n")
         meta[name] = {"region": [a, b], "flags": flags, "reads": rs.n, "fingerprint": readset_fingerprint(rs),
                       "records": len(recs)}
+        print(name, rs.n, "reads", len(recs), "records")
+    for name, fn in RECORDS_ONLY.items():
+        g, rs, (a, b), flags = fn()
+        with tempfile.TemporaryDirectory() as td:
+            bam = os.path.join(td, "s.bam")
+            fa = os.path.join(td, "ref.fa")
+            synth.write_bam(bam, rs)
+            synth.write_fasta(fa, rs.contig, g)
+            recs = O.reference_records(fa, bam, f"{rs.contig}:{a}-{b}", os.path.join(td, "out.txt"), flags)
+        with open(os.path.join(HERE, f"{name}.records.txt"), "w") as f:
+            f.write("\n".join(sorted(recs)) + "\n")
+        meta[name] = {"records_only": True, "region": [a, b], "flags": flags, "reads": rs.n,
+                      "fingerprint": readset_fingerprint(rs), "records": len(recs)}
         print(name, rs.n, "reads", len(recs), "records")
     for name, fn in SOMATIC.items():
         g, t, n, (a, b), flags = fn()

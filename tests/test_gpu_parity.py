@@ -18,7 +18,8 @@ R_TAGS = ["RN", "RI", "RC"]
 
 def _gpu_ctx(**kw):
     from rabbitvar_gb300 import api
-    return api, api.Context(api.default_params(local_realign=0, **kw))
+    kw.setdefault("local_realign", 0)
+    return api, api.Context(api.default_params(**kw))
 
 
 def _genome_bytes(g):

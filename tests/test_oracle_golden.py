@@ -17,7 +17,8 @@ from cmp import diff_dump, diff_records
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLD = os.path.join(HERE, "golden")
 META = json.load(open(os.path.join(GOLD, "golden.json")))
-SINGLE = sorted(k for k, v in META.items() if not v.get("somatic"))
+SINGLE = sorted(k for k, v in META.items() if not v.get("somatic") and not v.get("records_only"))
+RECORDS_ONLY = sorted(k for k, v in META.items() if v.get("records_only"))
 SOMATIC = sorted(k for k, v in META.items() if v.get("somatic"))
 
 P_TAGS = ["P_ML", "PN", "PI", "PC", "PS5", "PS3", "PCI", "PCD", "PMN"]
@@ -26,7 +27,7 @@ R_TAGS = ["RN", "RI", "RC"]
 
 def _params(flags):
     import oracle as O
-    kw = {"local_realign": 0}
+    kw = {"local_realign": int(flags[flags.index("-k") + 1]) if "-k" in flags else 1}
     if "-u" in flags:
         kw["unique_fwd"] = 1
     if "-t" in flags:
@@ -99,3 +100,15 @@ def test_oracle_somatic_matches_reference_golden(name):
         labels = {r.split("\t")[53] for r in recs}
         assert labels >= {"StrongSomatic", "LikelySomatic", "Germline", "AFDiff", "LikelyLOH", "StrongLOH",
                           "SampleSpecific"}
+
+
+@pytest.mark.parametrize("name", RECORDS_ONLY)
+def test_oracle_records_match_reference_golden(name):
+    import oracle as O
+    mg = _make_golden()
+    g, rs, (a, b), flags = mg.RECORDS_ONLY[name]()
+    assert mg.readset_fingerprint(rs) == META[name]["fingerprint"], "synthetic generator drifted: rerun make_golden.py"
+    recs = open(os.path.join(GOLD, f"{name}.records.txt")).read().splitlines()
+    ora = O.run_region(rs, g, a, b, stages="O", params=_params(flags))
+    assert len(recs) == META[name]["records"] > 5
+    assert diff_records(recs, ora.splitlines(), rel=0) == []
