@@ -135,6 +135,9 @@ WORKLOAD = ("somatic mode (-b 'T|N' -N 'T|N' --fisher -f 0.01 -k 0): synthetic 1
             "tumor 200x + normal 100x 2x150, 100 x 10 kb BED tiles")
 METRIC = "reads/s pileup+var scoring (somatic pair 1 Mb, T200x+N100x)"
 CPU_TILES = 40   # CPU sample: 40 of the 100 tiles (~0.8 M reads, ~10 s on one core)
+# DRAM bytes (read + write) of one tumor-sample k_pileup_tiles launch of this
+# workload, from one ncu capture (profiles/k_pileup_tiles_somatic1mb.md)
+PILEUP_TRAFFIC = 841.1e6
 
 
 def cpu_baseline_run(g, tumor, normal, regions, threads: int, n_regions: int):
@@ -178,6 +181,66 @@ def learned_filter_leg():
     return res
 
 
+def run_panel(args):
+    """Batched amplicon panel (the 10,000-region shape, scaled to N regions):
+    region lengths U(100, 2000), depth log-normal median 500x, amplicon
+    reads with 0.5% exact duplicates, -t -u, simple mode.  Batched: all
+    regions in one submit and one persistent pileup launch; region by
+    region: one submit + pipeline per region (the reference's per-region
+    stage sequence).  Both through the C ABI from pinned host batches."""
+    import numpy as np
+    from rabbitvar_gb300 import api, synth
+    n_reg = args.panel
+    g, _, rs, regions = synth.amplicon_panel(n_regions=n_reg, genome_len=n_reg * 5000)
+    params = api.default_params(local_realign=0, dedup=1, unique_fwd=1)
+    ctx = api.Context(params)
+    ctx.upload_reference(rs.contig, synth.genome_str(g).encode())
+    batch = api.Batch.from_readset(rs, pinned=True)
+    span = rs.pos.astype(np.int64) + 150
+    subs = []
+    for a, b in regions:
+        idx = np.nonzero((rs.pos < b) & (span > a - 1 - 200))[0]
+        subs.append(api.Batch.from_readset(synth.take(rs, idx), pinned=True))
+
+    def batched():
+        ctx.submit(batch, regions)
+        ctx.pileup()
+        ctx.realign()
+        ctx.score()
+        return ctx.format_records("S", rs.contig)[0]
+
+    def per_region():
+        out = []
+        for r, b in zip(regions, subs):
+            ctx.submit(b, [r])
+            ctx.pileup()
+            ctx.realign()
+            ctx.score()
+            out.append(ctx.format_records("S", rs.contig)[0])
+        return "".join(out)
+
+    for _ in range(args.warmup):
+        t_b = batched()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        t_b = batched()
+    dt_b = (time.perf_counter() - t0) / args.steps
+    t_r = per_region()
+    t0 = time.perf_counter()
+    t_r = per_region()
+    dt_r = time.perf_counter() - t0
+    same = sorted(t_b.splitlines()) == sorted(t_r.splitlines())
+    out = {"metric": f"reads/s batched amplicon panel ({n_reg} regions, -t -u)", "value": rs.n / dt_b,
+           "unit": "reads/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": dt_b * 1e3, "higher_is_better": True, "data": "synthetic",
+           "config": {"workload": f"{n_reg} regions U(100,2000) bp, depth lognormal median 500x, amplicon 2x150, "
+                                  "0.5% PCR duplicates, -t -u, simple mode", "reads": int(rs.n)},
+           "region_by_region": {"value": rs.n / dt_r, "unit": "reads/s", "ms": dt_r * 1e3},
+           "speedup_batched": dt_r / dt_b, "records": len(t_b.splitlines()), "records_equal": same}
+    print(json.dumps(out))
+    ctx.close()
+
+
 def run_reference(args, rank):
     if rank != 0:
         return
@@ -209,10 +272,15 @@ def main():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--panel", type=int, default=0, metavar="N",
+                    help="batched amplicon panel of N regions (-t -u): one launch for all regions vs one per region")
     args = ap.parse_args()
     rank, world, dist = dist_init()
     if args.impl == "reference":
         run_reference(args, rank)
+        return
+    if args.panel:
+        run_panel(args)
         return
     import numpy as np
     from rabbitvar_gb300 import api, synth
@@ -287,11 +355,12 @@ def main():
     ms_per_step = dev_dt / args.steps * 1e3
     value = n_reads * world * args.steps / dev_dt
     e2e = n_reads * world * args.steps / e2e_dt
-    # roofline of the dominant kernel (pileup tiles), event-timed per launch
-    tile_ms = statistics.mean(s["pileup_tiles"] for s in stages)  # per sample launch
-    per_launch_bytes = alg_read_bytes / len(samples)
+    # roofline of the dominant kernel: the tumor sample's k_pileup_tiles
+    # launch (1.33 M reads), event-timed on its stream; stages alternate
+    # tumor, normal
+    tile_ms = statistics.mean(s["pileup_tiles"] for s in stages[0::2])
     cells = sum(r[1] - r[0] + 1 for r in regions)
-    per_launch_bytes += cells * 256 + CONTIG  # site records + reference window
+    per_launch_bytes = read_alg_bytes(tumor) + cells * 256 + CONTIG  # reads + site records + reference window
     achieved = per_launch_bytes / (tile_ms * 1e-3) / 1e9
     peak, peak_kind = measured_peak_hbm()
     h2d = sum(b.nbytes for b in batches)
@@ -308,8 +377,9 @@ def main():
         "stage_ms": {k: statistics.mean(s[k] for s in stages) for k in stages[0]},
         "host_call_ms_per_step": {k: v / args.steps for k, v in host_ms.items()},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
-                     "kernel": "k_pileup_tiles", "alg_bytes_per_launch": per_launch_bytes},
+                     "frac": achieved / peak, "traffic": PILEUP_TRAFFIC, "peak_kind": peak_kind,
+                     "kernel": "k_pileup_tiles", "launch": "tumor sample, 1.33 M reads",
+                     "alg_bytes_per_launch": per_launch_bytes, "launch_ms": tile_ms},
         "clocks": clk,
     }
     # sites/s: region positions of both samples scored per second of k_score

@@ -303,7 +303,11 @@ rv_status rv_upload_reference(rv_ctx *ctx, const char *chr, const char *bases, i
         if (c >= 'a' && c <= 'z') c = (char)(c - 32);
     if (ctx->d_ref) cudaFree(ctx->d_ref);
     ctx->d_ref = nullptr;
-    RV_CUDA(cudaMalloc((void **)&ctx->d_ref, (size_t)n));
+    // padded to whole 16-byte words (plus one) so the walk can read the
+    // reference in 16-byte windows
+    const size_t padded = ((size_t)n + 15) / 16 * 16 + 16;
+    RV_CUDA(cudaMalloc((void **)&ctx->d_ref, padded));
+    RV_CUDA(cudaMemset(ctx->d_ref, 0, padded));
     RV_CUDA(cudaMemcpy(ctx->d_ref, ctx->ref_host.data(), (size_t)n, cudaMemcpyHostToDevice));
     ctx->ref_len = (int32_t)n;
     return RV_OK;

@@ -666,6 +666,8 @@ int pileup_variants() { return 3; }
 cudaError_t launch_pileup(const DevState &st, const DevParams &P, int grid, cudaStream_t s, int variant) {
     size_t smem = pileup_smem_bytes();
     PileupKernel k = pileup_variant(variant);
+    // (a larger shared-memory carveout was measured slower: the walker's
+    // local-memory state lives in L1)
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     k<<<grid, kPileupThreads, smem, s>>>(st, P);
@@ -674,6 +676,7 @@ cudaError_t launch_pileup(const DevState &st, const DevParams &P, int grid, cuda
 
 int pileup_blocks_per_sm(int variant) {
     int n = 0;
+    cudaFuncSetAttribute(pileup_variant(variant), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pileup_smem_bytes());
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pileup_variant(variant), kPileupThreads, pileup_smem_bytes());
     return n;
 }

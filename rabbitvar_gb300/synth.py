@@ -564,6 +564,89 @@ def somatic_mix(seed: int = 0x5EED0051, length: int = 30_000, tumor_depth: float
     return g, (germ, som, loh, art, lowq), tumor, normal
 
 
+def amplicon_panel(seed: int = 0x5EED0002, n_regions: int = 10_000, genome_len: int = 50_000_000,
+                   median_depth: float = 500.0, read_len: int = 150, dup_frac: float = 0.005,
+                   max_depth: float = 5000.0, min_depth: float = 50.0):
+    """Batched amplicon panel: `n_regions` regions with lengths ~U(100, 2000)
+    spread over a `genome_len` contig, per-region depth log-normal (median
+    `median_depth`, sigma ln(10)/3, clipped to [min_depth, max_depth]).
+    Each region is tiled by amplicons of 250..350 bp; read 1 starts at the
+    amplicon start (forward strand), read 2 ends at the amplicon end
+    (reverse strand), so the two reads of a pair overlap.  A fraction
+    `dup_frac` of pairs is duplicated as exact copies (PCR duplicates, no
+    duplicate flag).  Germline SNVs at 1e-3/bp with VAF 0.5 or 1.0;
+    substitution errors from the quality model.  Returns (genome, variants,
+    reads, regions)."""
+    rng = np.random.default_rng(seed)
+    L = read_len
+    g = make_genome(genome_len, rng)
+    lens = rng.integers(100, 2001, size=n_regions)
+    slot = genome_len // n_regions
+    starts = np.array([i * slot + int(rng.integers(600, max(601, slot - int(lens[i]) - 600)))
+                       for i in range(n_regions)])
+    regions = [(int(s) + 1, int(s + ln)) for s, ln in zip(starts.tolist(), lens.tolist())]
+    depth = np.clip(np.exp(np.log(median_depth) + rng.normal(0, np.log(10) / 3, n_regions)), min_depth, max_depth)
+    snv_pos = []
+    for a, b in regions:
+        k = rng.binomial(b - a + 1, 1e-3)
+        snv_pos += sorted(rng.integers(a - 1, b, size=k).tolist())
+    variants = [Variant(pos=int(p), kind="snv", ref="ACGT"[int(g[p])], alt="ACGT"[_rand_other(int(g[p]), rng)],
+                        vaf=0.5 if rng.random() < 0.7 else 1.0) for p in sorted(set(snv_pos))]
+    var_at = {v.pos: v for v in variants}
+    # amplicons: (start, end) 0-based half-open, covering each region
+    a_lo, a_hi, a_n = [], [], []
+    for (a, b), d in zip(regions, depth.tolist()):
+        p = a - 1 - 100
+        while p < b:
+            ln = int(rng.integers(250, 351))
+            n_pairs = max(1, int(round(d * ln / (2 * L))))
+            a_lo.append(p)
+            a_hi.append(p + ln)
+            a_n.append(n_pairs)
+            p += ln - 60
+    a_lo, a_hi, a_n = np.array(a_lo), np.array(a_hi), np.array(a_n)
+    frag_lo = np.repeat(a_lo, a_n)
+    frag_hi = np.repeat(a_hi, a_n)
+    dups = rng.random(frag_lo.shape[0]) < dup_frac
+    frag_lo = np.concatenate([frag_lo, frag_lo[dups]])
+    frag_hi = np.concatenate([frag_hi, frag_hi[dups]])
+    nf = frag_lo.shape[0]
+    start = np.concatenate([frag_lo, frag_hi - L])
+    rev = np.concatenate([np.zeros(nf, bool), np.ones(nf, bool)])
+    mate = np.concatenate([frag_hi - L, frag_lo])
+    isize = np.concatenate([frag_hi - frag_lo, frag_lo - frag_hi])
+    is_r1 = np.concatenate([np.ones(nf, bool), np.zeros(nf, bool)])
+    frag = np.concatenate([np.arange(nf), np.arange(nf)])
+    n = 2 * nf
+    seq = g[start[:, None] + np.arange(L)[None, :]]
+    # germline SNVs: one haplotype draw per fragment (both reads of a pair agree)
+    for p, v in var_at.items():
+        hit = np.nonzero((start <= p) & (start + L > p))[0]
+        if hit.size == 0:
+            continue
+        carry_f = rng.random(nf) < v.vaf
+        c = hit[carry_f[frag[hit]]]
+        seq[c, p - start[c]] = "ACGT".index(v.alt)
+    # exact duplicates keep their original's bases and qualities
+    qual = _qualities(n, L, rng)
+    qual[rev] = qual[rev][:, ::-1]
+    err = rng.random((n, L)) < np.power(10.0, -qual.astype(np.float64) / 10.0)
+    seq = np.where(err, (seq + rng.integers(1, 4, size=(n, L))) % 4, seq).astype(np.uint8)
+    n_orig = nf - int(dups.sum())
+    src = np.nonzero(dups)[0]
+    for half in (0, nf):
+        seq[half + n_orig:half + nf] = seq[half + src]
+        qual[half + n_orig:half + nf] = qual[half + src]
+    codes = CODE_OF[seq]
+    mapq = np.full(n, 60, dtype=np.uint8)
+    flag = (1 | 2 | np.where(rev, 16, 32) | np.where(is_r1, 64, 128)).astype(np.uint16)
+    ref_win = CODE_OF[g[start[:, None] + np.arange(L)[None, :]]]
+    nm = (codes != ref_win).sum(axis=1).astype(np.int32)
+    order = np.lexsort((frag, start))
+    return g, variants, _pack("ctg", genome_len, order, start, flag, mapq, mate, isize, nm, [None] * n, codes, qual,
+                              frag, L), regions
+
+
 def dense_multi(seed: int = 0x5EED00D0, length: int = 60_000, depth: float = 60.0):
     """A small contig with dense SNV/MNV/indel planting, more soft clips and
     reads kept away from the contig end, for exercising every pileup path."""
