@@ -833,10 +833,9 @@ struct Walker {
             int celr = cel;
             const uint4 *seq16 = reinterpret_cast<const uint4 *>(rv.seq);
             const uint4 *qual16 = reinterpret_cast<const uint4 *>(rv.qual);
-            // the reference in 16-byte windows (the device copy is padded to whole words)
-            const uint4 *ref16 = reinterpret_cast<const uint4 *>(ref);
-            uint4 qw = make_uint4(0, 0, 0, 0), sw = make_uint4(0, 0, 0, 0), rw = make_uint4(0, 0, 0, 0);
-            int qblk = -1, sblk = -1, rblk = -1;
+            const char *refp = ref;
+            uint4 qw = make_uint4(0, 0, 0, 0), sw = make_uint4(0, 0, 0, 0);
+            int qblk = -1, sblk = -1;
             for (int i = offset; i < celr; i++) {
                 if ((rp >> 5) != sblk) { sblk = rp >> 5; sw = __ldg(seq16 + sblk); }
                 const uint32_t swd_ = pick_word(sw, (rp & 31) >> 3);
@@ -849,12 +848,7 @@ struct Walker {
                 const int q0 = (int)((pick_word(qw, (rp & 15) >> 2) >> ((rp & 3) * 8)) & 255u);
                 const int b = code_base(code);
                 const bool hs = st >= ws && st <= we;
-                char rc = 0;
-                if (hs) {
-                    const int ro = st - 1;
-                    if ((ro >> 4) != rblk) { rblk = ro >> 4; rw = __ldg(ref16 + rblk); }
-                    rc = (char)((pick_word(rw, (ro & 15) >> 2) >> ((ro & 3) * 8)) & 255u);
-                }
+                const char rc = hs ? __ldg(refp + st - 1) : (char)0;
                 const bool mm = hs && base_index(rc) != b;
                 const bool slow = b < 0 || i >= tail_from ||
                                   (mm && q0 >= goodq && st + 1 >= rs && st + 1 <= re && i + 1 < celr && rc != 'N');
