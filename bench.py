@@ -135,9 +135,9 @@ WORKLOAD = ("somatic mode (-b 'T|N' -N 'T|N' --fisher -f 0.01 -k 0): synthetic 1
             "tumor 200x + normal 100x 2x150, 100 x 10 kb BED tiles")
 METRIC = "reads/s pileup+var scoring (somatic pair 1 Mb, T200x+N100x)"
 CPU_TILES = 40   # CPU sample: 40 of the 100 tiles (~0.8 M reads, ~10 s on one core)
-# DRAM bytes (read + write) of one tumor-sample k_pileup_tiles launch of this
-# workload, from one ncu capture (profiles/k_pileup_tiles_somatic1mb.md)
-PILEUP_TRAFFIC = 841.1e6
+# DRAM bytes (read + write) of one tumor-sample k_pileup_tiles<640, 3> launch
+# of this workload, from one ncu capture (profiles/k_pileup_tiles_somatic1mb.md)
+PILEUP_TRAFFIC = 1301.5e6
 
 
 def cpu_baseline_run(g, tumor, normal, regions, threads: int, n_regions: int):

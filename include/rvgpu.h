@@ -42,8 +42,8 @@ typedef struct {
     double goodq;          /* -q  22.5 */
     int32_t vext;          /* -X  2 */
     int32_t mismatch;      /* -m  8 */
-    int32_t local_realign; /* -k  1: the CIGAR rewrite runs in rv_pileup; rv_realign's indel passes
-                              are not in this build (RV_ERR_UNSUPPORTED) */
+    int32_t local_realign; /* -k  1: the CIGAR rewrite runs in rv_pileup; rv_realign runs adjustMNP
+                              and the indel passes (realignIndels) over the device maps */
     double freq;           /* -f  0.01 */
     int32_t minr;          /* -r  2 */
     int32_t read_pos_filter; /* -P 5 */
@@ -133,10 +133,14 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *reads, const rv_regi
  * CIGAR walk and allele-count maps for every region of the batch. */
 rv_status rv_pileup(rv_ctx *ctx, void *stream);
 
-/* Replaces VariationRealigner::process for -k 0
- * (adjustMNP, src/VariationRealigner.cpp:334-465): host realigner over the
- * device-built maps; reads the MNP keys and their neighbours from the
- * device, applies the merges on the host and writes the changes back. */
+/* Replaces VariationRealigner::process (src/VariationRealigner.cpp:135-161):
+ * host realigner over the device-built maps.  -k 0: adjustMNP (:334-465),
+ * reading only the MNP keys and their neighbours from the device.  -k 1:
+ * adjustMNP and realignIndels (:467-1360) per region (regions in parallel)
+ * over a mirror of the maps filled from the device around every candidate;
+ * noPassingReads reads the batch's alignment spans kept on the host.  The
+ * changes are written back to the device maps (realigned statistics, erased
+ * and new keys, coverage).  Once per batch (RV_ERR_STATE on a second call). */
 rv_status rv_realign(rv_ctx *ctx, void *stream);
 
 /* Replaces ToVarsBuilder::process (src/ToVarsBuilder.cpp:97-205), the hard

@@ -16,6 +16,7 @@
 
 namespace rv {
 rv_status host_realign_mnp(rv_ctx *ctx);
+rv_status host_realign_full(rv_ctx *ctx);
 rv_status host_format_records(rv_ctx *ctx, const char *sample, const char *gene, uint8_t *emitted = nullptr);
 rv_status host_export_maps(rv_ctx *ctx, int region, const char *stages);
 }  // namespace rv
@@ -285,7 +286,7 @@ void rv_destroy(rv_ctx *ctx) {
                     ctx->d_regions, ctx->d_tiles, ctx->d_score_base, ctx->d_cellmem, ctx->d_head, ctx->d_slots,
                     ctx->d_arena, ctx->d_deferred, ctx->d_cand, ctx->d_counters, ctx->d_tmp_idx,
                     ctx->d_tmp_slots, ctx->d_tmp_cells, ctx->d_tmp_views, ctx->d_tmp_n, ctx->d_list,
-                    ctx->d_ftab, ctx->d_logfact, ctx->d_skip};
+                    ctx->d_ftab, ctx->d_logfact, ctx->d_skip, ctx->d_patches, ctx->d_patch_keys};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (int i = 0; i < 12; i++)
@@ -359,6 +360,20 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
         RV_CUDA(cudaMemcpyAsync(ctx->d_cigar, b->cigar, b->n_cigar_words * 4, cudaMemcpyHostToDevice, s));
         RV_CUDA(cudaMemcpyAsync(ctx->d_seq, b->seq, (size_t)(b->n_bases + 1) / 2, cudaMemcpyHostToDevice, s));
         RV_CUDA(cudaMemcpyAsync(ctx->d_qual, b->qual, (size_t)b->n_bases, cudaMemcpyHostToDevice, s));
+    }
+    // -k 1: the alignment spans stay on the host for noPassingReads
+    if (ctx->params.local_realign) {
+        ctx->h_pos.assign(b->pos, b->pos + n);
+        ctx->h_flag.assign(b->flag, b->flag + n);
+        ctx->h_ncig.assign(b->n_cigar, b->n_cigar + n);
+        ctx->h_cigoff.assign(b->cig_off, b->cig_off + n);
+        ctx->h_cigar.assign(b->cigar, b->cigar + b->n_cigar_words);
+    } else {
+        ctx->h_pos.clear();
+        ctx->h_flag.clear();
+        ctx->h_ncig.clear();
+        ctx->h_cigoff.clear();
+        ctx->h_cigar.clear();
     }
     // batch-wide bounds used to size the per-region cell ranges
     int max_span = 1, max_lq = 1;
@@ -622,14 +637,10 @@ rv_status rv_pileup(rv_ctx *ctx, void *stream) {
 rv_status rv_realign(rv_ctx *ctx, void *stream) {
     if (!ctx) return RV_ERR_ARG;
     if (ctx->stage < 2) { ctx->err = "rv_realign before rv_pileup"; return RV_ERR_STATE; }
-    if (ctx->params.local_realign) {
-        ctx->err = "-k 1: the realigner's indel passes (realignIndels) are not in this build; "
-                   "rv_pileup and rv_export_maps support -k 1";
-        return RV_ERR_UNSUPPORTED;
-    }
+    if (ctx->stage >= 3) { ctx->err = "rv_realign called twice on one batch"; return RV_ERR_STATE; }
     (void)stream;
     RV_CUDA(cudaSetDevice(ctx->device));
-    rv_status st = host_realign_mnp(ctx);
+    rv_status st = ctx->params.local_realign ? host_realign_full(ctx) : host_realign_mnp(ctx);
     if (st) return st;
     ctx->stage = 3;
     return RV_OK;

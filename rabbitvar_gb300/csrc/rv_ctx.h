@@ -47,15 +47,25 @@ void launch_gather_cells(const DevState &st, const int64_t *cells, int64_t n, Ce
 
 // patch written back by the host realigner
 struct Patch {
-    int32_t type;       // 0 overwrite slot stats, 1 erase slot, 2 erase single cell key, 3 add coverage
+    // 0 overwrite a slot's statistics (adjustMNP: integer sums)
+    // 1 erase a slot (flags |= SF_ERASED | flags_or)
+    // 2 erase a single-base cell key
+    // 3 add coverage
+    // 4 set a slot's realigned statistics (SF_OVR)
+    // 5 find or create the slot (region, pos, kind, key bytes) and set them
+    // 6 remove a position's cell keys from the map
+    int32_t type;
     int32_t base;
     int64_t target;     // slot index or cell index
     int32_t fwd, rev, hi, lo, extracnt, flags_or;
     long long tp_sum, mq_sum, nm_sum;
     double q_sum;
-    int32_t cov_add, pad;
+    int32_t cov_add, cnt;
+    double tp, mq, nm;                  // types 4 and 5
+    int32_t region, pos, kind, klen;    // type 5
+    int64_t key_off;                    // type 5: key bytes in the patch key buffer
 };
-void launch_apply_patches(const DevState &st, const Patch *p, int64_t n, cudaStream_t s);
+void launch_apply_patches(const DevState &st, const Patch *p, int64_t n, const uint8_t *keys, cudaStream_t s);
 
 template <class T>
 struct DevBuf {
@@ -92,7 +102,10 @@ struct rv_ctx {
     uint8_t *d_skip = nullptr;  // -t duplicate flags
     size_t cap_skip = 0;
     bool use_skip = false;
-    std::vector<int32_t> h_pos;  // positions kept for region lookup
+    // -k 1: alignment spans of the batch kept on the host (noPassingReads)
+    std::vector<int32_t> h_pos;
+    std::vector<uint16_t> h_flag, h_ncig;
+    std::vector<uint32_t> h_cigoff, h_cigar;
 
     // regions / tiles
     std::vector<rv::Region> regions;
@@ -136,6 +149,10 @@ struct rv_ctx {
     void *d_tmp_views = nullptr;
     size_t cap_tmp_views = 0;
     unsigned int *d_tmp_n = nullptr;
+    rv::Patch *d_patches = nullptr;
+    size_t cap_patches = 0;
+    uint8_t *d_patch_keys = nullptr;
+    size_t cap_patch_keys = 0;
     // somatic mode: positions to score without screens; Fisher tables and results
     double *d_logfact = nullptr;  // log(k!) table for the Fisher tests
     int2 *d_list = nullptr;

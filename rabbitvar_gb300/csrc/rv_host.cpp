@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "rv_ctx.h"
+#include "rv_mirror.h"
 #include "rv_records.h"
 
 namespace rv {
@@ -41,27 +42,11 @@ namespace {
 
 constexpr uint32_t FC_PDIFF = 1u << 30, FC_QDIFF = 1u << 31;
 
-// Statistics of one allele key as the host realigner sees it.
-struct HVar {
-    int cnt = 0, fwd = 0, rev = 0, hi = 0, lo = 0, extracnt = 0;
-    double tp = 0, q = 0, mq = 0, nm = 0;
-    bool pstd = false, qstd = false;
-    int64_t slot = -1;   // hash slot, or -1 for a cell key
-    int64_t cell = -1;
-    int base = -1;
-    bool dirty = false, erased = false, force_std = false;
-};
-
-struct HClip {
-    HVar agg;
-    std::map<int, std::map<char, std::pair<int, double>>> nt;  // idx -> ch -> (count, quality sum)
-    std::string cons;
-    bool used = false;
-};
+}  // namespace
 
 // Measured iteration order of the reference's hash map over soft-clip
 // bases (N, A, T, G, C), which decides ties in the consensus.
-int clip_rank(char c) {
+static int clip_rank(char c) {
     switch (c) {
     case 'N': return 0;
     case 'A': return 1;
@@ -150,7 +135,7 @@ void add_into(HVar &to, const HVar &v) {  // adjCnt: include/VariationUtils.h:33
     to.dirty = true;
 }
 
-bool matches_ref(const std::string &s, const RefWin &R, int position, int dir) {  // ismatchref, MM = 3
+static bool matches_ref(const std::string &s, const RefWin &R, int position, int dir) {  // ismatchref, MM = 3
     int mm = 0, n = (int)s.size();
     for (int k = 0; k < n; k++) {
         int p = position + dir * k;
@@ -240,18 +225,30 @@ HVar from_slot(const Slot &s, int64_t slot) {
     h.hi = s.hi;
     h.lo = s.lo;
     h.extracnt = s.extracnt;
-    h.tp = (double)s.tp_sum;
     h.q = s.q_sum;
-    h.mq = (double)s.mq_sum;
-    h.nm = (double)s.nm_sum;
-    h.pstd = (s.flags & (SF_PDIFF | SF_FORCE_STD)) != 0;
-    h.qstd = (s.flags & (SF_QDIFF | SF_FORCE_STD)) != 0;
+    if (s.flags & SF_OVR) {
+        double d[3];
+        memcpy(&d[0], &s.tp_sum, 8);
+        memcpy(&d[1], &s.mq_sum, 8);
+        memcpy(&d[2], &s.nm_sum, 8);
+        h.cnt = s.first_tp;
+        h.tp = d[0];
+        h.mq = d[1];
+        h.nm = d[2];
+        h.pstd = (s.flags & SF_PDIFF) != 0;
+        h.qstd = (s.flags & SF_QDIFF) != 0;
+    } else {
+        h.tp = (double)s.tp_sum;
+        h.mq = (double)s.mq_sum;
+        h.nm = (double)s.nm_sum;
+        h.pstd = (s.flags & (SF_PDIFF | SF_FORCE_STD)) != 0;
+        h.qstd = (s.flags & (SF_QDIFF | SF_FORCE_STD)) != 0;
+    }
     h.erased = (s.flags & SF_ERASED) != 0;
     h.slot = slot;
     return h;
 }
 
-}  // namespace
 
 template <class T>
 rv_status ensure(rv_ctx *ctx, T *&p, size_t &cap, size_t need) {
@@ -487,19 +484,23 @@ rv_status host_realign_mnp(rv_ctx *ctx) {
             p.flags_or = h.force_std ? (int)SF_FORCE_STD : 0;
             patches.push_back(p);
         }
+    return apply_patches(ctx, patches, std::string());
+}
+
+rv_status apply_patches(rv_ctx *ctx, const std::vector<Patch> &patches, const std::string &keys) {
     if (patches.empty()) return RV_OK;
-    Patch *d_p = (Patch *)ctx->d_tmp_views;
-    size_t capp = ctx->cap_tmp_views * sizeof(CellView) / sizeof(Patch);
-    if (!d_p || capp < patches.size()) {
-        if (ctx->d_tmp_views) cudaFree(ctx->d_tmp_views);
-        ctx->d_tmp_views = nullptr;
-        size_t nv = (patches.size() * sizeof(Patch) + sizeof(CellView) - 1) / sizeof(CellView) + 64;
-        HCUDA(cudaMalloc(&ctx->d_tmp_views, nv * sizeof(CellView)));
-        ctx->cap_tmp_views = nv;
-        d_p = (Patch *)ctx->d_tmp_views;
+    rv_status st;
+    if ((st = ensure(ctx, ctx->d_patches, ctx->cap_patches, patches.size()))) return st;
+    const uint8_t *d_keys = nullptr;
+    if (!keys.empty()) {
+        if ((st = ensure(ctx, ctx->d_patch_keys, ctx->cap_patch_keys, keys.size()))) return st;
+        HCUDA(cudaMemcpyAsync(ctx->d_patch_keys, keys.data(), keys.size(), cudaMemcpyHostToDevice, ctx->stream));
+        d_keys = ctx->d_patch_keys;
     }
-    HCUDA(cudaMemcpyAsync(d_p, patches.data(), patches.size() * sizeof(Patch), cudaMemcpyHostToDevice, ctx->stream));
-    launch_apply_patches(ctx->state(), d_p, (int64_t)patches.size(), ctx->stream);
+    HCUDA(cudaMemcpyAsync(ctx->d_patches, patches.data(), patches.size() * sizeof(Patch), cudaMemcpyHostToDevice,
+                          ctx->stream));
+    ctx->io_h2d += (int64_t)(patches.size() * sizeof(Patch) + keys.size());
+    launch_apply_patches(ctx->state(), ctx->d_patches, (int64_t)patches.size(), d_keys, ctx->stream);
     ctx->kernels++;
     HCUDA(cudaStreamSynchronize(ctx->stream));
     return RV_OK;

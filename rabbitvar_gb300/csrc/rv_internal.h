@@ -34,6 +34,10 @@ enum : uint32_t {
     SF_ERASED = 8u,     // removed by the realigner
     SF_FIRST = 16u,     // first_tp / first_q hold a value
     SF_FORCE_STD = 32u, // pstd and qstd forced true (adjCnt)
+    SF_OVR = 64u,       // statistics set by the -k 1 realigner: the allele count is
+                        // in first_tp, tp_sum/mq_sum/nm_sum hold double bits, and
+                        // pstd/qstd are exactly SF_PDIFF/SF_QDIFF
+    SF_NOMAP = 128u,    // the realigner removed the position's map entry
 };
 
 // One allele key of the device hash table.

@@ -25,24 +25,6 @@ __device__ __forceinline__ void set_err(unsigned int *err, unsigned int bits) { 
 // ---------------------------------------------------------------------------
 // device hash table of string-keyed alleles
 // ---------------------------------------------------------------------------
-__device__ void key_hashes(int region, int kind, int pos, const char *k, int n, unsigned long long &h1,
-                           unsigned long long &h2) {
-    unsigned long long a = fmix64(((unsigned long long)(uint32_t)region << 32) ^ (uint32_t)pos ^
-                                  ((unsigned long long)kind << 58) ^ ((unsigned long long)n << 44));
-    unsigned long long b = fmix64(a ^ 0x9e3779b97f4a7c15ULL);
-    int i = 0;
-    while (i < n) {
-        unsigned long long w = 0;
-        int m = n - i < 8 ? n - i : 8;
-        for (int j = 0; j < m; j++) w |= (unsigned long long)(uint8_t)k[i + j] << (8 * j);
-        a = fmix64(a ^ w) + 0x632be59bd9b4e019ULL;
-        b = fmix64(b + w * 0x94d049bb133111ebULL);
-        i += m;
-    }
-    h1 = a ? a : 1;
-    h2 = b;
-}
-
 __device__ Slot *hash_get(const Hash &H, unsigned int *err, int region, int kind, int pos, const char *k, int n) {
     unsigned long long h1, h2;
     key_hashes(region, kind, pos, k, n, h1, h2);

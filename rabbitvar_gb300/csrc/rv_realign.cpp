@@ -1,0 +1,1288 @@
+// The local realigner of -k 1 over the device-built maps, on the host:
+// VariationRealigner::adjustMNP (src/VariationRealigner.cpp:334-465) followed
+// by realignIndels (:467-1360: realigndel :489-775, realignins :785-1114,
+// realignlgins30 :1119-1350, with findMM3/findMM5 :1857-1984, ismatch
+// :1507-1546, adjRefCnt :1753-1787, adjRefFactor :1794-1822, noPassingReads
+// :1447-1505, find35match :1396-1428).
+//
+// Each region runs over a lazily filled mirror of its maps: a position's
+// keys are read from the fetched cells and slots the first time the
+// realigner touches it, and a snapshot is kept.  At the end the mirror is
+// diffed against the snapshots and the differences go back to the device as
+// patches: realigned statistics (SF_OVR slots; a single-base key that
+// changes moves from its cell to a slot), erased keys, new keys, removed
+// position entries and coverage additions.  The score kernel reads the
+// patched maps.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <regex>
+#include <set>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "rv_mirror.h"
+
+namespace rv {
+
+namespace {
+
+#define HCUDA(call)                                                        \
+    do {                                                                   \
+        cudaError_t e_ = (call);                                           \
+        if (e_ != cudaSuccess) {                                           \
+            ctx->err = std::string(#call) + ": " + cudaGetErrorString(e_); \
+            return RV_ERR_CUDA;                                            \
+        }                                                                  \
+    } while (0)
+
+using std::string;
+
+constexpr int kBlock = 1024;  // cells fetched per block
+
+// Reference window of a region with the insert-on-lookup behaviour of the
+// reference's map: operator[] on a position outside the window stores base 0
+// there, and the position counts as present afterwards.
+struct PRef {
+    const string *ref = nullptr;
+    int ws = 1, we = 0;
+    std::set<int> phantom;
+    bool has(int p) const { return (p >= ws && p <= we) || phantom.count(p); }
+    char at(int p) const { return (p >= ws && p <= we) ? (*ref)[p - 1] : 0; }
+    char idx(int p) {
+        if (p >= ws && p <= we) return (*ref)[p - 1];
+        phantom.insert(p);
+        return 0;
+    }
+    bool has_eq(char c, int p) const { return has(p) && at(p) == c; }
+    bool has_ne(char c, int p) const { return has(p) && at(p) != c; }
+};
+
+struct RefFail {};     // joinRef's .at() on a missing position
+struct OutOfRange {};  // std::out_of_range from substr
+
+string join_ref(const PRef &R, int from, int to) {  // joinRef: include/VariationUtils.h:356-362
+    string s;
+    for (int i = from; i <= to; i++) {
+        if (!R.has(i)) throw RefFail();
+        s += R.at(i);
+    }
+    return s;
+}
+
+// vc_substr (include/util.h:27-57): negative indices count from the end; the
+// length test there is unsigned, so too negative an index throws
+string vsub(const string &s, int idx) {
+    size_t b = idx >= 0 ? (size_t)idx : s.size() + (size_t)(long long)idx;
+    if (b > s.size()) throw OutOfRange();
+    return s.substr(b);
+}
+string vsub(const string &s, int begin, int len) {
+    if (begin < 0) begin = (int)(s.size() + (size_t)(long long)begin);
+    if (len > 0) {
+        if ((size_t)(long long)begin > s.size()) throw OutOfRange();
+        return s.substr((size_t)(long long)begin, (size_t)len);
+    }
+    if (len == 0) return string();
+    len = (int)(s.size() + (size_t)(long long)len - (size_t)(long long)begin);
+    if (len < 0) return string();
+    if ((size_t)(long long)begin > s.size()) throw OutOfRange();
+    return s.substr((size_t)(long long)begin, (size_t)len);
+}
+char char_at(const string &s, int i) {  // charAt: include/util.h:171-179
+    if (i < 0) {
+        int k = (int)s.size() + i;
+        return k < 0 ? (char)-1 : s[k];
+    }
+    return s[i];
+}
+string drop_hash_caret(const string &s) {
+    string o;
+    for (char c : s)
+        if (c != '#' && c != '^') o += c;
+    return o;
+}
+void replace_first(string &s, const string &a, const string &b) {
+    size_t p = s.find(a);
+    if (p != string::npos) s.replace(p, a.size(), b);
+}
+bool low_complexity(const string &seq) {  // islowcomplexseq: include/VariationUtils.h:366-395
+    int len = (int)seq.size();
+    if (len == 0) return true;
+    int kinds = 0;
+    for (char b : string("ATGC")) {
+        int c = (int)std::count(seq.begin(), seq.end(), b);
+        if (c > 0) kinds++;
+        if (c / (double)len > 0.75) return true;
+    }
+    return kinds < 3;
+}
+
+void clamp_counts(HVar &r) {  // correctCnt: include/VariationUtils.h:263-280
+    if (r.cnt < 0) r.cnt = 0;
+    if (r.hi < 0) r.hi = 0;
+    if (r.lo < 0) r.lo = 0;
+    if (r.tp < 0) r.tp = 0;
+    if (r.q < 0) r.q = 0;
+    if (r.mq < 0) r.mq = 0;
+    if (r.rev < 0) r.rev = 0;
+    if (r.fwd < 0) r.fwd = 0;
+}
+// adjCnt(varToAdd, variant, referenceVar): include/VariationUtils.h:291-317
+void add_sub(HVar &to, const HVar &v, HVar *ref) {
+    add_into(to, v);
+    if (!ref) return;
+    ref->cnt -= v.cnt;
+    ref->hi -= v.hi;
+    ref->lo -= v.lo;
+    ref->tp -= v.tp;
+    ref->q -= v.q;
+    ref->mq -= v.mq;
+    ref->nm -= v.nm;
+    ref->rev -= v.rev;
+    ref->fwd -= v.fwd;
+    clamp_counts(*ref);
+}
+
+bool same_stats(const HVar &a, const HVar &b) {
+    return a.cnt == b.cnt && a.fwd == b.fwd && a.rev == b.rev && a.hi == b.hi && a.lo == b.lo &&
+           a.extracnt == b.extracnt && a.tp == b.tp && a.q == b.q && a.mq == b.mq && a.nm == b.nm &&
+           a.pstd == b.pstd && a.qstd == b.qstd;
+}
+
+uint64_t pos_key(int region, int pos) { return ((uint64_t)(uint32_t)region << 32) | (uint32_t)pos; }
+
+// ---------------------------------------------------------------------------
+// batch-wide mirror: every slot, the key arena, cells fetched by block
+// ---------------------------------------------------------------------------
+struct Mirror {
+    rv_ctx *ctx = nullptr;
+    std::vector<Slot> slots;
+    std::vector<uint32_t> sidx;
+    std::unordered_map<uint64_t, std::vector<uint32_t>> nonins_at, ins_at, sc5_at, sc3_at;
+    std::vector<Region> regions;  // device copies (max_read_len)
+    std::unordered_map<int64_t, std::vector<CellView>> blocks;
+    std::mutex mu;
+    rv_status failed = RV_OK;
+
+    string key(uint32_t i) const { return slot_key(ctx, slots[i]); }
+
+    rv_status fetch_blocks(const std::vector<int64_t> &want) {
+        std::vector<int64_t> need;
+        for (int64_t b : want)
+            if (!blocks.count(b)) need.push_back(b);
+        if (need.empty()) return RV_OK;
+        std::vector<int64_t> cells;
+        for (int64_t b : need)
+            for (int64_t c = b * kBlock; c < (b + 1) * kBlock; c++) cells.push_back(std::min(c, ctx->n_cells - 1));
+        std::vector<CellView> cv;
+        rv_status st = fetch_cells(ctx, cells, cv);
+        if (st) return st;
+        ctx->kernels++;
+        ctx->io_d2h += (int64_t)(cv.size() * sizeof(CellView));
+        for (size_t i = 0; i < need.size(); i++)
+            blocks[need[i]].assign(cv.begin() + (int64_t)i * kBlock, cv.begin() + (int64_t)(i + 1) * kBlock);
+        return RV_OK;
+    }
+
+    // cell view of cell c (fetched on demand when no prefetch covered it)
+    const CellView *cell(int64_t c) {
+        std::lock_guard<std::mutex> g(mu);
+        int64_t b = c / kBlock;
+        auto it = blocks.find(b);
+        if (it == blocks.end()) {
+            rv_status st = fetch_blocks({b});
+            if (st) {
+                failed = st;
+                return nullptr;
+            }
+            it = blocks.find(b);
+        }
+        return &it->second[(size_t)(c % kBlock)];
+    }
+};
+
+// One position of nonInsertionVariants or insertionVariants.
+struct PosMap {
+    bool present = false;
+    std::map<string, HVar> keys;
+};
+
+// ---------------------------------------------------------------------------
+// one region
+// ---------------------------------------------------------------------------
+struct RegionRealigner {
+    Mirror &mir;
+    rv_ctx *ctx;
+    const rv_params &P;
+    int region;
+    Region Rg;
+    int max_rl;
+    int chr_len;
+    PRef R;
+    std::map<int, PosMap> nonins, ins, nonins0, ins0;
+    std::map<int, int> cov_add;
+    struct Clip {
+        HClip c;
+        const std::vector<uint32_t> *seq = nullptr;
+        bool loaded = false;
+    };
+    std::map<int, Clip> sc5, sc3;
+
+    RegionRealigner(Mirror &m, rv_ctx *c, int r)
+        : mir(m), ctx(c), P(c->params), region(r), Rg(m.regions[r]), max_rl(m.regions[r].max_read_len),
+          chr_len(c->ref_len) {
+        R.ref = &ctx->ref_host;
+        R.ws = Rg.ws;
+        R.we = Rg.we;
+    }
+
+    bool in_cells(int p) const { return p >= Rg.clo && p <= Rg.chi; }
+    int64_t cell_of(int p) const { return Rg.cell_base + (p - Rg.clo); }
+
+    PosMap &N(int p) {
+        auto it = nonins.find(p);
+        if (it != nonins.end()) return it->second;
+        PosMap &m = nonins[p];
+        if (in_cells(p)) {
+            int64_t c = cell_of(p);
+            const CellView *v = mir.cell(c);
+            if (v) {
+                int exist = v->kflags & 15, erased = (v->kflags >> 4) & 15;
+                if (exist) m.present = true;
+                for (int b = 0; b < 4; b++)
+                    if (((exist & ~erased) >> b) & 1) m.keys[string(1, "ACGT"[b])] = from_cell(*v, b, c);
+            }
+            auto s = mir.nonins_at.find(pos_key(region, p));
+            if (s != mir.nonins_at.end())
+                for (uint32_t i : s->second) {
+                    m.present = true;
+                    HVar h = from_slot(mir.slots[i], mir.sidx[i]);
+                    if (!h.erased) m.keys[mir.key(i)] = h;
+                }
+        }
+        nonins0[p] = m;
+        return m;
+    }
+    PosMap &I(int p) {
+        auto it = ins.find(p);
+        if (it != ins.end()) return it->second;
+        PosMap &m = ins[p];
+        auto s = mir.ins_at.find(pos_key(region, p));
+        if (s != mir.ins_at.end())
+            for (uint32_t i : s->second) {
+                m.present = true;
+                HVar h = from_slot(mir.slots[i], mir.sidx[i]);
+                if (!h.erased) m.keys[mir.key(i)] = h;
+            }
+        ins0[p] = m;
+        return m;
+    }
+    bool has_key(int p, const string &k) {
+        PosMap &m = N(p);
+        return m.present && m.keys.count(k);
+    }
+    // map operator[] on position and key
+    HVar &nget(int p, const string &k) {
+        PosMap &m = N(p);
+        m.present = true;
+        return m.keys[k];
+    }
+    HVar &iget(int p, const string &k) {
+        PosMap &m = I(p);
+        m.present = true;
+        return m.keys[k];
+    }
+    // erase a key; drop the position entry when it becomes empty
+    void nerase_drop(int p, const string &k) {
+        PosMap &m = N(p);
+        m.present = true;  // operator[] before erase
+        m.keys.erase(k);
+        if (m.keys.empty()) m.present = false;
+    }
+    // getVariationMaybe: include/VariationUtils.h:218-239
+    HVar *maybe(int p, char base) {
+        if (base == 0) return nullptr;
+        PosMap &m = N(p);
+        if (!m.present) return nullptr;
+        auto j = m.keys.find(string(1, base));
+        return j == m.keys.end() ? nullptr : &j->second;
+    }
+    // nonInsertionVariants.count(p) && [p].count(k)
+    HVar *nfind(int p, const string &k) {
+        PosMap &m = N(p);
+        if (!m.present) return nullptr;
+        auto j = m.keys.find(k);
+        return j == m.keys.end() ? nullptr : &j->second;
+    }
+
+    Clip *clip(std::map<int, Clip> &sc, int p) {
+        auto it = sc.find(p);
+        return it == sc.end() ? nullptr : &it->second;
+    }
+    string consensus(Clip &k) {
+        if (!k.loaded) {
+            k.loaded = true;
+            if (k.seq)
+                for (uint32_t i : *k.seq) {
+                    string key = mir.key(i);
+                    if (key.size() != 3) continue;
+                    int idx = (uint8_t)key[0] | ((uint8_t)key[1] << 8);
+                    k.c.nt[idx][key[2]] = {mir.slots[i].obs, mir.slots[i].q_sum};
+                }
+        }
+        return clip_consensus(k.c);
+    }
+    void add_cov(int p, int n) { cov_add[p] += n; }
+
+    void load_clips() {
+        for (int side = 0; side < 2; side++) {
+            auto &src = side ? mir.sc3_at : mir.sc5_at;
+            auto &dst = side ? sc3 : sc5;
+            for (int p = Rg.clo; p <= Rg.chi; p++) {
+                auto it = src.find(pos_key(region, p));
+                if (it == src.end()) continue;
+                Clip &k = dst[p];
+                for (uint32_t i : it->second) {
+                    const Slot &s = mir.slots[i];
+                    if (s.kind == KIND_SC5 || s.kind == KIND_SC3) k.c.agg = from_slot(s, mir.sidx[i]);
+                }
+                k.seq = &it->second;
+            }
+        }
+    }
+
+    // ------------------------------------------------------------------
+    // adjustMNP (src/VariationRealigner.cpp:334-465)
+    // ------------------------------------------------------------------
+    void adjust_mnp(const std::map<int, std::map<string, int>> &mnp) {
+        struct T { int pos; string key; int cnt; };
+        std::vector<T> tmp;
+        for (auto &pe : mnp)
+            for (auto &ke : pe.second) tmp.push_back({pe.first, ke.first, ke.second});
+        std::sort(tmp.begin(), tmp.end(), [](const T &a, const T &b) {
+            if (a.cnt != b.cnt) return a.cnt > b.cnt;
+            if (a.pos != b.pos) return a.pos < b.pos;
+            return a.key.compare(b.key) > 0;
+        });
+        for (const T &t : tmp) {
+            const int position = t.pos;
+            const string &vn = t.key;
+            PosMap &pm = N(position);
+            if (!pm.present) continue;
+            std::set<string> local;  // keys of the by-value copy the reference iterates
+            for (auto &e : pm.keys) local.insert(e.first);
+            if (!local.count(vn)) continue;
+            HVar &vref = pm.keys.at(vn);
+            string mnt = vn;
+            size_t amp = mnt.find('&');
+            if (amp != string::npos) mnt.erase(amp, 1);
+            const int ml = (int)mnt.size();
+            for (int i = 0; i < ml - 1; i++) {
+                string left = mnt.substr(0, i + 1), right = mnt.substr(i + 1);
+                if (left.size() > 1) left.insert(1, "&");
+                if (right.size() > 1) right.insert(1, "&");
+                if (local.count(left)) {
+                    HVar &tref = pm.keys.at(left);
+                    if (tref.cnt <= 0) continue;
+                    if (tref.cnt < vref.cnt && tref.tp / tref.cnt <= i + 1) {
+                        add_into(vref, tref);
+                        local.erase(left);
+                    }
+                }
+                PosMap &rm = N(position + i + 1);
+                if (rm.present) {
+                    auto kit = rm.keys.find(right);
+                    if (kit != rm.keys.end()) {
+                        HVar &tref = kit->second;
+                        if (tref.cnt < 0) continue;
+                        if (tref.cnt < vref.cnt) {
+                            add_into(vref, tref);
+                            add_cov(position, tref.cnt);
+                            rm.keys.erase(kit);
+                        }
+                    }
+                }
+            }
+            Clip *s3 = clip(sc3, position);
+            if (s3 && !s3->c.used) {
+                string sq = consensus(*s3);
+                if (sq.compare(0, ml, mnt) == 0 && (int)sq.size() >= ml &&
+                    ((int)sq.size() == ml || ismatchref(sq.substr(ml), position + ml, 1))) {
+                    add_into(pm.keys[vn], s3->c.agg);
+                    add_cov(position, s3->c.agg.cnt);
+                    s3->c.used = true;
+                }
+            }
+            Clip *s5 = clip(sc5, position + ml);
+            if (s5 && !s5->c.used) {
+                string sq = consensus(*s5);
+                if (sq != " " && (int)sq.size() >= ml) {
+                    std::reverse(sq.begin(), sq.end());
+                    if (sq.substr(sq.size() - ml, ml) == mnt &&
+                        ((int)sq.size() == ml || ismatchref(sq.substr(0, sq.size() - ml), position - 1, -1))) {
+                        add_into(pm.keys[vn], s5->c.agg);
+                        add_cov(position, s5->c.agg.cnt);
+                        s5->c.used = true;
+                    }
+                }
+            }
+        }
+    }
+    // ismatchref: src/VariationRealigner.cpp:2004-2024 (MM = 3)
+    bool ismatchref(const string &sq, int position, int dir) {
+        int mm = 0, len = (int)sq.size();
+        for (int n = 0; n < len; n++) {
+            if (!R.has(position + dir * n)) return false;
+            char c = dir == 1 ? sq[n] : sq[len - n - 1];
+            if (c != R.idx(position + dir * n)) mm++;
+        }
+        return mm <= 3 && mm / (double)len < 0.15;
+    }
+
+    // ------------------------------------------------------------------
+    // indel passes
+    // ------------------------------------------------------------------
+    struct Mism { string seq; int pos; int end; };
+    struct MmResult { std::vector<Mism> mm; std::vector<int> scp; int nm = 0, misp = 0; string misnt; };
+
+    // findMM5 (:1857-1916)
+    MmResult find_mm5(int position, const string &wupseq) {
+        string seq = drop_hash_caret(wupseq);
+        MmResult r;
+        int n = 0, mcnt = 0;
+        string str;
+        while (R.has_ne(char_at(seq, -1 - n), position - n) && mcnt < 3) {
+            str.insert(0, 1, char_at(seq, -1 - n));
+            r.mm.push_back({str, position - n, 5});
+            n++;
+            mcnt++;
+        }
+        r.scp.push_back(position + 1);
+        if (str.size() == 1) {
+            while (R.has_eq(char_at(seq, -1 - n), position - n)) {
+                n++;
+                if (n != 0) r.nm++;
+            }
+            if (r.nm > 1) {
+                // the reference's second scan (-1 - n - 1 - n2 >= 0) never runs
+                r.scp.push_back(position - n);
+                if (Clip *k = clip(sc5, position - n)) k->c.used = true;
+            }
+        }
+        return r;
+    }
+    // findMM3 (:1919-1984)
+    MmResult find_mm3(int p, const string &sanpseq) {
+        string seq = drop_hash_caret(sanpseq);
+        MmResult r;
+        int n = 0, mcnt = 0, len = (int)seq.size();
+        string str;
+        while (n < len && R.has(p + n) && R.at(p + n) == seq[n]) n++;
+        r.scp.push_back(p + n);
+        const int tbp = p + n;
+        while (mcnt <= 3 && n < len && R.idx(p + n) != seq[n]) {
+            str += seq[n];
+            r.mm.push_back({str, tbp, 3});
+            n++;
+            mcnt++;
+        }
+        if (str.size() == 1) {
+            while (n < len && R.has_eq(seq[n], p + n)) {
+                n++;
+                if (n != 0) r.nm++;
+            }
+            if (r.nm > 1) {
+                int n2 = 0;
+                while (n + n2 + 1 < len && R.has_eq(seq[n + n2 + 1], p + n + 1 + n2)) n2++;
+                if (n2 > 2 && n + n2 + 1 < len) {
+                    r.scp.push_back(p + n + n2);
+                    r.misp = p + n;
+                    r.misnt = string(1, seq[n]);
+                    if (Clip *k = clip(sc3, p + n + n2)) k->c.used = true;
+                    r.nm += n2;
+                } else {
+                    r.scp.push_back(p + n);
+                    if (Clip *k = clip(sc3, p + n)) k->c.used = true;
+                }
+            }
+        }
+        return r;
+    }
+    // ismatch (:1507-1546), MM = 3
+    static bool ismatch(const string &seq1, const string &seq2_in, int dir) {
+        string seq2 = drop_hash_caret(seq2_in);
+        int mm = 0;
+        for (int n = 0; n < (int)seq1.size() && n < (int)seq2.size(); n++)
+            if (seq1[n] != vsub(seq2, dir * n - (dir == -1 ? 1 : 0), 1)[0]) mm++;
+        return mm <= 3 && mm / (double)seq1.size() < 0.15;
+    }
+    // adjRefCnt (:1753-1787)
+    static void adj_ref_cnt(const HVar &tv, HVar *ref, int len) {
+        if (!ref) return;
+        double f = tv.tp != 0 ? (tv.tp / (double)tv.cnt - len + 1) / (tv.tp / (double)tv.cnt) : 0;
+        if (f < 0) return;
+        if (f > 1) f = 1;
+        ref->cnt -= (int)(f * tv.cnt);
+        ref->hi -= (int)(f * tv.hi);
+        ref->lo -= (int)(f * tv.lo);
+        ref->tp -= f * tv.tp;
+        ref->q -= f * tv.q;
+        ref->mq -= f * tv.mq;
+        ref->nm -= f * tv.nm;
+        ref->rev -= (int)(f * tv.rev);
+        ref->fwd -= (int)(f * tv.fwd);
+        clamp_counts(*ref);
+    }
+    // adjRefFactor (:1794-1822)
+    static void adj_ref_factor(HVar *ref, double f) {
+        if (!ref) return;
+        if (f > 1) f = 1;
+        if (f < -1) return;
+        int old = ref->cnt;
+        ref->cnt -= (int)(f * ref->cnt);
+        ref->hi -= (int)(f * ref->hi);
+        ref->lo -= (int)(f * ref->lo);
+        double fc = old != 0 ? std::abs(ref->cnt - old) / (double)old : 1;
+        ref->tp -= ref->tp * f * fc;
+        ref->q -= ref->q * f * fc;
+        ref->mq -= ref->mq * f * fc;
+        ref->nm -= f * ref->nm;
+        ref->fwd -= (int)(f * ref->fwd);
+        ref->rev -= (int)(f * ref->rev);
+        clamp_counts(*ref);
+    }
+    // noPassingReads (:1447-1505): the batch's records over start..end, unfiltered
+    bool no_passing_reads(int start, int end) {
+        const rv_ctx *c = ctx;
+        int cnt = 0;
+        const uint32_t dlen = ((uint32_t)(end - start) << 4) | 2u;
+        const int64_t n = (int64_t)c->h_pos.size();
+        int64_t lo = std::lower_bound(c->h_pos.begin(), c->h_pos.end(), start - 1 - 4096) - c->h_pos.begin();
+        for (int64_t i = lo; i < n && c->h_pos[i] < end; i++) {
+            const uint32_t *cg = c->h_cigar.data() + c->h_cigoff[i];
+            int span = 0, aligned = 0;
+            bool has_d = false;
+            for (int k = 0; k < c->h_ncig[i]; k++) {
+                int o = cg[k] & 15;
+                if (o == 0 || o == 2 || o == 3 || o == 7 || o == 8) span += (int)(cg[k] >> 4);
+                if (o == 0 || o == 2) aligned += (int)(cg[k] >> 4);
+                if (cg[k] == dlen) has_d = true;
+            }
+            int endpos = ((c->h_flag[i] & 4) || span == 0) ? c->h_pos[i] + 1 : c->h_pos[i] + span;
+            if (endpos <= start - 1) continue;
+            if (has_d) continue;
+            int rs0 = c->h_pos[i] + 1, re0 = rs0 + aligned;
+            if (re0 > end + 2 && rs0 < start - 2) cnt++;
+        }
+        return cnt <= 0;
+    }
+
+    struct Cand { int pos; string key; int cnt; };
+    static std::vector<Cand> sorted(const std::map<int, std::map<string, int>> &ch) {  // CMP_tmp (:1362-1386)
+        std::vector<Cand> t;
+        for (auto &pe : ch)
+            for (auto &ke : pe.second) t.push_back({pe.first, ke.first, ke.second});
+        std::sort(t.begin(), t.end(), [](const Cand &a, const Cand &b) {
+            if (a.cnt != b.cnt) return a.cnt > b.cnt;
+            if (a.pos != b.pos) return a.pos < b.pos;
+            return a.key.compare(b.key) > 0;
+        });
+        return t;
+    }
+
+    // the leading number of a key ("-12..." -> 12), or -1
+    static int lead_num(const string &s, size_t from) {
+        size_t i = from;
+        int v = 0;
+        bool any = false;
+        while (i < s.size() && s[i] >= '0' && s[i] <= '9') { v = v * 10 + (s[i] - '0'); i++; any = true; }
+        return any ? v : -1;
+    }
+    static bool all_bases(const string &s, const char *alphabet) {
+        if (s.empty()) return false;
+        for (char c : s)
+            if (!strchr(alphabet, c)) return false;
+        return true;
+    }
+    // "^<digits>" at the end of the key: the digits, or -1
+    static int tail_caret_num(const string &s) {
+        size_t i = s.size();
+        while (i > 0 && s[i - 1] >= '0' && s[i - 1] <= '9') i--;
+        if (i == s.size() || i == 0 || s[i - 1] != '^') return -1;
+        return atoi(s.c_str() + i);
+    }
+
+    // realigndel (:489-775)
+    void realigndel(bool with_reads, const std::map<int, std::map<string, int>> &dcnt_map) {
+        std::vector<Cand> tmp = sorted(dcnt_map);
+        for (const Cand &tpl : tmp) {
+            try {
+                const int p = tpl.pos;
+                const string &vn = tpl.key;
+                const int dcnt = tpl.cnt;
+                HVar &vref = nget(p, vn);
+                int dellen = 0;
+                if (vn.size() > 1 && vn[0] == '-') {
+                    int d = lead_num(vn, 1);
+                    if (d >= 0) dellen = d;
+                }
+                int tc = tail_caret_num(vn);
+                if (tc >= 0) dellen += tc;
+                string extrains, extra, inv5, inv3;
+                std::smatch m;
+                static const std::regex re_inv("^-\\d+\\^([ATGNC]+)<...\\d+>([ATGNC]+)$");
+                static const std::regex re_rest("^-\\d+(.*)");
+                static const std::regex re_ins("\\^([ATGNC]+)");
+                if (std::regex_search(vn, m, re_inv)) {
+                    inv5 = m.str(1);
+                    inv3 = m.str(2);
+                } else if (std::regex_search(vn, m, re_rest)) {
+                    for (char c : m.str(1))
+                        if (c != '^' && c != '&' && c != '#') extra += c;
+                    if (std::regex_search(vn, m, re_ins)) extrains = m.str(1);
+                }
+                const int wustart = p - 200 > 1 ? p - 200 : 1;
+                string wupseq = join_ref(R, wustart, p - 1) + extra;
+                if (!inv3.empty()) wupseq = inv3;
+                const int sanend = p + 200 > chr_len ? chr_len : p + 200;
+                const int off = dellen + (int)extra.size() - (int)extrains.size();
+                string sanpseq = extra + join_ref(R, p + off, sanend);
+                if (!inv5.empty()) sanpseq = inv5;
+                MmResult r3 = find_mm3(p, sanpseq);
+                MmResult r5 = find_mm5(p + off - 1, wupseq);
+                std::vector<Mism> mmm = r3.mm;
+                mmm.insert(mmm.end(), r5.mm.begin(), r5.mm.end());
+                for (Mism &mi : mmm) {
+                    string mm = mi.seq;
+                    if (mm.size() > 1) mm.insert(1, 1, '&');
+                    const int mp = mi.pos, me = mi.end;
+                    if (!has_key(mp, mm)) continue;
+                    HVar &tv = N(mp).keys.at(mm);
+                    if (tv.cnt == 0) continue;
+                    if (tv.q / tv.cnt < P.goodq) continue;
+                    if (tv.tp / tv.cnt > (me == 3 ? r3.nm + 4 : r5.nm + 4)) continue;
+                    if (tv.cnt >= dcnt + dellen || tv.cnt / dcnt >= 8) continue;
+                    if (mp > p && me == 5) {
+                        double f = tv.tp != 0 ? (mp - p) / (tv.tp / (double)tv.cnt) : 1;
+                        if (f > 1) f = 1;
+                        add_cov(p, (int)(tv.cnt * f));
+                        char b = R.idx(p);
+                        adj_ref_cnt(tv, maybe(p, b), dellen);
+                    }
+                    HVar *lref = nullptr;
+                    if (mp > p && me == 3 && N(p).present) {
+                        char b = R.idx(p);
+                        lref = nfind(p, string(1, b));
+                    }
+                    if (lref) add_sub(vref, tv, lref);
+                    else add_into(vref, tv);
+                    nerase_drop(mp, mm);
+                }
+                if (r3.misp != 0 && r3.mm.size() == 1 && has_key(r3.misp, r3.misnt) &&
+                    N(r3.misp).keys.at(r3.misnt).cnt < dcnt)
+                    N(r3.misp).keys.erase(r3.misnt);
+                if (r5.misp != 0 && r5.mm.size() == 1 && has_key(r5.misp, r5.misnt) &&
+                    N(r5.misp).keys.at(r5.misnt).cnt < dcnt)
+                    N(r5.misp).keys.erase(r5.misnt);
+                for (int sc5pp : r5.scp) {
+                    Clip *k = clip(sc5, sc5pp);
+                    if (!k || k->c.used) continue;
+                    string seq = consensus(*k);
+                    if (dcnt <= 2 && k->c.agg.cnt / dcnt > 5) continue;
+                    if (seq != " " && ismatch(seq, wupseq, -1)) {
+                        if (sc5pp > p) add_cov(p, k->c.agg.cnt);
+                        add_into(vref, k->c.agg);
+                        k->c.used = true;
+                    }
+                }
+                for (int sc3pp : r3.scp) {
+                    Clip *k = clip(sc3, sc3pp);
+                    if (!k || k->c.used) continue;
+                    string seq = consensus(*k);
+                    if (dcnt <= 2 && k->c.agg.cnt / dcnt > 5) continue;
+                    if (seq != " " && ismatch(seq, vsub(sanpseq, sc3pp - p), 1)) {
+                        if (sc3pp <= p) add_cov(p, k->c.agg.cnt);
+                        HVar *lref = nullptr;
+                        if (sc3pp > p) {
+                            char b = R.idx(p);
+                            lref = maybe(p, b);
+                        }
+                        add_sub(vref, k->c.agg, lref);
+                        k->c.used = true;
+                    }
+                }
+                const int pe = p + off;
+                char b = R.idx(p);
+                HVar *h = maybe(p, b);
+                if (with_reads && pe - p >= 5 && pe - p < max_rl - 10 && h && h->cnt != 0 &&
+                    vref.cnt > 2 * h->cnt * (1 - (pe - p) / (double)max_rl) && no_passing_reads(p, pe))
+                    add_sub(vref, *h, h);
+            } catch (const RefFail &) {
+            } catch (const OutOfRange &) {
+            }
+        }
+        static const std::regex re_tail("(-\\d+)&[ATGC]+$");
+        for (int i = (int)tmp.size() - 1; i > 0; i--) {
+            const int p = tmp[i].pos;
+            const string &vn = tmp[i].key;
+            if (!has_key(p, vn)) continue;
+            HVar &vref = N(p).keys.at(vn);
+            std::smatch m;
+            if (std::regex_search(vn, m, re_tail)) {
+                string tn = m.str(1);
+                auto &keys = N(p).keys;
+                auto t = keys.find(tn);
+                if (t != keys.end() && vref.cnt < t->second.cnt) {
+                    add_into(t->second, vref);
+                    keys.erase(vn);
+                }
+            }
+        }
+    }
+
+    // realignins (:785-1114)
+    void realignins(const std::map<int, std::map<string, int>> &icnt_map) {
+        std::vector<Cand> tmp = sorted(icnt_map);
+        static const std::regex re_ins1("^\\+([ATGC]+).*");
+        static const std::regex re_dup("<dup(\\d+)>([ATGC]+)$");
+        static const std::regex re_extra(".*&([ATGC]+).*");
+        static const std::regex re_compm("#([ATGC]+).*");
+        static const std::regex re_newdel("\\^(\\d+)$");
+        static const std::regex re_caretnum("\\^\\d+$");
+        static const std::regex re_caret("\\^");
+        for (const Cand &tpl : tmp) {
+            try {
+                const int position = tpl.pos;
+                const string &vn = tpl.key;
+                const int icnt = tpl.cnt;
+                std::smatch m;
+                string insert1;
+                if (std::regex_search(vn, m, re_ins1)) insert1 = m.str(1);
+                else continue;
+                string ins3;
+                int inslen = (int)insert1.size();
+                if (std::regex_search(vn, m, re_dup)) {
+                    ins3 = m.str(2);
+                    inslen += atoi(m.str(1).c_str()) + (int)ins3.size();
+                }
+                string extra, compm;
+                if (std::regex_search(vn, m, re_extra)) extra = m.str(1);
+                if (std::regex_search(vn, m, re_compm)) compm = m.str(1);
+                int newdel = 0;
+                if (std::regex_search(vn, m, re_newdel)) newdel = atoi(m.str(1).c_str());
+                string tn = vn;
+                if (!tn.empty() && tn[0] == '+') tn.erase(0, 1);
+                replace_first(tn, "&", "");
+                replace_first(tn, "#", "");
+                tn = std::regex_replace(tn, re_caretnum, "", std::regex_constants::format_first_only);
+                tn = std::regex_replace(tn, re_caret, "", std::regex_constants::format_first_only);
+                const int wustart = position - 150 > 1 ? position - 150 : 1;
+                string wupseq = join_ref(R, wustart, position) + tn;
+                int sanend = position + (int)vn.size() + 100;
+                if (chr_len < sanend) sanend = chr_len;
+                string sanpseq;
+                MmResult r3;
+                if (!ins3.empty()) {
+                    int p3 = position + inslen - (int)ins3.size() + 50;
+                    if ((int)ins3.size() > 50) sanpseq = vsub(ins3, 50 - (int)ins3.size());
+                    sanpseq += join_ref(R, position + 1, position + 101);
+                    r3 = find_mm3(p3 + 1, sanpseq);
+                } else {
+                    sanpseq = tn + join_ref(R, position + (int)extra.size() + 1 + (int)compm.size() + newdel, sanend);
+                    r3 = find_mm3(position + 1, sanpseq);
+                }
+                MmResult r5 = find_mm5(position + (int)extra.size() + (int)compm.size() + newdel, wupseq);
+                std::vector<Mism> mmm = r3.mm;
+                mmm.insert(mmm.end(), r5.mm.begin(), r5.mm.end());
+                HVar &vref = iget(position, vn);
+                for (Mism &mi : mmm) {
+                    string mb = mi.seq;
+                    if (mb.size() > 1) mb = string(1, mb[0]) + "&" + mb.substr(1);
+                    const int mp = mi.pos, me = mi.end;
+                    if (!has_key(mp, mb)) continue;
+                    HVar &var = N(mp).keys.at(mb);
+                    if (var.cnt == 0) continue;
+                    if (var.q / var.cnt < P.goodq) continue;
+                    if (var.tp / var.cnt > (me == 3 ? r3.nm + 4 : r5.nm + 4)) continue;
+                    if (var.cnt >= icnt + (int)insert1.size() || var.cnt / icnt >= 8) continue;
+                    if (mp > position && me == 5) add_cov(position, var.cnt);
+                    HVar *lref = nullptr;
+                    if (mp > position && me == 3 && N(position).present && R.has(position)) {
+                        char b = R.idx(position);
+                        lref = nfind(position, string(1, b));
+                    }
+                    if (lref) add_sub(vref, var, lref);
+                    else add_into(vref, var);
+                    nerase_drop(mp, mb);
+                }
+                if (r3.misp != 0 && r3.mm.size() == 1 && has_key(r3.misp, r3.misnt) &&
+                    N(r3.misp).keys.at(r3.misnt).cnt < icnt)
+                    N(r3.misp).keys.erase(r3.misnt);
+                if (r5.misp != 0 && r5.mm.size() == 1 && has_key(r5.misp, r5.misnt) &&
+                    N(r5.misp).keys.at(r5.misnt).cnt < icnt)
+                    N(r5.misp).keys.erase(r5.misnt);
+                for (int sc5pp : r5.scp) {
+                    Clip *k = clip(sc5, sc5pp);
+                    if (!k || k->c.used) continue;
+                    string seq = consensus(*k);
+                    if (seq != " " && ismatch(seq, wupseq, -1)) {
+                        if (sc5pp > position) add_cov(position, k->c.agg.cnt);
+                        add_into(vref, k->c.agg);
+                        k->c.used = true;
+                    }
+                }
+                for (int sc3pp : r3.scp) {
+                    Clip *k = clip(sc3, sc3pp);
+                    if (!k || k->c.used) continue;
+                    string seq = consensus(*k);
+                    string mseq = !ins3.empty() ? sanpseq : vsub(sanpseq, sc3pp - position - 1);
+                    if (seq != " " && ismatch(seq, mseq, 1)) {
+                        const HVar &tv = k->c.agg;
+                        if (sc3pp <= position || (int)insert1.size() > tv.tp / tv.cnt) add_cov(position, tv.cnt);
+                        HVar *lref = nullptr;
+                        if (sc3pp > position && N(position).present && R.has(position)) {
+                            char b = R.idx(position);
+                            lref = nfind(position, string(1, b));
+                        }
+                        if ((int)insert1.size() > tv.tp / tv.cnt) lref = nullptr;
+                        add_sub(vref, tv, lref);
+                        k->c.used = true;
+                        if (insert1.size() + 1 == vn.size() && (int)insert1.size() > max_rl &&
+                            sc3pp >= position + 1 + (int)insert1.size()) {
+                            int flag = 0;
+                            int offset = (sc3pp - position - 1) % (int)insert1.size();
+                            string tvn = vn;
+                            for (int si = 0; si < (int)seq.size() && si + offset < (int)insert1.size(); si++) {
+                                if (vsub(seq, si, 1) != vsub(insert1, si + offset, 1)) {
+                                    flag++;
+                                    int shift = si + offset + 1;
+                                    tvn = tvn.substr(0, shift) + vsub(seq, si, 1) + tvn.substr(shift + 1);
+                                }
+                            }
+                            if (flag > 0) {
+                                HVar moved = iget(position, vn);
+                                iget(position, tvn) = moved;
+                                I(position).keys.erase(vn);
+                            }
+                        }
+                    }
+                }
+                if (!r3.scp.empty() && !r5.scp.empty()) {
+                    int first3 = r3.scp[0], first5 = r5.scp[0];
+                    if (first3 > first5 + 3 && first3 - first5 < max_rl * 0.75) {
+                        if (R.has(position) && N(position).present) {
+                            char b = R.idx(position);
+                            HVar *h = nfind(position, string(1, b));
+                            if (h) adj_ref_factor(h, (first3 - first5 - 1) / (double)max_rl);
+                        }
+                        adj_ref_factor(&vref, -(first3 - first5 - 1) / (double)max_rl);
+                    }
+                }
+            } catch (const RefFail &) {
+            } catch (const OutOfRange &) {
+            }
+        }
+        static const std::regex re_tail("(\\+[ATGC]+)&[ATGC]+$");
+        for (int i = (int)tmp.size() - 1; i > 0; i--) {
+            const int p = tmp[i].pos;
+            const string &vn = tmp[i].key;
+            PosMap &im = I(p);
+            if (!im.present || !im.keys.count(vn)) continue;
+            HVar &vref = im.keys.at(vn);
+            std::smatch m;
+            if (std::regex_search(vn, m, re_tail)) {
+                string tn = m.str(1);
+                auto t = im.keys.find(tn);
+                if (t != im.keys.end() && vref.cnt < t->second.cnt) {
+                    char b = R.idx(p);
+                    add_sub(t->second, vref, maybe(p, b));
+                    im.keys.erase(vn);
+                }
+            }
+        }
+    }
+
+    // find35match (:1396-1428)
+    static void find35(const string &s5, const string &s3, int &b5, int &b3, int &score) {
+        b5 = b3 = score = 0;
+        for (int i = 0; i < (int)s5.size() - 8; i++) {
+            for (int j = 1; j < (int)s3.size() - 8; j++) {
+                int nm = 0, n = 0;
+                while (n + j <= (int)s3.size() && i + n <= (int)s5.size()) {
+                    if (vsub(s3, -j - n, 1) != vsub(s5, i + n, 1)) nm++;
+                    if (nm > 2) break;
+                    n++;
+                }
+                if (n - nm > score && n - nm > 8 && nm / (double)n < 0.1 &&
+                    (n + j >= (int)s3.size() || i + n >= (int)s5.size())) {
+                    b5 = i;
+                    b3 = j;
+                    score = n - nm;
+                    return;
+                }
+            }
+        }
+    }
+
+    // realignlgins30 (:1119-1350); its reference map is a copy (lookups that
+    // insert stay local), the nested realignins/realigndel use the shared one
+    void realignlgins30() {
+        PRef RL = R;
+        struct T { int pos; Clip *c; int cnt; };
+        std::vector<T> t5, t3;
+        for (auto &e : sc5)
+            if (!(e.first < Rg.start - 5000 || e.first > Rg.end + 5000)) t5.push_back({e.first, &e.second, e.second.c.agg.cnt});
+        for (auto &e : sc3)
+            if (!(e.first < Rg.start - 5000 || e.first > Rg.end + 5000)) t3.push_back({e.first, &e.second, e.second.c.agg.cnt});
+        auto by_cnt = [](const T &a, const T &b) { return a.cnt != b.cnt ? a.cnt > b.cnt : a.pos < b.pos; };
+        std::sort(t5.begin(), t5.end(), by_cnt);
+        std::sort(t3.begin(), t3.end(), by_cnt);
+        for (T &a : t5) {
+            const int p5 = a.pos;
+            Clip &sc5v = *a.c;
+            const int cnt5 = a.cnt;
+            if (sc5v.c.used) continue;
+            string seq5 = consensus(sc5v);
+            if (seq5.size() <= 10) continue;
+            for (T &b : t3) {
+                try {
+                    const int p3 = b.pos;
+                    Clip &sc3v = *b.c;
+                    const int cnt3 = b.cnt;
+                    if (sc5v.c.used) break;
+                    if (sc3v.c.used) continue;
+                    if (p5 - p3 > max_rl * 2.5) continue;
+                    if (p3 - p5 > max_rl - 10) continue;
+                    string seq3 = consensus(sc3v);
+                    if (seq3.size() <= 10) continue;
+                    if (!(cnt5 / (double)cnt3 >= 0.08 && cnt5 / (double)cnt3 <= 12)) continue;
+                    int bp5, bp3, score;
+                    find35(seq5, seq3, bp5, bp3, score);
+                    if (score == 0) continue;
+                    const int sm = score / 2;
+                    string ins = bp3 + sm > 1 ? vsub(seq3, 0, -(bp3 + sm) + 1) : seq3;
+                    if (bp5 + sm > 0) {
+                        string tt = seq5.substr(0, bp5 + sm);
+                        std::reverse(tt.begin(), tt.end());
+                        ins += tt;
+                    }
+                    if (low_complexity(ins)) continue;
+                    int bi = 0;
+                    HVar *vref;
+                    const int il = (int)ins.size();
+                    if ((int)seq3.size() > il &&
+                        !ismatch(seq3.substr(il), join_ref(RL, p5, p5 + (int)seq3.size() - il + 2), 1))
+                        continue;
+                    if ((int)seq5.size() > il &&
+                        !ismatch(seq5.substr(il), join_ref(RL, p3 - ((int)seq5.size() - il) - 2, p3 - 1), -1))
+                        continue;
+                    if (p5 > p3) {
+                        string tmp = join_ref(RL, p3, p5 - 1);
+                        if (tmp.size() > ins.size()) {
+                            ins = std::to_string(p3 - p5) + "^" + ins;
+                            bi = p3;
+                            vref = &nget(p3, ins);
+                        } else if (tmp.size() < ins.size()) {
+                            ins = vsub(ins, 0, (int)ins.size() - (int)tmp.size()) + "&" + vsub(ins, p3 - p5);
+                            ins = "+" + ins;
+                            bi = p3 - 1;
+                            vref = &iget(bi, ins);
+                        } else {
+                            ins = "-" + std::to_string(ins.size()) + "^" + ins;
+                            bi = p3;
+                            vref = &nget(p3, ins);
+                        }
+                    } else {
+                        string tmp;
+                        if ((int)ins.size() <= p3 - p5) {
+                            int rpt = 2, tnr = 3;
+                            const int tot = p3 - p5 + (int)ins.size();
+                            while ((tot / (double)tnr) / (double)ins.size() > 1) {
+                                if (tot % tnr == 0) rpt++;
+                                tnr++;
+                            }
+                            const double to = p5 + tot / (double)rpt - ins.size();
+                            for (int i = p5; i < to; i++) {  // joinRef_double: include/VariationUtils.h:343-349
+                                if (!RL.has(i)) throw RefFail();
+                                tmp += RL.at(i);
+                            }
+                            ins = "+" + tmp + ins;
+                        } else {
+                            tmp += join_ref(RL, p5, p3 - 1);
+                            if ((ins.size() - tmp.size()) % 2 == 0) {
+                                int tex = (int)(ins.size() - tmp.size()) / 2;
+                                ins = (tmp + vsub(ins, 0, tex)) == vsub(ins, tex) ? "+" + vsub(ins, tex) : "+" + tmp + ins;
+                            } else {
+                                ins = "+" + tmp + ins;
+                            }
+                        }
+                        bi = p5 - 1;
+                        vref = &iget(bi, ins);
+                    }
+                    sc3v.c.used = true;
+                    sc5v.c.used = true;
+                    vref->pstd = true;
+                    vref->qstd = true;
+                    add_cov(bi, sc5v.c.agg.cnt);
+                    if (ins[0] == '+') {
+                        char rb = RL.idx(bi);
+                        HVar *mvref = maybe(bi, rb);
+                        add_sub(*vref, sc3v.c.agg, mvref);
+                        add_into(*vref, sc5v.c.agg);
+                        if (p3 - p5 >= 5 && p3 - p5 < max_rl - 10 && mvref && mvref->cnt != 0 &&
+                            vref->cnt > 2 * mvref->cnt && no_passing_reads(p5, p3))
+                            add_sub(*vref, *mvref, mvref);
+                        std::map<int, std::map<string, int>> tins;
+                        tins[bi][ins] = vref->cnt;
+                        realignins(tins);
+                    } else if (ins[0] == '-') {
+                        char rb = RL.idx(bi);
+                        add_sub(*vref, sc3v.c.agg, maybe(bi, rb));
+                        add_into(*vref, sc5v.c.agg);
+                        std::map<int, std::map<string, int>> tdel;
+                        tdel[bi][ins] = vref->cnt;
+                        realigndel(false, tdel);
+                    } else {
+                        add_into(*vref, sc3v.c.agg);
+                        add_into(*vref, sc5v.c.agg);
+                    }
+                    break;
+                } catch (const RefFail &) {
+                } catch (const OutOfRange &) {
+                }
+            }
+        }
+    }
+
+    // ------------------------------------------------------------------
+    // diff of the mirror against its snapshots -> patches
+    // ------------------------------------------------------------------
+    void stats_into(Patch &q, const HVar &h) {
+        q.fwd = h.fwd;
+        q.rev = h.rev;
+        q.hi = h.hi;
+        q.lo = h.lo;
+        q.extracnt = h.extracnt;
+        q.cnt = h.cnt;
+        q.tp = h.tp;
+        q.q_sum = h.q;
+        q.mq = h.mq;
+        q.nm = h.nm;
+        q.flags_or = (h.pstd ? (int)SF_PDIFF : 0) | (h.qstd ? (int)SF_QDIFF : 0);
+    }
+    void diff(std::vector<Patch> &out, string &keys) {
+        auto blank = [] {
+            Patch q;
+            memset(&q, 0, sizeof q);
+            return q;
+        };
+        auto create = [&](int p, int kind, const string &k, const HVar &h) {
+            Patch q = blank();
+            q.type = 5;
+            q.region = region;
+            q.pos = p;
+            q.kind = kind;
+            q.klen = (int)k.size();
+            q.key_off = (int64_t)keys.size();
+            keys += k;
+            stats_into(q, h);
+            out.push_back(q);
+        };
+        for (int pass = 0; pass < 2; pass++) {
+            auto &cur = pass ? ins : nonins;
+            auto &orig = pass ? ins0 : nonins0;
+            const int kind = pass ? KIND_INS : KIND_NONINS;
+            for (auto &pe : cur) {
+                const int p = pe.first;
+                if (!in_cells(p)) continue;
+                const int64_t c = cell_of(p);
+                const PosMap &F = pe.second, &O = orig.at(p);
+                if (!pass && O.present && !F.present) {
+                    // the entry left the map: its cell keys go and every slot
+                    // of the position stops counting as an entry
+                    Patch q = blank();
+                    q.type = 6;
+                    q.target = c;
+                    out.push_back(q);
+                    auto s = mir.nonins_at.find(pos_key(region, p));
+                    if (s != mir.nonins_at.end())
+                        for (uint32_t i : s->second) {
+                            Patch e = blank();
+                            e.type = 1;
+                            e.target = mir.sidx[i];
+                            e.flags_or = (int)SF_NOMAP;
+                            out.push_back(e);
+                        }
+                    continue;
+                }
+                for (auto &oe : O.keys) {
+                    if (F.keys.count(oe.first)) continue;
+                    Patch q = blank();
+                    if (oe.second.slot >= 0) {
+                        q.type = 1;
+                        q.target = oe.second.slot;
+                    } else {
+                        q.type = 2;
+                        q.target = oe.second.cell;
+                        q.base = oe.second.base;
+                    }
+                    out.push_back(q);
+                }
+                for (auto &fe : F.keys) {
+                    auto o = O.keys.find(fe.first);
+                    if (o != O.keys.end() && same_stats(o->second, fe.second)) continue;
+                    if (o != O.keys.end() && o->second.slot >= 0) {
+                        Patch q = blank();
+                        q.type = 4;
+                        q.target = o->second.slot;
+                        stats_into(q, fe.second);
+                        out.push_back(q);
+                        continue;
+                    }
+                    create(p, kind, fe.first, fe.second);
+                    if (o != O.keys.end()) {  // a cell key moves to a slot
+                        Patch q = blank();
+                        q.type = 2;
+                        q.target = o->second.cell;
+                        q.base = o->second.base;
+                        out.push_back(q);
+                    }
+                }
+            }
+        }
+        for (auto &ce : cov_add) {
+            if (!in_cells(ce.first) || ce.second == 0) continue;
+            Patch q = blank();
+            q.type = 3;
+            q.target = cell_of(ce.first);
+            q.cov_add = ce.second;
+            out.push_back(q);
+        }
+    }
+
+    void run(std::vector<Patch> &out, string &keys) {
+        load_clips();
+        std::map<int, std::map<string, int>> mnp, delcnt, inscnt;
+        for (int kind = 0; kind < 2; kind++) {
+            auto &idx = kind ? mir.ins_at : mir.nonins_at;
+            for (int p = Rg.clo; p <= Rg.chi; p++) {
+                auto it = idx.find(pos_key(region, p));
+                if (it == idx.end()) continue;
+                for (uint32_t i : it->second) {
+                    const Slot &s = mir.slots[i];
+                    if (s.obs <= 0) continue;
+                    string k = mir.key(i);
+                    if (kind) inscnt[p][k] = s.obs;
+                    else if (is_mnv(k)) mnp[p][k] = s.obs;
+                    else if (!k.empty() && k[0] == '-') delcnt[p][k] = s.obs;
+                }
+            }
+        }
+        adjust_mnp(mnp);
+        realigndel(true, delcnt);
+        realignins(inscnt);
+        realignlgins30();
+        diff(out, keys);
+    }
+};
+
+}  // namespace
+
+// VariationRealigner::process with -k 1 (src/VariationRealigner.cpp:135-161)
+rv_status host_realign_full(rv_ctx *ctx) {
+    Mirror mir;
+    mir.ctx = ctx;
+    rv_status st = fetch_slots(ctx, mir.slots, mir.sidx);
+    if (st) return st;
+    ctx->kernels += mir.slots.empty() ? 1 : 2;
+    ctx->io_d2h += (int64_t)(mir.slots.size() * (sizeof(Slot) + 4) + ctx->h_arena.size());
+    mir.regions.resize(ctx->regions.size());
+    if (!mir.regions.empty())
+        HCUDA(cudaMemcpy(mir.regions.data(), ctx->d_regions, mir.regions.size() * sizeof(Region),
+                         cudaMemcpyDeviceToHost));
+    for (uint32_t i = 0; i < (uint32_t)mir.slots.size(); i++) {
+        const Slot &s = mir.slots[i];
+        if (s.region < 0 || s.region >= (int)mir.regions.size()) continue;
+        uint64_t k = pos_key(s.region, s.pos);
+        switch (s.kind) {
+        case KIND_NONINS: mir.nonins_at[k].push_back(i); break;
+        case KIND_INS: mir.ins_at[k].push_back(i); break;
+        case KIND_SC5: case KIND_SC5_SEQ: mir.sc5_at[k].push_back(i); break;
+        case KIND_SC3: case KIND_SC3_SEQ: mir.sc3_at[k].push_back(i); break;
+        default: break;
+        }
+    }
+    // prefetch the cell blocks around every realigner candidate
+    std::set<int64_t> want;
+    auto around = [&](int region, int p, int margin) {
+        const Region &R = mir.regions[region];
+        int a = std::max(R.clo, p - margin), b = std::min(R.chi, p + margin);
+        if (a > b) return;
+        for (int64_t blk = (R.cell_base + (a - R.clo)) / kBlock; blk <= (R.cell_base + (b - R.clo)) / kBlock; blk++)
+            want.insert(blk);
+    };
+    for (uint32_t i = 0; i < (uint32_t)mir.slots.size(); i++) {
+        const Slot &s = mir.slots[i];
+        if (s.region < 0 || s.region >= (int)mir.regions.size()) continue;
+        const int mrl = std::max(1, mir.regions[s.region].max_read_len);
+        if (s.kind == KIND_NONINS || s.kind == KIND_INS) {
+            if (s.klen >= 2 && s.obs > 0) around(s.region, s.pos, 320 + 2 * s.klen);
+        } else if (s.kind == KIND_SC5 || s.kind == KIND_SC3) {
+            around(s.region, s.pos, 400 + 3 * mrl);
+        }
+    }
+    if ((st = mir.fetch_blocks(std::vector<int64_t>(want.begin(), want.end())))) return st;
+    // regions in parallel; patches concatenated in region order
+    const int nreg = (int)ctx->regions.size();
+    std::vector<std::vector<Patch>> patches((size_t)nreg);
+    std::vector<string> keys((size_t)nreg);
+    unsigned hw = std::thread::hardware_concurrency();
+    int nt = std::max(1, std::min<int>(nreg, (int)std::min(hw ? hw : 1u, 16u)));
+    std::atomic<int> next{0};
+    std::mutex err_mu;
+    string failure;
+    auto work = [&]() {
+        cudaSetDevice(ctx->device);
+        for (int r; (r = next.fetch_add(1)) < nreg;) {
+            try {
+                RegionRealigner rr(mir, ctx, r);
+                rr.run(patches[r], keys[r]);
+            } catch (const std::exception &e) {
+                // the reference's own realigner terminates here (an exception
+                // it does not catch); the batch reports it instead
+                std::lock_guard<std::mutex> g(err_mu);
+                if (failure.empty()) failure = "realigner, region " + std::to_string(r) + ": " + e.what();
+            }
+        }
+    };
+    std::vector<std::thread> th;
+    for (int t = 1; t < nt; t++) th.emplace_back(work);
+    work();
+    for (auto &t : th) t.join();
+    if (mir.failed) return mir.failed;
+    if (!failure.empty()) {
+        ctx->err = failure;
+        return RV_ERR_UNSUPPORTED;
+    }
+    std::vector<Patch> all;
+    string all_keys;
+    for (int r = 0; r < nreg; r++) {
+        for (Patch q : patches[r]) {
+            if (q.type == 5) q.key_off += (int64_t)all_keys.size();
+            all.push_back(q);
+        }
+        all_keys += keys[r];
+    }
+    return apply_patches(ctx, all, all_keys);
+}
+
+}  // namespace rv

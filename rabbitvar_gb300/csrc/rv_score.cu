@@ -120,21 +120,40 @@ __device__ bool cmp_vari(const DevState &st, const V &a, const V &b) {  // CMP_V
     return r > 0;
 }
 
+__device__ __forceinline__ int slot_cnt(const Slot &s) {
+    return (s.flags & SF_OVR) ? s.first_tp : s.fwd + s.rev;
+}
+
 __device__ void load_slot(const Slot &s, int idx, V &v) {
     v.kind = 1;
     v.key = idx;
-    v.cnt = s.fwd + s.rev;
+    v.cnt = slot_cnt(s);
     v.fwd = s.fwd;
     v.rev = s.rev;
     v.hi = s.hi;
     v.lo = s.lo;
     v.extracnt = s.extracnt;
-    v.tp = (double)s.tp_sum;
     v.q = s.q_sum;
-    v.mq = (double)s.mq_sum;
-    v.nm = (double)s.nm_sum;
-    v.pstd = (s.flags & (SF_PDIFF | SF_FORCE_STD)) != 0;
-    v.qstd = (s.flags & (SF_QDIFF | SF_FORCE_STD)) != 0;
+    if (s.flags & SF_OVR) {
+        v.tp = __longlong_as_double(s.tp_sum);
+        v.mq = __longlong_as_double(s.mq_sum);
+        v.nm = __longlong_as_double(s.nm_sum);
+        v.pstd = (s.flags & SF_PDIFF) != 0;
+        v.qstd = (s.flags & SF_QDIFF) != 0;
+    } else {
+        v.tp = (double)s.tp_sum;
+        v.mq = (double)s.mq_sum;
+        v.nm = (double)s.nm_sum;
+        v.pstd = (s.flags & (SF_PDIFF | SF_FORCE_STD)) != 0;
+        v.qstd = (s.flags & (SF_QDIFF | SF_FORCE_STD)) != 0;
+    }
+}
+
+// A single-base key the -k 1 realigner rewrote lives in a slot (its cell key
+// is erased): returns the base 0..3 of such a slot, else -1.
+__device__ __forceinline__ int promoted_base(const DevState &st, const Slot &s) {
+    if (s.kind != KIND_NONINS || s.klen != 1) return -1;
+    return base_index((char)st.hash.arena[s.koff]);
 }
 
 struct PosKeys {
@@ -156,8 +175,12 @@ __device__ void gather_keys(const DevState &st, const Region &R, int p, PosKeys 
     for (uint32_t s = st.head[c]; s != kNone; s = st.hash.slots[s].next) {
         const Slot &sl = st.hash.slots[s];
         if (sl.kind == KIND_NONINS) {
-            k.in_map = true;
-            if (!(sl.flags & SF_ERASED)) k.n_nonins++;
+            if (!(sl.flags & SF_NOMAP)) k.in_map = true;
+            if (!(sl.flags & SF_ERASED)) {
+                k.n_nonins++;
+                int b = promoted_base(st, sl);
+                if (b >= 0) k.single_mask |= 1 << b;
+            }
         } else if (sl.kind == KIND_INS && !(sl.flags & SF_ERASED)) {
             if (k.n_ins < kMaxVars) k.ins[k.n_ins++] = s;
             else atomicOr(st.err, ERR_UNSUPPORTED);
@@ -185,13 +208,27 @@ __device__ char ref_at(const DevState &st, const Region &R, int p) {
     return (p >= R.ws && p <= R.we) ? st.ref[p - 1] : (char)0;
 }
 
+// The reference-base key of position p (base b): its cell (returns 0, `g` =
+// cell word index), a promoted slot (returns 1, `slot`), or none (-1).
+__device__ int ref_key_at(const DevState &st, const Region &R, int p, int b, int64_t &g, uint32_t &slot) {
+    if (b < 0 || p < R.clo || p > R.chi) return -1;
+    int64_t c = cell_index(R, p);
+    uint8_t kf = st.cells.kflags[c];
+    if (((kf >> b) & 1) && !((kf >> (4 + b)) & 1)) { g = 4 * c + b; return 0; }
+    for (uint32_t s = st.head[c]; s != kNone; s = st.hash.slots[s].next) {
+        const Slot &sl = st.hash.slots[s];
+        if (!(sl.flags & SF_ERASED) && promoted_base(st, sl) == b) { slot = s; return 1; }
+    }
+    return -1;
+}
+
 // createInsertion's coverage bookkeeping for position p; when `apply` the
 // reference counts at p+1 are adjusted (src/ToVarsBuilder.cpp:403-417).
 // Returns the updated total coverage.
 __device__ int insertion_pass(const DevState &st, const Region &R, int p, int tpc, const PosKeys &k, bool apply) {
     for (int i = 0; i < k.n_ins; i++) {
         const Slot &s = st.hash.slots[k.ins[i]];
-        int cnt = s.fwd + s.rev;
+        int cnt = slot_cnt(s);
         int ttcov = tpc;
         if (cnt > tpc && s.extracnt != 0 && cnt - tpc < s.extracnt) ttcov = cnt;
         if (ttcov < cnt) {
@@ -204,11 +241,15 @@ __device__ int insertion_pass(const DevState &st, const Region &R, int p, int tp
                 if (cov1 != 0 && has1 && ttcov < (int)cov1 - cnt) {
                     ttcov = (int)cov1;
                     if (apply) {
-                        int b = base_index(ref_at(st, R, p1));
-                        uint8_t kf = st.cells.kflags[c1];
-                        if (b >= 0 && ((kf >> b) & 1) && !((kf >> (4 + b)) & 1)) {
-                            atomicSub(&st.cells.fwd[4 * c1 + b], (uint32_t)s.fwd);
-                            atomicSub(&st.cells.rev[4 * c1 + b], (uint32_t)s.rev);
+                        int64_t g = 0;
+                        uint32_t rs = kNone;
+                        int w = ref_key_at(st, R, p1, base_index(ref_at(st, R, p1)), g, rs);
+                        if (w == 0) {
+                            atomicSub(&st.cells.fwd[g], (uint32_t)s.fwd);
+                            atomicSub(&st.cells.rev[g], (uint32_t)s.rev);
+                        } else if (w == 1) {
+                            atomicSub(&st.hash.slots[rs].fwd, s.fwd);
+                            atomicSub(&st.hash.slots[rs].rev, s.rev);
                         }
                     }
                 }
@@ -345,8 +386,10 @@ __device__ void score_position(const DevState &st, const DevParams &P, int lo, i
     int hicov = 0;
     V vs[kMaxVars];
     int nv = 0;
+    const uint8_t kfc = st.cells.kflags[c];
+    const int cell_mask = kfc & 15 & ~(kfc >> 4);
     for (int b = 0; b < 4; b++) {
-        if (!((k.single_mask >> b) & 1)) continue;
+        if (!((cell_mask >> b) & 1)) continue;
         int64_t g = 4 * c + b;
         hicov += (int)st.cells.hi[g];
     }
@@ -356,7 +399,7 @@ __device__ void score_position(const DevState &st, const DevParams &P, int lo, i
     }
     // createVariant (non-insertion keys with a count)
     for (int b = 0; b < 4; b++) {
-        if (!((k.single_mask >> b) & 1)) continue;
+        if (!((cell_mask >> b) & 1)) continue;
         int64_t g = 4 * c + b;
         V v;
         v.kind = 0;
@@ -384,6 +427,8 @@ __device__ void score_position(const DevState &st, const DevParams &P, int lo, i
         V v;
         load_slot(sl, (int)s, v);
         if (v.cnt == 0) continue;
+        const int pb = promoted_base(st, sl);
+        if (pb >= 0) { v.kind = 0; v.key = pb; }
         int ttcov = tpc;
         if (v.cnt > tpc && v.extracnt > 0 && v.cnt - tpc < v.extracnt) ttcov = v.cnt;
         finish_var(v, ttcov, hicov, P);
@@ -451,13 +496,15 @@ __device__ void score_position(const DevState &st, const DevParams &P, int lo, i
     if (ref_i >= 0) { rfc = vs[ref_i].fwd; rrc = vs[ref_i].rev; }
     if (tpc > (int)st.cells.cov[c] && p + 1 <= R.chi) {
         int p1 = p + 1;
-        int64_t c1 = cell_index(R, p1);
-        char rb1 = ref_at(st, R, p1);
-        int b1 = base_index(rb1);
-        uint8_t kf1 = st.cells.kflags[c1];
-        if (p1 >= R.ws && p1 <= R.we && b1 >= 0 && ((kf1 >> b1) & 1) && !((kf1 >> (4 + b1)) & 1)) {
-            rfc = (int)st.cells.fwd[4 * c1 + b1];
-            rrc = (int)st.cells.rev[4 * c1 + b1];
+        int64_t g = 0;
+        uint32_t rs = kNone;
+        int w = (p1 >= R.ws && p1 <= R.we) ? ref_key_at(st, R, p1, base_index(ref_at(st, R, p1)), g, rs) : -1;
+        if (w == 0) {
+            rfc = (int)st.cells.fwd[g];
+            rrc = (int)st.cells.rev[g];
+        } else if (w == 1) {
+            rfc = st.hash.slots[rs].fwd;
+            rrc = st.hash.slots[rs].rev;
         }
     }
     unsigned int base = atomicAdd(st.n_cand, (unsigned int)nv);

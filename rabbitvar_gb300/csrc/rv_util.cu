@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include "rv_ctx.h"
+#include "rv_hash.cuh"
 
 namespace rv {
 
@@ -40,9 +41,70 @@ __global__ void k_gather_cells(DevState st, const int64_t *cells, int64_t n, Cel
     }
 }
 
+// Realigned statistics of one key (SF_OVR: the count rides in first_tp, the
+// fractional sums as double bits).
+__device__ void set_override(Slot &s, const Patch &q) {
+    s.fwd = q.fwd;
+    s.rev = q.rev;
+    s.hi = q.hi;
+    s.lo = q.lo;
+    s.extracnt = q.extracnt;
+    s.first_tp = q.cnt;
+    s.tp_sum = __double_as_longlong(q.tp);
+    s.mq_sum = __double_as_longlong(q.mq);
+    s.nm_sum = __double_as_longlong(q.nm);
+    s.q_sum = q.q_sum;
+    s.flags = (s.flags & ~(SF_ERASED | SF_NOMAP | SF_PDIFF | SF_QDIFF | SF_FORCE_STD)) | SF_OVR | (uint32_t)q.flags_or;
+}
+
+// Finds or creates the slot of a key the realigner added, sets its
+// statistics and links a new slot into its position's list.
+__device__ void create_slot(const DevState &st, const Patch &q, const uint8_t *keys) {
+    const char *k = (const char *)keys + q.key_off;
+    unsigned long long h1, h2;
+    key_hashes(q.region, q.kind, q.pos, k, q.klen, h1, h2);
+    const Hash &H = st.hash;
+    unsigned long long i = h1 & H.mask;
+    for (int step = 0; step <= 4096; step++) {
+        Slot &s = H.slots[i];
+        unsigned long long old = atomicCAS(&s.fp, 0ULL, h1);
+        if (old == 0ULL) {
+            s.region = q.region;
+            s.pos = q.pos;
+            s.kind = (uint16_t)q.kind;
+            s.klen = (uint16_t)q.klen;
+            unsigned long long off = q.klen ? atomicAdd(H.arena_used, (unsigned long long)q.klen) : 0ULL;
+            if (off + q.klen > H.arena_cap) {
+                atomicOr(st.err, ERR_ARENA_FULL);
+                s.koff = 0;
+                s.klen = 0;
+            } else {
+                s.koff = (uint32_t)off;
+                for (int j = 0; j < q.klen; j++) H.arena[off + j] = (uint8_t)k[j];
+            }
+            atomicAdd(H.n_used, 1u);
+            s.h2x = h2;
+            set_override(s, q);
+            const Region &R = st.regions[q.region];
+            if (q.pos >= R.clo && q.pos <= R.chi) {
+                int64_t c = R.cell_base + (q.pos - R.clo);
+                bool clip = q.kind != KIND_NONINS && q.kind != KIND_INS;
+                s.next = atomicExch(clip ? &st.head_sc[c] : &st.head[c], (uint32_t)i);
+            }
+            return;
+        }
+        if (old == h1) {
+            set_override(s, q);
+            return;
+        }
+        i = (i + 1) & H.mask;
+    }
+    atomicOr(st.err, ERR_HASH_FULL);
+}
+
 // Patches are applied by one thread each; a slot or cell key is named by at
-// most one overwrite patch, and coverage additions use atomics.
-__global__ void k_apply_patches(DevState st, const Patch *p, int64_t n) {
+// most one statistics patch, and coverage additions use atomics.
+__global__ void k_apply_patches(DevState st, const Patch *p, int64_t n, const uint8_t *keys) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const Patch &q = p[i];
         if (q.type == 0) {
@@ -58,12 +120,19 @@ __global__ void k_apply_patches(DevState st, const Patch *p, int64_t n) {
             s.q_sum = q.q_sum;
             s.flags |= (uint32_t)q.flags_or;
         } else if (q.type == 1) {
-            atomicOr(&st.hash.slots[q.target].flags, SF_ERASED);
+            atomicOr(&st.hash.slots[q.target].flags, SF_ERASED | (uint32_t)q.flags_or);
         } else if (q.type == 2) {
             int64_t c = q.target;
             atomicOr((unsigned int *)&st.cells.kflags[c & ~3LL], 1u << (4 + q.base + 8 * (c & 3)));
         } else if (q.type == 3) {
             atomicAdd(&st.cells.cov[q.target], (uint32_t)q.cov_add);
+        } else if (q.type == 4) {
+            set_override(st.hash.slots[q.target], q);
+        } else if (q.type == 5) {
+            if (keys) create_slot(st, q, keys);
+        } else if (q.type == 6) {
+            int64_t c = q.target;
+            atomicAnd((unsigned int *)&st.cells.kflags[c & ~3LL], ~(0xFFu << (8 * (c & 3))));
         }
     }
 }
@@ -115,8 +184,8 @@ void launch_gather_slots(const Slot *slots, const uint32_t *idx, int64_t n, Slot
 void launch_gather_cells(const DevState &st, const int64_t *cells, int64_t n, CellView *out, cudaStream_t s) {
     if (n > 0) k_gather_cells<<<(int)((n + 127) / 128 < 2048 ? (n + 127) / 128 : 2048), 128, 0, s>>>(st, cells, n, out);
 }
-void launch_apply_patches(const DevState &st, const Patch *p, int64_t n, cudaStream_t s) {
-    if (n > 0) k_apply_patches<<<(int)((n + 127) / 128 < 2048 ? (n + 127) / 128 : 2048), 128, 0, s>>>(st, p, n);
+void launch_apply_patches(const DevState &st, const Patch *p, int64_t n, const uint8_t *keys, cudaStream_t s) {
+    if (n > 0) k_apply_patches<<<(int)((n + 127) / 128 < 2048 ? (n + 127) / 128 : 2048), 128, 0, s>>>(st, p, n, keys);
 }
 
 }  // namespace rv

@@ -6,6 +6,7 @@
 #pragma once
 #include "rv_internal.h"
 #include "rv_cigar.cuh"
+#include "rv_hash.cuh"
 
 namespace rv {
 
@@ -23,16 +24,6 @@ __device__ __forceinline__ int base_index(char c) {
     case 'T': return 3;
     default: return -1;
     }
-}
-
-// MurmurHash3 64-bit finalizer (public-domain mixing function)
-__device__ __forceinline__ unsigned long long fmix64(unsigned long long k) {
-    k ^= k >> 33;
-    k *= 0xff51afd7ed558ccdULL;
-    k ^= k >> 33;
-    k *= 0xc4ceb9fe1a85ec53ULL;
-    k ^= k >> 33;
-    return k;
 }
 
 struct KeyBuf {

@@ -181,5 +181,3 @@ def test_local_realign_cigar_rewrite_maps(case, germline_small):
     for i in range(len(regions)) if len(regions) < 4 else (0, 4, 9):
         ora = O.run_region(rs, g, regions[i][0], regions[i][1], stages="P", params=prm)
         assert diff_dump(ora, ctx.export_maps(i, "P"), P_TAGS, rel=1e-9) == [], f"region {i}"
-    with pytest.raises(api.RvError):
-        ctx.realign()
