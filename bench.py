@@ -131,7 +131,8 @@ def barrier_max(dist, x: float) -> float:
     return float(t.item())
 
 
-WORKLOAD = ("somatic mode (-b 'T|N' -N 'T|N' --fisher -f 0.01 -k 0): synthetic 1 Mb contig, "
+def workload(k: int) -> str:
+    return (f"somatic mode (-b 'T|N' -N 'T|N' --fisher -f 0.01 -k {k}): synthetic 1 Mb contig, "
             "tumor 200x + normal 100x 2x150, 100 x 10 kb BED tiles")
 METRIC = "reads/s pileup+var scoring (somatic pair 1 Mb, T200x+N100x)"
 CPU_TILES = 40   # CPU sample: 40 of the 100 tiles (~0.8 M reads, ~10 s on one core)
@@ -140,13 +141,13 @@ CPU_TILES = 40   # CPU sample: 40 of the 100 tiles (~0.8 M reads, ~10 s on one c
 PILEUP_TRAFFIC = 1301.5e6
 
 
-def cpu_baseline_run(g, tumor, normal, regions, threads: int, n_regions: int):
+def cpu_baseline_run(g, tumor, normal, regions, threads: int, n_regions: int, k: int):
     """The oracle's CPU restatement of the path in somatic mode (OpenMP over
     regions, as the reference's BED mode) on a bounded sample of the
     workload's regions; returns reads/s."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
-    p = O.default_params(local_realign=0, fisher=1)
+    p = O.default_params(local_realign=k, fisher=1)
     sub = regions[:n_regions]
     lo, hi = sub[0][0], sub[-1][1]
     reads = sum(int(((rs.pos >= lo - 1) & (rs.pos < hi)).sum()) for rs in (tumor, normal))
@@ -249,15 +250,15 @@ def run_reference(args, rank):
     n_reg = CPU_TILES
     vals = []
     for _ in range(args.warmup):
-        cpu_baseline_run(g, tumor, normal, regions, threads, n_reg)
+        cpu_baseline_run(g, tumor, normal, regions, threads, n_reg, args.local_realign)
     for _ in range(args.steps):
-        v, dt, nr = cpu_baseline_run(g, tumor, normal, regions, threads, n_reg)
+        v, dt, nr = cpu_baseline_run(g, tumor, normal, regions, threads, n_reg, args.local_realign)
         vals.append(v)
     v = statistics.median(vals)
     out = {"impl": "reference", "metric": METRIC,
            "value": v, "unit": "reads/s", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
            "higher_is_better": True, "data": "synthetic",
-           "config": {"workload": WORKLOAD, "sample": f"first {n_reg} of 100 tiles, both samples"},
+           "config": {"workload": workload(args.local_realign), "sample": f"first {n_reg} of 100 tiles, both samples"},
            "cpu_baseline": {"value": v, "unit": "reads/s", "cores": threads, "kind": "port",
                             "sample": f"first {n_reg} of 100 10-kb tiles, tumor+normal ({nr} reads), per step"},
            "e2e": {"value": v, "unit": "reads/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -272,6 +273,8 @@ def main():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--local-realign", "-k", type=int, default=0, choices=[0, 1],
+                    help="the reference's -k: 1 adds the realigner's indel passes")
     ap.add_argument("--panel", type=int, default=0, metavar="N",
                     help="batched amplicon panel of N regions (-t -u): one launch for all regions vs one per region")
     args = ap.parse_args()
@@ -287,7 +290,7 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     g, tumor, normal, regions = make_workload(seed_offset=rank)
     samples = [("T", tumor), ("N", normal)]
-    params = api.default_params(local_realign=0, fisher=1)
+    params = api.default_params(local_realign=args.local_realign, fisher=1)
     pair = api.SomaticPair(params, device=local)
     pair.upload_reference(tumor.contig, synth.genome_str(g).encode())
     ctxs = [pair.tumor, pair.normal]
@@ -369,7 +372,7 @@ def main():
         "value": value, "unit": "reads/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "int32/fp64", "data": "synthetic (seeded)",
-        "config": {"workload": WORKLOAD, "reads_per_step": n_reads * world, "l2": "inputs (~0.5 GB) larger than L2, no flush",
+        "config": {"workload": workload(args.local_realign), "reads_per_step": n_reads * world, "l2": "inputs (~0.5 GB) larger than L2, no flush",
                    "records_per_step": recs},
         "e2e": {"value": e2e, "unit": "reads/s", "h2d_bytes_per_step": io["h2d"],
                 "d2h_bytes_per_step": io["d2h"]},
@@ -388,7 +391,7 @@ def main():
     if rank == 0 and not args.no_learned:
         out["learned_filter"] = learned_filter_leg()
     if rank == 0 and not args.no_cpu_baseline:
-        v, dt, nr = cpu_baseline_run(g, tumor, normal, regions, 1, CPU_TILES)
+        v, dt, nr = cpu_baseline_run(g, tumor, normal, regions, 1, CPU_TILES, args.local_realign)
         out["cpu_baseline"] = {"value": v, "unit": "reads/s", "cores": 1, "kind": "port",
                                "sample": f"first {CPU_TILES} of 100 10-kb tiles, tumor+normal ({nr} reads, {dt:.1f} s)"}
     if rank == 0:

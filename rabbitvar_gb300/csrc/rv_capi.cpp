@@ -286,9 +286,11 @@ void rv_destroy(rv_ctx *ctx) {
                     ctx->d_regions, ctx->d_tiles, ctx->d_score_base, ctx->d_cellmem, ctx->d_head, ctx->d_slots,
                     ctx->d_arena, ctx->d_deferred, ctx->d_cand, ctx->d_counters, ctx->d_tmp_idx,
                     ctx->d_tmp_slots, ctx->d_tmp_cells, ctx->d_tmp_views, ctx->d_tmp_n, ctx->d_list,
-                    ctx->d_ftab, ctx->d_logfact, ctx->d_skip, ctx->d_patches, ctx->d_patch_keys};
+                    ctx->d_ftab, ctx->d_logfact, ctx->d_skip, ctx->d_patches, ctx->d_patch_keys,
+                    ctx->d_list_off, ctx->d_list_bsum, ctx->d_list_idx, ctx->d_list_slots};
     for (void *p : ptrs)
         if (p) cudaFree(p);
+    if (ctx->h_mirror) cudaFreeHost(ctx->h_mirror);
     for (int i = 0; i < 12; i++)
         if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);

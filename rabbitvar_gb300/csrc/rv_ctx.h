@@ -66,6 +66,9 @@ struct Patch {
     int64_t key_off;                    // type 5: key bytes in the patch key buffer
 };
 void launch_apply_patches(const DevState &st, const Patch *p, int64_t n, const uint8_t *keys, cudaStream_t s);
+// flattened per-cell key lists (-k 1 realigner mirror): 5 launches, then 1
+void launch_list_offsets(const DevState &st, uint32_t *off, uint32_t *bsum, cudaStream_t s);
+void launch_list_fill(const DevState &st, const uint32_t *off, Slot *out, uint32_t *out_idx, cudaStream_t s);
 
 template <class T>
 struct DevBuf {
@@ -149,6 +152,13 @@ struct rv_ctx {
     void *d_tmp_views = nullptr;
     size_t cap_tmp_views = 0;
     unsigned int *d_tmp_n = nullptr;
+    // -k 1 realigner mirror: flattened key lists on the device, pinned host copies
+    uint32_t *d_list_off = nullptr, *d_list_bsum = nullptr, *d_list_idx = nullptr;
+    size_t cap_list_off = 0, cap_list_bsum = 0, cap_list_idx = 0;
+    rv::Slot *d_list_slots = nullptr;
+    size_t cap_list_slots = 0;
+    void *h_mirror = nullptr;  // pinned: cells, offsets, slots, slot indices
+    size_t cap_mirror = 0;
     rv::Patch *d_patches = nullptr;
     size_t cap_patches = 0;
     uint8_t *d_patch_keys = nullptr;

@@ -250,17 +250,6 @@ HVar from_slot(const Slot &s, int64_t slot) {
 }
 
 
-template <class T>
-rv_status ensure(rv_ctx *ctx, T *&p, size_t &cap, size_t need) {
-    if (p && need <= cap) return RV_OK;
-    if (p) cudaFree(p);
-    p = nullptr;
-    size_t n = std::max<size_t>(need + need / 2, 256);
-    HCUDA(cudaMalloc((void **)&p, n * sizeof(T)));
-    cap = n;
-    return RV_OK;
-}
-
 // Slots named by a device index list, copied to the host.
 rv_status pull_slots(rv_ctx *ctx, unsigned int n, std::vector<Slot> &slots, std::vector<uint32_t> &idx) {
     slots.resize(n);
@@ -283,7 +272,10 @@ rv_status pull_arena(rv_ctx *ctx) {
     HCUDA(cudaStreamSynchronize(ctx->stream));
     used = std::min<unsigned long long>(used, ctx->arena_cap);
     ctx->h_arena.resize(used);
-    if (used) HCUDA(cudaMemcpy(ctx->h_arena.data(), ctx->d_arena, used, cudaMemcpyDeviceToHost));
+    if (used) {
+        HCUDA(cudaMemcpyAsync(ctx->h_arena.data(), ctx->d_arena, used, cudaMemcpyDeviceToHost, ctx->stream));
+        HCUDA(cudaStreamSynchronize(ctx->stream));
+    }
     return RV_OK;
 }
 

@@ -8,6 +8,8 @@
 #include <string>
 #include <vector>
 
+#include <cuda_runtime.h>
+
 #include "rv_ctx.h"
 
 namespace rv {
@@ -43,5 +45,23 @@ rv_status fetch_slots(rv_ctx *ctx, std::vector<Slot> &slots, std::vector<uint32_
 rv_status fetch_cells(rv_ctx *ctx, const std::vector<int64_t> &cells, std::vector<CellView> &out);
 // copies patches (and the key bytes of type-5 patches) to the device and applies them
 rv_status apply_patches(rv_ctx *ctx, const std::vector<Patch> &patches, const std::string &keys);
+// the used part of the key arena into ctx->h_arena
+rv_status pull_arena(rv_ctx *ctx);
+
+// a device scratch array of at least `need` elements (grown by half again)
+template <class T>
+rv_status ensure(rv_ctx *ctx, T *&p, size_t &cap, size_t need) {
+    if (p && need <= cap) return RV_OK;
+    if (p) cudaFree(p);
+    p = nullptr;
+    size_t n = need + need / 2 > 256 ? need + need / 2 : 256;
+    cudaError_t e = cudaMalloc((void **)&p, n * sizeof(T));
+    if (e != cudaSuccess) {
+        ctx->err = std::string("cudaMalloc: ") + cudaGetErrorString(e);
+        return RV_ERR_CUDA;
+    }
+    cap = n;
+    return RV_OK;
+}
 
 }  // namespace rv

@@ -17,6 +17,8 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
+#include <cstdlib>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -45,8 +47,6 @@ namespace {
     } while (0)
 
 using std::string;
-
-constexpr int kBlock = 1024;  // cells fetched per block
 
 // Reference window of a region with the insert-on-lookup behaviour of the
 // reference's map: operator[] on a position outside the window stores base 0
@@ -161,52 +161,37 @@ bool same_stats(const HVar &a, const HVar &b) {
 uint64_t pos_key(int region, int pos) { return ((uint64_t)(uint32_t)region << 32) | (uint32_t)pos; }
 
 // ---------------------------------------------------------------------------
-// batch-wide mirror: every slot, the key arena, cells fetched by block
+// batch-wide mirror (pinned host copies, read-only while the regions run):
+// the cells, and every cell's keys flattened in list order
 // ---------------------------------------------------------------------------
 struct Mirror {
     rv_ctx *ctx = nullptr;
-    std::vector<Slot> slots;
-    std::vector<uint32_t> sidx;
-    std::unordered_map<uint64_t, std::vector<uint32_t>> nonins_at, ins_at, sc5_at, sc3_at;
-    std::vector<Region> regions;  // device copies (max_read_len)
-    std::unordered_map<int64_t, std::vector<CellView>> blocks;
-    std::mutex mu;
-    rv_status failed = RV_OK;
+    const uint32_t *fwd, *rev, *hi, *tp, *q, *mq, *first, *cov;
+    const int32_t *nm;
+    const uint8_t *kflags;
+    const uint32_t *off = nullptr;   // n_cells + 1
+    const Slot *slots = nullptr;     // off[n_cells]
+    const uint32_t *sidx = nullptr;  // hash slot index of each
+    std::vector<Region> regions;     // device copies (max_read_len)
 
     string key(uint32_t i) const { return slot_key(ctx, slots[i]); }
-
-    rv_status fetch_blocks(const std::vector<int64_t> &want) {
-        std::vector<int64_t> need;
-        for (int64_t b : want)
-            if (!blocks.count(b)) need.push_back(b);
-        if (need.empty()) return RV_OK;
-        std::vector<int64_t> cells;
-        for (int64_t b : need)
-            for (int64_t c = b * kBlock; c < (b + 1) * kBlock; c++) cells.push_back(std::min(c, ctx->n_cells - 1));
-        std::vector<CellView> cv;
-        rv_status st = fetch_cells(ctx, cells, cv);
-        if (st) return st;
-        ctx->kernels++;
-        ctx->io_d2h += (int64_t)(cv.size() * sizeof(CellView));
-        for (size_t i = 0; i < need.size(); i++)
-            blocks[need[i]].assign(cv.begin() + (int64_t)i * kBlock, cv.begin() + (int64_t)(i + 1) * kBlock);
-        return RV_OK;
-    }
-
-    // cell view of cell c (fetched on demand when no prefetch covered it)
-    const CellView *cell(int64_t c) {
-        std::lock_guard<std::mutex> g(mu);
-        int64_t b = c / kBlock;
-        auto it = blocks.find(b);
-        if (it == blocks.end()) {
-            rv_status st = fetch_blocks({b});
-            if (st) {
-                failed = st;
-                return nullptr;
-            }
-            it = blocks.find(b);
-        }
-        return &it->second[(size_t)(c % kBlock)];
+    HVar cell_var(int64_t c, int b) const {
+        HVar h;
+        const int64_t g = 4 * c + b;
+        h.fwd = (int)fwd[g];
+        h.rev = (int)rev[g];
+        h.cnt = h.fwd + h.rev;
+        h.hi = (int)hi[g];
+        h.lo = h.cnt - h.hi;
+        h.tp = (double)(int)tp[g];
+        h.q = (double)(int)q[g];
+        h.mq = (double)(int)mq[g];
+        h.nm = (double)nm[g];
+        h.pstd = (first[g] & (1u << 30)) != 0;
+        h.qstd = (first[g] & (1u << 31)) != 0;
+        h.cell = c;
+        h.base = b;
+        return h;
     }
 };
 
@@ -232,7 +217,8 @@ struct RegionRealigner {
     std::map<int, int> cov_add;
     struct Clip {
         HClip c;
-        const std::vector<uint32_t> *seq = nullptr;
+        int64_t cell = -1;  // the clip's per-offset counts are in this cell's list
+        int seq_kind = 0;
         bool loaded = false;
     };
     std::map<int, Clip> sc5, sc3;
@@ -253,21 +239,17 @@ struct RegionRealigner {
         if (it != nonins.end()) return it->second;
         PosMap &m = nonins[p];
         if (in_cells(p)) {
-            int64_t c = cell_of(p);
-            const CellView *v = mir.cell(c);
-            if (v) {
-                int exist = v->kflags & 15, erased = (v->kflags >> 4) & 15;
-                if (exist) m.present = true;
-                for (int b = 0; b < 4; b++)
-                    if (((exist & ~erased) >> b) & 1) m.keys[string(1, "ACGT"[b])] = from_cell(*v, b, c);
+            const int64_t c = cell_of(p);
+            const int exist = mir.kflags[c] & 15, erased = (mir.kflags[c] >> 4) & 15;
+            if (exist) m.present = true;
+            for (int b = 0; b < 4; b++)
+                if (((exist & ~erased) >> b) & 1) m.keys[string(1, "ACGT"[b])] = mir.cell_var(c, b);
+            for (uint32_t i = mir.off[c]; i < mir.off[c + 1]; i++) {
+                if (mir.slots[i].kind != KIND_NONINS) continue;
+                m.present = true;
+                HVar h = from_slot(mir.slots[i], mir.sidx[i]);
+                if (!h.erased) m.keys[mir.key(i)] = h;
             }
-            auto s = mir.nonins_at.find(pos_key(region, p));
-            if (s != mir.nonins_at.end())
-                for (uint32_t i : s->second) {
-                    m.present = true;
-                    HVar h = from_slot(mir.slots[i], mir.sidx[i]);
-                    if (!h.erased) m.keys[mir.key(i)] = h;
-                }
         }
         nonins0[p] = m;
         return m;
@@ -276,13 +258,15 @@ struct RegionRealigner {
         auto it = ins.find(p);
         if (it != ins.end()) return it->second;
         PosMap &m = ins[p];
-        auto s = mir.ins_at.find(pos_key(region, p));
-        if (s != mir.ins_at.end())
-            for (uint32_t i : s->second) {
+        if (in_cells(p)) {
+            const int64_t c = cell_of(p);
+            for (uint32_t i = mir.off[c]; i < mir.off[c + 1]; i++) {
+                if (mir.slots[i].kind != KIND_INS) continue;
                 m.present = true;
                 HVar h = from_slot(mir.slots[i], mir.sidx[i]);
                 if (!h.erased) m.keys[mir.key(i)] = h;
             }
+        }
         ins0[p] = m;
         return m;
     }
@@ -331,12 +315,14 @@ struct RegionRealigner {
     string consensus(Clip &k) {
         if (!k.loaded) {
             k.loaded = true;
-            if (k.seq)
-                for (uint32_t i : *k.seq) {
+            if (k.cell >= 0)
+                for (uint32_t i = mir.off[k.cell]; i < mir.off[k.cell + 1]; i++) {
+                    const Slot &s = mir.slots[i];
+                    if (s.kind != k.seq_kind) continue;
                     string key = mir.key(i);
                     if (key.size() != 3) continue;
                     int idx = (uint8_t)key[0] | ((uint8_t)key[1] << 8);
-                    k.c.nt[idx][key[2]] = {mir.slots[i].obs, mir.slots[i].q_sum};
+                    k.c.nt[idx][key[2]] = {s.obs, s.q_sum};
                 }
         }
         return clip_consensus(k.c);
@@ -344,18 +330,15 @@ struct RegionRealigner {
     void add_cov(int p, int n) { cov_add[p] += n; }
 
     void load_clips() {
-        for (int side = 0; side < 2; side++) {
-            auto &src = side ? mir.sc3_at : mir.sc5_at;
-            auto &dst = side ? sc3 : sc5;
-            for (int p = Rg.clo; p <= Rg.chi; p++) {
-                auto it = src.find(pos_key(region, p));
-                if (it == src.end()) continue;
-                Clip &k = dst[p];
-                for (uint32_t i : it->second) {
-                    const Slot &s = mir.slots[i];
-                    if (s.kind == KIND_SC5 || s.kind == KIND_SC3) k.c.agg = from_slot(s, mir.sidx[i]);
-                }
-                k.seq = &it->second;
+        for (int p = Rg.clo; p <= Rg.chi; p++) {
+            const int64_t c = cell_of(p);
+            for (uint32_t i = mir.off[c]; i < mir.off[c + 1]; i++) {
+                const Slot &s = mir.slots[i];
+                if (s.kind != KIND_SC5 && s.kind != KIND_SC3) continue;
+                Clip &k = (s.kind == KIND_SC3 ? sc3 : sc5)[p];
+                k.c.agg = from_slot(s, mir.sidx[i]);
+                k.cell = c;
+                k.seq_kind = s.kind == KIND_SC3 ? KIND_SC3_SEQ : KIND_SC5_SEQ;
             }
         }
     }
@@ -521,8 +504,9 @@ struct RegionRealigner {
     static bool ismatch(const string &seq1, const string &seq2_in, int dir) {
         string seq2 = drop_hash_caret(seq2_in);
         int mm = 0;
-        for (int n = 0; n < (int)seq1.size() && n < (int)seq2.size(); n++)
-            if (seq1[n] != vsub(seq2, dir * n - (dir == -1 ? 1 : 0), 1)[0]) mm++;
+        const int l2 = (int)seq2.size();
+        for (int n = 0; n < (int)seq1.size() && n < l2; n++)
+            if (seq1[n] != seq2[dir == 1 ? n : l2 - 1 - n]) mm++;
         return mm <= 3 && mm / (double)seq1.size() < 0.15;
     }
     // adjRefCnt (:1753-1787)
@@ -911,14 +895,17 @@ struct RegionRealigner {
         }
     }
 
-    // find35match (:1396-1428)
+    // find35match (:1396-1428).  Inside the loop bounds the reference's
+    // substr calls never throw: s3's index is always a character, s5's is one
+    // past the end (an empty string, a mismatch) when i + n == |s5|.
     static void find35(const string &s5, const string &s3, int &b5, int &b3, int &score) {
         b5 = b3 = score = 0;
-        for (int i = 0; i < (int)s5.size() - 8; i++) {
-            for (int j = 1; j < (int)s3.size() - 8; j++) {
+        const int l5 = (int)s5.size(), l3 = (int)s3.size();
+        for (int i = 0; i < l5 - 8; i++) {
+            for (int j = 1; j < l3 - 8; j++) {
                 int nm = 0, n = 0;
-                while (n + j <= (int)s3.size() && i + n <= (int)s5.size()) {
-                    if (vsub(s3, -j - n, 1) != vsub(s5, i + n, 1)) nm++;
+                while (n + j <= l3 && i + n <= l5) {
+                    if (i + n == l5 || s3[l3 - j - n] != s5[i + n]) nm++;
                     if (nm > 2) break;
                     n++;
                 }
@@ -1113,15 +1100,14 @@ struct RegionRealigner {
                     q.type = 6;
                     q.target = c;
                     out.push_back(q);
-                    auto s = mir.nonins_at.find(pos_key(region, p));
-                    if (s != mir.nonins_at.end())
-                        for (uint32_t i : s->second) {
-                            Patch e = blank();
-                            e.type = 1;
-                            e.target = mir.sidx[i];
-                            e.flags_or = (int)SF_NOMAP;
-                            out.push_back(e);
-                        }
+                    for (uint32_t i = mir.off[c]; i < mir.off[c + 1]; i++) {
+                        if (mir.slots[i].kind != KIND_NONINS) continue;
+                        Patch e = blank();
+                        e.type = 1;
+                        e.target = mir.sidx[i];
+                        e.flags_or = (int)SF_NOMAP;
+                        out.push_back(e);
+                    }
                     continue;
                 }
                 for (auto &oe : O.keys) {
@@ -1169,29 +1155,38 @@ struct RegionRealigner {
         }
     }
 
-    void run(std::vector<Patch> &out, string &keys) {
+    void run(std::vector<Patch> &out, string &keys, double *phase) {
+        auto clk = [] { return std::chrono::steady_clock::now(); };
+        auto t = clk();
+        auto lap = [&](int k) {
+            auto n = clk();
+            phase[k] += std::chrono::duration<double, std::milli>(n - t).count();
+            t = n;
+        };
         load_clips();
         std::map<int, std::map<string, int>> mnp, delcnt, inscnt;
-        for (int kind = 0; kind < 2; kind++) {
-            auto &idx = kind ? mir.ins_at : mir.nonins_at;
-            for (int p = Rg.clo; p <= Rg.chi; p++) {
-                auto it = idx.find(pos_key(region, p));
-                if (it == idx.end()) continue;
-                for (uint32_t i : it->second) {
-                    const Slot &s = mir.slots[i];
-                    if (s.obs <= 0) continue;
-                    string k = mir.key(i);
-                    if (kind) inscnt[p][k] = s.obs;
-                    else if (is_mnv(k)) mnp[p][k] = s.obs;
-                    else if (!k.empty() && k[0] == '-') delcnt[p][k] = s.obs;
-                }
+        for (int p = Rg.clo; p <= Rg.chi; p++) {
+            const int64_t c = cell_of(p);
+            for (uint32_t i = mir.off[c]; i < mir.off[c + 1]; i++) {
+                const Slot &s = mir.slots[i];
+                if ((s.kind != KIND_NONINS && s.kind != KIND_INS) || s.obs <= 0) continue;
+                string k = mir.key(i);
+                if (s.kind == KIND_INS) inscnt[p][k] = s.obs;
+                else if (is_mnv(k)) mnp[p][k] = s.obs;
+                else if (!k.empty() && k[0] == '-') delcnt[p][k] = s.obs;
             }
         }
+        lap(0);
         adjust_mnp(mnp);
+        lap(1);
         realigndel(true, delcnt);
+        lap(2);
         realignins(inscnt);
+        lap(3);
         realignlgins30();
+        lap(4);
         diff(out, keys);
+        lap(5);
     }
 };
 
@@ -1199,48 +1194,89 @@ struct RegionRealigner {
 
 // VariationRealigner::process with -k 1 (src/VariationRealigner.cpp:135-161)
 rv_status host_realign_full(rv_ctx *ctx) {
+    const bool trace = getenv("RV_REALIGN_TRACE") != nullptr;
+    auto now = [] { return std::chrono::steady_clock::now(); };
+    auto t0 = now();
+    auto ms = [&](std::chrono::steady_clock::time_point a) {
+        return std::chrono::duration<double, std::milli>(now() - a).count();
+    };
     Mirror mir;
     mir.ctx = ctx;
-    rv_status st = fetch_slots(ctx, mir.slots, mir.sidx);
-    if (st) return st;
-    ctx->kernels += mir.slots.empty() ? 1 : 2;
-    ctx->io_d2h += (int64_t)(mir.slots.size() * (sizeof(Slot) + 4) + ctx->h_arena.size());
+    rv_status st;
+    cudaStream_t s = ctx->stream;
+    const int64_t nc = ctx->n_cells;
+    const int64_t nb = (nc + 1023) / 1024;
+    if ((st = ensure(ctx, ctx->d_list_off, ctx->cap_list_off, (size_t)nc + 1)) ||
+        (st = ensure(ctx, ctx->d_list_bsum, ctx->cap_list_bsum, (size_t)nb + 1)))
+        return st;
+    DevState ds = ctx->state();
+    launch_list_offsets(ds, ctx->d_list_off, ctx->d_list_bsum, s);
+    ctx->kernels += 4;
+    uint32_t total = 0;
+    HCUDA(cudaMemcpyAsync(&total, ctx->d_list_off + nc, 4, cudaMemcpyDeviceToHost, s));
+    HCUDA(cudaStreamSynchronize(s));
+    if ((st = ensure(ctx, ctx->d_list_slots, ctx->cap_list_slots, (size_t)total + 1)) ||
+        (st = ensure(ctx, ctx->d_list_idx, ctx->cap_list_idx, (size_t)total + 1)))
+        return st;
+    launch_list_fill(ds, ctx->d_list_off, ctx->d_list_slots, ctx->d_list_idx, s);
+    ctx->kernels++;
+    // pinned host mirror: 8 cell arrays (16 B per cell each), cov, kflags,
+    // offsets, slots, slot indices
+    auto up16 = [](size_t x) { return (x + 15) & ~(size_t)15; };
+    const size_t b_arr = (size_t)nc * 16, b_cov = up16((size_t)nc * 4), b_kf = up16((size_t)nc),
+                 b_off = up16(((size_t)nc + 1) * 4), b_sl = (size_t)total * sizeof(Slot), b_ix = up16((size_t)total * 4);
+    const size_t need = 8 * b_arr + b_cov + b_kf + b_off + b_sl + b_ix;
+    if (!ctx->h_mirror || ctx->cap_mirror < need) {
+        if (ctx->h_mirror) cudaFreeHost(ctx->h_mirror);
+        ctx->h_mirror = nullptr;
+        size_t cap = need + need / 4;
+        HCUDA(cudaHostAlloc(&ctx->h_mirror, cap, cudaHostAllocDefault));
+        ctx->cap_mirror = cap;
+    }
+    char *h = (char *)ctx->h_mirror;
+    const Cells &C = ctx->cells;
+    const void *dev_arr[8] = {C.fwd, C.rev, C.hi, C.tp, C.q, C.mq, C.nm, C.first};
+    char *host_arr[8];
+    for (int k = 0; k < 8; k++) {
+        host_arr[k] = h;
+        if (nc) HCUDA(cudaMemcpyAsync(h, dev_arr[k], b_arr, cudaMemcpyDeviceToHost, s));
+        h += b_arr;
+    }
+    char *h_cov = h; h += b_cov;
+    char *h_kf = h; h += b_kf;
+    char *h_off = h; h += b_off;
+    char *h_sl = h; h += b_sl;
+    char *h_ix = h;
+    if (nc) {
+        HCUDA(cudaMemcpyAsync(h_cov, C.cov, (size_t)nc * 4, cudaMemcpyDeviceToHost, s));
+        HCUDA(cudaMemcpyAsync(h_kf, C.kflags, (size_t)nc, cudaMemcpyDeviceToHost, s));
+        HCUDA(cudaMemcpyAsync(h_off, ctx->d_list_off, ((size_t)nc + 1) * 4, cudaMemcpyDeviceToHost, s));
+    }
+    if (total) {
+        HCUDA(cudaMemcpyAsync(h_sl, ctx->d_list_slots, b_sl, cudaMemcpyDeviceToHost, s));
+        HCUDA(cudaMemcpyAsync(h_ix, ctx->d_list_idx, (size_t)total * 4, cudaMemcpyDeviceToHost, s));
+    }
     mir.regions.resize(ctx->regions.size());
     if (!mir.regions.empty())
-        HCUDA(cudaMemcpy(mir.regions.data(), ctx->d_regions, mir.regions.size() * sizeof(Region),
-                         cudaMemcpyDeviceToHost));
-    for (uint32_t i = 0; i < (uint32_t)mir.slots.size(); i++) {
-        const Slot &s = mir.slots[i];
-        if (s.region < 0 || s.region >= (int)mir.regions.size()) continue;
-        uint64_t k = pos_key(s.region, s.pos);
-        switch (s.kind) {
-        case KIND_NONINS: mir.nonins_at[k].push_back(i); break;
-        case KIND_INS: mir.ins_at[k].push_back(i); break;
-        case KIND_SC5: case KIND_SC5_SEQ: mir.sc5_at[k].push_back(i); break;
-        case KIND_SC3: case KIND_SC3_SEQ: mir.sc3_at[k].push_back(i); break;
-        default: break;
-        }
-    }
-    // prefetch the cell blocks around every realigner candidate
-    std::set<int64_t> want;
-    auto around = [&](int region, int p, int margin) {
-        const Region &R = mir.regions[region];
-        int a = std::max(R.clo, p - margin), b = std::min(R.chi, p + margin);
-        if (a > b) return;
-        for (int64_t blk = (R.cell_base + (a - R.clo)) / kBlock; blk <= (R.cell_base + (b - R.clo)) / kBlock; blk++)
-            want.insert(blk);
-    };
-    for (uint32_t i = 0; i < (uint32_t)mir.slots.size(); i++) {
-        const Slot &s = mir.slots[i];
-        if (s.region < 0 || s.region >= (int)mir.regions.size()) continue;
-        const int mrl = std::max(1, mir.regions[s.region].max_read_len);
-        if (s.kind == KIND_NONINS || s.kind == KIND_INS) {
-            if (s.klen >= 2 && s.obs > 0) around(s.region, s.pos, 320 + 2 * s.klen);
-        } else if (s.kind == KIND_SC5 || s.kind == KIND_SC3) {
-            around(s.region, s.pos, 400 + 3 * mrl);
-        }
-    }
-    if ((st = mir.fetch_blocks(std::vector<int64_t>(want.begin(), want.end())))) return st;
+        HCUDA(cudaMemcpyAsync(mir.regions.data(), ctx->d_regions, mir.regions.size() * sizeof(Region),
+                              cudaMemcpyDeviceToHost, s));
+    HCUDA(cudaStreamSynchronize(s));
+    if ((st = pull_arena(ctx))) return st;
+    ctx->io_d2h += (int64_t)(need - b_ix + (size_t)total * 4 + ctx->h_arena.size());
+    mir.fwd = (const uint32_t *)host_arr[0];
+    mir.rev = (const uint32_t *)host_arr[1];
+    mir.hi = (const uint32_t *)host_arr[2];
+    mir.tp = (const uint32_t *)host_arr[3];
+    mir.q = (const uint32_t *)host_arr[4];
+    mir.mq = (const uint32_t *)host_arr[5];
+    mir.nm = (const int32_t *)host_arr[6];
+    mir.first = (const uint32_t *)host_arr[7];
+    mir.cov = (const uint32_t *)h_cov;
+    mir.kflags = (const uint8_t *)h_kf;
+    mir.off = (const uint32_t *)h_off;
+    mir.slots = (const Slot *)h_sl;
+    mir.sidx = (const uint32_t *)h_ix;
+    double t_fetch = ms(t0);
     // regions in parallel; patches concatenated in region order
     const int nreg = (int)ctx->regions.size();
     std::vector<std::vector<Patch>> patches((size_t)nreg);
@@ -1250,12 +1286,14 @@ rv_status host_realign_full(rv_ctx *ctx) {
     std::atomic<int> next{0};
     std::mutex err_mu;
     string failure;
+    std::vector<double> phase((size_t)nt * 8, 0.0);
+    std::atomic<int> tid{0};
     auto work = [&]() {
-        cudaSetDevice(ctx->device);
+        double *ph = phase.data() + 8 * tid.fetch_add(1);
         for (int r; (r = next.fetch_add(1)) < nreg;) {
             try {
                 RegionRealigner rr(mir, ctx, r);
-                rr.run(patches[r], keys[r]);
+                rr.run(patches[r], keys[r], ph);
             } catch (const std::exception &e) {
                 // the reference's own realigner terminates here (an exception
                 // it does not catch); the batch reports it instead
@@ -1268,7 +1306,6 @@ rv_status host_realign_full(rv_ctx *ctx) {
     for (int t = 1; t < nt; t++) th.emplace_back(work);
     work();
     for (auto &t : th) t.join();
-    if (mir.failed) return mir.failed;
     if (!failure.empty()) {
         ctx->err = failure;
         return RV_ERR_UNSUPPORTED;
@@ -1282,7 +1319,17 @@ rv_status host_realign_full(rv_ctx *ctx) {
         }
         all_keys += keys[r];
     }
-    return apply_patches(ctx, all, all_keys);
+    double t_run = ms(t0);
+    st = apply_patches(ctx, all, all_keys);
+    if (trace) {
+        double sum[6] = {0};
+        for (int t = 0; t < nt; t++)
+            for (int k = 0; k < 6; k++) sum[k] += phase[8 * t + k];
+        fprintf(stderr, "realign -k 1: listed keys %u, patches %zu, threads %d; ms: fetch %.2f run %.2f total %.2f; "
+                "thread-ms: setup %.2f mnp %.2f del %.2f ins %.2f lgins %.2f diff %.2f\n", total,
+                all.size(), nt, t_fetch, t_run, ms(t0), sum[0], sum[1], sum[2], sum[3], sum[4], sum[5]);
+    }
+    return st;
 }
 
 }  // namespace rv

@@ -2,6 +2,8 @@
 // hash slots, gather cells for the host realigner, apply its patches.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "rv_ctx.h"
 #include "rv_hash.cuh"
 
@@ -137,6 +139,90 @@ __global__ void k_apply_patches(DevState st, const Patch *p, int64_t n, const ui
     }
 }
 
+// ---------------------------------------------------------------------------
+// Flattened key lists for the -k 1 realigner's host mirror: the keys of cell
+// c (its allele-key list, then its soft-clip list, each in list order) land
+// in out[off[c] .. off[c + 1]).
+// ---------------------------------------------------------------------------
+constexpr int kListLimit = 1 << 20;  // longest list walked (a corrupt list sets ERR_UNSUPPORTED)
+
+__global__ void k_list_count(DevState st, uint32_t *cnt) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < st.cells.n_cells;
+         c += (int64_t)gridDim.x * blockDim.x) {
+        int n = 0;
+        for (int l = 0; l < 2; l++)
+            for (uint32_t s = l ? st.head_sc[c] : st.head[c]; s != 0xFFFFFFFFu; s = st.hash.slots[s].next) {
+                if (++n > kListLimit) {
+                    atomicOr(st.err, ERR_UNSUPPORTED);
+                    break;
+                }
+            }
+        cnt[c] = (uint32_t)(n > kListLimit ? 0 : n);
+    }
+}
+
+// exclusive scan of n values in blocks of 1024 (block sums to bsum)
+__global__ void k_scan_blocks(uint32_t *v, int64_t n, uint32_t *bsum) {
+    __shared__ uint32_t sh[1024];
+    int64_t i = (int64_t)blockIdx.x * 1024 + threadIdx.x;
+    uint32_t x = i < n ? v[i] : 0u;
+    sh[threadIdx.x] = x;
+    __syncthreads();
+    for (int d = 1; d < 1024; d <<= 1) {
+        uint32_t y = threadIdx.x >= (unsigned)d ? sh[threadIdx.x - d] : 0u;
+        __syncthreads();
+        sh[threadIdx.x] += y;
+        __syncthreads();
+    }
+    if (i < n) v[i] = sh[threadIdx.x] - x;
+    if (threadIdx.x == 1023) bsum[blockIdx.x] = sh[1023];
+}
+
+// exclusive scan of the block sums (one block, chunks of 1024 with a carry);
+// bsum[nb] = total
+__global__ void k_scan_sums(uint32_t *bsum, int64_t nb) {
+    __shared__ uint32_t sh[1024];
+    __shared__ uint32_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int64_t b0 = 0; b0 < nb; b0 += 1024) {
+        int64_t i = b0 + threadIdx.x;
+        uint32_t x = i < nb ? bsum[i] : 0u;
+        sh[threadIdx.x] = x;
+        __syncthreads();
+        for (int d = 1; d < 1024; d <<= 1) {
+            uint32_t y = threadIdx.x >= (unsigned)d ? sh[threadIdx.x - d] : 0u;
+            __syncthreads();
+            sh[threadIdx.x] += y;
+            __syncthreads();
+        }
+        if (i < nb) bsum[i] = carry + sh[threadIdx.x] - x;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += sh[1023];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) bsum[nb] = carry;
+}
+
+__global__ void k_scan_add(uint32_t *v, int64_t n, const uint32_t *bsum) {
+    int64_t i = (int64_t)blockIdx.x * 1024 + threadIdx.x;
+    if (i < n) v[i] += bsum[blockIdx.x];
+    if (i == 0) v[n] = bsum[gridDim.x];
+}
+
+__global__ void k_list_fill(DevState st, const uint32_t *off, Slot *out, uint32_t *out_idx) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < st.cells.n_cells;
+         c += (int64_t)gridDim.x * blockDim.x) {
+        uint32_t k = off[c], e = off[c + 1];
+        for (int l = 0; l < 2; l++)
+            for (uint32_t s = l ? st.head_sc[c] : st.head[c]; s != 0xFFFFFFFFu && k < e; s = st.hash.slots[s].next) {
+                out[k] = st.hash.slots[s];
+                out_idx[k] = s;
+                k++;
+            }
+    }
+}
+
 // MNP keys (A/C/G/T '&' A/C/G/T...) that the realigner's adjustMNP visits.
 __global__ void k_select_mnv(DevState st, uint32_t *out, unsigned int *n_out) {
     unsigned long long n = st.hash.mask + 1ULL;
@@ -184,6 +270,22 @@ void launch_gather_slots(const Slot *slots, const uint32_t *idx, int64_t n, Slot
 void launch_gather_cells(const DevState &st, const int64_t *cells, int64_t n, CellView *out, cudaStream_t s) {
     if (n > 0) k_gather_cells<<<(int)((n + 127) / 128 < 2048 ? (n + 127) / 128 : 2048), 128, 0, s>>>(st, cells, n, out);
 }
+// off has n_cells + 1 entries, bsum (n_cells + 1023) / 1024 + 1
+void launch_list_offsets(const DevState &st, uint32_t *off, uint32_t *bsum, cudaStream_t s) {
+    const int64_t n = st.cells.n_cells;
+    if (n <= 0) return;
+    k_list_count<<<(int)std::min<int64_t>((n + 255) / 256, 4096), 256, 0, s>>>(st, off);
+    const int64_t nb = (n + 1023) / 1024;
+    k_scan_blocks<<<(unsigned)nb, 1024, 0, s>>>(off, n, bsum);
+    k_scan_sums<<<1, 1024, 0, s>>>(bsum, nb);
+    k_scan_add<<<(unsigned)nb, 1024, 0, s>>>(off, n, bsum);
+}
+
+void launch_list_fill(const DevState &st, const uint32_t *off, Slot *out, uint32_t *out_idx, cudaStream_t s) {
+    const int64_t n = st.cells.n_cells;
+    if (n > 0) k_list_fill<<<(int)std::min<int64_t>((n + 255) / 256, 4096), 256, 0, s>>>(st, off, out, out_idx);
+}
+
 void launch_apply_patches(const DevState &st, const Patch *p, int64_t n, const uint8_t *keys, cudaStream_t s) {
     if (n > 0) k_apply_patches<<<(int)((n + 127) / 128 < 2048 ? (n + 127) / 128 : 2048), 128, 0, s>>>(st, p, n, keys);
 }
