@@ -157,6 +157,46 @@ def cpu_baseline_run(g, tumor, normal, regions, threads: int, n_regions: int, k:
     return reads / dt, dt, reads
 
 
+def other_k_leg(g, tumor, normal, regions, k: int, steps: int, warmup: int, device: int) -> dict:
+    """The same workload with the other -k setting (reported beside the
+    main line): device-resident reads/s, end-to-end reads/s and the host
+    realigner's time per step."""
+    from rabbitvar_gb300 import api, synth
+    pair = api.SomaticPair(api.default_params(local_realign=k, fisher=1), device=device)
+    pair.upload_reference(tumor.contig, synth.genome_str(g).encode())
+    batches = [api.Batch.from_readset(rs, pinned=True) for rs in (tumor, normal)]
+    n_reads = tumor.n + normal.n
+
+    def step(submit: bool):
+        if submit:
+            pair.submit(batches[0], batches[1], regions)
+        t = time.perf_counter()
+        pair.pileup_realign()
+        dt = time.perf_counter() - t
+        pair.score()
+        _, n = pair.format_records("T", "ctg")
+        return dt, n
+
+    for _ in range(warmup):
+        step(True)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        step(True)
+    e2e_dt = time.perf_counter() - t0
+    for _ in range(warmup):
+        step(False)
+    t0 = time.perf_counter()
+    re_ms, recs = 0.0, 0
+    for _ in range(steps):
+        dt, recs = step(False)
+        re_ms += dt * 1e3
+    dev_dt = time.perf_counter() - t0
+    pair.close()
+    return {"workload": workload(k), "value": n_reads * steps / dev_dt, "e2e": n_reads * steps / e2e_dt,
+            "unit": "reads/s", "ms_per_step": dev_dt / steps * 1e3, "pileup_realign_ms_per_step": re_ms / steps,
+            "records_per_step": recs, "steps": steps, "warmup": warmup}
+
+
 def learned_filter_leg():
     """The learned filter against the hard filter on the deep-panel shape:
     trained on 4 seeded panels, evaluated on 2 held-out ones (planted truth),
@@ -275,6 +315,7 @@ def main():
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--local-realign", "-k", type=int, default=0, choices=[0, 1],
                     help="the reference's -k: 1 adds the realigner's indel passes")
+    ap.add_argument("--no-other-k", action="store_true", help="skip the leg with the other -k setting")
     ap.add_argument("--panel", type=int, default=0, metavar="N",
                     help="batched amplicon panel of N regions (-t -u): one launch for all regions vs one per region")
     args = ap.parse_args()
@@ -298,24 +339,21 @@ def main():
     n_reads = sum(rs.n for _, rs in samples)
     alg_read_bytes = sum(read_alg_bytes(rs) for _, rs in samples)
 
-    host_ms = {"pileup": 0.0, "realign": 0.0, "score": 0.0, "format": 0.0}
+    host_ms = {"pileup+realign": 0.0, "score": 0.0, "format": 0.0}
 
     def kernels_of():
         return sum(c.timings()["kernels"] for c in ctxs)
 
     def device_step(collect=None):
         t0 = time.perf_counter()
-        pair.pileup()
-        t1 = time.perf_counter()
-        pair.realign()
+        pair.pileup_realign()
         t2 = time.perf_counter()
         pair.score()
         t3 = time.perf_counter()
         text, n = pair.format_records("T", "ctg")
         t4 = time.perf_counter()
         if collect is not None:
-            host_ms["pileup"] += (t1 - t0) * 1e3
-            host_ms["realign"] += (t2 - t1) * 1e3
+            host_ms["pileup+realign"] += (t2 - t0) * 1e3
             host_ms["score"] += (t3 - t2) * 1e3
             host_ms["format"] += (t4 - t3) * 1e3
             collect.extend(c.stage_times() for c in ctxs)
@@ -327,8 +365,7 @@ def main():
         # both uploads are queued first (each context has its own stream), so
         # the second sample's copy overlaps the first sample's kernels
         pair.submit(batches[0], batches[1], regions)
-        pair.pileup()
-        pair.realign()
+        pair.pileup_realign()
         pair.score()
         text, n = pair.format_records("T", "ctg")
         io["h2d"] = sum(c.io_bytes()[0] for c in ctxs)
@@ -359,9 +396,15 @@ def main():
     value = n_reads * world * args.steps / dev_dt
     e2e = n_reads * world * args.steps / e2e_dt
     # roofline of the dominant kernel: the tumor sample's k_pileup_tiles
-    # launch (1.33 M reads), event-timed on its stream; stages alternate
-    # tumor, normal
-    tile_ms = statistics.mean(s["pileup_tiles"] for s in stages[0::2])
+    # launch (1.33 M reads), event-timed on its stream.  In the timed steps
+    # the two samples' kernels share the GPU (one stream each), so the launch
+    # is also timed alone, right after the timed region, on the same batch.
+    tile_ms_shared = statistics.mean(s["pileup_tiles"] for s in stages[0::2])
+    solo = []
+    for _ in range(3):
+        pair.tumor.pileup()
+        solo.append(pair.tumor.stage_times()["pileup_tiles"])
+    tile_ms = statistics.mean(solo)
     cells = sum(r[1] - r[0] + 1 for r in regions)
     per_launch_bytes = read_alg_bytes(tumor) + cells * 256 + CONTIG  # reads + site records + reference window
     achieved = per_launch_bytes / (tile_ms * 1e-3) / 1e9
@@ -381,13 +424,18 @@ def main():
         "host_call_ms_per_step": {k: v / args.steps for k, v in host_ms.items()},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": PILEUP_TRAFFIC, "peak_kind": peak_kind,
-                     "kernel": "k_pileup_tiles", "launch": "tumor sample, 1.33 M reads",
-                     "alg_bytes_per_launch": per_launch_bytes, "launch_ms": tile_ms},
+                     "kernel": "k_pileup_tiles", "launch": "tumor sample, 1.33 M reads, timed alone",
+                     "alg_bytes_per_launch": per_launch_bytes, "launch_ms": tile_ms,
+                     "launch_ms_sharing_gpu": tile_ms_shared},
         "clocks": clk,
     }
     # sites/s: region positions of both samples scored per second of k_score
     score_ms = statistics.mean(s["score"] for s in stages)
     out["sites_per_s"] = (sum(r[1] - r[0] + 1 for r in regions)) / (score_ms * 1e-3)
+    pair.close()
+    if rank == 0 and not args.no_other_k:
+        out["other_k"] = other_k_leg(g, tumor, normal, regions, 1 - args.local_realign, args.steps,
+                                     args.warmup, local)
     if rank == 0 and not args.no_learned:
         out["learned_filter"] = learned_filter_leg()
     if rank == 0 and not args.no_cpu_baseline:
@@ -396,7 +444,6 @@ def main():
                                "sample": f"first {CPU_TILES} of 100 10-kb tiles, tumor+normal ({nr} reads, {dt:.1f} s)"}
     if rank == 0:
         print(json.dumps(out))
-    pair.close()
     if dist is not None:
         dist.destroy_process_group()
 

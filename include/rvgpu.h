@@ -185,6 +185,12 @@ rv_status rv_call_regions(rv_ctx *ctx, const rv_read_batch *reads, const rv_regi
  * The text belongs to `tumor` until its next call.  rv_call_somatic runs the
  * whole sequence. */
 rv_status rv_score_pair(rv_ctx *tumor, rv_ctx *normal);
+
+/* rv_pileup then rv_realign on both samples of a pair, overlapped: both
+ * samples' pileup kernels are queued first (each context has its own
+ * stream) and the tumor's host realigner runs while the normal's pileup is
+ * on the device.  Same results and errors as the four calls in sequence. */
+rv_status rv_pileup_realign_pair(rv_ctx *tumor, rv_ctx *normal);
 rv_status rv_format_somatic(rv_ctx *tumor, rv_ctx *normal, const char *sample, const char *gene,
                             const char **text, size_t *text_len, int64_t *n_records);
 rv_status rv_call_somatic(rv_ctx *tumor, rv_ctx *normal, const rv_read_batch *tumor_reads,

@@ -65,7 +65,7 @@ class SiteRecord(C.Structure):
 
 EXPORTS = ["rv_default_params", "rv_create", "rv_destroy", "rv_last_error", "rv_upload_reference",
            "rv_submit_batch", "rv_pileup", "rv_realign", "rv_score", "rv_format_records", "rv_fetch_records",
-           "rv_call_regions", "rv_score_candidates", "rv_candidates", "rv_score_pair", "rv_format_somatic", "rv_call_somatic", "rv_export_maps", "rv_last_timings", "rv_stage_times", "rv_io_bytes", "rv_fisher_batch", "rv_bam_read",
+           "rv_call_regions", "rv_score_candidates", "rv_candidates", "rv_score_pair", "rv_pileup_realign_pair", "rv_format_somatic", "rv_call_somatic", "rv_export_maps", "rv_last_timings", "rv_stage_times", "rv_io_bytes", "rv_fisher_batch", "rv_bam_read",
            "rv_bam_contigs", "rv_bam_batch", "rv_bam_free", "rv_fasta_read", "rv_free", "rv_alloc_pinned",
            "rv_free_pinned", "rv_mlp_create", "rv_mlp_destroy", "rv_mlp_last_error", "rv_mlp_set_params",
            "rv_mlp_get_params", "rv_mlp_train", "rv_mlp_gradients", "rv_mlp_predict", "rv_mlp_step_ms"]
@@ -97,6 +97,7 @@ def lib():
                                     C.POINTER(i64)]
     L.rv_fetch_records.argtypes = [vp, C.POINTER(SiteRecord), sz, C.POINTER(sz)]
     L.rv_score_pair.argtypes = [vp, vp]
+    L.rv_pileup_realign_pair.argtypes = [vp, vp]
     L.rv_score_candidates.argtypes = [vp, C.c_int]
     L.rv_candidates.argtypes = [vp, vp, vp, i64, C.POINTER(i64)]
     L.rv_format_somatic.argtypes = [vp, vp, C.c_char_p, C.c_char_p, C.POINTER(C.c_char_p), C.POINTER(sz),
@@ -326,6 +327,11 @@ class SomaticPair:
     def realign(self):
         self.tumor.realign()
         self.normal.realign()
+
+    def pileup_realign(self):
+        """pileup() then realign(), overlapped: the tumor's host realigner
+        runs while the normal's pileup kernels are on the device."""
+        self.tumor._check(self.tumor.L.rv_pileup_realign_pair(self.tumor.h, self.normal.h))
 
     def score(self):
         self.tumor._check(self.tumor.L.rv_score_pair(self.tumor.h, self.normal.h))

@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "rv_ctx.h"
+#include "rv_pool.h"
 
 namespace rv {
 rv_status host_realign_mnp(rv_ctx *ctx);
@@ -324,8 +325,40 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
     cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
     const int64_t n = b->n_reads;
     if (n < 0 || b->n_cigar_words < 0 || b->n_bases < 0) return RV_ERR_ARG;
-    for (int64_t i = 0; i < n; i++)
-        if (b->base_off[i] & 31) { ctx->err = "base_off must be a multiple of 32"; return RV_ERR_ARG; }
+    PhaseTimer tm("submit");
+    // batch-wide bounds used to size the per-region cell ranges, and the
+    // base_off alignment check (host threads over chunks of reads)
+    int max_span = 1, max_lq = 1;
+    bool misaligned = false;
+    {
+        const int64_t nch = chunks_for(n, 1 << 16);
+        std::vector<int> ms((size_t)nch, 1), ml((size_t)nch, 1);
+        std::vector<uint8_t> bad((size_t)nch, 0);
+        parallel_chunks(n, 1 << 16, [&](int64_t k, int64_t a, int64_t e) {
+            int msp = 1, mlq = 1;
+            uint8_t bd = 0;
+            for (int64_t i = a; i < e; i++) {
+                bd |= (uint8_t)((b->base_off[i] & 31) != 0);
+                const uint32_t *c = b->cigar + b->cig_off[i];
+                int sp = 0;
+                for (int q = 0; q < b->n_cigar[i]; q++) {
+                    int o = c[q] & 15;
+                    if (o == 0 || o == 2 || o == 3 || o == 7 || o == 8) sp += (int)(c[q] >> 4);
+                }
+                msp = std::max(msp, sp);
+                mlq = std::max(mlq, (int)b->l_qseq[i]);
+            }
+            ms[k] = msp;
+            ml[k] = mlq;
+            bad[k] = bd;
+        });
+        for (int64_t k = 0; k < nch; k++) {
+            max_span = std::max(max_span, ms[k]);
+            max_lq = std::max(max_lq, ml[k]);
+            misaligned |= bad[k] != 0;
+        }
+    }
+    if (misaligned) { ctx->err = "base_off must be a multiple of 32"; return RV_ERR_ARG; }
     ctx->n_reads = n;
     ctx->n_cigar_words = b->n_cigar_words;
     ctx->n_bases = b->n_bases;
@@ -349,20 +382,7 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
     ctx->cap_bases = cb;
     ctx->io_h2d = n * (4 + 4 + 4 + 4 + 2 + 2 + 1 + 4 + 8) + b->n_cigar_words * 4 + (b->n_bases + 1) / 2 + b->n_bases;
     ctx->io_d2h = 0;
-    if (n > 0) {
-        RV_CUDA(cudaMemcpyAsync(ctx->d_pos, b->pos, n * 4, cudaMemcpyHostToDevice, s));
-        RV_CUDA(cudaMemcpyAsync(ctx->d_mpos, b->mpos, n * 4, cudaMemcpyHostToDevice, s));
-        RV_CUDA(cudaMemcpyAsync(ctx->d_nm, b->nm, n * 4, cudaMemcpyHostToDevice, s));
-        RV_CUDA(cudaMemcpyAsync(ctx->d_lq, b->l_qseq, n * 4, cudaMemcpyHostToDevice, s));
-        RV_CUDA(cudaMemcpyAsync(ctx->d_flag, b->flag, n * 2, cudaMemcpyHostToDevice, s));
-        RV_CUDA(cudaMemcpyAsync(ctx->d_ncig, b->n_cigar, n * 2, cudaMemcpyHostToDevice, s));
-        RV_CUDA(cudaMemcpyAsync(ctx->d_mapq, b->mapq, n, cudaMemcpyHostToDevice, s));
-        RV_CUDA(cudaMemcpyAsync(ctx->d_cigoff, b->cig_off, n * 4, cudaMemcpyHostToDevice, s));
-        RV_CUDA(cudaMemcpyAsync(ctx->d_boff, b->base_off, n * 8, cudaMemcpyHostToDevice, s));
-        RV_CUDA(cudaMemcpyAsync(ctx->d_cigar, b->cigar, b->n_cigar_words * 4, cudaMemcpyHostToDevice, s));
-        RV_CUDA(cudaMemcpyAsync(ctx->d_seq, b->seq, (size_t)(b->n_bases + 1) / 2, cudaMemcpyHostToDevice, s));
-        RV_CUDA(cudaMemcpyAsync(ctx->d_qual, b->qual, (size_t)b->n_bases, cudaMemcpyHostToDevice, s));
-    }
+    tm.lap("prep+alloc");
     // -k 1: the alignment spans stay on the host for noPassingReads
     if (ctx->params.local_realign) {
         ctx->h_pos.assign(b->pos, b->pos + n);
@@ -376,18 +396,6 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
         ctx->h_ncig.clear();
         ctx->h_cigoff.clear();
         ctx->h_cigar.clear();
-    }
-    // batch-wide bounds used to size the per-region cell ranges
-    int max_span = 1, max_lq = 1;
-    for (int64_t i = 0; i < n; i++) {
-        const uint32_t *c = b->cigar + b->cig_off[i];
-        int sp = 0;
-        for (int k = 0; k < b->n_cigar[i]; k++) {
-            int o = c[k] & 15;
-            if (o == 0 || o == 2 || o == 3 || o == 7 || o == 8) sp += (int)(c[k] >> 4);
-        }
-        max_span = std::max(max_span, sp);
-        max_lq = std::max(max_lq, (int)b->l_qseq[i]);
     }
     const int pad = max_span + max_lq + 4;
     const rv_params &P = ctx->params;
@@ -560,15 +568,36 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
         RV_CUDA(cudaMalloc((void **)&ctx->d_cand, (size_t)want_cand * sizeof(CandVar)));
         ctx->cand_cap = want_cand;
     }
+    tm.lap("regions+dedup+buffers");
+    // the read arrays last: the small pageable copies above are staged before
+    // these large pinned copies are queued, so none of them waits on the batch
+    // upload
+    if (n > 0) {
+        RV_CUDA(cudaMemcpyAsync(ctx->d_pos, b->pos, n * 4, cudaMemcpyHostToDevice, s));
+        RV_CUDA(cudaMemcpyAsync(ctx->d_mpos, b->mpos, n * 4, cudaMemcpyHostToDevice, s));
+        RV_CUDA(cudaMemcpyAsync(ctx->d_nm, b->nm, n * 4, cudaMemcpyHostToDevice, s));
+        RV_CUDA(cudaMemcpyAsync(ctx->d_lq, b->l_qseq, n * 4, cudaMemcpyHostToDevice, s));
+        RV_CUDA(cudaMemcpyAsync(ctx->d_flag, b->flag, n * 2, cudaMemcpyHostToDevice, s));
+        RV_CUDA(cudaMemcpyAsync(ctx->d_ncig, b->n_cigar, n * 2, cudaMemcpyHostToDevice, s));
+        RV_CUDA(cudaMemcpyAsync(ctx->d_mapq, b->mapq, n, cudaMemcpyHostToDevice, s));
+        RV_CUDA(cudaMemcpyAsync(ctx->d_cigoff, b->cig_off, n * 4, cudaMemcpyHostToDevice, s));
+        RV_CUDA(cudaMemcpyAsync(ctx->d_boff, b->base_off, n * 8, cudaMemcpyHostToDevice, s));
+        RV_CUDA(cudaMemcpyAsync(ctx->d_cigar, b->cigar, b->n_cigar_words * 4, cudaMemcpyHostToDevice, s));
+        RV_CUDA(cudaMemcpyAsync(ctx->d_seq, b->seq, (size_t)(b->n_bases + 1) / 2, cudaMemcpyHostToDevice, s));
+        RV_CUDA(cudaMemcpyAsync(ctx->d_qual, b->qual, (size_t)b->n_bases, cudaMemcpyHostToDevice, s));
+    }
+    tm.lap("queue copies");
     ctx->stage = 1;
     return RV_OK;
 }
 
-rv_status rv_pileup(rv_ctx *ctx, void *stream) {
-    if (!ctx) return RV_ERR_ARG;
+namespace {
+
+// Queues the pileup kernels of the submitted batch on stream s without
+// waiting for them; pileup_finish waits and reads the device error word.
+rv_status pileup_launch(rv_ctx *ctx, cudaStream_t s) {
     if (ctx->stage < 1) { ctx->err = "rv_pileup before rv_submit_batch"; return RV_ERR_STATE; }
     RV_CUDA(cudaSetDevice(ctx->device));
-    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
     size_t cap = ctx->cap_cells;
     RV_CUDA(cudaEventRecord(ctx->ev[0], s));
     RV_CUDA(cudaMemsetAsync(ctx->d_cellmem, 0, cap * (8 * 16 + 4 + 1), s));
@@ -606,9 +635,21 @@ rv_status rv_pileup(rv_ctx *ctx, void *stream) {
     RV_CUDA(cudaGetLastError());
     RV_CUDA(cudaEventRecord(ctx->ev[1], s));
     ctx->kernels = 8;  // init_slots, region_spans, edge_detect, pileup_tiles, serial, resolve, link, collisions
+    ctx->pileup_pin = pin && *pin;
+    ctx->stage = 1;  // launched, not finished
+    ctx->pileup_pending = true;
+    return RV_OK;
+}
+
+// Waits for the pileup queued by pileup_launch; timings, autotuner, errors.
+rv_status pileup_finish(rv_ctx *ctx, cudaStream_t s) {
+    if (!ctx->pileup_pending) { ctx->err = "no pileup in flight"; return RV_ERR_STATE; }
+    ctx->pileup_pending = false;
+    RV_CUDA(cudaSetDevice(ctx->device));
     unsigned int err = 0;
     RV_CUDA(cudaMemcpyAsync(&err, ctx->d_counters + CNT_ERR, 4, cudaMemcpyDeviceToHost, s));
     RV_CUDA(cudaStreamSynchronize(s));
+    const int nvar = pileup_variants(), variant = ctx->variant;
     float ms = 0;
     cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
     ctx->pileup_ms = ms;
@@ -620,7 +661,7 @@ rv_status rv_pileup(rv_ctx *ctx, void *stream) {
     }
     cudaEventElapsedTime(&ms, ctx->ev[7], ctx->ev[1]);
     ctx->stage_ms[4] = ms;
-    if (!(pin && *pin) && ctx->variant_runs < nvar) {
+    if (!ctx->pileup_pin && ctx->variant_runs < nvar) {
         ctx->variant_ms[variant] = ctx->stage_ms[2];
         ctx->variant_runs++;
     }
@@ -634,6 +675,16 @@ rv_status rv_pileup(rv_ctx *ctx, void *stream) {
     }
     ctx->stage = 2;
     return RV_OK;
+}
+
+}  // namespace
+
+rv_status rv_pileup(rv_ctx *ctx, void *stream) {
+    if (!ctx) return RV_ERR_ARG;
+    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+    rv_status st = pileup_launch(ctx, s);
+    if (st) return st;
+    return pileup_finish(ctx, s);
 }
 
 rv_status rv_realign(rv_ctx *ctx, void *stream) {
@@ -814,12 +865,41 @@ rv_status rv_score_pair(rv_ctx *tumor, rv_ctx *normal) {
         return RV_ERR_ARG;
     }
     rv_status s;
+    PhaseTimer tm("score_pair");
     if ((s = rv_score(tumor, nullptr))) return s;
     if ((s = rv_score(normal, nullptr))) { tumor->err = normal->err; return s; }
+    tm.lap("score");
     // every position where one sample has a candidate is needed in both
     std::vector<int2> pt = positions_of(tumor), pn = positions_of(normal);
+    tm.lap("positions");
     if ((s = score_list(tumor, missing(pn, pt)))) return s;
     if ((s = score_list(normal, missing(pt, pn)))) { tumor->err = normal->err; return s; }
+    tm.lap("score_list");
+    return RV_OK;
+}
+
+rv_status rv_pileup_realign_pair(rv_ctx *tumor, rv_ctx *normal) {
+    if (!tumor || !normal || tumor == normal) return RV_ERR_ARG;
+    rv_status s;
+    // both samples' kernels are queued first (one stream each); the tumor's
+    // host realigner then runs while the normal's pileup is on the device
+    if ((s = pileup_launch(tumor, tumor->stream))) return s;
+    if ((s = pileup_launch(normal, normal->stream))) {
+        tumor->err = normal->err;
+        pileup_finish(tumor, tumor->stream);
+        return s;
+    }
+    rv_status st = pileup_finish(tumor, tumor->stream);
+    if (st) {
+        pileup_finish(normal, normal->stream);
+        return st;
+    }
+    if ((st = rv_realign(tumor, nullptr))) {
+        pileup_finish(normal, normal->stream);
+        return st;
+    }
+    if ((s = pileup_finish(normal, normal->stream))) { tumor->err = normal->err; return s; }
+    if ((s = rv_realign(normal, nullptr))) { tumor->err = normal->err; return s; }
     return RV_OK;
 }
 
@@ -846,10 +926,7 @@ rv_status rv_call_somatic(rv_ctx *tumor, rv_ctx *normal, const rv_read_batch *tu
     rv_status s;
     if ((s = rv_submit_batch(tumor, tumor_reads, regions, n_regions, nullptr))) return s;
     if ((s = rv_submit_batch(normal, normal_reads, regions, n_regions, nullptr))) { tumor->err = normal->err; return s; }
-    if ((s = rv_pileup(tumor, nullptr))) return s;
-    if ((s = rv_pileup(normal, nullptr))) { tumor->err = normal->err; return s; }
-    if ((s = rv_realign(tumor, nullptr))) return s;
-    if ((s = rv_realign(normal, nullptr))) { tumor->err = normal->err; return s; }
+    if ((s = rv_pileup_realign_pair(tumor, normal))) return s;
     if ((s = rv_score_pair(tumor, normal))) return s;
     return rv_format_somatic(tumor, normal, sample, gene, text, text_len, n_records);
 }

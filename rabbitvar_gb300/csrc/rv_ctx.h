@@ -2,6 +2,9 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <string>
 #include <vector>
 
@@ -69,6 +72,21 @@ void launch_apply_patches(const DevState &st, const Patch *p, int64_t n, const u
 // flattened per-cell key lists (-k 1 realigner mirror): 5 launches, then 1
 void launch_list_offsets(const DevState &st, uint32_t *off, uint32_t *bsum, cudaStream_t s);
 void launch_list_fill(const DevState &st, const uint32_t *off, Slot *out, uint32_t *out_idx, cudaStream_t s);
+
+// Host phase timer: with RV_TRACE set in the environment, each lap prints
+// "<scope> <phase> <ms>" to stderr (diagnostics only; no effect on results).
+struct PhaseTimer {
+    const char *scope;
+    bool on;
+    std::chrono::steady_clock::time_point t;
+    explicit PhaseTimer(const char *s) : scope(s), on(getenv("RV_TRACE") != nullptr), t(std::chrono::steady_clock::now()) {}
+    void lap(const char *phase) {
+        if (!on) return;
+        auto n = std::chrono::steady_clock::now();
+        fprintf(stderr, "trace %s %s %.3f\n", scope, phase, std::chrono::duration<double, std::milli>(n - t).count());
+        t = n;
+    }
+};
 
 template <class T>
 struct DevBuf {
@@ -187,6 +205,8 @@ struct rv_ctx {
     int variant = -1;
     double variant_ms[8] = {};
     int variant_runs = 0;
+    bool pileup_pin = false;       // RV_PILEUP_VARIANT pinned the variant of the pileup in flight
+    bool pileup_pending = false;   // pileup queued, not yet finished
     int64_t kernels = 0;
     // bytes moved host<->device since the last rv_submit_batch
     int64_t io_h2d = 0, io_d2h = 0;

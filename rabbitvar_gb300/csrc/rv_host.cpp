@@ -23,6 +23,7 @@
 
 #include "rv_ctx.h"
 #include "rv_mirror.h"
+#include "rv_pool.h"
 #include "rv_records.h"
 
 namespace rv {
@@ -67,27 +68,31 @@ bool is_mnv(const std::string &k) {
 }
 
 
-// findconseq: include/VariationUtils.h:403-509
-std::string clip_consensus(HClip &sc) {
-    if (!sc.cons.empty()) return sc.cons;
+// findconseq: include/VariationUtils.h:403-509, over the per-offset base
+// counts sorted by (offset, clip_rank); sets `used` where the reference marks
+// a low-complexity consensus as used
+std::string consensus_of(const std::vector<NtCount> &nt, int agg_cnt, bool &used) {
+    int nts = 0;
+    for (size_t i = 0; i < nt.size(); i++)
+        if (i == 0 || nt[i].idx != nt[i - 1].idx) nts++;
     int total = 0, match = 0;
     std::string seqq;
     bool flag = false;
-    for (auto &nve : sc.nt) {
-        std::vector<std::pair<char, std::pair<int, double>>> nv(nve.second.begin(), nve.second.end());
-        std::sort(nv.begin(), nv.end(), [](const auto &a, const auto &b) { return clip_rank(a.first) < clip_rank(b.first); });
+    for (size_t i = 0; i < nt.size();) {
+        size_t j = i;
+        while (j < nt.size() && nt[j].idx == nt[i].idx) j++;
         int maxc = 0, tt = 0;
         double maxq = 0;
         char chosen = 0;
-        for (auto &e : nv) {
-            tt += e.second.first;
-            if (e.second.first > maxc || e.second.second > maxq) {
-                maxc = e.second.first;
-                chosen = e.first;
-                maxq = e.second.second;
+        for (size_t k = i; k < j; k++) {
+            tt += nt[k].cnt;
+            if (nt[k].cnt > maxc || nt[k].q > maxq) {
+                maxc = nt[k].cnt;
+                chosen = nt[k].ch;
+                maxq = nt[k].q;
             }
         }
-        if (nve.first == 3 && sc.nt.size() >= 6 && tt / (double)sc.agg.cnt < 0.2 && tt <= 2) break;
+        if (nt[i].idx == 3 && nts >= 6 && tt / (double)agg_cnt < 0.2 && tt <= 2) break;
         if ((tt - maxc > 2 || maxc <= tt - maxc) && maxc / (double)tt < 0.8) {
             if (flag) break;
             flag = true;
@@ -95,8 +100,9 @@ std::string clip_consensus(HClip &sc) {
         total += tt;
         match += maxc;
         if (chosen != 0) seqq += chosen;
+        i = j;
     }
-    int nts = (int)sc.nt.size(), sl = (int)seqq.size();
+    const int sl = (int)seqq.size();
     std::string out;
     if (total != 0 && match / (double)total > 0.9 && sl / 1.5 > nts - sl &&
         (sl / (double)nts > 0.8 || nts - sl < 10 || sl > 25))
@@ -105,7 +111,7 @@ std::string clip_consensus(HClip &sc) {
         out = " ";
     if (out.size() > 12) {
         bool a7 = out.compare(1, 7, "AAAAAAA") == 0, t7 = out.compare(1, 7, "TTTTTTT") == 0;
-        if (a7 || t7) sc.used = true;
+        if (a7 || t7) used = true;
         int len = (int)out.size(), kinds = 0;
         bool low = false;
         for (char b : std::string("ATGC")) {
@@ -113,10 +119,26 @@ std::string clip_consensus(HClip &sc) {
             if (c > 0) kinds++;
             if (c / (double)len > 0.75) low = true;
         }
-        if (low || kinds < 3) sc.used = true;
+        if (low || kinds < 3) used = true;
     }
-    sc.cons = out;
     return out;
+}
+
+void sort_nt(std::vector<NtCount> &nt) {
+    std::sort(nt.begin(), nt.end(), [](const NtCount &a, const NtCount &b) {
+        if (a.idx != b.idx) return a.idx < b.idx;
+        return clip_rank(a.ch) < clip_rank(b.ch);
+    });
+}
+
+std::string clip_consensus(HClip &sc) {
+    if (!sc.cons.empty()) return sc.cons;
+    std::vector<NtCount> nt;
+    for (auto &nve : sc.nt)
+        for (auto &e : nve.second) nt.push_back({nve.first, e.first, e.second.first, e.second.second});
+    sort_nt(nt);
+    sc.cons = consensus_of(nt, sc.agg.cnt, sc.used);
+    return sc.cons;
 }
 
 void add_into(HVar &to, const HVar &v) {  // adjCnt: include/VariationUtils.h:338-352
@@ -559,13 +581,12 @@ static void format_groups(const rv_ctx *ctx, const std::vector<const CandVar *> 
             // adjustVariantCounts (src/ToVarsBuilder.cpp:543-566): negative counts print as 0
             const int rfc = std::max(0, c.rfc), rrc = std::max(0, c.rrc);
             const int afwd = std::max(0, c.fwd), arev = std::max(0, c.rev);
-            char num[64];
             auto add = [&](const std::string &x, bool last = false) {
                 text += x;
                 text += last ? '\n' : '\t';
             };
-            auto addi = [&](long long x) { snprintf(num, sizeof num, "%lld", x); add(num); };
-            auto addf = [&](double x) { snprintf(num, sizeof num, "%f", x); add(num); };
+            auto addi = [&](long long x) { put_int(text, x); text += '\t'; };
+            auto addf = [&](double x) { put_f6(text, x); text += '\t'; };
             add(sample);
             add(gene);
             add(chr);
@@ -657,21 +678,12 @@ rv_status host_format_records(rv_ctx *ctx, const char *sample, const char *gene,
         i = j;
     }
     // candidate positions are independent: split them over host threads
-    int nt = (int)std::min<size_t>(std::max(1u, std::thread::hardware_concurrency()), 32);
-    nt = (int)std::min<size_t>((size_t)nt, std::max<size_t>(1, groups.size() / 64));
+    const int64_t nt = chunks_for((int64_t)groups.size(), 64);
     std::vector<std::string> texts(nt);
     std::vector<std::vector<rv_site_record>> recs(nt);
-    std::vector<std::thread> pool;
-    size_t per = (groups.size() + nt - 1) / std::max(1, nt);
-    for (int t = 0; t < nt; t++) {
-        size_t a = std::min(groups.size(), t * per), b = std::min(groups.size(), (t + 1) * per);
-        auto job = [&, t, a, b]() {
-            format_groups(ctx, order, groups, a, b, sample, gene, texts[t], recs[t], emitted);
-        };
-        if (t + 1 < nt) pool.emplace_back(job);
-        else job();
-    }
-    for (auto &th : pool) th.join();
+    parallel_chunks((int64_t)groups.size(), 64, [&](int64_t t, int64_t a, int64_t b) {
+        format_groups(ctx, order, groups, (size_t)a, (size_t)b, sample, gene, texts[t], recs[t], emitted);
+    });
     ctx->text.clear();
     ctx->h_records.clear();
     for (int t = 0; t < nt; t++) {

@@ -32,7 +32,17 @@ struct HClip {
     bool used = false;
 };
 
-// findconseq (include/VariationUtils.h:403-509), cached in the clip
+// one per-offset base count of a soft clip
+struct NtCount {
+    int idx;
+    char ch;
+    int cnt;
+    double q;
+};
+// findconseq (include/VariationUtils.h:403-509) over counts sorted by sort_nt
+std::string consensus_of(const std::vector<NtCount> &nt, int agg_cnt, bool &used);
+void sort_nt(std::vector<NtCount> &nt);
+// findconseq cached in the clip
 std::string clip_consensus(HClip &sc);
 // adjCnt(to, v) (include/VariationUtils.h:338-352)
 void add_into(HVar &to, const HVar &v);

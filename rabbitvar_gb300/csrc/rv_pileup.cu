@@ -189,26 +189,38 @@ struct SinkBase {
 // addressed in the shared state space (the generic forms cannot be proven not
 // to alias the walker's local-memory object).
 __device__ __forceinline__ void shared_add_u32(uint32_t addr, uint32_t v) {
-    asm volatile("red.shared.add.u32 [%0], %1;" ::"r"(addr), "r"(v) : "memory");
+    asm volatile("red.shared.add.u32 [%0], %1;" ::"r"(addr), "r"(v));
 }
 __device__ __forceinline__ uint32_t shared_ld_u32(uint32_t addr) {
     uint32_t v;
-    asm volatile("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(addr) : "memory");
+    asm volatile("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(addr));
     return v;
 }
 __device__ __forceinline__ void shared_or_u32(uint32_t addr, uint32_t v) {
-    asm volatile("red.shared.or.b32 [%0], %1;" ::"r"(addr), "r"(v) : "memory");
+    asm volatile("red.shared.or.b32 [%0], %1;" ::"r"(addr), "r"(v));
 }
 __device__ __forceinline__ uint32_t shared_cas_u32(uint32_t addr, uint32_t cmp, uint32_t v) {
     uint32_t old;
-    asm volatile("atom.shared.cas.b32 %0, [%1], %2, %3;" : "=r"(old) : "r"(addr), "r"(cmp), "r"(v) : "memory");
+    asm volatile("atom.shared.cas.b32 %0, [%1], %2, %3;" : "=r"(old) : "r"(addr), "r"(cmp), "r"(v));
     return old;
+}
+
+__device__ __forceinline__ uint32_t shared_ld_u8(uint32_t addr) {
+    uint32_t v;
+    asm volatile("ld.shared.u8 %0, [%1];" : "=r"(v) : "r"(addr));
+    return v;
 }
 
 struct TileFast {
     uint32_t w_s;       // shared-space address of the word arrays (w0 | w1 | w2 | first, 4*kTileW words each)
+    uint32_t ref_s;     // shared-space address of the reference bases wlo .. wlo + kTileW - 1
     int wlo;
     double goodq;
+    // reference base at p (inside the region's window): from the tile's shared copy
+    __device__ __forceinline__ char ref(const char *refp, int p) const {
+        unsigned d = (unsigned)(p - wlo);
+        return d < (unsigned)kTileW ? (char)shared_ld_u8(ref_s + d) : __ldg(refp + p - 1);
+    }
     __device__ __forceinline__ bool emit(int p, int b, int dir, int tp, int q, int mapq, int nm) const {
         return emit_any(p, b, dir, tp, q, mapq, nm, true);
     }
@@ -449,6 +461,7 @@ __global__ void __launch_bounds__(kPileupThreads, MINB) k_pileup_tiles(DevState 
     uint32_t *w2 = w1 + 4 * TW;
     uint32_t *first = w2 + 4 * TW;
     __shared__ int s_tile, s_wlo;
+    __shared__ char s_ref[TW];
     for (;;) {
         if (threadIdx.x == 0) {
             s_tile = (int)atomicAdd(st.tile_counter, 1u);
@@ -467,6 +480,11 @@ __global__ void __launch_bounds__(kPileupThreads, MINB) k_pileup_tiles(DevState 
         for (int i = threadIdx.x; i < 4 * 4 * TW; i += blockDim.x) w0[i] = 0u;
         __syncthreads();
         int wlo = max(s_wlo, R.clo);
+        for (int i = threadIdx.x; i < TW; i += blockDim.x) {
+            int p = wlo + i;  // 1-based; the walk reads it only inside [ws, we]
+            s_ref[i] = (p >= 1 && p <= st.ref_len) ? st.ref[p - 1] : (char)0;
+        }
+        __syncthreads();
         TileSink sink;
         sink.st = &st;
         sink.P = &P;
@@ -474,6 +492,7 @@ __global__ void __launch_bounds__(kPileupThreads, MINB) k_pileup_tiles(DevState 
         sink.region_idx = tile.region;
         sink.f.w_s = (uint32_t)__cvta_generic_to_shared(w0);
         sink.f.wlo = wlo;
+        sink.f.ref_s = (uint32_t)__cvta_generic_to_shared(s_ref);
         sink.f.goodq = P.goodq;
         {
             Walker<TileSink> w(P, sink, R, st.ref, st.ref_len);

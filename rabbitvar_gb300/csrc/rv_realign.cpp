@@ -32,6 +32,7 @@
 #include <vector>
 
 #include "rv_mirror.h"
+#include "rv_pool.h"
 
 namespace rv {
 
@@ -312,20 +313,21 @@ struct RegionRealigner {
         auto it = sc.find(p);
         return it == sc.end() ? nullptr : &it->second;
     }
-    string consensus(Clip &k) {
+    const string &consensus(Clip &k) {
         if (!k.loaded) {
             k.loaded = true;
+            std::vector<NtCount> nt;
             if (k.cell >= 0)
                 for (uint32_t i = mir.off[k.cell]; i < mir.off[k.cell + 1]; i++) {
                     const Slot &s = mir.slots[i];
-                    if (s.kind != k.seq_kind) continue;
-                    string key = mir.key(i);
-                    if (key.size() != 3) continue;
-                    int idx = (uint8_t)key[0] | ((uint8_t)key[1] << 8);
-                    k.c.nt[idx][key[2]] = {s.obs, s.q_sum};
+                    if (s.kind != k.seq_kind || s.klen != 3 || (size_t)s.koff + 3 > ctx->h_arena.size()) continue;
+                    const uint8_t *kb = ctx->h_arena.data() + s.koff;
+                    nt.push_back({kb[0] | (kb[1] << 8), (char)kb[2], s.obs, s.q_sum});
                 }
+            sort_nt(nt);
+            k.c.cons = consensus_of(nt, k.c.agg.cnt, k.c.used);
         }
-        return clip_consensus(k.c);
+        return k.c.cons;
     }
     void add_cov(int p, int n) { cov_add[p] += n; }
 
@@ -938,7 +940,7 @@ struct RegionRealigner {
             Clip &sc5v = *a.c;
             const int cnt5 = a.cnt;
             if (sc5v.c.used) continue;
-            string seq5 = consensus(sc5v);
+            const string &seq5 = consensus(sc5v);
             if (seq5.size() <= 10) continue;
             for (T &b : t3) {
                 try {
@@ -949,7 +951,7 @@ struct RegionRealigner {
                     if (sc3v.c.used) continue;
                     if (p5 - p3 > max_rl * 2.5) continue;
                     if (p3 - p5 > max_rl - 10) continue;
-                    string seq3 = consensus(sc3v);
+                    const string &seq3 = consensus(sc3v);
                     if (seq3.size() <= 10) continue;
                     if (!(cnt5 / (double)cnt3 >= 0.08 && cnt5 / (double)cnt3 <= 12)) continue;
                     int bp5, bp3, score;
@@ -1281,31 +1283,21 @@ rv_status host_realign_full(rv_ctx *ctx) {
     const int nreg = (int)ctx->regions.size();
     std::vector<std::vector<Patch>> patches((size_t)nreg);
     std::vector<string> keys((size_t)nreg);
-    unsigned hw = std::thread::hardware_concurrency();
-    int nt = std::max(1, std::min<int>(nreg, (int)std::min(hw ? hw : 1u, 16u)));
-    std::atomic<int> next{0};
+    const int nt = pool_threads();
     std::mutex err_mu;
     string failure;
-    std::vector<double> phase((size_t)nt * 8, 0.0);
-    std::atomic<int> tid{0};
-    auto work = [&]() {
-        double *ph = phase.data() + 8 * tid.fetch_add(1);
-        for (int r; (r = next.fetch_add(1)) < nreg;) {
-            try {
-                RegionRealigner rr(mir, ctx, r);
-                rr.run(patches[r], keys[r], ph);
-            } catch (const std::exception &e) {
-                // the reference's own realigner terminates here (an exception
-                // it does not catch); the batch reports it instead
-                std::lock_guard<std::mutex> g(err_mu);
-                if (failure.empty()) failure = "realigner, region " + std::to_string(r) + ": " + e.what();
-            }
+    std::vector<double> phase((size_t)nreg * 8, 0.0);
+    parallel_for(nreg, [&](int64_t r) {
+        try {
+            RegionRealigner rr(mir, ctx, (int)r);
+            rr.run(patches[r], keys[r], phase.data() + 8 * r);
+        } catch (const std::exception &e) {
+            // the reference's own realigner terminates here (an exception it
+            // does not catch); the batch reports it instead
+            std::lock_guard<std::mutex> g(err_mu);
+            if (failure.empty()) failure = "realigner, region " + std::to_string(r) + ": " + e.what();
         }
-    };
-    std::vector<std::thread> th;
-    for (int t = 1; t < nt; t++) th.emplace_back(work);
-    work();
-    for (auto &t : th) t.join();
+    });
     if (!failure.empty()) {
         ctx->err = failure;
         return RV_ERR_UNSUPPORTED;
@@ -1323,8 +1315,8 @@ rv_status host_realign_full(rv_ctx *ctx) {
     st = apply_patches(ctx, all, all_keys);
     if (trace) {
         double sum[6] = {0};
-        for (int t = 0; t < nt; t++)
-            for (int k = 0; k < 6; k++) sum[k] += phase[8 * t + k];
+        for (int r = 0; r < nreg; r++)
+            for (int k = 0; k < 6; k++) sum[k] += phase[8 * r + k];
         fprintf(stderr, "realign -k 1: listed keys %u, patches %zu, threads %d; ms: fetch %.2f run %.2f total %.2f; "
                 "thread-ms: setup %.2f mnp %.2f del %.2f ins %.2f lgins %.2f diff %.2f\n", total,
                 all.size(), nt, t_fetch, t_run, ms(t0), sum[0], sum[1], sum[2], sum[3], sum[4], sum[5]);

@@ -269,11 +269,5 @@ void adj_complex(RecVar &v) {
     }
 }
 
-std::string f6(double d) {
-    char b[64];
-    snprintf(b, sizeof b, "%f", d);
-    return b;
-}
-
 }  // namespace recs
 }  // namespace rv

@@ -5,6 +5,9 @@
 // isGoodVar / adjComplex (include/Variant.h:99-248).
 #pragma once
 
+#include <charconv>
+#include <cmath>
+#include <cstdio>
 #include <string>
 
 #include "rv_ctx.h"
@@ -45,7 +48,29 @@ std::string var_type(const RecVar &v);
 // Variant::isGoodVar; an empty `type` means the variant's own varType()
 bool good_var(const RecVar &v, const CandVar *ref, const rv_params &P, const std::string &type);
 void adj_complex(RecVar &v);
-std::string f6(double d);
+// printf("%f") and printf("%lld") appended to o: std::to_chars gives the
+// same correctly rounded digits as printf; non-finite values go through
+// snprintf for its exact spelling
+inline void put_f6(std::string &o, double d) {
+    char b[352];
+    if (!std::isfinite(d)) {
+        snprintf(b, sizeof b, "%f", d);
+        o += b;
+        return;
+    }
+    auto r = std::to_chars(b, b + sizeof b, d, std::chars_format::fixed, 6);
+    if (r.ec != std::errc()) {
+        snprintf(b, sizeof b, "%f", d);
+        o += b;
+        return;
+    }
+    o.append(b, r.ptr);
+}
+inline void put_int(std::string &o, long long x) {
+    char b[24];
+    auto r = std::to_chars(b, b + sizeof b, x);
+    o.append(b, r.ptr);
+}
 inline bool starts(const std::string &s, char c) { return !s.empty() && s[0] == c; }
 
 }  // namespace recs

@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "rv_ctx.h"
+#include "rv_pool.h"
 #include "rv_records.h"
 
 namespace rv {
@@ -290,9 +291,8 @@ void put_stats(std::string &o, const Rec &r, const SVar *v) {
         for (int i = 0; i < 18; i++) o += "0\t";
         return;
     }
-    char b[64];
-    auto I = [&](long long x) { snprintf(b, sizeof b, "%lld\t", x); o += b; };
-    auto F = [&](double x) { snprintf(b, sizeof b, "%f\t", x); o += b; };
+    auto I = [&](long long x) { put_int(o, x); o += '\t'; };
+    auto F = [&](double x) { put_f6(o, x); o += '\t'; };
     const CandVar &c = v->c;
     I(c.tpc);
     I(c.pc);
@@ -320,51 +320,31 @@ void put_stats(std::string &o, const Rec &r, const SVar *v) {
 // put_fisher_ext_and_odds (:130-149): the p-value, then a float32 log ratio
 // with +0.5 pseudocounts
 void put_fisher(std::string &o, double p, const int32_t *t) {
-    char b[64];
-    snprintf(b, sizeof b, "%f\t", p);
-    o += b;
+    put_f6(o, p);
+    o += '\t';
     const float a = t[0] + 0.5, bb = t[1] + 0.5, c = t[2] + 0.5, d = t[3] + 0.5;
     const float ad = a * d, bc = bb * c;
     const float ratio = std::log(ad / bc + bc / ad);
-    snprintf(b, sizeof b, "%f\t", (double)ratio);
-    o += b;
-}
-
-// Runs fn(thread, begin, end) over [0, n) split into contiguous chunks on
-// up to `max_threads` host threads (the calling thread takes the last chunk).
-template <class F>
-void parallel_chunks(size_t n, size_t min_per_thread, F fn) {
-    size_t nt = std::min<size_t>(std::max(1u, std::thread::hardware_concurrency()), 32);
-    nt = std::max<size_t>(1, std::min(nt, n / std::max<size_t>(1, min_per_thread)));
-    size_t per = (n + nt - 1) / nt;
-    std::vector<std::thread> pool;
-    for (size_t k = 0; k < nt; k++) {
-        size_t a = std::min(n, k * per), b = std::min(n, (k + 1) * per);
-        if (k + 1 < nt) pool.emplace_back(fn, k, a, b);
-        else fn(k, a, b);
-    }
-    for (auto &th : pool) th.join();
-}
-
-size_t threads_for(size_t n, size_t min_per_thread) {
-    size_t nt = std::min<size_t>(std::max(1u, std::thread::hardware_concurrency()), 32);
-    return std::max<size_t>(1, std::min(nt, n / std::max<size_t>(1, min_per_thread)));
+    put_f6(o, (double)ratio);
+    o += '\t';
 }
 
 }  // namespace
 
 rv_status host_format_somatic(rv_ctx *t, rv_ctx *n, const char *sample, const char *gene) {
+    PhaseTimer pt("format_somatic");
     const rv_params &P = t->params;
     std::vector<const CandVar *> to, no;
     std::vector<std::pair<size_t, size_t>> tg, ng;
     group(t, to, tg);
     group(n, no, ng);
+    pt.lap("group");
     // positions are independent: classify them on host threads, keeping order
-    const size_t kMinPos = 64;
-    std::vector<std::vector<Rec>> part(threads_for(tg.size(), kMinPos));
-    parallel_chunks(tg.size(), kMinPos, [&](size_t k, size_t a, size_t b) {
+    const int64_t kMinPos = 64;
+    std::vector<std::vector<Rec>> part(chunks_for((int64_t)tg.size(), kMinPos));
+    parallel_chunks((int64_t)tg.size(), kMinPos, [&](int64_t k, int64_t a, int64_t b) {
         Classifier C{P, part[k]};
-        for (size_t gi = a; gi < b; gi++) {
+        for (size_t gi = (size_t)a; gi < (size_t)b; gi++) {
             SPos v1;
             build_position(t, &to[tg[gi].first], tg[gi].second - tg[gi].first, v1);
             auto key = std::make_pair(v1.region, v1.pos);
@@ -384,6 +364,7 @@ rv_status host_format_somatic(rv_ctx *t, rv_ctx *n, const char *sample, const ch
             else C.second_sample(v1, v2);
         }
     });
+    pt.lap("classify");
     std::vector<Rec> recs;
     for (auto &pv : part)
         for (auto &r : pv) recs.push_back(std::move(r));
@@ -409,12 +390,13 @@ rv_status host_format_somatic(rv_ctx *t, rv_ctx *n, const char *sample, const ch
         rv_status s = device_fisher(t, tab.data(), (int64_t)recs.size() * 3, p2.data());
         if (s) return s;
     }
+    pt.lap("fisher");
     const Region *regs = t->regions.data();
-    std::vector<std::string> texts(threads_for(recs.size(), 256));
-    parallel_chunks(recs.size(), 256, [&](size_t k, size_t i0, size_t i1) {
+    std::vector<std::string> texts(chunks_for((int64_t)recs.size(), 256));
+    parallel_chunks((int64_t)recs.size(), 256, [&](int64_t k, int64_t i0, int64_t i1) {
     std::string &o = texts[k];
     char b[96];
-    for (size_t i = i0; i < i1; i++) {
+    for (size_t i = (size_t)i0; i < (size_t)i1; i++) {
         const Rec &r = recs[i];
         o += sample;
         o += '\t';
@@ -423,8 +405,10 @@ rv_status host_format_somatic(rv_ctx *t, rv_ctx *n, const char *sample, const ch
         o += t->chr;
         o += '\t';
         if (r.has_beg) {
-            snprintf(b, sizeof b, "%d\t%d\t", r.beg.r.startp, r.beg.r.endp);
-            o += b;
+            put_int(o, r.beg.r.startp);
+            o += '\t';
+            put_int(o, r.beg.r.endp);
+            o += '\t';
             o += r.beg.r.refallele + "\t" + r.beg.r.varallele + "\t";
         } else {
             o += "0\t0\t0\t0\t";
@@ -440,8 +424,12 @@ rv_status host_format_somatic(rv_ctx *t, rv_ctx *n, const char *sample, const ch
             else o += "0\t0\t";
         }
         if (r.has_end) {
-            snprintf(b, sizeof b, "%d\t%f\t%d\t", r.end.r.shift3, r.end.r.msi, r.end.r.msint);
-            o += b;
+            put_int(o, r.end.r.shift3);
+            o += '\t';
+            put_f6(o, r.end.r.msi);
+            o += '\t';
+            put_int(o, r.end.r.msint);
+            o += '\t';
             o += (r.end.r.leftseq.empty() ? std::string("0") : r.end.r.leftseq) + "\t";
             o += (r.end.r.rightseq.empty() ? std::string("0") : r.end.r.rightseq) + "\t";
         } else {
@@ -456,12 +444,11 @@ rv_status host_format_somatic(rv_ctx *t, rv_ctx *n, const char *sample, const ch
         if (P.fisher) {
             put_fisher(o, p2[3 * i + 2], &tab[12 * i + 8]);
             double tvaf = r.has_t ? r.t.c.freq : 0, nvaf = r.has_n ? r.n.c.freq : 0;
-            snprintf(b, sizeof b, "%f\t", std::log(std::max(tvaf, 0.0001) / std::max(nvaf, 0.0001)));
-            o += b;
+            put_f6(o, std::log(std::max(tvaf, 0.0001) / std::max(nvaf, 0.0001)));
+            o += '\t';
             int t_var = r.has_t ? r.t.c.pc : 0, n_var = r.has_n ? r.n.c.pc : 0;
-            snprintf(b, sizeof b, "%f\t",
-                     std::log((static_cast<float>(t_var) + 0.5) / (static_cast<float>(n_var) + 0.5)));
-            o += b;
+            put_f6(o, std::log((static_cast<float>(t_var) + 0.5) / (static_cast<float>(n_var) + 0.5)));
+            o += '\t';
         }
         o += '\n';
     }
@@ -470,6 +457,9 @@ rv_status host_format_somatic(rv_ctx *t, rv_ctx *n, const char *sample, const ch
     for (auto &x : texts) t->text += x;
     t->n_records = (int64_t)recs.size();
     t->h_records.clear();
+    pt.lap("text");
+    if (pt.on) fprintf(stderr, "trace format_somatic sizes cand_t %zu cand_n %zu positions %zu records %zu\n",
+                       t->h_cand.size(), n->h_cand.size(), tg.size(), recs.size());
     return RV_OK;
 }
 

@@ -87,6 +87,7 @@ __device__ __forceinline__ int code_base(int code) {
 
 // Sinks without an inline fast path for single-base observations.
 struct NoFast {
+    __device__ __forceinline__ char ref(const char *refp, int p) const { return __ldg(refp + p - 1); }
     __device__ __forceinline__ bool emit(int, int, int, int, int, int, int) const { return false; }
 };
 
@@ -839,7 +840,7 @@ struct Walker {
                 const int q0 = (int)((pick_word(qw, (rp & 15) >> 2) >> ((rp & 3) * 8)) & 255u);
                 const int b = code_base(code);
                 const bool hs = st >= ws && st <= we;
-                const char rc = hs ? __ldg(refp + st - 1) : (char)0;
+                const char rc = hs ? fe.ref(refp, st) : (char)0;
                 const bool mm = hs && base_index(rc) != b;
                 const bool slow = b < 0 || i >= tail_from ||
                                   (mm && q0 >= goodq && st + 1 >= rs && st + 1 <= re && i + 1 < celr && rc != 'N');
