@@ -65,10 +65,11 @@ struct Region {
     int64_t cell_base;       // index of position clo in the cell arrays
     int64_t r0, r1;          // candidate read range in the batch
     int32_t span_lo, span_hi; // min/max position any read of the region may touch
-    int32_t serial;          // 1: processed by the in-order exact walker
+    int32_t serial;          // 1: reads can reach past the window (edge reads); with edge_hit set,
+                             // the region is processed by the in-order exact walker
     int32_t max_read_len;    // maxReadLength of the region
     int32_t err;             // error bits
-    int32_t pad;
+    int32_t edge_hit;        // an edge read would insert a position past the window
 };
 
 struct Tile {

@@ -449,6 +449,7 @@ __global__ void k_region_spans(DevState st, DevParams P) {
         R.span_hi = hi;
         // reads that can reach outside the reference window take the in-order path
         R.serial = (R.r1 > R.r0) && is_edge(R, hi) ? 1 : 0;
+        R.edge_hit = 0;
         if (R.r1 > R.r0 && (lo < R.clo || hi > R.chi)) set_err(st.err, ERR_CELL_RANGE);
     }
 }
@@ -498,7 +499,7 @@ __global__ void __launch_bounds__(kPileupThreads, MINB) k_pileup_tiles(DevState 
             Walker<TileSink> w(P, sink, R, st.ref, st.ref_len);
             for (int64_t r = tile.r0 + threadIdx.x; r < tile.r1; r += blockDim.x) {
                 if (!read_passes(st.batch, P, R, r)) continue;
-                if (R.serial) {
+                if (R.serial && R.edge_hit) {
                     int a, b;
                     read_span(st.batch, r, a, b, P.local_realign != 0);
                     if (is_edge(R, b)) continue;
@@ -539,8 +540,11 @@ __global__ void __launch_bounds__(kPileupThreads, MINB) k_pileup_tiles(DevState 
 // For regions with edge reads: walk the edge reads in parallel with the
 // detection sink; if none would touch a position past the window, the
 // parallel walk is exact and the region leaves the in-order path.
+// kEdgeBlocks blocks per region, each over a slice of the reads near the
+// window end.
+constexpr int kEdgeBlocks = 16;
 __global__ void k_edge_detect(DevState st, DevParams P) {
-    int reg = blockIdx.x;
+    int reg = blockIdx.x / kEdgeBlocks, part = blockIdx.x % kEdgeBlocks;
     if (reg >= st.n_regions) return;
     Region &R = st.regions[reg];
     if (!R.serial) return;
@@ -557,7 +561,7 @@ __global__ void k_edge_detect(DevState st, DevParams P) {
     sink.R = &R;
     sink.hit = &hit;
     Walker<DetectSink> w(P, sink, R, st.ref, st.ref_len);
-    for (int64_t r = lo + threadIdx.x; r < R.r1; r += blockDim.x) {
+    for (int64_t r = lo + part * (int64_t)blockDim.x + threadIdx.x; r < R.r1; r += (int64_t)kEdgeBlocks * blockDim.x) {
         if (!read_passes(st.batch, P, R, r)) continue;
         int a, b;
         read_span(st.batch, r, a, b, P.local_realign != 0);
@@ -565,7 +569,7 @@ __global__ void k_edge_detect(DevState st, DevParams P) {
         w.walk(st.batch, r);
     }
     __syncthreads();
-    if (threadIdx.x == 0 && hit == 0) R.serial = 0;
+    if (threadIdx.x == 0 && hit != 0) atomicOr(&R.edge_hit, 1);
 }
 
 // One block per region with edge reads; thread 0 walks them in file order.
@@ -573,7 +577,7 @@ __global__ void k_pileup_serial(DevState st, DevParams P) {
     int reg = blockIdx.x;
     if (reg >= st.n_regions) return;
     const Region &R = st.regions[reg];
-    if (!R.serial) return;
+    if (!R.serial || !R.edge_hit) return;
     __shared__ uint32_t ph_hi[SerialSink::kPh / 32], ph_lo[SerialSink::kPh / 32];
     for (int i = threadIdx.x; i < SerialSink::kPh / 32; i += blockDim.x) { ph_hi[i] = 0; ph_lo[i] = 0; }
     __syncthreads();
@@ -683,7 +687,7 @@ int pileup_blocks_per_sm(int variant) {
 }
 
 void launch_edge_detect(const DevState &st, const DevParams &P, cudaStream_t s) {
-    if (st.n_regions > 0) k_edge_detect<<<st.n_regions, 128, 0, s>>>(st, P);
+    if (st.n_regions > 0) k_edge_detect<<<st.n_regions * kEdgeBlocks, 128, 0, s>>>(st, P);
 }
 
 void launch_serial(const DevState &st, const DevParams &P, cudaStream_t s) {

@@ -95,7 +95,8 @@ def dataset(seeds, min_count: int = 2, **kw):
 
 def compare(scores: np.ndarray, y: np.ndarray, hard: np.ndarray) -> dict:
     """Precision, recall and F1 of the hard filter and of the learned filter
-    thresholded at the hard filter's recall."""
+    thresholded at the hard filter's recall; also the learned filter's
+    highest recall at the hard filter's precision and its best F1."""
     pos = y > 0.5
     tp_h = float(np.sum(pos & (hard > 0.5)))
     n_h = float(np.sum(hard > 0.5))
@@ -111,7 +112,32 @@ def compare(scores: np.ndarray, y: np.ndarray, hard: np.ndarray) -> dict:
     prec_l = tp_l / max(1.0, float(sel.sum()))
     rec_l = tp_l / max(1.0, float(pos.sum()))
     f1_l = 2 * prec_l * rec_l / max(1e-12, prec_l + rec_l)
+    # the learned filter's whole precision/recall curve: the highest recall
+    # it reaches at the hard filter's precision (or better), and its best F1
+    order_all = np.argsort(-scores, kind="stable")
+    tp_c = np.cumsum(pos[order_all])
+    n_c = np.arange(1, len(order_all) + 1)
+    prec_c = tp_c / n_c
+    rec_c = tp_c / max(1.0, float(pos.sum()))
+    f1_c = 2 * prec_c * rec_c / np.maximum(1e-12, prec_c + rec_c)
+    # only cut points between distinct scores are thresholds
+    cut = np.ones(len(order_all), bool)
+    if len(order_all) > 1:
+        s_sorted = scores[order_all]
+        cut[:-1] = s_sorted[:-1] != s_sorted[1:]
+    ok = cut & (prec_c >= prec_h - 1e-12)
+    if ok.any():
+        j = int(np.flatnonzero(ok)[np.argmax(rec_c[ok])])
+        eq_prec = {"precision": float(prec_c[j]), "recall": float(rec_c[j]), "f1": float(f1_c[j]),
+                   "called": int(n_c[j]), "threshold": float(scores[order_all][j])}
+    else:
+        eq_prec = {"precision": 0.0, "recall": 0.0, "f1": 0.0, "called": 0, "threshold": float("inf")}
+    jb = int(np.argmax(np.where(cut, f1_c, -1.0))) if len(order_all) else 0
+    best = {"precision": float(prec_c[jb]), "recall": float(rec_c[jb]), "f1": float(f1_c[jb]),
+            "called": int(n_c[jb]), "threshold": float(scores[order_all][jb])} if len(order_all) else {}
     return {"candidates": int(len(y)), "true": int(pos.sum()),
             "hard": {"precision": prec_h, "recall": rec_h, "f1": f1_h, "called": int(n_h)},
             "learned": {"precision": prec_l, "recall": rec_l, "f1": f1_l, "called": int(sel.sum()),
-                        "threshold": float(thr)}}
+                        "threshold": float(thr)},
+            "learned_at_hard_precision": eq_prec,
+            "learned_best_f1": best}

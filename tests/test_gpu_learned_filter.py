@@ -1,6 +1,7 @@
 """The learned filter against the hard filter on held-out synthetic deep
 panels (planted truth): at the hard filter's recall the learned filter's
-F1 must be at least the hard filter's."""
+F1 must be at least the hard filter's, and at the hard filter's precision
+its recall must be at least the hard filter's."""
 import pytest
 
 pytestmark = pytest.mark.gpu
@@ -18,3 +19,6 @@ def test_learned_filter_f1_at_equal_recall():
     m.close()
     assert res["learned"]["recall"] >= res["hard"]["recall"] - 1e-9
     assert res["learned"]["f1"] >= res["hard"]["f1"], res
+    eq = res["learned_at_hard_precision"]
+    assert eq["precision"] >= res["hard"]["precision"] - 1e-12
+    assert eq["recall"] >= res["hard"]["recall"], res
