@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <iterator>
 #include <cstdlib>
 #include <climits>
@@ -334,17 +335,32 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
         const int64_t nch = chunks_for(n, 1 << 16);
         std::vector<int> ms((size_t)nch, 1), ml((size_t)nch, 1);
         std::vector<uint8_t> bad((size_t)nch, 0);
+        ctx->h_span_lo.resize((size_t)n);
+        ctx->h_span_hi.resize((size_t)n);
+        const bool widen = ctx->params.local_realign != 0;
         parallel_chunks(n, 1 << 16, [&](int64_t k, int64_t a, int64_t e) {
             int msp = 1, mlq = 1;
             uint8_t bd = 0;
             for (int64_t i = a; i < e; i++) {
                 bd |= (uint8_t)((b->base_off[i] & 31) != 0);
                 const uint32_t *c = b->cigar + b->cig_off[i];
-                int sp = 0;
-                for (int q = 0; q < b->n_cigar[i]; q++) {
+                const int nc = b->n_cigar[i];
+                int sp = 0, ins = 0, clip5 = 0, clip3 = 0;
+                for (int q = 0; q < nc; q++) {
                     int o = c[q] & 15;
                     if (o == 0 || o == 2 || o == 3 || o == 7 || o == 8) sp += (int)(c[q] >> 4);
+                    if (o == 1) ins += (int)(c[q] >> 4);
                 }
+                // the read's span as the tile windows see it (the device's
+                // read_span): soft clips and edge insertions widen it
+                if (nc > 0) {
+                    if ((c[0] & 15) == 4 || (c[0] & 15) == 1) clip5 = (int)(c[0] >> 4);
+                    if ((c[nc - 1] & 15) == 4 || (c[nc - 1] & 15) == 1) clip3 = (int)(c[nc - 1] >> 4);
+                }
+                if (!widen) ins = 0;
+                const int pos1 = b->pos[i] + 1;
+                ctx->h_span_lo[i] = pos1 - clip5 - 1 - ins;
+                ctx->h_span_hi[i] = pos1 + sp + clip3 + ins;
                 msp = std::max(msp, sp);
                 mlq = std::max(mlq, (int)b->l_qseq[i]);
             }
@@ -402,6 +418,7 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
     ctx->regions.clear();
     ctx->tiles.clear();
     ctx->score_base.clear();
+    std::vector<int64_t> tile_begin;
     int64_t cell_base = 0, score = 0;
     for (int r = 0; r < n_regions; r++) {
         Region R;
@@ -424,6 +441,7 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
         R.r0 = std::lower_bound(b->pos, b->pos + n, lo_pos) - b->pos;
         R.r1 = std::lower_bound(b->pos, b->pos + n, R.end) - b->pos;
         ctx->regions.push_back(R);
+        tile_begin.push_back((int64_t)ctx->tiles.size());
         ctx->score_base.push_back(score);
         score += R.end - R.start + 1;
         // tiles of consecutive reads sized so a tile's window fits kTileW positions
@@ -435,13 +453,39 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
             for (int64_t a = R.r0; a < R.r1; a += tr) {
                 Tile t;
                 t.region = r;
-                t.pad = 0;
                 t.r0 = a;
                 t.r1 = std::min(R.r1, a + tr);
+                t.wlo = 0;  // set below from the read spans
                 ctx->tiles.push_back(t);
             }
         }
     }
+    tile_begin.push_back((int64_t)ctx->tiles.size());
+    // per region, from the read spans: the reads' reach, the edge-read flag
+    // and each tile's window start (the lowest span start of its non-edge
+    // reads); regions on host threads
+    std::atomic<int> span_bad{0};
+    parallel_for(n_regions, [&](int64_t r) {
+        Region &R = ctx->regions[r];
+        if (R.r1 <= R.r0) return;
+        int lo = INT32_MAX, hi = INT32_MIN;
+        for (int64_t i = R.r0; i < R.r1; i++) {
+            lo = std::min(lo, std::max(ctx->h_span_lo[i], 1));
+            hi = std::max(hi, ctx->h_span_hi[i]);
+        }
+        R.span_lo = lo;
+        R.span_hi = hi;
+        R.serial = hi + kEdgeMargin > R.we ? 1 : 0;
+        if (lo < R.clo || hi > R.chi) span_bad.store(1);
+        for (int64_t k = tile_begin[r]; k < tile_begin[r + 1]; k++) {
+            Tile &t = ctx->tiles[k];
+            int wlo = INT32_MAX;
+            for (int64_t i = t.r0; i < t.r1; i++)
+                if (ctx->h_span_hi[i] + kEdgeMargin <= R.we) wlo = std::min(wlo, ctx->h_span_lo[i]);
+            t.wlo = std::max(wlo, R.clo);
+        }
+    });
+    if (span_bad.load()) { ctx->err = "read span outside the region's cell range"; return RV_ERR_UNSUPPORTED; }
     ctx->n_score = score;
     ctx->n_cells = cell_base + 4;
     // -t: RecordPreprocessor::next_record's duplicate filter
@@ -607,7 +651,7 @@ rv_status pileup_launch(rv_ctx *ctx, cudaStream_t s) {
     launch_init_slots(ctx->d_slots, ctx->hash_cap, s);
     DevState st = ctx->state();
     RV_CUDA(cudaEventRecord(ctx->ev[4], s));
-    launch_region_spans(st, ctx->dp, s);
+    launch_region_reset(st, s);
     launch_edge_detect(st, ctx->dp, s);
     RV_CUDA(cudaEventRecord(ctx->ev[5], s));
     // autotuner: unless RV_PILEUP_VARIANT pins one, the first batches try each

@@ -14,7 +14,7 @@ namespace rv {
 
 // kernel launchers (rv_pileup.cu, rv_score.cu)
 void launch_init_slots(Slot *slots, unsigned long long n, cudaStream_t s);
-void launch_region_spans(const DevState &st, const DevParams &P, cudaStream_t s);
+void launch_region_reset(const DevState &st, cudaStream_t s);
 cudaError_t launch_pileup(const DevState &st, const DevParams &P, int grid, cudaStream_t s, int variant);
 int pileup_variants();
 void launch_serial(const DevState &st, const DevParams &P, cudaStream_t s);
@@ -127,6 +127,7 @@ struct rv_ctx {
     std::vector<int32_t> h_pos;
     std::vector<uint16_t> h_flag, h_ncig;
     std::vector<uint32_t> h_cigoff, h_cigar;
+    std::vector<int32_t> h_span_lo, h_span_hi;  // per read: the span the tile windows cover
 
     // regions / tiles
     std::vector<rv::Region> regions;

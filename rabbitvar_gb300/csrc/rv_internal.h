@@ -74,9 +74,13 @@ struct Region {
 
 struct Tile {
     int32_t region;
-    int32_t pad;
+    int32_t wlo;             // first position of the tile's shared-memory window (host-computed)
     int64_t r0, r1;          // reads [r0, r1) of the batch
 };
+
+// A read is an edge read of a region when its span reaches within this many
+// positions of the reference window's end.
+constexpr int kEdgeMargin = 8;
 
 // Device copy of rv_params plus derived values.
 struct DevParams {

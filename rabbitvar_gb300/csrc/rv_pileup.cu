@@ -330,7 +330,6 @@ struct SerialSink : SinkBase {
 // A read is an edge read when its walk may look up reference positions past
 // the loaded window (the reference's map then inserts 0 entries that later
 // lookups see); edge reads of a region are walked in file order by one thread.
-constexpr int kEdgeMargin = 8;
 __device__ __forceinline__ bool is_edge(const Region &R, int span_hi) { return span_hi + kEdgeMargin > R.we; }
 
 // Probe sink: reports whether the walked read creates key (pos, base) before
@@ -425,33 +424,11 @@ __device__ void read_span(const Batch &B, int64_t r, int &lo, int &hi, bool wide
 // ---------------------------------------------------------------------------
 // kernels
 // ---------------------------------------------------------------------------
-__global__ void k_region_spans(DevState st, DevParams P) {
-    int reg = blockIdx.x;
-    if (reg >= st.n_regions) return;
-    Region &R = st.regions[reg];
-    __shared__ int lo, hi;
-    if (threadIdx.x == 0) { lo = INT32_MAX; hi = INT32_MIN; }
-    __syncthreads();
-    int mylo = INT32_MAX, myhi = INT32_MIN;
-    for (int64_t r = R.r0 + threadIdx.x; r < R.r1; r += blockDim.x) {
-        int a, b;
-        read_span(st.batch, r, a, b, P.local_realign != 0);
-        // a 5' clip of a read at the contig start reaches below position 1,
-        // where there is no reference base and so no cell is touched
-        mylo = min(mylo, max(a, 1));
-        myhi = max(myhi, b);
-    }
-    atomicMin(&lo, mylo);
-    atomicMax(&hi, myhi);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        R.span_lo = lo;
-        R.span_hi = hi;
-        // reads that can reach outside the reference window take the in-order path
-        R.serial = (R.r1 > R.r0) && is_edge(R, hi) ? 1 : 0;
-        R.edge_hit = 0;
-        if (R.r1 > R.r0 && (lo < R.clo || hi > R.chi)) set_err(st.err, ERR_CELL_RANGE);
-    }
+// The region fields the host computed from the read spans (span_lo/hi,
+// serial) stay; only the per-launch edge flag is reset.
+__global__ void k_region_reset(DevState st) {
+    int reg = blockIdx.x * blockDim.x + threadIdx.x;
+    if (reg < st.n_regions) st.regions[reg].edge_hit = 0;
 }
 
 template <int TW, int MINB>
@@ -461,28 +438,21 @@ __global__ void __launch_bounds__(kPileupThreads, MINB) k_pileup_tiles(DevState 
     uint32_t *w1 = w0 + 4 * TW;
     uint32_t *w2 = w1 + 4 * TW;
     uint32_t *first = w2 + 4 * TW;
-    __shared__ int s_tile, s_wlo;
+    __shared__ int s_tile;
     __shared__ char s_ref[TW];
     for (;;) {
-        if (threadIdx.x == 0) {
-            s_tile = (int)atomicAdd(st.tile_counter, 1u);
-            s_wlo = INT32_MAX;
-        }
+        if (threadIdx.x == 0) s_tile = (int)atomicAdd(st.tile_counter, 1u);
         __syncthreads();
         int t = s_tile;
         if (t >= st.n_tiles) return;
         const Tile tile = st.tiles[t];
         const Region &R = st.regions[tile.region];
-        for (int64_t r = tile.r0 + threadIdx.x; r < tile.r1; r += blockDim.x) {
-            int a, b;
-            read_span(st.batch, r, a, b, P.local_realign != 0);
-            if (!is_edge(R, b)) atomicMin(&s_wlo, a);
-        }
+        // window start: the lowest span start of the tile's non-edge reads
+        // (computed on the host from the same CIGAR arithmetic as read_span)
+        const int wlo = tile.wlo;
         for (int i = threadIdx.x; i < 4 * 4 * TW; i += blockDim.x) w0[i] = 0u;
-        __syncthreads();
-        int wlo = max(s_wlo, R.clo);
         for (int i = threadIdx.x; i < TW; i += blockDim.x) {
-            int p = wlo + i;  // 1-based; the walk reads it only inside [ws, we]
+            const int64_t p = (int64_t)wlo + i;  // 1-based; the walk reads it only inside [ws, we]
             s_ref[i] = (p >= 1 && p <= st.ref_len) ? st.ref[p - 1] : (char)0;
         }
         __syncthreads();
@@ -649,8 +619,8 @@ void launch_init_slots(Slot *slots, unsigned long long n, cudaStream_t s) {
     k_init_slots<<<592, 256, 0, s>>>(slots, n);
 }
 
-void launch_region_spans(const DevState &st, const DevParams &P, cudaStream_t s) {
-    if (st.n_regions > 0) k_region_spans<<<st.n_regions, 256, 0, s>>>(st, P);
+void launch_region_reset(const DevState &st, cudaStream_t s) {
+    if (st.n_regions > 0) k_region_reset<<<(st.n_regions + 255) / 256, 256, 0, s>>>(st);
 }
 
 size_t pileup_smem_bytes() { return (size_t)kTileW * 4 * 4 * 4; }
