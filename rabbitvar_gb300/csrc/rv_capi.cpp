@@ -293,6 +293,7 @@ void rv_destroy(rv_ctx *ctx) {
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (ctx->h_mirror) cudaFreeHost(ctx->h_mirror);
+    if (ctx->h_mirror_slots) cudaFreeHost(ctx->h_mirror_slots);
     for (int i = 0; i < 12; i++)
         if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -680,6 +681,7 @@ rv_status pileup_launch(rv_ctx *ctx, cudaStream_t s) {
     RV_CUDA(cudaEventRecord(ctx->ev[1], s));
     ctx->kernels = 8;  // init_slots, region_spans, edge_detect, pileup_tiles, serial, resolve, link, collisions
     ctx->pileup_pin = pin && *pin;
+    ctx->mirror_pending = false;
     ctx->stage = 1;  // launched, not finished
     ctx->pileup_pending = true;
     return RV_OK;
@@ -928,6 +930,21 @@ rv_status rv_pileup_realign_pair(rv_ctx *tumor, rv_ctx *normal) {
     // both samples' kernels are queued first (one stream each); the tumor's
     // host realigner then runs while the normal's pileup is on the device
     if ((s = pileup_launch(tumor, tumor->stream))) return s;
+    if (tumor->params.local_realign) {
+        // the tumor's mirror kernels go before the normal's pileup, whose
+        // persistent blocks would otherwise hold every SM until they finish;
+        // the mirror's copies then overlap the normal's kernels
+        if ((s = mirror_launch(tumor, tumor->ev[11]))) {
+            pileup_finish(tumor, tumor->stream);
+            return s;
+        }
+        cudaError_t e = cudaStreamWaitEvent(normal->stream, tumor->ev[11], 0);
+        if (e != cudaSuccess) {
+            tumor->err = std::string("cudaStreamWaitEvent: ") + cudaGetErrorString(e);
+            pileup_finish(tumor, tumor->stream);
+            return RV_ERR_CUDA;
+        }
+    }
     if ((s = pileup_launch(normal, normal->stream))) {
         tumor->err = normal->err;
         pileup_finish(tumor, tumor->stream);

@@ -176,8 +176,11 @@ struct rv_ctx {
     size_t cap_list_off = 0, cap_list_bsum = 0, cap_list_idx = 0;
     rv::Slot *d_list_slots = nullptr;
     size_t cap_list_slots = 0;
-    void *h_mirror = nullptr;  // pinned: cells, offsets, slots, slot indices
+    void *h_mirror = nullptr;  // pinned: cells, list offsets
     size_t cap_mirror = 0;
+    void *h_mirror_slots = nullptr;  // pinned: listed keys, slot indices
+    size_t cap_mirror_slots = 0;
+    bool mirror_pending = false;     // mirror_launch queued, not yet consumed
     rv::Patch *d_patches = nullptr;
     size_t cap_patches = 0;
     uint8_t *d_patch_keys = nullptr;
@@ -219,4 +222,6 @@ namespace rv {
 // two-sided Fisher p-values of n (a, b, c, d) tables on the context's device
 rv_status device_fisher(rv_ctx *ctx, const int32_t *tables, int64_t n, double *p2);
 rv_status host_format_somatic(rv_ctx *tumor, rv_ctx *normal, const char *sample, const char *gene);
+// -k 1 realigner: queue the mirror's device work (record `after_kernels` once its kernels are queued)
+rv_status mirror_launch(rv_ctx *ctx, cudaEvent_t after_kernels);
 }  // namespace rv

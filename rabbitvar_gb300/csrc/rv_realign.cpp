@@ -313,8 +313,10 @@ struct RegionRealigner {
         auto it = sc.find(p);
         return it == sc.end() ? nullptr : &it->second;
     }
+    double *prof = nullptr;  // per-region phase times (trace)
     const string &consensus(Clip &k) {
         if (!k.loaded) {
+            auto t0 = std::chrono::steady_clock::now();
             k.loaded = true;
             std::vector<NtCount> nt;
             if (k.cell >= 0)
@@ -326,21 +328,42 @@ struct RegionRealigner {
                 }
             sort_nt(nt);
             k.c.cons = consensus_of(nt, k.c.agg.cnt, k.c.used);
+            if (prof) prof[6] += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
         }
         return k.c.cons;
     }
     void add_cov(int p, int n) { cov_add[p] += n; }
 
-    void load_clips() {
+    // one pass over the region's key lists: the soft-clip aggregates, and
+    // the MNV / deletion / insertion counts the passes iterate
+    // (VariationData's mnp, positionToDeletionCount, positionToInsertionCount)
+    void load_lists(std::map<int, std::map<string, int>> &mnp, std::map<int, std::map<string, int>> &delcnt,
+                    std::map<int, std::map<string, int>> &inscnt) {
+        const uint8_t *arena = ctx->h_arena.data();
+        const size_t arena_n = ctx->h_arena.size();
         for (int p = Rg.clo; p <= Rg.chi; p++) {
             const int64_t c = cell_of(p);
-            for (uint32_t i = mir.off[c]; i < mir.off[c + 1]; i++) {
+            const uint32_t e = mir.off[c + 1];
+            for (uint32_t i = mir.off[c]; i < e; i++) {
                 const Slot &s = mir.slots[i];
-                if (s.kind != KIND_SC5 && s.kind != KIND_SC3) continue;
-                Clip &k = (s.kind == KIND_SC3 ? sc3 : sc5)[p];
-                k.c.agg = from_slot(s, mir.sidx[i]);
-                k.cell = c;
-                k.seq_kind = s.kind == KIND_SC3 ? KIND_SC3_SEQ : KIND_SC5_SEQ;
+                if (s.kind == KIND_SC5 || s.kind == KIND_SC3) {
+                    Clip &k = (s.kind == KIND_SC3 ? sc3 : sc5)[p];
+                    k.c.agg = from_slot(s, mir.sidx[i]);
+                    k.cell = c;
+                    k.seq_kind = s.kind == KIND_SC3 ? KIND_SC3_SEQ : KIND_SC5_SEQ;
+                    continue;
+                }
+                if ((s.kind != KIND_NONINS && s.kind != KIND_INS) || s.obs <= 0) continue;
+                if (s.kind == KIND_NONINS) {
+                    // only MNV ("X&Y...") and deletion keys are counted
+                    if (s.klen == 0 || (size_t)s.koff + s.klen > arena_n) continue;
+                    const uint8_t k0 = arena[s.koff];
+                    if (k0 != '-' && !(s.klen > 2 && arena[s.koff + 1] == '&')) continue;
+                }
+                string k = mir.key(i);
+                if (s.kind == KIND_INS) inscnt[p][k] = s.obs;
+                else if (is_mnv(k)) mnp[p][k] = s.obs;
+                else if (!k.empty() && k[0] == '-') delcnt[p][k] = s.obs;
             }
         }
     }
@@ -935,6 +958,14 @@ struct RegionRealigner {
         auto by_cnt = [](const T &a, const T &b) { return a.cnt != b.cnt ? a.cnt > b.cnt : a.pos < b.pos; };
         std::sort(t5.begin(), t5.end(), by_cnt);
         std::sort(t3.begin(), t3.end(), by_cnt);
+        // the 3' clips by position (with their rank in t3): a 5' clip only
+        // pairs with 3' clips in [p5 - 2.5 max_rl, p5 + max_rl - 10], and the
+        // reference's loop over t3 does nothing else for the others, so the
+        // pass visits just those, in t3 order
+        std::vector<std::pair<int, int>> by_pos(t3.size());
+        for (size_t i = 0; i < t3.size(); i++) by_pos[i] = {t3[i].pos, (int)i};
+        std::sort(by_pos.begin(), by_pos.end());
+        std::vector<int> near;
         for (T &a : t5) {
             const int p5 = a.pos;
             Clip &sc5v = *a.c;
@@ -942,7 +973,14 @@ struct RegionRealigner {
             if (sc5v.c.used) continue;
             const string &seq5 = consensus(sc5v);
             if (seq5.size() <= 10) continue;
-            for (T &b : t3) {
+            const int lo3 = (int)std::ceil(p5 - max_rl * 2.5) - 1, hi3 = p5 + max_rl - 10 + 1;
+            near.clear();
+            for (auto it = std::lower_bound(by_pos.begin(), by_pos.end(), std::make_pair(lo3, INT32_MIN));
+                 it != by_pos.end() && it->first <= hi3; ++it)
+                near.push_back(it->second);
+            std::sort(near.begin(), near.end());
+            for (int ni : near) {
+                T &b = t3[ni];
                 try {
                     const int p3 = b.pos;
                     Clip &sc3v = *b.c;
@@ -955,7 +993,9 @@ struct RegionRealigner {
                     if (seq3.size() <= 10) continue;
                     if (!(cnt5 / (double)cnt3 >= 0.08 && cnt5 / (double)cnt3 <= 12)) continue;
                     int bp5, bp3, score;
+                    auto tf = std::chrono::steady_clock::now();
                     find35(seq5, seq3, bp5, bp3, score);
+                    if (prof) prof[7] += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tf).count();
                     if (score == 0) continue;
                     const int sm = score / 2;
                     string ins = bp3 + sm > 1 ? vsub(seq3, 0, -(bp3 + sm) + 1) : seq3;
@@ -1158,6 +1198,7 @@ struct RegionRealigner {
     }
 
     void run(std::vector<Patch> &out, string &keys, double *phase) {
+        prof = phase;
         auto clk = [] { return std::chrono::steady_clock::now(); };
         auto t = clk();
         auto lap = [&](int k) {
@@ -1165,19 +1206,8 @@ struct RegionRealigner {
             phase[k] += std::chrono::duration<double, std::milli>(n - t).count();
             t = n;
         };
-        load_clips();
         std::map<int, std::map<string, int>> mnp, delcnt, inscnt;
-        for (int p = Rg.clo; p <= Rg.chi; p++) {
-            const int64_t c = cell_of(p);
-            for (uint32_t i = mir.off[c]; i < mir.off[c + 1]; i++) {
-                const Slot &s = mir.slots[i];
-                if ((s.kind != KIND_NONINS && s.kind != KIND_INS) || s.obs <= 0) continue;
-                string k = mir.key(i);
-                if (s.kind == KIND_INS) inscnt[p][k] = s.obs;
-                else if (is_mnv(k)) mnp[p][k] = s.obs;
-                else if (!k.empty() && k[0] == '-') delcnt[p][k] = s.obs;
-            }
-        }
+        load_lists(mnp, delcnt, inscnt);
         lap(0);
         adjust_mnp(mnp);
         lap(1);
@@ -1194,6 +1224,63 @@ struct RegionRealigner {
 
 }  // namespace
 
+namespace {
+struct MirrorLayout {
+    size_t b_arr, b_cov, b_kf, b_off, cells;
+    explicit MirrorLayout(int64_t nc) {
+        auto up16 = [](size_t x) { return (x + 15) & ~(size_t)15; };
+        b_arr = (size_t)nc * 16;
+        b_cov = up16((size_t)nc * 4);
+        b_kf = up16((size_t)nc);
+        b_off = up16(((size_t)nc + 1) * 4);
+        cells = 8 * b_arr + b_cov + b_kf + b_off;
+    }
+};
+}  // namespace
+
+// Queues the device side of the realigner's mirror on the context's stream
+// without waiting: the flattened key lists (then `after_kernels` is recorded,
+// if given), and the copies of the cells and the list offsets into pinned
+// host memory.
+rv_status mirror_launch(rv_ctx *ctx, cudaEvent_t after_kernels) {
+    rv_status st;
+    cudaStream_t s = ctx->stream;
+    const int64_t nc = ctx->n_cells;
+    const int64_t nb = (nc + 1023) / 1024;
+    // list capacity: every listed key is a used slot
+    if ((st = ensure(ctx, ctx->d_list_off, ctx->cap_list_off, (size_t)nc + 1)) ||
+        (st = ensure(ctx, ctx->d_list_bsum, ctx->cap_list_bsum, (size_t)nb + 1)) ||
+        (st = ensure(ctx, ctx->d_list_slots, ctx->cap_list_slots, (size_t)ctx->hash_cap)) ||
+        (st = ensure(ctx, ctx->d_list_idx, ctx->cap_list_idx, (size_t)ctx->hash_cap)))
+        return st;
+    DevState ds = ctx->state();
+    launch_list_offsets(ds, ctx->d_list_off, ctx->d_list_bsum, s);
+    launch_list_fill(ds, ctx->d_list_off, ctx->d_list_slots, ctx->d_list_idx, s);
+    ctx->kernels += 5;
+    if (after_kernels) HCUDA(cudaEventRecord(after_kernels, s));
+    // pinned host copies: 8 cell arrays (16 B per cell each), cov, kflags, offsets
+    const MirrorLayout L(nc);
+    if (!ctx->h_mirror || ctx->cap_mirror < L.cells) {
+        if (ctx->h_mirror) cudaFreeHost(ctx->h_mirror);
+        ctx->h_mirror = nullptr;
+        size_t cap = L.cells + L.cells / 4;
+        HCUDA(cudaHostAlloc(&ctx->h_mirror, cap, cudaHostAllocDefault));
+        ctx->cap_mirror = cap;
+    }
+    char *h = (char *)ctx->h_mirror;
+    const Cells &C = ctx->cells;
+    const void *dev_arr[8] = {C.fwd, C.rev, C.hi, C.tp, C.q, C.mq, C.nm, C.first};
+    for (int k = 0; k < 8; k++, h += L.b_arr)
+        if (nc) HCUDA(cudaMemcpyAsync(h, dev_arr[k], L.b_arr, cudaMemcpyDeviceToHost, s));
+    if (nc) {
+        HCUDA(cudaMemcpyAsync(h, C.cov, (size_t)nc * 4, cudaMemcpyDeviceToHost, s));
+        HCUDA(cudaMemcpyAsync(h + L.b_cov, C.kflags, (size_t)nc, cudaMemcpyDeviceToHost, s));
+        HCUDA(cudaMemcpyAsync(h + L.b_cov + L.b_kf, ctx->d_list_off, ((size_t)nc + 1) * 4, cudaMemcpyDeviceToHost, s));
+    }
+    ctx->mirror_pending = true;
+    return RV_OK;
+}
+
 // VariationRealigner::process with -k 1 (src/VariationRealigner.cpp:135-161)
 rv_status host_realign_full(rv_ctx *ctx) {
     const bool trace = getenv("RV_REALIGN_TRACE") != nullptr;
@@ -1207,53 +1294,28 @@ rv_status host_realign_full(rv_ctx *ctx) {
     rv_status st;
     cudaStream_t s = ctx->stream;
     const int64_t nc = ctx->n_cells;
-    const int64_t nb = (nc + 1023) / 1024;
-    if ((st = ensure(ctx, ctx->d_list_off, ctx->cap_list_off, (size_t)nc + 1)) ||
-        (st = ensure(ctx, ctx->d_list_bsum, ctx->cap_list_bsum, (size_t)nb + 1)))
-        return st;
-    DevState ds = ctx->state();
-    launch_list_offsets(ds, ctx->d_list_off, ctx->d_list_bsum, s);
-    ctx->kernels += 4;
-    uint32_t total = 0;
-    HCUDA(cudaMemcpyAsync(&total, ctx->d_list_off + nc, 4, cudaMemcpyDeviceToHost, s));
+    if (!ctx->mirror_pending && (st = mirror_launch(ctx, nullptr))) return st;
+    ctx->mirror_pending = false;
     HCUDA(cudaStreamSynchronize(s));
-    if ((st = ensure(ctx, ctx->d_list_slots, ctx->cap_list_slots, (size_t)total + 1)) ||
-        (st = ensure(ctx, ctx->d_list_idx, ctx->cap_list_idx, (size_t)total + 1)))
-        return st;
-    launch_list_fill(ds, ctx->d_list_off, ctx->d_list_slots, ctx->d_list_idx, s);
-    ctx->kernels++;
-    // pinned host mirror: 8 cell arrays (16 B per cell each), cov, kflags,
-    // offsets, slots, slot indices
-    auto up16 = [](size_t x) { return (x + 15) & ~(size_t)15; };
-    const size_t b_arr = (size_t)nc * 16, b_cov = up16((size_t)nc * 4), b_kf = up16((size_t)nc),
-                 b_off = up16(((size_t)nc + 1) * 4), b_sl = (size_t)total * sizeof(Slot), b_ix = up16((size_t)total * 4);
-    const size_t need = 8 * b_arr + b_cov + b_kf + b_off + b_sl + b_ix;
-    if (!ctx->h_mirror || ctx->cap_mirror < need) {
-        if (ctx->h_mirror) cudaFreeHost(ctx->h_mirror);
-        ctx->h_mirror = nullptr;
-        size_t cap = need + need / 4;
-        HCUDA(cudaHostAlloc(&ctx->h_mirror, cap, cudaHostAllocDefault));
-        ctx->cap_mirror = cap;
-    }
+    const MirrorLayout L(nc);
     char *h = (char *)ctx->h_mirror;
-    const Cells &C = ctx->cells;
-    const void *dev_arr[8] = {C.fwd, C.rev, C.hi, C.tp, C.q, C.mq, C.nm, C.first};
     char *host_arr[8];
-    for (int k = 0; k < 8; k++) {
-        host_arr[k] = h;
-        if (nc) HCUDA(cudaMemcpyAsync(h, dev_arr[k], b_arr, cudaMemcpyDeviceToHost, s));
-        h += b_arr;
+    for (int k = 0; k < 8; k++) host_arr[k] = h + k * L.b_arr;
+    char *h_cov = h + 8 * L.b_arr;
+    char *h_kf = h_cov + L.b_cov;
+    char *h_off = h_kf + L.b_kf;
+    const uint32_t total = ((const uint32_t *)h_off)[nc];
+    // the listed keys and their slot indices
+    const size_t b_sl = (size_t)total * sizeof(Slot), b_ix = ((size_t)total * 4 + 15) & ~(size_t)15;
+    if (!ctx->h_mirror_slots || ctx->cap_mirror_slots < b_sl + b_ix) {
+        if (ctx->h_mirror_slots) cudaFreeHost(ctx->h_mirror_slots);
+        ctx->h_mirror_slots = nullptr;
+        size_t cap = (b_sl + b_ix) + (b_sl + b_ix) / 4 + 4096;
+        HCUDA(cudaHostAlloc(&ctx->h_mirror_slots, cap, cudaHostAllocDefault));
+        ctx->cap_mirror_slots = cap;
     }
-    char *h_cov = h; h += b_cov;
-    char *h_kf = h; h += b_kf;
-    char *h_off = h; h += b_off;
-    char *h_sl = h; h += b_sl;
-    char *h_ix = h;
-    if (nc) {
-        HCUDA(cudaMemcpyAsync(h_cov, C.cov, (size_t)nc * 4, cudaMemcpyDeviceToHost, s));
-        HCUDA(cudaMemcpyAsync(h_kf, C.kflags, (size_t)nc, cudaMemcpyDeviceToHost, s));
-        HCUDA(cudaMemcpyAsync(h_off, ctx->d_list_off, ((size_t)nc + 1) * 4, cudaMemcpyDeviceToHost, s));
-    }
+    char *h_sl = (char *)ctx->h_mirror_slots;
+    char *h_ix = h_sl + b_sl;
     if (total) {
         HCUDA(cudaMemcpyAsync(h_sl, ctx->d_list_slots, b_sl, cudaMemcpyDeviceToHost, s));
         HCUDA(cudaMemcpyAsync(h_ix, ctx->d_list_idx, (size_t)total * 4, cudaMemcpyDeviceToHost, s));
@@ -1264,7 +1326,7 @@ rv_status host_realign_full(rv_ctx *ctx) {
                               cudaMemcpyDeviceToHost, s));
     HCUDA(cudaStreamSynchronize(s));
     if ((st = pull_arena(ctx))) return st;
-    ctx->io_d2h += (int64_t)(need - b_ix + (size_t)total * 4 + ctx->h_arena.size());
+    ctx->io_d2h += (int64_t)(L.cells + (size_t)total * (sizeof(Slot) + 4) + ctx->h_arena.size());
     mir.fwd = (const uint32_t *)host_arr[0];
     mir.rev = (const uint32_t *)host_arr[1];
     mir.hi = (const uint32_t *)host_arr[2];
@@ -1314,12 +1376,13 @@ rv_status host_realign_full(rv_ctx *ctx) {
     double t_run = ms(t0);
     st = apply_patches(ctx, all, all_keys);
     if (trace) {
-        double sum[6] = {0};
+        double sum[8] = {0};
         for (int r = 0; r < nreg; r++)
-            for (int k = 0; k < 6; k++) sum[k] += phase[8 * r + k];
+            for (int k = 0; k < 8; k++) sum[k] += phase[8 * r + k];
         fprintf(stderr, "realign -k 1: listed keys %u, patches %zu, threads %d; ms: fetch %.2f run %.2f total %.2f; "
-                "thread-ms: setup %.2f mnp %.2f del %.2f ins %.2f lgins %.2f diff %.2f\n", total,
-                all.size(), nt, t_fetch, t_run, ms(t0), sum[0], sum[1], sum[2], sum[3], sum[4], sum[5]);
+                "thread-ms: setup %.2f mnp %.2f del %.2f ins %.2f lgins %.2f diff %.2f (consensus %.2f find35 %.2f)\n",
+                total, all.size(), nt, t_fetch, t_run, ms(t0), sum[0], sum[1], sum[2], sum[3], sum[4], sum[5], sum[6],
+                sum[7]);
     }
     return st;
 }
