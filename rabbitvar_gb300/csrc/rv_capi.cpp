@@ -117,11 +117,23 @@ rv_status device_fisher(rv_ctx *ctx, const int32_t *tables, int64_t n, double *p
         ctx->cap_ftab = cap;
     }
     double *dp = (double *)(ctx->d_ftab + 4 * n);
-    RV_CUDA(cudaMemcpyAsync(ctx->d_ftab, tables, (size_t)n * 16, cudaMemcpyHostToDevice, ctx->stream));
+    // through a pinned staging buffer: pageable copies would each wait for the stream
+    const size_t stage = (size_t)n * 24;
+    if (!ctx->h_fstage || ctx->cap_fstage < stage) {
+        if (ctx->h_fstage) cudaFreeHost(ctx->h_fstage);
+        ctx->h_fstage = nullptr;
+        size_t cap = std::max<size_t>(stage + stage / 4, 1 << 16);
+        RV_CUDA(cudaHostAlloc(&ctx->h_fstage, cap, cudaHostAllocDefault));
+        ctx->cap_fstage = cap;
+    }
+    char *hs = (char *)ctx->h_fstage;
+    memcpy(hs, tables, (size_t)n * 16);
+    RV_CUDA(cudaMemcpyAsync(ctx->d_ftab, hs, (size_t)n * 16, cudaMemcpyHostToDevice, ctx->stream));
     launch_fisher(ctx->d_ftab, n, dp, dp + n, ctx->stream, ctx->d_logfact);
     RV_CUDA(cudaGetLastError());
-    RV_CUDA(cudaMemcpyAsync(p2, dp, (size_t)n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    RV_CUDA(cudaMemcpyAsync(hs + (size_t)n * 16, dp, (size_t)n * 8, cudaMemcpyDeviceToHost, ctx->stream));
     RV_CUDA(cudaStreamSynchronize(ctx->stream));
+    memcpy(p2, hs + (size_t)n * 16, (size_t)n * 8);
     ctx->io_h2d += n * 16;
     ctx->io_d2h += n * 8;
     ctx->kernels += 1;
@@ -289,11 +301,13 @@ void rv_destroy(rv_ctx *ctx) {
                     ctx->d_arena, ctx->d_deferred, ctx->d_cand, ctx->d_counters, ctx->d_tmp_idx,
                     ctx->d_tmp_slots, ctx->d_tmp_cells, ctx->d_tmp_views, ctx->d_tmp_n, ctx->d_list,
                     ctx->d_ftab, ctx->d_logfact, ctx->d_skip, ctx->d_patches, ctx->d_patch_keys,
-                    ctx->d_list_off, ctx->d_list_bsum, ctx->d_list_idx, ctx->d_list_slots};
+                    ctx->d_list_off, ctx->d_list_bsum, ctx->d_list_idx, ctx->d_list_slots,
+                    ctx->d_cons_meta, ctx->d_cons};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (ctx->h_mirror) cudaFreeHost(ctx->h_mirror);
     if (ctx->h_mirror_slots) cudaFreeHost(ctx->h_mirror_slots);
+    if (ctx->h_fstage) cudaFreeHost(ctx->h_fstage);
     for (int i = 0; i < 12; i++)
         if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -948,6 +962,14 @@ rv_status rv_pileup_realign_pair(rv_ctx *tumor, rv_ctx *normal) {
     if ((s = pileup_launch(normal, normal->stream))) {
         tumor->err = normal->err;
         pileup_finish(tumor, tumor->stream);
+        return s;
+    }
+    // the normal's mirror queues behind its pileup and runs while the host
+    // realigns the tumor
+    if (normal->params.local_realign && (s = mirror_launch(normal, nullptr))) {
+        tumor->err = normal->err;
+        pileup_finish(tumor, tumor->stream);
+        pileup_finish(normal, normal->stream);
         return s;
     }
     rv_status st = pileup_finish(tumor, tumor->stream);

@@ -72,6 +72,8 @@ void launch_apply_patches(const DevState &st, const Patch *p, int64_t n, const u
 // flattened per-cell key lists (-k 1 realigner mirror): 5 launches, then 1
 void launch_list_offsets(const DevState &st, uint32_t *off, uint32_t *bsum, cudaStream_t s);
 void launch_list_fill(const DevState &st, const uint32_t *off, Slot *out, uint32_t *out_idx, cudaStream_t s);
+void launch_clip_consensus(const DevState &st, const uint32_t *off, const Slot *list, uint32_t *meta, uint8_t *cons,
+                           cudaStream_t s);
 
 // Host phase timer: with RV_TRACE set in the environment, each lap prints
 // "<scope> <phase> <ms>" to stderr (diagnostics only; no effect on results).
@@ -176,6 +178,10 @@ struct rv_ctx {
     size_t cap_list_off = 0, cap_list_bsum = 0, cap_list_idx = 0;
     rv::Slot *d_list_slots = nullptr;
     size_t cap_list_slots = 0;
+    uint32_t *d_cons_meta = nullptr;  // soft-clip consensus per listed aggregate
+    size_t cap_cons_meta = 0;
+    uint8_t *d_cons = nullptr;
+    size_t cap_cons = 0;
     void *h_mirror = nullptr;  // pinned: cells, list offsets
     size_t cap_mirror = 0;
     void *h_mirror_slots = nullptr;  // pinned: listed keys, slot indices
@@ -191,6 +197,8 @@ struct rv_ctx {
     size_t cap_list = 0;
     int32_t *d_ftab = nullptr;
     size_t cap_ftab = 0;  // tables
+    void *h_fstage = nullptr;  // pinned staging of the Fisher tables and p-values
+    size_t cap_fstage = 0;
 
     // host mirrors
     std::vector<rv::CandVar> h_cand;

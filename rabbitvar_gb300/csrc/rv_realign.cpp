@@ -173,6 +173,8 @@ struct Mirror {
     const uint32_t *off = nullptr;   // n_cells + 1
     const Slot *slots = nullptr;     // off[n_cells]
     const uint32_t *sidx = nullptr;  // hash slot index of each
+    const uint32_t *cmeta = nullptr; // per clip aggregate: its device-computed consensus (k_clip_consensus)
+    const uint8_t *cons = nullptr;
     std::vector<Region> regions;     // device copies (max_read_len)
 
     string key(uint32_t i) const { return slot_key(ctx, slots[i]); }
@@ -219,6 +221,7 @@ struct RegionRealigner {
     struct Clip {
         HClip c;
         int64_t cell = -1;  // the clip's per-offset counts are in this cell's list
+        int64_t agg = -1;   // list index of the aggregate
         int seq_kind = 0;
         bool loaded = false;
     };
@@ -315,6 +318,14 @@ struct RegionRealigner {
     }
     double *prof = nullptr;  // per-region phase times (trace)
     const string &consensus(Clip &k) {
+        if (!k.loaded && k.agg >= 0 && (mir.cmeta[k.agg] >> 31)) {
+            // computed on the device; the low-complexity mark applies now, at
+            // the first use, as in the reference
+            k.loaded = true;
+            const uint32_t m = mir.cmeta[k.agg];
+            k.c.cons.assign((const char *)mir.cons + mir.off[k.cell] + ((m >> 16) & 0x3FFFu), m & 0xFFFFu);
+            if (m & (1u << 30)) k.c.used = true;
+        }
         if (!k.loaded) {
             auto t0 = std::chrono::steady_clock::now();
             k.loaded = true;
@@ -350,6 +361,7 @@ struct RegionRealigner {
                     Clip &k = (s.kind == KIND_SC3 ? sc3 : sc5)[p];
                     k.c.agg = from_slot(s, mir.sidx[i]);
                     k.cell = c;
+                    k.agg = i;
                     k.seq_kind = s.kind == KIND_SC3 ? KIND_SC3_SEQ : KIND_SC5_SEQ;
                     continue;
                 }
@@ -1251,12 +1263,15 @@ rv_status mirror_launch(rv_ctx *ctx, cudaEvent_t after_kernels) {
     if ((st = ensure(ctx, ctx->d_list_off, ctx->cap_list_off, (size_t)nc + 1)) ||
         (st = ensure(ctx, ctx->d_list_bsum, ctx->cap_list_bsum, (size_t)nb + 1)) ||
         (st = ensure(ctx, ctx->d_list_slots, ctx->cap_list_slots, (size_t)ctx->hash_cap)) ||
-        (st = ensure(ctx, ctx->d_list_idx, ctx->cap_list_idx, (size_t)ctx->hash_cap)))
+        (st = ensure(ctx, ctx->d_list_idx, ctx->cap_list_idx, (size_t)ctx->hash_cap)) ||
+        (st = ensure(ctx, ctx->d_cons_meta, ctx->cap_cons_meta, (size_t)ctx->hash_cap)) ||
+        (st = ensure(ctx, ctx->d_cons, ctx->cap_cons, (size_t)ctx->hash_cap)))
         return st;
     DevState ds = ctx->state();
     launch_list_offsets(ds, ctx->d_list_off, ctx->d_list_bsum, s);
     launch_list_fill(ds, ctx->d_list_off, ctx->d_list_slots, ctx->d_list_idx, s);
-    ctx->kernels += 5;
+    launch_clip_consensus(ds, ctx->d_list_off, ctx->d_list_slots, ctx->d_cons_meta, ctx->d_cons, s);
+    ctx->kernels += 6;
     if (after_kernels) HCUDA(cudaEventRecord(after_kernels, s));
     // pinned host copies: 8 cell arrays (16 B per cell each), cov, kflags, offsets
     const MirrorLayout L(nc);
@@ -1305,20 +1320,26 @@ rv_status host_realign_full(rv_ctx *ctx) {
     char *h_kf = h_cov + L.b_cov;
     char *h_off = h_kf + L.b_kf;
     const uint32_t total = ((const uint32_t *)h_off)[nc];
-    // the listed keys and their slot indices
+    // the listed keys, their slot indices, the clip consensus records and characters
     const size_t b_sl = (size_t)total * sizeof(Slot), b_ix = ((size_t)total * 4 + 15) & ~(size_t)15;
-    if (!ctx->h_mirror_slots || ctx->cap_mirror_slots < b_sl + b_ix) {
+    const size_t b_cm = b_ix, b_cc = ((size_t)total + 15) & ~(size_t)15;
+    const size_t need_sl = b_sl + b_ix + b_cm + b_cc;
+    if (!ctx->h_mirror_slots || ctx->cap_mirror_slots < need_sl) {
         if (ctx->h_mirror_slots) cudaFreeHost(ctx->h_mirror_slots);
         ctx->h_mirror_slots = nullptr;
-        size_t cap = (b_sl + b_ix) + (b_sl + b_ix) / 4 + 4096;
+        size_t cap = need_sl + need_sl / 4 + 4096;
         HCUDA(cudaHostAlloc(&ctx->h_mirror_slots, cap, cudaHostAllocDefault));
         ctx->cap_mirror_slots = cap;
     }
     char *h_sl = (char *)ctx->h_mirror_slots;
     char *h_ix = h_sl + b_sl;
+    char *h_cm = h_ix + b_ix;
+    char *h_cc = h_cm + b_cm;
     if (total) {
         HCUDA(cudaMemcpyAsync(h_sl, ctx->d_list_slots, b_sl, cudaMemcpyDeviceToHost, s));
         HCUDA(cudaMemcpyAsync(h_ix, ctx->d_list_idx, (size_t)total * 4, cudaMemcpyDeviceToHost, s));
+        HCUDA(cudaMemcpyAsync(h_cm, ctx->d_cons_meta, (size_t)total * 4, cudaMemcpyDeviceToHost, s));
+        HCUDA(cudaMemcpyAsync(h_cc, ctx->d_cons, (size_t)total, cudaMemcpyDeviceToHost, s));
     }
     mir.regions.resize(ctx->regions.size());
     if (!mir.regions.empty())
@@ -1326,7 +1347,7 @@ rv_status host_realign_full(rv_ctx *ctx) {
                               cudaMemcpyDeviceToHost, s));
     HCUDA(cudaStreamSynchronize(s));
     if ((st = pull_arena(ctx))) return st;
-    ctx->io_d2h += (int64_t)(L.cells + (size_t)total * (sizeof(Slot) + 4) + ctx->h_arena.size());
+    ctx->io_d2h += (int64_t)(L.cells + (size_t)total * (sizeof(Slot) + 9) + ctx->h_arena.size());
     mir.fwd = (const uint32_t *)host_arr[0];
     mir.rev = (const uint32_t *)host_arr[1];
     mir.hi = (const uint32_t *)host_arr[2];
@@ -1340,6 +1361,8 @@ rv_status host_realign_full(rv_ctx *ctx) {
     mir.off = (const uint32_t *)h_off;
     mir.slots = (const Slot *)h_sl;
     mir.sidx = (const uint32_t *)h_ix;
+    mir.cmeta = (const uint32_t *)h_cm;
+    mir.cons = (const uint8_t *)h_cc;
     double t_fetch = ms(t0);
     // regions in parallel; patches concatenated in region order
     const int nreg = (int)ctx->regions.size();

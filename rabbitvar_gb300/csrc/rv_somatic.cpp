@@ -336,8 +336,10 @@ rv_status host_format_somatic(rv_ctx *t, rv_ctx *n, const char *sample, const ch
     const rv_params &P = t->params;
     std::vector<const CandVar *> to, no;
     std::vector<std::pair<size_t, size_t>> tg, ng;
-    group(t, to, tg);
-    group(n, no, ng);
+    parallel_for(2, [&](int64_t k) {
+        if (k == 0) group(t, to, tg);
+        else group(n, no, ng);
+    });
     pt.lap("group");
     // positions are independent: classify them on host threads, keeping order
     const int64_t kMinPos = 64;
@@ -366,6 +368,9 @@ rv_status host_format_somatic(rv_ctx *t, rv_ctx *n, const char *sample, const ch
     });
     pt.lap("classify");
     std::vector<Rec> recs;
+    size_t nrec = 0;
+    for (auto &pv : part) nrec += pv.size();
+    recs.reserve(nrec);
     for (auto &pv : part)
         for (auto &r : pv) recs.push_back(std::move(r));
     // the three Fisher tables of every record, tested on the device
@@ -392,9 +397,10 @@ rv_status host_format_somatic(rv_ctx *t, rv_ctx *n, const char *sample, const ch
     }
     pt.lap("fisher");
     const Region *regs = t->regions.data();
-    std::vector<std::string> texts(chunks_for((int64_t)recs.size(), 256));
-    parallel_chunks((int64_t)recs.size(), 256, [&](int64_t k, int64_t i0, int64_t i1) {
+    std::vector<std::string> texts(chunks_for((int64_t)recs.size(), 64));
+    parallel_chunks((int64_t)recs.size(), 64, [&](int64_t k, int64_t i0, int64_t i1) {
     std::string &o = texts[k];
+    o.reserve((size_t)(i1 - i0) * 640);
     char b[96];
     for (size_t i = (size_t)i0; i < (size_t)i1; i++) {
         const Rec &r = recs[i];
@@ -454,6 +460,9 @@ rv_status host_format_somatic(rv_ctx *t, rv_ctx *n, const char *sample, const ch
     }
     });
     t->text.clear();
+    size_t tl = 0;
+    for (auto &x : texts) tl += x.size();
+    t->text.reserve(tl);
     for (auto &x : texts) t->text += x;
     t->n_records = (int64_t)recs.size();
     t->h_records.clear();

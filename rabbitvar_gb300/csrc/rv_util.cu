@@ -223,6 +223,143 @@ __global__ void k_list_fill(DevState st, const uint32_t *off, Slot *out, uint32_
     }
 }
 
+// ---------------------------------------------------------------------------
+// Soft-clip consensus (findconseq, include/VariationUtils.h:403-509) of every
+// clip aggregate in the flattened lists, for the -k 1 realigner.  For an
+// aggregate at list index i: meta[i] = bit 31 computed | bit 30 the clip is
+// marked used (a low-complexity consensus) | bits 16-29 offset of its
+// characters from off[c] in `cons` | bits 0-15 length.  Clips with more than
+// kMaxNt per-offset base counts are left to the host (meta[i] = 0).
+// ---------------------------------------------------------------------------
+constexpr int kMaxNt = 256;
+
+__device__ __forceinline__ int clip_rank_d(char c) {
+    // measured iteration order of the reference's hash map over soft-clip
+    // bases: N, A, T, G, C
+    switch (c) {
+    case 'N': return 0;
+    case 'A': return 1;
+    case 'T': return 2;
+    case 'G': return 3;
+    case 'C': return 4;
+    default: return 5 + (unsigned char)c;
+    }
+}
+
+__global__ void k_clip_consensus(const Slot *list, const uint32_t *off, int64_t n_cells, const uint8_t *arena,
+                                 const unsigned long long *arena_used, uint32_t *meta, uint8_t *cons) {
+    const unsigned long long used_bytes = *arena_used;
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n_cells; c += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t b = off[c], e = off[c + 1];
+        uint32_t written = 0;
+        for (uint32_t i = b; i < e; i++) {
+            const int kind = list[i].kind;
+            meta[i] = 0u;
+            if (kind != KIND_SC5 && kind != KIND_SC3) continue;
+            const int seqk = kind == KIND_SC3 ? KIND_SC3_SEQ : KIND_SC5_SEQ;
+            const int agg_cnt = list[i].fwd + list[i].rev;
+            int idx[kMaxNt], cnt[kMaxNt], rk[kMaxNt];
+            char ch[kMaxNt];
+            double q[kMaxNt];
+            int n = 0;
+            bool over = false;
+            for (uint32_t j = b; j < e; j++) {
+                const Slot &t = list[j];
+                if (t.kind != seqk || t.klen != 3 || (unsigned long long)t.koff + 3 > used_bytes) continue;
+                if (n == kMaxNt) { over = true; break; }
+                const uint8_t *kb = arena + t.koff;
+                idx[n] = kb[0] | (kb[1] << 8);
+                ch[n] = (char)kb[2];
+                rk[n] = clip_rank_d(ch[n]);
+                cnt[n] = t.obs;
+                q[n] = t.q_sum;
+                n++;
+            }
+            if (over) continue;
+            // order by (offset, rank)
+            for (int x = 1; x < n; x++) {
+                int ix = idx[x], rx = rk[x], cx = cnt[x];
+                char hx = ch[x];
+                double qx = q[x];
+                int y = x - 1;
+                while (y >= 0 && (idx[y] > ix || (idx[y] == ix && rk[y] > rx))) {
+                    idx[y + 1] = idx[y]; rk[y + 1] = rk[y]; cnt[y + 1] = cnt[y]; ch[y + 1] = ch[y]; q[y + 1] = q[y];
+                    y--;
+                }
+                idx[y + 1] = ix; rk[y + 1] = rx; cnt[y + 1] = cx; ch[y + 1] = hx; q[y + 1] = qx;
+            }
+            int nts = 0;
+            for (int x = 0; x < n; x++)
+                if (x == 0 || idx[x] != idx[x - 1]) nts++;
+            // the consensus characters go straight to this clip's output range
+            if (written > 16383u) continue;
+            uint8_t *out = cons + b + written;
+            int total = 0, match = 0, sl = 0;
+            bool flag = false;
+            for (int x = 0; x < n;) {
+                int y = x;
+                while (y < n && idx[y] == idx[x]) y++;
+                int maxc = 0, tt = 0;
+                double maxq = 0;
+                char chosen = 0;
+                for (int k = x; k < y; k++) {
+                    tt += cnt[k];
+                    if (cnt[k] > maxc || q[k] > maxq) {
+                        maxc = cnt[k];
+                        chosen = ch[k];
+                        maxq = q[k];
+                    }
+                }
+                if (idx[x] == 3 && nts >= 6 && tt / (double)agg_cnt < 0.2 && tt <= 2) break;
+                if ((tt - maxc > 2 || maxc <= tt - maxc) && maxc / (double)tt < 0.8) {
+                    if (flag) break;
+                    flag = true;
+                }
+                total += tt;
+                match += maxc;
+                if (chosen != 0) out[sl++] = (uint8_t)chosen;
+                x = y;
+            }
+            bool keep = total != 0 && match / (double)total > 0.9 && sl / 1.5 > nts - sl &&
+                        (sl / (double)nts > 0.8 || nts - sl < 10 || sl > 25);
+            int len = sl;
+            if (!keep) {
+                out[0] = (uint8_t)' ';
+                len = 1;
+            }
+            bool used = false;
+            if (len > 12) {
+                bool a7 = true, t7 = true;
+                for (int k = 1; k < 8; k++) {
+                    a7 = a7 && out[k] == 'A';
+                    t7 = t7 && out[k] == 'T';
+                }
+                if (a7 || t7) used = true;
+                const char bases[4] = {'A', 'T', 'G', 'C'};
+                int kinds = 0;
+                bool low = false;
+                for (int m = 0; m < 4; m++) {
+                    int cc = 0;
+                    for (int k = 0; k < len; k++) cc += out[k] == (uint8_t)bases[m];
+                    if (cc > 0) kinds++;
+                    if (cc / (double)len > 0.75) low = true;
+                }
+                if (low || kinds < 3) used = true;
+            }
+            meta[i] = (1u << 31) | (used ? (1u << 30) : 0u) | (written << 16) | (uint32_t)len;
+            written += (uint32_t)len;
+        }
+    }
+}
+
+void launch_clip_consensus(const DevState &st, const uint32_t *off, const Slot *list, uint32_t *meta, uint8_t *cons,
+                           cudaStream_t s) {
+    const int64_t n = st.cells.n_cells;
+    if (n > 0)
+        k_clip_consensus<<<(int)std::min<int64_t>((n + 127) / 128, 4096), 128, 0, s>>>(
+            list, off, n, st.hash.arena, st.hash.arena_used, meta, cons);
+}
+
 // MNP keys (A/C/G/T '&' A/C/G/T...) that the realigner's adjustMNP visits.
 __global__ void k_select_mnv(DevState st, uint32_t *out, unsigned int *n_out) {
     unsigned long long n = st.hash.mask + 1ULL;
