@@ -137,8 +137,9 @@ def workload(k: int) -> str:
 METRIC = "reads/s pileup+var scoring (somatic pair 1 Mb, T200x+N100x)"
 CPU_TILES = 40   # CPU sample: 40 of the 100 tiles (~0.8 M reads, ~10 s on one core)
 # DRAM bytes (read + write) of one tumor-sample k_pileup_tiles<640, 3> launch
-# of this workload, from one ncu capture (profiles/k_pileup_tiles_somatic1mb.md)
-PILEUP_TRAFFIC = 1301.5e6
+# of this workload, from one ncu capture each (by -k:
+# profiles/k_pileup_tiles_somatic1mb.md, profiles/k_pileup_tiles_somatic1mb_k1.md)
+PILEUP_TRAFFIC = {0: 1301.5e6, 1: 1627.2e6}
 
 
 def cpu_baseline_run(g, tumor, normal, regions, threads: int, n_regions: int, k: int):
@@ -423,7 +424,7 @@ def main():
         "stage_ms": {k: statistics.mean(s[k] for s in stages) for k in stages[0]},
         "host_call_ms_per_step": {k: v / args.steps for k, v in host_ms.items()},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": PILEUP_TRAFFIC, "peak_kind": peak_kind,
+                     "frac": achieved / peak, "traffic": PILEUP_TRAFFIC[args.local_realign], "peak_kind": peak_kind,
                      "kernel": "k_pileup_tiles", "launch": "tumor sample, 1.33 M reads, timed alone",
                      "alg_bytes_per_launch": per_launch_bytes, "launch_ms": tile_ms,
                      "launch_ms_sharing_gpu": tile_ms_shared},
