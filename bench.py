@@ -178,12 +178,16 @@ def other_k_leg(g, tumor, normal, regions, k: int, steps: int, warmup: int, devi
         _, n = pair.format_records("T", "ctg")
         return dt, n
 
-    for _ in range(warmup):
-        step(True)
+    # end to end: the same stream of batches as the main line
+    stream = api.SomaticStream(api.default_params(local_realign=k, fisher=1), device=device)
+    stream.upload_reference(tumor.contig, synth.genome_str(g).encode())
+    job = (batches[0], batches[1], regions)
+    stream.run([job] * max(1, warmup), "T", "ctg")
     t0 = time.perf_counter()
-    for _ in range(steps):
-        step(True)
+    stream.run([job] * steps, "T", "ctg")
     e2e_dt = time.perf_counter() - t0
+    stream.close()
+    pair.submit(batches[0], batches[1], regions)
     for _ in range(warmup):
         step(False)
     t0 = time.perf_counter()
@@ -361,26 +365,23 @@ def main():
         return kernels_of(), n
 
     io = {"h2d": 0, "d2h": 0}
-
-    def e2e_step():
-        # both uploads are queued first (each context has its own stream), so
-        # the second sample's copy overlaps the first sample's kernels
-        pair.submit(batches[0], batches[1], regions)
-        pair.pileup_realign()
-        pair.score()
-        text, n = pair.format_records("T", "ctg")
-        io["h2d"] = sum(c.io_bytes()[0] for c in ctxs)
-        io["d2h"] = sum(c.io_bytes()[1] for c in ctxs)
-        return kernels_of(), n
-
-    # e2e: pinned host batch -> device every step
-    for _ in range(args.warmup):
-        e2e_step()
+    # e2e: a stream of batches through rv_call_somatic_stream (two context
+    # pairs: one pair's records are formatted on a host thread while the
+    # other pair's next batch is uploaded and piled up); every step uploads
+    # its pinned host batches and reads back its records
+    stream = api.SomaticStream(params, device=local)
+    stream.upload_reference(tumor.contig, synth.genome_str(g).encode())
+    job = (batches[0], batches[1], regions)
+    stream.run([job] * max(1, args.warmup), "T", "ctg")
     clocks = Clocks(local)
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        e2e_step()
+    e2e_texts = stream.run([job] * args.steps, "T", "ctg")
     e2e_dt = barrier_max(dist, time.perf_counter() - t0)
+    last = stream.pairs[(args.steps - 1) % 2]
+    io["h2d"] = sum(c.io_bytes()[0] for c in (last.tumor, last.normal))
+    io["d2h"] = sum(c.io_bytes()[1] for c in (last.tumor, last.normal))
+    stream.close()
+    pair.submit(batches[0], batches[1], regions)
     # value: reads resident on the device (submitted once above), device-side steps
     for _ in range(args.warmup):
         device_step()
@@ -393,6 +394,8 @@ def main():
         kernels += k
     dev_dt = barrier_max(dist, time.perf_counter() - t0)
     clk = clocks.stop()
+    if any(len(t.splitlines()) != recs for t in e2e_texts):
+        raise RuntimeError("the streamed batches gave a different record count from the resident steps")
     ms_per_step = dev_dt / args.steps * 1e3
     value = n_reads * world * args.steps / dev_dt
     e2e = n_reads * world * args.steps / e2e_dt

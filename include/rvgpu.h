@@ -198,6 +198,28 @@ rv_status rv_call_somatic(rv_ctx *tumor, rv_ctx *normal, const rv_read_batch *tu
                           const char *sample, const char *gene, const char **text, size_t *text_len,
                           int64_t *n_records);
 
+/* A sequence of somatic batches (the contigs of a pair of BAM files, or
+ * chunks of a BED file): the two samples' reads of one region list. */
+typedef struct {
+    const rv_read_batch *tumor, *normal;
+    const rv_region *regions;
+    int n_regions;
+    const char *sample, *gene;
+} rv_somatic_job;
+
+/* Receives each job's records, in job order, on the calling thread; the text
+ * is valid during the call. */
+typedef void (*rv_somatic_sink)(void *user, int64_t job, const char *text, size_t text_len, int64_t n_records);
+
+/* rv_call_somatic over n_jobs jobs with two context pairs (tumor0/normal0 take
+ * the even jobs, tumor1/normal1 the odd ones): while one pair's records are
+ * formatted on a host thread, the other pair's next batch is uploaded and
+ * piled up.  The records are those of n_jobs rv_call_somatic calls (the
+ * reference's per-region loop over a BED file, SomaticMode::process,
+ * src/modes/somaticMode.cpp:736-990, emits them in the same order). */
+rv_status rv_call_somatic_stream(rv_ctx *tumor0, rv_ctx *normal0, rv_ctx *tumor1, rv_ctx *normal1,
+                                 const rv_somatic_job *jobs, int64_t n_jobs, rv_somatic_sink sink, void *user);
+
 /* Candidate set of the learned filter (include/rvgpu_mlp.h); no counterpart in
  * the reference.  rv_score_candidates replaces rv_score after rv_realign: every
  * position with a non-reference allele seen at least `min_count` times keeps all

@@ -49,6 +49,14 @@ class Region(C.Structure):
     _fields_ = [("start", C.c_int32), ("end", C.c_int32)]
 
 
+class SomaticJob(C.Structure):
+    _fields_ = [("tumor", C.POINTER(ReadBatch)), ("normal", C.POINTER(ReadBatch)), ("regions", C.POINTER(Region)),
+                ("n_regions", C.c_int), ("sample", C.c_char_p), ("gene", C.c_char_p)]
+
+
+SomaticSink = C.CFUNCTYPE(None, C.c_void_p, C.c_int64, C.POINTER(C.c_char), C.c_size_t, C.c_int64)
+
+
 class Candidate(C.Structure):
     _fields_ = [("region", C.c_int32), ("position", C.c_int32), ("hard_pass", C.c_int32), ("key_len", C.c_int32),
                 ("key", C.c_char * 48)]
@@ -65,7 +73,7 @@ class SiteRecord(C.Structure):
 
 EXPORTS = ["rv_default_params", "rv_create", "rv_destroy", "rv_last_error", "rv_upload_reference",
            "rv_submit_batch", "rv_pileup", "rv_realign", "rv_score", "rv_format_records", "rv_fetch_records",
-           "rv_call_regions", "rv_score_candidates", "rv_candidates", "rv_score_pair", "rv_pileup_realign_pair", "rv_format_somatic", "rv_call_somatic", "rv_export_maps", "rv_last_timings", "rv_stage_times", "rv_io_bytes", "rv_fisher_batch", "rv_bam_read",
+           "rv_call_regions", "rv_score_candidates", "rv_candidates", "rv_score_pair", "rv_pileup_realign_pair", "rv_format_somatic", "rv_call_somatic", "rv_call_somatic_stream", "rv_export_maps", "rv_last_timings", "rv_stage_times", "rv_io_bytes", "rv_fisher_batch", "rv_bam_read",
            "rv_bam_contigs", "rv_bam_batch", "rv_bam_free", "rv_fasta_read", "rv_free", "rv_alloc_pinned",
            "rv_free_pinned", "rv_mlp_create", "rv_mlp_destroy", "rv_mlp_last_error", "rv_mlp_set_params",
            "rv_mlp_get_params", "rv_mlp_train", "rv_mlp_gradients", "rv_mlp_predict", "rv_mlp_step_ms"]
@@ -98,6 +106,7 @@ def lib():
     L.rv_fetch_records.argtypes = [vp, C.POINTER(SiteRecord), sz, C.POINTER(sz)]
     L.rv_score_pair.argtypes = [vp, vp]
     L.rv_pileup_realign_pair.argtypes = [vp, vp]
+    L.rv_call_somatic_stream.argtypes = [vp, vp, vp, vp, C.POINTER(SomaticJob), i64, SomaticSink, vp]
     L.rv_score_candidates.argtypes = [vp, C.c_int]
     L.rv_candidates.argtypes = [vp, vp, vp, i64, C.POINTER(i64)]
     L.rv_format_somatic.argtypes = [vp, vp, C.c_char_p, C.c_char_p, C.POINTER(C.c_char_p), C.POINTER(sz),
@@ -351,6 +360,46 @@ class SomaticPair:
         self.realign()
         self.score()
         return self.format_records(sample, gene)[0]
+
+
+class SomaticStream:
+    """Somatic calling over a sequence of batches with two tumor/normal
+    context pairs (rv_call_somatic_stream): while one pair's records are
+    formatted on a host thread, the other pair's next batch is uploaded and
+    piled up.  The records are those of one SomaticPair.call per batch."""
+
+    def __init__(self, params: Params | None = None, device: int = 0, budget: int = 0):
+        self.pairs = [SomaticPair(params, device, budget), SomaticPair(params, device, budget)]
+
+    def close(self):
+        for p in self.pairs:
+            p.close()
+
+    def upload_reference(self, chr_name: str, bases: bytes):
+        for p in self.pairs:
+            p.upload_reference(chr_name, bases)
+
+    def run(self, jobs, sample: str = "T", gene: str | None = None) -> list[str]:
+        """jobs: (tumor Batch, normal Batch, regions) per batch; returns the
+        record text of each, in order."""
+        keep = []
+        arr = (SomaticJob * max(1, len(jobs)))()
+        for i, (tb, nb, regions) in enumerate(jobs):
+            ts, ns = tb.struct(), nb.struct()
+            rg = (Region * max(len(regions), 1))(*[Region(a, b) for a, b in regions])
+            keep += [ts, ns, rg]
+            arr[i] = SomaticJob(C.pointer(ts), C.pointer(ns), C.cast(rg, C.POINTER(Region)), len(regions),
+                                sample.encode(), gene.encode() if gene else None)
+        out = [None] * len(jobs)
+
+        def sink(_user, k, text, n, _nrec):
+            out[k] = C.string_at(text, n).decode()
+
+        cb = SomaticSink(sink)
+        t0, n0 = self.pairs[0].tumor, self.pairs[0].normal
+        t1, n1 = self.pairs[1].tumor, self.pairs[1].normal
+        t0._check(t0.L.rv_call_somatic_stream(t0.h, n0.h, t1.h, n1.h, arr, len(jobs), cb, None))
+        return out
 
 
 def read_bam(path: str, threads: int = 0):

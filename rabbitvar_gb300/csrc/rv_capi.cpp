@@ -11,6 +11,7 @@
 #include <cstring>
 #include <set>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "rv_ctx.h"
@@ -984,6 +985,68 @@ rv_status rv_pileup_realign_pair(rv_ctx *tumor, rv_ctx *normal) {
     if ((s = pileup_finish(normal, normal->stream))) { tumor->err = normal->err; return s; }
     if ((s = rv_realign(normal, nullptr))) { tumor->err = normal->err; return s; }
     return RV_OK;
+}
+
+rv_status rv_call_somatic_stream(rv_ctx *tumor0, rv_ctx *normal0, rv_ctx *tumor1, rv_ctx *normal1,
+                                 const rv_somatic_job *jobs, int64_t n_jobs, rv_somatic_sink sink, void *user) {
+    rv_ctx *T[2] = {tumor0, tumor1}, *N[2] = {normal0, normal1};
+    if (!tumor0 || !normal0 || !tumor1 || !normal1 || (!jobs && n_jobs > 0) || n_jobs < 0) return RV_ERR_ARG;
+    rv_ctx *all[4] = {tumor0, normal0, tumor1, normal1};
+    for (int a = 0; a < 4; a++)
+        for (int b = a + 1; b < 4; b++)
+            if (all[a] == all[b]) { tumor0->err = "rv_call_somatic_stream needs four distinct contexts"; return RV_ERR_ARG; }
+    struct Fmt {
+        std::thread th;
+        rv_status st = RV_OK;
+        bool active = false;
+    } fmt[2];
+    auto join_all = [&] {
+        for (auto &f : fmt)
+            if (f.active) { f.th.join(); f.active = false; }
+    };
+    auto finish = [&](int pi, int64_t k) -> rv_status {
+        if (!fmt[pi].active) return RV_OK;
+        fmt[pi].th.join();
+        fmt[pi].active = false;
+        if (fmt[pi].st) return fmt[pi].st;
+        if (sink) sink(user, k, T[pi]->text.c_str(), T[pi]->text.size(), T[pi]->n_records);
+        return RV_OK;
+    };
+    auto submit = [&](int pi, int64_t k) -> rv_status {
+        const rv_somatic_job &j = jobs[k];
+        rv_status s = rv_submit_batch(T[pi], j.tumor, j.regions, j.n_regions, nullptr);
+        if (!s && (s = rv_submit_batch(N[pi], j.normal, j.regions, j.n_regions, nullptr))) T[pi]->err = N[pi]->err;
+        return s;
+    };
+    rv_status s = RV_OK;
+    int bad = 0;  // the pair whose context holds the error message
+    if (n_jobs > 0) s = submit(0, 0);
+    for (int64_t k = 0; k < n_jobs && !s; k++) {
+        const int pi = (int)(k & 1);
+        bad = pi;
+        // device stages of job k on pair pi; the host thread formats job k - 1 meanwhile
+        if ((s = rv_pileup_realign_pair(T[pi], N[pi]))) break;
+        bad = pi ^ 1;
+        if ((s = finish(pi ^ 1, k - 1))) break;
+        // the other pair is free: upload job k + 1 while job k is scored
+        if (k + 1 < n_jobs && (s = submit(pi ^ 1, k + 1))) break;
+        bad = pi;
+        if ((s = rv_score_pair(T[pi], N[pi]))) break;
+        fmt[pi].active = true;
+        const rv_somatic_job *j = &jobs[k];
+        rv_ctx *t = T[pi], *n = N[pi];
+        rv_status *out = &fmt[pi].st;
+        fmt[pi].th = std::thread([t, n, j, out] {
+            *out = rv_format_somatic(t, n, j->sample, j->gene, nullptr, nullptr, nullptr);
+        });
+    }
+    if (!s && n_jobs > 0) {
+        bad = (int)((n_jobs - 1) & 1);
+        s = finish(bad, n_jobs - 1);
+    }
+    join_all();
+    if (s && bad != 0) T[0]->err = T[bad]->err;
+    return s;
 }
 
 rv_status rv_format_somatic(rv_ctx *tumor, rv_ctx *normal, const char *sample, const char *gene, const char **text,

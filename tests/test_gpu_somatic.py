@@ -57,3 +57,24 @@ def test_somatic_tiles_match_golden():
     ora_t = ora_t.splitlines()
     assert len(mine_t) == len(ora_t) > 100
     assert diff_records(ora_t, mine_t, somatic=True) == []
+
+
+def test_somatic_stream_matches_calls():
+    """rv_call_somatic_stream over three batches (two context pairs, records
+    formatted on a host thread while the next batch is piled up) gives the
+    records of one call per batch, in order."""
+    from rabbitvar_gb300 import api, synth
+    g, _, t, n = synth.somatic_mix(0x5EED0051)
+    regions = [[(1, g.shape[0])], [(1, 3000), (3001, 9000), (9001, g.shape[0])], [(8001, 20000)]]
+    params = dict(local_realign=1, fisher=1)
+    pair = api.SomaticPair(api.default_params(**params))
+    pair.upload_reference(t.contig, synth.genome_str(g).encode())
+    bt, bn = api.Batch.from_readset(t), api.Batch.from_readset(n)
+    want = [pair.call(bt, bn, rg, "T", t.contig) for rg in regions]
+    pair.close()
+    stream = api.SomaticStream(api.default_params(**params))
+    stream.upload_reference(t.contig, synth.genome_str(g).encode())
+    got = stream.run([(bt, bn, rg) for rg in regions + regions[:1]], "T", t.contig)
+    stream.close()
+    assert got == want + want[:1]
+    assert all(len(w.splitlines()) > 10 for w in want)
