@@ -55,15 +55,18 @@ def make_workload(seed_offset: int = 0):
 
 
 class Clocks:
-    """nvidia-smi sampling during the timed region."""
+    """nvidia-smi sampling (every 200 ms) started before the warm-up, so that
+    its start-up does not fall in a timed region; the samples taken inside the
+    timed regions (marked with window()) are the ones reported."""
 
     def __init__(self, index: int = 0):
         self.p = None
+        self.windows = []
         self.path = f"/tmp/rv_clocks_{os.getpid()}.csv"
         try:
             self.p = subprocess.Popen(
                 ["nvidia-smi", f"--id={index}",
-                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "--query-gpu=timestamp,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
                  "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
                  "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
                  "--format=csv,noheader,nounits", "-lms", "200"],
@@ -71,29 +74,41 @@ class Clocks:
         except (OSError, FileNotFoundError):
             self.p = None
 
+    def window(self, t0: float, t1: float):
+        """A timed region, in time.time() seconds."""
+        self.windows.append((t0, t1))
+
     def stop(self) -> dict:
         if not self.p:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.p.terminate()
         self.p.wait()
-        sm, mx, reasons = [], [], set()
+        rows = []
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         with open(self.path) as f:
             for ln in f:
                 c = [x.strip() for x in ln.split(",")]
-                if len(c) < 8:
+                if len(c) < 9:
                     continue
                 try:
-                    sm.append(float(c[0]))
-                    mx.append(float(c[1]))
-                except ValueError:
+                    ts = time.mktime(time.strptime(c[0].split(".")[0], "%Y/%m/%d %H:%M:%S"))
+                    ts += float("0." + c[0].split(".")[1]) if "." in c[0] else 0.0
+                    rows.append((ts, float(c[1]), float(c[2]), c[5:9]))
+                except (ValueError, IndexError):
                     continue
-                for n, v in zip(names, c[4:8]):
-                    if v.lower() == "active":
-                        reasons.add(n)
         os.unlink(self.path)
+        inside = [r for r in rows if any(a - 0.25 <= r[0] <= b + 0.25 for a, b in self.windows)]
+        use = inside or rows
+        reasons = set()
+        for r in use:
+            for n, v in zip(names, r[3]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        sm = [r[1] for r in use]
+        mx = [r[2] for r in use]
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(use),
+                "window": "timed regions" if inside else "whole run (no sample fell inside the timed regions)"}
 
 
 def measured_peak_hbm():
@@ -372,11 +387,13 @@ def main():
     stream = api.SomaticStream(params, device=local)
     stream.upload_reference(tumor.contig, synth.genome_str(g).encode())
     job = (batches[0], batches[1], regions)
-    stream.run([job] * max(1, args.warmup), "T", "ctg")
     clocks = Clocks(local)
+    stream.run([job] * max(1, args.warmup), "T", "ctg")
+    w0 = time.time()
     t0 = time.perf_counter()
     e2e_texts = stream.run([job] * args.steps, "T", "ctg")
     e2e_dt = barrier_max(dist, time.perf_counter() - t0)
+    clocks.window(w0, time.time())
     last = stream.pairs[(args.steps - 1) % 2]
     io["h2d"] = sum(c.io_bytes()[0] for c in (last.tumor, last.normal))
     io["d2h"] = sum(c.io_bytes()[1] for c in (last.tumor, last.normal))
@@ -386,6 +403,7 @@ def main():
     for _ in range(args.warmup):
         device_step()
     stages = []
+    w0 = time.time()
     t0 = time.perf_counter()
     kernels = 0
     recs = 0
@@ -393,6 +411,7 @@ def main():
         k, recs = device_step(stages)
         kernels += k
     dev_dt = barrier_max(dist, time.perf_counter() - t0)
+    clocks.window(w0, time.time())
     clk = clocks.stop()
     if any(len(t.splitlines()) != recs for t in e2e_texts):
         raise RuntimeError("the streamed batches gave a different record count from the resident steps")

@@ -417,11 +417,21 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
     tm.lap("prep+alloc");
     // -k 1: the alignment spans stay on the host for noPassingReads
     if (ctx->params.local_realign) {
-        ctx->h_pos.assign(b->pos, b->pos + n);
-        ctx->h_flag.assign(b->flag, b->flag + n);
-        ctx->h_ncig.assign(b->n_cigar, b->n_cigar + n);
-        ctx->h_cigoff.assign(b->cig_off, b->cig_off + n);
-        ctx->h_cigar.assign(b->cigar, b->cigar + b->n_cigar_words);
+        // copied in chunks on the host threads (tens of MB for a deep batch)
+        ctx->h_pos.resize((size_t)n);
+        ctx->h_flag.resize((size_t)n);
+        ctx->h_ncig.resize((size_t)n);
+        ctx->h_cigoff.resize((size_t)n);
+        ctx->h_cigar.resize((size_t)b->n_cigar_words);
+        parallel_chunks(n, 1 << 16, [&](int64_t, int64_t a, int64_t e) {
+            std::copy(b->pos + a, b->pos + e, ctx->h_pos.data() + a);
+            std::copy(b->flag + a, b->flag + e, ctx->h_flag.data() + a);
+            std::copy(b->n_cigar + a, b->n_cigar + e, ctx->h_ncig.data() + a);
+            std::copy(b->cig_off + a, b->cig_off + e, ctx->h_cigoff.data() + a);
+        });
+        parallel_chunks(b->n_cigar_words, 1 << 18, [&](int64_t, int64_t a, int64_t e) {
+            std::copy(b->cigar + a, b->cigar + e, ctx->h_cigar.data() + a);
+        });
     } else {
         ctx->h_pos.clear();
         ctx->h_flag.clear();
@@ -484,13 +494,15 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
     parallel_for(n_regions, [&](int64_t r) {
         Region &R = ctx->regions[r];
         if (R.r1 <= R.r0) return;
-        int lo = INT32_MAX, hi = INT32_MIN;
+        int lo = INT32_MAX, hi = INT32_MIN, reach = 0;
         for (int64_t i = R.r0; i < R.r1; i++) {
             lo = std::min(lo, std::max(ctx->h_span_lo[i], 1));
             hi = std::max(hi, ctx->h_span_hi[i]);
+            reach = std::max(reach, ctx->h_span_hi[i] - (b->pos[i] + 1));
         }
         R.span_lo = lo;
         R.span_hi = hi;
+        R.reach = reach;
         R.serial = hi + kEdgeMargin > R.we ? 1 : 0;
         if (lo < R.clo || hi > R.chi) span_bad.store(1);
         for (int64_t k = tile_begin[r]; k < tile_begin[r + 1]; k++) {

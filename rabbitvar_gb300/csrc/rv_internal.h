@@ -70,6 +70,8 @@ struct Region {
     int32_t max_read_len;    // maxReadLength of the region
     int32_t err;             // error bits
     int32_t edge_hit;        // an edge read would insert a position past the window
+    int32_t reach;           // max over the region's reads of (span end - 1-based start)
+    int32_t pad;
 };
 
 struct Tile {

@@ -521,11 +521,12 @@ __global__ void k_edge_detect(DevState st, DevParams P) {
     __shared__ int hit;
     if (threadIdx.x == 0) hit = 0;
     __syncthreads();
-    const int kEdgeGuard = 4096;
+    // the first read that can reach within kEdgeMargin of the window end
+    // (R.reach: the farthest any read of the region reaches past its start)
     int64_t lo = R.r0, hi = R.r1;
     while (lo < hi) {
         int64_t mid = (lo + hi) / 2;
-        if (st.batch.pos[mid] + 1 + kEdgeGuard < R.we) lo = mid + 1; else hi = mid;
+        if (st.batch.pos[mid] + 1 + R.reach + kEdgeMargin <= R.we) lo = mid + 1; else hi = mid;
     }
     DetectSink sink;
     sink.R = &R;
@@ -560,20 +561,19 @@ __global__ void k_pileup_serial(DevState st, DevParams P) {
     sink.ph_hi = ph_hi;
     sink.ph_lo = ph_lo;
     Walker<SerialSink> w(P, sink, R, st.ref, st.ref_len);
-    // edge reads start within kEdgeGuard of the window end (reads are
-    // coordinate sorted); find the first candidate by binary search
-    const int kEdgeGuard = 4096;
+    // edge reads are the ones that can reach within kEdgeMargin of the window
+    // end (reads are coordinate sorted; R.reach is the farthest any read of
+    // the region reaches past its start): the first by binary search
     int64_t lo = R.r0, hi = R.r1;
     while (lo < hi) {
         int64_t mid = (lo + hi) / 2;
-        if (st.batch.pos[mid] + 1 + kEdgeGuard < R.we) lo = mid + 1; else hi = mid;
+        if (st.batch.pos[mid] + 1 + R.reach + kEdgeMargin <= R.we) lo = mid + 1; else hi = mid;
     }
     for (int64_t r = lo; r < R.r1; r++) {
         if (!read_passes(st.batch, P, R, r)) continue;
         int a, b;
         read_span(st.batch, r, a, b, P.local_realign != 0);
         if (!is_edge(R, b)) continue;
-        if (b - (st.batch.pos[r] + 1) > kEdgeGuard) { sink.error(ERR_UNSUPPORTED); continue; }
         w.walk(st.batch, r);
     }
 }
@@ -599,8 +599,9 @@ __global__ void k_resolve_deferred(DevState st, DevParams P, int max_probe_reads
         for (int64_t r = d.read - 1; !ps.found && r >= R.r0; r--) {
             int a, b;
             read_span(st.batch, r, a, b, P.local_realign != 0);
-            // reads are coordinate-sorted: stop once no earlier read can reach pos
-            if (st.batch.pos[r] + 1 + 4 * 1024 < d.pos) break;
+            // reads are coordinate-sorted: stop once no earlier read can reach
+            // pos (R.reach: the farthest any read of the region reaches past its start)
+            if (st.batch.pos[r] + 1 + R.reach < d.pos) break;
             if (a > d.pos || b < d.pos) continue;
             if (!read_passes(st.batch, P, R, r)) continue;
             if (++probes > max_probe_reads) { set_err(st.err, ERR_PROBE_LIMIT); break; }

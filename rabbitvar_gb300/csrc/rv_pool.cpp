@@ -18,8 +18,12 @@ thread_local bool t_in_section = false;
 class Pool {
   public:
     Pool() {
+        // leaves two cores to the threads outside the pool (the caller's other
+        // host work, a record-formatting thread, the CUDA runtime's threads):
+        // an oversubscribed core would stall a whole parallel section
         unsigned hw = std::thread::hardware_concurrency();
-        int n = (int)std::min(hw ? hw : 1u, 32u) - 1;
+        int n = (int)std::min(hw ? hw : 1u, 32u) - 3;
+        if (n < 0) n = 0;
         for (int i = 0; i < n; i++) workers_.emplace_back([this] { loop(); });
     }
     int threads() const { return (int)workers_.size() + 1; }
