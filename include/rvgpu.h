@@ -212,9 +212,9 @@ typedef struct {
 typedef void (*rv_somatic_sink)(void *user, int64_t job, const char *text, size_t text_len, int64_t n_records);
 
 /* rv_call_somatic over n_jobs jobs with two context pairs (tumor0/normal0 take
- * the even jobs, tumor1/normal1 the odd ones): while one pair's records are
- * formatted on a host thread, the other pair's next batch is uploaded and
- * piled up.  The records are those of n_jobs rv_call_somatic calls (the
+ * the even jobs, tumor1/normal1 the odd ones): while one pair's batch is piled
+ * up, realigned and scored, a host thread formats the other pair's records and
+ * uploads that pair's next batch.  The records are those of n_jobs rv_call_somatic calls (the
  * reference's per-region loop over a BED file, SomaticMode::process,
  * src/modes/somaticMode.cpp:736-990, emits them in the same order). */
 rv_status rv_call_somatic_stream(rv_ctx *tumor0, rv_ctx *normal0, rv_ctx *tumor1, rv_ctx *normal1,

@@ -1032,24 +1032,37 @@ rv_status rv_call_somatic_stream(rv_ctx *tumor0, rv_ctx *normal0, rv_ctx *tumor1
     };
     rv_status s = RV_OK;
     int bad = 0;  // the pair whose context holds the error message
+    // jobs 0 and 1 are uploaded here; job k + 2 by the host thread that
+    // formats job k, on the same pair, right after it
     if (n_jobs > 0) s = submit(0, 0);
+    if (!s && n_jobs > 1) {
+        bad = 1;
+        s = submit(1, 1);
+    }
     for (int64_t k = 0; k < n_jobs && !s; k++) {
         const int pi = (int)(k & 1);
         bad = pi;
-        // device stages of job k on pair pi; the host thread formats job k - 1 meanwhile
+        // device stages of job k on pair pi; the host thread formats job k - 1
+        // and uploads job k + 1 on the other pair meanwhile
         if ((s = rv_pileup_realign_pair(T[pi], N[pi]))) break;
         bad = pi ^ 1;
         if ((s = finish(pi ^ 1, k - 1))) break;
-        // the other pair is free: upload job k + 1 while job k is scored
-        if (k + 1 < n_jobs && (s = submit(pi ^ 1, k + 1))) break;
         bad = pi;
         if ((s = rv_score_pair(T[pi], N[pi]))) break;
         fmt[pi].active = true;
         const rv_somatic_job *j = &jobs[k];
         rv_ctx *t = T[pi], *n = N[pi];
         rv_status *out = &fmt[pi].st;
-        fmt[pi].th = std::thread([t, n, j, out] {
-            *out = rv_format_somatic(t, n, j->sample, j->gene, nullptr, nullptr, nullptr);
+        const rv_somatic_job *next = k + 2 < n_jobs ? &jobs[k + 2] : nullptr;
+        fmt[pi].th = std::thread([t, n, j, next, out] {
+            rv_status st = rv_format_somatic(t, n, j->sample, j->gene, nullptr, nullptr, nullptr);
+            // the records stay in t->text until this pair is formatted again
+            if (!st && next) {
+                st = rv_submit_batch(t, next->tumor, next->regions, next->n_regions, nullptr);
+                if (!st && (st = rv_submit_batch(n, next->normal, next->regions, next->n_regions, nullptr)))
+                    t->err = n->err;
+            }
+            *out = st;
         });
     }
     if (!s && n_jobs > 0) {
