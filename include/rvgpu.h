@@ -199,7 +199,9 @@ rv_status rv_call_somatic(rv_ctx *tumor, rv_ctx *normal, const rv_read_batch *tu
                           int64_t *n_records);
 
 /* A sequence of somatic batches (the contigs of a pair of BAM files, or
- * chunks of a BED file): the two samples' reads of one region list. */
+ * chunks of a BED file): the two samples' reads of one region list.  A job
+ * whose tumor and normal batches are both NULL runs again on the batch its
+ * context pair already holds (regions as submitted then). */
 typedef struct {
     const rv_read_batch *tumor, *normal;
     const rv_region *regions;

@@ -385,10 +385,14 @@ class SomaticStream:
         keep = []
         arr = (SomaticJob * max(1, len(jobs)))()
         for i, (tb, nb, regions) in enumerate(jobs):
-            ts, ns = tb.struct(), nb.struct()
+            # (None, None, regions): run again on the batch the pair holds
+            ts = tb.struct() if tb is not None else None
+            ns = nb.struct() if nb is not None else None
             rg = (Region * max(len(regions), 1))(*[Region(a, b) for a, b in regions])
             keep += [ts, ns, rg]
-            arr[i] = SomaticJob(C.pointer(ts), C.pointer(ns), C.cast(rg, C.POINTER(Region)), len(regions),
+            arr[i] = SomaticJob(C.pointer(ts) if ts is not None else C.POINTER(ReadBatch)(),
+                                C.pointer(ns) if ns is not None else C.POINTER(ReadBatch)(),
+                                C.cast(rg, C.POINTER(Region)), len(regions),
                                 sample.encode(), gene.encode() if gene else None)
         out = [None] * len(jobs)
 

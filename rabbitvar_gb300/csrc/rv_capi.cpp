@@ -1024,8 +1024,17 @@ rv_status rv_call_somatic_stream(rv_ctx *tumor0, rv_ctx *normal0, rv_ctx *tumor1
         if (sink) sink(user, k, T[pi]->text.c_str(), T[pi]->text.size(), T[pi]->n_records);
         return RV_OK;
     };
+    // a job without batches reuses the batch already on its pair's devices
+    auto resident = [&](int pi) -> rv_status {
+        if (T[pi]->stage < 1 || N[pi]->stage < 1) {
+            T[pi]->err = "rv_call_somatic_stream: a job without batches needs a batch submitted on its pair";
+            return RV_ERR_STATE;
+        }
+        return RV_OK;
+    };
     auto submit = [&](int pi, int64_t k) -> rv_status {
         const rv_somatic_job &j = jobs[k];
+        if (!j.tumor && !j.normal) return resident(pi);
         rv_status s = rv_submit_batch(T[pi], j.tumor, j.regions, j.n_regions, nullptr);
         if (!s && (s = rv_submit_batch(N[pi], j.normal, j.regions, j.n_regions, nullptr))) T[pi]->err = N[pi]->err;
         return s;
@@ -1039,16 +1048,20 @@ rv_status rv_call_somatic_stream(rv_ctx *tumor0, rv_ctx *normal0, rv_ctx *tumor1
         bad = 1;
         s = submit(1, 1);
     }
+    PhaseTimer tm("stream");
     for (int64_t k = 0; k < n_jobs && !s; k++) {
         const int pi = (int)(k & 1);
         bad = pi;
         // device stages of job k on pair pi; the host thread formats job k - 1
         // and uploads job k + 1 on the other pair meanwhile
         if ((s = rv_pileup_realign_pair(T[pi], N[pi]))) break;
+        tm.lap("pileup_realign");
         bad = pi ^ 1;
         if ((s = finish(pi ^ 1, k - 1))) break;
+        tm.lap("wait_format");
         bad = pi;
         if ((s = rv_score_pair(T[pi], N[pi]))) break;
+        tm.lap("score");
         fmt[pi].active = true;
         const rv_somatic_job *j = &jobs[k];
         rv_ctx *t = T[pi], *n = N[pi];
@@ -1057,7 +1070,7 @@ rv_status rv_call_somatic_stream(rv_ctx *tumor0, rv_ctx *normal0, rv_ctx *tumor1
         fmt[pi].th = std::thread([t, n, j, next, out] {
             rv_status st = rv_format_somatic(t, n, j->sample, j->gene, nullptr, nullptr, nullptr);
             // the records stay in t->text until this pair is formatted again
-            if (!st && next) {
+            if (!st && next && (next->tumor || next->normal)) {
                 st = rv_submit_batch(t, next->tumor, next->regions, next->n_regions, nullptr);
                 if (!st && (st = rv_submit_batch(n, next->normal, next->regions, next->n_regions, nullptr)))
                     t->err = n->err;
