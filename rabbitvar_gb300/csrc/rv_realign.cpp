@@ -167,7 +167,7 @@ uint64_t pos_key(int region, int pos) { return ((uint64_t)(uint32_t)region << 32
 // ---------------------------------------------------------------------------
 struct Mirror {
     rv_ctx *ctx = nullptr;
-    const uint32_t *fwd, *rev, *hi, *tp, *q, *mq, *first, *cov;
+    const uint32_t *fwd, *rev, *hi, *tp, *q, *mq, *first;
     const int32_t *nm;
     const uint8_t *kflags;
     const uint32_t *off = nullptr;   // n_cells + 1
@@ -1288,7 +1288,7 @@ rv_status mirror_launch(rv_ctx *ctx, cudaEvent_t after_kernels) {
     for (int k = 0; k < 8; k++, h += L.b_arr)
         if (nc) HCUDA(cudaMemcpyAsync(h, dev_arr[k], L.b_arr, cudaMemcpyDeviceToHost, s));
     if (nc) {
-        HCUDA(cudaMemcpyAsync(h, C.cov, (size_t)nc * 4, cudaMemcpyDeviceToHost, s));
+        // (coverage is not read by the realigner: its additions go back as deltas)
         HCUDA(cudaMemcpyAsync(h + L.b_cov, C.kflags, (size_t)nc, cudaMemcpyDeviceToHost, s));
         HCUDA(cudaMemcpyAsync(h + L.b_cov + L.b_kf, ctx->d_list_off, ((size_t)nc + 1) * 4, cudaMemcpyDeviceToHost, s));
     }
@@ -1347,7 +1347,7 @@ rv_status host_realign_full(rv_ctx *ctx) {
                               cudaMemcpyDeviceToHost, s));
     HCUDA(cudaStreamSynchronize(s));
     if ((st = pull_arena(ctx))) return st;
-    ctx->io_d2h += (int64_t)(L.cells + (size_t)total * (sizeof(Slot) + 9) + ctx->h_arena.size());
+    ctx->io_d2h += (int64_t)(L.cells - L.b_cov + (size_t)total * (sizeof(Slot) + 9) + ctx->h_arena.size());
     mir.fwd = (const uint32_t *)host_arr[0];
     mir.rev = (const uint32_t *)host_arr[1];
     mir.hi = (const uint32_t *)host_arr[2];
@@ -1356,7 +1356,6 @@ rv_status host_realign_full(rv_ctx *ctx) {
     mir.mq = (const uint32_t *)host_arr[5];
     mir.nm = (const int32_t *)host_arr[6];
     mir.first = (const uint32_t *)host_arr[7];
-    mir.cov = (const uint32_t *)h_cov;
     mir.kflags = (const uint8_t *)h_kf;
     mir.off = (const uint32_t *)h_off;
     mir.slots = (const Slot *)h_sl;
