@@ -133,7 +133,8 @@ rv_status device_fisher(rv_ctx *ctx, const int32_t *tables, int64_t n, double *p
     launch_fisher(ctx->d_ftab, n, dp, dp + n, ctx->stream, ctx->d_logfact);
     RV_CUDA(cudaGetLastError());
     RV_CUDA(cudaMemcpyAsync(hs + (size_t)n * 16, dp, (size_t)n * 8, cudaMemcpyDeviceToHost, ctx->stream));
-    RV_CUDA(cudaStreamSynchronize(ctx->stream));
+    RV_CUDA(cudaEventRecord(ctx->ev_block, ctx->stream));
+    RV_CUDA(cudaEventSynchronize(ctx->ev_block));
     memcpy(p2, hs + (size_t)n * 16, (size_t)n * 8);
     ctx->io_h2d += n * 16;
     ctx->io_d2h += n * 8;
@@ -248,6 +249,10 @@ rv_status rv_create(rv_ctx **out, const rv_params *p, int device, size_t hbm_bud
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
     for (int i = 0; e == cudaSuccess && i < 12; i++) e = cudaEventCreate(&ctx->ev[i]);
+    // a blocking-wait event for waits off the critical path (the record
+    // formatter's Fisher batch): the waiting thread sleeps instead of spinning
+    // on a core the host pool needs
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_block, cudaEventBlockingSync | cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc((void **)&ctx->d_counters, 64 * sizeof(unsigned int));
     if (e == cudaSuccess) e = cudaMalloc((void **)&ctx->d_logfact, (size_t)kLogFact * sizeof(double));
     if (e == cudaSuccess) {
@@ -311,6 +316,7 @@ void rv_destroy(rv_ctx *ctx) {
     if (ctx->h_fstage) cudaFreeHost(ctx->h_fstage);
     for (int i = 0; i < 12; i++)
         if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
+    if (ctx->ev_block) cudaEventDestroy(ctx->ev_block);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }

@@ -211,6 +211,7 @@ struct rv_ctx {
     // stage
     int stage = 0;  // 0 none, 1 submitted, 2 piled up, 3 realigned, 4 scored
     cudaEvent_t ev[12] = {};
+    cudaEvent_t ev_block = nullptr;  // blocking-sync event (waits off the critical path)
     double pileup_ms = 0, score_ms = 0, total_ms = 0;
     double stage_ms[8] = {};
     // pileup kernel autotuning: variant in use, per-variant best time seen
