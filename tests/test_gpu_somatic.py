@@ -51,6 +51,10 @@ def test_somatic_tiles_match_golden():
     gold = open(os.path.join(os.path.dirname(__file__), "golden", "somatic_mix.records.txt")).read().splitlines()
     mine = _run(g, t, n, [(1, g.shape[0])], fisher=1)
     assert diff_records(gold, mine, somatic=True) == []
+    # and through the VCF writer: the reference writer's VCF of its own records
+    from rabbitvar_gb300 import vcf
+    want = open(os.path.join(os.path.dirname(__file__), "golden", "somatic_mix.vcf")).read()
+    assert vcf.write("\n".join(mine) + "\n", "TUMOR") == want
     tiles = [(1 + 3000 * i, 3000 * (i + 1)) for i in range(10)]
     mine_t = _run(g, t, n, tiles, fisher=1)
     _, ora_t = O.run_somatic_regions(t, n, g, tiles, "T", O.default_params(local_realign=0, fisher=1))
