@@ -79,3 +79,42 @@ def diff_records(ra: list[str], rb: list[str], rel=2e-6, somatic: bool = False):
             problems.append(f"record {k} col {i}: {u} != {v}")
             break
     return problems
+
+
+def diff_vcf(va: str, vb: str, rel=2e-6):
+    """VCF texts: same header, same body lines in the same (CHROM, POS) order,
+    each line's fields equal or, where numeric with a decimal point, within
+    rel (plus one unit in the sixth decimal)."""
+    import re
+    ha = [l for l in va.splitlines() if l.startswith("#")]
+    hb = [l for l in vb.splitlines() if l.startswith("#")]
+    a = [l for l in va.splitlines() if l and not l.startswith("#")]
+    b = [l for l in vb.splitlines() if l and not l.startswith("#")]
+    problems = [] if ha == hb else ["headers differ"]
+    if len(a) != len(b):
+        return problems + [f"{len(a)} != {len(b)} body lines"]
+
+    def key(l):
+        f = l.split("\t")
+        return (f[0], int(f[1]), f[3], f[4], f[7].split(";")[0])
+    if [key(l)[:2] for l in a] != [key(l)[:2] for l in b]:
+        problems.append("line order differs")
+    A, B = {key(l): l for l in a}, {key(l): l for l in b}
+    if set(A) != set(B):
+        return problems + [f"line keys differ: {sorted(set(A) ^ set(B))[:5]}"]
+    for k in A:
+        ta, tb = re.split(r"[\t;:,=]", A[k]), re.split(r"[\t;:,=]", B[k])
+        if len(ta) != len(tb):
+            problems.append(f"{k}: field counts differ")
+            continue
+        for u, v in zip(ta, tb):
+            if u == v:
+                continue
+            try:
+                if "." in u and abs(float(u) - float(v)) <= rel * max(1.0, abs(float(u))) + 1.5e-6:
+                    continue
+            except ValueError:
+                pass
+            problems.append(f"{k}: {u} != {v}")
+            break
+    return problems

@@ -27,3 +27,21 @@ def test_vcf_learned_scores_and_threshold():
     assert 0 < len(body) < 55
     assert all(";RFV=" in l for l in body)
     assert all(float(l.split("RFV=")[1].split("\t")[0]) >= 0.5 for l in body)
+
+
+def test_diff_vcf_tolerates_last_digit_only():
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    from cmp import diff_vcf
+    want = open(os.path.join(GOLD, "somatic_mix.vcf")).read()
+    lines = want.splitlines()
+    i = next(j for j, l in enumerate(lines) if not l.startswith("#"))
+    f = lines[i].split("\t")
+    assert diff_vcf(want, want) == []
+    # one unit in the sixth decimal of AF is tolerated, a changed depth is not
+    af = f[7].split("AF=")[1].split(";")[0]
+    near = lines[:i] + [lines[i].replace(f"AF={af}", f"AF={float(af) + 1e-6:.6f}", 1)] + lines[i + 1:]
+    assert diff_vcf(want, "\n".join(near)) == []
+    dp = f[7].split("DP=")[1].split(";")[0]
+    far = lines[:i] + [lines[i].replace(f"DP={dp}", f"DP={int(dp) + 1}", 1)] + lines[i + 1:]
+    assert diff_vcf(want, "\n".join(far)) != []
