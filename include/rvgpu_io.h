@@ -26,6 +26,22 @@ rv_status rv_bam_contigs(const rv_bam *bam, int *n, const char *const **names, c
  * in pinned host memory owned by `bam` (valid until rv_bam_free). */
 rv_status rv_bam_batch(rv_bam *bam, int tid, rv_read_batch *out);
 
+/* BGZF/BAM decode on the GPU `device`: `bgzf` (n bytes of host memory,
+ * pinned for a fast upload) is a whole BAM file.  Each BGZF member is inflated
+ * by one device thread; record starts are found per member on the device and
+ * checked as one chain from the header's end; fixed fields and the NM tag are
+ * read per record on the device.  Same records, fields and layout as
+ * rv_bam_read; replaces htslib's BGZF reader and record iterator
+ * (src/recordPreprocessor.cpp:10-32,101-180).  RV_ERR_FORMAT on malformed
+ * input (the device decoder bounds every access and reports instead). */
+rv_status rv_bam_read_gpu(const uint8_t *bgzf, size_t n, int device, rv_bam **out);
+
+/* For a BAM from rv_bam_read_gpu, rv_bam_batch leaves `seq` and `qual` in
+ * device memory of that GPU (rv_submit_batch copies them device to device)
+ * and the other arrays in pinned host memory; rv_bam_batch_host returns every
+ * array in pinned host memory.  For a BAM from rv_bam_read both are the same. */
+rv_status rv_bam_batch_host(rv_bam *bam, int tid, rv_read_batch *out);
+
 void rv_bam_free(rv_bam *bam);
 
 /* Reads sequence `name` (NULL = first) of a FASTA file; *seq is malloc'd,

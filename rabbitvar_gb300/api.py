@@ -74,7 +74,7 @@ class SiteRecord(C.Structure):
 EXPORTS = ["rv_default_params", "rv_create", "rv_destroy", "rv_last_error", "rv_upload_reference",
            "rv_submit_batch", "rv_pileup", "rv_realign", "rv_score", "rv_format_records", "rv_fetch_records",
            "rv_call_regions", "rv_score_candidates", "rv_candidates", "rv_score_pair", "rv_pileup_realign_pair", "rv_format_somatic", "rv_call_somatic", "rv_call_somatic_stream", "rv_export_maps", "rv_last_timings", "rv_stage_times", "rv_io_bytes", "rv_fisher_batch", "rv_bam_read",
-           "rv_bam_contigs", "rv_bam_batch", "rv_bam_free", "rv_fasta_read", "rv_free", "rv_alloc_pinned",
+           "rv_bam_contigs", "rv_bam_batch", "rv_bam_read_gpu", "rv_bam_batch_host", "rv_bam_free", "rv_fasta_read", "rv_free", "rv_alloc_pinned",
            "rv_free_pinned", "rv_mlp_create", "rv_mlp_destroy", "rv_mlp_last_error", "rv_mlp_set_params",
            "rv_mlp_get_params", "rv_mlp_train", "rv_mlp_gradients", "rv_mlp_predict", "rv_mlp_step_ms"]
 
@@ -120,6 +120,8 @@ def lib():
     L.rv_bam_read.argtypes = [C.c_char_p, C.c_int, C.POINTER(vp)]
     L.rv_bam_contigs.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(vp), C.POINTER(vp)]
     L.rv_bam_batch.argtypes = [vp, C.c_int, C.POINTER(ReadBatch)]
+    L.rv_bam_read_gpu.argtypes = [vp, sz, C.c_int, C.POINTER(vp)]
+    L.rv_bam_batch_host.argtypes = [vp, C.c_int, C.POINTER(ReadBatch)]
     L.rv_bam_free.argtypes = [vp]
     L.rv_fasta_read.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(vp), C.POINTER(i64)]
     L.rv_free.argtypes = [vp]
@@ -406,6 +408,37 @@ class SomaticStream:
         return out
 
 
+def _host_batches(L, h, batch_fn):
+    n = C.c_int()
+    names = C.c_void_p()
+    lens = C.c_void_p()
+    L.rv_bam_contigs(h, C.byref(n), C.byref(names), C.byref(lens))
+    nm = [C.cast(names, C.POINTER(C.c_char_p))[i].decode() for i in range(n.value)]
+    ln = [C.cast(lens, C.POINTER(C.c_int32))[i] for i in range(n.value)]
+    out = {}
+    for tid in range(n.value):
+        rb = ReadBatch()
+        st = batch_fn(h, tid, C.byref(rb))
+        if st != 0:
+            raise RvError(st, "rv_bam_batch")
+        nr = rb.n_reads
+
+        def arr(ptr, dt, count):
+            if count == 0:
+                return np.zeros(0, dt)
+            return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(np.ctypeslib.as_ctypes_type(dt))),
+                                         shape=(count,)).copy()
+        arrays = dict(pos=arr(rb.pos, np.int32, nr), flag=arr(rb.flag, np.uint16, nr),
+                      mapq=arr(rb.mapq, np.uint8, nr), mpos=arr(rb.mpos, np.int32, nr),
+                      nm=arr(rb.nm, np.int32, nr), n_cigar=arr(rb.n_cigar, np.uint16, nr),
+                      cig_off=arr(rb.cig_off, np.uint32, nr), cigar=arr(rb.cigar, np.uint32, rb.n_cigar_words),
+                      l_qseq=arr(rb.l_qseq, np.int32, nr), base_off=arr(rb.base_off, np.uint64, nr),
+                      seq=arr(rb.seq, np.uint8, (rb.n_bases + 1) // 2), qual=arr(rb.qual, np.uint8, rb.n_bases),
+                      n_bases=rb.n_bases)
+        out[tid] = Batch(arrays)
+    return nm, ln, out
+
+
 def read_bam(path: str, threads: int = 0):
     """Decode a BAM file with the library's host decoder; returns
     (contig names, lengths, {tid: Batch}) with copies of the arrays."""
@@ -415,36 +448,68 @@ def read_bam(path: str, threads: int = 0):
     if st != 0:
         raise RvError(st, f"cannot decode {path}")
     try:
+        return _host_batches(L, h, L.rv_bam_batch)
+    finally:
+        L.rv_bam_free(h)
+
+
+class DeviceBatch:
+    """A read batch of a BAM decoded on the GPU: bases and qualities in device
+    memory, the other arrays in pinned host memory (owned by the DeviceBam)."""
+
+    def __init__(self, owner: "DeviceBam", rb: ReadBatch):
+        self._owner = owner
+        self._rb = rb
+        self.n_reads = int(rb.n_reads)
+        self.n_bases = int(rb.n_bases)
+        self.nbytes = 0
+
+    def struct(self) -> ReadBatch:
+        return self._rb
+
+
+class DeviceBam:
+    """BGZF/BAM decode on the GPU (rv_bam_read_gpu) of a file's bytes."""
+
+    def __init__(self, data: bytes | str, device: int = 0):
+        self.L = lib()
+        if isinstance(data, str):
+            with open(data, "rb") as f:
+                data = f.read()
+        self.compressed_bytes = len(data)
+        ptr = self.L.rv_alloc_pinned(max(len(data), 1))
+        if not ptr:
+            raise RvError(-2, "pinned allocation failed")
+        try:
+            C.memmove(ptr, data, len(data))
+            self.h = C.c_void_p()
+            st = self.L.rv_bam_read_gpu(ptr, len(data), device, C.byref(self.h))
+        finally:
+            self.L.rv_free_pinned(ptr)
+        if st != 0:
+            raise RvError(st, "rv_bam_read_gpu")
         n = C.c_int()
         names = C.c_void_p()
         lens = C.c_void_p()
-        L.rv_bam_contigs(h, C.byref(n), C.byref(names), C.byref(lens))
-        nm = [C.cast(names, C.POINTER(C.c_char_p))[i].decode() for i in range(n.value)]
-        ln = [C.cast(lens, C.POINTER(C.c_int32))[i] for i in range(n.value)]
-        out = {}
-        for tid in range(n.value):
-            rb = ReadBatch()
-            st = L.rv_bam_batch(h, tid, C.byref(rb))
-            if st != 0:
-                raise RvError(st, "rv_bam_batch")
-            nr = rb.n_reads
+        self.L.rv_bam_contigs(self.h, C.byref(n), C.byref(names), C.byref(lens))
+        self.names = [C.cast(names, C.POINTER(C.c_char_p))[i].decode() for i in range(n.value)]
+        self.lens = [C.cast(lens, C.POINTER(C.c_int32))[i] for i in range(n.value)]
 
-            def arr(ptr, dt, count):
-                if count == 0:
-                    return np.zeros(0, dt)
-                return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(np.ctypeslib.as_ctypes_type(dt))),
-                                             shape=(count,)).copy()
-            arrays = dict(pos=arr(rb.pos, np.int32, nr), flag=arr(rb.flag, np.uint16, nr),
-                          mapq=arr(rb.mapq, np.uint8, nr), mpos=arr(rb.mpos, np.int32, nr),
-                          nm=arr(rb.nm, np.int32, nr), n_cigar=arr(rb.n_cigar, np.uint16, nr),
-                          cig_off=arr(rb.cig_off, np.uint32, nr), cigar=arr(rb.cigar, np.uint32, rb.n_cigar_words),
-                          l_qseq=arr(rb.l_qseq, np.int32, nr), base_off=arr(rb.base_off, np.uint64, nr),
-                          seq=arr(rb.seq, np.uint8, (rb.n_bases + 1) // 2), qual=arr(rb.qual, np.uint8, rb.n_bases),
-                          n_bases=rb.n_bases)
-            out[tid] = Batch(arrays)
-        return nm, ln, out
-    finally:
-        L.rv_bam_free(h)
+    def batch(self, tid: int = 0) -> DeviceBatch:
+        rb = ReadBatch()
+        st = self.L.rv_bam_batch(self.h, tid, C.byref(rb))
+        if st != 0:
+            raise RvError(st, "rv_bam_batch")
+        return DeviceBatch(self, rb)
+
+    def host_batches(self):
+        """(names, lengths, {tid: Batch}) with host copies of every array."""
+        return _host_batches(self.L, self.h, self.L.rv_bam_batch_host)
+
+    def close(self):
+        if self.h:
+            self.L.rv_bam_free(self.h)
+            self.h = C.c_void_p()
 
 
 def read_fasta(path: str, name: str | None = None) -> bytes:

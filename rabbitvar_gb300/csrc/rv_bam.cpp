@@ -17,6 +17,7 @@
 #include <thread>
 #include <vector>
 
+#include "rv_bam_internal.h"
 #include "rvgpu_io.h"
 
 namespace {
@@ -230,16 +231,61 @@ T *pinned(size_t n, std::vector<void *> &owned) {
 
 }  // namespace
 
-struct rv_bam {
-    std::vector<std::string> names;
-    std::vector<int32_t> lens;
-    std::vector<const char *> name_ptrs;
-    std::vector<uint8_t> data;        // inflated BAM stream
-    std::vector<size_t> rec_off;      // record offsets (block_size field)
-    std::vector<int32_t> rec_tid;
-    std::vector<void *> owned;        // batch buffers
-    std::string err;
-};
+bool bgzf_members(const uint8_t *raw, size_t n, std::vector<BgzfMember> &out, uint64_t &total) {
+    out.clear();
+    size_t p = 0;
+    total = 0;
+    while (p + 18 <= n) {
+        const uint8_t *h = raw + p;
+        if (h[0] != 31 || h[1] != 139 || h[2] != 8 || !(h[3] & 4)) return false;
+        uint16_t xlen = rd16(h + 10);
+        int bsize = -1;
+        for (size_t q = 12; q + 4 <= 12u + xlen && p + q + 4 <= n;) {
+            uint16_t slen = rd16(h + q + 2);
+            if (h[q] == 'B' && h[q + 1] == 'C' && slen == 2 && p + q + 6 <= n) bsize = rd16(h + q + 4);
+            q += 4 + slen;
+        }
+        if (bsize < 0) return false;
+        size_t blen = (size_t)bsize + 1;
+        if (p + blen > n || blen < 12u + xlen + 8) return false;
+        BgzfMember m;
+        m.in_off = p + 12 + xlen;
+        m.in_len = (uint32_t)(blen - 12 - xlen - 8);
+        m.out_len = rd32(h + blen - 4);
+        if (m.out_len > 65536) return false;
+        m.out_off = total;
+        total += m.out_len;
+        out.push_back(m);
+        p += blen;
+    }
+    return p == n;
+}
+
+int64_t bam_parse_header(const uint8_t *d, uint64_t n, uint64_t total, rv_bam *bam) {
+    bam->names.clear();
+    bam->lens.clear();
+    auto need = [&](uint64_t k) { return k <= n ? 1 : (k <= total ? 0 : -1); };
+    int r;
+    if ((r = need(8)) <= 0) return r;
+    if (memcmp(d, "BAM\1", 4) != 0) return -1;
+    uint64_t q = 8 + (uint64_t)rd32(d + 4);
+    if ((r = need(q + 4)) <= 0) return r;
+    uint32_t n_ref = rd32(d + q);
+    q += 4;
+    for (uint32_t i = 0; i < n_ref; i++) {
+        if ((r = need(q + 4)) <= 0) return r;
+        uint32_t ln = rd32(d + q);
+        q += 4;
+        if ((r = need(q + ln + 4)) <= 0) return r;
+        bam->names.emplace_back((const char *)d + q, strnlen((const char *)d + q, ln));
+        q += ln;
+        bam->lens.push_back((int32_t)rd32(d + q));
+        q += 4;
+    }
+    bam->name_ptrs.clear();
+    for (auto &s : bam->names) bam->name_ptrs.push_back(s.c_str());
+    return (int64_t)q;
+}
 
 extern "C" {
 
@@ -255,33 +301,9 @@ rv_status rv_bam_read(const char *path, int threads, rv_bam **out) {
     size_t got = sz > 0 ? fread(raw.data(), 1, raw.size(), f) : 0;
     fclose(f);
     if (got != raw.size()) return RV_ERR_FORMAT;
-    // BGZF members: gzip header with a BC extra subfield holding the member size
-    struct Blk { size_t in_off, in_len, out_off; uint32_t out_len; };
-    std::vector<Blk> blks;
-    size_t p = 0, total = 0;
-    while (p + 18 <= raw.size()) {
-        const uint8_t *h = raw.data() + p;
-        if (h[0] != 31 || h[1] != 139 || h[2] != 8 || !(h[3] & 4)) return RV_ERR_FORMAT;
-        uint16_t xlen = rd16(h + 10);
-        int bsize = -1;
-        for (size_t q = 12; q + 4 <= 12u + xlen;) {
-            uint16_t slen = rd16(h + q + 2);
-            if (h[q] == 'B' && h[q + 1] == 'C' && slen == 2) bsize = rd16(h + q + 4);
-            q += 4 + slen;
-        }
-        if (bsize < 0) return RV_ERR_FORMAT;
-        size_t blen = (size_t)bsize + 1;
-        if (p + blen > raw.size() || blen < 12u + xlen + 8) return RV_ERR_FORMAT;
-        Blk b;
-        b.in_off = p + 12 + xlen;
-        b.in_len = blen - 12 - xlen - 8;
-        b.out_len = rd32(h + blen - 4);
-        b.out_off = total;
-        total += b.out_len;
-        blks.push_back(b);
-        p += blen;
-    }
-    if (p != raw.size()) return RV_ERR_FORMAT;
+    std::vector<BgzfMember> blks;
+    uint64_t total = 0;
+    if (!bgzf_members(raw.data(), raw.size(), blks, total)) return RV_ERR_FORMAT;
     rv_bam *bam = new rv_bam();
     bam->data.resize(total + 8);
     std::atomic<size_t> next{0};
@@ -292,7 +314,7 @@ rv_status rv_bam_read(const char *path, int threads, rv_bam **out) {
         for (;;) {
             size_t i = next.fetch_add(1);
             if (i >= blks.size()) break;
-            const Blk &b = blks[i];
+            const BgzfMember &b = blks[i];
             size_t produced = 0;
             if (b.out_len && (!inflate_raw(raw.data() + b.in_off, b.in_len, bam->data.data() + b.out_off, b.out_len,
                                            produced) ||
@@ -306,23 +328,9 @@ rv_status rv_bam_read(const char *path, int threads, rv_bam **out) {
     for (auto &t : pool) t.join();
     if (bad.load()) { delete bam; return RV_ERR_FORMAT; }
     const std::vector<uint8_t> &d = bam->data;
-    if (total < 12 || memcmp(d.data(), "BAM\1", 4) != 0) { delete bam; return RV_ERR_FORMAT; }
-    size_t q = 4;
-    uint32_t l_text = rd32(&d[q]);
-    q += 4 + l_text;
-    if (q + 4 > total) { delete bam; return RV_ERR_FORMAT; }
-    uint32_t n_ref = rd32(&d[q]);
-    q += 4;
-    for (uint32_t i = 0; i < n_ref; i++) {
-        if (q + 4 > total) { delete bam; return RV_ERR_FORMAT; }
-        uint32_t ln = rd32(&d[q]);
-        q += 4;
-        if (q + ln + 4 > total) { delete bam; return RV_ERR_FORMAT; }
-        bam->names.emplace_back((const char *)&d[q]);
-        q += ln;
-        bam->lens.push_back((int32_t)rd32(&d[q]));
-        q += 4;
-    }
+    const int64_t hdr = bam_parse_header(d.data(), total, total, bam);
+    if (hdr <= 0) { delete bam; return RV_ERR_FORMAT; }
+    size_t q = (size_t)hdr;
     while (q + 4 <= total) {
         uint32_t bs = rd32(&d[q]);
         if (bs < 32 || q + 4 + bs > total) { delete bam; return RV_ERR_FORMAT; }
@@ -330,7 +338,6 @@ rv_status rv_bam_read(const char *path, int threads, rv_bam **out) {
         bam->rec_tid.push_back((int32_t)rd32(&d[q + 4]));
         q += 4 + bs;
     }
-    for (auto &s : bam->names) bam->name_ptrs.push_back(s.c_str());
     *out = bam;
     return RV_OK;
 }
@@ -345,6 +352,7 @@ rv_status rv_bam_contigs(const rv_bam *bam, int *n, const char *const **names, c
 
 rv_status rv_bam_batch(rv_bam *bam, int tid, rv_read_batch *out) {
     if (!bam || !out) return RV_ERR_ARG;
+    if (bam->gpu) return bam_gpu_batch(bam, tid, out, false);
     const std::vector<uint8_t> &d = bam->data;
     std::vector<size_t> sel;
     int64_t ncig = 0, nb = 0;
@@ -439,8 +447,15 @@ rv_status rv_bam_batch(rv_bam *bam, int tid, rv_read_batch *out) {
     return RV_OK;
 }
 
+rv_status rv_bam_batch_host(rv_bam *bam, int tid, rv_read_batch *out) {
+    if (!bam || !out) return RV_ERR_ARG;
+    if (bam->gpu) return bam_gpu_batch(bam, tid, out, true);
+    return rv_bam_batch(bam, tid, out);
+}
+
 void rv_bam_free(rv_bam *bam) {
     if (!bam) return;
+    if (bam->gpu) bam_gpu_free(bam->gpu);
     for (void *p : bam->owned) {
         if ((uintptr_t)p & 1) free((void *)((uintptr_t)p & ~(uintptr_t)1));
         else cudaFreeHost(p);

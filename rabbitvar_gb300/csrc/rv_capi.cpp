@@ -418,7 +418,14 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
         (st = grow(ctx, ctx->d_seq, cb2, (size_t)std::max<int64_t>(b->n_bases, 32) / 2 + 64)))
         return st;
     ctx->cap_bases = cb;
-    ctx->io_h2d = n * (4 + 4 + 4 + 4 + 2 + 2 + 1 + 4 + 8) + b->n_cigar_words * 4 + (b->n_bases + 1) / 2 + b->n_bases;
+    ctx->io_h2d = n * (4 + 4 + 4 + 4 + 2 + 2 + 1 + 4 + 8) + b->n_cigar_words * 4;
+    {
+        cudaPointerAttributes pa;
+        const bool dev_bases = n > 0 && cudaPointerGetAttributes(&pa, b->qual) == cudaSuccess &&
+                               pa.type == cudaMemoryTypeDevice;
+        cudaGetLastError();
+        if (!dev_bases) ctx->io_h2d += (b->n_bases + 1) / 2 + b->n_bases;
+    }
     ctx->io_d2h = 0;
     tm.lap("prep+alloc");
     // -k 1: the alignment spans stay on the host for noPassingReads
@@ -661,8 +668,11 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
         RV_CUDA(cudaMemcpyAsync(ctx->d_cigoff, b->cig_off, n * 4, cudaMemcpyHostToDevice, s));
         RV_CUDA(cudaMemcpyAsync(ctx->d_boff, b->base_off, n * 8, cudaMemcpyHostToDevice, s));
         RV_CUDA(cudaMemcpyAsync(ctx->d_cigar, b->cigar, b->n_cigar_words * 4, cudaMemcpyHostToDevice, s));
-        RV_CUDA(cudaMemcpyAsync(ctx->d_seq, b->seq, (size_t)(b->n_bases + 1) / 2, cudaMemcpyHostToDevice, s));
-        RV_CUDA(cudaMemcpyAsync(ctx->d_qual, b->qual, (size_t)b->n_bases, cudaMemcpyHostToDevice, s));
+        // bases and qualities may already be on the device (a batch of a
+        // BAM decoded there, rv_bam_read_gpu): the copy direction follows
+        // the pointers
+        RV_CUDA(cudaMemcpyAsync(ctx->d_seq, b->seq, (size_t)(b->n_bases + 1) / 2, cudaMemcpyDefault, s));
+        RV_CUDA(cudaMemcpyAsync(ctx->d_qual, b->qual, (size_t)b->n_bases, cudaMemcpyDefault, s));
     }
     tm.lap("queue copies");
     ctx->stage = 1;

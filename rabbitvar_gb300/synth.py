@@ -443,35 +443,82 @@ def _reg2bin(beg: int, end: int) -> int:
     return 0
 
 
+def _segments(dst_start: np.ndarray, src_start: np.ndarray, length: np.ndarray):
+    """Flat (destination, source) byte indices of variable-length segments."""
+    length = length.astype(np.int64)
+    tot = int(length.sum())
+    within = np.arange(tot, dtype=np.int64) - np.repeat(np.cumsum(length) - length, length)
+    return np.repeat(dst_start.astype(np.int64), length) + within, np.repeat(src_start.astype(np.int64), length) + within
+
+
 def bam_bytes(rs: ReadSet, sample: str = "S") -> bytes:
+    """Uncompressed BAM stream of a read set (records built with numpy)."""
     text = f"@HD\tVN:1.6\tSO:coordinate\n@SQ\tSN:{rs.contig}\tLN:{rs.contig_len}\n@RG\tID:{sample}\tSM:{sample}\n".encode()
-    out = [b"BAM\x01", struct.pack("<I", len(text)), text, struct.pack("<I", 1),
-           struct.pack("<I", len(rs.contig) + 1), rs.contig.encode() + b"\x00",
-           struct.pack("<I", rs.contig_len)]
+    head = b"".join([b"BAM\x01", struct.pack("<I", len(text)), text, struct.pack("<I", 1),
+                     struct.pack("<I", len(rs.contig) + 1), rs.contig.encode() + b"\x00",
+                     struct.pack("<I", rs.contig_len)])
+    n = rs.n
+    if n == 0:
+        return head
+    names = np.frombuffer(b"".join(b"r%d\x00" % int(x) for x in rs.name_id), np.uint8)
+    l_name = np.char.str_len(np.char.mod("r%d", rs.name_id.astype(np.int64))).astype(np.int64) + 1
+    nc = rs.n_cigar.astype(np.int64)
+    L = rs.l_qseq.astype(np.int64)
+    bo = rs.base_off.astype(np.int64)
+    co = rs.cig_off.astype(np.int64)
+    # reference span for the bin
+    words = rs.cigar.astype(np.int64)
+    consumes = np.isin(words & 15, (0, 2, 3, 7, 8))
+    span_w = np.where(consumes, words >> 4, 0)
+    csum = np.concatenate([[0], np.cumsum(span_w)])
+    ref_len = csum[co + nc] - csum[co]
+    p = rs.pos.astype(np.int64)
+    end = p + np.maximum(ref_len, 1) - 1
+    bins = np.zeros(n, np.int64)
+    done = np.zeros(n, bool)
+    for shift, off in ((14, ((1 << 15) - 1) // 7), (17, ((1 << 12) - 1) // 7), (20, ((1 << 9) - 1) // 7),
+                       (23, ((1 << 6) - 1) // 7), (26, ((1 << 3) - 1) // 7)):
+        hit = ~done & ((p >> shift) == (end >> shift))
+        bins[hit] = off + (p[hit] >> shift)
+        done |= hit
+    rec_len = 32 + l_name + 4 * nc + (L + 1) // 2 + L + 7
+    start = np.concatenate([[0], np.cumsum(rec_len + 4)[:-1]])
+    buf = np.zeros(int((rec_len + 4).sum()), np.uint8)
+    fixed = np.zeros(n, dtype=np.dtype([("bs", "<u4"), ("tid", "<i4"), ("pos", "<i4"), ("lrn", "u1"), ("mapq", "u1"),
+                                        ("bin", "<u2"), ("nc", "<u2"), ("flag", "<u2"), ("lq", "<i4"),
+                                        ("ntid", "<i4"), ("npos", "<i4"), ("tlen", "<i4")]))
+    fixed["bs"] = rec_len
+    fixed["pos"] = p
+    fixed["lrn"] = l_name
+    fixed["mapq"] = rs.mapq
+    fixed["bin"] = bins
+    fixed["nc"] = nc
+    fixed["flag"] = rs.flag
+    fixed["lq"] = L
+    fixed["npos"] = rs.mpos
+    fixed["tlen"] = rs.isize
+    fb = fixed.view(np.uint8).reshape(n, 36)
+    buf[(start[:, None] + np.arange(36)[None, :]).ravel()] = fb.ravel()
+    at = start + 36
+    d, sidx = _segments(at, np.concatenate([[0], np.cumsum(l_name)[:-1]]), l_name)
+    buf[d] = names[sidx]
+    at = at + l_name
+    cb = rs.cigar.astype("<u4").view(np.uint8)
+    d, sidx = _segments(at, 4 * co, 4 * nc)
+    buf[d] = cb[sidx]
+    at = at + 4 * nc
     packed = rs.packed_seq()
-    cig = rs.cigar
-    for i in range(rs.n):
-        name = b"r%d\x00" % int(rs.name_id[i])
-        nc = int(rs.n_cigar[i])
-        co = int(rs.cig_off[i])
-        words = cig[co:co + nc]
-        L = int(rs.l_qseq[i])
-        bo = int(rs.base_off[i])
-        ref_len = 0
-        for w in words.tolist():
-            if (w & 15) in (0, 2, 3, 7, 8):
-                ref_len += w >> 4
-        p = int(rs.pos[i])
-        b = _reg2bin(p, p + max(ref_len, 1))
-        seqb = packed[bo // 2: bo // 2 + (L + 1) // 2].tobytes()
-        qb = rs.qual[bo:bo + L].tobytes()
-        aux = b"NMi" + struct.pack("<i", int(rs.nm[i]))
-        body = struct.pack("<iiBBHHHiiii", 0, p, len(name), int(rs.mapq[i]), b, nc,
-                           int(rs.flag[i]), L, 0, int(rs.mpos[i]), int(rs.isize[i]))
-        rec = body + name + words.astype("<u4").tobytes() + seqb + qb + aux
-        out.append(struct.pack("<I", len(rec)))
-        out.append(rec)
-    return b"".join(out)
+    d, sidx = _segments(at, bo // 2, (L + 1) // 2)
+    buf[d] = packed[sidx]
+    at = at + (L + 1) // 2
+    d, sidx = _segments(at, bo, L)
+    buf[d] = rs.qual[sidx]
+    at = at + L
+    aux = np.zeros(n, dtype=np.dtype([("t", "S3"), ("v", "<i4")]))
+    aux["t"] = b"NMi"
+    aux["v"] = rs.nm
+    buf[(at[:, None] + np.arange(7)[None, :]).ravel()] = aux.view(np.uint8).reshape(n, 7).ravel()
+    return head + buf.tobytes()
 
 
 def write_bam(path: str, rs: ReadSet, sample: str = "S") -> None:
