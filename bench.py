@@ -217,6 +217,97 @@ def other_k_leg(g, tumor, normal, regions, k: int, steps: int, warmup: int, devi
             "records_per_step": recs, "steps": steps, "warmup": warmup}
 
 
+def bgzf_bytes(payload: bytes, level: int = 1) -> bytes:
+    """BGZF members (zlib level 1, 0xFF00 bytes of stream each) + EOF member."""
+    import struct
+    import zlib
+    from rabbitvar_gb300 import synth
+    parts = []
+    for i in range(0, len(payload), 0xFF00):
+        d = payload[i:i + 0xFF00]
+        co = zlib.compressobj(level, zlib.DEFLATED, -15)
+        c = co.compress(d) + co.flush()
+        parts.append(struct.pack("<BBBBIBBHBBHH", 31, 139, 8, 4, 0, 0, 255, 6, 66, 67, 2, len(c) + 25) + c +
+                     struct.pack("<II", zlib.crc32(d) & 0xFFFFFFFF, len(d)))
+    return b"".join(parts) + synth._BGZF_EOF
+
+
+def bam_leg(g, tumor, normal, regions, k: int, steps: int, warmup: int, device: int, want_text: str) -> dict:
+    """End to end from BGZF-compressed BAM bytes in pinned host memory: each
+    step decodes both samples on the GPU (rv_bam_reread_gpu into reused
+    buffers, contig batches as windows of the decoded layout) and calls the
+    pair on those batches; beside it the same step with the library's host
+    decoder (all host threads) feeding pinned host batches."""
+    import ctypes as C
+    from rabbitvar_gb300 import api, synth
+    L = api.lib()
+    data = [bgzf_bytes(synth.bam_bytes(rs, name)) for rs, name in ((tumor, "T"), (normal, "N"))]
+    ptrs = []
+    for d in data:
+        p = L.rv_alloc_pinned(len(d))
+        C.memmove(p, d, len(d))
+        ptrs.append(p)
+    n_reads = tumor.n + normal.n
+    pair = api.SomaticPair(api.default_params(local_realign=k, fisher=1), device=device)
+    pair.upload_reference(tumor.contig, synth.genome_str(g).encode())
+    dbams = [api.DeviceBam(d, device) for d in data]
+    dec_ms = []
+
+    def gpu_step():
+        t = time.perf_counter()
+        for db, d, p in zip(dbams, data, ptrs):
+            db.reread(d, pinned_ptr=p)
+        bt, bn = dbams[0].batch(0), dbams[1].batch(0)
+        dec_ms.append((time.perf_counter() - t) * 1e3)
+        return pair.call(bt, bn, regions, "T", "ctg")
+
+    for _ in range(max(1, warmup)):
+        gpu_step()
+    dec_ms.clear()
+    t0 = time.perf_counter()
+    texts = [gpu_step() for _ in range(steps)]
+    gpu_dt = time.perf_counter() - t0
+    host_dec = []
+
+    def host_step():
+        t = time.perf_counter()
+        hs, bs = [], []
+        for d, p in zip(data, ptrs):
+            h = C.c_void_p()
+            st = L.rv_bam_read_mem(p, len(d), 0, C.byref(h))
+            if st != 0:
+                raise api.RvError(st, "rv_bam_read_mem")
+            rb = api.ReadBatch()
+            L.rv_bam_batch(h, 0, C.byref(rb))
+            hs.append(h)
+            bs.append(type("HostBatch", (), {"struct": lambda self, rb=rb: rb, "n_reads": rb.n_reads})())
+        host_dec.append((time.perf_counter() - t) * 1e3)
+        text = pair.call(bs[0], bs[1], regions, "T", "ctg")
+        for h in hs:
+            L.rv_bam_free(h)
+        return text
+
+    host_step()
+    host_dec.clear()
+    host_steps = max(1, min(steps, 3))
+    t0 = time.perf_counter()
+    htexts = [host_step() for _ in range(host_steps)]
+    host_dt = time.perf_counter() - t0
+    for db in dbams:
+        db.close()
+    pair.close()
+    for p in ptrs:
+        L.rv_free_pinned(p)
+    same = all(t == want_text for t in texts + htexts)
+    return {"value": n_reads * steps / gpu_dt, "unit": "reads/s", "steps": steps,
+            "bgzf_bytes_per_step": sum(len(d) for d in data),
+            "decode_ms_per_step": statistics.mean(dec_ms),
+            "host_decoder": {"value": n_reads * host_steps / host_dt, "unit": "reads/s", "steps": host_steps,
+                             "decode_ms_per_step": statistics.mean(host_dec), "threads": os.cpu_count()},
+            "records_equal_to_batch_path": same,
+            "note": "BGZF level-1 members of the synthetic BAMs in pinned host memory; decode + pileup + scoring + records"}
+
+
 def learned_filter_leg():
     """The learned filter against the hard filter on the deep-panel shape:
     trained on 4 seeded panels, evaluated on 2 held-out ones (planted truth),
@@ -336,6 +427,7 @@ def main():
     ap.add_argument("--local-realign", "-k", type=int, default=1, choices=[0, 1],
                     help="the reference's -k (default 1, as the reference): 0 leaves out the realigner's indel passes")
     ap.add_argument("--no-other-k", action="store_true", help="skip the leg with the other -k setting")
+    ap.add_argument("--no-bam", action="store_true", help="skip the leg that starts from BGZF-compressed BAM bytes")
     ap.add_argument("--panel", type=int, default=0, metavar="N",
                     help="batched amplicon panel of N regions (-t -u): one launch for all regions vs one per region")
     args = ap.parse_args()
@@ -469,6 +561,9 @@ def main():
     score_ms = statistics.mean(s["score"] for s in stages)
     out["sites_per_s"] = (sum(r[1] - r[0] + 1 for r in regions)) / (score_ms * 1e-3)
     pair.close()
+    if rank == 0 and not args.no_bam:
+        out["e2e_from_bam"] = bam_leg(g, tumor, normal, regions, args.local_realign, args.steps, args.warmup, local,
+                                      e2e_texts[0])
     if rank == 0 and not args.no_other_k:
         out["other_k"] = other_k_leg(g, tumor, normal, regions, 1 - args.local_realign, args.steps,
                                      args.warmup, local)

@@ -19,6 +19,9 @@ typedef struct rv_bam rv_bam;
  * sam_hdr_read + the record iterator (src/recordPreprocessor.cpp:10-32). */
 rv_status rv_bam_read(const char *path, int threads, rv_bam **out);
 
+/* rv_bam_read on a BGZF/BAM file already in memory (n bytes at bgzf). */
+rv_status rv_bam_read_mem(const uint8_t *bgzf, size_t n, int threads, rv_bam **out);
+
 /* Reference sequences named in the BAM header (bam_hdr_t target_name/len). */
 rv_status rv_bam_contigs(const rv_bam *bam, int *n, const char *const **names, const int32_t **lens);
 
@@ -35,6 +38,11 @@ rv_status rv_bam_batch(rv_bam *bam, int tid, rv_read_batch *out);
  * (src/recordPreprocessor.cpp:10-32,101-180).  RV_ERR_FORMAT on malformed
  * input (the device decoder bounds every access and reports instead). */
 rv_status rv_bam_read_gpu(const uint8_t *bgzf, size_t n, int device, rv_bam **out);
+
+/* Decodes another BGZF/BAM file into a handle from rv_bam_read_gpu, reusing
+ * its device and pinned buffers (they only grow); batches taken from the
+ * handle before are invalid afterwards. */
+rv_status rv_bam_reread_gpu(rv_bam *bam, const uint8_t *bgzf, size_t n);
 
 /* For a BAM from rv_bam_read_gpu, rv_bam_batch leaves `seq` and `qual` in
  * device memory of that GPU (rv_submit_batch copies them device to device)

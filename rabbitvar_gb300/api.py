@@ -74,7 +74,7 @@ class SiteRecord(C.Structure):
 EXPORTS = ["rv_default_params", "rv_create", "rv_destroy", "rv_last_error", "rv_upload_reference",
            "rv_submit_batch", "rv_pileup", "rv_realign", "rv_score", "rv_format_records", "rv_fetch_records",
            "rv_call_regions", "rv_score_candidates", "rv_candidates", "rv_score_pair", "rv_pileup_realign_pair", "rv_format_somatic", "rv_call_somatic", "rv_call_somatic_stream", "rv_export_maps", "rv_last_timings", "rv_stage_times", "rv_io_bytes", "rv_fisher_batch", "rv_bam_read",
-           "rv_bam_contigs", "rv_bam_batch", "rv_bam_read_gpu", "rv_bam_batch_host", "rv_bam_free", "rv_fasta_read", "rv_free", "rv_alloc_pinned",
+           "rv_bam_contigs", "rv_bam_batch", "rv_bam_read_mem", "rv_bam_read_gpu", "rv_bam_reread_gpu", "rv_bam_batch_host", "rv_bam_free", "rv_fasta_read", "rv_free", "rv_alloc_pinned",
            "rv_free_pinned", "rv_mlp_create", "rv_mlp_destroy", "rv_mlp_last_error", "rv_mlp_set_params",
            "rv_mlp_get_params", "rv_mlp_train", "rv_mlp_gradients", "rv_mlp_predict", "rv_mlp_step_ms"]
 
@@ -122,6 +122,8 @@ def lib():
     L.rv_bam_batch.argtypes = [vp, C.c_int, C.POINTER(ReadBatch)]
     L.rv_bam_read_gpu.argtypes = [vp, sz, C.c_int, C.POINTER(vp)]
     L.rv_bam_batch_host.argtypes = [vp, C.c_int, C.POINTER(ReadBatch)]
+    L.rv_bam_reread_gpu.argtypes = [vp, vp, sz]
+    L.rv_bam_read_mem.argtypes = [vp, sz, C.c_int, C.POINTER(vp)]
     L.rv_bam_free.argtypes = [vp]
     L.rv_fasta_read.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(vp), C.POINTER(i64)]
     L.rv_free.argtypes = [vp]
@@ -494,6 +496,23 @@ class DeviceBam:
         self.L.rv_bam_contigs(self.h, C.byref(n), C.byref(names), C.byref(lens))
         self.names = [C.cast(names, C.POINTER(C.c_char_p))[i].decode() for i in range(n.value)]
         self.lens = [C.cast(lens, C.POINTER(C.c_int32))[i] for i in range(n.value)]
+
+    def reread(self, data: bytes, pinned_ptr: int | None = None):
+        """Decode another file into this handle's buffers (earlier batches
+        become invalid); `pinned_ptr` may point at a pinned copy of `data`."""
+        ptr = pinned_ptr
+        if ptr is None:
+            ptr = self.L.rv_alloc_pinned(max(len(data), 1))
+            if not ptr:
+                raise RvError(-2, "pinned allocation failed")
+            C.memmove(ptr, data, len(data))
+        try:
+            st = self.L.rv_bam_reread_gpu(self.h, ptr, len(data))
+        finally:
+            if pinned_ptr is None:
+                self.L.rv_free_pinned(ptr)
+        if st != 0:
+            raise RvError(st, "rv_bam_reread_gpu")
 
     def batch(self, tid: int = 0) -> DeviceBatch:
         rb = ReadBatch()

@@ -301,6 +301,18 @@ rv_status rv_bam_read(const char *path, int threads, rv_bam **out) {
     size_t got = sz > 0 ? fread(raw.data(), 1, raw.size(), f) : 0;
     fclose(f);
     if (got != raw.size()) return RV_ERR_FORMAT;
+    return rv_bam_read_mem(raw.data(), raw.size(), threads, out);
+}
+
+rv_status rv_bam_read_mem(const uint8_t *bgzf, size_t n, int threads, rv_bam **out) {
+    if (!bgzf || !out) return RV_ERR_ARG;
+    *out = nullptr;
+    struct {
+        const uint8_t *p;
+        size_t n;
+        const uint8_t *data() const { return p; }
+        size_t size() const { return n; }
+    } raw{bgzf, n};
     std::vector<BgzfMember> blks;
     uint64_t total = 0;
     if (!bgzf_members(raw.data(), raw.size(), blks, total)) return RV_ERR_FORMAT;

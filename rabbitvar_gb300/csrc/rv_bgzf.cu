@@ -15,10 +15,15 @@
 //            chunk whose start disagrees is re-walked from the right offset)
 //   k_bam_index        record offsets, one thread per chunk
 //   k_bam_fields       fixed fields + NM tag, one thread per record
-//   host     select one contig's records, prefix sums of CIGAR words and
-//            32-aligned base slots (per-read fields are mirrored on the host,
-//            which lays out regions and tiles from them)
-//   k_bam_unpack       CIGAR words, 4-bit bases and qualities, one warp per read
+//   host     prefix sums of CIGAR words and 32-aligned base slots over all
+//            records (host threads; the per-read fields are mirrored on the
+//            host, which lays out regions and tiles from them), and each
+//            reference id's span of records
+//   k_bam_unpack       CIGAR words, 4-bit bases and qualities of every record
+//                      into that layout, one warp per read
+//   rv_bam_batch       a contig whose records are contiguous (a sorted BAM)
+//                      is a window of the layout; otherwise its records are
+//                      gathered by a second k_bam_unpack
 //
 // Every device access is bounded: members by their compressed length and
 // ISIZE, records by the chain-verified block_size, aux fields by the record.
@@ -35,6 +40,7 @@
 
 #include "rv_bam_internal.h"
 #include "rv_inflate.cuh"
+#include "rv_pool.h"
 #include "rvgpu_io.h"
 
 namespace {
@@ -60,7 +66,9 @@ struct ChunkOut {
     int32_t status;  // 1: the walk met an impossible block_size
 };
 
-__global__ void __launch_bounds__(kInflateWarps * 32) k_inflate(const uint8_t *in, uint64_t in_bytes,
+// 12 blocks (48 warps) per SM: 152 x 48 = 7296 members in flight, more than
+// the ~5700 members of a 1.33 M-read BAM, so such a file inflates in one wave
+__global__ void __launch_bounds__(kInflateWarps * 32, 12) k_inflate(const uint8_t *in, uint64_t in_bytes,
                                                                 const BgzfMember *m, int n, uint8_t *out,
                                                                 int32_t *err) {
     __shared__ rvz::Tables tabs[kInflateWarps];
@@ -224,14 +232,15 @@ __global__ void k_bam_fields(const uint8_t *d, const uint64_t *rec, int64_t n, i
     }
 }
 
-// One warp per selected read: CIGAR words, packed bases and qualities.
+// One warp per selected read (every read when sel is null): CIGAR words,
+// packed bases and qualities.
 __global__ void k_bam_unpack(const uint8_t *d, const uint64_t *rec, const int64_t *sel, int64_t n,
                              const uint32_t *cig_off, const uint64_t *base_off, uint32_t *cigar, uint8_t *seq,
                              uint8_t *qual) {
     const int lane = threadIdx.x & 31;
     const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t k = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; k < n; k += warps) {
-        const uint8_t *r = d + rec[sel[k]] + 4;
+        const uint8_t *r = d + rec[sel ? sel[k] : k] + 4;
         const uint32_t lrn = r[8], ncig = rvz::rd16(r + 12);
         const uint32_t l = rvz::rd32(r + 16);
         const uint8_t *c = r + 32 + lrn;
@@ -247,77 +256,76 @@ __global__ void k_bam_unpack(const uint8_t *d, const uint64_t *rec, const int64_
     }
 }
 
-struct DevBuf {
-    std::vector<void *> ptrs;
-    ~DevBuf() {
-        for (void *p : ptrs) cudaFree(p);
-    }
-    template <class T>
-    T *get(size_t n) {
-        void *p = nullptr;
-        if (cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess) return nullptr;
-        ptrs.push_back(p);
-        return (T *)p;
-    }
-};
-
-template <class T>
-T *pinned_host(size_t n, std::vector<void *> &owned) {
-    void *p = nullptr;
-    if (cudaHostAlloc(&p, std::max<size_t>(n, 1) * sizeof(T), cudaHostAllocDefault) != cudaSuccess) return nullptr;
-    owned.push_back(p);
-    return (T *)p;
-}
-
-#define BG_CUDA(x)                                                 \
-    do {                                                           \
-        cudaError_t e_ = (x);                                      \
-        if (e_ != cudaSuccess) {                                   \
+#define BG_CUDA(x)                                                            \
+    do {                                                                      \
+        cudaError_t e_ = (x);                                                 \
+        if (e_ != cudaSuccess) {                                              \
             fprintf(stderr, "rv_bam_read_gpu: %s\n", cudaGetErrorString(e_)); \
-            return RV_ERR_CUDA;                                    \
-        }                                                          \
+            return RV_ERR_CUDA;                                               \
+        }                                                                     \
     } while (0)
 
 int grid_for(int64_t n, int per, int cap = 1 << 20) {
     return (int)std::max<int64_t>(1, std::min<int64_t>((n + per - 1) / per, cap));
 }
 
-rv_status decode(const uint8_t *bgzf, size_t nbytes, int device, rv_bam *bam) {
+template <class T>
+T *pinned_host(size_t n, std::vector<void *> &owned) {
+    void *p = nullptr;
+    if (cudaHostAlloc(&p, std::max<size_t>(n, 1) * sizeof(T), cudaHostAllocDefault) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    owned.push_back(p);
+    return (T *)p;
+}
+
+template <class T>
+T *device_buf(size_t n, std::vector<void *> &owned) {
+    void *p = nullptr;
+    if (cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    owned.push_back(p);
+    return (T *)p;
+}
+
+rv_status decode(const uint8_t *bgzf, size_t nbytes, rv_bam *bam) {
     Lap lap;
+    BamGpu *g = bam->gpu;
     std::vector<BgzfMember> mem;
     uint64_t total = 0;
     if (!bgzf_members(bgzf, nbytes, mem, total)) return RV_ERR_FORMAT;
     const int M = (int)mem.size();
     lap("members");
-    BG_CUDA(cudaSetDevice(device));
-    cudaStream_t s;
-    BG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
-    struct StreamGuard {
-        cudaStream_t s;
-        ~StreamGuard() { cudaStreamDestroy(s); }
-    } sg{s};
-    BamGpu *g = new BamGpu();
-    bam->gpu = g;
-    g->device = device;
+    BG_CUDA(cudaSetDevice(g->device));
+    cudaStream_t s = g->stream;
     g->total = total;
-    DevBuf tmp;
+    g->n_rec = g->n_cig = g->n_bases = 0;
     // compressed bytes and the member table; the stream is padded so that
     // word loads and field reads past the last byte stay in the allocation
     const uint64_t in_pad = (nbytes + 15) / 16 * 16 + 16;
-    uint8_t *d_in = tmp.get<uint8_t>(in_pad);
-    BgzfMember *d_mem = tmp.get<BgzfMember>((size_t)M);
-    int32_t *d_err = tmp.get<int32_t>(4);
-    ChunkOut *d_chunk = tmp.get<ChunkOut>((size_t)M);
-    if (!d_in || !d_mem || !d_err || !d_chunk) return RV_ERR_CUDA;
-    BG_CUDA(cudaMalloc((void **)&g->d_data, total + 64));
-    BG_CUDA(cudaMemsetAsync(g->d_data + total, 0, 64, s));
+    if (!g->d_in.grow(in_pad) || !g->d_mem.grow((size_t)M) || !g->d_err.grow(4) ||
+        !g->d_chunk.grow((size_t)M * 3) || !g->d_data.grow(total + 64))
+        return RV_ERR_CUDA;
+    uint8_t *d_in = g->d_in.p, *d_data = g->d_data.p;
+    BgzfMember *d_mem = g->d_mem.p;
+    int32_t *d_err = g->d_err.p;
+    ChunkOut *d_chunk = (ChunkOut *)g->d_chunk.p;
+    static_assert(sizeof(ChunkOut) == 24, "ChunkOut is three words");
+    BG_CUDA(cudaMemsetAsync(d_data + total, 0, 64, s));
     BG_CUDA(cudaMemsetAsync(d_in + nbytes, 0, in_pad - nbytes, s));
     BG_CUDA(cudaMemsetAsync(d_err, 0, 16, s));
     BG_CUDA(cudaMemcpyAsync(d_in, bgzf, nbytes, cudaMemcpyHostToDevice, s));
     BG_CUDA(cudaMemcpyAsync(d_mem, mem.data(), (size_t)M * sizeof(BgzfMember), cudaMemcpyHostToDevice, s));
+    if (lap.on) {
+        BG_CUDA(cudaStreamSynchronize(s));
+        lap("upload");
+    }
     if (M > 0)
         k_inflate<<<(M + kInflateWarps - 1) / kInflateWarps, kInflateWarps * 32, 0, s>>>(d_in, nbytes, d_mem, M,
-                                                                                      g->d_data, d_err);
+                                                                                      d_data, d_err);
     BG_CUDA(cudaGetLastError());
     int32_t err = 0;
     BG_CUDA(cudaMemcpyAsync(&err, d_err, 4, cudaMemcpyDeviceToHost, s));
@@ -327,7 +335,7 @@ rv_status decode(const uint8_t *bgzf, size_t nbytes, int device, rv_bam *bam) {
     int64_t hdr = 0;
     for (;;) {
         head.resize(have);
-        BG_CUDA(cudaMemcpyAsync(head.data(), g->d_data, have, cudaMemcpyDeviceToHost, s));
+        BG_CUDA(cudaMemcpyAsync(head.data(), d_data, have, cudaMemcpyDeviceToHost, s));
         BG_CUDA(cudaStreamSynchronize(s));
         if (err) {
             fprintf(stderr, "rv_bam_read_gpu: member %d: inflate error %d\n", err & 0xFFFFFF, err >> 24);
@@ -338,10 +346,10 @@ rv_status decode(const uint8_t *bgzf, size_t nbytes, int device, rv_bam *bam) {
         have = std::min<uint64_t>(total, have * 4);
     }
     if (hdr < 0) return RV_ERR_FORMAT;
-    lap("upload+inflate+header");
+    lap("inflate+header");
     const int32_t n_ref = (int32_t)bam->names.size();
     // record starts per chunk, then the chain check on the host
-    if (M > 0) k_bam_chunks<<<grid_for((int64_t)M * 32, 256), 256, 0, s>>>(g->d_data, total, (uint64_t)hdr, n_ref,
+    if (M > 0) k_bam_chunks<<<grid_for((int64_t)M * 32, 256), 256, 0, s>>>(d_data, total, (uint64_t)hdr, n_ref,
                                                                            d_mem, M, d_chunk);
     BG_CUDA(cudaGetLastError());
     std::vector<ChunkOut> ch((size_t)M);
@@ -357,7 +365,7 @@ rv_status decode(const uint8_t *bgzf, size_t nbytes, int device, rv_bam *bam) {
         if (E <= expect) continue;  // no record starts here (inside the header or a long record)
         ChunkOut r = ch[c];
         if (r.first != (int64_t)expect || r.status) {
-            k_bam_walk<<<1, 32, 0, s>>>(g->d_data, total, expect, E, d_chunk + c);
+            k_bam_walk<<<1, 32, 0, s>>>(d_data, total, expect, E, d_chunk + c);
             BG_CUDA(cudaGetLastError());
             BG_CUDA(cudaMemcpyAsync(&r, d_chunk + c, sizeof r, cudaMemcpyDeviceToHost, s));
             BG_CUDA(cudaStreamSynchronize(s));
@@ -371,164 +379,320 @@ rv_status decode(const uint8_t *bgzf, size_t nbytes, int device, rv_bam *bam) {
     if (expect > total) return RV_ERR_FORMAT;
     lap("verify");
     const int64_t N = base[(size_t)M];
-    g->n_rec = N;
-    BG_CUDA(cudaMalloc((void **)&g->d_rec, (size_t)std::max<int64_t>(N, 1) * 8));
-    int64_t *d_first = tmp.get<int64_t>((size_t)M), *d_base = tmp.get<int64_t>((size_t)M + 1);
-    int32_t *d_count = tmp.get<int32_t>((size_t)M);
-    if (!d_first || !d_base || !d_count) return RV_ERR_CUDA;
-    BG_CUDA(cudaMemcpyAsync(d_first, first.data(), (size_t)M * 8, cudaMemcpyHostToDevice, s));
-    BG_CUDA(cudaMemcpyAsync(d_base, base.data(), (size_t)M * 8, cudaMemcpyHostToDevice, s));
-    BG_CUDA(cudaMemcpyAsync(d_count, count.data(), (size_t)M * 4, cudaMemcpyHostToDevice, s));
-    if (M > 0) k_bam_index<<<grid_for(M, 128), 128, 0, s>>>(g->d_data, total, d_first, d_base, d_count, M, g->d_rec);
-    BG_CUDA(cudaGetLastError());
-    // fixed fields of every record, mirrored to pinned host memory
     const size_t n1 = (size_t)std::max<int64_t>(N, 1);
-    int32_t *d_tid = tmp.get<int32_t>(n1), *d_pos = tmp.get<int32_t>(n1), *d_mpos = tmp.get<int32_t>(n1),
-            *d_nm = tmp.get<int32_t>(n1), *d_lq = tmp.get<int32_t>(n1);
-    uint16_t *d_flag = tmp.get<uint16_t>(n1), *d_nc = tmp.get<uint16_t>(n1);
-    uint8_t *d_mapq = tmp.get<uint8_t>(n1);
-    if (!d_tid || !d_pos || !d_mpos || !d_nm || !d_lq || !d_flag || !d_nc || !d_mapq) return RV_ERR_CUDA;
-    auto &ho = g->host_owned;
-    g->h_tid = pinned_host<int32_t>(n1, ho);
-    g->h_pos = pinned_host<int32_t>(n1, ho);
-    g->h_mpos = pinned_host<int32_t>(n1, ho);
-    g->h_nm = pinned_host<int32_t>(n1, ho);
-    g->h_lq = pinned_host<int32_t>(n1, ho);
-    g->h_flag = pinned_host<uint16_t>(n1, ho);
-    g->h_nc = pinned_host<uint16_t>(n1, ho);
-    g->h_mapq = pinned_host<uint8_t>(n1, ho);
-    if (!g->h_tid || !g->h_pos || !g->h_mpos || !g->h_nm || !g->h_lq || !g->h_flag || !g->h_nc || !g->h_mapq)
+    if (!g->d_first.grow((size_t)M) || !g->d_base.grow((size_t)M + 1) || !g->d_count.grow((size_t)M) ||
+        !g->d_rec.grow(n1) || !g->d_tid.grow(n1) || !g->d_pos.grow(n1) || !g->d_mpos.grow(n1) ||
+        !g->d_nm.grow(n1) || !g->d_lq.grow(n1) || !g->d_flag.grow(n1) || !g->d_nc.grow(n1) ||
+        !g->d_mapq.grow(n1) || !g->d_cigoff.grow(n1) || !g->d_boff.grow(n1))
+        return RV_ERR_CUDA;
+    if (!g->h_tid.grow(n1) || !g->h_pos.grow(n1) || !g->h_mpos.grow(n1) || !g->h_nm.grow(n1) ||
+        !g->h_lq.grow(n1) || !g->h_flag.grow(n1) || !g->h_nc.grow(n1) || !g->h_mapq.grow(n1) ||
+        !g->h_cigoff.grow(n1) || !g->h_boff.grow(n1))
         return RV_ERR_CAPACITY;
-    if (N > 0)
-        k_bam_fields<<<grid_for(N, 256, 152 * 16), 256, 0, s>>>(g->d_data, g->d_rec, N, d_tid, d_pos, d_mpos, d_nm,
-                                                                 d_lq, d_flag, d_nc, d_mapq, d_err + 1);
+    BG_CUDA(cudaMemcpyAsync(g->d_first.p, first.data(), (size_t)M * 8, cudaMemcpyHostToDevice, s));
+    BG_CUDA(cudaMemcpyAsync(g->d_base.p, base.data(), (size_t)M * 8, cudaMemcpyHostToDevice, s));
+    BG_CUDA(cudaMemcpyAsync(g->d_count.p, count.data(), (size_t)M * 4, cudaMemcpyHostToDevice, s));
+    if (M > 0)
+        k_bam_index<<<grid_for(M, 128), 128, 0, s>>>(d_data, total, g->d_first.p, g->d_base.p, g->d_count.p, M,
+                                                     g->d_rec.p);
     BG_CUDA(cudaGetLastError());
-    BG_CUDA(cudaMemcpyAsync(g->h_tid, d_tid, (size_t)N * 4, cudaMemcpyDeviceToHost, s));
-    BG_CUDA(cudaMemcpyAsync(g->h_pos, d_pos, (size_t)N * 4, cudaMemcpyDeviceToHost, s));
-    BG_CUDA(cudaMemcpyAsync(g->h_mpos, d_mpos, (size_t)N * 4, cudaMemcpyDeviceToHost, s));
-    BG_CUDA(cudaMemcpyAsync(g->h_nm, d_nm, (size_t)N * 4, cudaMemcpyDeviceToHost, s));
-    BG_CUDA(cudaMemcpyAsync(g->h_lq, d_lq, (size_t)N * 4, cudaMemcpyDeviceToHost, s));
-    BG_CUDA(cudaMemcpyAsync(g->h_flag, d_flag, (size_t)N * 2, cudaMemcpyDeviceToHost, s));
-    BG_CUDA(cudaMemcpyAsync(g->h_nc, d_nc, (size_t)N * 2, cudaMemcpyDeviceToHost, s));
-    BG_CUDA(cudaMemcpyAsync(g->h_mapq, d_mapq, (size_t)N, cudaMemcpyDeviceToHost, s));
+    if (N > 0)
+        k_bam_fields<<<grid_for(N, 256, 152 * 16), 256, 0, s>>>(d_data, g->d_rec.p, N, g->d_tid.p, g->d_pos.p,
+                                                                 g->d_mpos.p, g->d_nm.p, g->d_lq.p, g->d_flag.p,
+                                                                 g->d_nc.p, g->d_mapq.p, d_err + 1);
+    BG_CUDA(cudaGetLastError());
+    BG_CUDA(cudaMemcpyAsync(g->h_tid.p, g->d_tid.p, (size_t)N * 4, cudaMemcpyDeviceToHost, s));
+    BG_CUDA(cudaMemcpyAsync(g->h_nc.p, g->d_nc.p, (size_t)N * 2, cudaMemcpyDeviceToHost, s));
+    BG_CUDA(cudaMemcpyAsync(g->h_lq.p, g->d_lq.p, (size_t)N * 4, cudaMemcpyDeviceToHost, s));
     BG_CUDA(cudaMemcpyAsync(&err, d_err + 1, 4, cudaMemcpyDeviceToHost, s));
     BG_CUDA(cudaStreamSynchronize(s));
-    lap("index+fields");
     if (err) return RV_ERR_FORMAT;
+    // the rest of the per-read fields come back while the host lays out the batch
+    BG_CUDA(cudaMemcpyAsync(g->h_pos.p, g->d_pos.p, (size_t)N * 4, cudaMemcpyDeviceToHost, s));
+    BG_CUDA(cudaMemcpyAsync(g->h_mpos.p, g->d_mpos.p, (size_t)N * 4, cudaMemcpyDeviceToHost, s));
+    BG_CUDA(cudaMemcpyAsync(g->h_nm.p, g->d_nm.p, (size_t)N * 4, cudaMemcpyDeviceToHost, s));
+    BG_CUDA(cudaMemcpyAsync(g->h_flag.p, g->d_flag.p, (size_t)N * 2, cudaMemcpyDeviceToHost, s));
+    BG_CUDA(cudaMemcpyAsync(g->h_mapq.p, g->d_mapq.p, (size_t)N, cudaMemcpyDeviceToHost, s));
+    lap("index+fields");
+    // batch layout over all records in file order: CIGAR word offsets and
+    // 32-aligned base slots (prefix sums on the host threads); the records
+    // of each reference id
+    {
+        const int64_t nch = rv::chunks_for(N, 1 << 16);
+        std::vector<int64_t> cs((size_t)nch + 1, 0), bs((size_t)nch + 1, 0);
+        struct Run {
+            int32_t tid;
+            int64_t lo, hi, n;
+        };
+        std::vector<std::vector<Run>> runs((size_t)nch);
+        rv::parallel_chunks(N, 1 << 16, [&](int64_t k, int64_t a, int64_t e) {
+            int64_t c = 0, b = 0;
+            std::vector<Run> &rk = runs[(size_t)k];
+            for (int64_t i = a; i < e; i++) {
+                c += g->h_nc.p[i];
+                b += ((int64_t)g->h_lq.p[i] + 31) / 32 * 32;
+                const int32_t t = g->h_tid.p[i];
+                if (rk.empty() || rk.back().tid != t) rk.push_back(Run{t, i, i + 1, 1});
+                else {
+                    rk.back().hi = i + 1;
+                    rk.back().n++;
+                }
+            }
+            cs[(size_t)k + 1] = c;
+            bs[(size_t)k + 1] = b;
+        });
+        for (int64_t k = 0; k < nch; k++) {
+            cs[(size_t)k + 1] += cs[(size_t)k];
+            bs[(size_t)k + 1] += bs[(size_t)k];
+        }
+        if (cs[(size_t)nch] > (int64_t)UINT32_MAX) return RV_ERR_UNSUPPORTED;
+        rv::parallel_chunks(N, 1 << 16, [&](int64_t k, int64_t a, int64_t e) {
+            int64_t c = cs[(size_t)k], b = bs[(size_t)k];
+            for (int64_t i = a; i < e; i++) {
+                g->h_cigoff.p[i] = (uint32_t)c;
+                g->h_boff.p[i] = (uint64_t)b;
+                c += g->h_nc.p[i];
+                b += ((int64_t)g->h_lq.p[i] + 31) / 32 * 32;
+            }
+        });
+        g->n_cig = cs[(size_t)nch];
+        g->n_bases = bs[(size_t)nch];
+        // each reference id's span from the runs of equal ids (file order)
+        g->tid_lo.assign((size_t)n_ref + 1, -1);
+        g->tid_hi.assign((size_t)n_ref + 1, -1);
+        g->tid_n.assign((size_t)n_ref + 1, 0);
+        for (const auto &rk : runs)
+            for (const Run &r : rk) {
+                if (r.tid < -1 || r.tid >= n_ref) continue;  // cannot happen: fields were range-checked
+                const size_t k = (size_t)(r.tid + 1);
+                if (g->tid_lo[k] < 0) g->tid_lo[k] = r.lo;
+                g->tid_hi[k] = r.hi;
+                g->tid_n[k] += r.n;
+            }
+    }
+    lap("layout");
+    if (!g->d_cig.grow((size_t)g->n_cig) || !g->d_seq.grow((size_t)g->n_bases / 2 + 16) ||
+        !g->d_qual.grow((size_t)g->n_bases + 32) || !g->h_cig.grow((size_t)g->n_cig))
+        return RV_ERR_CUDA;
+    BG_CUDA(cudaMemcpyAsync(g->d_cigoff.p, g->h_cigoff.p, (size_t)N * 4, cudaMemcpyHostToDevice, s));
+    BG_CUDA(cudaMemcpyAsync(g->d_boff.p, g->h_boff.p, (size_t)N * 8, cudaMemcpyHostToDevice, s));
+    BG_CUDA(cudaMemsetAsync(g->d_seq.p, 0, (size_t)g->n_bases / 2 + 16, s));
+    BG_CUDA(cudaMemsetAsync(g->d_qual.p, 0, (size_t)g->n_bases + 32, s));
+    if (N > 0)
+        k_bam_unpack<<<grid_for(N * 32, 256, 152 * 16), 256, 0, s>>>(d_data, g->d_rec.p, nullptr, N, g->d_cigoff.p,
+                                                                     g->d_boff.p, g->d_cig.p, g->d_seq.p, g->d_qual.p);
+    BG_CUDA(cudaGetLastError());
+    BG_CUDA(cudaMemcpyAsync(g->h_cig.p, g->d_cig.p, (size_t)g->n_cig * 4, cudaMemcpyDeviceToHost, s));
+    BG_CUDA(cudaStreamSynchronize(s));
+    g->n_rec = N;
+    lap("unpack");
     return RV_OK;
 }
 
 }  // namespace
 
+void bam_gpu_drop_batches(BamGpu *g) {
+    for (void *p : g->batch_dev) cudaFree(p);
+    for (void *p : g->batch_host) cudaFreeHost(p);
+    g->batch_dev.clear();
+    g->batch_host.clear();
+}
+
 rv_status bam_gpu_batch(rv_bam *bam, int tid, rv_read_batch *out, bool host_bases) {
     BamGpu *g = bam->gpu;
     const int64_t N = g->n_rec;
-    // this contig's records in file order; CIGAR and 32-aligned base slots
-    std::vector<int64_t> sel;
-    for (int64_t i = 0; i < N; i++)
-        if (g->h_tid[i] == tid) sel.push_back(i);
-    const int64_t n = (int64_t)sel.size();
-    auto &own = bam->owned;
-    int32_t *pos = pinned_host<int32_t>(n, own), *mpos = pinned_host<int32_t>(n, own),
-            *nm = pinned_host<int32_t>(n, own), *lq = pinned_host<int32_t>(n, own);
-    uint16_t *flag = pinned_host<uint16_t>(n, own), *nc = pinned_host<uint16_t>(n, own);
-    uint8_t *mapq = pinned_host<uint8_t>(n, own);
-    uint32_t *coff = pinned_host<uint32_t>(n, own);
-    uint64_t *boff = pinned_host<uint64_t>(n, own);
-    if (!pos || !mpos || !nm || !lq || !flag || !nc || !mapq || !coff || !boff) return RV_ERR_CAPACITY;
-    int64_t ci = 0, bi = 0;
-    for (int64_t k = 0; k < n; k++) {
-        const int64_t i = sel[k];
-        pos[k] = g->h_pos[i];
-        mpos[k] = g->h_mpos[i];
-        nm[k] = g->h_nm[i];
-        lq[k] = g->h_lq[i];
-        flag[k] = g->h_flag[i];
-        nc[k] = g->h_nc[i];
-        mapq[k] = g->h_mapq[i];
-        coff[k] = (uint32_t)ci;
-        boff[k] = (uint64_t)bi;
-        ci += nc[k];
-        bi += ((int64_t)lq[k] + 31) / 32 * 32;
-    }
-    if (ci > (int64_t)UINT32_MAX) return RV_ERR_UNSUPPORTED;
-    uint32_t *cig = pinned_host<uint32_t>((size_t)ci, own);
-    if (!cig) return RV_ERR_CAPACITY;
     BG_CUDA(cudaSetDevice(g->device));
-    cudaStream_t s;
-    BG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
-    struct StreamGuard {
-        cudaStream_t s;
-        ~StreamGuard() { cudaStreamDestroy(s); }
-    } sg{s};
-    DevBuf tmp;
-    int64_t *d_sel = tmp.get<int64_t>((size_t)n);
-    uint32_t *d_coff = tmp.get<uint32_t>((size_t)n), *d_cig = tmp.get<uint32_t>((size_t)ci);
-    uint64_t *d_boff = tmp.get<uint64_t>((size_t)n);
-    if (!d_sel || !d_coff || !d_cig || !d_boff) return RV_ERR_CUDA;
-    // bases and qualities stay on the device with the batch (zeroed slots)
-    uint8_t *d_seq = nullptr, *d_qual = nullptr;
-    BG_CUDA(cudaMalloc((void **)&d_seq, (size_t)bi / 2 + 16));
-    g->dev_owned.push_back(d_seq);
-    BG_CUDA(cudaMalloc((void **)&d_qual, (size_t)bi + 32));
-    g->dev_owned.push_back(d_qual);
-    BG_CUDA(cudaMemsetAsync(d_seq, 0, (size_t)bi / 2 + 16, s));
-    BG_CUDA(cudaMemsetAsync(d_qual, 0, (size_t)bi + 32, s));
-    BG_CUDA(cudaMemcpyAsync(d_sel, sel.data(), (size_t)n * 8, cudaMemcpyHostToDevice, s));
-    BG_CUDA(cudaMemcpyAsync(d_coff, coff, (size_t)n * 4, cudaMemcpyHostToDevice, s));
-    BG_CUDA(cudaMemcpyAsync(d_boff, boff, (size_t)n * 8, cudaMemcpyHostToDevice, s));
-    if (n > 0)
-        k_bam_unpack<<<grid_for(n * 32, 256, 152 * 16), 256, 0, s>>>(g->d_data, g->d_rec, d_sel, n, d_coff, d_boff,
-                                                                     d_cig, d_seq, d_qual);
-    BG_CUDA(cudaGetLastError());
-    BG_CUDA(cudaMemcpyAsync(cig, d_cig, (size_t)ci * 4, cudaMemcpyDeviceToHost, s));
-    const uint8_t *seq = d_seq, *qual = d_qual;
-    if (host_bases) {
-        uint8_t *hs = pinned_host<uint8_t>((size_t)bi / 2 + 16, own), *hq = pinned_host<uint8_t>((size_t)bi + 32, own);
-        if (!hs || !hq) return RV_ERR_CAPACITY;
-        BG_CUDA(cudaMemcpyAsync(hs, d_seq, (size_t)bi / 2 + 16, cudaMemcpyDeviceToHost, s));
-        BG_CUDA(cudaMemcpyAsync(hq, d_qual, (size_t)bi + 32, cudaMemcpyDeviceToHost, s));
-        seq = hs;
-        qual = hq;
-    }
-    BG_CUDA(cudaStreamSynchronize(s));
+    cudaStream_t s = g->stream;
+    const int64_t k = (int64_t)tid + 1;
+    const bool known = k >= 0 && k < (int64_t)g->tid_n.size();
+    const int64_t n = known ? g->tid_n[(size_t)k] : 0;
+    const int64_t lo = n > 0 ? g->tid_lo[(size_t)k] : 0;
+    memset(out, 0, sizeof *out);
     out->n_reads = n;
-    out->pos = pos;
-    out->flag = flag;
-    out->mapq = mapq;
-    out->mpos = mpos;
-    out->nm = nm;
-    out->n_cigar = nc;
-    out->cig_off = coff;
-    out->cigar = cig;
-    out->n_cigar_words = ci;
-    out->l_qseq = lq;
-    out->base_off = boff;
-    out->seq = seq;
-    out->qual = qual;
-    out->n_bases = bi;
+    if (n == 0 || g->tid_hi[(size_t)k] - lo == n) {
+        // the contig's records are contiguous in the file (a sorted BAM):
+        // the batch is a window of the all-records layout
+        const int64_t hi = lo + n;
+        const uint32_t c0 = n ? g->h_cigoff.p[lo] : 0;
+        const uint64_t b0 = n ? g->h_boff.p[lo] : 0;
+        const int64_t c1 = hi < N ? (int64_t)g->h_cigoff.p[hi] : g->n_cig;
+        const int64_t b1 = hi < N ? (int64_t)g->h_boff.p[hi] : g->n_bases;
+        out->pos = g->h_pos.p + lo;
+        out->flag = g->h_flag.p + lo;
+        out->mapq = g->h_mapq.p + lo;
+        out->mpos = g->h_mpos.p + lo;
+        out->nm = g->h_nm.p + lo;
+        out->n_cigar = g->h_nc.p + lo;
+        out->l_qseq = g->h_lq.p + lo;
+        out->cigar = g->h_cig.p + c0;
+        out->n_cigar_words = c1 - (int64_t)c0;
+        out->n_bases = b1 - (int64_t)b0;
+        if (lo == 0) {
+            out->cig_off = g->h_cigoff.p;
+            out->base_off = g->h_boff.p;
+        } else {
+            uint32_t *co = pinned_host<uint32_t>((size_t)n, g->batch_host);
+            uint64_t *bo = pinned_host<uint64_t>((size_t)n, g->batch_host);
+            if (!co || !bo) return RV_ERR_CAPACITY;
+            for (int64_t i = 0; i < n; i++) {
+                co[i] = g->h_cigoff.p[lo + i] - c0;
+                bo[i] = g->h_boff.p[lo + i] - b0;
+            }
+            out->cig_off = co;
+            out->base_off = bo;
+        }
+        out->seq = g->d_seq.p + b0 / 2;
+        out->qual = g->d_qual.p + b0;
+    } else {
+        // records of the contig scattered through the file: gather them
+        std::vector<int64_t> sel;
+        sel.reserve((size_t)n);
+        for (int64_t i = g->tid_lo[(size_t)k]; i < g->tid_hi[(size_t)k]; i++)
+            if (g->h_tid.p[i] == tid) sel.push_back(i);
+        auto &own = g->batch_host;
+        int32_t *pos = pinned_host<int32_t>(n, own), *mpos = pinned_host<int32_t>(n, own),
+                *nm = pinned_host<int32_t>(n, own), *lq = pinned_host<int32_t>(n, own);
+        uint16_t *flag = pinned_host<uint16_t>(n, own), *nc = pinned_host<uint16_t>(n, own);
+        uint8_t *mapq = pinned_host<uint8_t>(n, own);
+        uint32_t *coff = pinned_host<uint32_t>(n, own);
+        uint64_t *boff = pinned_host<uint64_t>(n, own);
+        if (!pos || !mpos || !nm || !lq || !flag || !nc || !mapq || !coff || !boff) return RV_ERR_CAPACITY;
+        int64_t ci = 0, bi = 0;
+        for (int64_t j = 0; j < n; j++) {
+            const int64_t i = sel[(size_t)j];
+            pos[j] = g->h_pos.p[i];
+            mpos[j] = g->h_mpos.p[i];
+            nm[j] = g->h_nm.p[i];
+            lq[j] = g->h_lq.p[i];
+            flag[j] = g->h_flag.p[i];
+            nc[j] = g->h_nc.p[i];
+            mapq[j] = g->h_mapq.p[i];
+            coff[j] = (uint32_t)ci;
+            boff[j] = (uint64_t)bi;
+            ci += nc[j];
+            bi += ((int64_t)lq[j] + 31) / 32 * 32;
+        }
+        uint32_t *cig = pinned_host<uint32_t>((size_t)ci, own);
+        int64_t *d_sel = device_buf<int64_t>((size_t)n, g->batch_dev);
+        uint32_t *d_coff = device_buf<uint32_t>((size_t)n, g->batch_dev), *d_cig = device_buf<uint32_t>((size_t)ci, g->batch_dev);
+        uint64_t *d_boff = device_buf<uint64_t>((size_t)n, g->batch_dev);
+        uint8_t *d_seq = device_buf<uint8_t>((size_t)bi / 2 + 16, g->batch_dev);
+        uint8_t *d_qual = device_buf<uint8_t>((size_t)bi + 32, g->batch_dev);
+        if (!cig || !d_sel || !d_coff || !d_cig || !d_boff || !d_seq || !d_qual) return RV_ERR_CAPACITY;
+        BG_CUDA(cudaMemsetAsync(d_seq, 0, (size_t)bi / 2 + 16, s));
+        BG_CUDA(cudaMemsetAsync(d_qual, 0, (size_t)bi + 32, s));
+        BG_CUDA(cudaMemcpyAsync(d_sel, sel.data(), (size_t)n * 8, cudaMemcpyHostToDevice, s));
+        BG_CUDA(cudaMemcpyAsync(d_coff, coff, (size_t)n * 4, cudaMemcpyHostToDevice, s));
+        BG_CUDA(cudaMemcpyAsync(d_boff, boff, (size_t)n * 8, cudaMemcpyHostToDevice, s));
+        k_bam_unpack<<<grid_for(n * 32, 256, 152 * 16), 256, 0, s>>>(g->d_data.p, g->d_rec.p, d_sel, n, d_coff,
+                                                                     d_boff, d_cig, d_seq, d_qual);
+        BG_CUDA(cudaGetLastError());
+        BG_CUDA(cudaMemcpyAsync(cig, d_cig, (size_t)ci * 4, cudaMemcpyDeviceToHost, s));
+        BG_CUDA(cudaStreamSynchronize(s));
+        out->pos = pos;
+        out->flag = flag;
+        out->mapq = mapq;
+        out->mpos = mpos;
+        out->nm = nm;
+        out->n_cigar = nc;
+        out->cig_off = coff;
+        out->cigar = cig;
+        out->n_cigar_words = ci;
+        out->l_qseq = lq;
+        out->base_off = boff;
+        out->seq = d_seq;
+        out->qual = d_qual;
+        out->n_bases = bi;
+    }
+    if (host_bases) {
+        const size_t ns = (size_t)(out->n_bases + 1) / 2, nq = (size_t)out->n_bases;
+        uint8_t *hs = pinned_host<uint8_t>(ns + 16, g->batch_host), *hq = pinned_host<uint8_t>(nq + 32, g->batch_host);
+        if (!hs || !hq) return RV_ERR_CAPACITY;
+        BG_CUDA(cudaMemcpyAsync(hs, out->seq, ns, cudaMemcpyDeviceToHost, s));
+        BG_CUDA(cudaMemcpyAsync(hq, out->qual, nq, cudaMemcpyDeviceToHost, s));
+        BG_CUDA(cudaStreamSynchronize(s));
+        out->seq = hs;
+        out->qual = hq;
+    }
     return RV_OK;
 }
 
 void bam_gpu_free(BamGpu *g) {
     if (!g) return;
     cudaSetDevice(g->device);
-    cudaFree(g->d_data);
-    cudaFree(g->d_rec);
-    for (void *p : g->dev_owned) cudaFree(p);
-    for (void *p : g->host_owned) cudaFreeHost(p);
+    if (g->stream) cudaStreamSynchronize(g->stream);
+    bam_gpu_drop_batches(g);
+    g->d_in.release();
+    g->d_data.release();
+    g->d_mem.release();
+    g->d_chunk.release();
+    g->d_first.release();
+    g->d_base.release();
+    g->d_count.release();
+    g->d_err.release();
+    g->d_rec.release();
+    g->d_boff.release();
+    g->d_tid.release();
+    g->d_pos.release();
+    g->d_mpos.release();
+    g->d_nm.release();
+    g->d_lq.release();
+    g->d_flag.release();
+    g->d_nc.release();
+    g->d_mapq.release();
+    g->d_seq.release();
+    g->d_qual.release();
+    g->d_cigoff.release();
+    g->d_cig.release();
+    g->h_tid.release();
+    g->h_pos.release();
+    g->h_mpos.release();
+    g->h_nm.release();
+    g->h_lq.release();
+    g->h_flag.release();
+    g->h_nc.release();
+    g->h_mapq.release();
+    g->h_cigoff.release();
+    g->h_cig.release();
+    g->h_boff.release();
+    if (g->stream) cudaStreamDestroy(g->stream);
     delete g;
 }
 
 extern "C" rv_status rv_bam_read_gpu(const uint8_t *bgzf, size_t n, int device, rv_bam **out) {
     if (!bgzf || !out) return RV_ERR_ARG;
     *out = nullptr;
+    if (cudaSetDevice(device) != cudaSuccess) {
+        cudaGetLastError();
+        return RV_ERR_CUDA;
+    }
     rv_bam *bam = new rv_bam();
-    const rv_status st = decode(bgzf, n, device, bam);
+    bam->gpu = new BamGpu();
+    bam->gpu->device = device;
+    if (cudaStreamCreateWithFlags(&bam->gpu->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        bam->gpu->stream = nullptr;
+        rv_bam_free(bam);
+        return RV_ERR_CUDA;
+    }
+    const rv_status st = decode(bgzf, n, bam);
     if (st != RV_OK) {
         rv_bam_free(bam);
         return st;
     }
     *out = bam;
     return RV_OK;
+}
+
+extern "C" rv_status rv_bam_reread_gpu(rv_bam *bam, const uint8_t *bgzf, size_t n) {
+    if (!bam || !bam->gpu || !bgzf) return RV_ERR_ARG;
+    if (cudaSetDevice(bam->gpu->device) != cudaSuccess) {
+        cudaGetLastError();
+        return RV_ERR_CUDA;
+    }
+    cudaStreamSynchronize(bam->gpu->stream);
+    bam_gpu_drop_batches(bam->gpu);
+    bam->gpu->tid_n.clear();
+    bam->gpu->n_rec = 0;
+    return decode(bgzf, n, bam);
 }

@@ -134,11 +134,19 @@ def test_contigs_long_header_long_records_odd_names(tmp_path, mix):
             assert [got[2][k].n_reads for k in range(3)] == [n // 3, 2 * n // 3 - n // 3, n - 2 * n // 3 - 50]
         finally:
             db.close()
+    # names the record finder rejects; then, decoded into the same handle,
+    # contigs interleaved record by record (batches gathered, not windows)
     payload, _ = bam_stream(t, name_fn=lambda i: b"r\t%d" % i)
     data = bgzf(payload, 1)
     db = api.DeviceBam(data)
     try:
         same_batches(db.host_batches(), host_decode(tmp_path, data))
+        payload, _ = bam_stream(t, np.arange(n) % 2, contigs[:2])
+        data = bgzf(payload, 6)
+        db.reread(data)
+        got = db.host_batches()
+        same_batches(got, host_decode(tmp_path, data))
+        assert got[2][0].n_reads == (n + 1) // 2
     finally:
         db.close()
 
