@@ -57,7 +57,7 @@ struct Lap {
     }
 };
 
-constexpr int kInflateWarps = 4;  // members per block (one warp each; tables 4 x 2.5 KB of shared memory)
+constexpr int kInflateWarps = 2;  // warps (members) per block
 
 struct ChunkOut {
     int64_t first;   // first record start found in the chunk, -1 none
@@ -66,9 +66,9 @@ struct ChunkOut {
     int32_t status;  // 1: the walk met an impossible block_size
 };
 
-// 12 blocks (48 warps) per SM: 152 x 48 = 7296 members in flight, more than
-// the ~5700 members of a 1.33 M-read BAM, so such a file inflates in one wave
-__global__ void __launch_bounds__(kInflateWarps * 32, 12) k_inflate(const uint8_t *in, uint64_t in_bytes,
+// One warp per member: its lanes run the bit-level decoder in lockstep and
+// share table fills and match copies; its tables live in shared memory.
+__global__ void __launch_bounds__(kInflateWarps * 32) k_inflate(const uint8_t *in, uint64_t in_bytes,
                                                                 const BgzfMember *m, int n, uint8_t *out,
                                                                 int32_t *err) {
     __shared__ rvz::Tables tabs[kInflateWarps];
@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(kInflateWarps * 32, 12) k_inflate(const uint8_
     if (i >= n) return;  // whole warps leave together
     const BgzfMember mb = m[i];
     if (mb.out_len == 0) return;
-    const rvz::Lanes w{(int)(threadIdx.x & 31), 32};
+    const rvz::Lanes w{(int)(threadIdx.x & 31), 32, 0xFFFFFFFFu};
     const int e = rvz::inflate(in + mb.in_off, mb.in_len, in + in_bytes, out + mb.out_off, mb.out_len, tabs[wib], w);
     if (e && w.lane == 0) atomicCAS(err, 0, (e << 24) | (i & 0xFFFFFF));
 }

@@ -50,8 +50,8 @@ enum : int {
 
 // One member's decode tables (shared memory of the warp on the device).
 struct Tables {
-    int16_t lit_fast[1 << kLitFast];    // (symbol << 4 | length), -1: longer code or unused
-    int16_t dist_fast[1 << kDistFast];
+    uint32_t lit_fast[1 << kLitFast];   // decoded entries (entry_of), 0: longer code or unused
+    uint32_t dist_fast[1 << kDistFast];
     uint16_t lit_count[16], dist_count[16];
     uint16_t lit_sym[288], dist_sym[32];
     uint8_t lens[320];
@@ -123,25 +123,57 @@ struct BitIn {
     RVZ_HD int64_t overrun() const { return -(left_bits + have); }
 };
 
-// The lanes cooperating on one member: lane index, lane count (32 on the
-// device, 1 on the host) and the warp barrier that orders their shared- and
+// The lanes cooperating on one member: lane index within the group, group
+// size (a warp or part of one on the device, 1 on the host), the group's
+// lane mask, and the barrier that orders the group's shared- and
 // global-memory writes.
 struct Lanes {
     int lane, n;
+    unsigned mask;
     RVZ_HD void sync() const {
 #ifdef __CUDA_ARCH__
-        __syncwarp();
+        __syncwarp(mask);
 #elif defined(RVZ_HOST_SYNC)
         RVZ_HOST_SYNC(n);  // a host build may emulate a warp with threads and a barrier
 #endif
     }
 };
 
+RVZ_HD int len_base(int s);
+RVZ_HD int len_extra(int s);
+RVZ_HD int dist_base(int s);
+RVZ_HD int dist_extra(int s);
+
+// A decoded symbol as one word, so the decode loop needs no per-symbol
+// arithmetic: bits 0-3 code length (0: no code), bits 4-5 kind, bits 8+
+// the payload.  Literal/length alphabet: a literal (byte at 8-15), the end
+// of the block, or a length (base at 8-16, extra bits at 20-23).  Distance
+// alphabet: base at 8-22, extra bits at 24-27.  Code-length alphabet: the
+// symbol at 8-15.
+enum : int { MAP_LIT = 0, MAP_DIST = 1, MAP_RAW = 2 };
+enum : uint32_t { K_LIT = 0, K_EOB = 1, K_LEN = 2, K_BAD = 3 };
+
+RVZ_HD uint32_t entry_of(int sym, int l, int map) {
+    const uint32_t L = (uint32_t)l;
+    if (map == MAP_LIT) {
+        if (sym < 256) return L | (K_LIT << 4) | ((uint32_t)sym << 8);
+        if (sym == 256) return L | (K_EOB << 4);
+        if (sym < 286)
+            return L | (K_LEN << 4) | ((uint32_t)len_base(sym - 257) << 8) | ((uint32_t)len_extra(sym - 257) << 20);
+        return L | (K_BAD << 4);
+    }
+    if (map == MAP_DIST) {
+        if (sym < 30) return L | ((uint32_t)dist_base(sym) << 8) | ((uint32_t)dist_extra(sym) << 24);
+        return L | (K_BAD << 4);
+    }
+    return L | ((uint32_t)sym << 8);
+}
+
 // Canonical Huffman code (RFC 1951 3.2.2) from code lengths: a first-level
 // table of `fbits` bits plus count/symbol arrays for the bit-serial slow path.
 // Every lane computes the counts and offsets; the symbol list and the table
 // entries are written by the lanes in parallel.
-RVZ_HD bool build(const uint8_t *len, int n, int16_t *fast, int fbits, uint16_t *count, uint16_t *sym,
+RVZ_HD bool build(const uint8_t *len, int n, uint32_t *fast, int fbits, uint16_t *count, uint16_t *sym, int map,
                   const Lanes &w) {
     uint16_t cnt[16];
     for (int l = 0; l < 16; l++) cnt[l] = 0;
@@ -173,7 +205,7 @@ RVZ_HD bool build(const uint8_t *len, int n, int16_t *fast, int fbits, uint16_t 
         sym[offs[l] + r] = (uint16_t)i;
     }
     const int size = 1 << fbits;
-    for (int i = w.lane; i < size; i += w.n) fast[i] = -1;
+    for (int i = w.lane; i < size; i += w.n) fast[i] = 0;
     w.sync();
     // codes no longer than fbits fill every table entry they prefix
     const int nfast = offs[fbits < 15 ? fbits + 1 : 15] + (fbits < 15 ? 0 : cnt[15]);
@@ -181,20 +213,20 @@ RVZ_HD bool build(const uint8_t *len, int n, int16_t *fast, int fbits, uint16_t 
         int l = 1;
         while (l < 15 && idx >= offs[l + 1]) l++;
         const uint32_t code = first[l] + (uint32_t)(idx - offs[l]);
-        const int16_t e = (int16_t)((sym[idx] << 4) | l);
+        const uint32_t e = entry_of(sym[idx], l, map);
         for (uint32_t f = rev_bits(code, l); f < (uint32_t)size; f += 1u << l) fast[f] = e;
     }
     w.sync();
     return true;
 }
 
-// One symbol; -1 for a code that is not in the table.
-RVZ_HD int decode(BitIn &b, const int16_t *fast, int fbits, const uint16_t *count, const uint16_t *sym) {
+// One symbol's entry (entry_of); 0 for a code that is not in the table.
+RVZ_HD uint32_t decode(BitIn &b, const uint32_t *fast, int fbits, const uint16_t *count, const uint16_t *sym, int map) {
     b.refill();
-    const int e = fast[b.peek(fbits)];
-    if (e >= 0) {
-        b.drop(e & 15);
-        return e >> 4;
+    const uint32_t e = fast[b.peek(fbits)];
+    if (e & 15) {
+        b.drop((int)(e & 15));
+        return e;
     }
     int code = 0, first = 0, index = 0;
     uint64_t a = b.acc;
@@ -204,14 +236,14 @@ RVZ_HD int decode(BitIn &b, const int16_t *fast, int fbits, const uint16_t *coun
         const int c = count[l];
         if (code - c < first) {
             b.drop(l);
-            return sym[index + (code - first)];
+            return entry_of(sym[index + (code - first)], l, map);
         }
         index += c;
         first += c;
         first <<= 1;
         code <<= 1;
     }
-    return -1;
+    return 0;
 }
 
 RVZ_HD int len_base(int s) {  // s in [0, 28]
@@ -223,48 +255,63 @@ RVZ_HD int dist_base(int s) {  // s in [0, 29]
 }
 RVZ_HD int dist_extra(int s) { return s < 4 ? 0 : (s >> 1) - 1; }
 
-RVZ_HD int codes(BitIn &b, Tables &t, uint8_t *out, uint32_t cap, uint32_t &o, const Lanes &w) {
+// A member's output slot and the bytes produced so far.
+struct Out {
+    uint8_t *g;
+    uint32_t cap;  // ISIZE
+    uint32_t o;
+
+    RVZ_HD void put(uint8_t v, const Lanes &w) {
+        if (w.lane == 0) g[o] = v;
+        o++;
+    }
+    // out[o + k] = out[o - d + k mod d]: reads only bytes written before this
+    // match, so the lanes copy in any order
+    RVZ_HD void copy(uint32_t d, uint32_t len, const Lanes &w) {
+        w.sync();
+        const uint8_t *src = g + (o - d);
+        uint8_t *dst = g + o;
+        if (d >= len)
+            for (uint32_t k = (uint32_t)w.lane; k < len; k += (uint32_t)w.n) dst[k] = src[k];
+        else
+            for (uint32_t k = (uint32_t)w.lane; k < len; k += (uint32_t)w.n) dst[k] = src[k % d];
+        o += len;
+    }
+};
+
+// The symbols of one block up to its end-of-block code.  Every symbol other
+// than end-of-block adds at least one byte, so a block ends within ISIZE + 1
+// symbols; reads past the member's end are checked once per block.
+RVZ_HD int codes(BitIn &b, Tables &t, Out &out, const Lanes &w) {
     for (;;) {
-        int s = decode(b, t.lit_fast, kLitFast, t.lit_count, t.lit_sym);
-        if (s < 0) return ERR_CODE;
-        if (b.overrun() > 0) return ERR_INPUT;
-        if (s < 256) {
-            if (o >= cap) return ERR_OUTPUT;
-            if (w.lane == 0) out[o] = (uint8_t)s;
-            o++;
+        const uint32_t e = decode(b, t.lit_fast, kLitFast, t.lit_count, t.lit_sym, MAP_LIT);
+        if (!e) return ERR_CODE;
+        const uint32_t kind = (e >> 4) & 3;
+        if (kind == K_LIT) {
+            if (out.o >= out.cap) return ERR_OUTPUT;
+            out.put((uint8_t)(e >> 8), w);
             continue;
         }
-        if (s == 256) return ERR_NONE;
-        s -= 257;
-        if (s >= 29) return ERR_SYMBOL;
-        const uint32_t len = (uint32_t)len_base(s) + b.get(len_extra(s));
-        const int ds = decode(b, t.dist_fast, kDistFast, t.dist_count, t.dist_sym);
-        if (ds < 0) return ERR_CODE;
-        if (ds >= 30) return ERR_SYMBOL;
-        const uint32_t d = (uint32_t)dist_base(ds) + b.get(dist_extra(ds));
-        if (d > o) return ERR_DISTANCE;
-        if (len > cap - o) return ERR_OUTPUT;
-        // out[o + k] = out[o - d + k mod d]: reads only bytes written before
-        // this match, so the lanes copy in any order
-        const uint8_t *src = out + (o - d);
-        uint8_t *dst = out + o;
-        w.sync();
-        if (d >= len) {
-            for (uint32_t k = (uint32_t)w.lane; k < len; k += (uint32_t)w.n) dst[k] = src[k];
-        } else {
-            for (uint32_t k = (uint32_t)w.lane; k < len; k += (uint32_t)w.n) dst[k] = src[k % d];
-        }
-        o += len;
+        if (kind == K_EOB) return ERR_NONE;
+        if (kind == K_BAD) return ERR_SYMBOL;
+        const uint32_t len = ((e >> 8) & 0x1FF) + b.get((int)((e >> 20) & 15));
+        const uint32_t f = decode(b, t.dist_fast, kDistFast, t.dist_count, t.dist_sym, MAP_DIST);
+        if (!f) return ERR_CODE;
+        if (f & 0x30) return ERR_SYMBOL;
+        const uint32_t d = ((f >> 8) & 0x7FFF) + b.get((int)((f >> 24) & 15));
+        if (d > out.o) return ERR_DISTANCE;
+        if (len > out.cap - out.o) return ERR_OUTPUT;
+        out.copy(d, len, w);
     }
 }
 
 // Inflates the raw DEFLATE stream [in, in + n) into out[0, cap); returns an
 // ERR_* code (ERR_NONE when exactly `cap` bytes came out).
-RVZ_HD int inflate(const uint8_t *in, uint32_t n, const uint8_t *buf_end, uint8_t *out, uint32_t cap, Tables &t,
+RVZ_HD int inflate(const uint8_t *in, uint32_t n, const uint8_t *buf_end, uint8_t *dst, uint32_t cap, Tables &t,
                    const Lanes &w) {
     BitIn b;
     b.init(in, n, buf_end);
-    uint32_t o = 0;
+    Out out{dst, cap, 0u};
     int last = 0;
     do {
         last = (int)b.get(1);
@@ -273,21 +320,17 @@ RVZ_HD int inflate(const uint8_t *in, uint32_t n, const uint8_t *buf_end, uint8_
             b.drop(b.have & 7);
             const uint32_t len = b.get(16), nlen = b.get(16);
             if ((len ^ 0xFFFFu) != nlen) return ERR_STORED_LEN;
-            if (len > cap - o) return ERR_OUTPUT;
-            for (uint32_t k = 0; k < len; k++) {
-                const uint8_t v = (uint8_t)b.get(8);
-                if (w.lane == 0) out[o] = v;
-                o++;
-            }
+            if (len > cap - out.o) return ERR_OUTPUT;
+            for (uint32_t k = 0; k < len; k++) out.put((uint8_t)b.get(8), w);
         } else if (type == 1) {
             w.sync();
             for (int i = w.lane; i < 288; i += w.n) t.lens[i] = i < 144 ? 8 : (i < 256 ? 9 : (i < 280 ? 7 : 8));
             w.sync();
-            build(t.lens, 288, t.lit_fast, kLitFast, t.lit_count, t.lit_sym, w);
+            build(t.lens, 288, t.lit_fast, kLitFast, t.lit_count, t.lit_sym, MAP_LIT, w);
             for (int i = w.lane; i < 30; i += w.n) t.lens[i] = 5;
             w.sync();
-            build(t.lens, 30, t.dist_fast, kDistFast, t.dist_count, t.dist_sym, w);
-            const int e = codes(b, t, out, cap, o, w);
+            build(t.lens, 30, t.dist_fast, kDistFast, t.dist_count, t.dist_sym, MAP_DIST, w);
+            const int e = codes(b, t, out, w);
             if (e) return e;
         } else if (type == 2) {
             const int hlit = (int)b.get(5) + 257, hdist = (int)b.get(5) + 1, hclen = (int)b.get(4) + 4;
@@ -300,12 +343,13 @@ RVZ_HD int inflate(const uint8_t *in, uint32_t n, const uint8_t *buf_end, uint8_
             for (int i = w.lane; i < 19; i += w.n) t.lens[i] = cl[i];
             w.sync();
             // the code-length code borrows the distance tables
-            if (!build(t.lens, 19, t.dist_fast, kDistFast, t.dist_count, t.dist_sym, w)) return ERR_CODE;
+            if (!build(t.lens, 19, t.dist_fast, kDistFast, t.dist_count, t.dist_sym, MAP_RAW, w)) return ERR_CODE;
             int k = 0;
             uint8_t prev = 0;
             while (k < hlit + hdist) {
-                const int s = decode(b, t.dist_fast, kDistFast, t.dist_count, t.dist_sym);
-                if (s < 0) return ERR_CODE;
+                const uint32_t ce = decode(b, t.dist_fast, kDistFast, t.dist_count, t.dist_sym, MAP_RAW);
+                if (!ce) return ERR_CODE;
+                const int s = (int)(ce >> 8);
                 if (b.overrun() > 0) return ERR_INPUT;
                 if (s < 16) {
                     if (w.lane == 0) t.lens[k] = (uint8_t)s;
@@ -331,16 +375,16 @@ RVZ_HD int inflate(const uint8_t *in, uint32_t n, const uint8_t *buf_end, uint8_
             }
             w.sync();
             if (t.lens[256] == 0) return ERR_CODE;  // no end-of-block code
-            if (!build(t.lens, hlit, t.lit_fast, kLitFast, t.lit_count, t.lit_sym, w)) return ERR_CODE;
-            if (!build(t.lens + hlit, hdist, t.dist_fast, kDistFast, t.dist_count, t.dist_sym, w)) return ERR_CODE;
-            const int e = codes(b, t, out, cap, o, w);
+            if (!build(t.lens, hlit, t.lit_fast, kLitFast, t.lit_count, t.lit_sym, MAP_LIT, w)) return ERR_CODE;
+            if (!build(t.lens + hlit, hdist, t.dist_fast, kDistFast, t.dist_count, t.dist_sym, MAP_DIST, w)) return ERR_CODE;
+            const int e = codes(b, t, out, w);
             if (e) return e;
         } else {
             return ERR_BLOCK_TYPE;
         }
         if (b.overrun() > 0) return ERR_INPUT;
     } while (!last);
-    return o == cap ? ERR_NONE : ERR_SHORT;
+    return out.o == cap ? ERR_NONE : ERR_SHORT;
 }
 
 // ---------------------------------------------------------------------------
