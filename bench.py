@@ -18,7 +18,11 @@ classification, the hard filter, three Fisher tests per record and the
 Inputs (~0.5 GB of reads) exceed the 129 MB L2, so no flush is needed
 between steps.
 
+    e2e_from_bam : reads/s from BGZF-compressed BAM bytes in pinned host
+            memory: the BAM decode on the GPU, then the same calls
+
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
+    python bench.py --bam-decode      # BAM decode alone, GPU vs host decoder
 """
 from __future__ import annotations
 
@@ -308,6 +312,53 @@ def bam_leg(g, tumor, normal, regions, k: int, steps: int, warmup: int, device: 
             "note": "BGZF level-1 members of the synthetic BAMs in pinned host memory; decode + pileup + scoring + records"}
 
 
+def run_bam_decode(args):
+    """`--bam-decode`: BGZF/BAM decode of the workload's tumor sample (1.33 M
+    reads, BGZF level 1) on the GPU (rv_bam_reread_gpu into reused buffers,
+    then its contig batch) against the library's host decoder with all host
+    threads (rv_bam_read_mem + rv_bam_batch); one JSON line."""
+    import ctypes as C
+    from rabbitvar_gb300 import api, synth
+    g, tumor, normal, regions = make_workload()
+    payload = synth.bam_bytes(tumor, "T")
+    data = bgzf_bytes(payload)
+    L = api.lib()
+    ptr = L.rv_alloc_pinned(len(data))
+    C.memmove(ptr, data, len(data))
+    h = C.c_void_p()
+    if L.rv_bam_read_gpu(ptr, len(data), int(os.environ.get("LOCAL_RANK", "0")), C.byref(h)) != 0:
+        raise RuntimeError("rv_bam_read_gpu failed")
+    gpu = []
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        st = L.rv_bam_reread_gpu(h, ptr, len(data))
+        rb = api.ReadBatch()
+        st2 = L.rv_bam_batch(h, 0, C.byref(rb))
+        if st or st2 or rb.n_reads != tumor.n:
+            raise RuntimeError("device decode failed")
+        if i >= args.warmup:
+            gpu.append((time.perf_counter() - t0) * 1e3)
+    L.rv_bam_free(h)
+    host = []
+    for i in range(1 + min(args.steps, 3)):
+        t0 = time.perf_counter()
+        hh = C.c_void_p()
+        if L.rv_bam_read_mem(ptr, len(data), 0, C.byref(hh)) != 0:
+            raise RuntimeError("host decode failed")
+        rb = api.ReadBatch()
+        L.rv_bam_batch(hh, 0, C.byref(rb))
+        if i:
+            host.append((time.perf_counter() - t0) * 1e3)
+        L.rv_bam_free(hh)
+    L.rv_free_pinned(ptr)
+    gms, hms = statistics.median(gpu), statistics.median(host)
+    print(json.dumps({"metric": "BAM decode (BGZF inflate + records -> read batch)", "value": tumor.n / (gms * 1e-3),
+                      "unit": "reads/s", "ms": gms, "steps": args.steps, "warmup": args.warmup,
+                      "host_decoder": {"value": tumor.n / (hms * 1e-3), "ms": hms, "threads": os.cpu_count()},
+                      "bgzf_bytes": len(data), "stream_bytes": len(payload), "reads": tumor.n,
+                      "stream_GBps": len(payload) / (gms * 1e-3) / 1e9}))
+
+
 def learned_filter_leg():
     """The learned filter against the hard filter on the deep-panel shape:
     trained on 4 seeded panels, evaluated on 2 held-out ones (planted truth),
@@ -428,6 +479,8 @@ def main():
                     help="the reference's -k (default 1, as the reference): 0 leaves out the realigner's indel passes")
     ap.add_argument("--no-other-k", action="store_true", help="skip the leg with the other -k setting")
     ap.add_argument("--no-bam", action="store_true", help="skip the leg that starts from BGZF-compressed BAM bytes")
+    ap.add_argument("--bam-decode", action="store_true",
+                    help="only time the BAM decode of the tumor sample, GPU against the host decoder")
     ap.add_argument("--panel", type=int, default=0, metavar="N",
                     help="batched amplicon panel of N regions (-t -u): one launch for all regions vs one per region")
     args = ap.parse_args()
@@ -437,6 +490,9 @@ def main():
         return
     if args.panel:
         run_panel(args)
+        return
+    if args.bam_decode:
+        run_bam_decode(args)
         return
     import numpy as np
     from rabbitvar_gb300 import api, synth
