@@ -39,6 +39,41 @@ def test_bam_rejects_truncated(tmp_path, germline_small):
     assert e.value.status == -8
 
 
+def test_bam_read_mem_matches_file_decoder(tmp_path, germline_small):
+    """rv_bam_read_mem (bytes already in memory) decodes the same records as
+    rv_bam_read; bam_bytes' numpy records match a field-by-field rebuild."""
+    import ctypes as C
+    import struct
+    from rabbitvar_gb300 import api, synth
+    g, vs, rs = germline_small
+    bam = str(tmp_path / "s.bam")
+    synth.write_bam(bam, rs)
+    data = open(bam, "rb").read()
+    L = api.lib()
+    h = C.c_void_p()
+    buf = C.create_string_buffer(data, len(data))
+    assert L.rv_bam_read_mem(C.cast(buf, C.c_void_p), len(data), 2, C.byref(h)) == 0
+    try:
+        got = api._host_batches(L, h, L.rv_bam_batch)
+    finally:
+        L.rv_bam_free(h)
+    want = api.read_bam(bam, threads=2)
+    assert got[0] == want[0] and got[1] == want[1]
+    for k in ("pos", "flag", "mapq", "mpos", "nm", "n_cigar", "cig_off", "cigar", "l_qseq", "base_off"):
+        assert np.array_equal(got[2][0].arrays[k], want[2][0].arrays[k]), k
+    # first record rebuilt field by field
+    stream = synth.bam_bytes(rs, "S")
+    q = 8 + struct.unpack("<I", stream[4:8])[0]        # magic, l_text, text
+    q += 4 + 4 + len(rs.contig) + 1 + 4                 # n_ref, l_name, name, l_ref
+    bs = struct.unpack("<I", stream[q:q + 4])[0]
+    tid, pos, lrn, mapq, _bin, nc, flag, lq, ntid, npos, tlen = struct.unpack("<iiBBHHHiiii", stream[q + 4:q + 36])
+    assert (tid, pos, mapq, nc, flag, lq, npos, tlen) == (0, int(rs.pos[0]), int(rs.mapq[0]), int(rs.n_cigar[0]),
+                                                          int(rs.flag[0]), int(rs.l_qseq[0]), int(rs.mpos[0]),
+                                                          int(rs.isize[0]))
+    assert stream[q + 36:q + 36 + lrn] == b"r%d\x00" % int(rs.name_id[0])
+    assert bs == 32 + lrn + 4 * nc + (lq + 1) // 2 + lq + 7
+
+
 def test_fasta(tmp_path, germline_small):
     from rabbitvar_gb300 import api, synth
     g, vs, rs = germline_small
