@@ -254,8 +254,24 @@ rv_status rv_last_timings(const rv_ctx *ctx, double *pileup_ms, double *score_ms
  * stages: [0] cell/table reset, [1] region spans, [2] pileup tiles,
  * [3] in-order edge walk, [4] deferred subtraction + list linking +
  * collision check, [5] insertion coverage adjustment, [6] site scoring;
- * [7] the pileup kernel variant the autotuner used (not a time). */
+ * [7] the pileup kernel variant the autotuner used (not a time).
+ * Stages [0]-[4] read 0 after a pileup launched as a graph. */
 rv_status rv_stage_times(const rv_ctx *ctx, double *ms, int n);
+
+/* Batched-region form of CigarParser::process (src/parseCigar.cpp:410-440)
+ * under a CUDA graph: with enable != 0, rv_pileup captures its chain of
+ * memsets and kernels (table resets, edge detection, the persistent tile
+ * kernel fed from the device tile queue, in-order edge walk, deferred
+ * subtraction, list linking, collision check) into a graph and launches that,
+ * once the autotuner has settled on a kernel variant.  Each batch's chain is
+ * applied to the previous executable graph with cudaGraphExecUpdate; a new
+ * one is instantiated only when the update is refused.  The stream must not
+ * be the legacy default stream (NULL selects the context's own stream).
+ * Results are the same as without the graph. */
+rv_status rv_set_pileup_graph(rv_ctx *ctx, int enable);
+
+/* Graph launches and graph instantiations of rv_pileup since rv_create. */
+rv_status rv_pileup_graph_stats(const rv_ctx *ctx, int64_t *launches, int64_t *instantiations);
 
 /* Bytes copied host->device by the last rv_submit_batch and device->host
  * by the calls since then (realigner boundary, scored candidates). */

@@ -73,7 +73,7 @@ class SiteRecord(C.Structure):
 
 EXPORTS = ["rv_default_params", "rv_create", "rv_destroy", "rv_last_error", "rv_upload_reference",
            "rv_submit_batch", "rv_pileup", "rv_realign", "rv_score", "rv_format_records", "rv_fetch_records",
-           "rv_call_regions", "rv_score_candidates", "rv_candidates", "rv_score_pair", "rv_pileup_realign_pair", "rv_format_somatic", "rv_call_somatic", "rv_call_somatic_stream", "rv_export_maps", "rv_last_timings", "rv_stage_times", "rv_io_bytes", "rv_fisher_batch", "rv_bam_read",
+           "rv_call_regions", "rv_score_candidates", "rv_candidates", "rv_score_pair", "rv_pileup_realign_pair", "rv_format_somatic", "rv_call_somatic", "rv_call_somatic_stream", "rv_export_maps", "rv_last_timings", "rv_stage_times", "rv_set_pileup_graph", "rv_pileup_graph_stats", "rv_io_bytes", "rv_fisher_batch", "rv_bam_read",
            "rv_bam_contigs", "rv_bam_batch", "rv_bam_read_mem", "rv_bam_read_gpu", "rv_bam_reread_gpu", "rv_bam_batch_host", "rv_bam_free", "rv_fasta_read", "rv_free", "rv_alloc_pinned",
            "rv_free_pinned", "rv_mlp_create", "rv_mlp_destroy", "rv_mlp_last_error", "rv_mlp_set_params",
            "rv_mlp_get_params", "rv_mlp_train", "rv_mlp_gradients", "rv_mlp_predict", "rv_mlp_step_ms"]
@@ -116,6 +116,8 @@ def lib():
                                   C.POINTER(i64)]
     L.rv_fisher_batch.argtypes = [vp, vp, i64, vp, vp]
     L.rv_stage_times.argtypes = [vp, vp, C.c_int]
+    L.rv_set_pileup_graph.argtypes = [vp, C.c_int]
+    L.rv_pileup_graph_stats.argtypes = [vp, C.POINTER(i64), C.POINTER(i64)]
     L.rv_io_bytes.argtypes = [vp, C.POINTER(i64), C.POINTER(i64)]
     L.rv_bam_read.argtypes = [C.c_char_p, C.c_int, C.POINTER(vp)]
     L.rv_bam_contigs.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(vp), C.POINTER(vp)]
@@ -287,6 +289,17 @@ class Context:
         ms = np.zeros(8)
         self._check(self.L.rv_stage_times(self.h, ms.ctypes.data, 8))
         return {k: float(ms[i]) for i, k in enumerate(self.STAGES)}
+
+    def set_pileup_graph(self, enable: bool = True):
+        """rv_pileup launches its kernel chain as a CUDA graph once the
+        kernel variant is settled."""
+        self._check(self.L.rv_set_pileup_graph(self.h, int(bool(enable))))
+
+    def pileup_graph_stats(self) -> tuple[int, int]:
+        """(graph launches, graph instantiations) since the context was made."""
+        a, b = C.c_int64(), C.c_int64()
+        self._check(self.L.rv_pileup_graph_stats(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
 
     def score_candidates(self, min_count: int = 2):
         self._check(self.L.rv_score_candidates(self.h, min_count))

@@ -317,6 +317,7 @@ void rv_destroy(rv_ctx *ctx) {
     for (int i = 0; i < 12; i++)
         if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
     if (ctx->ev_block) cudaEventDestroy(ctx->ev_block);
+    if (ctx->pileup_exec) cudaGraphExecDestroy(ctx->pileup_exec);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -681,29 +682,81 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
 
 namespace {
 
-// Queues the pileup kernels of the submitted batch on stream s without
-// waiting for them; pileup_finish waits and reads the device error word.
-rv_status pileup_launch(rv_ctx *ctx, cudaStream_t s) {
-    if (ctx->stage < 1) { ctx->err = "rv_pileup before rv_submit_batch"; return RV_ERR_STATE; }
-    RV_CUDA(cudaSetDevice(ctx->device));
+// The memsets and kernels of one pileup, queued on s; `marks` records the
+// per-stage events (left out when the chain is captured into a graph).
+rv_status queue_pileup_chain(rv_ctx *ctx, cudaStream_t s, int grid, int variant, bool marks) {
     size_t cap = ctx->cap_cells;
-    RV_CUDA(cudaEventRecord(ctx->ev[0], s));
     RV_CUDA(cudaMemsetAsync(ctx->d_cellmem, 0, cap * (8 * 16 + 4 + 1), s));
     RV_CUDA(cudaMemsetAsync(ctx->d_head, 0xFF, cap * 8, s));
     RV_CUDA(cudaMemsetAsync(ctx->d_counters, 0, 64 * sizeof(unsigned int), s));
     RV_CUDA(cudaMemsetAsync(ctx->d_arena, 0, 16, s));
     launch_init_slots(ctx->d_slots, ctx->hash_cap, s);
     DevState st = ctx->state();
-    RV_CUDA(cudaEventRecord(ctx->ev[4], s));
+    if (marks) RV_CUDA(cudaEventRecord(ctx->ev[4], s));
     launch_region_reset(st, s);
     launch_edge_detect(st, ctx->dp, s);
-    RV_CUDA(cudaEventRecord(ctx->ev[5], s));
+    if (marks) RV_CUDA(cudaEventRecord(ctx->ev[5], s));
+    RV_CUDA(launch_pileup(st, ctx->dp, grid, s, variant));
+    if (marks) RV_CUDA(cudaEventRecord(ctx->ev[6], s));
+    launch_serial(st, ctx->dp, s);
+    if (marks) RV_CUDA(cudaEventRecord(ctx->ev[7], s));
+    launch_resolve(st, ctx->dp, s);
+    launch_link(st, s);
+    launch_collisions(st, s);
+    RV_CUDA(cudaGetLastError());
+    return RV_OK;
+}
+
+// The same chain through the context's executable graph: captured from s,
+// applied to the graph of the previous batch by cudaGraphExecUpdate (kernel
+// arguments, grids and memset sizes may change between batches), instantiated
+// again when the update is refused, then launched on s.
+rv_status launch_pileup_graph(rv_ctx *ctx, cudaStream_t s, int grid, int variant) {
+    cudaGraph_t g = nullptr;
+    RV_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
+    rv_status st = queue_pileup_chain(ctx, s, grid, variant, false);
+    cudaError_t e = cudaStreamEndCapture(s, &g);
+    if (st != RV_OK) {
+        if (g) cudaGraphDestroy(g);
+        return st;
+    }
+    if (e != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        ctx->err = std::string("pileup graph capture: ") + cudaGetErrorString(e);
+        return RV_ERR_CUDA;
+    }
+    if (ctx->pileup_exec) {
+        cudaGraphExecUpdateResultInfo info;
+        if (cudaGraphExecUpdate(ctx->pileup_exec, g, &info) != cudaSuccess) {
+            (void)cudaGetLastError();  // a refused update is not an error: instantiate anew
+            cudaGraphExecDestroy(ctx->pileup_exec);
+            ctx->pileup_exec = nullptr;
+        }
+    }
+    if (!ctx->pileup_exec) {
+        e = cudaGraphInstantiate(&ctx->pileup_exec, g, 0);
+        if (e == cudaSuccess) ctx->graph_instantiations++;
+        else ctx->pileup_exec = nullptr;
+    }
+    cudaGraphDestroy(g);
+    RV_CUDA(e);
+    RV_CUDA(cudaGraphLaunch(ctx->pileup_exec, s));
+    ctx->graph_launches++;
+    return RV_OK;
+}
+
+// Queues the pileup kernels of the submitted batch on stream s without
+// waiting for them; pileup_finish waits and reads the device error word.
+rv_status pileup_launch(rv_ctx *ctx, cudaStream_t s) {
+    if (ctx->stage < 1) { ctx->err = "rv_pileup before rv_submit_batch"; return RV_ERR_STATE; }
+    RV_CUDA(cudaSetDevice(ctx->device));
     // autotuner: unless RV_PILEUP_VARIANT pins one, the first batches try each
     // kernel variant once and later batches use the fastest seen
     int nvar = pileup_variants();
     int variant;
     const char *pin = getenv("RV_PILEUP_VARIANT");
-    if (pin && *pin) variant = std::max(0, std::min(nvar - 1, atoi(pin)));
+    const bool pinned = pin && *pin;
+    if (pinned) variant = std::max(0, std::min(nvar - 1, atoi(pin)));
     else if (ctx->variant_runs < nvar) variant = ctx->variant_runs;
     else {
         variant = 0;
@@ -713,17 +766,17 @@ rv_status pileup_launch(rv_ctx *ctx, cudaStream_t s) {
     ctx->variant = variant;
     int per_sm = std::max(1, pileup_blocks_per_sm(variant));
     int grid = std::max(1, std::min<int>((int)ctx->tiles.size(), per_sm * ctx->sm_count));
-    RV_CUDA(launch_pileup(st, ctx->dp, grid, s, variant));
-    RV_CUDA(cudaEventRecord(ctx->ev[6], s));
-    launch_serial(st, ctx->dp, s);
-    RV_CUDA(cudaEventRecord(ctx->ev[7], s));
-    launch_resolve(st, ctx->dp, s);
-    launch_link(st, s);
-    launch_collisions(st, s);
-    RV_CUDA(cudaGetLastError());
+    // a graph once the variant is settled (the autotuner's trial runs need
+    // the per-stage events); the legacy default stream cannot be captured
+    const bool graphed = ctx->use_graph && s != nullptr && (pinned || ctx->variant_runs >= nvar);
+    RV_CUDA(cudaEventRecord(ctx->ev[0], s));
+    rv_status qs = graphed ? launch_pileup_graph(ctx, s, grid, variant)
+                           : queue_pileup_chain(ctx, s, grid, variant, true);
+    if (qs != RV_OK) return qs;
     RV_CUDA(cudaEventRecord(ctx->ev[1], s));
+    ctx->pileup_graphed = graphed;
     ctx->kernels = 8;  // init_slots, region_spans, edge_detect, pileup_tiles, serial, resolve, link, collisions
-    ctx->pileup_pin = pin && *pin;
+    ctx->pileup_pin = pinned;
     ctx->mirror_pending = false;
     ctx->stage = 1;  // launched, not finished
     ctx->pileup_pending = true;
@@ -742,14 +795,19 @@ rv_status pileup_finish(rv_ctx *ctx, cudaStream_t s) {
     float ms = 0;
     cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
     ctx->pileup_ms = ms;
-    const int marks[5] = {0, 4, 5, 6, 7};
-    for (int k = 0; k < 4; k++) {
-        float m = 0;
-        cudaEventElapsedTime(&m, ctx->ev[marks[k]], ctx->ev[marks[k + 1]]);
-        ctx->stage_ms[k] = m;
+    if (ctx->pileup_graphed) {
+        // no per-stage events inside the graph: only the whole chain is timed
+        for (int k = 0; k < 5; k++) ctx->stage_ms[k] = 0;
+    } else {
+        const int marks[5] = {0, 4, 5, 6, 7};
+        for (int k = 0; k < 4; k++) {
+            float m = 0;
+            cudaEventElapsedTime(&m, ctx->ev[marks[k]], ctx->ev[marks[k + 1]]);
+            ctx->stage_ms[k] = m;
+        }
+        cudaEventElapsedTime(&ms, ctx->ev[7], ctx->ev[1]);
+        ctx->stage_ms[4] = ms;
     }
-    cudaEventElapsedTime(&ms, ctx->ev[7], ctx->ev[1]);
-    ctx->stage_ms[4] = ms;
     if (!ctx->pileup_pin && ctx->variant_runs < nvar) {
         ctx->variant_ms[variant] = ctx->stage_ms[2];
         ctx->variant_runs++;
@@ -1163,6 +1221,20 @@ rv_status rv_stage_times(const rv_ctx *ctx, double *ms, int n) {
     if (!ctx || !ms || n < 0) return RV_ERR_ARG;
     for (int i = 0; i < n && i < 8; i++) ms[i] = ctx->stage_ms[i];
     if (n > 7) ms[7] = ctx->variant;
+    return RV_OK;
+}
+
+rv_status rv_set_pileup_graph(rv_ctx *ctx, int enable) {
+    if (!ctx) return RV_ERR_ARG;
+    if (ctx->pileup_pending) { ctx->err = "rv_set_pileup_graph while a pileup is in flight"; return RV_ERR_STATE; }
+    ctx->use_graph = enable != 0;
+    return RV_OK;
+}
+
+rv_status rv_pileup_graph_stats(const rv_ctx *ctx, int64_t *launches, int64_t *instantiations) {
+    if (!ctx) return RV_ERR_ARG;
+    if (launches) *launches = ctx->graph_launches;
+    if (instantiations) *instantiations = ctx->graph_instantiations;
     return RV_OK;
 }
 

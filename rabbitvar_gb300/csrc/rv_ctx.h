@@ -220,6 +220,13 @@ struct rv_ctx {
     int variant_runs = 0;
     bool pileup_pin = false;       // RV_PILEUP_VARIANT pinned the variant of the pileup in flight
     bool pileup_pending = false;   // pileup queued, not yet finished
+    // pileup chain as a CUDA graph (rv_set_pileup_graph): each batch's chain
+    // is captured and applied to one executable graph with cudaGraphExecUpdate
+    // (instantiated again only when the update is refused)
+    bool use_graph = false;
+    bool pileup_graphed = false;   // the pileup in flight was launched as a graph
+    cudaGraphExec_t pileup_exec = nullptr;
+    int64_t graph_launches = 0, graph_instantiations = 0;
     int64_t kernels = 0;
     // bytes moved host<->device since the last rv_submit_batch
     int64_t io_h2d = 0, io_d2h = 0;
