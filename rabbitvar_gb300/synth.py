@@ -405,6 +405,104 @@ def _pack(contig, G, order, pos, flag, mapq, mpos, isize, nm, cig_list, codes, q
                    seq4=seq4, qual=qv, name_id=names[order].astype(np.int64))
 
 
+_OPS = {"M": 0, "I": 1, "D": 2, "N": 3, "S": 4, "H": 5}
+_BASE = {"A": 0, "C": 1, "G": 2, "T": 3}
+
+
+def explicit_reads(contig: str, genome: np.ndarray, reads: list[dict]) -> ReadSet:
+    """A read set written out read by read, for cases that pin one code path.
+
+    Each read is a dict: `pos` (0-based leftmost reference base the CIGAR
+    starts at) and `segs`, a list of CIGAR segments:
+      ("M", n) or ("M", n, {offset: "ACGTN"})  aligned bases, substitutions at
+                                              offsets within the segment
+      ("I", "ACG")                            inserted bases
+      ("D", n) / ("N", n)                     reference skipped
+      ("S", "ACG")                            clipped bases as given
+      ("S", n)                                clipped bases copied from the
+                                              reference beside the clip
+      ("H", n)                                hard clip (no bases)
+    and optionally `qual` (an int for every base, or a list), `qual_at`
+    ({read offset: Phred}), `rev` (reverse strand), `flag`, `mapq`, `mpos`
+    and `nm` (default: substitutions + inserted + deleted bases).  Reads are
+    sorted by position (stable), as a coordinate-sorted BAM holds them.
+    """
+    G = int(genome.shape[0])
+    recs = []
+    for i, r in enumerate(reads):
+        pos = int(r["pos"])
+        rp = pos
+        codes, cig = [], []
+        nm = 0
+        segs = r["segs"]
+        for j, sg in enumerate(segs):
+            op = sg[0]
+            if op == "M":
+                n = int(sg[1])
+                subs = sg[2] if len(sg) > 2 else {}
+                for k in range(n):
+                    if k in subs:
+                        b = subs[k]
+                        c = CODE_N if b == "N" else int(CODE_OF[_BASE[b]])
+                        if b == "N" or _BASE[b] != int(genome[rp + k]):
+                            nm += 1
+                    else:
+                        c = int(CODE_OF[int(genome[rp + k])])
+                    codes.append(c)
+                rp += n
+            elif op == "I":
+                codes += [int(CODE_OF[_BASE[b]]) for b in sg[1]]
+                nm += len(sg[1])
+                n = len(sg[1])
+            elif op in ("D", "N"):
+                n = int(sg[1])
+                rp += n
+                if op == "D":
+                    nm += n
+            elif op == "S":
+                if isinstance(sg[1], str):
+                    codes += [CODE_N if b == "N" else int(CODE_OF[_BASE[b]]) for b in sg[1]]
+                    n = len(sg[1])
+                else:
+                    n = int(sg[1])
+                    at = pos - n if j == 0 or all(x[0] == "H" for x in segs[:j]) else rp
+                    codes += [int(CODE_OF[int(genome[at + k])]) for k in range(n)]
+            elif op == "H":
+                n = int(sg[1])
+            else:
+                raise ValueError(op)
+            cig.append((n << 4) | _OPS[op])
+        L = len(codes)
+        q = r.get("qual", 37)
+        qual = list(q) if not isinstance(q, int) else [q] * L
+        for k, v in r.get("qual_at", {}).items():
+            qual[k] = v
+        assert len(qual) == L and rp <= G
+        flag = r.get("flag", 0x1 | 0x2 | (0x10 if r.get("rev") else 0x20) | 0x40)
+        recs.append((pos, i, flag, r.get("mapq", 60), r.get("mpos", pos + 200), r.get("nm", nm), cig, codes, qual))
+    recs.sort(key=lambda t: (t[0], t[1]))
+    n = len(recs)
+    stride = max([32] + [(len(t[7]) + 31) // 32 * 32 for t in recs])
+    seq4 = np.zeros(n * stride, np.uint8)
+    qv = np.zeros(n * stride, np.uint8)
+    for k, t in enumerate(recs):
+        seq4[k * stride:k * stride + len(t[7])] = t[7]
+        qv[k * stride:k * stride + len(t[8])] = t[8]
+    n_cigar = np.array([len(t[6]) for t in recs], np.uint16)
+    cig_off = np.zeros(n, np.uint32)
+    if n:
+        cig_off[1:] = np.cumsum(n_cigar[:-1].astype(np.uint32))
+    pos = np.array([t[0] for t in recs], np.int32)
+    mpos = np.array([t[4] for t in recs], np.int32)
+    return ReadSet(contig=contig, contig_len=G, pos=pos, flag=np.array([t[2] for t in recs], np.uint16),
+                   mapq=np.array([t[3] for t in recs], np.uint8), mpos=mpos, isize=(mpos - pos + 150).astype(np.int32),
+                   nm=np.array([t[5] for t in recs], np.int32), n_cigar=n_cigar, cig_off=cig_off,
+                   cigar=np.array([w for t in recs for w in t[6]], np.uint32),
+                   l_qseq=np.array([len(t[7]) for t in recs], np.int32),
+                   base_off=np.arange(n, dtype=np.uint64) * stride, seq4=seq4, qual=qv,
+                   name_id=np.array([t[1] for t in recs], np.int64))
+
+
 # --------------------------------------------------------------------------
 # writers (BGZF/BAM per SAM spec 4.1-4.2, FASTA + .fai, BED)
 # --------------------------------------------------------------------------

@@ -10,7 +10,8 @@ fingerprint of the generated reads so a change of the generator is reported
 as such rather than as a parity failure.  The somatic cases (a tumor/normal
 pair run in the reference's somatic mode) keep the emitted records only.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py             # every case
+    python tests/golden/make_golden.py paths_k0    # only the named cases
 """
 from __future__ import annotations
 
@@ -76,8 +77,89 @@ def case_germline_dense_k1():
     return g, rs, region, ["-k", "1"]
 
 
+def _path_reads():
+    """Hand-written reads over an 8 kb contig, one locus per pileup code path,
+    on a background of reference reads (depth ~12, both strands).  Every read
+    set below would change the maps or records if its path were handled
+    differently: MNV growth and its quality stop (parseCigar.cpp:711-767),
+    deletions and their flank-quality rule (:1525-1727), insertions shifted
+    3' in a homopolymer and after a leading soft clip (:1303-1523), soft
+    clips that match the reference and ones with low-quality stops
+    (:1112-1301), mismatches next to indels (complex tails, :779-882),
+    record filters (recordPreprocessor.cpp:101-180; parseCigar.cpp:517-606),
+    hard clips, N bases and low base/mapping qualities."""
+    rng = np.random.default_rng(0x60D7)
+    g = synth.make_genome(8_000, rng)
+    g[1_500:1_508] = 0  # an A homopolymer for the insertion shift
+    other = lambda p: "ACGT"[(int(g[p]) + 1) % 4]  # noqa: E731
+    reads = [{"pos": p, "segs": [("M", 150)], "rev": (p // 12) % 2 == 1} for p in range(0, 8_000 - 150, 12)]
+
+    def add(starts, segs_of, **kw):
+        for j, p in enumerate(starts):
+            reads.append(dict(pos=p, segs=segs_of(p), rev=j % 2 == 1, **kw))
+
+    # MNV: two adjacent mismatches, a gap of one matching base, a low-quality second base
+    add([440, 455, 470, 480], lambda p: [("M", 150, {500 - p: other(500), 501 - p: other(501)})])
+    add([540, 560, 575], lambda p: [("M", 150, {600 - p: other(600), 602 - p: other(602)})])
+    for p in (640, 655, 670):
+        reads.append({"pos": p, "segs": [("M", 150, {700 - p: other(700), 701 - p: other(701)})],
+                      "qual_at": {701 - p: 14}})
+    # deletion with unequal flank qualities; a longer deletion
+    for j, p in enumerate((940, 950, 965, 975)):
+        reads.append({"pos": p, "segs": [("M", 1000 - p), ("D", 3), ("M", 150 - (1000 - p))],
+                      "qual_at": {1000 - p - 1: 20 + 5 * j}, "rev": j % 2 == 0})
+    add([1040, 1062], lambda p: [("M", 1100 - p), ("D", 9), ("M", 150 - (1100 - p))])
+    # insertion inside the homopolymer (shifted 3'); insertion after a leading soft clip
+    add([1440, 1452, 1466], lambda p: [("M", 1503 - p), ("I", "A"), ("M", 149 - (1503 - p))])
+    add([1700, 1700], lambda p: [("S", 5), ("I", "GT"), ("M", 143)])
+    # soft clips: matching the reference (3' and 5'), foreign bases with low-quality stops
+    add([1900, 1910, 1920], lambda p: [("M", 2000 - p), ("S", 150 - (2000 - p))])
+    add([2050, 2060], lambda p: [("S", 25), ("M", 125)])
+    for p in (2150, 2160, 2170):
+        clip = "".join(other(2250 + k) for k in range(30))
+        reads.append({"pos": p, "segs": [("M", 2250 - p), ("S", clip)],
+                      "qual_at": {2250 - p + 4: 11, 2250 - p + 9: 8}})
+    # mismatch two bases before a deletion; mismatch just after an insertion
+    add([2440, 2455, 2470], lambda p: [("M", 2500 - p, {2498 - p: other(2498)}), ("D", 2),
+                                       ("M", 148 - (2500 - p))])
+    add([2640, 2652, 2664], lambda p: [("M", 2700 - p), ("I", "GT"),
+                                       ("M", 148 - (2700 - p), {1: other(2701)})])
+    # record filters: flags 0x4/0x100/0x400/0x800, a one-base read, too many mismatches,
+    # both ends clipped >= 10; each would add an SNV at 3000 if it were counted
+    snv = lambda p: {3000 - p: other(3000)}  # noqa: E731
+    for f in (0x4 | 0x1, 0x100 | 0x1, 0x400 | 0x1, 0x800 | 0x1):
+        reads.append({"pos": 2950, "segs": [("M", 150, snv(2950))], "flag": f})
+    reads.append({"pos": 2999, "segs": [("M", 1)]})
+    reads.append({"pos": 2940, "segs": [("M", 150, {**snv(2940), **{k: other(2940 + k) for k in range(20, 29)}})]})
+    reads.append({"pos": 2930, "segs": [("S", 12), ("M", 126, snv(2930 + 12)), ("S", 12)]})
+    # counted: MAPQ 0, a hard clip, an N base, low base quality (below goodq)
+    add([3140, 3150], lambda p: [("M", 150, {3200 - p: other(3200)})], mapq=0)
+    add([3160, 3170], lambda p: [("H", 10), ("M", 140, {3200 - p: other(3200)})])
+    add([3340, 3350, 3360], lambda p: [("M", 150, {3400 - p: "N"})])
+    for p in (3540, 3550, 3560):
+        reads.append({"pos": p, "segs": [("M", 150, {3600 - p: other(3600)})], "qual_at": {3600 - p: 15}})
+    # CIGAR shapes the -k 1 rewrite acts on: leading/trailing insertion, close indels,
+    # a short match block before a soft clip
+    add([3800, 3810], lambda p: [("I", "TT"), ("M", 148)])
+    add([3900, 3910], lambda p: [("M", 148), ("I", "CC")])
+    add([4040, 4052, 4064], lambda p: [("M", 4100 - p), ("D", 2), ("M", 4), ("I", "GA"), ("M", 144 - (4100 - p))])
+    add([4240, 4250], lambda p: [("M", 4300 - p), ("D", 1), ("M", 3), ("S", 150 - (4300 - p) - 3)])
+    return g, synth.explicit_reads("ctg", g, reads)
+
+
+def case_paths_k0():
+    g, rs = _path_reads()
+    return g, rs, (1, 8_000), ["-k", "0", "--fisher"]
+
+
+def case_paths_k1():
+    g, rs = _path_reads()
+    return g, rs, (1, 8_000), ["-k", "1"]
+
+
 CASES = {"germline_dense": case_germline_dense, "contig_end": case_contig_end, "unique_fisher": case_unique_fisher,
-         "dedup": case_dedup, "germline_dense_k1": case_germline_dense_k1}
+         "dedup": case_dedup, "germline_dense_k1": case_germline_dense_k1, "paths_k0": case_paths_k0,
+         "paths_k1": case_paths_k1}
 
 
 # records only
@@ -120,12 +202,18 @@ def readset_fingerprint(rs) -> str:
     return h.hexdigest()
 
 
-def main():
+def main(only=()):
+    """Regenerate every case, or only the named ones (their golden.json
+    entries are replaced, the others kept)."""
     import oracle as O
     if not O.have_reference():
         raise SystemExit("oracle/_ref is not built (needs the reference tree): make -C oracle ref")
     meta = {}
-    for name, fn in CASES.items():
+    if only:
+        with open(os.path.join(HERE, "golden.json")) as f:
+            meta = json.load(f)
+    pick = lambda d: {k: v for k, v in d.items() if not only or k in only}  # noqa: E731
+    for name, fn in pick(CASES).items():
         g, rs, (a, b), flags = fn()
         with tempfile.TemporaryDirectory() as td:
             bam = os.path.join(td, "s.bam")
@@ -144,7 +232,7 @@ def main():
         meta[name] = {"region": [a, b], "flags": flags, "reads": rs.n, "fingerprint": readset_fingerprint(rs),
                       "records": len(recs)}
         print(name, rs.n, "reads", len(recs), "records")
-    for name, fn in RECORDS_ONLY.items():
+    for name, fn in pick(RECORDS_ONLY).items():
         g, rs, (a, b), flags = fn()
         with tempfile.TemporaryDirectory() as td:
             bam = os.path.join(td, "s.bam")
@@ -157,7 +245,7 @@ def main():
         meta[name] = {"records_only": True, "region": [a, b], "flags": flags, "reads": rs.n,
                       "fingerprint": readset_fingerprint(rs), "records": len(recs)}
         print(name, rs.n, "reads", len(recs), "records")
-    for name, fn in SOMATIC.items():
+    for name, fn in pick(SOMATIC).items():
         g, t, n, (a, b), flags = fn()
         with tempfile.TemporaryDirectory() as td:
             tb, nb, fa = (os.path.join(td, x) for x in ("T.bam", "N.bam", "ref.fa"))
@@ -176,4 +264,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(tuple(sys.argv[1:]))
