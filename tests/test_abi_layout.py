@@ -1,0 +1,63 @@
+"""The C ABI as its callers see it, without a GPU.
+
+A C compiler lays out every public struct of include/rvgpu.h; the ctypes
+mirrors in rabbitvar_gb300/api.py must have the same size and field offsets
+(a mismatch would hand the library shifted fields).  rv_default_params must
+give RabbitVar's Configuration defaults (include/Configuration.h)."""
+import os
+import shutil
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _structs():
+    from rabbitvar_gb300 import api
+    return {"rv_params": api.Params, "rv_read_batch": api.ReadBatch, "rv_region": api.Region,
+            "rv_site_record": api.SiteRecord, "rv_somatic_job": api.SomaticJob, "rv_candidate": api.Candidate}
+
+
+def test_struct_layouts_match_ctypes_mirrors(tmp_path):
+    import ctypes as C
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    structs = _structs()
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "rvgpu.h"', "int main(void) {"]
+    for cname, cls in structs.items():
+        lines.append(f'    printf("{cname} sizeof %zu\\n", sizeof({cname}));')
+        for fname, _ in cls._fields_:
+            lines.append(f'    printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["    return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c99", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)],
+                   check=True, capture_output=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    seen = 0
+    for line in filter(None, out):
+        cname, fname, value = line.split()
+        cls = structs[cname]
+        want = C.sizeof(cls) if fname == "sizeof" else getattr(cls, fname).offset
+        assert int(value) == want, f"{cname}.{fname}: C {value}, ctypes {want}"
+        seen += 1
+    assert seen == sum(len(c._fields_) + 1 for c in structs.values())
+
+
+def test_default_params_are_the_reference_defaults():
+    from rabbitvar_gb300 import api
+    p = api.default_params()
+    # include/Configuration.h: goodq :173, vext :177, mismatch :165, -k :185,
+    # freq :210, minr :201, readPosFilter :228, qratio :232, mapq :236,
+    # mappingQuality :157, lofreq :244, bias :193, minBiasReads :197,
+    # samfilter "0x504" :219, referenceExtension :320, SVMINLEN :316;
+    # the flags (-x -T -M -t -u -UN -p --fisher -3) default to off
+    want = dict(goodq=22.5, vext=2, mismatch=8, local_realign=1, freq=0.01, minr=2, read_pos_filter=5, qratio=1.5,
+                mapq_filter=0.0, min_mapq=0, lofreq=0.05, bias=0.05, min_bias_reads=2, samfilter=0x504,
+                ref_extension=1200, extend_nt=0, trim_bases_after=0, minmatch=0, dedup=0, unique_fwd=0,
+                unique_first=0, do_pileup=0, fisher=0, move_indels_3=0, svminlen=1000, somatic=0)
+    assert {k: getattr(p, k) for k in want} == want
+    assert {f for f, _ in api.Params._fields_} == set(want)
