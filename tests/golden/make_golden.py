@@ -157,9 +157,56 @@ def case_paths_k1():
     return g, rs, (1, 8_000), ["-k", "1"]
 
 
+def _cigar_rule_reads():
+    """Hand-written reads whose CIGARs hit each rule of the -k 1 CIGAR rewrite
+    (cigarModifier.cpp:219-380, patterns include/patterns.h:52-122), three
+    copies per shape (two strands) on a background of reference reads: a clip
+    followed by an indel at either end, a short match block between a clip and
+    an indel, a 1-9 base match block before/after an indel at either end, three
+    close deletions, three close indels, insertion-match-deletion, adjacent
+    deletions, adjacent insertions, and mismatches next to a clip or at the
+    read ends (the rules applied after the loop)."""
+    rng = np.random.default_rng(0x60D8)
+    g = synth.make_genome(8_000, rng)
+    other = lambda p: "ACGT"[(int(g[p]) + 1) % 4]  # noqa: E731
+    reads = [{"pos": p, "segs": [("M", 150)], "rev": (p // 12) % 2 == 1} for p in range(0, 8_000 - 150, 12)]
+    shapes = [
+        lambda p: [("S", 10), ("I", "GTA"), ("M", 137)],
+        lambda p: [("S", 10), ("D", 3), ("M", 140)],
+        lambda p: [("M", 137), ("I", "CAG"), ("S", 10)],
+        lambda p: [("M", 140), ("D", 3), ("S", 10)],
+        lambda p: [("S", 10), ("M", 8), ("I", "TG"), ("M", 130)],
+        lambda p: [("S", 10), ("M", 8), ("D", 2), ("M", 132)],
+        lambda p: [("M", 130), ("I", "TG"), ("M", 8), ("S", 10)],
+        lambda p: [("M", 5), ("D", 2), ("M", 145)],
+        lambda p: [("M", 5), ("I", "AC"), ("M", 143)],
+        lambda p: [("M", 143), ("I", "AC"), ("M", 5)],
+        lambda p: [("M", 145), ("D", 2), ("M", 5)],
+        lambda p: [("M", 50), ("D", 2), ("M", 3), ("D", 2), ("M", 3), ("D", 2), ("M", 94)],
+        lambda p: [("M", 50), ("D", 2), ("M", 3), ("I", "TT"), ("M", 3), ("D", 1), ("M", 92)],
+        lambda p: [("M", 60), ("I", "GG"), ("M", 4), ("D", 3), ("M", 84)],
+        lambda p: [("M", 60), ("D", 2), ("D", 3), ("M", 90)],
+        lambda p: [("M", 60), ("I", "AC"), ("I", "GTA"), ("M", 85)],
+        lambda p: [("M", 140, {137: other(p + 137), 138: other(p + 138)}), ("S", 10)],
+        lambda p: [("S", 10), ("M", 140, {2: other(p + 2), 3: other(p + 3)})],
+        lambda p: [("M", 150, {1: other(p + 1), 2: other(p + 2)})],
+        lambda p: [("M", 150, {146: other(p + 146), 148: other(p + 148)})],
+    ]
+    for k, shape in enumerate(shapes):
+        base = 200 + 370 * k
+        for j in range(3):
+            reads.append({"pos": base, "segs": shape(base), "rev": j == 1})
+    return g, synth.explicit_reads("ctg", g, reads)
+
+
+def case_paths_cigar_k1():
+    g, rs = _cigar_rule_reads()
+    return g, rs, (1, 8_000), ["-k", "1"]
+
+
 CASES = {"germline_dense": case_germline_dense, "contig_end": case_contig_end, "unique_fisher": case_unique_fisher,
          "dedup": case_dedup, "germline_dense_k1": case_germline_dense_k1, "paths_k0": case_paths_k0,
-         "paths_k1": case_paths_k1}
+         "paths_k1": case_paths_k1, "paths_cigar_k1": case_paths_cigar_k1}
 
 
 # records only
