@@ -9,7 +9,8 @@ foreign soft clips with low-quality stops, mismatches beside indels, the
 record filters (unmapped/secondary/duplicate/supplementary flags, a one-base
 read, too many mismatches, both ends clipped), MAPQ 0, hard clips, N bases,
 low base qualities, and CIGAR shapes the -k 1 rewrite changes (leading and
-trailing insertions, close indels, a short block before a clip).  The maps
+trailing insertions, close indels, a short block before a clip);
+`paths_cigar_k1` hits each rule of the -k 1 CIGAR rewrite in turn.  The maps
 after the CIGAR walk (P) and after the realigner (R) must equal the
 reference's dump, and the records its records: counts and keys exact,
 fractional sums within 1e-9 relative."""
@@ -38,7 +39,7 @@ def _make_golden():
     return mg
 
 
-@pytest.mark.parametrize("name", ["paths_k0", "paths_k1"])
+@pytest.mark.parametrize("name", ["paths_k0", "paths_k1", "paths_cigar_k1"])
 def test_path_cases_match_reference_golden(name):
     from rabbitvar_gb300 import api, synth
     mg = _make_golden()
