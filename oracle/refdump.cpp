@@ -10,7 +10,8 @@
 // GPU path are compared against.
 //
 // usage: rvref_dump -G ref.fa -b in.bam -R chr:start-end [-k 0|1] [-f F]
-//                   [-u] [-t] [-q Q] [-X N] [-m N] [-Q N] [-F hex] [-stage PRV]
+//                   [-u] [-t] [-q Q] [-X N] [-m N] [-Q N] [-F hex] [-T N] [-M N] [-3]
+//                   [-O F] [-P N] [-o F] [-B N] [-x N] [-r N] [-V F] [-Y N] [--UN] [-stage PRV]
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -125,13 +126,29 @@ int main(int argc, char **argv) {
         else if (a == "-m") conf->mismatch = atoi(nxt().c_str());
         else if (a == "-Q") conf->mappingQuality = atoi(nxt().c_str());
         else if (a == "-F") conf->samfilter = nxt();
+        // the other options the path reads, set as Launcher.cpp:388-470 sets them
+        else if (a == "-T") conf->trimBasesAfter = atoi(nxt().c_str());
+        else if (a == "-M") conf->minmatch = atoi(nxt().c_str());
+        else if (a == "-3") conf->moveIndelsTo3 = true;
+        else if (a == "-O") conf->mapq = atof(nxt().c_str());
+        else if (a == "-P") conf->readPosFilter = atoi(nxt().c_str());
+        else if (a == "-o") conf->qratio = atof(nxt().c_str());
+        else if (a == "-B") conf->minBiasReads = atoi(nxt().c_str());
+        else if (a == "-x") conf->numberNucleotideToExtend = atoi(nxt().c_str());
+        else if (a == "-r") conf->minr = atoi(nxt().c_str());
+        else if (a == "-V") conf->lofreq = atof(nxt().c_str());
+        else if (a == "-Y") conf->referenceExtension = atoi(nxt().c_str());
+        else if (a == "--UN") conf->uniqueModeSecondInPairEnabled = true;
         else if (a == "-stage") stages = nxt();
         else { fprintf(stderr, "unknown arg %s\n", a.c_str()); return 2; }
     }
     size_t colon = region_s.rfind(':');
     size_t dash = region_s.find('-', colon);
-    Region region(region_s.substr(0, colon), atoi(region_s.substr(colon + 1, dash - colon - 1).c_str()),
-                  atoi(region_s.substr(dash + 1).c_str()), "g");
+    // -x widens the -R region on both sides (RegionBuilder.cpp:187-188)
+    int r_start = atoi(region_s.substr(colon + 1, dash - colon - 1).c_str()) - conf->numberNucleotideToExtend;
+    int r_end = atoi(region_s.substr(dash + 1).c_str()) + conf->numberNucleotideToExtend;
+    if (r_start > r_end) r_start = r_end;
+    Region region(region_s.substr(0, colon), r_start, r_end, "g");
 
     std::vector<bamReader> readers;
     for (const std::string &bn : ssplit(conf->bam.getBam1(), ":")) {

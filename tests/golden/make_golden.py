@@ -204,9 +204,22 @@ def case_paths_cigar_k1():
     return g, rs, (1, 8_000), ["-k", "1"]
 
 
+def case_options_k0():
+    # non-default values of the options the path reads (-x widens the -R region on both sides)
+    g, rs, region, _ = case_unique_fisher()
+    return g, rs, region, ["-k", "0", "-x", "30", "-T", "120", "-P", "10", "-3", "-O", "20", "-B", "4", "-o", "2",
+                           "-q", "25", "-m", "6", "-r", "3", "-X", "3", "--fisher"]
+
+
+def case_options_k1():
+    g, rs, region, _ = case_germline_dense()
+    return g, rs, region, ["-k", "1", "--UN", "-M", "20", "-Q", "10", "-Y", "600", "-f", "0.05"]
+
+
 CASES = {"germline_dense": case_germline_dense, "contig_end": case_contig_end, "unique_fisher": case_unique_fisher,
          "dedup": case_dedup, "germline_dense_k1": case_germline_dense_k1, "paths_k0": case_paths_k0,
-         "paths_k1": case_paths_k1, "paths_cigar_k1": case_paths_cigar_k1}
+         "paths_k1": case_paths_k1, "paths_cigar_k1": case_paths_cigar_k1, "options_k0": case_options_k0,
+         "options_k1": case_options_k1}
 
 
 # records only

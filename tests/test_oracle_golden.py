@@ -25,16 +25,35 @@ P_TAGS = ["P_ML", "PN", "PI", "PC", "PS5", "PS3", "PCI", "PCD", "PMN"]
 R_TAGS = ["RN", "RI", "RC"]
 
 
+# command-line options of the reference (src/Launcher.cpp:299-470) -> oracle parameters
+VALUED = {"-k": ("local_realign", int), "-f": ("freq", float), "-q": ("goodq", float), "-X": ("vext", int),
+          "-m": ("mismatch", int), "-Q": ("min_mapq", int), "-T": ("trim_bases_after", int), "-M": ("minmatch", int),
+          "-O": ("mapq_filter", float), "-P": ("read_pos_filter", int), "-o": ("qratio", float),
+          "-B": ("min_bias_reads", int), "-x": ("extend_nt", int), "-r": ("minr", int), "-V": ("lofreq", float),
+          "-Y": ("ref_extension", int)}
+SWITCHES = {"-u": "unique_fwd", "-t": "dedup", "--fisher": "fisher", "-3": "move_indels_3", "--UN": "unique_first"}
+
+
 def _params(flags):
     import oracle as O
-    kw = {"local_realign": int(flags[flags.index("-k") + 1]) if "-k" in flags else 1}
-    if "-u" in flags:
-        kw["unique_fwd"] = 1
-    if "-t" in flags:
-        kw["dedup"] = 1
-    if "--fisher" in flags:
-        kw["fisher"] = 1
+    kw = {"local_realign": 1}
+    i = 0
+    while i < len(flags):
+        if flags[i] in SWITCHES:
+            kw[SWITCHES[flags[i]]] = 1
+            i += 1
+        else:
+            name, ty = VALUED[flags[i]]
+            kw[name] = ty(flags[i + 1])
+            i += 2
     return O.default_params(**kw)
+
+
+def _widened(a, b, flags):
+    """The -R region as the reference's region builder widens it by -x
+    (src/RegionBuilder.cpp:187-188)."""
+    x = int(flags[flags.index("-x") + 1]) if "-x" in flags else 0
+    return a - x, b + x
 
 
 def _make_golden():
@@ -52,7 +71,7 @@ def test_oracle_matches_reference_golden(name):
     g, rs, (a, b), flags = mg.CASES[name]()
     assert mg.readset_fingerprint(rs) == META[name]["fingerprint"], "synthetic generator drifted: rerun make_golden.py"
     gold = gzip.open(os.path.join(GOLD, f"{name}.dump.txt.gz"), "rt").read()
-    ora = O.run_region(rs, g, a, b, stages="PRVO", params=_params(flags))
+    ora = O.run_region(rs, g, *_widened(a, b, flags), stages="PRVO", params=_params(flags))
     # pp/pq (last-seen read position/quality) are compared too: the oracle is sequential
     assert diff_dump(gold, ora, P_TAGS, skip=(), rel=1e-12) == []
     assert diff_dump(gold, ora, R_TAGS, skip=(), rel=1e-12) == []
@@ -109,6 +128,6 @@ def test_oracle_records_match_reference_golden(name):
     g, rs, (a, b), flags = mg.RECORDS_ONLY[name]()
     assert mg.readset_fingerprint(rs) == META[name]["fingerprint"], "synthetic generator drifted: rerun make_golden.py"
     recs = open(os.path.join(GOLD, f"{name}.records.txt")).read().splitlines()
-    ora = O.run_region(rs, g, a, b, stages="O", params=_params(flags))
+    ora = O.run_region(rs, g, *_widened(a, b, flags), stages="O", params=_params(flags))
     assert len(recs) == META[name]["records"] > 5
     assert diff_records(recs, ora.splitlines(), rel=0) == []
