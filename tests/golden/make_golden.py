@@ -252,7 +252,14 @@ def case_somatic_mix_k1():
     return g, t, n, (1, g.shape[0]), ["-k", "1", "--fisher"]
 
 
-SOMATIC = {"somatic_mix": case_somatic_mix, "somatic_sub": case_somatic_sub, "somatic_mix_k1": case_somatic_mix_k1}
+def case_somatic_options():
+    # somatic mode with non-default thresholds, -V (lofreq) included
+    g, _, t, n = synth.somatic_mix(0x5EED0053)
+    return g, t, n, (1, g.shape[0]), ["-k", "0", "--fisher", "-V", "0.1", "-f", "0.02", "-r", "3", "-q", "25",
+                                      "-B", "3", "-o", "2", "-P", "8", "-O", "10", "-3"]
+
+
+SOMATIC = {"somatic_mix": case_somatic_mix, "somatic_options": case_somatic_options, "somatic_sub": case_somatic_sub, "somatic_mix_k1": case_somatic_mix_k1}
 
 
 def readset_fingerprint(rs) -> str:
