@@ -61,3 +61,42 @@ def test_default_params_are_the_reference_defaults():
                 unique_first=0, do_pileup=0, fisher=0, move_indels_3=0, svminlen=1000, somatic=0)
     assert {k: getattr(p, k) for k in want} == want
     assert {f for f, _ in api.Params._fields_} == set(want)
+
+
+def test_cpp_caller_compiles_and_links(tmp_path):
+    """A C++ translation unit like the reference's would-be GpuSimpleMode
+    includes the three headers, links librvgpu.so and calls through the C
+    ABI (without a GPU rv_create reports a CUDA error; with one it succeeds)."""
+    from rabbitvar_gb300 import api
+    cxx = shutil.which("g++")
+    if not cxx:
+        pytest.skip("no C++ compiler")
+    lib = api.lib()._name
+    src = tmp_path / "caller.cpp"
+    src.write_text(r'''
+#include "rvgpu.h"
+#include "rvgpu_io.h"
+#include "rvgpu_mlp.h"
+#include <cstdio>
+int main() {
+    rv_params p;
+    rv_default_params(&p);
+    p.local_realign = 0;
+    p.fisher = 1;
+    rv_ctx *ctx = nullptr;
+    rv_status st = rv_create(&ctx, &p, 0, 0);
+    std::printf("%d %d %s\n", st, p.samfilter, st == RV_OK ? "ok" : rv_last_error(ctx));
+    rv_destroy(ctx);
+    return 0;
+}
+''')
+    exe = tmp_path / "caller"
+    libdir = os.path.dirname(lib)
+    subprocess.run([cxx, "-std=c++17", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), str(src), "-o",
+                    str(exe), "-L", libdir, "-l:" + os.path.basename(lib), "-Wl,-rpath," + libdir],
+                   check=True, capture_output=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
+    st, samfilter = int(out[0]), int(out[1])
+    assert samfilter == 0x504
+    assert st in (0, -2)  # RV_OK with a GPU, RV_ERR_CUDA without one
+    assert len(out) > 2
