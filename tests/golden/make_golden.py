@@ -204,6 +204,28 @@ def case_paths_cigar_k1():
     return g, rs, (1, 8_000), ["-k", "1"]
 
 
+def case_paths_q0():
+    """Zero-quality bases at variant sites (the order-dependent pstd/qstd rule,
+    parseCigar.cpp:902-914): three carrying reads per site with base
+    qualities, in read order, 37/0/37, 0/37/37, 37/37/0, 0/0/37, 0/37/0 and
+    0/0/0.  The oracle replays the
+    rule in read order; the GPU path's order-free form differs where a Q0
+    base follows a nonzero one (not used by the GPU tests)."""
+    rng = np.random.default_rng(0x60D9)
+    g = synth.make_genome(3_000, rng)
+    other = lambda p: "ACGT"[(int(g[p]) + 1) % 4]  # noqa: E731
+    reads = [{"pos": p, "segs": [("M", 150)], "rev": (p // 12) % 2 == 1} for p in range(0, 3_000 - 150, 12)]
+    sites = ((400, (37, 0, 37)), (800, (0, 37, 37)), (1200, (37, 37, 0)), (1600, (0, 0, 37)), (2000, (0, 37, 0)),
+             (2400, (0, 0, 0)))
+    for site, quals in sites:
+        for j, q in enumerate(quals):  # read order = j
+            p = site - 80 + 10 * j
+            reads.append({"pos": p, "segs": [("M", 150, {site - p: other(site)})], "qual_at": {site - p: q},
+                          "rev": j == 1})
+    rs = synth.explicit_reads("ctg", g, reads)
+    return g, rs, (1, 3_000), ["-k", "0", "-q", "0", "-P", "0"]
+
+
 def case_options_k0():
     # non-default values of the options the path reads (-x widens the -R region on both sides)
     g, rs, region, _ = case_unique_fisher()
@@ -218,7 +240,7 @@ def case_options_k1():
 
 CASES = {"germline_dense": case_germline_dense, "contig_end": case_contig_end, "unique_fisher": case_unique_fisher,
          "dedup": case_dedup, "germline_dense_k1": case_germline_dense_k1, "paths_k0": case_paths_k0,
-         "paths_k1": case_paths_k1, "paths_cigar_k1": case_paths_cigar_k1, "options_k0": case_options_k0,
+         "paths_k1": case_paths_k1, "paths_cigar_k1": case_paths_cigar_k1, "paths_q0": case_paths_q0, "options_k0": case_options_k0,
          "options_k1": case_options_k1}
 
 
