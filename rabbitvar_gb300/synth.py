@@ -14,7 +14,6 @@ coordinate-sorted BAM plus FASTA/.fai so the reference binary can read them.
 from __future__ import annotations
 
 import dataclasses
-import os
 import struct
 import zlib
 

@@ -5,7 +5,6 @@ data path needs no GPU to test the host logic)."""
 import os
 import socket
 
-import numpy as np
 import torch.distributed as dist
 import torch.multiprocessing as mp
 
