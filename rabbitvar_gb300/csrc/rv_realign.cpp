@@ -159,8 +159,6 @@ bool same_stats(const HVar &a, const HVar &b) {
            a.pstd == b.pstd && a.qstd == b.qstd;
 }
 
-uint64_t pos_key(int region, int pos) { return ((uint64_t)(uint32_t)region << 32) | (uint32_t)pos; }
-
 // ---------------------------------------------------------------------------
 // batch-wide mirror (pinned host copies, read-only while the regions run):
 // the cells, and every cell's keys flattened in list order
