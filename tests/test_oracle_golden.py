@@ -131,3 +131,24 @@ def test_oracle_records_match_reference_golden(name):
     ora = O.run_region(rs, g, *_widened(a, b, flags), stages="O", params=_params(flags))
     assert len(recs) == META[name]["records"] > 5
     assert diff_records(recs, ora.splitlines(), rel=0) == []
+
+
+def test_oracle_somatic_matches_reference_binary_bench_shape(tmp_path):
+    """The somatic pair at the bench workload's depths (tumor 200x, normal
+    100x, 2x150) on a 100 kb contig, -k 1 --fisher: the oracle's records equal
+    the reference binary's, byte for byte.  The bench's CPU baseline times the
+    oracle, so this pins it on that shape."""
+    import oracle as O
+    if not O.have_reference():
+        pytest.skip("reference binaries not built (reference tree absent)")
+    from rabbitvar_gb300 import synth
+    g, _, t, n = synth.somatic_pair(length=100_000)
+    tb, nb, fa = str(tmp_path / "T.bam"), str(tmp_path / "N.bam"), str(tmp_path / "ref.fa")
+    synth.write_bam(tb, t)
+    synth.write_bam(nb, n)
+    synth.write_fasta(fa, t.contig, g)
+    recs = O.reference_records(fa, f"{tb}|{nb}", f"{t.contig}:1-100000", str(tmp_path / "o.txt"),
+                               ["-k", "1", "--fisher"], sample="T|N")
+    mine = O.run_somatic(t, n, g, 1, 100_000, "O", "T", O.default_params(local_realign=1, fisher=1)).splitlines()
+    assert len(recs) > 100
+    assert sorted(mine) == sorted(recs)
