@@ -100,3 +100,16 @@ int main() {
     assert samfilter == 0x504
     assert st in (0, -2)  # RV_OK with a GPU, RV_ERR_CUDA without one
     assert len(out) > 2
+
+
+def test_product_code_does_not_use_the_oracle():
+    """The library and its Python front end neither import, load nor link
+    anything under oracle/ (the oracle is test infrastructure only)."""
+    import re
+    pkg = os.path.join(ROOT, "rabbitvar_gb300")
+    files = [os.path.join(pkg, f) for f in os.listdir(pkg) if f.endswith(".py")]
+    files += [os.path.join(pkg, "csrc", f) for f in os.listdir(os.path.join(pkg, "csrc"))]
+    files += [os.path.join(ROOT, "include", f) for f in os.listdir(os.path.join(ROOT, "include"))]
+    bad = re.compile(r"import\s+oracle|from\s+oracle|librvoracle|oracle/|rvo_[a-z]|#include\s+\"rv_oracle")
+    hits = [f for f in files if os.path.isfile(f) and bad.search(open(f, errors="replace").read())]
+    assert hits == []
