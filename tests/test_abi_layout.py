@@ -113,3 +113,13 @@ def test_product_code_does_not_use_the_oracle():
     bad = re.compile(r"import\s+oracle|from\s+oracle|librvoracle|oracle/|rvo_[a-z]|#include\s+\"rv_oracle")
     hits = [f for f in files if os.path.isfile(f) and bad.search(open(f, errors="replace").read())]
     assert hits == []
+
+
+def test_graph_entry_points_reject_a_null_context():
+    import ctypes as C
+    from rabbitvar_gb300 import api
+    L = api.lib()
+    n = C.c_int64(-1)
+    assert L.rv_set_pileup_graph(None, 1) == -1          # RV_ERR_ARG
+    assert L.rv_pileup_graph_stats(None, C.byref(n), None) == -1
+    assert n.value == -1
