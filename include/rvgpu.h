@@ -283,9 +283,9 @@ rv_status rv_io_bytes(const rv_ctx *ctx, int64_t *h2d, int64_t *d2h);
 rv_status rv_fisher_batch(rv_ctx *ctx, const int32_t *tables, int64_t n, double *two_sided, double *ratio);
 
 /* Allocation-free variant of rv_fisher_batch for callers that cannot call
- * cudaMalloc (code inside a CUDA-graph capture that must not allocate,
- * processes whose device memory belongs to another allocator or a fixed
- * budget, plugin hosts that forbid hidden allocations).  It has no
+ * cudaMalloc: processes whose device memory belongs to another allocator (a
+ * framework's caching pool) or to a fixed budget, and plugin hosts that
+ * forbid a library from allocating behind their back.  It has no
  * counterpart in the reference (which calls htslib's kt_fisher_exact on the
  * host per record); it runs the same two-sided test as rv_fisher_batch.
  *
@@ -298,12 +298,12 @@ rv_status rv_fisher_batch(rv_ctx *ctx, const int32_t *tables, int64_t n, double 
  * larger total is rejected with RV_ERR_ARG and a message in errbuf (when
  * errbuf_len > 0); nothing is written to the outputs then.
  * The first call on each device looks up the device address of that array
- * (cudaGetSymbolAddress, with the device current); make that first call
- * before any stream capture.  Every call shares the array and re-clears the
- * words that must start at zero; calls whose work overlaps on the GPU (two
- * streams, two host threads on one device) race on it and must be
- * serialised by the caller.  The call reads one scratch word back to the host
- * and synchronises `stream` before launching the test kernels. */
+ * (cudaGetSymbolAddress, with the device current).  Every call shares the
+ * array and re-clears the words that must start at zero; calls whose work
+ * overlaps on the GPU (two streams, two host threads on one device) race on
+ * it and must be serialised by the caller.  The call reads the largest
+ * table total back to the host and synchronises `stream` (a host wait)
+ * before it launches the test kernels. */
 rv_status rv_fisher_batch_static(const int32_t *d_tables, int64_t n, double *d_two_sided, double *d_ratio,
                                  void *stream, char *errbuf, size_t errbuf_len);
 

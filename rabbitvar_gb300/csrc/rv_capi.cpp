@@ -54,7 +54,7 @@ unsigned long long next_pow2(unsigned long long x) {
     return p;
 }
 
-enum { CNT_TILE = 0, CNT_DEFER = 1, CNT_USED = 2, CNT_ERR = 3, CNT_CAND = 4, CNT_AUX = 5 };
+enum { CNT_TILE = 0, CNT_DEFER = 1, CNT_USED = 2, CNT_ERR = 3, CNT_CAND = 4, CNT_AUX = 5, CNT_FIX = 6 };
 
 }  // namespace
 
@@ -74,6 +74,7 @@ DevState rv_ctx::state() const {
     s.batch.seq = d_seq;
     s.batch.qual = d_qual;
     s.batch.skip = use_skip ? d_skip : nullptr;
+    s.batch.max_lq = max_lq;
     s.regions = d_regions;
     s.n_regions = (int32_t)regions.size();
     s.tiles = d_tiles;
@@ -100,6 +101,9 @@ DevState rv_ctx::state() const {
     s.n_cand = d_counters + CNT_CAND;
     s.cand_cap = cand_cap;
     s.logfact = d_logfact;
+    s.ofix = d_ofix;
+    s.n_ofix = d_counters + CNT_FIX;
+    s.ofix_cap = ofix_cap;
     return s;
 }
 
@@ -308,7 +312,7 @@ void rv_destroy(rv_ctx *ctx) {
                     ctx->d_tmp_slots, ctx->d_tmp_cells, ctx->d_tmp_views, ctx->d_tmp_n, ctx->d_list,
                     ctx->d_ftab, ctx->d_logfact, ctx->d_skip, ctx->d_patches, ctx->d_patch_keys,
                     ctx->d_list_off, ctx->d_list_bsum, ctx->d_list_idx, ctx->d_list_slots,
-                    ctx->d_cons_meta, ctx->d_cons};
+                    ctx->d_cons_meta, ctx->d_cons, ctx->d_ofix};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (ctx->h_mirror) cudaFreeHost(ctx->h_mirror);
@@ -399,6 +403,7 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
     }
     if (misaligned) { ctx->err = "base_off must be a multiple of 32"; return RV_ERR_ARG; }
     ctx->n_reads = n;
+    ctx->max_lq = max_lq;
     ctx->n_cigar_words = b->n_cigar_words;
     ctx->n_bases = b->n_bases;
     size_t cr = ctx->cap_reads, cr2 = cr, cr3 = cr, cr4 = cr, cr5 = cr, cr6 = cr, cr7 = cr, cr8 = cr, cr9 = cr;
@@ -647,6 +652,13 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
         RV_CUDA(cudaMalloc((void **)&ctx->d_deferred, (size_t)want_def * sizeof(Deferred)));
         ctx->deferred_cap = want_def;
     }
+    unsigned int want_fix = (unsigned int)std::min<int64_t>(INT32_MAX, n / 64 + 4096);
+    if (want_fix > ctx->ofix_cap || !ctx->d_ofix) {
+        if (ctx->d_ofix) cudaFree(ctx->d_ofix);
+        ctx->d_ofix = nullptr;
+        RV_CUDA(cudaMalloc((void **)&ctx->d_ofix, (size_t)want_fix * sizeof(OrderFix)));
+        ctx->ofix_cap = want_fix;
+    }
     unsigned int want_cand = (unsigned int)std::min<int64_t>(INT32_MAX, std::max<int64_t>(1 << 16, score / 4 + 1024));
     if (want_cand > ctx->cand_cap || !ctx->d_cand) {
         if (ctx->d_cand) cudaFree(ctx->d_cand);
@@ -701,6 +713,7 @@ rv_status queue_pileup_chain(rv_ctx *ctx, cudaStream_t s, int grid, int variant,
     launch_serial(st, ctx->dp, s);
     if (marks) RV_CUDA(cudaEventRecord(ctx->ev[7], s));
     launch_resolve(st, ctx->dp, s);
+    launch_fix_order(st, ctx->dp, s);
     launch_link(st, s);
     launch_collisions(st, s);
     RV_CUDA(cudaGetLastError());
@@ -775,7 +788,7 @@ rv_status pileup_launch(rv_ctx *ctx, cudaStream_t s) {
     if (qs != RV_OK) return qs;
     RV_CUDA(cudaEventRecord(ctx->ev[1], s));
     ctx->pileup_graphed = graphed;
-    ctx->kernels = 8;  // init_slots, region_spans, edge_detect, pileup_tiles, serial, resolve, link, collisions
+    ctx->kernels = 9;  // init_slots, region_reset, edge_detect, pileup_tiles, serial, resolve, fix_order, link, collisions
     ctx->pileup_pin = pinned;
     ctx->mirror_pending = false;
     ctx->stage = 1;  // launched, not finished
@@ -816,7 +829,7 @@ rv_status pileup_finish(rv_ctx *ctx, cudaStream_t s) {
         char buf[160];
         snprintf(buf, sizeof buf, "pileup device error bits 0x%x", err);
         ctx->err = buf;
-        if (err & (ERR_HASH_FULL | ERR_ARENA_FULL | ERR_DEFER_FULL)) return RV_ERR_CAPACITY;
+        if (err & (ERR_HASH_FULL | ERR_ARENA_FULL | ERR_DEFER_FULL | ERR_FIX_FULL)) return RV_ERR_CAPACITY;
         if (err & ERR_COLLISION) return RV_ERR_COLLISION;
         return RV_ERR_UNSUPPORTED;
     }

@@ -20,6 +20,7 @@ int pileup_variants();
 void launch_serial(const DevState &st, const DevParams &P, cudaStream_t s);
 void launch_edge_detect(const DevState &st, const DevParams &P, cudaStream_t s);
 void launch_resolve(const DevState &st, const DevParams &P, cudaStream_t s);
+void launch_fix_order(const DevState &st, const DevParams &P, cudaStream_t s);
 int pileup_blocks_per_sm(int variant);
 size_t pileup_smem_bytes();
 void launch_link(const DevState &st, cudaStream_t s);
@@ -159,8 +160,12 @@ struct rv_ctx {
     unsigned int deferred_cap = 0;
     rv::CandVar *d_cand = nullptr;
     unsigned int cand_cap = 0;
+    // map entries whose pstd/qstd are replayed in read order
+    rv::OrderFix *d_ofix = nullptr;
+    unsigned int ofix_cap = 0;
+    int32_t max_lq = 0;   // longest read of the batch
 
-    // small counters: tile_counter, n_deferred, n_used, err, n_cand, pad, arena_used(64)
+    // small counters: tile_counter, n_deferred, n_used, err, n_cand, pad, n_ofix, pad, arena_used(64)
     unsigned int *d_counters = nullptr;
 
     // scratch for the realigner boundary (grown on demand, owned by the context)

@@ -30,7 +30,8 @@ enum KeyKind : uint16_t {
 enum : uint32_t {
     SF_PDIFF = 1u,      // two pstd-relevant observations with different read positions
     SF_QDIFF = 2u,      // ... with different mean qualities
-    SF_ZERO = 4u,       // an observation with read position 0 or quality 0 (order-sensitive)
+    SF_ZERO = 4u,       // an observation with read position 0 or quality 0: pstd/qstd depend on
+                        // the order of observations and are replayed in read order (k_fix_order)
     SF_ERASED = 8u,     // removed by the realigner
     SF_FIRST = 16u,     // first_tp / first_q hold a value
     SF_FORCE_STD = 32u, // pstd and qstd forced true (adjCnt)
@@ -113,6 +114,8 @@ struct Batch {
     const uint64_t *base_off;
     const uint8_t *seq, *qual;
     const uint8_t *skip;    // -t: 1 = duplicate read (null when -t is off)
+    int32_t max_lq;         // longest read of the batch (bounds how far left of its
+                            // position a read can reach)
 };
 
 struct Hash {
@@ -136,6 +139,19 @@ struct Deferred {
     int32_t pad;
 };
 
+// A map entry whose pstd/qstd the pileup cannot settle without the order of
+// its observations: the reference sets the flag when an observation differs
+// from the previous one and the previous one is nonzero
+// (src/parseCigar.cpp:902-914, 1446-1457), so an observation with read
+// position 0 or quality 0 (or a value outside the packed cell range) makes
+// the result order-dependent.  k_fix_order replays such entries in read order.
+struct OrderFix {
+    int32_t region, pos;
+    int32_t base;            // 0..3: the A/C/G/T cell key; -1: a hash slot
+    int32_t pad;
+    int64_t index;           // cell word (4 * cell + base) or slot index
+};
+
 // Error word bits (per context)
 enum : uint32_t {
     ERR_HASH_FULL = 1u,
@@ -146,6 +162,7 @@ enum : uint32_t {
     ERR_UNSUPPORTED = 32u,
     ERR_PROBE_LIMIT = 64u,
     ERR_COLLISION = 128u,
+    ERR_FIX_FULL = 256u,     // more order-dependent entries than the OrderFix list holds
 };
 
 // One scored allele at a candidate position, handed to the host for the
@@ -184,6 +201,9 @@ struct DevState {
     unsigned int *n_cand;
     unsigned int cand_cap;
     const double *logfact;   // log(k!) for k < kLogFact (Fisher tests)
+    OrderFix *ofix;          // entries k_fix_order replays
+    unsigned int *n_ofix;
+    unsigned int ofix_cap;
 };
 
 constexpr int kLogFact = 1 << 16;

@@ -1,14 +1,17 @@
 // Allocation-free Fisher exact tests.
 //
-// Some callers of this library cannot call cudaMalloc: code running inside a
-// CUDA-graph capture that must not allocate, host processes whose device
-// memory is owned by another allocator (a framework's caching pool) or that
-// run under a fixed device-memory budget, and plugin hosts that forbid a
-// library from allocating behind their back.  rv_fisher_batch_static serves
-// them: the caller passes device buffers for the tables and the results, and
-// the only extra memory the kernels use is a file-scope __device__ array
-// (the log-factorial table below), reserved on every GPU that loads the
-// library for as long as the process runs.
+// Some callers of this library cannot call cudaMalloc: host processes whose
+// device memory is owned by another allocator (a framework's caching pool)
+// or that run under a fixed device-memory budget, and plugin hosts that
+// forbid a library from allocating behind their back.  rv_fisher_batch_static
+// serves them: the caller passes device buffers for the tables and the
+// results, and the only extra memory the kernels use is a file-scope
+// __device__ array (the log-factorial table below), reserved on every GPU
+// that loads the library for as long as the process runs.
+//
+// The call scans the tables on the device, reads the largest total back to
+// the host and waits for `stream` (cudaStreamSynchronize) before it launches
+// the test kernels.
 //
 // The two-sided test is the same computation as rv_fisher_batch (the
 // hypergeometric definition, relative tie slack 1e-7); here the log
@@ -49,19 +52,29 @@ __global__ void k_scan_totals(const int32_t *tab, int64_t n, unsigned int *words
     }
 }
 
-// log(k!) for k = 0..words[0]
-__global__ void k_fill_logfact(double *lf, const unsigned int *words) {
-    unsigned int top = words[0];
+// log(k!) for k = 0..top (top <= kMaxTotal, checked by the host)
+__global__ void k_fill_logfact(double *lf, unsigned int top) {
     for (unsigned int k = blockIdx.x * blockDim.x + threadIdx.x; k <= top; k += gridDim.x * blockDim.x)
         lf[k] = lgamma((double)k + 1.0);
 }
 
 __device__ __forceinline__ double log_choose_t(const double *lf, int n, int k) { return lf[n] - lf[k] - lf[n - k]; }
 
-__global__ void k_fisher_table(const int32_t *tab, int64_t n, const double *lf, double *p2, double *ratio) {
+// `top`: the largest total this call filled the table for.  A table outside
+// [0, top] (possible only if another call changed the tables or the scratch
+// words in between, which the caller must not allow) gets NaN instead of an
+// index past the filled part of the table.
+__global__ void k_fisher_table(const int32_t *tab, int64_t n, const double *lf, unsigned int top, double *p2,
+                               double *ratio) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         int n11 = tab[4 * i], n12 = tab[4 * i + 1], n21 = tab[4 * i + 2], n22 = tab[4 * i + 3];
-        int r1 = n11 + n12, c1 = n11 + n21, nn = n11 + n12 + n21 + n22;
+        const long long total = (long long)n11 + n12 + n21 + n22;
+        if (n11 < 0 || n12 < 0 || n21 < 0 || n22 < 0 || total > (long long)top) {
+            p2[i] = __longlong_as_double(0x7FF8000000000000LL);
+            ratio[i] = __longlong_as_double(0x7FF8000000000000LL);
+            continue;
+        }
+        int r1 = n11 + n12, c1 = n11 + n21, nn = (int)total;
         int lo = r1 + c1 - nn > 0 ? r1 + c1 - nn : 0;
         int hi = r1 < c1 ? r1 : c1;
         double two = 1.0;
@@ -146,9 +159,9 @@ extern "C" rv_status rv_fisher_batch_static(const int32_t *d_tables, int64_t n, 
         put_err(errbuf, errbuf_len, msg);
         return RV_ERR_ARG;
     }
-    k_fill_logfact<<<(int)((host_words[0] + 256) / 256 < 1024 ? (host_words[0] + 256) / 256 : 1024), 256, 0, s>>>(
-        lf, words);
-    k_fisher_table<<<grid, 128, 0, s>>>(d_tables, n, lf, d_two_sided, d_ratio);
+    const unsigned int top = host_words[0];  // <= kMaxTotal: larger totals set the invalid word
+    k_fill_logfact<<<(int)((top + 256) / 256 < 1024 ? (top + 256) / 256 : 1024), 256, 0, s>>>(lf, top);
+    k_fisher_table<<<grid, 128, 0, s>>>(d_tables, n, lf, top, d_two_sided, d_ratio);
     e = cudaGetLastError();
     if (e != cudaSuccess) {
         put_err(errbuf, errbuf_len, cudaGetErrorString(e));

@@ -60,7 +60,20 @@ __device__ Slot *hash_get(const Hash &H, unsigned int *err, int region, int kind
     return nullptr;
 }
 
-__device__ void slot_obs(Slot *s, const Obs &o, double goodq, uint32_t stamp) {
+// Queues a map entry for the in-order replay of its pstd/qstd (k_fix_order).
+__device__ void push_order_fix(const DevState &st, int region, int pos, int base, int64_t index) {
+    unsigned int k = atomicAdd(st.n_ofix, 1u);
+    if (k >= st.ofix_cap) { set_err(st.err, ERR_FIX_FULL); return; }
+    OrderFix f;
+    f.region = region;
+    f.pos = pos;
+    f.base = base;
+    f.pad = 0;
+    f.index = index;
+    st.ofix[k] = f;
+}
+
+__device__ void slot_obs(const DevState &st, Slot *s, const Obs &o, double goodq, uint32_t stamp) {
     if (o.dir) atomicAdd(&s->rev, 1); else atomicAdd(&s->fwd, 1);
     if (o.q >= goodq) atomicAdd(&s->hi, 1); else atomicAdd(&s->lo, 1);
     atomicAdd((unsigned long long *)&s->tp_sum, (unsigned long long)(long long)o.tp);
@@ -77,7 +90,10 @@ __device__ void slot_obs(Slot *s, const Obs &o, double goodq, uint32_t stamp) {
         unsigned long long qb = (unsigned long long)__double_as_longlong(o.q);
         unsigned long long old_q = atomicCAS(&s->first_q, 0xFFF8DEADBEEF0001ULL, qb);
         if (old_q != 0xFFF8DEADBEEF0001ULL && old_q != qb) atomicOr(&s->flags, SF_QDIFF);
-        if (o.tp == 0 || o.q == 0.0) atomicOr(&s->flags, SF_ZERO);
+        if (o.tp == 0 || o.q == 0.0) {
+            if (!(atomicOr(&s->flags, SF_ZERO) & SF_ZERO))
+                push_order_fix(st, s->region, s->pos, -1, (int64_t)(s - st.hash.slots));
+        }
     }
 }
 
@@ -134,8 +150,10 @@ __device__ __forceinline__ int64_t cell_of(const Region &R, int p) { return R.ce
 
 // Direct global update of one A/C/G/T observation (outside a tile window, or
 // the in-order walker).
-__device__ void cell_obs_global(const Cells &C, const Region &R, unsigned int *err, int p, int b, const Obs &o,
+__device__ void cell_obs_global(const DevState &st, int region, const Region &R, int p, int b, const Obs &o,
                                 double goodq) {
+    const Cells &C = st.cells;
+    unsigned int *err = st.err;
     if (p < R.clo || p > R.chi) { set_err(err, ERR_CELL_RANGE); return; }
     int64_t c = cell_of(R, p);
     int64_t g = 4 * c + b;
@@ -150,8 +168,9 @@ __device__ void cell_obs_global(const Cells &C, const Region &R, unsigned int *e
     atomicOr((unsigned int *)&C.kflags[c & ~3LL], 1u << (b + 8 * (c & 3)));
     if (o.std_rel) {
         if (o.tp <= 0 || o.tp > 4095 || qi <= 0 || qi > 1023) {
-            set_err(err, o.tp > 4095 ? ERR_UNSUPPORTED : 0u);
-            atomicOr(&C.first[g], FC_ZERO);
+            // outside the packed value range (a zero among them): replayed in
+            // read order after the pileup
+            if (!(atomicOr(&C.first[g], FC_ZERO) & FC_ZERO)) push_order_fix(st, region, p, b, g);
         } else {
             first_merge(&C.first[g], (uint32_t)o.tp | ((uint32_t)qi << 12), 0u);
         }
@@ -173,7 +192,7 @@ struct SinkBase {
     }
     __device__ void event(int kind, int pos, const char *k, int n, const Obs &o, int64_t read) {
         Slot *s = hash_get(st->hash, st->err, region_idx, kind, pos, k, n);
-        if (s) slot_obs(s, o, P->goodq, (uint32_t)read);
+        if (s) slot_obs(*st, s, o, P->goodq, (uint32_t)read);
     }
     __device__ void max_len(int tlen) { atomicMax((int *)&R->max_read_len, tlen); }
 };
@@ -270,7 +289,7 @@ struct TileSink : SinkBase {
     }
     __device__ void single(int p, int b, const Obs &o, int64_t) {
         if (f.emit_any(p, b, o.dir, o.tp, (int)o.q, o.mapq, o.nm, o.std_rel)) return;
-        cell_obs_global(st->cells, *R, st->err, p, b, o, P->goodq);
+        cell_obs_global(*st, region_idx, *R, p, b, o, P->goodq);
     }
     __device__ void subtract(int p, int b, int dir, int tp, int q, int mapq, int nm, int64_t read, int ci) {
         unsigned int k = atomicAdd(st->n_deferred, 1u);
@@ -315,7 +334,7 @@ struct SerialSink : SinkBase {
         }
     }
     __device__ void single(int p, int b, const Obs &o, int64_t) {
-        cell_obs_global(st->cells, *R, st->err, p, b, o, P->goodq);
+        cell_obs_global(*st, region_idx, *R, p, b, o, P->goodq);
     }
     // existence of the key is decided in read order by k_resolve_deferred
     __device__ void subtract(int p, int b, int dir, int tp, int q, int mapq, int nm, int64_t read, int ci) {
@@ -374,6 +393,62 @@ struct DetectSink {
     __device__ void max_len(int) {}
     __device__ void single(int, int, const Obs &, int64_t) {}
     __device__ void subtract(int, int, int, int, int, int, int, int64_t, int) {}
+};
+
+// Replay sink of k_fix_order: follows one map entry's observations in read
+// order and applies the reference's pstd/qstd rule to them ("set when the
+// value differs from the previous one and the previous one is nonzero",
+// src/parseCigar.cpp:902-914 for M-op keys, 1446-1451 for insertions, and
+// the same rule for deletions).  On the edge reads of a region the in-order
+// walker handles, the reference map's insert-on-lookup past the window is
+// emulated as k_pileup_serial does.
+struct OrderSink {
+    using Fast = NoFast;
+    __device__ Fast fast() const { return Fast(); }
+    const Region *R;
+    int region_idx;
+    int pos, base, kind;        // base >= 0: A/C/G/T cell key; base < 0: slot of `kind` with fingerprint fp
+    unsigned long long fp;
+    bool track;                 // emulate insert-on-lookup (an edge read of an in-order region)
+    uint32_t *ph_hi, *ph_lo;    // SerialSink::kPh bits each
+    int pp;
+    double pq;
+    bool pstd, qstd;
+    __device__ bool phantom(int p) const {
+        if (!track) return false;
+        if (p > R->we) { int d = p - R->we - 1; return d < SerialSink::kPh && ((ph_hi[d >> 5] >> (d & 31)) & 1u); }
+        if (p < R->ws) { int d = R->ws - 1 - p; return d < SerialSink::kPh && ((ph_lo[d >> 5] >> (d & 31)) & 1u); }
+        return false;
+    }
+    __device__ void touch_phantom(int p) {
+        if (!track) return;
+        if (p > R->we) {
+            int d = p - R->we - 1;
+            if (d < SerialSink::kPh) ph_hi[d >> 5] |= 1u << (d & 31);
+        } else if (p < R->ws) {
+            int d = R->ws - 1 - p;
+            if (d < SerialSink::kPh) ph_lo[d >> 5] |= 1u << (d & 31);
+        }
+    }
+    __device__ void take(const Obs &o) {
+        if (!pstd && pp != 0 && o.tp != pp) pstd = true;
+        if (!qstd && pq != 0.0 && o.q != pq) qstd = true;
+        pp = o.tp;
+        pq = o.q;
+    }
+    __device__ void error(unsigned int) {}
+    __device__ void cov(int, int) {}
+    __device__ void max_len(int) {}
+    __device__ void subtract(int, int, int, int, int, int, int, int64_t, int) {}
+    __device__ void single(int p, int b, const Obs &o, int64_t) {
+        if (base >= 0 && p == pos && b == base && o.std_rel) take(o);
+    }
+    __device__ void event(int k, int p, const char *key, int n, const Obs &o, int64_t) {
+        if (base >= 0 || p != pos || k != kind || !o.std_rel) return;
+        unsigned long long h1, h2;
+        key_hashes(region_idx, k, p, key, n, h1, h2);
+        if (h1 == fp) take(o);
+    }
 };
 
 // Record filters of next_record (src/recordPreprocessor.cpp:101-180) plus the
@@ -613,6 +688,77 @@ __global__ void k_resolve_deferred(DevState st, DevParams P, int max_probe_reads
     }
 }
 
+// One thread per queued entry (OrderFix): replays the reads that can observe
+// the entry's position, in file order, and sets its pstd/qstd flags to the
+// reference's order-dependent result.  Entries are rare (zero qualities or
+// read positions), so the replay walks whole reads with the general walker.
+__global__ void k_fix_order(DevState st, DevParams P) {
+    unsigned int n = *st.n_ofix;
+    if (n > st.ofix_cap) n = st.ofix_cap;
+    uint32_t ph_hi[SerialSink::kPh / 32], ph_lo[SerialSink::kPh / 32];
+    for (unsigned int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const OrderFix f = st.ofix[k];
+        const Region &R = st.regions[f.region];
+        OrderSink os;
+        os.R = &R;
+        os.region_idx = f.region;
+        os.pos = f.pos;
+        os.base = f.base;
+        os.kind = 0;
+        os.fp = 0;
+        if (f.base < 0) {
+            const Slot &sl = st.hash.slots[f.index];
+            os.kind = sl.kind;
+            os.fp = sl.fp;
+        }
+        os.track = false;
+        os.ph_hi = ph_hi;
+        os.ph_lo = ph_lo;
+        os.pp = 0;
+        os.pq = 0.0;
+        os.pstd = os.qstd = false;
+        const bool in_order = R.serial && R.edge_hit;
+        if (in_order)
+            for (int i = 0; i < SerialSink::kPh / 32; i++) { ph_hi[i] = 0; ph_lo[i] = 0; }
+        // first read that can reach the position (R.reach: the farthest any
+        // read of the region reaches past its start); in an in-order region,
+        // the first edge read if that comes earlier (its inserts past the
+        // window are seen by later edge reads)
+        int64_t lo = R.r0, hi = R.r1;
+        while (lo < hi) {
+            int64_t mid = (lo + hi) / 2;
+            if (st.batch.pos[mid] + 1 + R.reach < f.pos) lo = mid + 1; else hi = mid;
+        }
+        if (in_order) {
+            int64_t a = R.r0, b = R.r1;
+            while (a < b) {
+                int64_t mid = (a + b) / 2;
+                if (st.batch.pos[mid] + 1 + R.reach + kEdgeMargin <= R.we) a = mid + 1; else b = mid;
+            }
+            if (a < lo) lo = a;
+        }
+        Walker<OrderSink> w(P, os, R, st.ref, st.ref_len);
+        for (int64_t r = lo; r < R.r1; r++) {
+            // a read starts at most its length before its position
+            if (st.batch.pos[r] - st.batch.max_lq > f.pos) break;
+            if (!read_passes(st.batch, P, R, r)) continue;
+            int a, b;
+            read_span(st.batch, r, a, b, P.local_realign != 0);
+            const bool edge = in_order && is_edge(R, b);
+            if (!edge && (a > f.pos || b < f.pos)) continue;
+            os.track = edge;
+            w.walk(st.batch, r);
+        }
+        if (f.base >= 0) {
+            uint32_t v = st.cells.first[f.index] & ~(FC_PDIFF | FC_QDIFF);
+            st.cells.first[f.index] = v | (os.pstd ? FC_PDIFF : 0u) | (os.qstd ? FC_QDIFF : 0u);
+        } else {
+            Slot &sl = st.hash.slots[f.index];
+            sl.flags = (sl.flags & ~(SF_PDIFF | SF_QDIFF)) | (os.pstd ? SF_PDIFF : 0u) | (os.qstd ? SF_QDIFF : 0u);
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // host-side launchers
 // ---------------------------------------------------------------------------
@@ -667,6 +813,10 @@ void launch_serial(const DevState &st, const DevParams &P, cudaStream_t s) {
 
 void launch_resolve(const DevState &st, const DevParams &P, cudaStream_t s) {
     k_resolve_deferred<<<152, 128, 0, s>>>(st, P, 1 << 16);
+}
+
+void launch_fix_order(const DevState &st, const DevParams &P, cudaStream_t s) {
+    k_fix_order<<<16, 64, 0, s>>>(st, P);
 }
 
 

@@ -1,6 +1,39 @@
 """Comparison helpers for map dumps and records (shared by the tests)."""
 from __future__ import annotations
 
+# command-line options of the reference (src/Launcher.cpp:299-470) -> the
+# rv_params / oracle parameter names (both mirror Configuration)
+VALUED = {"-k": ("local_realign", int), "-f": ("freq", float), "-q": ("goodq", float), "-X": ("vext", int),
+          "-m": ("mismatch", int), "-Q": ("min_mapq", int), "-T": ("trim_bases_after", int), "-M": ("minmatch", int),
+          "-O": ("mapq_filter", float), "-P": ("read_pos_filter", int), "-o": ("qratio", float),
+          "-B": ("min_bias_reads", int), "-x": ("extend_nt", int), "-r": ("minr", int), "-V": ("lofreq", float),
+          "-Y": ("ref_extension", int)}
+SWITCHES = {"-u": "unique_fwd", "-t": "dedup", "--fisher": "fisher", "-3": "move_indels_3", "--UN": "unique_first",
+            "-p": "do_pileup"}
+
+
+def flag_params(flags) -> dict:
+    """Parameter values of a reference command line (default -k 1)."""
+    kw = {"local_realign": 1}
+    i = 0
+    while i < len(flags):
+        if flags[i] in SWITCHES:
+            kw[SWITCHES[flags[i]]] = 1
+            i += 1
+        else:
+            name, ty = VALUED[flags[i]]
+            kw[name] = ty(flags[i + 1])
+            i += 2
+    return kw
+
+
+def widened(a, b, flags):
+    """The -R region as the reference's region builder widens it by -x
+    (src/RegionBuilder.cpp:187-188)."""
+    x = int(flags[flags.index("-x") + 1]) if "-x" in flags else 0
+    return a - x, b + x
+
+
 # column index (0-based, tag first) of pp and pq in stat lines: the last-seen
 # read position / quality the reference keeps only to derive pstd/qstd
 STAT_SKIP = (14, 15)

@@ -12,7 +12,7 @@ import os
 
 import pytest
 
-from cmp import diff_dump, diff_records
+from cmp import diff_dump, diff_records, flag_params, widened
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLD = os.path.join(HERE, "golden")
@@ -25,35 +25,12 @@ P_TAGS = ["P_ML", "PN", "PI", "PC", "PS5", "PS3", "PCI", "PCD", "PMN"]
 R_TAGS = ["RN", "RI", "RC"]
 
 
-# command-line options of the reference (src/Launcher.cpp:299-470) -> oracle parameters
-VALUED = {"-k": ("local_realign", int), "-f": ("freq", float), "-q": ("goodq", float), "-X": ("vext", int),
-          "-m": ("mismatch", int), "-Q": ("min_mapq", int), "-T": ("trim_bases_after", int), "-M": ("minmatch", int),
-          "-O": ("mapq_filter", float), "-P": ("read_pos_filter", int), "-o": ("qratio", float),
-          "-B": ("min_bias_reads", int), "-x": ("extend_nt", int), "-r": ("minr", int), "-V": ("lofreq", float),
-          "-Y": ("ref_extension", int)}
-SWITCHES = {"-u": "unique_fwd", "-t": "dedup", "--fisher": "fisher", "-3": "move_indels_3", "--UN": "unique_first"}
-
-
 def _params(flags):
     import oracle as O
-    kw = {"local_realign": 1}
-    i = 0
-    while i < len(flags):
-        if flags[i] in SWITCHES:
-            kw[SWITCHES[flags[i]]] = 1
-            i += 1
-        else:
-            name, ty = VALUED[flags[i]]
-            kw[name] = ty(flags[i + 1])
-            i += 2
-    return O.default_params(**kw)
+    return O.default_params(**flag_params(flags))
 
 
-def _widened(a, b, flags):
-    """The -R region as the reference's region builder widens it by -x
-    (src/RegionBuilder.cpp:187-188)."""
-    x = int(flags[flags.index("-x") + 1]) if "-x" in flags else 0
-    return a - x, b + x
+_widened = widened
 
 
 def _make_golden():

@@ -10,23 +10,32 @@ record filters (unmapped/secondary/duplicate/supplementary flags, a one-base
 read, too many mismatches, both ends clipped), MAPQ 0, hard clips, N bases,
 low base qualities, and CIGAR shapes the -k 1 rewrite changes (leading and
 trailing insertions, close indels, a short block before a clip);
-`paths_cigar_k1` hits each rule of the -k 1 CIGAR rewrite in turn.  The maps
-after the CIGAR walk (P) and after the realigner (R) must equal the
+`paths_cigar_k1` hits each rule of the -k 1 CIGAR rewrite in turn;
+`paths_q0` puts zero-quality bases before, between and after nonzero ones in
+read order (the reference's order-dependent qstd rule).  `options_k0` /
+`options_k1` run read sets with non-default values of every option the path
+reads, and the remaining single-sample golden cases (dense germline sets
+with -k 0 and -k 1, a contig end, -u --fisher, -t) run their own flags.  The
+maps after the CIGAR walk (P) and after the realigner (R) must equal the
 reference's dump, and the records its records: counts and keys exact,
-fractional sums within 1e-9 relative."""
+fractional sums within 1e-9 relative.  The somatic golden cases (including
+`somatic_options`, non-default somatic options) must give the reference's
+63-column records."""
 import gzip
 import json
 import os
 
 import pytest
 
-from cmp import diff_dump, diff_records
+from cmp import diff_dump, diff_records, flag_params, widened
 
 pytestmark = pytest.mark.gpu
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLD = os.path.join(HERE, "golden")
 META = json.load(open(os.path.join(GOLD, "golden.json")))
+SINGLE = sorted(k for k, v in META.items() if not v.get("somatic") and not v.get("records_only"))
+SOMATIC = sorted(k for k, v in META.items() if v.get("somatic"))
 P_TAGS = ["P_ML", "PN", "PI", "PC", "PS5", "PS3", "PCI", "PCD", "PMN"]
 R_TAGS = ["RN", "RI", "RC"]
 
@@ -39,16 +48,15 @@ def _make_golden():
     return mg
 
 
-@pytest.mark.parametrize("name", ["paths_k0", "paths_k1", "paths_cigar_k1"])
-def test_path_cases_match_reference_golden(name):
+@pytest.mark.parametrize("name", SINGLE)
+def test_single_sample_golden_cases_match_reference(name):
     from rabbitvar_gb300 import api, synth
     mg = _make_golden()
     g, rs, (a, b), flags = mg.CASES[name]()
     assert mg.readset_fingerprint(rs) == META[name]["fingerprint"]
-    k = int(flags[flags.index("-k") + 1])
-    ctx = api.Context(api.default_params(local_realign=k, fisher=1 if "--fisher" in flags else 0))
+    ctx = api.Context(api.default_params(**flag_params(flags)))
     ctx.upload_reference(rs.contig, synth.genome_str(g).encode())
-    ctx.submit(api.Batch.from_readset(rs), [(a, b)])
+    ctx.submit(api.Batch.from_readset(rs), [widened(a, b, flags)])
     ctx.pileup()
     p_dump = ctx.export_maps(0, "P")
     ctx.realign()
@@ -62,3 +70,18 @@ def test_path_cases_match_reference_golden(name):
     recs = open(os.path.join(GOLD, f"{name}.records.txt")).read().splitlines()
     assert len(recs) == META[name]["records"] > 5
     assert diff_records(recs, mine) == []
+
+
+@pytest.mark.parametrize("name", SOMATIC)
+def test_somatic_golden_cases_match_reference(name):
+    from rabbitvar_gb300 import api, synth
+    mg = _make_golden()
+    g, t, n, (a, b), flags = mg.SOMATIC[name]()
+    assert [mg.readset_fingerprint(t), mg.readset_fingerprint(n)] == META[name]["fingerprint"]
+    pair = api.SomaticPair(api.default_params(**flag_params(flags)))
+    pair.upload_reference(t.contig, synth.genome_str(g).encode())
+    mine = pair.call(api.Batch.from_readset(t), api.Batch.from_readset(n), [widened(a, b, flags)], "T", t.contig)
+    pair.close()
+    recs = open(os.path.join(GOLD, f"{name}.records.txt")).read().splitlines()
+    assert len(recs) == META[name]["records"] > 50
+    assert diff_records(recs, mine.splitlines(), somatic=True) == []
