@@ -1,28 +1,31 @@
 """Benchmark: reads/s of pileup + variant scoring on one GB300.
 
-Workload (the somatic-pair shape the reference's metric is quoted on): a
-seeded synthetic 1 Mb contig, tumor 200x + normal 100x 2x150 bp pairs
-(~2.0 M reads), germline SNVs 1e-3/bp and indels 1e-4/bp in both samples,
-somatic SNV/MNV 2e-5/bp (VAF U(0.01, 0.5)) and strand-biased artifacts
-5e-6/bp in the tumor, called in somatic mode (the reference's
-`-b 'T.bam|N.bam' -N 'T|N' --fisher`) over 100 BED tiles of 10 kb with -k 0:
-both samples through the full per-region path (record filters, CIGAR walk,
-allele maps, MNP realignment, site statistics), then the tumor/normal
-classification, the hard filter, three Fisher tests per record and the
-63-column record text.  One step = both samples, all regions.
+Headline workload: the deep targeted somatic panel -- a seeded synthetic
+contig with 400 regions of 5 kb (2 Mb), tumor 5000x + normal 1000x 2x150 bp
+pairs (~80 M reads), germline SNVs/indels in both samples, low-VAF somatic
+SNVs/MNVs/indels (VAF log-uniform(0.001, 0.05)) in the tumor and C>A
+artifacts at 1e-4 per C base with quality 20, called in somatic mode (the
+reference's `-b 'T.bam|N.bam' -N 'T|N' --fisher` over the 400-region BED,
+its default -k 1): both samples through the full per-region path (record
+filters, CIGAR rewrite and walk, allele maps, the realigner, site
+statistics), then the tumor/normal classification, the hard filter, three
+Fisher tests per record and the 63-column record text.  One step = both
+samples, all regions.
 
     value : reads/s with the read batches already resident in HBM
     e2e   : reads/s through the C ABI from pinned host batches, including
             the host->device copy of the reads and the device->host copy of
             the scored candidates every step
-Inputs (~0.5 GB of reads) exceed the 129 MB L2, so no flush is needed
-between steps.
-
-    e2e_from_bam : reads/s from BGZF-compressed BAM bytes in pinned host
-            memory: the BAM decode on the GPU, then the same calls
+Inputs (~22 GB of reads) exceed the 129 MB L2, so no flush is needed
+between steps.  `parity` compares the GPU's records of four regions with
+the oracle's on the same reads (the CPU baseline sample); a mismatch fails
+the run.  Secondary keys: the 1 Mb somatic pair at 200x/100x
+(`somatic_pair_1mb`, with its BAM-decode leg), the other -k setting,
+the learned filter.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
     python bench.py --bam-decode      # BAM decode alone, GPU vs host decoder
+    python bench.py --panel N         # batched amplicon panel of N regions
 """
 from __future__ import annotations
 
@@ -153,12 +156,86 @@ def barrier_max(dist, x: float) -> float:
 def workload(k: int) -> str:
     return (f"somatic mode (-b 'T|N' -N 'T|N' --fisher -f 0.01 -k {k}): synthetic 1 Mb contig, "
             "tumor 200x + normal 100x 2x150, 100 x 10 kb BED tiles")
-METRIC = "reads/s pileup+var scoring (somatic pair 1 Mb, T200x+N100x)"
-CPU_TILES = 40   # CPU sample: 40 of the 100 tiles (~0.8 M reads, ~10 s on one core)
-# DRAM bytes (read + write) of one tumor-sample k_pileup_tiles<640, 3> launch
-# of this workload, from one ncu capture each (by -k:
-# profiles/k_pileup_tiles_somatic1mb.md, profiles/k_pileup_tiles_somatic1mb_k1.md)
-PILEUP_TRAFFIC = {0: 1301.5e6, 1: 1627.2e6}
+
+
+def deep_workload_name(k: int, n_regions: int = 400) -> str:
+    return (f"somatic mode (-b 'T|N' -N 'T|N' --fisher -f 0.01 -k {k}): deep targeted panel, {n_regions} x 5 kb "
+            "regions, tumor 5000x + normal 1000x 2x150, somatic VAF log-U(0.001,0.05), C>A 1e-4/base at Q20")
+
+
+METRIC = "reads/s pileup+var scoring (deep somatic panel 400 x 5 kb, T5000x+N1000x)"
+PANEL_REGIONS = 400
+# the oracle's sample of the panel: the CPU baseline and the records check
+PARITY_REGIONS = [0, 137, 263, 399]
+# the reference arm's sample (all host threads): 16 regions, ~3.2 M reads
+REF_REGIONS = list(range(0, PANEL_REGIONS, 25))
+CPU_TILES = 40   # 1 Mb pair: CPU sample of 40 of the 100 tiles
+# DRAM bytes (read + write) per read of one k_pileup_tiles launch, from one
+# ncu capture of a tumor launch of the deep panel on a 16-region slice
+# (2.7 M reads); the headline launch's traffic is this times its reads
+PILEUP_TRAFFIC_PER_READ = None
+
+
+def deep_workload(rank: int = 0, world: int = 1, only=None):
+    """The deep panel (400 x world regions, LPT-partitioned across ranks by
+    expected reads: each rank generates and calls its own share) or the
+    regions `only`; returns (genome, tumor, normal, regions of the reads)."""
+    from rabbitvar_gb300 import shard, synth
+    n_reg = PANEL_REGIONS * world
+    if only is None and world > 1:
+        only = shard.partition([1] * n_reg, world)[rank]
+    g, _, t, n, regions = synth.deep_somatic_panel(n_regions=n_reg, only=only)
+    regs = regions if only is None else [regions[i] for i in sorted(only)]
+    return g, t, n, regs
+
+
+def oracle_regions(g, tumor, normal, regions, k: int, threads: int = 1):
+    """The oracle on `regions` of a read set whose regions are separated by
+    more than a read pair (each region's reads sliced out): returns (record
+    text, reads, seconds)."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from rabbitvar_gb300 import synth
+    p = O.default_params(local_realign=k, fisher=1)
+    sl = []
+    for rs in (tumor, normal):
+        lo = [int(np.searchsorted(rs.pos, a - 1 - 1000)) for a, _ in regions]
+        hi = [int(np.searchsorted(rs.pos, b + 1000)) for _, b in regions]
+        if rs.seq4 is not None:
+            sl.append(synth.take(rs, np.concatenate([np.arange(a, b) for a, b in zip(lo, hi)])))
+        else:
+            sl.append(_slices(rs, lo, hi))
+    reads = sl[0].n + sl[1].n
+    t0 = time.perf_counter()
+    _, text = O.run_somatic_regions(sl[0], sl[1], g, regions, "T", p, threads=threads)
+    return text, reads, time.perf_counter() - t0
+
+
+def _slices(rs, lo, hi):
+    """Concatenation of the read ranges [lo[i], hi[i]) (ascending, disjoint)
+    of a packed read set, unpacked."""
+    import dataclasses
+    import numpy as np
+    from rabbitvar_gb300 import synth
+    parts = [synth.read_range(rs, a, b) for a, b in zip(lo, hi)]
+    cig = np.concatenate([p.cigar for p in parts])
+    ncig = np.concatenate([p.n_cigar for p in parts])
+    cig_off = np.zeros(ncig.shape[0], np.uint32)
+    cig_off[1:] = np.cumsum(ncig[:-1].astype(np.uint64)).astype(np.uint32)
+    n = ncig.shape[0]
+    stride = 160
+    cat = lambda f: np.concatenate([getattr(p, f) for p in parts])  # noqa: E731
+    return dataclasses.replace(parts[0], pos=cat("pos"), flag=cat("flag"), mapq=cat("mapq"), mpos=cat("mpos"),
+                               isize=cat("isize"), nm=cat("nm"), n_cigar=ncig, cig_off=cig_off, cigar=cig,
+                               l_qseq=cat("l_qseq"), base_off=np.arange(n, dtype=np.uint64) * np.uint64(stride),
+                               seq4=cat("seq4"), qual=cat("qual"), name_id=cat("name_id"))
+
+
+def region_records(text: str, contig: str, regions) -> list[str]:
+    """Records of `text` whose region column names one of `regions`."""
+    keys = {f"\t{contig}:{a}-{b}\t" for a, b in regions}
+    return [ln for ln in text.splitlines() if any(k in ln for k in keys)]
 
 
 def cpu_baseline_run(g, tumor, normal, regions, threads: int, n_regions: int, k: int):
@@ -448,26 +525,157 @@ def run_panel(args):
 
 
 def run_reference(args, rank):
+    """The reference arm: the oracle (the CPU restatement of the reference's
+    path, pinned to the reference binary) on the machine's host cores, all
+    threads, somatic mode, on a 16-region sample of the deep panel per step."""
     if rank != 0:
         return
-    g, tumor, normal, regions = make_workload()
     threads = os.cpu_count() or 1
-    n_reg = CPU_TILES
+    g, tumor, normal, regs = deep_workload(only=REF_REGIONS)
     vals = []
-    for _ in range(args.warmup):
-        cpu_baseline_run(g, tumor, normal, regions, threads, n_reg, args.local_realign)
-    for _ in range(args.steps):
-        v, dt, nr = cpu_baseline_run(g, tumor, normal, regions, threads, n_reg, args.local_realign)
-        vals.append(v)
+    nr = 0
+    for i in range(args.warmup + args.steps):
+        _, nr, dt = oracle_regions(g, tumor, normal, regs, args.local_realign, threads=threads)
+        if i >= args.warmup:
+            vals.append(nr / dt)
     v = statistics.median(vals)
+    sample = f"{len(REF_REGIONS)} of {PANEL_REGIONS} regions (every 25th), tumor+normal ({nr} reads), per step"
     out = {"impl": "reference", "metric": METRIC,
            "value": v, "unit": "reads/s", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
-           "higher_is_better": True, "data": "synthetic",
-           "config": {"workload": workload(args.local_realign), "sample": f"first {n_reg} of 100 tiles, both samples"},
-           "cpu_baseline": {"value": v, "unit": "reads/s", "cores": threads, "kind": "port",
-                            "sample": f"first {n_reg} of 100 10-kb tiles, tumor+normal ({nr} reads), per step"},
+           "higher_is_better": True, "data": "synthetic (seeded)",
+           "config": {"workload": deep_workload_name(args.local_realign), "sample": sample},
+           "cpu_baseline": {"value": v, "unit": "reads/s", "cores": threads, "kind": "port", "sample": sample},
            "e2e": {"value": v, "unit": "reads/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
+
+
+def measure_pair(g, tumor, normal, regions, args, dist, clocks, device: int, world: int, contig: str = "ctg",
+                 roofline: bool = True) -> dict:
+    """One somatic workload through the pair: e2e (a stream of pinned host
+    batches uploaded every step), value (the stream on batches resident in
+    HBM), the same steps one after the other (stage times, launches), and the
+    tumor's pileup launch timed alone.  Returns the measurements and the
+    first step's record text."""
+    from rabbitvar_gb300 import api, synth
+    params = api.default_params(local_realign=args.local_realign, fisher=1)
+    pair = api.SomaticPair(params, device=device)
+    pair.upload_reference(contig, synth.genome_str(g).encode())
+    ctxs = [pair.tumor, pair.normal]
+    batches = [api.Batch.from_readset(rs, pinned=True) for rs in (tumor, normal)]
+    n_reads = tumor.n + normal.n
+    host_ms = {"pileup+realign": 0.0, "score": 0.0, "format": 0.0}
+
+    def kernels_of():
+        return sum(c.timings()["kernels"] for c in ctxs)
+
+    def device_step(collect=None):
+        t0 = time.perf_counter()
+        pair.pileup_realign()
+        t2 = time.perf_counter()
+        pair.score()
+        t3 = time.perf_counter()
+        text, n = pair.format_records("T", contig)
+        t4 = time.perf_counter()
+        if collect is not None:
+            host_ms["pileup+realign"] += (t2 - t0) * 1e3
+            host_ms["score"] += (t3 - t2) * 1e3
+            host_ms["format"] += (t4 - t3) * 1e3
+            collect.extend(c.stage_times() for c in ctxs)
+        return kernels_of(), n
+
+    stream = api.SomaticStream(params, device=device)
+    stream.upload_reference(contig, synth.genome_str(g).encode())
+    job = (batches[0], batches[1], regions)
+    stream.run([job] * max(1, args.warmup), "T", contig)
+    w0 = time.time()
+    t0 = time.perf_counter()
+    e2e_texts = stream.run([job] * args.steps, "T", contig)
+    e2e_dt = barrier_max(dist, time.perf_counter() - t0)
+    clocks.window(w0, time.time())
+    last = stream.pairs[(args.steps - 1) % 2]
+    h2d = sum(c.io_bytes()[0] for c in (last.tumor, last.normal))
+    d2h = sum(c.io_bytes()[1] for c in (last.tumor, last.normal))
+    resident = (None, None, regions)
+    stream.run([resident] * max(1, args.warmup), "T", contig)
+    w0 = time.time()
+    t0 = time.perf_counter()
+    res_texts = stream.run([resident] * args.steps, "T", contig)
+    res_dt = barrier_max(dist, time.perf_counter() - t0)
+    clocks.window(w0, time.time())
+    stream.close()
+    pair.submit(batches[0], batches[1], regions)
+    for _ in range(args.warmup):
+        device_step()
+    stages = []
+    w0 = time.time()
+    t0 = time.perf_counter()
+    kernels = 0
+    recs = 0
+    for _ in range(args.steps):
+        k, recs = device_step(stages)
+        kernels += k
+    dev_dt = barrier_max(dist, time.perf_counter() - t0)
+    clocks.window(w0, time.time())
+    if any(t != e2e_texts[0] for t in e2e_texts + res_texts):
+        raise RuntimeError("the streamed steps gave different records")
+    if len(e2e_texts[0].splitlines()) != recs:
+        raise RuntimeError("the streamed batches gave a different record count from the resident steps")
+    out = {"value": n_reads * world * args.steps / res_dt, "ms_per_step": res_dt / args.steps * 1e3,
+           "e2e": {"value": n_reads * world * args.steps / e2e_dt, "unit": "reads/s",
+                   "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+           "value_sequential": {"value": n_reads * world * args.steps / dev_dt, "unit": "reads/s",
+                                "note": "the same steps one after the other on one context pair, no overlap"},
+           "gpu_launches": kernels, "reads_per_step": n_reads * world, "records_per_step": recs,
+           "stage_ms": {k: statistics.mean(s_[k] for s_ in stages) for k in stages[0]},
+           "host_call_ms_per_step": {k: v / args.steps for k, v in host_ms.items()},
+           "capacity": pair.tumor.capacity_stats()}
+    # sites/s: region positions of both samples over the whole scoring stage
+    # (device k_score plus the host's allele strings, MSI and record text)
+    sites = 2 * sum(b - a + 1 for a, b in regions)
+    score_stage_ms = (host_ms["score"] + host_ms["format"]) / args.steps
+    out["sites_per_s"] = sites / (score_stage_ms * 1e-3)
+    if roofline:
+        # the tumor's k_pileup_tiles launch, timed alone right after the timed
+        # region on the same batch (in the timed steps both samples' kernels
+        # share the GPU, one stream each)
+        tile_ms_shared = statistics.mean(s_["pileup_tiles"] for s_ in stages[0::2])
+        solo = []
+        for _ in range(3):
+            pair.tumor.pileup()
+            solo.append(pair.tumor.stage_times()["pileup_tiles"])
+        tile_ms = statistics.mean(solo)
+        cells = sum(b - a + 1 for a, b in regions)
+        window = sum(b - a + 1 + 2 * 1200 for a, b in regions)
+        per_launch_bytes = read_alg_bytes(tumor) + cells * 256 + window  # reads + site records + reference windows
+        achieved = per_launch_bytes / (tile_ms * 1e-3) / 1e9
+        peak, peak_kind = measured_peak_hbm()
+        traffic = PILEUP_TRAFFIC_PER_READ * tumor.n if PILEUP_TRAFFIC_PER_READ else None
+        out["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                           "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                           "kernel": "k_pileup_tiles", "launch": f"tumor sample, {tumor.n} reads, timed alone",
+                           "alg_bytes_per_launch": per_launch_bytes, "launch_ms": tile_ms,
+                           "launch_ms_sharing_gpu": tile_ms_shared}
+    pair.close()
+    for b in batches:
+        b.close()
+    out["text"] = e2e_texts[0]
+    return out
+
+
+def pair_1mb_leg(args, device: int) -> dict:
+    """The 1 Mb somatic pair (tumor 200x + normal 100x): value and e2e as
+    the headline, plus its BAM-decode leg."""
+    from rabbitvar_gb300 import api  # noqa: F401
+    g, tumor, normal, regions = make_workload()
+    clocks = type("NoClocks", (), {"window": lambda self, a, b: None})()
+    r = measure_pair(g, tumor, normal, regions, args, None, clocks, device, 1, roofline=False)
+    out = {"workload": workload(args.local_realign), "value": r["value"], "e2e": r["e2e"]["value"],
+           "unit": "reads/s", "ms_per_step": r["ms_per_step"], "reads_per_step": r["reads_per_step"],
+           "records_per_step": r["records_per_step"], "host_call_ms_per_step": r["host_call_ms_per_step"]}
+    if not args.no_bam:
+        out["e2e_from_bam"] = bam_leg(g, tumor, normal, regions, args.local_realign, args.steps, args.warmup,
+                                      device, r["text"])
+    return out
 
 
 def main():
@@ -482,6 +690,9 @@ def main():
                     help="the reference's -k (default 1, as the reference): 0 leaves out the realigner's indel passes")
     ap.add_argument("--no-other-k", action="store_true", help="skip the leg with the other -k setting")
     ap.add_argument("--no-bam", action="store_true", help="skip the leg that starts from BGZF-compressed BAM bytes")
+    ap.add_argument("--no-1mb", action="store_true", help="skip the 1 Mb somatic pair leg")
+    ap.add_argument("--regions", type=int, default=0, metavar="N",
+                    help="run the headline on the first N regions of the panel only (for profiling)")
     ap.add_argument("--bam-decode", action="store_true",
                     help="only time the BAM decode of the tumor sample, GPU against the host decoder")
     ap.add_argument("--panel", type=int, default=0, metavar="N",
@@ -497,145 +708,70 @@ def main():
     if args.bam_decode:
         run_bam_decode(args)
         return
-    import numpy as np
-    from rabbitvar_gb300 import api, synth
     local = int(os.environ.get("LOCAL_RANK", "0"))
-    g, tumor, normal, regions = make_workload(seed_offset=rank)
-    samples = [("T", tumor), ("N", normal)]
-    params = api.default_params(local_realign=args.local_realign, fisher=1)
-    pair = api.SomaticPair(params, device=local)
-    pair.upload_reference(tumor.contig, synth.genome_str(g).encode())
-    ctxs = [pair.tumor, pair.normal]
-    batches = [api.Batch.from_readset(rs, pinned=True) for _, rs in samples]
-    n_reads = sum(rs.n for _, rs in samples)
-    alg_read_bytes = sum(read_alg_bytes(rs) for _, rs in samples)
-
-    host_ms = {"pileup+realign": 0.0, "score": 0.0, "format": 0.0}
-
-    def kernels_of():
-        return sum(c.timings()["kernels"] for c in ctxs)
-
-    def device_step(collect=None):
-        t0 = time.perf_counter()
-        pair.pileup_realign()
-        t2 = time.perf_counter()
-        pair.score()
-        t3 = time.perf_counter()
-        text, n = pair.format_records("T", "ctg")
-        t4 = time.perf_counter()
-        if collect is not None:
-            host_ms["pileup+realign"] += (t2 - t0) * 1e3
-            host_ms["score"] += (t3 - t2) * 1e3
-            host_ms["format"] += (t4 - t3) * 1e3
-            collect.extend(c.stage_times() for c in ctxs)
-        return kernels_of(), n
-
-    io = {"h2d": 0, "d2h": 0}
-    # e2e: a stream of batches through rv_call_somatic_stream (two context
-    # pairs: one pair's records are formatted on a host thread while the
-    # other pair's next batch is uploaded and piled up); every step uploads
-    # its pinned host batches and reads back its records
-    stream = api.SomaticStream(params, device=local)
-    stream.upload_reference(tumor.contig, synth.genome_str(g).encode())
-    job = (batches[0], batches[1], regions)
+    only = list(range(args.regions)) if args.regions else None
+    t_gen = time.perf_counter()
+    g, tumor, normal, regions = deep_workload(rank, world, only=only)
+    print(f"bench: generated {tumor.n + normal.n} reads in {time.perf_counter() - t_gen:.1f} s", file=sys.stderr)
     clocks = Clocks(local)
-    stream.run([job] * max(1, args.warmup), "T", "ctg")
-    w0 = time.time()
-    t0 = time.perf_counter()
-    e2e_texts = stream.run([job] * args.steps, "T", "ctg")
-    e2e_dt = barrier_max(dist, time.perf_counter() - t0)
-    clocks.window(w0, time.time())
-    last = stream.pairs[(args.steps - 1) % 2]
-    io["h2d"] = sum(c.io_bytes()[0] for c in (last.tumor, last.normal))
-    io["d2h"] = sum(c.io_bytes()[1] for c in (last.tumor, last.normal))
-    # value: the same stream on the batches both pairs now hold (inputs
-    # resident in HBM; no upload in the timed region)
-    resident = (None, None, regions)
-    stream.run([resident] * max(1, args.warmup), "T", "ctg")
-    w0 = time.time()
-    t0 = time.perf_counter()
-    res_texts = stream.run([resident] * args.steps, "T", "ctg")
-    res_dt = barrier_max(dist, time.perf_counter() - t0)
-    clocks.window(w0, time.time())
-    stream.close()
-    pair.submit(batches[0], batches[1], regions)
-    # the same steps one after the other on one pair (no overlap between
-    # steps): stage times, launch counts, and `value_sequential`
-    for _ in range(args.warmup):
-        device_step()
-    stages = []
-    w0 = time.time()
-    t0 = time.perf_counter()
-    kernels = 0
-    recs = 0
-    for _ in range(args.steps):
-        k, recs = device_step(stages)
-        kernels += k
-    dev_dt = barrier_max(dist, time.perf_counter() - t0)
-    clocks.window(w0, time.time())
+    r = measure_pair(g, tumor, normal, regions, args, dist, clocks, local, world)
     clk = clocks.stop()
-    if any(len(t.splitlines()) != recs for t in e2e_texts + res_texts):
-        raise RuntimeError("the streamed batches gave a different record count from the resident steps")
-    ms_per_step = res_dt / args.steps * 1e3
-    value = n_reads * world * args.steps / res_dt
-    value_seq = n_reads * world * args.steps / dev_dt
-    e2e = n_reads * world * args.steps / e2e_dt
-    # roofline of the dominant kernel: the tumor sample's k_pileup_tiles
-    # launch (1.33 M reads), event-timed on its stream.  In the timed steps
-    # the two samples' kernels share the GPU (one stream each), so the launch
-    # is also timed alone, right after the timed region, on the same batch.
-    tile_ms_shared = statistics.mean(s["pileup_tiles"] for s in stages[0::2])
-    solo = []
-    for _ in range(3):
-        pair.tumor.pileup()
-        solo.append(pair.tumor.stage_times()["pileup_tiles"])
-    tile_ms = statistics.mean(solo)
-    cells = sum(r[1] - r[0] + 1 for r in regions)
-    per_launch_bytes = read_alg_bytes(tumor) + cells * 256 + CONTIG  # reads + site records + reference window
-    achieved = per_launch_bytes / (tile_ms * 1e-3) / 1e9
-    peak, peak_kind = measured_peak_hbm()
-    h2d = sum(b.nbytes for b in batches)
+    text = r.pop("text")
     out = {
         "metric": METRIC,
-        "value": value, "unit": "reads/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "value": r["value"], "unit": "reads/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "int32/fp64", "data": "synthetic (seeded)",
-        "config": {"workload": workload(args.local_realign), "reads_per_step": n_reads * world, "l2": "inputs (~0.5 GB) larger than L2, no flush",
-                   "records_per_step": recs},
-        "e2e": {"value": e2e, "unit": "reads/s", "h2d_bytes_per_step": io["h2d"],
-                "d2h_bytes_per_step": io["d2h"]},
-        "value_sequential": {"value": value_seq, "unit": "reads/s",
-                             "note": "the same steps one after the other on one context pair, no overlap"},
-        "gpu_launches": kernels,
-        "stage_ms": {k: statistics.mean(s[k] for s in stages) for k in stages[0]},
-        "host_call_ms_per_step": {k: v / args.steps for k, v in host_ms.items()},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": PILEUP_TRAFFIC[args.local_realign], "peak_kind": peak_kind,
-                     "kernel": "k_pileup_tiles", "launch": "tumor sample, 1.33 M reads, timed alone",
-                     "alg_bytes_per_launch": per_launch_bytes, "launch_ms": tile_ms,
-                     "launch_ms_sharing_gpu": tile_ms_shared},
-        "clocks": clk,
+        "config": {"workload": deep_workload_name(args.local_realign, len(regions)),
+                   "reads_per_step": r["reads_per_step"], "records_per_step": r["records_per_step"],
+                   "l2": "inputs (~22 GB) larger than L2, no flush",
+                   "regions_per_rank": len(regions),
+                   "sharding": "regions LPT-partitioned across ranks (rabbitvar_gb300/shard.py), no collective"},
+        "e2e": r["e2e"], "value_sequential": r["value_sequential"], "gpu_launches": r["gpu_launches"],
+        "stage_ms": r["stage_ms"], "host_call_ms_per_step": r["host_call_ms_per_step"],
+        "roofline": r["roofline"], "clocks": clk, "sites_per_s": r["sites_per_s"], "capacity": r["capacity"],
     }
-    # sites/s: region positions of both samples scored per second of k_score
-    score_ms = statistics.mean(s["score"] for s in stages)
-    out["sites_per_s"] = (sum(r[1] - r[0] + 1 for r in regions)) / (score_ms * 1e-3)
-    pair.close()
-    if rank == 0 and not args.no_bam:
-        out["e2e_from_bam"] = bam_leg(g, tumor, normal, regions, args.local_realign, args.steps, args.warmup, local,
-                                      e2e_texts[0])
+    parity_ok = True
+    if rank == 0 and not args.no_cpu_baseline:
+        # the oracle on four regions of the same reads, one core: the CPU
+        # baseline, and the records check of the GPU's output for them
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        from cmp import diff_records
+        pr = [regions[i] for i in PARITY_REGIONS if i < len(regions)] if only is None and world == 1 else regions[:4]
+        ora, nr, dt = oracle_regions(g, tumor, normal, pr, args.local_realign, threads=1)
+        mine = region_records(text, "ctg", pr)
+        problems = diff_records(ora.splitlines(), mine, somatic=True)
+        parity_ok = not problems and len(mine) == len(ora.splitlines())
+        out["parity"] = {"records_equal": parity_ok, "records": len(mine), "oracle_records": len(ora.splitlines()),
+                         "regions": [f"ctg:{a}-{b}" for a, b in pr], "problems": problems[:3],
+                         "against": "oracle (pinned to the reference binary) on the same reads"}
+        out["cpu_baseline"] = {"value": nr / dt, "unit": "reads/s", "cores": 1, "kind": "port",
+                               "sample": f"{len(pr)} of {len(regions)} regions, tumor+normal ({nr} reads, {dt:.1f} s)"}
+    del text, tumor, normal
     if rank == 0 and not args.no_other_k:
-        out["other_k"] = other_k_leg(g, tumor, normal, regions, 1 - args.local_realign, args.steps,
-                                     args.warmup, local)
+        from types import SimpleNamespace
+        a2 = SimpleNamespace(**vars(args))
+        a2.local_realign = 1 - args.local_realign
+        a2.steps = min(args.steps, 5)
+        a2.warmup = min(args.warmup, 3)
+        g2, t2, n2, regs2 = deep_workload(rank, world, only=only)
+        nclk = type("NoClocks", (), {"window": lambda self, a, b: None})()
+        r2 = measure_pair(g2, t2, n2, regs2, a2, None, nclk, local, 1, roofline=False)
+        out["other_k"] = {"workload": deep_workload_name(a2.local_realign, len(regs2)), "value": r2["value"],
+                          "e2e": r2["e2e"]["value"], "unit": "reads/s", "ms_per_step": r2["ms_per_step"],
+                          "records_per_step": r2["records_per_step"], "steps": a2.steps, "warmup": a2.warmup,
+                          "host_call_ms_per_step": r2["host_call_ms_per_step"]}
+        del t2, n2
+    if rank == 0 and not args.no_1mb:
+        out["somatic_pair_1mb"] = pair_1mb_leg(args, local)
     if rank == 0 and not args.no_learned:
         out["learned_filter"] = learned_filter_leg()
-    if rank == 0 and not args.no_cpu_baseline:
-        v, dt, nr = cpu_baseline_run(g, tumor, normal, regions, 1, CPU_TILES, args.local_realign)
-        out["cpu_baseline"] = {"value": v, "unit": "reads/s", "cores": 1, "kind": "port",
-                               "sample": f"first {CPU_TILES} of 100 10-kb tiles, tumor+normal ({nr} reads, {dt:.1f} s)"}
     if rank == 0:
         print(json.dumps(out))
     if dist is not None:
         dist.destroy_process_group()
+    if not parity_ok:
+        sys.exit(1)
 
 
 if __name__ == "__main__":

@@ -273,6 +273,22 @@ rv_status rv_set_pileup_graph(rv_ctx *ctx, int enable);
 /* Graph launches and graph instantiations of rv_pileup since rv_create. */
 rv_status rv_pileup_graph_stats(const rv_ctx *ctx, int64_t *launches, int64_t *instantiations);
 
+/* Capacities of the context's device tables for the next rv_submit_batch
+ * (0 keeps the automatic size): hash slots of string-keyed alleles (rounded
+ * up to a power of two), bytes of allele-key text, deferred reference-base
+ * subtractions after insertions, and map entries whose pstd/qstd are replayed
+ * in read order.  A table that overflows during rv_pileup grows to what the
+ * run needed and the pileup runs again (at most three times, then
+ * RV_ERR_CAPACITY), so these set where growth starts.  No counterpart in
+ * the reference, whose maps grow on the host heap (include/VariationUtils.h:
+ * 148-195); the automatic sizes follow the keys per read seen so far. */
+rv_status rv_set_capacities(rv_ctx *ctx, size_t hash_slots, size_t arena_bytes, size_t deferred,
+                            size_t order_fix);
+
+/* Pileups run again after a table grew (since rv_create), and the current
+ * hash-slot and key-arena capacities. */
+rv_status rv_capacity_stats(const rv_ctx *ctx, int64_t *retries, int64_t *hash_slots, int64_t *arena_bytes);
+
 /* Bytes copied host->device by the last rv_submit_batch and device->host
  * by the calls since then (realigner boundary, scored candidates). */
 rv_status rv_io_bytes(const rv_ctx *ctx, int64_t *h2d, int64_t *d2h);

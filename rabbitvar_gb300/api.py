@@ -118,6 +118,8 @@ def lib():
     L.rv_stage_times.argtypes = [vp, vp, C.c_int]
     L.rv_set_pileup_graph.argtypes = [vp, C.c_int]
     L.rv_pileup_graph_stats.argtypes = [vp, C.POINTER(i64), C.POINTER(i64)]
+    L.rv_set_capacities.argtypes = [vp, sz, sz, sz, sz]
+    L.rv_capacity_stats.argtypes = [vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64)]
     L.rv_io_bytes.argtypes = [vp, C.POINTER(i64), C.POINTER(i64)]
     L.rv_bam_read.argtypes = [C.c_char_p, C.c_int, C.POINTER(vp)]
     L.rv_bam_contigs.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(vp), C.POINTER(vp)]
@@ -300,6 +302,16 @@ class Context:
         a, b = C.c_int64(), C.c_int64()
         self._check(self.L.rv_pileup_graph_stats(self.h, C.byref(a), C.byref(b)))
         return a.value, b.value
+
+    def set_capacities(self, hash_slots: int = 0, arena_bytes: int = 0, deferred: int = 0, order_fix: int = 0):
+        """Table capacities for the next submit (0 = automatic); a table that
+        overflows grows and the pileup runs again."""
+        self._check(self.L.rv_set_capacities(self.h, hash_slots, arena_bytes, deferred, order_fix))
+
+    def capacity_stats(self) -> dict:
+        r, h, a = C.c_int64(), C.c_int64(), C.c_int64()
+        self._check(self.L.rv_capacity_stats(self.h, C.byref(r), C.byref(h), C.byref(a)))
+        return {"retries": r.value, "hash_slots": h.value, "arena_bytes": a.value}
 
     def score_candidates(self, min_count: int = 2):
         self._check(self.L.rv_score_candidates(self.h, min_count))

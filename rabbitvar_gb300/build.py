@@ -18,6 +18,9 @@ LIB = os.path.join(HERE, "librvgpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU = ["rv_pileup.cu", "rv_score.cu", "rv_util.cu", "rv_noalloc.cu", "rv_mlp.cu", "rv_bgzf.cu"]
 CPP = ["rv_capi.cpp", "rv_host.cpp", "rv_realign.cpp", "rv_records.cpp", "rv_somatic.cpp", "rv_bam.cpp", "rv_pool.cpp"]
+# the native generator of the large synthetic workloads (host only, its own library)
+SYNTH_SRC = "rv_synth.cpp"
+SYNTH_LIB = os.path.join(HERE, "librvsynth.so")
 
 
 def _nvcc() -> str:
@@ -70,9 +73,12 @@ def build(verbose: bool = False) -> str:
             raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
         return r
 
+    synth_src = os.path.join(CSRC, SYNTH_SRC)
+    if _needs(SYNTH_LIB, [synth_src]):
+        jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", synth_src, "-o", SYNTH_LIB])
     with cf.ThreadPoolExecutor(max_workers=min(8, max(1, len(jobs)))) as ex:
         list(ex.map(run, jobs))
-    if jobs or not os.path.exists(LIB):
+    if _needs(LIB, objs):
         run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"])
     return LIB
 

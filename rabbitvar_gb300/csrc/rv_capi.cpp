@@ -56,6 +56,47 @@ unsigned long long next_pow2(unsigned long long x) {
 
 enum { CNT_TILE = 0, CNT_DEFER = 1, CNT_USED = 2, CNT_ERR = 3, CNT_CAND = 4, CNT_AUX = 5, CNT_FIX = 6 };
 
+// (Re)allocates the hash table and its used-slot list with `cap` slots.
+rv_status alloc_hash(rv_ctx *ctx, unsigned long long cap) {
+    if (ctx->d_slots) cudaFree(ctx->d_slots);
+    if (ctx->d_used) cudaFree(ctx->d_used);
+    ctx->d_slots = nullptr;
+    ctx->d_used = nullptr;
+    ctx->hash_cap = 0;
+    RV_CUDA(cudaMalloc((void **)&ctx->d_slots, cap * sizeof(Slot)));
+    RV_CUDA(cudaMalloc((void **)&ctx->d_used, cap * sizeof(uint32_t)));
+    ctx->hash_cap = cap;
+    ctx->slots_fresh = true;
+    return RV_OK;
+}
+
+rv_status alloc_arena(rv_ctx *ctx, unsigned long long cap) {
+    if (ctx->d_arena) cudaFree(ctx->d_arena);
+    ctx->d_arena = nullptr;
+    ctx->arena_cap = 0;
+    RV_CUDA(cudaMalloc((void **)&ctx->d_arena, cap));
+    ctx->arena_cap = cap;
+    return RV_OK;
+}
+
+rv_status alloc_deferred(rv_ctx *ctx, unsigned int cap) {
+    if (ctx->d_deferred) cudaFree(ctx->d_deferred);
+    ctx->d_deferred = nullptr;
+    ctx->deferred_cap = 0;
+    RV_CUDA(cudaMalloc((void **)&ctx->d_deferred, (size_t)cap * sizeof(Deferred)));
+    ctx->deferred_cap = cap;
+    return RV_OK;
+}
+
+rv_status alloc_fix(rv_ctx *ctx, unsigned int cap) {
+    if (ctx->d_ofix) cudaFree(ctx->d_ofix);
+    ctx->d_ofix = nullptr;
+    ctx->ofix_cap = 0;
+    RV_CUDA(cudaMalloc((void **)&ctx->d_ofix, (size_t)cap * sizeof(OrderFix)));
+    ctx->ofix_cap = cap;
+    return RV_OK;
+}
+
 }  // namespace
 
 DevState rv_ctx::state() const {
@@ -87,6 +128,7 @@ DevState rv_ctx::state() const {
     s.hash.arena_cap = arena_cap;
     s.hash.arena_used = (unsigned long long *)(d_counters + 8);
     s.hash.n_used = d_counters + CNT_USED;
+    s.hash.used = d_used;
     s.deferred = d_deferred;
     s.n_deferred = d_counters + CNT_DEFER;
     s.deferred_cap = deferred_cap;
@@ -312,7 +354,7 @@ void rv_destroy(rv_ctx *ctx) {
                     ctx->d_tmp_slots, ctx->d_tmp_cells, ctx->d_tmp_views, ctx->d_tmp_n, ctx->d_list,
                     ctx->d_ftab, ctx->d_logfact, ctx->d_skip, ctx->d_patches, ctx->d_patch_keys,
                     ctx->d_list_off, ctx->d_list_bsum, ctx->d_list_idx, ctx->d_list_slots,
-                    ctx->d_cons_meta, ctx->d_cons, ctx->d_ofix};
+                    ctx->d_cons_meta, ctx->d_cons, ctx->d_ofix, ctx->d_used};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (ctx->h_mirror) cudaFreeHost(ctx->h_mirror);
@@ -630,34 +672,29 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
         C.kflags = (uint8_t *)m;
         C.n_cells = ctx->n_cells;
     }
-    // hash table / arena / deferred / candidates sized from the batch
-    unsigned long long want_hash = next_pow2(std::max<unsigned long long>(1ULL << 16, (unsigned long long)n));
-    if (want_hash > ctx->hash_cap || !ctx->d_slots) {
-        if (ctx->d_slots) cudaFree(ctx->d_slots);
-        ctx->d_slots = nullptr;
-        RV_CUDA(cudaMalloc((void **)&ctx->d_slots, want_hash * sizeof(Slot)));
-        ctx->hash_cap = want_hash;
-    }
-    unsigned long long want_arena = std::max<unsigned long long>(1ULL << 20, (unsigned long long)n * 16);
-    if (want_arena > ctx->arena_cap || !ctx->d_arena) {
-        if (ctx->d_arena) cudaFree(ctx->d_arena);
-        ctx->d_arena = nullptr;
-        RV_CUDA(cudaMalloc((void **)&ctx->d_arena, want_arena));
-        ctx->arena_cap = want_arena;
-    }
-    unsigned int want_def = (unsigned int)std::min<int64_t>(INT32_MAX, n / 8 + 4096);
-    if (want_def > ctx->deferred_cap || !ctx->d_deferred) {
-        if (ctx->d_deferred) cudaFree(ctx->d_deferred);
-        ctx->d_deferred = nullptr;
-        RV_CUDA(cudaMalloc((void **)&ctx->d_deferred, (size_t)want_def * sizeof(Deferred)));
-        ctx->deferred_cap = want_def;
-    }
-    unsigned int want_fix = (unsigned int)std::min<int64_t>(INT32_MAX, n / 64 + 4096);
-    if (want_fix > ctx->ofix_cap || !ctx->d_ofix) {
-        if (ctx->d_ofix) cudaFree(ctx->d_ofix);
-        ctx->d_ofix = nullptr;
-        RV_CUDA(cudaMalloc((void **)&ctx->d_ofix, (size_t)want_fix * sizeof(OrderFix)));
-        ctx->ofix_cap = want_fix;
+    // hash table / arena / deferred / order-fix list sized from the batch (or
+    // the capacities rv_set_capacities forced for this batch); every table
+    // grows when a pileup overflows it (pileup_finish runs the pileup again)
+    {
+        const double est = ctx->keys_per_read > 0 ? 2.5 * ctx->keys_per_read * (double)n : (double)n;
+        unsigned long long want = next_pow2(std::max<unsigned long long>(1ULL << 16, (unsigned long long)est));
+        if (ctx->force_hash) want = next_pow2(ctx->force_hash);
+        if (want > ctx->hash_cap || !ctx->d_slots || (ctx->force_hash && want != ctx->hash_cap))
+            if ((st = alloc_hash(ctx, want))) return st;
+        unsigned long long want_arena = std::max<unsigned long long>(1ULL << 20, (unsigned long long)n * 16);
+        if (ctx->force_arena) want_arena = ctx->force_arena;
+        if (want_arena > ctx->arena_cap || !ctx->d_arena || (ctx->force_arena && want_arena != ctx->arena_cap))
+            if ((st = alloc_arena(ctx, want_arena))) return st;
+        unsigned int want_def = (unsigned int)std::min<int64_t>(INT32_MAX, n / 8 + 4096);
+        if (ctx->force_deferred) want_def = ctx->force_deferred;
+        if (want_def > ctx->deferred_cap || !ctx->d_deferred || (ctx->force_deferred && want_def != ctx->deferred_cap))
+            if ((st = alloc_deferred(ctx, want_def))) return st;
+        unsigned int want_fix = (unsigned int)std::min<int64_t>(INT32_MAX, n / 64 + 4096);
+        if (ctx->force_fix) want_fix = ctx->force_fix;
+        if (want_fix > ctx->ofix_cap || !ctx->d_ofix || (ctx->force_fix && want_fix != ctx->ofix_cap))
+            if ((st = alloc_fix(ctx, want_fix))) return st;
+        ctx->force_hash = ctx->force_arena = 0;
+        ctx->force_deferred = ctx->force_fix = 0;
     }
     unsigned int want_cand = (unsigned int)std::min<int64_t>(INT32_MAX, std::max<int64_t>(1 << 16, score / 4 + 1024));
     if (want_cand > ctx->cand_cap || !ctx->d_cand) {
@@ -700,9 +737,13 @@ rv_status queue_pileup_chain(rv_ctx *ctx, cudaStream_t s, int grid, int variant,
     size_t cap = ctx->cap_cells;
     RV_CUDA(cudaMemsetAsync(ctx->d_cellmem, 0, cap * (8 * 16 + 4 + 1), s));
     RV_CUDA(cudaMemsetAsync(ctx->d_head, 0xFF, cap * 8, s));
+    // the slots the previous run claimed (its used-slot list, whose length is
+    // still in the counters), or the whole table when it was just allocated
+    if (ctx->slots_fresh) launch_init_slots(ctx->d_slots, ctx->hash_cap, s);
+    else launch_clear_used(ctx->d_slots, ctx->d_used, ctx->d_counters + CNT_USED, ctx->hash_cap, s);
+    ctx->slots_fresh = false;
     RV_CUDA(cudaMemsetAsync(ctx->d_counters, 0, 64 * sizeof(unsigned int), s));
     RV_CUDA(cudaMemsetAsync(ctx->d_arena, 0, 16, s));
-    launch_init_slots(ctx->d_slots, ctx->hash_cap, s);
     DevState st = ctx->state();
     if (marks) RV_CUDA(cudaEventRecord(ctx->ev[4], s));
     launch_region_reset(st, s);
@@ -797,13 +838,56 @@ rv_status pileup_launch(rv_ctx *ctx, cudaStream_t s) {
 }
 
 // Waits for the pileup queued by pileup_launch; timings, autotuner, errors.
+// A table that overflowed (hash slots, key arena, deferred subtractions,
+// order-dependent entries: the kernels set an error bit and drop the
+// observation) is grown to what the run needed and the pileup runs again,
+// up to kRetries times; the realigner mirror queued behind the failed run is
+// queued again behind the new one.
 rv_status pileup_finish(rv_ctx *ctx, cudaStream_t s) {
     if (!ctx->pileup_pending) { ctx->err = "no pileup in flight"; return RV_ERR_STATE; }
     ctx->pileup_pending = false;
     RV_CUDA(cudaSetDevice(ctx->device));
-    unsigned int err = 0;
-    RV_CUDA(cudaMemcpyAsync(&err, ctx->d_counters + CNT_ERR, 4, cudaMemcpyDeviceToHost, s));
-    RV_CUDA(cudaStreamSynchronize(s));
+    constexpr int kRetries = 3;
+    constexpr unsigned int kCapBits = ERR_HASH_FULL | ERR_ARENA_FULL | ERR_DEFER_FULL | ERR_FIX_FULL;
+    unsigned int cnt[16];
+    bool retried = false;
+    for (int attempt = 0;; attempt++) {
+        RV_CUDA(cudaMemcpyAsync(cnt, ctx->d_counters, sizeof cnt, cudaMemcpyDeviceToHost, s));
+        RV_CUDA(cudaStreamSynchronize(s));
+        const unsigned int cap = cnt[CNT_ERR] & kCapBits;
+        if (!cap || attempt >= kRetries) break;
+        rv_status st;
+        if (cap & ERR_HASH_FULL) {
+            // at least one slot per read (the automatic size before any keys
+            // were counted), at least four times the table that overflowed
+            const unsigned long long want = std::max<unsigned long long>(
+                ctx->hash_cap * 4, next_pow2(std::max<unsigned long long>(1ULL << 16, (unsigned long long)ctx->n_reads)));
+            if ((st = alloc_hash(ctx, want))) return st;
+        }
+        if (cap & ERR_ARENA_FULL) {
+            unsigned long long need;
+            memcpy(&need, cnt + 8, sizeof need);  // arena_used counts every key, also those that did not fit
+            need = std::max<unsigned long long>(need, ctx->arena_cap);
+            if ((st = alloc_arena(ctx, need + need / 2 + (1ULL << 20)))) return st;
+        }
+        if (cap & ERR_DEFER_FULL) {
+            const unsigned long long need = std::max<unsigned long long>(cnt[CNT_DEFER], ctx->deferred_cap);
+            if ((st = alloc_deferred(ctx, (unsigned int)std::min<unsigned long long>(INT32_MAX, need + need / 2 + 4096))))
+                return st;
+        }
+        if (cap & ERR_FIX_FULL) {
+            const unsigned long long need = std::max<unsigned long long>(cnt[CNT_FIX], ctx->ofix_cap);
+            if ((st = alloc_fix(ctx, (unsigned int)std::min<unsigned long long>(INT32_MAX, need + need / 2 + 4096))))
+                return st;
+        }
+        const bool mirror = ctx->mirror_pending;
+        if ((st = pileup_launch(ctx, s))) return st;
+        ctx->pileup_pending = false;
+        if (mirror && (st = mirror_launch(ctx, nullptr))) return st;
+        ctx->capacity_retries++;
+        retried = true;
+    }
+    const unsigned int err = cnt[CNT_ERR];
     const int nvar = pileup_variants(), variant = ctx->variant;
     float ms = 0;
     cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
@@ -821,7 +905,8 @@ rv_status pileup_finish(rv_ctx *ctx, cudaStream_t s) {
         cudaEventElapsedTime(&ms, ctx->ev[7], ctx->ev[1]);
         ctx->stage_ms[4] = ms;
     }
-    if (!ctx->pileup_pin && ctx->variant_runs < nvar) {
+    // (a run after a table grew starts from a whole-table reset: not a fair trial)
+    if (!ctx->pileup_pin && ctx->variant_runs < nvar && !retried) {
         ctx->variant_ms[variant] = ctx->stage_ms[2];
         ctx->variant_runs++;
     }
@@ -829,10 +914,12 @@ rv_status pileup_finish(rv_ctx *ctx, cudaStream_t s) {
         char buf[160];
         snprintf(buf, sizeof buf, "pileup device error bits 0x%x", err);
         ctx->err = buf;
-        if (err & (ERR_HASH_FULL | ERR_ARENA_FULL | ERR_DEFER_FULL | ERR_FIX_FULL)) return RV_ERR_CAPACITY;
+        if (err & kCapBits) return RV_ERR_CAPACITY;
         if (err & ERR_COLLISION) return RV_ERR_COLLISION;
         return RV_ERR_UNSUPPORTED;
     }
+    if (ctx->n_reads > 0)
+        ctx->keys_per_read = std::max(ctx->keys_per_read, (double)cnt[CNT_USED] / (double)ctx->n_reads);
     ctx->stage = 2;
     return RV_OK;
 }
@@ -1241,6 +1328,28 @@ rv_status rv_set_pileup_graph(rv_ctx *ctx, int enable) {
     if (!ctx) return RV_ERR_ARG;
     if (ctx->pileup_pending) { ctx->err = "rv_set_pileup_graph while a pileup is in flight"; return RV_ERR_STATE; }
     ctx->use_graph = enable != 0;
+    return RV_OK;
+}
+
+rv_status rv_set_capacities(rv_ctx *ctx, size_t hash_slots, size_t arena_bytes, size_t deferred, size_t order_fix) {
+    if (!ctx) return RV_ERR_ARG;
+    if (ctx->pileup_pending) { ctx->err = "rv_set_capacities while a pileup is in flight"; return RV_ERR_STATE; }
+    if (deferred > (size_t)INT32_MAX || order_fix > (size_t)INT32_MAX || hash_slots > (1ULL << 32)) {
+        ctx->err = "rv_set_capacities: capacity out of range";
+        return RV_ERR_ARG;
+    }
+    ctx->force_hash = hash_slots;
+    ctx->force_arena = arena_bytes;
+    ctx->force_deferred = (unsigned int)deferred;
+    ctx->force_fix = (unsigned int)order_fix;
+    return RV_OK;
+}
+
+rv_status rv_capacity_stats(const rv_ctx *ctx, int64_t *retries, int64_t *hash_slots, int64_t *arena_bytes) {
+    if (!ctx) return RV_ERR_ARG;
+    if (retries) *retries = ctx->capacity_retries;
+    if (hash_slots) *hash_slots = (int64_t)ctx->hash_cap;
+    if (arena_bytes) *arena_bytes = (int64_t)ctx->arena_cap;
     return RV_OK;
 }
 

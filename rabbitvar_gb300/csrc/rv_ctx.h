@@ -14,6 +14,8 @@ namespace rv {
 
 // kernel launchers (rv_pileup.cu, rv_score.cu)
 void launch_init_slots(Slot *slots, unsigned long long n, cudaStream_t s);
+void launch_clear_used(Slot *slots, const uint32_t *used, const unsigned int *n_used, unsigned long long cap,
+                       cudaStream_t s);
 void launch_region_reset(const DevState &st, cudaStream_t s);
 cudaError_t launch_pileup(const DevState &st, const DevParams &P, int grid, cudaStream_t s, int variant);
 int pileup_variants();
@@ -152,6 +154,13 @@ struct rv_ctx {
     // hash
     unsigned long long hash_cap = 0;
     rv::Slot *d_slots = nullptr;
+    uint32_t *d_used = nullptr;       // used-slot list (hash_cap entries)
+    bool slots_fresh = true;          // the table needs a whole-table reset (just allocated)
+    double keys_per_read = 0;         // largest keys / reads seen (sizes the next table)
+    // capacities forced by rv_set_capacities for the next batch (0 = automatic)
+    unsigned long long force_hash = 0, force_arena = 0;
+    unsigned int force_deferred = 0, force_fix = 0;
+    int64_t capacity_retries = 0;     // pileups run again after a table grew
     uint8_t *d_arena = nullptr;
     unsigned long long arena_cap = 0;
 

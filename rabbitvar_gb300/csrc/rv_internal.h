@@ -124,8 +124,24 @@ struct Hash {
     uint8_t *arena;
     unsigned long long arena_cap;
     unsigned long long *arena_used;
-    unsigned int *n_used;
+    unsigned int *n_used;      // slots claimed so far
+    uint32_t *used;            // their indexes, in claim order (mask + 1 entries):
+                               // scans and the next reset visit only these
 };
+
+#ifdef __CUDACC__
+// Number of valid entries of the used-slot list.
+__device__ __forceinline__ unsigned long long used_count(const Hash &H) {
+    const unsigned long long n = *H.n_used;
+    return n <= H.mask ? n : H.mask + 1ULL;
+}
+
+// Claims the next entry of the used-slot list for slot i.
+__device__ __forceinline__ void note_used(const Hash &H, unsigned long long i) {
+    const unsigned int k = atomicAdd(H.n_used, 1u);
+    if ((unsigned long long)k <= H.mask) H.used[k] = (uint32_t)i;
+}
+#endif
 
 // Deferred subtraction of a reference-base observation after an insertion
 // (src/parseCigar.cpp:1471-1490): applied only if the key existed when the

@@ -46,7 +46,7 @@ __device__ Slot *hash_get(const Hash &H, unsigned int *err, int region, int kind
                 s->koff = (uint32_t)off;
                 for (int j = 0; j < n; j++) H.arena[off + j] = (uint8_t)k[j];
             }
-            atomicAdd(H.n_used, 1u);
+            note_used(H, i);
             atomicXor(&s->h2x, h2);
             return s;
         }
@@ -97,26 +97,40 @@ __device__ void slot_obs(const DevState &st, Slot *s, const Obs &o, double goodq
     }
 }
 
+__device__ __forceinline__ void clear_slot(Slot &s) {
+    s.fp = 0;
+    s.h2x = 0;
+    s.region = 0;
+    s.pos = 0;
+    s.kind = 0;
+    s.klen = 0;
+    s.koff = 0;
+    s.fwd = s.rev = s.hi = s.lo = s.obs = s.extracnt = 0;
+    s.tp_sum = s.mq_sum = s.nm_sum = 0;
+    s.q_sum = 0.0;
+    s.first_q = 0xFFF8DEADBEEF0001ULL;
+    s.first_tp = INT32_MIN;
+    s.flags = 0;
+    s.min_stamp = 0xFFFFFFFFu;
+    s.next = 0xFFFFFFFFu;
+}
+
+// Whole table (a table just allocated).
 __global__ void k_init_slots(Slot *slots, unsigned long long n) {
     for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
-         i += (unsigned long long)gridDim.x * blockDim.x) {
-        Slot &s = slots[i];
-        s.fp = 0;
-        s.h2x = 0;
-        s.region = 0;
-        s.pos = 0;
-        s.kind = 0;
-        s.klen = 0;
-        s.koff = 0;
-        s.fwd = s.rev = s.hi = s.lo = s.obs = s.extracnt = 0;
-        s.tp_sum = s.mq_sum = s.nm_sum = 0;
-        s.q_sum = 0.0;
-        s.first_q = 0xFFF8DEADBEEF0001ULL;
-        s.first_tp = INT32_MIN;
-        s.flags = 0;
-        s.min_stamp = 0xFFFFFFFFu;
-        s.next = 0xFFFFFFFFu;
-    }
+         i += (unsigned long long)gridDim.x * blockDim.x)
+        clear_slot(slots[i]);
+}
+
+// Only the slots the previous run claimed (its used-slot list); the count is
+// read before the counters are reset.
+__global__ void k_clear_used(Slot *slots, const uint32_t *used, const unsigned int *n_used,
+                             unsigned long long cap) {
+    unsigned long long n = *n_used;
+    if (n > cap) n = cap;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x)
+        clear_slot(slots[used[i]]);
 }
 
 // ---------------------------------------------------------------------------
@@ -764,6 +778,11 @@ __global__ void k_fix_order(DevState st, DevParams P) {
 // ---------------------------------------------------------------------------
 void launch_init_slots(Slot *slots, unsigned long long n, cudaStream_t s) {
     k_init_slots<<<592, 256, 0, s>>>(slots, n);
+}
+
+void launch_clear_used(Slot *slots, const uint32_t *used, const unsigned int *n_used, unsigned long long cap,
+                       cudaStream_t s) {
+    k_clear_used<<<592, 256, 0, s>>>(slots, used, n_used, cap);
 }
 
 void launch_region_reset(const DevState &st, cudaStream_t s) {

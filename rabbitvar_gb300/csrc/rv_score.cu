@@ -21,9 +21,10 @@ __device__ __forceinline__ int64_t cell_index(const Region &R, int p) { return R
 
 // Link every string-keyed allele into the list of its position.
 __global__ void k_link_slots(DevState st) {
-    unsigned long long n = st.hash.mask + 1ULL;
-    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
-         i += (unsigned long long)gridDim.x * blockDim.x) {
+    unsigned long long n = used_count(st.hash);
+    for (unsigned long long u = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; u < n;
+         u += (unsigned long long)gridDim.x * blockDim.x) {
+        const uint32_t i = st.hash.used[u];
         Slot &s = st.hash.slots[i];
         if (s.fp == 0ULL || s.kind == KIND_SPLICE) continue;
         const Region &R = st.regions[s.region];
@@ -37,10 +38,10 @@ __global__ void k_link_slots(DevState st) {
 __global__ void k_check_collisions(DevState st) {
     // every inserter XORs h2 of its key into the slot: for an odd number of
     // inserters of one key the result is h2, for an even number it is 0
-    unsigned long long n = st.hash.mask + 1ULL;
-    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
-         i += (unsigned long long)gridDim.x * blockDim.x) {
-        const Slot &s = st.hash.slots[i];
+    unsigned long long n = used_count(st.hash);
+    for (unsigned long long u = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; u < n;
+         u += (unsigned long long)gridDim.x * blockDim.x) {
+        const Slot &s = st.hash.slots[st.hash.used[u]];
         if (s.fp == 0ULL) continue;
         unsigned long long h1, h2;
         unsigned long long a = fmix64(((unsigned long long)(uint32_t)s.region << 32) ^ (uint32_t)s.pos ^

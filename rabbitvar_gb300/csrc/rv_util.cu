@@ -10,10 +10,11 @@
 namespace rv {
 
 __global__ void k_compact_slots(DevState st, uint32_t *out, unsigned int *n_out) {
-    unsigned long long n = st.hash.mask + 1ULL;
-    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
-         i += (unsigned long long)gridDim.x * blockDim.x) {
-        if (st.hash.slots[i].fp != 0ULL) out[atomicAdd(n_out, 1u)] = (uint32_t)i;
+    unsigned long long n = used_count(st.hash);
+    for (unsigned long long u = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; u < n;
+         u += (unsigned long long)gridDim.x * blockDim.x) {
+        const uint32_t i = st.hash.used[u];
+        if (st.hash.slots[i].fp != 0ULL) out[atomicAdd(n_out, 1u)] = i;
     }
 }
 
@@ -84,7 +85,7 @@ __device__ void create_slot(const DevState &st, const Patch &q, const uint8_t *k
                 s.koff = (uint32_t)off;
                 for (int j = 0; j < q.klen; j++) H.arena[off + j] = (uint8_t)k[j];
             }
-            atomicAdd(H.n_used, 1u);
+            note_used(H, i);
             s.h2x = h2;
             set_override(s, q);
             const Region &R = st.regions[q.region];
@@ -362,9 +363,10 @@ void launch_clip_consensus(const DevState &st, const uint32_t *off, const Slot *
 
 // MNP keys (A/C/G/T '&' A/C/G/T...) that the realigner's adjustMNP visits.
 __global__ void k_select_mnv(DevState st, uint32_t *out, unsigned int *n_out) {
-    unsigned long long n = st.hash.mask + 1ULL;
-    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
-         i += (unsigned long long)gridDim.x * blockDim.x) {
+    unsigned long long n = used_count(st.hash);
+    for (unsigned long long u = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; u < n;
+         u += (unsigned long long)gridDim.x * blockDim.x) {
+        const uint32_t i = st.hash.used[u];
         const Slot &s = st.hash.slots[i];
         if (s.fp == 0ULL || s.kind != KIND_NONINS || (s.flags & SF_ERASED) || s.obs <= 0 || s.klen < 3) continue;
         const uint8_t *k = st.hash.arena + s.koff;

@@ -66,9 +66,10 @@ class ReadSet:
     cigar: np.ndarray
     l_qseq: np.ndarray
     base_off: np.ndarray
-    seq4: np.ndarray
+    seq4: np.ndarray | None
     qual: np.ndarray
     name_id: np.ndarray
+    packed: np.ndarray | None = None   # BAM-packed bases (native generator; seq4 is then None)
 
     @property
     def n(self) -> int:
@@ -77,6 +78,8 @@ class ReadSet:
     def packed_seq(self) -> np.ndarray:
         """BAM-packed 4-bit sequence (two bases per byte, high nibble first),
         indexed by base_off // 2 for every read."""
+        if self.packed is not None:
+            return self.packed
         s = self.seq4
         if s.shape[0] % 2:
             s = np.concatenate([s, np.zeros(1, np.uint8)])
@@ -86,6 +89,40 @@ class ReadSet:
 def subset(rs: ReadSet, keep: np.ndarray) -> ReadSet:
     """The reads of `rs` where `keep` is true, in the same order and layout."""
     return take(rs, np.nonzero(keep)[0])
+
+
+def unpacked(rs: ReadSet) -> ReadSet:
+    """The same reads with one 4-bit code per byte (seq4), as the numpy
+    generator holds them (a read set of the native generator has only the
+    packed bases)."""
+    if rs.seq4 is not None:
+        return rs
+    seq4 = np.empty(rs.packed.shape[0] * 2, dtype=np.uint8)
+    seq4[0::2] = rs.packed >> 4
+    seq4[1::2] = rs.packed & 15
+    return dataclasses.replace(rs, seq4=seq4, packed=None)
+
+
+def read_range(rs: ReadSet, a: int, b: int) -> ReadSet:
+    """Reads [a, b) of `rs` (a contiguous, coordinate-sorted slice) with
+    unpacked bases."""
+    stride = int(rs.base_off[1] - rs.base_off[0]) if rs.n > 1 else 160
+    c0 = int(rs.cig_off[a]) if a < rs.n else int(rs.cigar.shape[0])
+    c1 = int(rs.cig_off[b]) if b < rs.n else int(rs.cigar.shape[0])
+    b0, b1 = a * stride, b * stride
+    if rs.packed is not None:
+        pk = rs.packed[b0 // 2:b1 // 2]
+        seq4 = np.empty(pk.shape[0] * 2, dtype=np.uint8)
+        seq4[0::2] = pk >> 4
+        seq4[1::2] = pk & 15
+    else:
+        seq4 = rs.seq4[b0:b1].copy()
+    return ReadSet(contig=rs.contig, contig_len=rs.contig_len, pos=rs.pos[a:b].copy(), flag=rs.flag[a:b].copy(),
+                   mapq=rs.mapq[a:b].copy(), mpos=rs.mpos[a:b].copy(), isize=rs.isize[a:b].copy(),
+                   nm=rs.nm[a:b].copy(), n_cigar=rs.n_cigar[a:b].copy(),
+                   cig_off=(rs.cig_off[a:b] - np.uint32(c0)).astype(np.uint32), cigar=rs.cigar[c0:c1].copy(),
+                   l_qseq=rs.l_qseq[a:b].copy(), base_off=(rs.base_off[a:b] - np.uint64(b0)).astype(np.uint64),
+                   seq4=seq4, qual=rs.qual[b0:b1].copy(), name_id=rs.name_id[a:b].copy())
 
 
 def take(rs: ReadSet, idx: np.ndarray) -> ReadSet:
@@ -799,3 +836,186 @@ def dense_multi(seed: int = 0x5EED00D0, length: int = 60_000, depth: float = 60.
     vs = plant_variants(g, rng, 4e-3, 1e-3, lambda r: r.choice([0.2, 0.5, 1.0]), mnv_frac=0.2, spacing=12)
     rs = simulate(g, vs, depth, rng, softclip_frac=0.06, n_rate=1e-3, tail_margin=300)
     return g, vs, rs
+
+
+# --------------------------------------------------------------------------
+# native generator (rv_synth.cpp -> librvsynth.so) for the large workloads
+# --------------------------------------------------------------------------
+_KIND_CODE = {"snv": 0, "mnv": 1, "ins": 2, "del": 3}
+_native = None
+
+
+def _native_lib():
+    global _native
+    if _native is None:
+        import ctypes as C
+        import os
+        path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "librvsynth.so")
+        if not os.path.exists(path):
+            from . import build
+            build.build()
+        L = C.CDLL(path)
+        L.rvs_region_reads.restype = C.c_int64
+        L.rvs_region_reads.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
+        L.rvs_simulate_region.restype = C.c_int64
+        L.rvs_simulate_region.argtypes = ([C.c_void_p, C.c_int64, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
+                                           C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int64] +
+                                          [C.c_void_p] * 11)
+        L.rvs_max_ops.restype = C.c_int
+        _native = L
+    return _native
+
+
+_VAR_DT = np.dtype([("pos", np.int64), ("kind", np.int32), ("ref_len", np.int32), ("alt_off", np.int32),
+                    ("alt_len", np.int32), ("vaf", np.float64), ("strand_bias", np.float64), ("strand", np.int32),
+                    ("vq", np.int32)], align=True)
+_PAR_DT = np.dtype([("seed", np.uint64), ("read_len", np.int32), ("amplicon", np.int32), ("depth", np.float64),
+                    ("lo", np.int64), ("hi", np.int64), ("insert_mean", np.float64), ("insert_sd", np.float64),
+                    ("softclip_frac", np.float64), ("mapq0_frac", np.float64), ("n_rate", np.float64),
+                    ("artifact_rate", np.float64), ("artifact_q", np.int32), ("tail_margin", np.int32),
+                    ("name_base", np.int64), ("dup_frac", np.float64)], align=True)
+
+
+def _variant_table(variants: list[Variant]):
+    tab = np.zeros(len(variants), dtype=_VAR_DT)
+    alt = bytearray()
+    for i, v in enumerate(variants):
+        tab[i]["pos"] = v.pos
+        tab[i]["kind"] = _KIND_CODE[v.kind]
+        tab[i]["ref_len"] = len(v.ref) if v.kind == "del" else max(len(v.alt), 1)
+        tab[i]["alt_off"] = len(alt)
+        tab[i]["alt_len"] = len(v.alt)
+        tab[i]["vaf"] = v.vaf
+        tab[i]["strand_bias"] = v.strand_bias
+        tab[i]["strand"] = v.strand
+        tab[i]["vq"] = v.vq or 0
+        alt += bytes("ACGT".index(c) for c in v.alt)
+    return tab, np.frombuffer(bytes(alt) or b"\0", dtype=np.uint8)
+
+
+def simulate_regions(genome: np.ndarray, variants: list[Variant], spans: list[tuple[int, int]], depth, seed: int,
+                     contig: str = "ctg", read_len: int = 150, softclip_frac: float = 0.02,
+                     mapq0_frac: float = 0.05, n_rate: float = 2e-4, artifact_rate: float = 0.0,
+                     artifact_q: int = 0, name_base: int = 0, amplicons=None, dup_frac: float = 0.0,
+                     threads: int | None = None, span_ids: list[int] | None = None) -> ReadSet:
+    """Reads over disjoint, ascending `spans` (0-based, half-open) from the
+    native generator, one seeded stream per span (`depth` a number or one
+    per span): 2x`read_len` pairs with fragments over each span (or, with
+    `amplicons` = per span a list of (lo, hi, pairs), the given amplicons),
+    the same error / quality / clip / MAPQ model as `simulate`.  Spans must
+    be far enough apart that their reads do not interleave (the result is
+    the concatenation of the per-span sorted reads).  `span_ids` picks the
+    spans to generate (each span's stream is seeded by its index, so a span
+    gives the same reads alone as in the whole set).  Returns a ReadSet with
+    packed bases (seq4 None)."""
+    import concurrent.futures as cf
+    import ctypes as C
+    import os
+    L = _native_lib()
+    G = genome.shape[0]
+    g = np.ascontiguousarray(genome, dtype=np.uint8)
+    vt, alt = _variant_table(sorted(variants, key=lambda v: v.pos))
+    vpos = vt["pos"]
+    depths = [float(depth)] * len(spans) if np.isscalar(depth) else [float(d) for d in depth]
+    ids = list(range(len(spans))) if span_ids is None else list(span_ids)
+    pars, counts, amp = [], [], []
+    for i in ids:
+        lo, hi = spans[i]
+        p = np.zeros(1, dtype=_PAR_DT)
+        p["seed"] = np.uint64((seed * 0x9E3779B97F4A7C15 + i * 0xD1B54A32D192ED03) % (1 << 64))
+        p["read_len"] = read_len
+        p["depth"] = depths[i]
+        p["lo"], p["hi"] = lo, hi
+        p["insert_mean"], p["insert_sd"] = 350.0, 50.0
+        p["softclip_frac"], p["mapq0_frac"], p["n_rate"] = softclip_frac, mapq0_frac, n_rate
+        p["artifact_rate"], p["artifact_q"] = artifact_rate, artifact_q
+        p["name_base"] = name_base + i * 100_000_000
+        p["dup_frac"] = dup_frac
+        a_lo = a_hi = a_n = None
+        if amplicons is not None and i < len(amplicons):
+            p["amplicon"] = 1
+            arr = np.array(amplicons[i], dtype=np.int64).reshape(-1, 3)
+            a_lo, a_hi, a_n = (np.ascontiguousarray(arr[:, 0]), np.ascontiguousarray(arr[:, 1]),
+                               np.ascontiguousarray(arr[:, 2].astype(np.int32)))
+        amp.append((a_lo, a_hi, a_n))
+        pars.append(p)
+        counts.append(int(L.rvs_region_reads(p.ctypes.data, a_n.ctypes.data if a_n is not None else None,
+                                             len(a_n) if a_n is not None else 0)))
+    n = sum(counts)
+    off = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+    stride = (read_len + 31) // 32 * 32
+    pos = np.empty(n, np.int32)
+    mpos = np.empty(n, np.int32)
+    isize = np.empty(n, np.int32)
+    nm = np.empty(n, np.int32)
+    flag = np.empty(n, np.uint16)
+    mapq = np.empty(n, np.uint8)
+    ncig = np.empty(n, np.uint16)
+    name = np.empty(n, np.int64)
+    packed = np.empty(n * stride // 2, np.uint8)
+    qual = np.empty(n * stride, np.uint8)
+    max_ops = int(L.rvs_max_ops())
+    cigars = [None] * len(ids)
+
+    def one(i):
+        lo, hi = spans[ids[i]]
+        a = int(np.searchsorted(vpos, lo - 400))
+        b = int(np.searchsorted(vpos, hi + 400))
+        sub = np.ascontiguousarray(vt[a:b])
+        k0, k1 = int(off[i]), int(off[i + 1])
+        cg = np.empty(max(1, (k1 - k0) * max_ops), np.uint32)
+        a_lo, a_hi, a_n = amp[i]
+        ptr = lambda x: x.ctypes.data if x is not None else None  # noqa: E731
+        nw = L.rvs_simulate_region(
+            g.ctypes.data, G, sub.ctypes.data, len(sub), alt.ctypes.data, pars[i].ctypes.data, ptr(a_lo), ptr(a_hi),
+            ptr(a_n), len(a_n) if a_n is not None else 0, k1 - k0,
+            pos[k0:].ctypes.data, mpos[k0:].ctypes.data, isize[k0:].ctypes.data, nm[k0:].ctypes.data,
+            flag[k0:].ctypes.data, mapq[k0:].ctypes.data, ncig[k0:].ctypes.data, name[k0:].ctypes.data,
+            packed[k0 * stride // 2:].ctypes.data, qual[k0 * stride:].ctypes.data, cg.ctypes.data)
+        if nw < 0:
+            raise RuntimeError(f"native generator failed on span {i}")
+        cigars[i] = cg[:nw].copy()
+
+    with cf.ThreadPoolExecutor(max_workers=threads or os.cpu_count() or 1) as ex:
+        list(ex.map(one, range(len(ids))))
+    cigar = np.concatenate(cigars) if cigars else np.zeros(0, np.uint32)
+    cig_off = np.zeros(n, dtype=np.uint32)
+    if n:
+        cig_off[1:] = np.cumsum(ncig[:-1].astype(np.uint64)).astype(np.uint32)
+    del C
+    return ReadSet(contig=contig, contig_len=int(G), pos=pos, flag=flag, mapq=mapq, mpos=mpos, isize=isize, nm=nm,
+                   n_cigar=ncig, cig_off=cig_off, cigar=cigar, l_qseq=np.full(n, read_len, dtype=np.int32),
+                   base_off=np.arange(n, dtype=np.uint64) * np.uint64(stride), seq4=None, qual=qual, name_id=name,
+                   packed=packed)
+
+
+def deep_somatic_panel(seed: int = 0x5EED0003, n_regions: int = 400, region_len: int = 5000, gap: int = 1000,
+                       tumor_depth: float = 5000.0, normal_depth: float = 1000.0, threads: int | None = None,
+                       only: list[int] | None = None):
+    """Deep targeted somatic panel: `n_regions` regions of `region_len` bp
+    (2 Mb for 400 x 5 kb) on one contig, `gap` bp apart; tumor 5000x and
+    normal 1000x 2x150 pairs (native generator).  Germline SNVs 1e-3/bp
+    (VAF 0.5 or 1.0) and indels 1e-4/bp in both samples; low-VAF somatic SNVs
+    (1e-4/bp, 10 % MNVs) and indels (2e-5/bp) with VAF ~log-uniform(0.001,
+    0.05) in the tumor; oxidation-like C>A artifacts at 1e-4 per C base with
+    quality 20 in both samples.  Returns (genome, (germline, somatic),
+    tumor, normal, regions) with regions 1-based inclusive.  With `only` (a
+    list of region indexes) only those regions' reads are generated; each
+    region's reads are the same as in the whole panel (one seeded stream per
+    region)."""
+    rng = np.random.default_rng(seed)
+    glen = n_regions * (region_len + gap) + gap
+    g = make_genome(glen, rng)
+    regions = [(gap + i * (region_len + gap) + 1, gap + i * (region_len + gap) + region_len)
+               for i in range(n_regions)]
+    germ = plant_variants(g, rng, 1e-3, 1e-4, lambda r: 0.5 if r.random() < 0.7 else 1.0)
+    lo_v, hi_v = np.log(0.001), np.log(0.05)
+    som = plant_variants(g, rng, 1e-4, 2e-5, lambda r: float(np.exp(r.uniform(lo_v, hi_v))), mnv_frac=0.1,
+                         avoid=germ)
+    spans = [(a - 1, b) for a, b in regions]
+    idx = list(range(n_regions)) if only is None else sorted(only)
+    tumor = simulate_regions(g, germ + som, spans, tumor_depth, seed=seed * 2 + 1, artifact_rate=1e-4,
+                             artifact_q=20, threads=threads, span_ids=idx)
+    normal = simulate_regions(g, germ, spans, normal_depth, seed=seed * 2 + 2, artifact_rate=1e-4, artifact_q=20,
+                              name_base=1 << 40, threads=threads, span_ids=idx)
+    return g, (germ, som), tumor, normal, regions

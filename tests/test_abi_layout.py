@@ -123,3 +123,28 @@ def test_graph_entry_points_reject_a_null_context():
     assert L.rv_set_pileup_graph(None, 1) == -1          # RV_ERR_ARG
     assert L.rv_pileup_graph_stats(None, C.byref(n), None) == -1
     assert n.value == -1
+
+
+def test_capacity_entry_points_check_their_arguments():
+    """rv_set_capacities / rv_capacity_stats without a GPU: a null context and
+    out-of-range capacities are argument errors; valid ones are accepted on a
+    context whose device set-up failed (no device memory is touched)."""
+    import ctypes as C
+    from rabbitvar_gb300 import api
+    L = api.lib()
+    assert L.rv_set_capacities(None, 1, 1, 1, 1) == -1
+    assert L.rv_capacity_stats(None, None, None, None) == -1
+    h = C.c_void_p()
+    p = api.default_params()
+    st = L.rv_create(C.byref(h), C.byref(p), 0, 0)
+    assert st in (0, -2) and h
+    try:
+        assert L.rv_set_capacities(h, 0, 0, 1 << 40, 0) == -1      # deferred above INT32_MAX
+        assert L.rv_set_capacities(h, 0, 0, 0, 1 << 40) == -1      # order-fix entries above INT32_MAX
+        assert L.rv_set_capacities(h, (1 << 32) + 1, 0, 0, 0) == -1  # more slots than 32-bit indexes reach
+        assert L.rv_set_capacities(h, 64, 256, 4, 4) == 0
+        r, hs, ab = C.c_int64(-1), C.c_int64(-1), C.c_int64(-1)
+        assert L.rv_capacity_stats(h, C.byref(r), C.byref(hs), C.byref(ab)) == 0
+        assert r.value == 0
+    finally:
+        L.rv_destroy(h)

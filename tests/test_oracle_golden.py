@@ -129,3 +129,26 @@ def test_oracle_somatic_matches_reference_binary_bench_shape(tmp_path):
     mine = O.run_somatic(t, n, g, 1, 100_000, "O", "T", O.default_params(local_realign=1, fisher=1)).splitlines()
     assert len(recs) > 100
     assert sorted(mine) == sorted(recs)
+
+
+def test_oracle_somatic_matches_reference_binary_deep_panel(tmp_path):
+    """One region of the deep targeted panel (5 kb, tumor 5000x + normal
+    1000x, low-VAF somatic variants, C>A artifacts at Q20), -k 1 --fisher:
+    the oracle's records equal the reference binary's byte for byte, so the
+    oracle is pinned on the panel the GPU parity test and the bench use."""
+    import oracle as O
+    if not O.have_reference():
+        pytest.skip("reference binaries not built (reference tree absent)")
+    from rabbitvar_gb300 import synth
+    g, _, t, n, regions = synth.deep_somatic_panel(only=[137])
+    t, n = synth.unpacked(t), synth.unpacked(n)
+    a, b = regions[137]
+    tb, nb, fa = str(tmp_path / "T.bam"), str(tmp_path / "N.bam"), str(tmp_path / "ref.fa")
+    synth.write_bam(tb, t)
+    synth.write_bam(nb, n)
+    synth.write_fasta(fa, t.contig, g)
+    recs = O.reference_records(fa, f"{tb}|{nb}", f"{t.contig}:{a}-{b}", str(tmp_path / "o.txt"),
+                               ["-k", "1", "--fisher"], sample="T|N")
+    mine = O.run_somatic(t, n, g, a, b, "O", "T", O.default_params(local_realign=1, fisher=1)).splitlines()
+    assert len(recs) >= 3
+    assert sorted(mine) == sorted(recs)
