@@ -61,7 +61,7 @@ typedef struct {
     int32_t dedup;         /* -t */
     int32_t unique_fwd;    /* -u */
     int32_t unique_first;  /* --UN */
-    int32_t do_pileup;     /* -p (this build supports 0) */
+    int32_t do_pileup;     /* -p: every covered position printed (simple mode; no effect in somatic mode) */
     int32_t fisher;        /* --fisher */
     int32_t move_indels_3; /* -3 */
     int32_t svminlen;      /* 1000 */

@@ -54,7 +54,8 @@ unsigned long long next_pow2(unsigned long long x) {
     return p;
 }
 
-enum { CNT_TILE = 0, CNT_DEFER = 1, CNT_USED = 2, CNT_ERR = 3, CNT_CAND = 4, CNT_AUX = 5, CNT_FIX = 6 };
+enum { CNT_TILE = 0, CNT_DEFER = 1, CNT_USED = 2, CNT_ERR = 3, CNT_CAND = 4, CNT_AUX = 5, CNT_FIX = 6,
+       CNT_WIDE_INS = 7, CNT_WIDE_SCORE = 10 };
 
 // (Re)allocates the hash table and its used-slot list with `cap` slots.
 rv_status alloc_hash(rv_ctx *ctx, unsigned long long cap) {
@@ -146,6 +147,11 @@ DevState rv_ctx::state() const {
     s.ofix = d_ofix;
     s.n_ofix = d_counters + CNT_FIX;
     s.ofix_cap = ofix_cap;
+    s.wide_ins = d_wide;
+    s.wide_score = d_wide ? d_wide + wide_cap : nullptr;
+    s.n_wide_ins = d_counters + CNT_WIDE_INS;
+    s.n_wide_score = d_counters + CNT_WIDE_SCORE;
+    s.wide_cap = wide_cap;
     return s;
 }
 
@@ -192,6 +198,8 @@ rv_status device_fisher(rv_ctx *ctx, const int32_t *tables, int64_t n, double *p
 
 namespace {
 
+rv_status run_wide(rv_ctx *ctx, int list, unsigned int n, cudaStream_t s);
+
 // Scores the listed (region, position) pairs of `ctx` without screens and
 // appends their CandVars to the host copy.
 rv_status score_list(rv_ctx *ctx, const std::vector<int2> &list) {
@@ -205,15 +213,53 @@ rv_status score_list(rv_ctx *ctx, const std::vector<int2> &list) {
     }
     cudaStream_t s = ctx->stream;
     RV_CUDA(cudaMemcpyAsync(ctx->d_list, list.data(), list.size() * sizeof(int2), cudaMemcpyHostToDevice, s));
+    RV_CUDA(cudaMemsetAsync(ctx->d_counters + CNT_WIDE_SCORE, 0, 4, s));
     DevState st = ctx->state();
     launch_score_list(st, ctx->dp, ctx->d_list, (int)list.size(), s);
     RV_CUDA(cudaGetLastError());
-    unsigned int hdr[8];
+    unsigned int hdr[12];
     RV_CUDA(cudaMemcpyAsync(hdr, ctx->d_counters, sizeof hdr, cudaMemcpyDeviceToHost, s));
     RV_CUDA(cudaStreamSynchronize(s));
+    if (hdr[CNT_WIDE_SCORE] && !(hdr[CNT_ERR] & ERR_CAND_FULL)) {
+        rv_status ws = run_wide(ctx, 1, hdr[CNT_WIDE_SCORE], s);
+        if (ws) return ws;
+        RV_CUDA(cudaMemcpyAsync(hdr, ctx->d_counters, sizeof hdr, cudaMemcpyDeviceToHost, s));
+        RV_CUDA(cudaStreamSynchronize(s));
+    }
     unsigned int n0 = (unsigned int)ctx->h_cand.size(), n = hdr[CNT_CAND];
-    if (n > ctx->cand_cap || (hdr[CNT_ERR] & ERR_HASH_FULL)) {
+    if (hdr[CNT_ERR] & ERR_CAND_FULL) {
+        // grow the buffer to the count reached and score the list again (the
+        // candidates before n0 are already on the host)
+        const unsigned long long need = n;
+        cudaFree(ctx->d_cand);
+        ctx->d_cand = nullptr;
+        ctx->cand_cap = 0;
+        const unsigned int cap = (unsigned int)std::min<unsigned long long>(INT32_MAX, need + need / 4 + 65536);
+        RV_CUDA(cudaMalloc((void **)&ctx->d_cand, (size_t)cap * sizeof(CandVar)));
+        ctx->cand_cap = cap;
+        RV_CUDA(cudaMemcpyAsync(ctx->d_counters + CNT_CAND, &n0, 4, cudaMemcpyHostToDevice, s));
+        RV_CUDA(cudaMemsetAsync(ctx->d_counters + CNT_WIDE_SCORE, 0, 4, s));
+        st = ctx->state();
+        launch_clear_err_bits(st, ~ERR_CAND_FULL, s);
+        launch_score_list(st, ctx->dp, ctx->d_list, (int)list.size(), s);
+        RV_CUDA(cudaGetLastError());
+        RV_CUDA(cudaMemcpyAsync(hdr, ctx->d_counters, sizeof hdr, cudaMemcpyDeviceToHost, s));
+        RV_CUDA(cudaStreamSynchronize(s));
+        if (hdr[CNT_WIDE_SCORE]) {
+            rv_status ws = run_wide(ctx, 1, hdr[CNT_WIDE_SCORE], s);
+            if (ws) return ws;
+            RV_CUDA(cudaMemcpyAsync(hdr, ctx->d_counters, sizeof hdr, cudaMemcpyDeviceToHost, s));
+            RV_CUDA(cudaStreamSynchronize(s));
+        }
+        n = hdr[CNT_CAND];
+        ctx->kernels += 2;
+    }
+    if (n > ctx->cand_cap || (hdr[CNT_ERR] & ERR_CAND_FULL)) {
         ctx->err = "candidate buffer overflow";
+        return RV_ERR_CAPACITY;
+    }
+    if (hdr[CNT_ERR] & ERR_WIDE_FULL) {
+        ctx->err = "more positions with many alleles than the wide list holds";
         return RV_ERR_CAPACITY;
     }
     if (hdr[CNT_ERR] & (ERR_UNSUPPORTED | ERR_CELL_RANGE)) {
@@ -229,6 +275,49 @@ rv_status score_list(rv_ctx *ctx, const std::vector<int2> &list) {
     ctx->io_h2d += (int64_t)(list.size() * sizeof(int2));
     ctx->io_d2h += (int64_t)sizeof hdr + (int64_t)(n - n0) * (int64_t)sizeof(CandVar);
     ctx->kernels += 1;
+    return RV_OK;
+}
+
+// The wide pass of one list (k_ins_adjust_wide for list 0, k_score_wide for
+// list 1): the queued positions' scratch offsets from their allele counts,
+// scratch grown to the total, then the kernel on stream s (not waited for).
+rv_status run_wide(rv_ctx *ctx, int list, unsigned int n, cudaStream_t s) {
+    if (n == 0) return RV_OK;
+    if (n > ctx->wide_cap) {
+        ctx->err = "more positions with many alleles than the wide list holds";
+        return RV_ERR_CAPACITY;
+    }
+    std::vector<WidePos> w(n);
+    RV_CUDA(cudaMemcpyAsync(w.data(), ctx->d_wide + (size_t)list * ctx->wide_cap, n * sizeof(WidePos),
+                            cudaMemcpyDeviceToHost, s));
+    RV_CUDA(cudaStreamSynchronize(s));
+    std::vector<int64_t> off(n + 1, 0);
+    for (unsigned int i = 0; i < n; i++) off[i + 1] = off[i] + std::max(1, w[i].need) + 8;
+    const int64_t total = off[n];
+    if (ctx->cap_wide_off < n + 1 || !ctx->d_wide_off) {
+        if (ctx->d_wide_off) cudaFree(ctx->d_wide_off);
+        ctx->d_wide_off = nullptr;
+        ctx->cap_wide_off = 0;
+        RV_CUDA(cudaMalloc((void **)&ctx->d_wide_off, (n + 1) * sizeof(int64_t) * 2));
+        ctx->cap_wide_off = (n + 1) * 2;
+    }
+    const size_t bytes = (size_t)total * wide_entry_bytes();
+    if (ctx->cap_wide_scratch < bytes || !ctx->d_wide_scratch) {
+        if (ctx->d_wide_scratch) cudaFree(ctx->d_wide_scratch);
+        ctx->d_wide_scratch = nullptr;
+        ctx->cap_wide_scratch = 0;
+        RV_CUDA(cudaMalloc(&ctx->d_wide_scratch, bytes + bytes / 2));
+        ctx->cap_wide_scratch = bytes + bytes / 2;
+    }
+    // (a pageable copy: staged before the call returns, so `off` may go)
+    RV_CUDA(cudaMemcpy(ctx->d_wide_off, off.data(), (n + 1) * sizeof(int64_t), cudaMemcpyHostToDevice));
+    DevState st = ctx->state();
+    if (list == 0) launch_ins_adjust_wide(st, ctx->d_wide_off, ctx->d_wide_scratch, total, s);
+    else launch_score_wide(st, ctx->dp, ctx->d_wide_off, ctx->d_wide_scratch, total, s);
+    RV_CUDA(cudaGetLastError());
+    ctx->kernels += 1;
+    ctx->io_d2h += (int64_t)(n * sizeof(WidePos));
+    ctx->io_h2d += (int64_t)((n + 1) * sizeof(int64_t));
     return RV_OK;
 }
 
@@ -336,11 +425,11 @@ rv_status rv_create(rv_ctx **out, const rv_params *p, int device, size_t hbm_bud
     d.move_indels_3 = p->move_indels_3;
     d.svminlen = p->svminlen;
     d.somatic = p->somatic;
+    // -p changes nothing in somatic mode: ToVarsBuilder keeps every position
+    // of a pair anyway (src/ToVarsBuilder.cpp:170-175, 228) and the somatic
+    // writer does not read it (src/modes/somaticMode.cpp)
+    if (p->somatic) d.do_pileup = 0;
     *out = ctx;
-    if (p->do_pileup) {
-        ctx->err = "pileup mode (-p) is not supported by this build";
-        return RV_ERR_UNSUPPORTED;
-    }
     return RV_OK;
 }
 
@@ -354,7 +443,8 @@ void rv_destroy(rv_ctx *ctx) {
                     ctx->d_tmp_slots, ctx->d_tmp_cells, ctx->d_tmp_views, ctx->d_tmp_n, ctx->d_list,
                     ctx->d_ftab, ctx->d_logfact, ctx->d_skip, ctx->d_patches, ctx->d_patch_keys,
                     ctx->d_list_off, ctx->d_list_bsum, ctx->d_list_idx, ctx->d_list_slots,
-                    ctx->d_cons_meta, ctx->d_cons, ctx->d_ofix, ctx->d_used};
+                    ctx->d_cons_meta, ctx->d_cons, ctx->d_ofix, ctx->d_used, ctx->d_wide, ctx->d_wide_off,
+                    ctx->d_wide_scratch};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (ctx->h_mirror) cudaFreeHost(ctx->h_mirror);
@@ -696,7 +786,17 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
         ctx->force_hash = ctx->force_arena = 0;
         ctx->force_deferred = ctx->force_fix = 0;
     }
-    unsigned int want_cand = (unsigned int)std::min<int64_t>(INT32_MAX, std::max<int64_t>(1 << 16, score / 4 + 1024));
+    unsigned int want_wide = (unsigned int)std::min<int64_t>(INT32_MAX / 2, score / 8 + 4096);
+    if (want_wide > ctx->wide_cap || !ctx->d_wide) {
+        if (ctx->d_wide) cudaFree(ctx->d_wide);
+        ctx->d_wide = nullptr;
+        ctx->wide_cap = 0;
+        RV_CUDA(cudaMalloc((void **)&ctx->d_wide, 2 * (size_t)want_wide * sizeof(WidePos)));
+        ctx->wide_cap = want_wide;
+    }
+    // candidates: a few per candidate position; pileup mode scores every position
+    const int64_t cand_est = ctx->dp.do_pileup ? 2 * score + 65536 : score / 4 + 1024;
+    unsigned int want_cand = (unsigned int)std::min<int64_t>(INT32_MAX, std::max<int64_t>(1 << 16, cand_est));
     if (want_cand > ctx->cand_cap || !ctx->d_cand) {
         if (ctx->d_cand) cudaFree(ctx->d_cand);
         ctx->d_cand = nullptr;
@@ -955,14 +1055,59 @@ static rv_status score_impl(rv_ctx *ctx, void *stream, const DevParams &dp) {
     DevState st = ctx->state();
     RV_CUDA(cudaEventRecord(ctx->ev[2], s));
     RV_CUDA(cudaMemsetAsync(ctx->d_counters + CNT_CAND, 0, 4, s));
+    RV_CUDA(cudaMemsetAsync(ctx->d_counters + CNT_WIDE_INS, 0, 4, s));
+    RV_CUDA(cudaMemsetAsync(ctx->d_counters + CNT_WIDE_SCORE, 0, 4, s));
     launch_ins_adjust(st, s);
+    {
+        // positions with more insertion keys than the kernel's arrays: their
+        // adjustments must land before any position is scored
+        unsigned int nw = 0;
+        RV_CUDA(cudaMemcpyAsync(&nw, ctx->d_counters + CNT_WIDE_INS, 4, cudaMemcpyDeviceToHost, s));
+        RV_CUDA(cudaStreamSynchronize(s));
+        rv_status ws = run_wide(ctx, 0, nw, s);
+        if (ws) return ws;
+    }
     RV_CUDA(cudaEventRecord(ctx->ev[8], s));
     launch_score(st, dp, s);
     RV_CUDA(cudaGetLastError());
-    RV_CUDA(cudaEventRecord(ctx->ev[3], s));
-    unsigned int hdr[8];
+    unsigned int hdr[12];
     RV_CUDA(cudaMemcpyAsync(hdr, ctx->d_counters, sizeof hdr, cudaMemcpyDeviceToHost, s));
     RV_CUDA(cudaStreamSynchronize(s));
+    if (hdr[CNT_WIDE_SCORE] && !(hdr[CNT_ERR] & ERR_CAND_FULL)) {
+        rv_status ws = run_wide(ctx, 1, hdr[CNT_WIDE_SCORE], s);
+        if (ws) return ws;
+        RV_CUDA(cudaMemcpyAsync(hdr, ctx->d_counters, sizeof hdr, cudaMemcpyDeviceToHost, s));
+        RV_CUDA(cudaStreamSynchronize(s));
+    }
+    RV_CUDA(cudaEventRecord(ctx->ev[3], s));
+    if (hdr[CNT_ERR] & ERR_CAND_FULL) {
+        // more scored alleles than the buffer holds: grow it to the count
+        // the run reached and score again (the kernel only reads the maps)
+        const unsigned long long need = hdr[CNT_CAND];
+        if (ctx->d_cand) cudaFree(ctx->d_cand);
+        ctx->d_cand = nullptr;
+        ctx->cand_cap = 0;
+        const unsigned int cap = (unsigned int)std::min<unsigned long long>(INT32_MAX, need + need / 4 + 65536);
+        RV_CUDA(cudaMalloc((void **)&ctx->d_cand, (size_t)cap * sizeof(CandVar)));
+        ctx->cand_cap = cap;
+        st = ctx->state();
+        RV_CUDA(cudaMemsetAsync(ctx->d_counters + CNT_CAND, 0, 4, s));
+        RV_CUDA(cudaMemsetAsync(ctx->d_counters + CNT_WIDE_SCORE, 0, 4, s));
+        launch_clear_err_bits(st, ~ERR_CAND_FULL, s);
+        launch_score(st, dp, s);
+        RV_CUDA(cudaGetLastError());
+        RV_CUDA(cudaMemcpyAsync(hdr, ctx->d_counters, sizeof hdr, cudaMemcpyDeviceToHost, s));
+        RV_CUDA(cudaStreamSynchronize(s));
+        if (hdr[CNT_WIDE_SCORE]) {
+            rv_status ws = run_wide(ctx, 1, hdr[CNT_WIDE_SCORE], s);
+            if (ws) return ws;
+            RV_CUDA(cudaMemcpyAsync(hdr, ctx->d_counters, sizeof hdr, cudaMemcpyDeviceToHost, s));
+            RV_CUDA(cudaStreamSynchronize(s));
+        }
+        RV_CUDA(cudaEventRecord(ctx->ev[3], s));
+        RV_CUDA(cudaStreamSynchronize(s));
+        ctx->kernels += 2;
+    }
     float ms = 0;
     cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]);
     ctx->score_ms = ms;
@@ -972,8 +1117,12 @@ static rv_status score_impl(rv_ctx *ctx, void *stream, const DevParams &dp) {
     ctx->stage_ms[6] = ms;
     ctx->kernels += 2;
     unsigned int n = hdr[CNT_CAND];
-    if (n > ctx->cand_cap) {
+    if (n > ctx->cand_cap || (hdr[CNT_ERR] & ERR_CAND_FULL)) {
         ctx->err = "candidate buffer overflow";
+        return RV_ERR_CAPACITY;
+    }
+    if (hdr[CNT_ERR] & ERR_WIDE_FULL) {
+        ctx->err = "more positions with many alleles than the wide list holds";
         return RV_ERR_CAPACITY;
     }
     if (hdr[CNT_ERR] & (ERR_UNSUPPORTED | ERR_CELL_RANGE)) {

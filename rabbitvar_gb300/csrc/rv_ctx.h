@@ -29,6 +29,11 @@ void launch_link(const DevState &st, cudaStream_t s);
 void launch_collisions(const DevState &st, cudaStream_t s);
 void launch_ins_adjust(const DevState &st, cudaStream_t s);
 void launch_score(const DevState &st, const DevParams &P, cudaStream_t s);
+void launch_clear_err_bits(const DevState &st, unsigned int keep, cudaStream_t s);
+size_t wide_entry_bytes();
+void launch_ins_adjust_wide(const DevState &st, const int64_t *off, void *scratch, int64_t total, cudaStream_t s);
+void launch_score_wide(const DevState &st, const DevParams &P, const int64_t *off, void *scratch, int64_t total,
+                       cudaStream_t s);
 void launch_fisher(const int32_t *tab, int64_t n, double *p2, double *ratio, cudaStream_t s,
                    const double *lf = nullptr);
 void launch_fill_logfact(double *lf, cudaStream_t s);
@@ -172,9 +177,19 @@ struct rv_ctx {
     // map entries whose pstd/qstd are replayed in read order
     rv::OrderFix *d_ofix = nullptr;
     unsigned int ofix_cap = 0;
+    // positions with more alleles than the scoring kernels' per-thread arrays:
+    // two lists (insertion adjustment, scoring) of wide_cap entries, their
+    // scratch offsets and the scratch itself (grown on demand)
+    rv::WidePos *d_wide = nullptr;
+    unsigned int wide_cap = 0;
+    int64_t *d_wide_off = nullptr;
+    size_t cap_wide_off = 0;
+    void *d_wide_scratch = nullptr;
+    size_t cap_wide_scratch = 0;
     int32_t max_lq = 0;   // longest read of the batch
 
-    // small counters: tile_counter, n_deferred, n_used, err, n_cand, pad, n_ofix, pad, arena_used(64)
+    // small counters: tile_counter, n_deferred, n_used, err, n_cand, pad, n_ofix, n_wide_ins,
+    // arena_used (64-bit, words 8-9), n_wide_score
     unsigned int *d_counters = nullptr;
 
     // scratch for the realigner boundary (grown on demand, owned by the context)

@@ -554,9 +554,10 @@ static void format_groups(const rv_ctx *ctx, const std::vector<const CandVar *> 
         else if (!vs.empty()) g1s = vs[0].desc;
         else g1s = refdesc;
         if (starts(g1s, '+')) g1s = "+" + std::to_string(g1s.size() - 1);
+        const bool pileup = ctx->dp.do_pileup != 0 && ctx->dp.dataset_min == 0;
         try {
             for (RecVar &v : vs) {
-                describe(v, g1s, position, R, P, v.c->pass != 0);
+                describe(v, g1s, position, R, P, v.c->pass != 0 || pileup);
                 v.sbf = std::string(ref ? std::to_string(ref->bias) : std::string("0")) + ";" + std::to_string(v.c->bias);
             }
         } catch (const NoRef &) {
@@ -571,16 +572,36 @@ static void format_groups(const rv_ctx *ctx, const std::vector<const CandVar *> 
             for (RecVar &v : vs) maxfreq = std::max(maxfreq, v.c->freq);
             if (maxfreq <= P.freq) continue;
         }
+        // pileup mode, a position without variants: its reference allele
+        // (collectReferenceVariants, src/ToVarsBuilder.cpp:1063-1091: no
+        // variant reads, genotype ref/ref, no flanks, empty type)
+        RecVar refrec;
+        if (pileup && vs.empty() && ref) {
+            refrec.c = ref;
+            refrec.filled = true;
+            refrec.startp = refrec.endp = position;
+            refrec.refallele = refrec.varallele = refdesc;
+            refrec.genotype = refdesc + "/" + refdesc;
+            refrec.shift3 = 0;
+            refrec.msi = 0;
+            refrec.msint = 0;
+            refrec.sbf = std::to_string(ref->bias) + ";0";
+            refrec.vartype_fixed = true;
+            vs.push_back(refrec);
+        }
         for (RecVar &v : vs) {
-            if (!v.filled || !v.c->pass) continue;
-            if (v.refallele.find('N') != std::string::npos) continue;
-            v.vartype = var_type(v);
-            if (!good_var(v, ref, P, v.vartype)) continue;
-            if (v.vartype == "Complex") adj_complex(v);
+            if (!v.filled || (!v.c->pass && !pileup)) continue;
+            const bool ref_only = v.vartype_fixed;
+            if (!ref_only) {
+                if (v.refallele.find('N') != std::string::npos) continue;
+                v.vartype = var_type(v);
+                if (!good_var(v, ref, P, v.vartype) && !pileup) continue;
+                if (v.vartype == "Complex") adj_complex(v);
+            }
             const CandVar &c = *v.c;
             // adjustVariantCounts (src/ToVarsBuilder.cpp:543-566): negative counts print as 0
             const int rfc = std::max(0, c.rfc), rrc = std::max(0, c.rrc);
-            const int afwd = std::max(0, c.fwd), arev = std::max(0, c.rev);
+            const int afwd = ref_only ? 0 : std::max(0, c.fwd), arev = ref_only ? 0 : std::max(0, c.rev);
             auto add = [&](const std::string &x, bool last = false) {
                 text += x;
                 text += last ? '\n' : '\t';
@@ -595,13 +616,13 @@ static void format_groups(const rv_ctx *ctx, const std::vector<const CandVar *> 
             add(v.refallele);
             add(v.varallele);
             addi(c.tpc);
-            addi(c.pc);
+            addi(ref_only ? 0 : c.pc);
             addi(rfc);
             addi(rrc);
             addi(afwd);
             addi(arev);
             add(v.genotype.empty() ? "0" : v.genotype);
-            addf(c.freq);
+            addf(ref_only ? 0.0 : c.freq);
             add(v.sbf);
             addf(c.pmean);
             add(c.pstd ? "1" : "0");
@@ -634,12 +655,12 @@ static void format_groups(const rv_ctx *ctx, const std::vector<const CandVar *> 
             r.start = v.startp;
             r.end = v.endp;
             r.total_cov = c.tpc;
-            r.var_cov = c.pc;
+            r.var_cov = ref_only ? 0 : c.pc;
             r.ref_fwd = rfc;
             r.ref_rev = rrc;
             r.alt_fwd = afwd;
             r.alt_rev = arev;
-            r.freq = c.freq;
+            r.freq = ref_only ? 0.0 : c.freq;
             r.pmean = c.pmean;
             r.qual = c.qual;
             r.mapq = c.mq;

@@ -168,6 +168,15 @@ struct OrderFix {
     int64_t index;           // cell word (4 * cell + base) or slot index
 };
 
+// A position whose alleles do not fit the per-thread arrays of the scoring
+// kernels (kMaxVars): scored again by the wide kernels with `need` entries
+// of global scratch.
+struct WidePos {
+    int32_t region, pos;
+    int32_t need;            // alleles (and insertion keys) at the position
+    int32_t forced;          // scored without screens (somatic list)
+};
+
 // Error word bits (per context)
 enum : uint32_t {
     ERR_HASH_FULL = 1u,
@@ -179,6 +188,8 @@ enum : uint32_t {
     ERR_PROBE_LIMIT = 64u,
     ERR_COLLISION = 128u,
     ERR_FIX_FULL = 256u,     // more order-dependent entries than the OrderFix list holds
+    ERR_CAND_FULL = 512u,    // more scored alleles than the candidate buffer holds
+    ERR_WIDE_FULL = 1024u,   // more wide positions than the WidePos lists hold
 };
 
 // One scored allele at a candidate position, handed to the host for the
@@ -220,6 +231,10 @@ struct DevState {
     OrderFix *ofix;          // entries k_fix_order replays
     unsigned int *n_ofix;
     unsigned int ofix_cap;
+    WidePos *wide_ins;       // positions k_ins_adjust left to the wide pass
+    WidePos *wide_score;     // positions the score kernels left to the wide pass
+    unsigned int *n_wide_ins, *n_wide_score;
+    unsigned int wide_cap;
 };
 
 constexpr int kLogFact = 1 << 16;

@@ -36,6 +36,7 @@ struct RecVar {
     double msi = 0;
     std::string leftseq, rightseq, genotype, refallele, varallele, vartype;
     bool filled = false;
+    bool vartype_fixed = false;   // pileup mode's reference-allele record (type "")
 };
 
 Msi find_msi(const std::string &t1, const std::string &t2, const std::string &left);

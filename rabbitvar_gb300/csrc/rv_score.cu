@@ -158,12 +158,27 @@ __device__ __forceinline__ int promoted_base(const DevState &st, const Slot &s) 
 }
 
 struct PosKeys {
-    uint32_t ins[kMaxVars];
-    int n_ins;
+    uint32_t *ins;       // insertion slots (storage of the caller, ins_cap entries)
+    int ins_cap;
+    int n_ins;           // insertion keys at the position (may exceed ins_cap: then only counted)
     int n_nonins;        // keys present in the position's nonInsertionVariants map
     bool in_map;         // the position has an entry in nonInsertionVariants
     int single_mask;     // present A/C/G/T keys
+    __device__ bool overflow() const { return n_ins > ins_cap; }
 };
+
+// Queues a position for the wide pass (its alleles exceed the caller's arrays).
+__device__ void push_wide(WidePos *list, unsigned int *n, unsigned int cap, unsigned int *err, int region, int pos,
+                          int need, bool forced) {
+    const unsigned int k = atomicAdd(n, 1u);
+    if (k >= cap) { atomicOr(err, ERR_WIDE_FULL); return; }
+    WidePos w;
+    w.region = region;
+    w.pos = pos;
+    w.need = need;
+    w.forced = forced ? 1 : 0;
+    list[k] = w;
+}
 
 __device__ void gather_keys(const DevState &st, const Region &R, int p, PosKeys &k) {
     int64_t c = cell_index(R, p);
@@ -183,8 +198,8 @@ __device__ void gather_keys(const DevState &st, const Region &R, int p, PosKeys 
                 if (b >= 0) k.single_mask |= 1 << b;
             }
         } else if (sl.kind == KIND_INS && !(sl.flags & SF_ERASED)) {
-            if (k.n_ins < kMaxVars) k.ins[k.n_ins++] = s;
-            else atomicOr(st.err, ERR_UNSUPPORTED);
+            if (k.n_ins < k.ins_cap) k.ins[k.n_ins] = s;
+            k.n_ins++;
         }
     }
 }
@@ -272,7 +287,8 @@ __device__ bool visited(const DevState &st, const Region &R, int p, PosKeys &k) 
 
 // Apply the insertion adjustments of every visited position (in ascending
 // position order semantics: a position's adjustment of p+1 is visible when
-// p+1 is scored).
+// p+1 is scored).  Positions with more than kMaxVars insertion keys are left
+// to k_ins_adjust_wide.
 __global__ void k_ins_adjust(DevState st) {
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < st.cells.n_cells;
          t += (int64_t)gridDim.x * blockDim.x) {
@@ -285,10 +301,34 @@ __global__ void k_ins_adjust(DevState st) {
         }
         const Region &R = st.regions[lo];
         int p = R.clo + (int)(t - R.cell_base);
+        uint32_t ins[kMaxVars];
         PosKeys k;
+        k.ins = ins;
+        k.ins_cap = kMaxVars;
         if (!visited(st, R, p, k) || k.n_ins == 0) continue;
+        if (k.overflow()) {
+            push_wide(st.wide_ins, st.n_wide_ins, st.wide_cap, st.err, lo, p, k.n_ins, false);
+            continue;
+        }
         sort_ins(st, k);
         insertion_pass(st, R, p, (int)st.cells.cov[t], k, true);
+    }
+}
+
+// The same for the queued wide positions, one thread each, with their
+// insertion keys in global scratch (off[i]: first scratch entry of entry i).
+__global__ void k_ins_adjust_wide(DevState st, const int64_t *off, uint32_t *ins_scratch) {
+    unsigned int n = *st.n_wide_ins;
+    if (n > st.wide_cap) n = st.wide_cap;
+    for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const WidePos w = st.wide_ins[i];
+        const Region &R = st.regions[w.region];
+        PosKeys k;
+        k.ins = ins_scratch + off[i];
+        k.ins_cap = (int)(off[i + 1] - off[i]);
+        if (!visited(st, R, w.pos, k) || k.n_ins == 0 || k.overflow()) continue;
+        sort_ins(st, k);
+        insertion_pass(st, R, w.pos, (int)st.cells.cov[cell_index(R, w.pos)], k, true);
     }
 }
 
@@ -337,7 +377,11 @@ __device__ double fisher_two_sided(int n11, int n12, int n21, int n22, const dou
 // Scores position p of region `lo`: ToVarsBuilder::process for one position
 // (src/ToVarsBuilder.cpp:97-205).  Positions that pass the screens (or every
 // position with variants when `forced`) write all their alleles as CandVars.
-__device__ void score_position(const DevState &st, const DevParams &P, int lo, int p, bool forced) {
+// `vs` / `insbuf` hold up to vcap alleles / insertion keys (per-thread
+// arrays, or global scratch in the wide pass); a position with more is
+// queued for the wide pass (when `wide` is false) and not scored here.
+__device__ void score_position(const DevState &st, const DevParams &P, int lo, int p, bool forced, V *vs, int vcap,
+                               uint32_t *insbuf, bool wide) {
     const Region &R = st.regions[lo];
     if (p < R.clo || p > R.chi) return;
     int64_t c = cell_index(R, p);
@@ -377,7 +421,22 @@ __device__ void score_position(const DevState &st, const DevParams &P, int lo, i
         if (!pass || !(gate || P.somatic)) return;
     }
     PosKeys k;
+    k.ins = insbuf;
+    k.ins_cap = vcap;
     if (!visited(st, R, p, k)) return;
+    {
+        // alleles at the position: present A/C/G/T cells, live string keys
+        int need = k.n_ins + __popc(k.single_mask & 15);
+        for (uint32_t s = st.head[cell_index(R, p)]; s != kNone; s = st.hash.slots[s].next) {
+            const Slot &sl = st.hash.slots[s];
+            if (sl.kind == KIND_NONINS && !(sl.flags & SF_ERASED)) need++;
+        }
+        if (need > vcap || k.overflow()) {
+            if (!wide) push_wide(st.wide_score, st.n_wide_score, st.wide_cap, st.err, lo, p, need, forced);
+            else atomicOr(st.err, ERR_WIDE_FULL);
+            return;
+        }
+    }
     // isTheSameVariationOnRef (src/ToVarsBuilder.cpp:213-233)
     if (!forced && !P.do_pileup && !P.somatic && k.n_nonins == 1 && k.n_ins == 0 && hasp && rbi >= 0 &&
         k.single_mask == (1 << rbi))
@@ -385,7 +444,6 @@ __device__ void score_position(const DevState &st, const DevParams &P, int lo, i
     int tpc = (int)st.cells.cov[c];
     // calcHicov
     int hicov = 0;
-    V vs[kMaxVars];
     int nv = 0;
     const uint8_t kfc = st.cells.kflags[c];
     const int cell_mask = kfc & 15 & ~(kfc >> 4);
@@ -420,7 +478,7 @@ __device__ void score_position(const DevState &st, const DevParams &P, int lo, i
         v.pstd = (f & FCS_PDIFF) != 0;
         v.qstd = (f & FCS_QDIFF) != 0;
         finish_var(v, tpc, hicov, P);
-        if (nv < kMaxVars) vs[nv++] = v;
+        if (nv < vcap) vs[nv++] = v;
     }
     for (uint32_t s = st.head[c]; s != kNone; s = st.hash.slots[s].next) {
         const Slot &sl = st.hash.slots[s];
@@ -433,7 +491,7 @@ __device__ void score_position(const DevState &st, const DevParams &P, int lo, i
         int ttcov = tpc;
         if (v.cnt > tpc && v.extracnt > 0 && v.cnt - tpc < v.extracnt) ttcov = v.cnt;
         finish_var(v, ttcov, hicov, P);
-        if (nv < kMaxVars) vs[nv++] = v; else atomicOr(st.err, ERR_UNSUPPORTED);
+        if (nv < vcap) vs[nv++] = v; else atomicOr(st.err, ERR_UNSUPPORTED);
     }
     // createInsertion
     if (k.n_ins > 0) {
@@ -456,7 +514,7 @@ __device__ void score_position(const DevState &st, const DevParams &P, int lo, i
             }
             if (hic < v.hi) hic = v.hi;
             finish_var(v, ttcov, hic, P);
-            if (nv < kMaxVars) vs[nv++] = v; else atomicOr(st.err, ERR_UNSUPPORTED);
+            if (nv < vcap) vs[nv++] = v; else atomicOr(st.err, ERR_UNSUPPORTED);
         }
     }
     // sort by CMP_VARI (insertion sort; few alleles per position)
@@ -479,7 +537,9 @@ __device__ void score_position(const DevState &st, const DevParams &P, int lo, i
     if (nv == 0) return;
     if (!forced) {
         if (!P.do_pileup && !P.somatic && !P.dataset_min && maxfreq <= P.freq) return;
-        if (n_var == 0) return;
+        // pileup mode (-p) prints the reference allele of a position without
+        // variants (src/modes/simpleMode.cpp:163-174)
+        if (n_var == 0 && !(P.do_pileup && ref_i >= 0)) return;
     }
     // numeric pre-screen of isGoodVar: a necessary condition for emission
     bool any = false;
@@ -509,7 +569,7 @@ __device__ void score_position(const DevState &st, const DevParams &P, int lo, i
         }
     }
     unsigned int base = atomicAdd(st.n_cand, (unsigned int)nv);
-    if (base + nv > st.cand_cap) { atomicOr(st.err, ERR_HASH_FULL); return; }
+    if (base + nv > st.cand_cap) { atomicOr(st.err, ERR_CAND_FULL); return; }
     int rank = 0;
     for (int i = 0; i < nv; i++) {
         const V &v = vs[i];
@@ -546,10 +606,17 @@ __device__ void score_position(const DevState &st, const DevParams &P, int lo, i
         o.hifreq = v.hifreq;
         o.extrafreq = v.extrafreq;
         o.nm = v.nmv;
-        if (P.fisher && !P.somatic && !P.dataset_min && o.kind == 1 && o.pass) {
+        // the records' Fisher test (src/modes/simpleMode.cpp:96-108): every
+        // printed allele; pileup mode also prints alleles failing isGoodVar
+        // and, at a position without variants, the reference allele with no
+        // variant reads
+        if (P.fisher && !P.somatic && !P.dataset_min && o.kind == 1 && (o.pass || P.do_pileup)) {
             o.fisher_p = fisher_two_sided(rf, rr, fwd, rev, st.logfact);
             double ad = (double)(rf * rev), bc = (double)(rr * fwd);
             o.fisher_ratio = (bc != 0 && ad != 0) ? (ad > bc ? ad / bc : bc / ad) : 0.0;
+        } else if (P.fisher && !P.somatic && !P.dataset_min && o.kind == 0 && P.do_pileup && n_var == 0) {
+            o.fisher_p = fisher_two_sided(rf, rr, 0, 0, st.logfact);
+            o.fisher_ratio = 0.0;
         } else {
             o.fisher_p = 0;
             o.fisher_ratio = 0;
@@ -578,7 +645,10 @@ __global__ void k_score(DevState st, DevParams P) {
         for (int64_t t = c0 + threadIdx.x; t < c0 + kScoreChunk && t < st.n_score; t += blockDim.x) {
             int lo = lo0;
             while (lo + 1 < st.n_regions && st.score_base[lo + 1] <= t) lo++;
-            score_position(st, P, lo, st.regions[lo].start + (int)(t - st.score_base[lo]), false);
+            V vs[kMaxVars];
+            uint32_t ins[kMaxVars];
+            score_position(st, P, lo, st.regions[lo].start + (int)(t - st.score_base[lo]), false, vs, kMaxVars, ins,
+                           false);
         }
     }
 }
@@ -591,8 +661,36 @@ __global__ void k_score_list(DevState st, DevParams P, const int2 *list, int n) 
         if (e.x < 0 || e.x >= st.n_regions) continue;
         const Region &R = st.regions[e.x];
         if (e.y < R.start || e.y > R.end) continue;
-        score_position(st, P, e.x, e.y, true);
+        V vs[kMaxVars];
+        uint32_t ins[kMaxVars];
+        score_position(st, P, e.x, e.y, true, vs, kMaxVars, ins, false);
     }
+}
+
+// The queued wide positions, one thread each, with their alleles and
+// insertion keys in global scratch (off[i]: first scratch entry of entry i).
+__global__ void k_score_wide(DevState st, DevParams P, const int64_t *off, V *v_scratch, uint32_t *ins_scratch) {
+    unsigned int n = *st.n_wide_score;
+    if (n > st.wide_cap) n = st.wide_cap;
+    for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const WidePos w = st.wide_score[i];
+        const int cap = (int)(off[i + 1] - off[i]);
+        score_position(st, P, w.region, w.pos, w.forced != 0, v_scratch + off[i], cap, ins_scratch + off[i], true);
+    }
+}
+
+size_t wide_entry_bytes() { return sizeof(V) + sizeof(uint32_t); }
+
+void launch_ins_adjust_wide(const DevState &st, const int64_t *off, void *scratch, int64_t total, cudaStream_t s) {
+    (void)total;
+    k_ins_adjust_wide<<<64, 64, 0, s>>>(st, off, (uint32_t *)scratch);
+}
+
+void launch_score_wide(const DevState &st, const DevParams &P, const int64_t *off, void *scratch, int64_t total,
+                       cudaStream_t s) {
+    V *vs = (V *)scratch;
+    uint32_t *ins = (uint32_t *)(vs + total);
+    k_score_wide<<<64, 64, 0, s>>>(st, P, off, vs, ins);
 }
 
 // Features of the learned filter: 40 floats per candidate allele, from its
@@ -685,6 +783,12 @@ __global__ void k_fisher(const int32_t *tab, int64_t n, double *p2, double *rati
         double ad = (double)a * d, bc = (double)b * c;
         ratio[i] = (bc != 0 && ad != 0) ? (ad > bc ? ad / bc : bc / ad) : 0.0;
     }
+}
+
+__global__ void k_clear_err_bits(unsigned int *err, unsigned int keep) { atomicAnd(err, keep); }
+
+void launch_clear_err_bits(const DevState &st, unsigned int keep, cudaStream_t s) {
+    k_clear_err_bits<<<1, 1, 0, s>>>(st.err, keep);
 }
 
 void launch_link(const DevState &st, cudaStream_t s) { k_link_slots<<<592, 256, 0, s>>>(st); }

@@ -255,7 +255,19 @@ def case_dense_multi_k1():
     return g, rs, (1, 30_000), ["-k", "1", "--fisher"]
 
 
-RECORDS_ONLY = {"contig_end_k1": case_contig_end_k1, "dense_multi_k1": case_dense_multi_k1}
+def case_pileup_k0():
+    # pileup mode (-p): every covered position printed, failing variants kept
+    g, rs, _, _ = case_germline_dense()
+    return g, rs, (1_001, 2_500), ["-k", "0", "-p"]
+
+
+def case_pileup_k1():
+    g, _, rs = synth.dense_multi()
+    return g, rs, (2_001, 4_000), ["-k", "1", "-p", "--fisher"]
+
+
+RECORDS_ONLY = {"contig_end_k1": case_contig_end_k1, "dense_multi_k1": case_dense_multi_k1,
+                "pileup_k0": case_pileup_k0, "pileup_k1": case_pileup_k1}
 
 
 # somatic mode (`-b 'T.bam|N.bam' -N 'T|N'`): records only

@@ -35,6 +35,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 GOLD = os.path.join(HERE, "golden")
 META = json.load(open(os.path.join(GOLD, "golden.json")))
 SINGLE = sorted(k for k, v in META.items() if not v.get("somatic") and not v.get("records_only"))
+RECORDS_ONLY = sorted(k for k, v in META.items() if v.get("records_only"))
 SOMATIC = sorted(k for k, v in META.items() if v.get("somatic"))
 P_TAGS = ["P_ML", "PN", "PI", "PC", "PS5", "PS3", "PCI", "PCD", "PMN"]
 R_TAGS = ["RN", "RI", "RC"]
@@ -67,6 +68,24 @@ def test_single_sample_golden_cases_match_reference(name):
     gold = gzip.open(os.path.join(GOLD, f"{name}.dump.txt.gz"), "rt").read()
     assert diff_dump(gold, p_dump, P_TAGS, rel=1e-9) == []
     assert diff_dump(gold, r_dump, R_TAGS, rel=1e-9) == []
+    recs = open(os.path.join(GOLD, f"{name}.records.txt")).read().splitlines()
+    assert len(recs) == META[name]["records"] > 5
+    assert diff_records(recs, mine) == []
+
+
+@pytest.mark.parametrize("name", RECORDS_ONLY)
+def test_records_only_golden_cases_match_reference(name):
+    """Records against the reference's: -k 1 at a contig end and on a dense
+    multi-variant set, and pileup mode (-p: every covered position printed,
+    alleles failing isGoodVar kept) with -k 0 and with -k 1 --fisher."""
+    from rabbitvar_gb300 import api, synth
+    mg = _make_golden()
+    g, rs, (a, b), flags = mg.RECORDS_ONLY[name]()
+    assert mg.readset_fingerprint(rs) == META[name]["fingerprint"]
+    ctx = api.Context(api.default_params(**flag_params(flags)))
+    ctx.upload_reference(rs.contig, synth.genome_str(g).encode())
+    mine = ctx.call(api.Batch.from_readset(rs), [widened(a, b, flags)], "S", rs.contig).splitlines()
+    ctx.close()
     recs = open(os.path.join(GOLD, f"{name}.records.txt")).read().splitlines()
     assert len(recs) == META[name]["records"] > 5
     assert diff_records(recs, mine) == []
