@@ -904,25 +904,40 @@ rv_status launch_pileup_graph(rv_ctx *ctx, cudaStream_t s, int grid, int variant
 rv_status pileup_launch(rv_ctx *ctx, cudaStream_t s) {
     if (ctx->stage < 1) { ctx->err = "rv_pileup before rv_submit_batch"; return RV_ERR_STATE; }
     RV_CUDA(cudaSetDevice(ctx->device));
-    // autotuner: unless RV_PILEUP_VARIANT pins one, the first batches try each
-    // kernel variant once and later batches use the fastest seen
+    // autotuner: unless RV_PILEUP_VARIANT pins one, the first batch of the
+    // context runs the whole pileup chain once with every tile-kernel variant
+    // (register budget x warp aggregation), timing the tile kernel of each;
+    // that batch and the later ones use the fastest
     int nvar = pileup_variants();
     int variant;
     const char *pin = getenv("RV_PILEUP_VARIANT");
     const bool pinned = pin && *pin;
-    if (pinned) variant = std::max(0, std::min(nvar - 1, atoi(pin)));
-    else if (ctx->variant_runs < nvar) variant = ctx->variant_runs;
-    else {
+    auto grid_of = [&](int v) {
+        const int per_sm = std::max(1, pileup_blocks_per_sm(v));
+        return std::max(1, std::min<int>((int)ctx->tiles.size(), per_sm * ctx->sm_count));
+    };
+    if (pinned) {
+        variant = std::max(0, std::min(nvar - 1, atoi(pin)));
+    } else {
+        if (ctx->variant_runs < nvar && !ctx->tiles.empty()) {
+            for (int v = 0; v < nvar; v++) {
+                rv_status ts = queue_pileup_chain(ctx, s, grid_of(v), v, true);
+                if (ts != RV_OK) return ts;
+                RV_CUDA(cudaStreamSynchronize(s));
+                float m = 0;
+                cudaEventElapsedTime(&m, ctx->ev[5], ctx->ev[6]);
+                ctx->variant_ms[v] = m;
+            }
+            ctx->variant_runs = nvar;
+        }
         variant = 0;
         for (int v = 1; v < nvar; v++)
             if (ctx->variant_ms[v] < ctx->variant_ms[variant]) variant = v;
     }
     ctx->variant = variant;
-    int per_sm = std::max(1, pileup_blocks_per_sm(variant));
-    int grid = std::max(1, std::min<int>((int)ctx->tiles.size(), per_sm * ctx->sm_count));
-    // a graph once the variant is settled (the autotuner's trial runs need
-    // the per-stage events); the legacy default stream cannot be captured
-    const bool graphed = ctx->use_graph && s != nullptr && (pinned || ctx->variant_runs >= nvar);
+    const int grid = grid_of(variant);
+    // the legacy default stream cannot be captured
+    const bool graphed = ctx->use_graph && s != nullptr;
     RV_CUDA(cudaEventRecord(ctx->ev[0], s));
     rv_status qs = graphed ? launch_pileup_graph(ctx, s, grid, variant)
                            : queue_pileup_chain(ctx, s, grid, variant, true);
@@ -988,7 +1003,6 @@ rv_status pileup_finish(rv_ctx *ctx, cudaStream_t s) {
         retried = true;
     }
     const unsigned int err = cnt[CNT_ERR];
-    const int nvar = pileup_variants(), variant = ctx->variant;
     float ms = 0;
     cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
     ctx->pileup_ms = ms;
@@ -1005,11 +1019,7 @@ rv_status pileup_finish(rv_ctx *ctx, cudaStream_t s) {
         cudaEventElapsedTime(&ms, ctx->ev[7], ctx->ev[1]);
         ctx->stage_ms[4] = ms;
     }
-    // (a run after a table grew starts from a whole-table reset: not a fair trial)
-    if (!ctx->pileup_pin && ctx->variant_runs < nvar && !retried) {
-        ctx->variant_ms[variant] = ctx->stage_ms[2];
-        ctx->variant_runs++;
-    }
+    (void)retried;
     if (err) {
         char buf[160];
         snprintf(buf, sizeof buf, "pileup device error bits 0x%x", err);

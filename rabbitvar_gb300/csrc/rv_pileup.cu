@@ -244,6 +244,12 @@ __device__ __forceinline__ uint32_t shared_ld_u8(uint32_t addr) {
     return v;
 }
 
+// AGG: lanes of a warp that emit into the same (position, base) cell at
+// the same time (reads starting at the same position, as in deep pileups)
+// are found with __match_any_sync; their three packed words are summed with
+// warp reductions and one lane does the shared atomics and the first-value
+// check for the group.
+template <bool AGG>
 struct TileFast {
     uint32_t w_s;       // shared-space address of the word arrays (w0 | w1 | w2 | first, 4*kTileW words each)
     uint32_t ref_s;     // shared-space address of the reference bases wlo .. wlo + kTileW - 1
@@ -255,7 +261,54 @@ struct TileFast {
         return d < (unsigned)kTileW ? (char)shared_ld_u8(ref_s + d) : __ldg(refp + p - 1);
     }
     __device__ __forceinline__ bool emit(int p, int b, int dir, int tp, int q, int mapq, int nm) const {
+        if (AGG) return emit_warp(p, b, dir, tp, q, mapq, nm);
         return emit_any(p, b, dir, tp, q, mapq, nm, true);
+    }
+    // The observation of each active lane, aggregated over the lanes that hit
+    // the same cell; lanes whose observation does not fit the packing return
+    // false (the caller's global path).
+    __device__ __forceinline__ bool emit_warp(int p, int b, int dir, int tp, int q, int mapq, int nm) const {
+        const unsigned d = (unsigned)(p - wlo);
+        const bool ok = d < (unsigned)kTileW && (unsigned)(tp - 1) <= 510u && (unsigned)(q - 1) <= 126u &&
+                        (unsigned)mapq <= 255u && (unsigned)(nm + 128) <= 255u;
+        const unsigned act = __activemask();
+        const unsigned okm = __ballot_sync(act, ok);
+        if (!ok) return false;
+        const uint32_t ix = 4u * d + (uint32_t)b;
+        const unsigned peers = __match_any_sync(okm, ix);
+        const uint32_t v0 = (dir ? (1u << 10) : 1u) + (q >= goodq ? (1u << 20) : 0u);
+        const uint32_t v1 = (uint32_t)tp | ((uint32_t)q << 17);
+        const uint32_t v2 = (uint32_t)mapq | ((uint32_t)(nm + 128) << 16);
+        const uint32_t s0 = __reduce_add_sync(peers, v0);
+        const uint32_t s1 = __reduce_add_sync(peers, v1);
+        const uint32_t s2 = __reduce_add_sync(peers, v2);
+        int same_tp = 0, same_q = 0;
+        __match_all_sync(peers, tp, &same_tp);
+        __match_all_sync(peers, q, &same_q);
+        const int lane = (int)(threadIdx.x & 31u);
+        if (lane != __ffs(peers) - 1) return true;
+        const uint32_t a0 = w_s + 4u * ix;
+        constexpr uint32_t kArr = 4u * 4u * kTileW;  // bytes per word array
+        shared_add_u32(a0, s0);
+        shared_add_u32(a0 + kArr, s1);
+        shared_add_u32(a0 + 2u * kArr, s2);
+        const uint32_t v = (uint32_t)tp | ((uint32_t)q << 12);
+        const uint32_t fa = a0 + 3u * kArr;
+        uint32_t need = (same_tp ? 0u : FC_PDIFF) | (same_q ? 0u : FC_QDIFF);
+        uint32_t f = shared_ld_u32(fa);
+        bool claimed = false;
+        for (int it = 0; it < 64 && (f & FC_VAL) == 0u; it++) {
+            uint32_t old = shared_cas_u32(fa, f, f | v);
+            if (old == f) { claimed = true; f |= v; break; }
+            f = old;
+        }
+        if (!claimed) {
+            const uint32_t fv = f & FC_VAL;
+            if ((fv & 0xFFFu) != (v & 0xFFFu)) need |= FC_PDIFF;
+            if ((fv >> 12) != (v >> 12)) need |= FC_QDIFF;
+        }
+        if (need & ~f) shared_or_u32(fa, need);
+        return true;
     }
     // std_rel: the observation takes part in pstd/qstd (M-op bases do, the
     // soft-clip re-alignment counts do not)
@@ -291,9 +344,10 @@ struct TileFast {
 
 // Tile sink: A/C/G/T observations inside [wlo, wlo + kTileW) accumulate in
 // shared memory; subtractions are deferred.
+template <bool AGG>
 struct TileSink : SinkBase {
-    TileFast f;
-    using Fast = TileFast;
+    TileFast<AGG> f;
+    using Fast = TileFast<AGG>;
     __device__ Fast fast() const { return f; }
     __device__ bool phantom(int) const { return false; }
     // Positions below 1 never get queried by the walk; above the window only
@@ -520,7 +574,7 @@ __global__ void k_region_reset(DevState st) {
     if (reg < st.n_regions) st.regions[reg].edge_hit = 0;
 }
 
-template <int TW, int MINB>
+template <int TW, int MINB, bool AGG>
 __global__ void __launch_bounds__(kPileupThreads, MINB) k_pileup_tiles(DevState st, DevParams P) {
     extern __shared__ __align__(16) unsigned char smem[];
     uint32_t *w0 = (uint32_t *)smem;
@@ -545,7 +599,7 @@ __global__ void __launch_bounds__(kPileupThreads, MINB) k_pileup_tiles(DevState 
             s_ref[i] = (p >= 1 && p <= st.ref_len) ? st.ref[p - 1] : (char)0;
         }
         __syncthreads();
-        TileSink sink;
+        TileSink<AGG> sink;
         sink.st = &st;
         sink.P = &P;
         sink.R = &R;
@@ -555,7 +609,7 @@ __global__ void __launch_bounds__(kPileupThreads, MINB) k_pileup_tiles(DevState 
         sink.f.ref_s = (uint32_t)__cvta_generic_to_shared(s_ref);
         sink.f.goodq = P.goodq;
         {
-            Walker<TileSink> w(P, sink, R, st.ref, st.ref_len);
+            Walker<TileSink<AGG>> w(P, sink, R, st.ref, st.ref_len);
             for (int64_t r = tile.r0 + threadIdx.x; r < tile.r1; r += blockDim.x) {
                 if (!read_passes(st.batch, P, R, r)) continue;
                 if (R.serial && R.edge_hit) {
@@ -792,17 +846,22 @@ void launch_region_reset(const DevState &st, cudaStream_t s) {
 size_t pileup_smem_bytes() { return (size_t)kTileW * 4 * 4 * 4; }
 
 // Instantiations differing in the minimum resident blocks per SM (and so in
-// the register budget per thread); the autotuner times them on the first
-// batch and keeps the fastest (RV_PILEUP_VARIANT pins one: 0, 1 or 2).
+// the register budget per thread) and in warp aggregation of the shared
+// histogram updates; the autotuner times them and keeps the fastest
+// (RV_PILEUP_VARIANT pins one, 0..5: 0-2 direct updates with 2/3/4 blocks
+// per SM, 3-5 the same with warp aggregation).
 using PileupKernel = void (*)(DevState, DevParams);
 static PileupKernel pileup_variant(int v) {
     switch (v) {
-    case 0: return k_pileup_tiles<kTileW, 2>;
-    case 1: return k_pileup_tiles<kTileW, 3>;
-    default: return k_pileup_tiles<kTileW, 4>;
+    case 0: return k_pileup_tiles<kTileW, 2, false>;
+    case 1: return k_pileup_tiles<kTileW, 3, false>;
+    case 2: return k_pileup_tiles<kTileW, 4, false>;
+    case 3: return k_pileup_tiles<kTileW, 2, true>;
+    case 4: return k_pileup_tiles<kTileW, 3, true>;
+    default: return k_pileup_tiles<kTileW, 4, true>;
     }
 }
-int pileup_variants() { return 3; }
+int pileup_variants() { return 6; }
 
 cudaError_t launch_pileup(const DevState &st, const DevParams &P, int grid, cudaStream_t s, int variant) {
     size_t smem = pileup_smem_bytes();
