@@ -444,7 +444,7 @@ void rv_destroy(rv_ctx *ctx) {
                     ctx->d_ftab, ctx->d_logfact, ctx->d_skip, ctx->d_patches, ctx->d_patch_keys,
                     ctx->d_list_off, ctx->d_list_bsum, ctx->d_list_idx, ctx->d_list_slots,
                     ctx->d_cons_meta, ctx->d_cons, ctx->d_ofix, ctx->d_used, ctx->d_wide, ctx->d_wide_off,
-                    ctx->d_wide_scratch};
+                    ctx->d_wide_scratch, ctx->d_f35};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (ctx->h_mirror) cudaFreeHost(ctx->h_mirror);

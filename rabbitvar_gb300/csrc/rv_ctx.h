@@ -77,6 +77,7 @@ struct Patch {
     int64_t key_off;                    // type 5: key bytes in the patch key buffer
 };
 void launch_apply_patches(const DevState &st, const Patch *p, int64_t n, const uint8_t *keys, cudaStream_t s);
+void launch_find35(const int32_t *pairs, int64_t n, const char *strs, int32_t *res, cudaStream_t s);
 // flattened per-cell key lists (-k 1 realigner mirror): 5 launches, then 1
 void launch_list_offsets(const DevState &st, uint32_t *off, uint32_t *bsum, cudaStream_t s);
 void launch_list_fill(const DevState &st, const uint32_t *off, Slot *out, uint32_t *out_idx, cudaStream_t s);
@@ -216,6 +217,8 @@ struct rv_ctx {
     void *h_mirror_slots = nullptr;  // pinned: listed keys, slot indices
     size_t cap_mirror_slots = 0;
     bool mirror_pending = false;     // mirror_launch queued, not yet consumed
+    void *d_f35 = nullptr;           // realigner: clip pairs, their strings and find35 results
+    size_t cap_f35 = 0;
     rv::Patch *d_patches = nullptr;
     size_t cap_patches = 0;
     uint8_t *d_patch_keys = nullptr;

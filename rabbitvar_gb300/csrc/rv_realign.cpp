@@ -23,14 +23,15 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <mutex>
-#include <regex>
 #include <set>
 #include <string>
 #include <thread>
 #include <unordered_map>
 #include <vector>
 
+#include "rv_keymatch.h"
 #include "rv_mirror.h"
 #include "rv_pool.h"
 
@@ -340,6 +341,27 @@ struct RegionRealigner {
             if (prof) prof[6] += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
         }
         return k.c.cons;
+    }
+    // The consensus string of a clip without the side effect consensus() has
+    // at its first use (the low-complexity mark); the string itself does not
+    // depend on when it is computed.
+    string peek_consensus(Clip &k) {
+        if (k.loaded) return k.c.cons;
+        if (k.agg >= 0 && (mir.cmeta[k.agg] >> 31)) {
+            const uint32_t m = mir.cmeta[k.agg];
+            return string((const char *)mir.cons + mir.off[k.cell] + ((m >> 16) & 0x3FFFu), m & 0xFFFFu);
+        }
+        std::vector<NtCount> nt;
+        if (k.cell >= 0)
+            for (uint32_t i = mir.off[k.cell]; i < mir.off[k.cell + 1]; i++) {
+                const Slot &s = mir.slots[i];
+                if (s.kind != k.seq_kind || s.klen != 3 || (size_t)s.koff + 3 > ctx->h_arena.size()) continue;
+                const uint8_t *kb = ctx->h_arena.data() + s.koff;
+                nt.push_back({kb[0] | (kb[1] << 8), (char)kb[2], s.obs, s.q_sum});
+            }
+        sort_nt(nt);
+        bool unused = false;
+        return consensus_of(nt, k.c.agg.cnt, unused);
     }
     void add_cov(int p, int n) { cov_add[p] += n; }
 
@@ -656,18 +678,13 @@ struct RegionRealigner {
                 }
                 int tc = tail_caret_num(vn);
                 if (tc >= 0) dellen += tc;
-                string extrains, extra, inv5, inv3;
-                std::smatch m;
-                static const std::regex re_inv("^-\\d+\\^([ATGNC]+)<...\\d+>([ATGNC]+)$");
-                static const std::regex re_rest("^-\\d+(.*)");
-                static const std::regex re_ins("\\^([ATGNC]+)");
-                if (std::regex_search(vn, m, re_inv)) {
-                    inv5 = m.str(1);
-                    inv3 = m.str(2);
-                } else if (std::regex_search(vn, m, re_rest)) {
-                    for (char c : m.str(1))
+                string extrains, extra, inv5, inv3, rest;
+                // ^-\d+\^([ATGNC]+)<...\d+>([ATGNC]+)$, else ^-\d+(.*) and \^([ATGNC]+)
+                if (keymatch::inv(vn, inv5, inv3)) {
+                } else if (keymatch::del_rest(vn, rest)) {
+                    for (char c : rest)
                         if (c != '^' && c != '&' && c != '#') extra += c;
-                    if (std::regex_search(vn, m, re_ins)) extrains = m.str(1);
+                    keymatch::caret_bases(vn, extrains);
                 }
                 const int wustart = p - 200 > 1 ? p - 200 : 1;
                 string wupseq = join_ref(R, wustart, p - 1) + extra;
@@ -749,15 +766,13 @@ struct RegionRealigner {
             } catch (const OutOfRange &) {
             }
         }
-        static const std::regex re_tail("(-\\d+)&[ATGC]+$");
         for (int i = (int)tmp.size() - 1; i > 0; i--) {
             const int p = tmp[i].pos;
             const string &vn = tmp[i].key;
             if (!has_key(p, vn)) continue;
             HVar &vref = N(p).keys.at(vn);
-            std::smatch m;
-            if (std::regex_search(vn, m, re_tail)) {
-                string tn = m.str(1);
+            string tn;
+            if (keymatch::del_amp_tail(vn, tn)) {  // (-\d+)&[ATGC]+$
                 auto &keys = N(p).keys;
                 auto t = keys.find(tn);
                 if (t != keys.end() && vref.cnt < t->second.cnt) {
@@ -771,39 +786,32 @@ struct RegionRealigner {
     // realignins (:785-1114)
     void realignins(const std::map<int, std::map<string, int>> &icnt_map) {
         std::vector<Cand> tmp = sorted(icnt_map);
-        static const std::regex re_ins1("^\\+([ATGC]+).*");
-        static const std::regex re_dup("<dup(\\d+)>([ATGC]+)$");
-        static const std::regex re_extra(".*&([ATGC]+).*");
-        static const std::regex re_compm("#([ATGC]+).*");
-        static const std::regex re_newdel("\\^(\\d+)$");
-        static const std::regex re_caretnum("\\^\\d+$");
-        static const std::regex re_caret("\\^");
         for (const Cand &tpl : tmp) {
             try {
                 const int position = tpl.pos;
                 const string &vn = tpl.key;
                 const int icnt = tpl.cnt;
-                std::smatch m;
                 string insert1;
-                if (std::regex_search(vn, m, re_ins1)) insert1 = m.str(1);
-                else continue;
-                string ins3;
+                if (!keymatch::ins_lead(vn, insert1)) continue;  // ^\+([ATGC]+).*
+                string ins3, dupn;
                 int inslen = (int)insert1.size();
-                if (std::regex_search(vn, m, re_dup)) {
-                    ins3 = m.str(2);
-                    inslen += atoi(m.str(1).c_str()) + (int)ins3.size();
-                }
+                if (keymatch::dup_tail(vn, dupn, ins3))  // <dup(\d+)>([ATGC]+)$
+                    inslen += atoi(dupn.c_str()) + (int)ins3.size();
                 string extra, compm;
-                if (std::regex_search(vn, m, re_extra)) extra = m.str(1);
-                if (std::regex_search(vn, m, re_compm)) compm = m.str(1);
+                keymatch::last_amp_bases(vn, extra);  // .*&([ATGC]+).*
+                keymatch::hash_bases(vn, compm);      // #([ATGC]+).*
                 int newdel = 0;
-                if (std::regex_search(vn, m, re_newdel)) newdel = atoi(m.str(1).c_str());
+                const size_t nd = keymatch::caret_num_tail(vn);  // \^(\d+)$
+                if (nd != string::npos) newdel = atoi(vn.c_str() + nd + 1);
                 string tn = vn;
                 if (!tn.empty() && tn[0] == '+') tn.erase(0, 1);
                 replace_first(tn, "&", "");
                 replace_first(tn, "#", "");
-                tn = std::regex_replace(tn, re_caretnum, "", std::regex_constants::format_first_only);
-                tn = std::regex_replace(tn, re_caret, "", std::regex_constants::format_first_only);
+                // the first \^\d+$, then the first \^, removed
+                const size_t cn = keymatch::caret_num_tail(tn);
+                if (cn != string::npos) tn.erase(cn);
+                const size_t c1 = tn.find('^');
+                if (c1 != string::npos) tn.erase(c1, 1);
                 const int wustart = position - 150 > 1 ? position - 150 : 1;
                 string wupseq = join_ref(R, wustart, position) + tn;
                 int sanend = position + (int)vn.size() + 100;
@@ -910,16 +918,14 @@ struct RegionRealigner {
             } catch (const OutOfRange &) {
             }
         }
-        static const std::regex re_tail("(\\+[ATGC]+)&[ATGC]+$");
         for (int i = (int)tmp.size() - 1; i > 0; i--) {
             const int p = tmp[i].pos;
             const string &vn = tmp[i].key;
             PosMap &im = I(p);
             if (!im.present || !im.keys.count(vn)) continue;
             HVar &vref = im.keys.at(vn);
-            std::smatch m;
-            if (std::regex_search(vn, m, re_tail)) {
-                string tn = m.str(1);
+            string tn;
+            if (keymatch::ins_amp_tail(vn, tn)) {  // (\+[ATGC]+)&[ATGC]+$
                 auto t = im.keys.find(tn);
                 if (t != im.keys.end() && vref.cnt < t->second.cnt) {
                     char b = R.idx(p);
@@ -930,27 +936,86 @@ struct RegionRealigner {
         }
     }
 
-    // find35match (:1396-1428).  Inside the loop bounds the reference's
-    // substr calls never throw: s3's index is always a character, s5's is one
-    // past the end (an empty string, a mismatch) when i + n == |s5|.
-    static void find35(const string &s5, const string &s3, int &b5, int &b3, int &score) {
-        b5 = b3 = score = 0;
-        const int l5 = (int)s5.size(), l3 = (int)s3.size();
-        for (int i = 0; i < l5 - 8; i++) {
-            for (int j = 1; j < l3 - 8; j++) {
-                int nm = 0, n = 0;
-                while (n + j <= l3 && i + n <= l5) {
-                    if (i + n == l5 || s3[l3 - j - n] != s5[i + n]) nm++;
-                    if (nm > 2) break;
-                    n++;
+    // find35match (:1396-1428) of the clip pair (ia in t5, ib in t3): from the
+    // batch's device results when collect_lgins_pairs listed the pair, else
+    // on the host
+    std::unordered_map<uint64_t, int64_t> f35_index;  // (ia, ib) -> pair index
+    const int32_t *f35_res = nullptr;                // per pair: b5, b3, score
+    void find35(int ia, int ib, const string &s5, const string &s3, int &b5, int &b3, int &score) {
+        if (f35_res) {
+            auto it = f35_index.find(((uint64_t)(uint32_t)ia << 32) | (uint32_t)ib);
+            if (it != f35_index.end()) {
+                const int32_t *r = f35_res + 3 * it->second;
+                b5 = r[0];
+                b3 = r[1];
+                score = r[2];
+                return;
+            }
+        }
+        keymatch::find35(s5, s3, b5, b3, score);
+    }
+
+    // The 5'/3' clip lists realignlgins30 walks (by count), and the 3' clips
+    // by position with their rank in t3.
+    struct LgT { int pos; Clip *c; int cnt; };
+    void lgins_lists(std::vector<LgT> &t5, std::vector<LgT> &t3, std::vector<std::pair<int, int>> &by_pos) {
+        for (auto &e : sc5)
+            if (!(e.first < Rg.start - 5000 || e.first > Rg.end + 5000)) t5.push_back({e.first, &e.second, e.second.c.agg.cnt});
+        for (auto &e : sc3)
+            if (!(e.first < Rg.start - 5000 || e.first > Rg.end + 5000)) t3.push_back({e.first, &e.second, e.second.c.agg.cnt});
+        auto by_cnt = [](const LgT &a, const LgT &b) { return a.cnt != b.cnt ? a.cnt > b.cnt : a.pos < b.pos; };
+        std::sort(t5.begin(), t5.end(), by_cnt);
+        std::sort(t3.begin(), t3.end(), by_cnt);
+        by_pos.resize(t3.size());
+        for (size_t i = 0; i < t3.size(); i++) by_pos[i] = {t3[i].pos, (int)i};
+        std::sort(by_pos.begin(), by_pos.end());
+    }
+
+    // Every clip pair realignlgins30 may hand to find35match: the pairs that
+    // pass its position window, consensus lengths and count ratio (the clips'
+    // `used` marks, which only skip pairs, are left out).  Appends each pair
+    // as four int32 (offset and length of the 5' and of the 3' consensus in
+    // `strs`) and records its index for find35.
+    void collect_lgins_pairs(std::vector<int32_t> &pairs, string &strs) {
+        std::vector<LgT> t5, t3;
+        std::vector<std::pair<int, int>> by_pos;
+        lgins_lists(t5, t3, by_pos);
+        std::vector<std::pair<int32_t, int32_t>> s3at(t3.size(), {-1, 0});
+        auto str3 = [&](int ib) {
+            if (s3at[ib].first < 0) {
+                const string q = peek_consensus(*t3[ib].c);
+                s3at[ib] = {(int32_t)strs.size(), (int32_t)q.size()};
+                strs += q;
+            }
+            return s3at[ib];
+        };
+        std::vector<int> near;
+        int64_t k = 0;
+        for (size_t ia = 0; ia < t5.size(); ia++) {
+            const LgT &a = t5[ia];
+            const string seq5 = peek_consensus(*a.c);
+            if (seq5.size() <= 10) continue;
+            const int p5 = a.pos;
+            const int lo3 = (int)std::ceil(p5 - max_rl * 2.5) - 1, hi3 = p5 + max_rl - 10 + 1;
+            near.clear();
+            for (auto it = std::lower_bound(by_pos.begin(), by_pos.end(), std::make_pair(lo3, INT32_MIN));
+                 it != by_pos.end() && it->first <= hi3; ++it)
+                near.push_back(it->second);
+            std::sort(near.begin(), near.end());
+            int32_t off5 = -1;
+            for (int ib : near) {
+                const LgT &b = t3[ib];
+                if (p5 - b.pos > max_rl * 2.5) continue;
+                if (b.pos - p5 > max_rl - 10) continue;
+                if (!(a.cnt / (double)b.cnt >= 0.08 && a.cnt / (double)b.cnt <= 12)) continue;
+                const auto s3v = str3(ib);
+                if (s3v.second <= 10) continue;
+                if (off5 < 0) {
+                    off5 = (int32_t)strs.size();
+                    strs += seq5;
                 }
-                if (n - nm > score && n - nm > 8 && nm / (double)n < 0.1 &&
-                    (n + j >= (int)s3.size() || i + n >= (int)s5.size())) {
-                    b5 = i;
-                    b3 = j;
-                    score = n - nm;
-                    return;
-                }
+                pairs.insert(pairs.end(), {off5, (int32_t)seq5.size(), s3v.first, s3v.second});
+                f35_index[((uint64_t)(uint32_t)ia << 32) | (uint32_t)ib] = k++;
             }
         }
     }
@@ -959,24 +1024,16 @@ struct RegionRealigner {
     // insert stay local), the nested realignins/realigndel use the shared one
     void realignlgins30() {
         PRef RL = R;
-        struct T { int pos; Clip *c; int cnt; };
-        std::vector<T> t5, t3;
-        for (auto &e : sc5)
-            if (!(e.first < Rg.start - 5000 || e.first > Rg.end + 5000)) t5.push_back({e.first, &e.second, e.second.c.agg.cnt});
-        for (auto &e : sc3)
-            if (!(e.first < Rg.start - 5000 || e.first > Rg.end + 5000)) t3.push_back({e.first, &e.second, e.second.c.agg.cnt});
-        auto by_cnt = [](const T &a, const T &b) { return a.cnt != b.cnt ? a.cnt > b.cnt : a.pos < b.pos; };
-        std::sort(t5.begin(), t5.end(), by_cnt);
-        std::sort(t3.begin(), t3.end(), by_cnt);
+        std::vector<LgT> t5, t3;
         // the 3' clips by position (with their rank in t3): a 5' clip only
         // pairs with 3' clips in [p5 - 2.5 max_rl, p5 + max_rl - 10], and the
         // reference's loop over t3 does nothing else for the others, so the
         // pass visits just those, in t3 order
-        std::vector<std::pair<int, int>> by_pos(t3.size());
-        for (size_t i = 0; i < t3.size(); i++) by_pos[i] = {t3[i].pos, (int)i};
-        std::sort(by_pos.begin(), by_pos.end());
+        std::vector<std::pair<int, int>> by_pos;
+        lgins_lists(t5, t3, by_pos);
         std::vector<int> near;
-        for (T &a : t5) {
+        for (size_t ia = 0; ia < t5.size(); ia++) {
+            LgT &a = t5[ia];
             const int p5 = a.pos;
             Clip &sc5v = *a.c;
             const int cnt5 = a.cnt;
@@ -990,7 +1047,7 @@ struct RegionRealigner {
                 near.push_back(it->second);
             std::sort(near.begin(), near.end());
             for (int ni : near) {
-                T &b = t3[ni];
+                LgT &b = t3[ni];
                 try {
                     const int p3 = b.pos;
                     Clip &sc3v = *b.c;
@@ -1004,7 +1061,7 @@ struct RegionRealigner {
                     if (!(cnt5 / (double)cnt3 >= 0.08 && cnt5 / (double)cnt3 <= 12)) continue;
                     int bp5, bp3, score;
                     auto tf = std::chrono::steady_clock::now();
-                    find35(seq5, seq3, bp5, bp3, score);
+                    find35((int)ia, ni, seq5, seq3, bp5, bp3, score);
                     if (prof) prof[7] += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tf).count();
                     if (score == 0) continue;
                     const int sm = score / 2;
@@ -1207,7 +1264,10 @@ struct RegionRealigner {
         }
     }
 
-    void run(std::vector<Patch> &out, string &keys, double *phase) {
+    // VariationRealigner::process (:135-161) in two parts: up to the indel
+    // passes (collect_lgins_pairs then lists the clip pairs for the batch's
+    // device find35 pass), and realignlgins30 plus the diff into patches
+    void run_first(double *phase) {
         prof = phase;
         auto clk = [] { return std::chrono::steady_clock::now(); };
         auto t = clk();
@@ -1225,6 +1285,16 @@ struct RegionRealigner {
         lap(2);
         realignins(inscnt);
         lap(3);
+    }
+    void run_second(std::vector<Patch> &out, string &keys, double *phase) {
+        prof = phase;
+        auto clk = [] { return std::chrono::steady_clock::now(); };
+        auto t = clk();
+        auto lap = [&](int k) {
+            auto n = clk();
+            phase[k] += std::chrono::duration<double, std::milli>(n - t).count();
+            t = n;
+        };
         realignlgins30();
         lap(4);
         diff(out, keys);
@@ -1291,6 +1361,32 @@ rv_status mirror_launch(rv_ctx *ctx, cudaEvent_t after_kernels) {
         HCUDA(cudaMemcpyAsync(h + L.b_cov + L.b_kf, ctx->d_list_off, ((size_t)nc + 1) * 4, cudaMemcpyDeviceToHost, s));
     }
     ctx->mirror_pending = true;
+    return RV_OK;
+}
+
+// find35match of n clip pairs on the context's device (k_find35): pairs as
+// int32 quadruples into `strs`, results as (b5, b3, score) triples.
+static rv_status device_find35(rv_ctx *ctx, const int32_t *pairs, int64_t n, const string &strs, int32_t *res) {
+    const size_t b_pairs = (size_t)n * 16, b_strs = (strs.size() + 15) & ~(size_t)15, b_res = (size_t)n * 12;
+    const size_t need = b_pairs + b_strs + b_res;
+    if (ctx->cap_f35 < need || !ctx->d_f35) {
+        if (ctx->d_f35) cudaFree(ctx->d_f35);
+        ctx->d_f35 = nullptr;
+        ctx->cap_f35 = 0;
+        HCUDA(cudaMalloc(&ctx->d_f35, need + need / 4));
+        ctx->cap_f35 = need + need / 4;
+    }
+    char *d = (char *)ctx->d_f35;
+    cudaStream_t s = ctx->stream;
+    HCUDA(cudaMemcpyAsync(d, pairs, b_pairs, cudaMemcpyHostToDevice, s));
+    if (!strs.empty()) HCUDA(cudaMemcpyAsync(d + b_pairs, strs.data(), strs.size(), cudaMemcpyHostToDevice, s));
+    launch_find35((const int32_t *)d, n, d + b_pairs, (int32_t *)(d + b_pairs + b_strs), s);
+    HCUDA(cudaGetLastError());
+    HCUDA(cudaMemcpyAsync(res, d + b_pairs + b_strs, b_res, cudaMemcpyDeviceToHost, s));
+    HCUDA(cudaStreamSynchronize(s));
+    ctx->kernels += 1;
+    ctx->io_h2d += (int64_t)(b_pairs + strs.size());
+    ctx->io_d2h += (int64_t)b_res;
     return RV_OK;
 }
 
@@ -1369,13 +1465,66 @@ rv_status host_realign_full(rv_ctx *ctx) {
     std::mutex err_mu;
     string failure;
     std::vector<double> phase((size_t)nreg * 8, 0.0);
+    std::vector<std::unique_ptr<RegionRealigner>> rrs((size_t)nreg);
+    std::vector<std::vector<int32_t>> f35_pairs((size_t)nreg);
+    std::vector<string> f35_strs((size_t)nreg);
+    // the realigner up to the indel passes, and the clip pairs each region's
+    // realignlgins30 may test (offsets local to the region)
     parallel_for(nreg, [&](int64_t r) {
         try {
-            RegionRealigner rr(mir, ctx, (int)r);
-            rr.run(patches[r], keys[r], phase.data() + 8 * r);
+            rrs[r].reset(new RegionRealigner(mir, ctx, (int)r));
+            rrs[r]->run_first(phase.data() + 8 * r);
+            rrs[r]->collect_lgins_pairs(f35_pairs[r], f35_strs[r]);
         } catch (const std::exception &e) {
             // the reference's own realigner terminates here (an exception it
             // does not catch); the batch reports it instead
+            std::lock_guard<std::mutex> g(err_mu);
+            if (failure.empty()) failure = "realigner, region " + std::to_string(r) + ": " + e.what();
+        }
+    });
+    if (!failure.empty()) {
+        ctx->err = failure;
+        return RV_ERR_UNSUPPORTED;
+    }
+    // find35match of every listed pair of the batch, on the device
+    auto tf = now();
+    std::vector<int32_t> f35_res;
+    std::vector<int64_t> pair_base((size_t)nreg + 1, 0), str_base((size_t)nreg + 1, 0);
+    for (int r = 0; r < nreg; r++) {
+        pair_base[r + 1] = pair_base[r] + (int64_t)f35_pairs[r].size() / 4;
+        str_base[r + 1] = str_base[r] + (int64_t)f35_strs[r].size();
+    }
+    const int64_t np = pair_base[nreg];
+    if (np > 0) {
+        if (str_base[nreg] > INT32_MAX) {
+            ctx->err = "realigner: clip consensus strings exceed 2 GB";
+            return RV_ERR_CAPACITY;
+        }
+        std::vector<int32_t> all_pairs((size_t)np * 4);
+        string all_strs;
+        all_strs.reserve((size_t)str_base[nreg]);
+        for (int r = 0; r < nreg; r++) {
+            const std::vector<int32_t> &v = f35_pairs[r];
+            int32_t *o = all_pairs.data() + 4 * pair_base[r];
+            for (size_t i = 0; i < v.size(); i += 4) {
+                o[i] = v[i] + (int32_t)str_base[r];
+                o[i + 1] = v[i + 1];
+                o[i + 2] = v[i + 2] + (int32_t)str_base[r];
+                o[i + 3] = v[i + 3];
+            }
+            all_strs += f35_strs[r];
+        }
+        f35_res.resize((size_t)np * 3);
+        if ((st = device_find35(ctx, all_pairs.data(), np, all_strs, f35_res.data()))) return st;
+    }
+    const double t_f35 = ms(tf);
+    parallel_for(nreg, [&](int64_t r) {
+        try {
+            RegionRealigner &rr = *rrs[r];
+            if (np > 0) rr.f35_res = f35_res.data() + 3 * pair_base[r];
+            rr.run_second(patches[r], keys[r], phase.data() + 8 * r);
+            rrs[r].reset();
+        } catch (const std::exception &e) {
             std::lock_guard<std::mutex> g(err_mu);
             if (failure.empty()) failure = "realigner, region " + std::to_string(r) + ": " + e.what();
         }
@@ -1399,10 +1548,11 @@ rv_status host_realign_full(rv_ctx *ctx) {
         double sum[8] = {0};
         for (int r = 0; r < nreg; r++)
             for (int k = 0; k < 8; k++) sum[k] += phase[8 * r + k];
-        fprintf(stderr, "realign -k 1: listed keys %u, patches %zu, threads %d; ms: fetch %.2f run %.2f total %.2f; "
-                "thread-ms: setup %.2f mnp %.2f del %.2f ins %.2f lgins %.2f diff %.2f (consensus %.2f find35 %.2f)\n",
-                total, all.size(), nt, t_fetch, t_run, ms(t0), sum[0], sum[1], sum[2], sum[3], sum[4], sum[5], sum[6],
-                sum[7]);
+        fprintf(stderr, "realign -k 1: listed keys %u, patches %zu, threads %d, find35 pairs %lld; ms: fetch %.2f "
+                "device-find35 %.2f run %.2f total %.2f; thread-ms: setup %.2f mnp %.2f del %.2f ins %.2f lgins %.2f "
+                "diff %.2f (consensus %.2f find35 %.2f)\n",
+                total, all.size(), nt, (long long)np, t_fetch, t_f35, t_run, ms(t0), sum[0], sum[1], sum[2], sum[3],
+                sum[4], sum[5], sum[6], sum[7]);
     }
     return st;
 }

@@ -430,3 +430,47 @@ void launch_apply_patches(const DevState &st, const Patch *p, int64_t n, const u
 }
 
 }  // namespace rv
+
+namespace rv {
+
+// find35match (src/VariationRealigner.cpp:1396-1428) for a batch of soft-clip
+// consensus pairs, one thread per pair: pairs[4k..4k+3] = offset and length
+// of the 5' clip's string, offset and length of the 3' clip's string in
+// `strs`; res[3k..3k+2] = b5, b3, score (0, 0, 0 when no start passes).
+// Every start (i, j) in the reference's order; the first that passes wins.
+__global__ void k_find35(const int32_t *pairs, int64_t n, const char *strs, int32_t *res) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        const char *s5 = strs + pairs[4 * k];
+        const int l5 = pairs[4 * k + 1];
+        const char *s3 = strs + pairs[4 * k + 2];
+        const int l3 = pairs[4 * k + 3];
+        int b5 = 0, b3 = 0, score = 0;
+        for (int i = 0; i < l5 - 8 && score == 0; i++) {
+            for (int j = 1; j < l3 - 8; j++) {
+                int nm = 0, m = 0;
+                while (m + j <= l3 && i + m <= l5) {
+                    if (i + m == l5 || s3[l3 - j - m] != s5[i + m]) nm++;
+                    if (nm > 2) break;
+                    m++;
+                }
+                if (m - nm > 8 && nm / (double)m < 0.1 && (m + j >= l3 || i + m >= l5)) {
+                    b5 = i;
+                    b3 = j;
+                    score = m - nm;
+                    break;
+                }
+            }
+        }
+        res[3 * k] = b5;
+        res[3 * k + 1] = b3;
+        res[3 * k + 2] = score;
+    }
+}
+
+void launch_find35(const int32_t *pairs, int64_t n, const char *strs, int32_t *res, cudaStream_t s) {
+    if (n <= 0) return;
+    const int64_t blocks = (n + 127) / 128;
+    k_find35<<<(int)std::min<int64_t>(blocks, 152 * 64), 128, 0, s>>>(pairs, n, strs, res);
+}
+
+}  // namespace rv
