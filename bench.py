@@ -20,8 +20,9 @@ Inputs (~22 GB of reads) exceed the 129 MB L2, so no flush is needed
 between steps.  `parity` compares the GPU's records of four regions with
 the oracle's on the same reads (the CPU baseline sample); a mismatch fails
 the run.  Secondary keys: the 1 Mb somatic pair at 200x/100x
-(`somatic_pair_1mb`, with its BAM-decode leg), the other -k setting,
-the learned filter.
+(`somatic_pair_1mb`, with its BAM-decode leg), the batched 10,000-region
+amplicon panel against region-by-region calls (`panel`), the other -k
+setting, the learned filter.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
     python bench.py --bam-decode      # BAM decode alone, GPU vs host decoder
@@ -461,28 +462,32 @@ def learned_filter_leg():
     return res
 
 
-def run_panel(args):
-    """Batched amplicon panel (the 10,000-region shape, scaled to N regions):
-    region lengths U(100, 2000), depth log-normal median 500x, amplicon
-    reads with 0.5% exact duplicates, -t -u, simple mode.  Batched: all
-    regions in one submit and one persistent pileup launch; region by
-    region: one submit + pipeline per region (the reference's per-region
-    stage sequence).  Both through the C ABI from pinned host batches."""
+def panel_leg(n_reg: int, k: int, steps: int, warmup: int, device: int = 0, per_region_sample: int = 500) -> dict:
+    """Batched amplicon panel (config 2's shape: n_reg regions of U(100, 2000)
+    bp, depth log-normal median 500x, amplicon reads with 0.5% exact
+    duplicates, -t -u, simple mode), from pinned host batches through the C
+    ABI.  Batched: all regions in one submit and one persistent pileup
+    launch (the pileup chain as a CUDA graph); region by region: one submit
+    and pipeline per region (the reference's per-region stage sequence), on
+    the first `per_region_sample` regions, whose records must equal the
+    batched run's records for them."""
     import numpy as np
     from rabbitvar_gb300 import api, synth
-    n_reg = args.panel
-    g, _, rs, regions = synth.amplicon_panel(n_regions=n_reg, genome_len=n_reg * 5000)
-    params = api.default_params(local_realign=args.local_realign, dedup=1, unique_fwd=1)
-    ctx = api.Context(params)
+    t_gen = time.perf_counter()
+    g, _, rs, regions = synth.amplicon_panel_native(n_regions=n_reg, genome_len=n_reg * 5000)
+    t_gen = time.perf_counter() - t_gen
+    params = api.default_params(local_realign=k, dedup=1, unique_fwd=1)
+    ctx = api.Context(params, device=device)
     ctx.upload_reference(rs.contig, synth.genome_str(g).encode())
-    # the pileup chain as a CUDA graph (updated per batch), in both legs
     ctx.set_pileup_graph(True)
     batch = api.Batch.from_readset(rs, pinned=True)
-    span = rs.pos.astype(np.int64) + 150
+    sample = regions[:min(per_region_sample, len(regions))]
     subs = []
-    for a, b in regions:
-        idx = np.nonzero((rs.pos < b) & (span > a - 1 - 200))[0]
-        subs.append(api.Batch.from_readset(synth.take(rs, idx), pinned=True))
+    for a, b in sample:
+        lo = int(np.searchsorted(rs.pos, a - 1 - 400))
+        hi = int(np.searchsorted(rs.pos, b))
+        subs.append(api.Batch.from_readset(synth.read_range(rs, lo, hi), pinned=True))
+    sample_reads = sum(sb.n_reads for sb in subs)
 
     def batched():
         ctx.submit(batch, regions)
@@ -493,7 +498,7 @@ def run_panel(args):
 
     def per_region():
         out = []
-        for r, b in zip(regions, subs):
+        for r, b in zip(sample, subs):
             ctx.submit(b, [r])
             ctx.pileup()
             ctx.realign()
@@ -501,27 +506,43 @@ def run_panel(args):
             out.append(ctx.format_records("S", rs.contig)[0])
         return "".join(out)
 
-    for _ in range(args.warmup):
+    for _ in range(max(1, warmup)):
         t_b = batched()
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(steps):
         t_b = batched()
-    dt_b = (time.perf_counter() - t0) / args.steps
-    t_r = per_region()
+    dt_b = (time.perf_counter() - t0) / steps
+    per_region()
     t0 = time.perf_counter()
     t_r = per_region()
     dt_r = time.perf_counter() - t0
-    same = sorted(t_b.splitlines()) == sorted(t_r.splitlines())
-    out = {"metric": f"reads/s batched amplicon panel ({n_reg} regions, -t -u)", "value": rs.n / dt_b,
-           "unit": "reads/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-           "ms_per_step": dt_b * 1e3, "higher_is_better": True, "data": "synthetic",
-           "config": {"workload": f"{n_reg} regions U(100,2000) bp, depth lognormal median 500x, amplicon 2x150, "
-                                  f"0.5% PCR duplicates, -t -u -k {args.local_realign}, simple mode", "reads": int(rs.n)},
-           "region_by_region": {"value": rs.n / dt_r, "unit": "reads/s", "ms": dt_r * 1e3},
-           "speedup_batched": dt_r / dt_b, "records": len(t_b.splitlines()), "records_equal": same,
+    mine = sorted(region_records(t_b, rs.contig, sample))
+    same = mine == sorted(t_r.splitlines())
+    out = {"workload": f"{n_reg} regions U(100,2000) bp, depth lognormal median 500x, amplicon 2x150, "
+                       f"0.5% PCR duplicates, -t -u -k {k}, simple mode",
+           "value": rs.n / dt_b, "unit": "reads/s", "reads": int(rs.n), "ms_per_step": dt_b * 1e3, "steps": steps,
+           "records": len(t_b.splitlines()), "generate_s": t_gen,
+           "region_by_region": {"value": sample_reads / dt_r, "unit": "reads/s", "regions": len(sample),
+                                "reads": int(sample_reads), "ms": dt_r * 1e3},
+           "speedup_batched": (rs.n / dt_b) / (sample_reads / dt_r),
+           "records_equal_region_by_region": same, "sample_records": len(mine),
            "pileup_graph": dict(zip(("launches", "instantiations"), ctx.pileup_graph_stats()))}
-    print(json.dumps(out))
     ctx.close()
+    batch.close()
+    for sb in subs:
+        sb.close()
+    return out
+
+
+def run_panel(args):
+    """`--panel N`: the batched amplicon panel leg alone, as one JSON line."""
+    r = panel_leg(args.panel, args.local_realign, args.steps, args.warmup)
+    out = {"metric": f"reads/s batched amplicon panel ({args.panel} regions, -t -u)", "value": r["value"],
+           "unit": "reads/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": r["ms_per_step"], "higher_is_better": True, "data": "synthetic (seeded)",
+           "config": {"workload": r["workload"], "reads": r["reads"]}}
+    out.update({k: v for k, v in r.items() if k not in ("value", "workload", "ms_per_step", "steps")})
+    print(json.dumps(out))
 
 
 def run_reference(args, rank):
@@ -691,6 +712,7 @@ def main():
     ap.add_argument("--no-other-k", action="store_true", help="skip the leg with the other -k setting")
     ap.add_argument("--no-bam", action="store_true", help="skip the leg that starts from BGZF-compressed BAM bytes")
     ap.add_argument("--no-1mb", action="store_true", help="skip the 1 Mb somatic pair leg")
+    ap.add_argument("--no-panel", action="store_true", help="skip the 10,000-region amplicon panel leg")
     ap.add_argument("--regions", type=int, default=0, metavar="N",
                     help="run the headline on the first N regions of the panel only (for profiling)")
     ap.add_argument("--bam-decode", action="store_true",
@@ -764,6 +786,9 @@ def main():
         del t2, n2
     if rank == 0 and not args.no_1mb:
         out["somatic_pair_1mb"] = pair_1mb_leg(args, local)
+    if rank == 0 and not args.no_panel:
+        out["panel"] = panel_leg(10_000, args.local_realign, min(args.steps, 3), min(args.warmup, 2), local)
+        parity_ok = parity_ok and out["panel"]["records_equal_region_by_region"]
     if rank == 0 and not args.no_learned:
         out["learned_filter"] = learned_filter_leg()
     if rank == 0:

@@ -7,6 +7,7 @@
 #include <iterator>
 #include <cstdlib>
 #include <climits>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <set>
@@ -402,6 +403,9 @@ rv_status rv_create(rv_ctx **out, const rv_params *p, int device, size_t hbm_bud
     DevParams &d = ctx->dp;
     memset(&d, 0, sizeof d);
     d.goodq = p->goodq;
+    // the hot loops compare integer base qualities with an integer threshold
+    // (FP64 compares are slow on this part)
+    d.goodq_i = !(p->goodq > -1e9) ? INT32_MIN : (p->goodq > 1e9 ? INT32_MAX : (int32_t)std::ceil(p->goodq));
     d.freq = p->freq;
     d.qratio = p->qratio;
     d.mapq_filter = p->mapq_filter;

@@ -92,7 +92,7 @@ struct DevParams {
     int32_t trim_bases_after, minmatch, dedup, unique_fwd, unique_first, do_pileup, fisher, move_indels_3;
     int32_t svminlen, somatic;
     int32_t dataset_min;  // > 0: candidate-set scoring (every allele seen this many times)
-    int32_t pad;
+    int32_t goodq_i;      // ceil(goodq): for an integer quality q, q >= goodq exactly when q >= goodq_i
 };
 
 // Cell arrays: one cell per (position, base A/C/G/T); index = 4 * cell + b.

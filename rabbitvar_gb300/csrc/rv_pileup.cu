@@ -254,7 +254,7 @@ struct TileFast {
     uint32_t w_s;       // shared-space address of the word arrays (w0 | w1 | w2 | first, 4*kTileW words each)
     uint32_t ref_s;     // shared-space address of the reference bases wlo .. wlo + kTileW - 1
     int wlo;
-    double goodq;
+    int goodq;          // integer quality threshold (DevParams::goodq_i)
     // reference base at p (inside the region's window): from the tile's shared copy
     __device__ __forceinline__ char ref(const char *refp, int p) const {
         unsigned d = (unsigned)(p - wlo);
@@ -607,10 +607,16 @@ __global__ void __launch_bounds__(kPileupThreads, MINB) k_pileup_tiles(DevState 
         sink.f.w_s = (uint32_t)__cvta_generic_to_shared(w0);
         sink.f.wlo = wlo;
         sink.f.ref_s = (uint32_t)__cvta_generic_to_shared(s_ref);
-        sink.f.goodq = P.goodq;
+        sink.f.goodq = P.goodq_i;
         {
             Walker<TileSink<AGG>> w(P, sink, R, st.ref, st.ref_len);
-            for (int64_t r = tile.r0 + threadIdx.x; r < tile.r1; r += blockDim.x) {
+            // lane-strided read order: warp w, lane l walks the tile's read
+            // 8 l + w, so a warp's lanes hold reads spread over the whole tile
+            // (consecutive reads of a deep pileup start at the same position
+            // and would hit the same histogram words together)
+            static_assert(kTileReads == 256 && kPileupThreads == 256, "tile read permutation");
+            const int64_t k = (int64_t)((threadIdx.x & 31u) * 8u + (threadIdx.x >> 5));
+            for (int64_t r = tile.r0 + k; r < tile.r1; r += blockDim.x) {
                 if (!read_passes(st.batch, P, R, r)) continue;
                 if (R.serial && R.edge_hit) {
                     int a, b;

@@ -936,24 +936,13 @@ struct RegionRealigner {
         }
     }
 
-    // find35match (:1396-1428) of the clip pair (ia in t5, ib in t3): from the
-    // batch's device results when collect_lgins_pairs listed the pair, else
-    // on the host
-    std::unordered_map<uint64_t, int64_t> f35_index;  // (ia, ib) -> pair index
-    const int32_t *f35_res = nullptr;                // per pair: b5, b3, score
-    void find35(int ia, int ib, const string &s5, const string &s3, int &b5, int &b3, int &score) {
-        if (f35_res) {
-            auto it = f35_index.find(((uint64_t)(uint32_t)ia << 32) | (uint32_t)ib);
-            if (it != f35_index.end()) {
-                const int32_t *r = f35_res + 3 * it->second;
-                b5 = r[0];
-                b3 = r[1];
-                score = r[2];
-                return;
-            }
-        }
-        keymatch::find35(s5, s3, b5, b3, score);
-    }
+    // The batch's device find35match results for this region's listed clip
+    // pairs (collect_lgins_pairs: per 5' clip its first pair, the 3' clips in
+    // its position window, and each listed 3' clip's consensus length)
+    const int32_t *f35_res = nullptr;            // per pair: b5, b3, score
+    std::vector<int64_t> f35_first;              // per t5 entry: its first pair, or -1
+    std::vector<std::vector<int>> f35_near;      // per t5 entry: the 3' clips in its window, t3 order
+    std::vector<int32_t> f35_len3;               // per t3 entry: consensus length (-1: not needed)
 
     // The 5'/3' clip lists realignlgins30 walks (by count), and the 3' clips
     // by position with their rank in t3.
@@ -980,16 +969,10 @@ struct RegionRealigner {
         std::vector<LgT> t5, t3;
         std::vector<std::pair<int, int>> by_pos;
         lgins_lists(t5, t3, by_pos);
-        std::vector<std::pair<int32_t, int32_t>> s3at(t3.size(), {-1, 0});
-        auto str3 = [&](int ib) {
-            if (s3at[ib].first < 0) {
-                const string q = peek_consensus(*t3[ib].c);
-                s3at[ib] = {(int32_t)strs.size(), (int32_t)q.size()};
-                strs += q;
-            }
-            return s3at[ib];
-        };
-        std::vector<int> near;
+        std::vector<int32_t> off3(t3.size(), -1);
+        f35_len3.assign(t3.size(), -1);
+        f35_first.assign(t5.size(), -1);
+        f35_near.assign(t5.size(), std::vector<int>());
         int64_t k = 0;
         for (size_t ia = 0; ia < t5.size(); ia++) {
             const LgT &a = t5[ia];
@@ -997,25 +980,31 @@ struct RegionRealigner {
             if (seq5.size() <= 10) continue;
             const int p5 = a.pos;
             const int lo3 = (int)std::ceil(p5 - max_rl * 2.5) - 1, hi3 = p5 + max_rl - 10 + 1;
-            near.clear();
+            std::vector<int> &near = f35_near[ia];
             for (auto it = std::lower_bound(by_pos.begin(), by_pos.end(), std::make_pair(lo3, INT32_MIN));
                  it != by_pos.end() && it->first <= hi3; ++it)
                 near.push_back(it->second);
             std::sort(near.begin(), near.end());
+            f35_first[ia] = k;
             int32_t off5 = -1;
             for (int ib : near) {
                 const LgT &b = t3[ib];
                 if (p5 - b.pos > max_rl * 2.5) continue;
                 if (b.pos - p5 > max_rl - 10) continue;
                 if (!(a.cnt / (double)b.cnt >= 0.08 && a.cnt / (double)b.cnt <= 12)) continue;
-                const auto s3v = str3(ib);
-                if (s3v.second <= 10) continue;
+                if (f35_len3[ib] < 0) {
+                    const string q = peek_consensus(*t3[ib].c);
+                    off3[ib] = (int32_t)strs.size();
+                    f35_len3[ib] = (int32_t)q.size();
+                    strs += q;
+                }
+                if (f35_len3[ib] <= 10) continue;
                 if (off5 < 0) {
                     off5 = (int32_t)strs.size();
                     strs += seq5;
                 }
-                pairs.insert(pairs.end(), {off5, (int32_t)seq5.size(), s3v.first, s3v.second});
-                f35_index[((uint64_t)(uint32_t)ia << 32) | (uint32_t)ib] = k++;
+                pairs.insert(pairs.end(), {off5, (int32_t)seq5.size(), off3[ib], f35_len3[ib]});
+                k++;
             }
         }
     }
@@ -1031,7 +1020,8 @@ struct RegionRealigner {
         // pass visits just those, in t3 order
         std::vector<std::pair<int, int>> by_pos;
         lgins_lists(t5, t3, by_pos);
-        std::vector<int> near;
+        const bool dev = f35_res != nullptr;  // device results for the listed pairs
+        std::vector<int> near_host;
         for (size_t ia = 0; ia < t5.size(); ia++) {
             LgT &a = t5[ia];
             const int p5 = a.pos;
@@ -1040,14 +1030,29 @@ struct RegionRealigner {
             if (sc5v.c.used) continue;
             const string &seq5 = consensus(sc5v);
             if (seq5.size() <= 10) continue;
-            const int lo3 = (int)std::ceil(p5 - max_rl * 2.5) - 1, hi3 = p5 + max_rl - 10 + 1;
-            near.clear();
-            for (auto it = std::lower_bound(by_pos.begin(), by_pos.end(), std::make_pair(lo3, INT32_MIN));
-                 it != by_pos.end() && it->first <= hi3; ++it)
-                near.push_back(it->second);
-            std::sort(near.begin(), near.end());
-            for (int ni : near) {
+            const std::vector<int> *nearp = &near_host;
+            if (dev) {
+                nearp = &f35_near[ia];
+            } else {
+                const int lo3 = (int)std::ceil(p5 - max_rl * 2.5) - 1, hi3 = p5 + max_rl - 10 + 1;
+                near_host.clear();
+                for (auto it = std::lower_bound(by_pos.begin(), by_pos.end(), std::make_pair(lo3, INT32_MIN));
+                     it != by_pos.end() && it->first <= hi3; ++it)
+                    near_host.push_back(it->second);
+                std::sort(near_host.begin(), near_host.end());
+            }
+            // the listed pairs of this 5' clip come in the order of its
+            // window's 3' clips that pass the static tests
+            int64_t kcur = dev ? f35_first[ia] : -1;
+            for (int ni : *nearp) {
                 LgT &b = t3[ni];
+                int64_t kidx = -1;
+                if (dev) {
+                    const int pb = b.pos;
+                    if (!(p5 - pb > max_rl * 2.5) && !(pb - p5 > max_rl - 10) &&
+                        (cnt5 / (double)b.cnt >= 0.08 && cnt5 / (double)b.cnt <= 12) && f35_len3[ni] > 10)
+                        kidx = kcur++;
+                }
                 try {
                     const int p3 = b.pos;
                     Clip &sc3v = *b.c;
@@ -1060,9 +1065,14 @@ struct RegionRealigner {
                     if (seq3.size() <= 10) continue;
                     if (!(cnt5 / (double)cnt3 >= 0.08 && cnt5 / (double)cnt3 <= 12)) continue;
                     int bp5, bp3, score;
-                    auto tf = std::chrono::steady_clock::now();
-                    find35((int)ia, ni, seq5, seq3, bp5, bp3, score);
-                    if (prof) prof[7] += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tf).count();
+                    if (kidx >= 0) {
+                        const int32_t *rr = f35_res + 3 * kidx;
+                        bp5 = rr[0];
+                        bp3 = rr[1];
+                        score = rr[2];
+                    } else {
+                        keymatch::find35(seq5, seq3, bp5, bp3, score);
+                    }
                     if (score == 0) continue;
                     const int sm = score / 2;
                     string ins = bp3 + sm > 1 ? vsub(seq3, 0, -(bp3 + sm) + 1) : seq3;

@@ -775,13 +775,40 @@ void launch_features(const DevState &st, const DevParams &P, const CandVar *cand
     if (n > 0) k_features<<<(int)std::min<int64_t>((n + 127) / 128, 4096), 128, 0, s>>>(st, P, cand, n, out);
 }
 
-// Batched Fisher tests (rv_fisher_batch)
+// Batched Fisher tests (rv_fisher_batch): one warp per table.  The lanes
+// split the hypergeometric terms x = lo, lo + 1, ..., hi (a deep table has
+// thousands, each an FP64 exp) and the partial sums are added by shuffles;
+// the same terms and tie slack as fisher_two_sided, summed in another order.
 __global__ void k_fisher(const int32_t *tab, int64_t n, double *p2, double *ratio, const double *lf) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        int a = tab[4 * i], b = tab[4 * i + 1], c = tab[4 * i + 2], d = tab[4 * i + 3];
-        p2[i] = fisher_two_sided(a, b, c, d, lf);
-        double ad = (double)a * d, bc = (double)b * c;
-        ratio[i] = (bc != 0 && ad != 0) ? (ad > bc ? ad / bc : bc / ad) : 0.0;
+    const int lane = (int)(threadIdx.x & 31u);
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
+        const int a = tab[4 * i], b = tab[4 * i + 1], c = tab[4 * i + 2], d = tab[4 * i + 3];
+        const int r1 = a + b, c1 = a + c, nn = a + b + c + d;
+        const int lo = r1 + c1 - nn > 0 ? r1 + c1 - nn : 0;
+        const int hi = r1 < c1 ? r1 : c1;
+        double two;
+        if (a < 0 || b < 0 || c < 0 || d < 0 || lo >= hi) {
+            two = 1.0;
+        } else if (!lf || nn >= kLogFact) {
+            two = fisher_two_sided(a, b, c, d, lf);  // (no table: one lane, lgamma terms)
+        } else {
+            const double base = log_choose_t(lf, nn, c1);
+            const double p_obs = exp(log_choose_t(lf, r1, a) + log_choose_t(lf, nn - r1, c1 - a) - base);
+            const double thr = p_obs * (1.0 + 1e-7);
+            double part = 0.0;
+            for (int x = lo + lane; x <= hi; x += 32) {
+                const double p = exp(log_choose_t(lf, r1, x) + log_choose_t(lf, nn - r1, c1 - x) - base);
+                if (p <= thr) part += p;
+            }
+            for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xFFFFFFFFu, part, o);
+            two = part > 1.0 ? 1.0 : part;
+        }
+        if (lane == 0) {
+            p2[i] = two;
+            const double ad = (double)a * d, bc = (double)b * c;
+            ratio[i] = (bc != 0 && ad != 0) ? (ad > bc ? ad / bc : bc / ad) : 0.0;
+        }
     }
 }
 
@@ -806,8 +833,8 @@ void launch_score_list(const DevState &st, const DevParams &P, const int2 *list,
     if (n > 0) k_score_list<<<(n + 127) / 128 < 1216 ? (n + 127) / 128 : 1216, 128, 0, s>>>(st, P, list, n);
 }
 void launch_fisher(const int32_t *tab, int64_t n, double *p2, double *ratio, cudaStream_t s, const double *lf) {
-    if (n > 0)
-        k_fisher<<<(int)((n + 127) / 128 < 4096 ? (n + 127) / 128 : 4096), 128, 0, s>>>(tab, n, p2, ratio, lf);
+    if (n > 0)  // four tables (warps) per block
+        k_fisher<<<(int)((n + 3) / 4 < 8192 ? (n + 3) / 4 : 8192), 128, 0, s>>>(tab, n, p2, ratio, lf);
 }
 void launch_fill_logfact(double *lf, cudaStream_t s) { k_fill_logfact<<<256, 256, 0, s>>>(lf, kLogFact); }
 

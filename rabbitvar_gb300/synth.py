@@ -1019,3 +1019,50 @@ def deep_somatic_panel(seed: int = 0x5EED0003, n_regions: int = 400, region_len:
     normal = simulate_regions(g, germ, spans, normal_depth, seed=seed * 2 + 2, artifact_rate=1e-4, artifact_q=20,
                               name_base=1 << 40, threads=threads, span_ids=idx)
     return g, (germ, som), tumor, normal, regions
+
+
+def amplicon_panel_native(seed: int = 0x5EED0002, n_regions: int = 10_000, genome_len: int = 50_000_000,
+                          median_depth: float = 500.0, read_len: int = 150, dup_frac: float = 0.005,
+                          max_depth: float = 5000.0, min_depth: float = 50.0, threads: int | None = None,
+                          only: list[int] | None = None):
+    """The batched amplicon panel (the shape of `amplicon_panel`) from the
+    native generator, for its full size (10,000 regions, ~47 M reads):
+    regions of U(100, 2000) bp, one per genome_len / n_regions slot; per-region
+    depth log-normal (median `median_depth`, sigma ln(10)/3, clipped to
+    [min_depth, max_depth]); each region tiled by amplicons of 250..350 bp
+    with read 1 at the amplicon start (forward) and read 2 ending at its end
+    (reverse); a fraction `dup_frac` of pairs duplicated as exact copies;
+    germline SNVs at 1e-3/bp with VAF 0.5 or 1.0, carried per read.  Returns
+    (genome, variants, reads, regions of the reads); `only` picks regions
+    (each region's reads are the same as in the whole panel)."""
+    rng = np.random.default_rng(seed)
+    L = read_len
+    g = make_genome(genome_len, rng)
+    lens = rng.integers(100, 2001, size=n_regions)
+    slot = genome_len // n_regions
+    starts = np.array([i * slot + int(rng.integers(600, max(601, slot - int(lens[i]) - 600)))
+                       for i in range(n_regions)])
+    regions = [(int(s) + 1, int(s + ln)) for s, ln in zip(starts.tolist(), lens.tolist())]
+    depth = np.clip(np.exp(np.log(median_depth) + rng.normal(0, np.log(10) / 3, n_regions)), min_depth, max_depth)
+    variants = []
+    for a, b in regions:
+        k = rng.binomial(b - a + 1, 1e-3)
+        for p in sorted(set(rng.integers(a - 1, b, size=k).tolist())):
+            variants.append(Variant(pos=int(p), kind="snv", ref="ACGT"[int(g[p])],
+                                    alt="ACGT"[_rand_other(int(g[p]), rng)],
+                                    vaf=0.5 if rng.random() < 0.7 else 1.0))
+    amplicons, spans = [], []
+    for (a, b), d in zip(regions, depth.tolist()):
+        p = a - 1 - 100
+        amps = []
+        while p < b:
+            ln = int(rng.integers(250, 351))
+            amps.append((p, p + ln, max(1, int(round(d * ln / (2 * L))))))
+            p += ln - 60
+        amplicons.append(amps)
+        spans.append((a - 1 - 100, p + 350))
+    idx = list(range(n_regions)) if only is None else sorted(only)
+    rs = simulate_regions(g, variants, spans, 0.0, seed=seed * 2 + 3, read_len=L, softclip_frac=0.0,
+                          mapq0_frac=0.0, n_rate=0.0, amplicons=amplicons, dup_frac=dup_frac, threads=threads,
+                          span_ids=idx)
+    return g, variants, rs, [regions[i] for i in idx]
