@@ -73,7 +73,7 @@ class SiteRecord(C.Structure):
 
 EXPORTS = ["rv_default_params", "rv_create", "rv_destroy", "rv_last_error", "rv_upload_reference",
            "rv_submit_batch", "rv_pileup", "rv_realign", "rv_score", "rv_format_records", "rv_fetch_records",
-           "rv_call_regions", "rv_score_candidates", "rv_candidates", "rv_score_pair", "rv_pileup_realign_pair", "rv_format_somatic", "rv_call_somatic", "rv_call_somatic_stream", "rv_export_maps", "rv_last_timings", "rv_stage_times", "rv_set_pileup_graph", "rv_pileup_graph_stats", "rv_io_bytes", "rv_fisher_batch", "rv_bam_read",
+           "rv_call_regions", "rv_score_candidates", "rv_candidates", "rv_score_pair", "rv_pileup_realign_pair", "rv_format_somatic", "rv_call_somatic", "rv_call_somatic_stream", "rv_export_maps", "rv_last_timings", "rv_stage_times", "rv_set_pileup_graph", "rv_pileup_graph_stats", "rv_set_capacities", "rv_capacity_stats", "rv_io_bytes", "rv_fisher_batch", "rv_bam_read",
            "rv_bam_contigs", "rv_bam_batch", "rv_bam_read_mem", "rv_bam_read_gpu", "rv_bam_reread_gpu", "rv_bam_batch_host", "rv_bam_free", "rv_fasta_read", "rv_free", "rv_alloc_pinned",
            "rv_free_pinned", "rv_mlp_create", "rv_mlp_destroy", "rv_mlp_last_error", "rv_mlp_set_params",
            "rv_mlp_get_params", "rv_mlp_train", "rv_mlp_gradients", "rv_mlp_predict", "rv_mlp_step_ms"]

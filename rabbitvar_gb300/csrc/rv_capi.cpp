@@ -10,6 +10,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <set>
 #include <string>
 #include <thread>
@@ -1288,16 +1289,17 @@ rv_status rv_score_pair(rv_ctx *tumor, rv_ctx *normal) {
     return RV_OK;
 }
 
-rv_status rv_pileup_realign_pair(rv_ctx *tumor, rv_ctx *normal) {
-    if (!tumor || !normal || tumor == normal) return RV_ERR_ARG;
+namespace {
+
+// Queues both samples' pileups (and, with -k 1, their realigner mirrors)
+// without waiting.  The tumor's mirror kernels go before the normal's
+// pileup, whose persistent blocks would otherwise hold every SM until they
+// finish; the mirror's copies then overlap the normal's kernels.  On an
+// error nothing stays in flight.
+rv_status pair_launch(rv_ctx *tumor, rv_ctx *normal) {
     rv_status s;
-    // both samples' kernels are queued first (one stream each); the tumor's
-    // host realigner then runs while the normal's pileup is on the device
     if ((s = pileup_launch(tumor, tumor->stream))) return s;
     if (tumor->params.local_realign) {
-        // the tumor's mirror kernels go before the normal's pileup, whose
-        // persistent blocks would otherwise hold every SM until they finish;
-        // the mirror's copies then overlap the normal's kernels
         if ((s = mirror_launch(tumor, tumor->ev[11]))) {
             pileup_finish(tumor, tumor->stream);
             return s;
@@ -1322,8 +1324,20 @@ rv_status rv_pileup_realign_pair(rv_ctx *tumor, rv_ctx *normal) {
         pileup_finish(normal, normal->stream);
         return s;
     }
+    return RV_OK;
+}
+
+// Waits for the tumor's pileup and realigns it on the host (while the
+// normal's kernels run), then the normal's.  `between` runs after the
+// tumor's pileup finished and before its realigner (the stream uses it to
+// queue the next batch's pileups behind this one's).
+rv_status pair_finish(rv_ctx *tumor, rv_ctx *normal, const std::function<rv_status()> &between) {
     rv_status st = pileup_finish(tumor, tumor->stream);
     if (st) {
+        pileup_finish(normal, normal->stream);
+        return st;
+    }
+    if ((st = between())) {
         pileup_finish(normal, normal->stream);
         return st;
     }
@@ -1331,9 +1345,20 @@ rv_status rv_pileup_realign_pair(rv_ctx *tumor, rv_ctx *normal) {
         pileup_finish(normal, normal->stream);
         return st;
     }
-    if ((s = pileup_finish(normal, normal->stream))) { tumor->err = normal->err; return s; }
-    if ((s = rv_realign(normal, nullptr))) { tumor->err = normal->err; return s; }
+    if ((st = pileup_finish(normal, normal->stream))) { tumor->err = normal->err; return st; }
+    if ((st = rv_realign(normal, nullptr))) { tumor->err = normal->err; return st; }
     return RV_OK;
+}
+
+}  // namespace
+
+rv_status rv_pileup_realign_pair(rv_ctx *tumor, rv_ctx *normal) {
+    if (!tumor || !normal || tumor == normal) return RV_ERR_ARG;
+    // both samples' kernels are queued first (one stream each); the tumor's
+    // host realigner then runs while the normal's pileup is on the device
+    rv_status s = pair_launch(tumor, normal);
+    if (s) return s;
+    return pair_finish(tumor, normal, [] { return (rv_status)RV_OK; });
 }
 
 rv_status rv_call_somatic_stream(rv_ctx *tumor0, rv_ctx *normal0, rv_ctx *tumor1, rv_ctx *normal1,
@@ -1379,24 +1404,49 @@ rv_status rv_call_somatic_stream(rv_ctx *tumor0, rv_ctx *normal0, rv_ctx *tumor1
     rv_status s = RV_OK;
     int bad = 0;  // the pair whose context holds the error message
     // jobs 0 and 1 are uploaded here; job k + 2 by the host thread that
-    // formats job k, on the same pair, right after it
+    // formats job k, on the same pair, right after it.  Job k + 1's pileups
+    // are queued as soon as job k's tumor pileup has finished (and job
+    // k - 1's formatting, which uploads job k + 1, has joined), so the device
+    // piles up the next batch while the host realigns this one.
     if (n_jobs > 0) s = submit(0, 0);
     if (!s && n_jobs > 1) {
         bad = 1;
         s = submit(1, 1);
     }
+    if (!s && n_jobs > 0) {
+        bad = 0;
+        s = pair_launch(T[0], N[0]);
+    }
+    bool next_in_flight = false;  // job k + 1's pileups are queued
     PhaseTimer tm("stream");
     for (int64_t k = 0; k < n_jobs && !s; k++) {
         const int pi = (int)(k & 1);
         bad = pi;
-        // device stages of job k on pair pi; the host thread formats job k - 1
-        // and uploads job k + 1 on the other pair meanwhile
-        if ((s = rv_pileup_realign_pair(T[pi], N[pi]))) break;
-        tm.lap("pileup_realign");
-        bad = pi ^ 1;
-        if ((s = finish(pi ^ 1, k - 1))) break;
-        tm.lap("wait_format");
-        bad = pi;
+        next_in_flight = false;
+        // device stages of job k on pair pi: its pileups were queued earlier;
+        // once the tumor's has finished, the host thread that formatted job
+        // k - 1 (and uploaded job k + 1) is joined and job k + 1's pileups
+        // are queued on the other pair
+        auto between = [&]() -> rv_status {
+            tm.lap("pileup_wait");
+            rv_status f = finish(pi ^ 1, k - 1);
+            if (f) {
+                bad = pi ^ 1;
+                return f;
+            }
+            tm.lap("wait_format");
+            if (k + 1 < n_jobs) {
+                rv_status l = pair_launch(T[pi ^ 1], N[pi ^ 1]);
+                if (l) {
+                    bad = pi ^ 1;
+                    return l;
+                }
+                next_in_flight = true;
+            }
+            return (rv_status)RV_OK;
+        };
+        if ((s = pair_finish(T[pi], N[pi], between))) break;
+        tm.lap("realign");
         if ((s = rv_score_pair(T[pi], N[pi]))) break;
         tm.lap("score");
         fmt[pi].active = true;
@@ -1414,6 +1464,12 @@ rv_status rv_call_somatic_stream(rv_ctx *tumor0, rv_ctx *normal0, rv_ctx *tumor1
             }
             *out = st;
         });
+    }
+    // a failure leaves no pileup of the next job in flight
+    if (s && next_in_flight) {
+        const int pn = bad ^ 1;
+        for (rv_ctx *c : {T[pn], N[pn]})
+            if (c->pileup_pending) pileup_finish(c, c->stream);
     }
     if (!s && n_jobs > 0) {
         bad = (int)((n_jobs - 1) & 1);

@@ -1496,6 +1496,7 @@ rv_status host_realign_full(rv_ctx *ctx) {
         ctx->err = failure;
         return RV_ERR_UNSUPPORTED;
     }
+    const double t_first = ms(t0);
     // find35match of every listed pair of the batch, on the device
     auto tf = now();
     std::vector<int32_t> f35_res;
@@ -1559,10 +1560,10 @@ rv_status host_realign_full(rv_ctx *ctx) {
         for (int r = 0; r < nreg; r++)
             for (int k = 0; k < 8; k++) sum[k] += phase[8 * r + k];
         fprintf(stderr, "realign -k 1: listed keys %u, patches %zu, threads %d, find35 pairs %lld; ms: fetch %.2f "
-                "device-find35 %.2f run %.2f total %.2f; thread-ms: setup %.2f mnp %.2f del %.2f ins %.2f lgins %.2f "
-                "diff %.2f (consensus %.2f find35 %.2f)\n",
-                total, all.size(), nt, (long long)np, t_fetch, t_f35, t_run, ms(t0), sum[0], sum[1], sum[2], sum[3],
-                sum[4], sum[5], sum[6], sum[7]);
+                "first-half %.2f device-find35 %.2f run %.2f total %.2f; thread-ms: setup %.2f mnp %.2f del %.2f "
+                "ins %.2f lgins %.2f diff %.2f (consensus %.2f)\n",
+                total, all.size(), nt, (long long)np, t_fetch, t_first, t_f35, t_run, ms(t0), sum[0], sum[1], sum[2],
+                sum[3], sum[4], sum[5], sum[6]);
     }
     return st;
 }

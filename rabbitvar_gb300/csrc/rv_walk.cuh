@@ -823,22 +823,20 @@ struct Walker {
             // object itself is in local memory for the out-of-line paths)
             int st = start, rp = rpis, rq = rpes;
             int celr = cel;
-            // the read's bases and qualities are read once: streaming loads
-            // (evict first) leave L2 to the tables and the walkers' state
             const uint4 *seq16 = reinterpret_cast<const uint4 *>(rv.seq);
             const uint4 *qual16 = reinterpret_cast<const uint4 *>(rv.qual);
             const char *refp = ref;
             uint4 qw = make_uint4(0, 0, 0, 0), sw = make_uint4(0, 0, 0, 0);
             int qblk = -1, sblk = -1;
             for (int i = offset; i < celr; i++) {
-                if ((rp >> 5) != sblk) { sblk = rp >> 5; sw = __ldcs(seq16 + sblk); }
+                if ((rp >> 5) != sblk) { sblk = rp >> 5; sw = __ldg(seq16 + sblk); }
                 const uint32_t swd_ = pick_word(sw, (rp & 31) >> 3);
                 const int code = (int)((swd_ >> (((rp & 7) ^ 1) * 4)) & 15u);
                 if (code == 15) {  // 'N': skipped (src/parseCigar.cpp:686-692)
                     st++; rp++; rq++;
                     continue;
                 }
-                if ((rp >> 4) != qblk) { qblk = rp >> 4; qw = __ldcs(qual16 + qblk); }
+                if ((rp >> 4) != qblk) { qblk = rp >> 4; qw = __ldg(qual16 + qblk); }
                 const int q0 = (int)((pick_word(qw, (rp & 15) >> 2) >> ((rp & 3) * 8)) & 255u);
                 const int b = code_base(code);
                 const bool hs = st >= ws && st <= we;
