@@ -208,7 +208,11 @@ struct SinkBase {
         Slot *s = hash_get(st->hash, st->err, region_idx, kind, pos, k, n);
         if (s) slot_obs(*st, s, o, P->goodq, (uint32_t)read);
     }
-    __device__ void max_len(int tlen) { atomicMax((int *)&R->max_read_len, tlen); }
+    // maxReadLength: every read of a region would hit the same word, so the
+    // atomic is taken only when the read is longer than the value seen
+    __device__ void max_len(int tlen) {
+        if (tlen > *(const volatile int *)&R->max_read_len) atomicMax((int *)&R->max_read_len, tlen);
+    }
 };
 
 // Tile-histogram packing of one (position, base) cell in shared memory,

@@ -937,8 +937,9 @@ struct RegionRealigner {
     }
 
     // The batch's device find35match results for this region's listed clip
-    // pairs (collect_lgins_pairs: per 5' clip its first pair, the 3' clips in
-    // its position window, and each listed 3' clip's consensus length)
+    // pairs (collect_lgins_pairs: per 5' clip its first pair and the 3'
+    // clips of more than 10 characters in its position window, and every 3'
+    // clip's consensus length)
     const int32_t *f35_res = nullptr;            // per pair: b5, b3, score
     std::vector<int64_t> f35_first;              // per t5 entry: its first pair, or -1
     std::vector<std::vector<int>> f35_near;      // per t5 entry: the 3' clips in its window, t3 order
@@ -969,8 +970,24 @@ struct RegionRealigner {
         std::vector<LgT> t5, t3;
         std::vector<std::pair<int, int>> by_pos;
         lgins_lists(t5, t3, by_pos);
+        // every 3' clip's consensus length; the "long" ones (more than 10
+        // characters) by position with their rank in t3.  A 3' clip of 10 or
+        // fewer characters does nothing in realignlgins30's loop: its
+        // consensus is skipped right away, and consensus() marks a clip used
+        // only for more than 12 characters
         std::vector<int32_t> off3(t3.size(), -1);
         f35_len3.assign(t3.size(), -1);
+        std::vector<std::pair<int, int>> long_by_pos;
+        for (const auto &pe : by_pos) {
+            const int ib = pe.second;
+            const string q = peek_consensus(*t3[ib].c);
+            f35_len3[ib] = (int32_t)q.size();
+            if (q.size() > 10) {
+                off3[ib] = (int32_t)strs.size();
+                strs += q;
+                long_by_pos.push_back(pe);
+            }
+        }
         f35_first.assign(t5.size(), -1);
         f35_near.assign(t5.size(), std::vector<int>());
         int64_t k = 0;
@@ -981,8 +998,8 @@ struct RegionRealigner {
             const int p5 = a.pos;
             const int lo3 = (int)std::ceil(p5 - max_rl * 2.5) - 1, hi3 = p5 + max_rl - 10 + 1;
             std::vector<int> &near = f35_near[ia];
-            for (auto it = std::lower_bound(by_pos.begin(), by_pos.end(), std::make_pair(lo3, INT32_MIN));
-                 it != by_pos.end() && it->first <= hi3; ++it)
+            for (auto it = std::lower_bound(long_by_pos.begin(), long_by_pos.end(), std::make_pair(lo3, INT32_MIN));
+                 it != long_by_pos.end() && it->first <= hi3; ++it)
                 near.push_back(it->second);
             std::sort(near.begin(), near.end());
             f35_first[ia] = k;
@@ -992,13 +1009,6 @@ struct RegionRealigner {
                 if (p5 - b.pos > max_rl * 2.5) continue;
                 if (b.pos - p5 > max_rl - 10) continue;
                 if (!(a.cnt / (double)b.cnt >= 0.08 && a.cnt / (double)b.cnt <= 12)) continue;
-                if (f35_len3[ib] < 0) {
-                    const string q = peek_consensus(*t3[ib].c);
-                    off3[ib] = (int32_t)strs.size();
-                    f35_len3[ib] = (int32_t)q.size();
-                    strs += q;
-                }
-                if (f35_len3[ib] <= 10) continue;
                 if (off5 < 0) {
                     off5 = (int32_t)strs.size();
                     strs += seq5;
@@ -1484,7 +1494,9 @@ rv_status host_realign_full(rv_ctx *ctx) {
         try {
             rrs[r].reset(new RegionRealigner(mir, ctx, (int)r));
             rrs[r]->run_first(phase.data() + 8 * r);
+            auto tc = now();
             rrs[r]->collect_lgins_pairs(f35_pairs[r], f35_strs[r]);
+            phase[8 * r + 6] += std::chrono::duration<double, std::milli>(now() - tc).count();
         } catch (const std::exception &e) {
             // the reference's own realigner terminates here (an exception it
             // does not catch); the batch reports it instead
@@ -1512,9 +1524,8 @@ rv_status host_realign_full(rv_ctx *ctx) {
             return RV_ERR_CAPACITY;
         }
         std::vector<int32_t> all_pairs((size_t)np * 4);
-        string all_strs;
-        all_strs.reserve((size_t)str_base[nreg]);
-        for (int r = 0; r < nreg; r++) {
+        string all_strs((size_t)str_base[nreg], '\0');
+        parallel_for(nreg, [&](int64_t r) {
             const std::vector<int32_t> &v = f35_pairs[r];
             int32_t *o = all_pairs.data() + 4 * pair_base[r];
             for (size_t i = 0; i < v.size(); i += 4) {
@@ -1523,12 +1534,13 @@ rv_status host_realign_full(rv_ctx *ctx) {
                 o[i + 2] = v[i + 2] + (int32_t)str_base[r];
                 o[i + 3] = v[i + 3];
             }
-            all_strs += f35_strs[r];
-        }
+            if (!f35_strs[r].empty()) memcpy(&all_strs[(size_t)str_base[r]], f35_strs[r].data(), f35_strs[r].size());
+        });
         f35_res.resize((size_t)np * 3);
         if ((st = device_find35(ctx, all_pairs.data(), np, all_strs, f35_res.data()))) return st;
     }
     const double t_f35 = ms(tf);
+    const double t_dev_done = ms(t0);
     parallel_for(nreg, [&](int64_t r) {
         try {
             RegionRealigner &rr = *rrs[r];
@@ -1560,10 +1572,10 @@ rv_status host_realign_full(rv_ctx *ctx) {
         for (int r = 0; r < nreg; r++)
             for (int k = 0; k < 8; k++) sum[k] += phase[8 * r + k];
         fprintf(stderr, "realign -k 1: listed keys %u, patches %zu, threads %d, find35 pairs %lld; ms: fetch %.2f "
-                "first-half %.2f device-find35 %.2f run %.2f total %.2f; thread-ms: setup %.2f mnp %.2f del %.2f "
-                "ins %.2f lgins %.2f diff %.2f (consensus %.2f)\n",
-                total, all.size(), nt, (long long)np, t_fetch, t_first, t_f35, t_run, ms(t0), sum[0], sum[1], sum[2],
-                sum[3], sum[4], sum[5], sum[6]);
+                "first-half %.2f device-find35 %.2f (done at %.2f) run %.2f total %.2f; thread-ms: setup %.2f mnp %.2f "
+                "del %.2f ins %.2f lgins %.2f diff %.2f collect %.2f\n",
+                total, all.size(), nt, (long long)np, t_fetch, t_first, t_f35, t_dev_done, t_run, ms(t0), sum[0],
+                sum[1], sum[2], sum[3], sum[4], sum[5], sum[6]);
     }
     return st;
 }

@@ -141,3 +141,41 @@ def compare(scores: np.ndarray, y: np.ndarray, hard: np.ndarray) -> dict:
                         "threshold": float(thr)},
             "learned_at_hard_precision": eq_prec,
             "learned_best_f1": best}
+
+
+def shape_samples(seed: int, deep_regions: int = 12, amp_regions: int = 150, pair_len: int = 300_000):
+    """One seed's samples at the shapes of the three calling workloads: a
+    slice of the deep somatic panel (tumor 5000x, low-VAF somatic variants,
+    C>A artifacts at Q20), a slice of the amplicon panel (log-normal depth,
+    PCR duplicates) and the tumor of a 200x/100x somatic pair (strand-biased
+    artifacts, which are not truth).  Yields (genome, truth, reads, regions)."""
+    g, (germ, som), t, _, regions = synth.deep_somatic_panel(seed=seed, n_regions=max(deep_regions, 1),
+                                                            tumor_depth=5000.0, normal_depth=1.0,
+                                                            only=list(range(deep_regions)))
+    yield g, germ + som, synth.unpacked(t), regions
+    ga, va, ra, rega = synth.amplicon_panel_native(seed=seed + 7, n_regions=amp_regions,
+                                                    genome_len=amp_regions * 5000)
+    yield ga, va, synth.unpacked(ra), rega
+    gp, (germp, somp, _art), tp, _np = synth.somatic_pair(seed=seed + 13, length=pair_len)
+    tiles = [(1 + 10_000 * i, 10_000 * (i + 1)) for i in range(pair_len // 10_000)]
+    yield gp, germp + somp, tp, tiles
+
+
+def dataset_shapes(seeds, min_count: int = 2, **kw):
+    """Features, labels and hard-filter flags of every candidate of the
+    shape samples of `seeds` (see shape_samples); also the per-seed slices
+    (start, end) of the arrays."""
+    X, Y, Hd, bounds = [], [], [], []
+    ctx = api.Context(api.default_params(local_realign=0))
+    n = 0
+    for s in seeds:
+        n0 = n
+        for g, truth, rs, regions in shape_samples(s, **kw):
+            f, table = sample_candidates(ctx, g, rs, regions, min_count)
+            X.append(f)
+            Y.append(label(table, truth))
+            Hd.append(np.array([t[3] for t in table], np.float32))
+            n += len(table)
+        bounds.append((n0, n))
+    ctx.close()
+    return np.concatenate(X), np.concatenate(Y), np.concatenate(Hd), bounds
