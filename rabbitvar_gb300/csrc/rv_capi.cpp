@@ -1296,8 +1296,17 @@ namespace {
 // pileup, whose persistent blocks would otherwise hold every SM until they
 // finish; the mirror's copies then overlap the normal's kernels.  On an
 // error nothing stays in flight.
-rv_status pair_launch(rv_ctx *tumor, rv_ctx *normal) {
+rv_status pair_launch(rv_ctx *tumor, rv_ctx *normal, cudaEvent_t after = nullptr) {
     rv_status s;
+    // `after`: the pileups queue behind that event (another pair's pileup),
+    // so the two pairs' persistent tile kernels do not share the SMs
+    if (after) {
+        cudaError_t e = cudaStreamWaitEvent(tumor->stream, after, 0);
+        if (e != cudaSuccess) {
+            tumor->err = std::string("cudaStreamWaitEvent: ") + cudaGetErrorString(e);
+            return RV_ERR_CUDA;
+        }
+    }
     if ((s = pileup_launch(tumor, tumor->stream))) return s;
     if (tumor->params.local_realign) {
         if ((s = mirror_launch(tumor, tumor->ev[11]))) {
@@ -1436,7 +1445,8 @@ rv_status rv_call_somatic_stream(rv_ctx *tumor0, rv_ctx *normal0, rv_ctx *tumor1
             }
             tm.lap("wait_format");
             if (k + 1 < n_jobs) {
-                rv_status l = pair_launch(T[pi ^ 1], N[pi ^ 1]);
+                // behind this job's normal pileup (its end event, ev[1])
+                rv_status l = pair_launch(T[pi ^ 1], N[pi ^ 1], N[pi]->ev[1]);
                 if (l) {
                     bad = pi ^ 1;
                     return l;
