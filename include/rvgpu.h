@@ -260,8 +260,8 @@ rv_status rv_stage_times(const rv_ctx *ctx, double *ms, int n);
 
 /* Batched-region form of CigarParser::process (src/parseCigar.cpp:410-440)
  * under a CUDA graph: with enable != 0, rv_pileup captures its chain of
- * memsets and kernels (table resets, edge detection, the persistent tile
- * kernel fed from the device tile queue, in-order edge walk, deferred
+ * memsets and kernels (table resets, edge detection, the tile kernel fed
+ * from the device tile queue, in-order edge walk, deferred
  * subtraction, list linking, collision check) into a graph and launches that,
  * once the autotuner has settled on a kernel variant.  Each batch's chain is
  * applied to the previous executable graph with cudaGraphExecUpdate; a new

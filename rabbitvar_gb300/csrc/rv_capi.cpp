@@ -56,7 +56,7 @@ unsigned long long next_pow2(unsigned long long x) {
     return p;
 }
 
-enum { CNT_TILE = 0, CNT_DEFER = 1, CNT_USED = 2, CNT_ERR = 3, CNT_CAND = 4, CNT_AUX = 5, CNT_FIX = 6,
+enum { CNT_TILE = 32, CNT_DEFER = 1, CNT_USED = 2, CNT_ERR = 3, CNT_CAND = 4, CNT_AUX = 5, CNT_FIX = 6,
        CNT_WIDE_INS = 7, CNT_WIDE_SCORE = 10 };
 
 // (Re)allocates the hash table and its used-slot list with `cap` slots.
@@ -200,64 +200,75 @@ rv_status device_fisher(rv_ctx *ctx, const int32_t *tables, int64_t n, double *p
 
 namespace {
 
-rv_status run_wide(rv_ctx *ctx, int list, unsigned int n, cudaStream_t s);
+// counter words copied back after a scoring kernel
+constexpr int kHdrWords = 12;
+constexpr unsigned int kScoreRetryBits = ERR_CAND_FULL | ERR_WIDE_INS_SCRATCH | ERR_WIDE_SCORE_SCRATCH;
 
-// Scores the listed (region, position) pairs of `ctx` without screens and
-// appends their CandVars to the host copy.
-rv_status score_list(rv_ctx *ctx, const std::vector<int2> &list) {
-    if (list.empty()) return RV_OK;
-    if (list.size() > ctx->cap_list || !ctx->d_list) {
-        if (ctx->d_list) cudaFree(ctx->d_list);
-        ctx->d_list = nullptr;
-        size_t cap = std::max<size_t>(list.size() + list.size() / 4, 4096);
-        RV_CUDA(cudaMalloc((void **)&ctx->d_list, cap * sizeof(int2)));
-        ctx->cap_list = cap;
-    }
-    cudaStream_t s = ctx->stream;
-    RV_CUDA(cudaMemcpyAsync(ctx->d_list, list.data(), list.size() * sizeof(int2), cudaMemcpyHostToDevice, s));
-    RV_CUDA(cudaMemsetAsync(ctx->d_counters + CNT_WIDE_SCORE, 0, 4, s));
+int64_t *wide_off(rv_ctx *ctx, int list) { return ctx->d_wide_off + (size_t)list * ((size_t)ctx->wide_cap + 1); }
+
+int64_t wide_entries(const rv_ctx *ctx) {
+    return ctx->d_wide_scratch ? (int64_t)(ctx->cap_wide_scratch / wide_entry_bytes()) : 0;
+}
+
+// The wide pass of one list (k_ins_adjust_wide for list 0, k_score_wide for
+// list 1), queued on s behind the kernel that fills the list: the scratch
+// offsets from the positions' allele counts (k_wide_offsets), then the
+// kernel.  Nothing is read back; a pass whose scratch is too small sets its
+// error bit and is run again by the caller after grow_wide_scratch.
+void queue_wide(rv_ctx *ctx, int list, const DevParams &dp, cudaStream_t s) {
     DevState st = ctx->state();
-    launch_score_list(st, ctx->dp, ctx->d_list, (int)list.size(), s);
-    RV_CUDA(cudaGetLastError());
-    unsigned int hdr[12];
-    RV_CUDA(cudaMemcpyAsync(hdr, ctx->d_counters, sizeof hdr, cudaMemcpyDeviceToHost, s));
+    launch_wide_offsets(st, list, wide_off(ctx, list), s);
+    if (list == 0) launch_ins_adjust_wide(st, wide_off(ctx, 0), ctx->d_wide_scratch, wide_entries(ctx), s);
+    else launch_score_wide(st, dp, wide_off(ctx, 1), ctx->d_wide_scratch, wide_entries(ctx), s);
+    ctx->kernels += 2;
+}
+
+// Grows the wide scratch to the larger of the two lists' totals (their
+// offsets' last entries, from the passes that overflowed), with headroom.
+rv_status grow_wide_scratch(rv_ctx *ctx, cudaStream_t s) {
+    unsigned int n[2];
+    RV_CUDA(cudaMemcpyAsync(&n[0], ctx->d_counters + CNT_WIDE_INS, 4, cudaMemcpyDeviceToHost, s));
+    RV_CUDA(cudaMemcpyAsync(&n[1], ctx->d_counters + CNT_WIDE_SCORE, 4, cudaMemcpyDeviceToHost, s));
     RV_CUDA(cudaStreamSynchronize(s));
-    if (hdr[CNT_WIDE_SCORE] && !(hdr[CNT_ERR] & ERR_CAND_FULL)) {
-        rv_status ws = run_wide(ctx, 1, hdr[CNT_WIDE_SCORE], s);
-        if (ws) return ws;
-        RV_CUDA(cudaMemcpyAsync(hdr, ctx->d_counters, sizeof hdr, cudaMemcpyDeviceToHost, s));
+    int64_t need = 0;
+    for (int l = 0; l < 2; l++) {
+        int64_t t = 0;
+        const unsigned int k = std::min(n[l], ctx->wide_cap);
+        RV_CUDA(cudaMemcpyAsync(&t, wide_off(ctx, l) + k, 8, cudaMemcpyDeviceToHost, s));
         RV_CUDA(cudaStreamSynchronize(s));
+        need = std::max(need, t);
     }
-    unsigned int n0 = (unsigned int)ctx->h_cand.size(), n = hdr[CNT_CAND];
-    if (hdr[CNT_ERR] & ERR_CAND_FULL) {
-        // grow the buffer to the count reached and score the list again (the
-        // candidates before n0 are already on the host)
-        const unsigned long long need = n;
-        cudaFree(ctx->d_cand);
-        ctx->d_cand = nullptr;
-        ctx->cand_cap = 0;
-        const unsigned int cap = (unsigned int)std::min<unsigned long long>(INT32_MAX, need + need / 4 + 65536);
-        RV_CUDA(cudaMalloc((void **)&ctx->d_cand, (size_t)cap * sizeof(CandVar)));
-        ctx->cand_cap = cap;
-        RV_CUDA(cudaMemcpyAsync(ctx->d_counters + CNT_CAND, &n0, 4, cudaMemcpyHostToDevice, s));
-        RV_CUDA(cudaMemsetAsync(ctx->d_counters + CNT_WIDE_SCORE, 0, 4, s));
-        st = ctx->state();
-        launch_clear_err_bits(st, ~ERR_CAND_FULL, s);
-        launch_score_list(st, ctx->dp, ctx->d_list, (int)list.size(), s);
-        RV_CUDA(cudaGetLastError());
-        RV_CUDA(cudaMemcpyAsync(hdr, ctx->d_counters, sizeof hdr, cudaMemcpyDeviceToHost, s));
-        RV_CUDA(cudaStreamSynchronize(s));
-        if (hdr[CNT_WIDE_SCORE]) {
-            rv_status ws = run_wide(ctx, 1, hdr[CNT_WIDE_SCORE], s);
-            if (ws) return ws;
-            RV_CUDA(cudaMemcpyAsync(hdr, ctx->d_counters, sizeof hdr, cudaMemcpyDeviceToHost, s));
-            RV_CUDA(cudaStreamSynchronize(s));
-        }
-        n = hdr[CNT_CAND];
-        ctx->kernels += 2;
+    const size_t bytes = (size_t)need * wide_entry_bytes();
+    if (bytes > ctx->cap_wide_scratch || !ctx->d_wide_scratch) {
+        if (ctx->d_wide_scratch) cudaFree(ctx->d_wide_scratch);
+        ctx->d_wide_scratch = nullptr;
+        ctx->cap_wide_scratch = 0;
+        const size_t cap = std::max<size_t>(bytes + bytes / 2, 65536 * wide_entry_bytes());
+        RV_CUDA(cudaMalloc(&ctx->d_wide_scratch, cap));
+        ctx->cap_wide_scratch = cap;
     }
+    return RV_OK;
+}
+
+// Grows the candidate buffer to `need` entries with headroom.
+rv_status grow_cand(rv_ctx *ctx, unsigned long long need) {
+    if (ctx->d_cand) cudaFree(ctx->d_cand);
+    ctx->d_cand = nullptr;
+    ctx->cand_cap = 0;
+    const unsigned int cap = (unsigned int)std::min<unsigned long long>(INT32_MAX, need + need / 4 + 65536);
+    RV_CUDA(cudaMalloc((void **)&ctx->d_cand, (size_t)cap * sizeof(CandVar)));
+    ctx->cand_cap = cap;
+    return RV_OK;
+}
+
+// The error bits every score step checks last.
+rv_status score_errors(rv_ctx *ctx, const unsigned int *hdr, unsigned int n) {
     if (n > ctx->cand_cap || (hdr[CNT_ERR] & ERR_CAND_FULL)) {
         ctx->err = "candidate buffer overflow";
+        return RV_ERR_CAPACITY;
+    }
+    if (hdr[CNT_ERR] & (ERR_WIDE_INS_SCRATCH | ERR_WIDE_SCORE_SCRATCH)) {
+        ctx->err = "wide scratch still too small after regrowth";
         return RV_ERR_CAPACITY;
     }
     if (hdr[CNT_ERR] & ERR_WIDE_FULL) {
@@ -270,56 +281,70 @@ rv_status score_list(rv_ctx *ctx, const std::vector<int2> &list) {
         ctx->err = buf;
         return RV_ERR_UNSUPPORTED;
     }
-    ctx->h_cand.resize(n);
-    if (n > n0)
-        RV_CUDA(cudaMemcpy(ctx->h_cand.data() + n0, ctx->d_cand + n0, (size_t)(n - n0) * sizeof(CandVar),
-                           cudaMemcpyDeviceToHost));
-    ctx->io_h2d += (int64_t)(list.size() * sizeof(int2));
-    ctx->io_d2h += (int64_t)sizeof hdr + (int64_t)(n - n0) * (int64_t)sizeof(CandVar);
-    ctx->kernels += 1;
     return RV_OK;
 }
 
-// The wide pass of one list (k_ins_adjust_wide for list 0, k_score_wide for
-// list 1): the queued positions' scratch offsets from their allele counts,
-// scratch grown to the total, then the kernel on stream s (not waited for).
-rv_status run_wide(rv_ctx *ctx, int list, unsigned int n, cudaStream_t s) {
-    if (n == 0) return RV_OK;
-    if (n > ctx->wide_cap) {
-        ctx->err = "more positions with many alleles than the wide list holds";
-        return RV_ERR_CAPACITY;
+// Scores the listed (region, position) pairs of `ctx` without screens and
+// appends their CandVars to the host copy.
+// score_list_a queues the kernel, its wide pass and the counters' copy to
+// the pinned words; score_list_b waits for them and collects (two contexts'
+// lists are queued before either is waited for).
+rv_status score_list_a(rv_ctx *ctx, const std::vector<int2> &list) {
+    if (list.empty()) return RV_OK;
+    if (list.size() > ctx->cap_list || !ctx->d_list) {
+        if (ctx->d_list) cudaFree(ctx->d_list);
+        ctx->d_list = nullptr;
+        size_t cap = std::max<size_t>(list.size() + list.size() / 4, 4096);
+        RV_CUDA(cudaMalloc((void **)&ctx->d_list, cap * sizeof(int2)));
+        ctx->cap_list = cap;
     }
-    std::vector<WidePos> w(n);
-    RV_CUDA(cudaMemcpyAsync(w.data(), ctx->d_wide + (size_t)list * ctx->wide_cap, n * sizeof(WidePos),
-                            cudaMemcpyDeviceToHost, s));
-    RV_CUDA(cudaStreamSynchronize(s));
-    std::vector<int64_t> off(n + 1, 0);
-    for (unsigned int i = 0; i < n; i++) off[i + 1] = off[i] + std::max(1, w[i].need) + 8;
-    const int64_t total = off[n];
-    if (ctx->cap_wide_off < n + 1 || !ctx->d_wide_off) {
-        if (ctx->d_wide_off) cudaFree(ctx->d_wide_off);
-        ctx->d_wide_off = nullptr;
-        ctx->cap_wide_off = 0;
-        RV_CUDA(cudaMalloc((void **)&ctx->d_wide_off, (n + 1) * sizeof(int64_t) * 2));
-        ctx->cap_wide_off = (n + 1) * 2;
-    }
-    const size_t bytes = (size_t)total * wide_entry_bytes();
-    if (ctx->cap_wide_scratch < bytes || !ctx->d_wide_scratch) {
-        if (ctx->d_wide_scratch) cudaFree(ctx->d_wide_scratch);
-        ctx->d_wide_scratch = nullptr;
-        ctx->cap_wide_scratch = 0;
-        RV_CUDA(cudaMalloc(&ctx->d_wide_scratch, bytes + bytes / 2));
-        ctx->cap_wide_scratch = bytes + bytes / 2;
-    }
-    // (a pageable copy: staged before the call returns, so `off` may go)
-    RV_CUDA(cudaMemcpy(ctx->d_wide_off, off.data(), (n + 1) * sizeof(int64_t), cudaMemcpyHostToDevice));
-    DevState st = ctx->state();
-    if (list == 0) launch_ins_adjust_wide(st, ctx->d_wide_off, ctx->d_wide_scratch, total, s);
-    else launch_score_wide(st, ctx->dp, ctx->d_wide_off, ctx->d_wide_scratch, total, s);
+    cudaStream_t s = ctx->stream;
+    RV_CUDA(cudaMemcpyAsync(ctx->d_list, list.data(), list.size() * sizeof(int2), cudaMemcpyHostToDevice, s));
+    RV_CUDA(cudaMemsetAsync(ctx->d_counters + CNT_WIDE_SCORE, 0, 4, s));
+    launch_score_list(ctx->state(), ctx->dp, ctx->d_list, (int)list.size(), s);
+    queue_wide(ctx, 1, ctx->dp, s);
     RV_CUDA(cudaGetLastError());
+    RV_CUDA(cudaMemcpyAsync(ctx->h_cnt, ctx->d_counters, kHdrWords * 4, cudaMemcpyDeviceToHost, s));
+    return RV_OK;
+}
+
+rv_status score_list_b(rv_ctx *ctx, const std::vector<int2> &list) {
+    if (list.empty()) return RV_OK;
+    cudaStream_t s = ctx->stream;
+    RV_CUDA(cudaStreamSynchronize(s));
+    unsigned int hdr[kHdrWords];
+    std::memcpy(hdr, ctx->h_cnt, sizeof hdr);
+    const unsigned int n0 = (unsigned int)ctx->h_cand.size();
+    // a full candidate buffer or too little wide scratch: grow what
+    // overflowed and score the list again (the candidates before n0 are
+    // already on the host)
+    for (int attempt = 0; attempt < 3 && (hdr[CNT_ERR] & kScoreRetryBits); attempt++) {
+        rv_status g;
+        if ((hdr[CNT_ERR] & ERR_CAND_FULL) && (g = grow_cand(ctx, hdr[CNT_CAND]))) return g;
+        if ((hdr[CNT_ERR] & ERR_WIDE_SCORE_SCRATCH) && (g = grow_wide_scratch(ctx, s))) return g;
+        RV_CUDA(cudaMemcpyAsync(ctx->d_counters + CNT_CAND, &n0, 4, cudaMemcpyHostToDevice, s));
+        RV_CUDA(cudaMemsetAsync(ctx->d_counters + CNT_WIDE_SCORE, 0, 4, s));
+        DevState st = ctx->state();
+        launch_clear_err_bits(st, ~kScoreRetryBits, s);
+        launch_score_list(st, ctx->dp, ctx->d_list, (int)list.size(), s);
+        queue_wide(ctx, 1, ctx->dp, s);
+        RV_CUDA(cudaGetLastError());
+        RV_CUDA(cudaMemcpyAsync(hdr, ctx->d_counters, sizeof hdr, cudaMemcpyDeviceToHost, s));
+        RV_CUDA(cudaStreamSynchronize(s));
+        ctx->kernels += 2;
+    }
+    const unsigned int n = hdr[CNT_CAND];
+    rv_status e = score_errors(ctx, hdr, n);
+    if (e) return e;
+    ctx->h_cand.resize(n);
+    if (n > n0) {
+        RV_CUDA(cudaMemcpyAsync(ctx->h_cand.data() + n0, ctx->d_cand + n0, (size_t)(n - n0) * sizeof(CandVar),
+                                cudaMemcpyDeviceToHost, s));
+        RV_CUDA(cudaStreamSynchronize(s));
+    }
+    ctx->io_h2d += (int64_t)(list.size() * sizeof(int2));
+    ctx->io_d2h += (int64_t)sizeof hdr + (int64_t)(n - n0) * (int64_t)sizeof(CandVar);
     ctx->kernels += 1;
-    ctx->io_d2h += (int64_t)(n * sizeof(WidePos));
-    ctx->io_h2d += (int64_t)((n + 1) * sizeof(int64_t));
     return RV_OK;
 }
 
@@ -383,7 +408,14 @@ rv_status rv_create(rv_ctx **out, const rv_params *p, int device, size_t hbm_bud
     ctx->params = *p;
     ctx->budget = hbm_budget;
     cudaError_t e = cudaSetDevice(device);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    // the context's stream runs at the highest priority; only the tile
+    // kernel is launched at the lowest (launch_pileup), so a realigner pass
+    // or a scoring kernel queued while another batch's tile kernel runs takes
+    // the block slots that kernel's retiring blocks free
+    int least = 0, greatest = 0;
+    if (e == cudaSuccess) e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+    ctx->low_priority = least;
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&ctx->stream, cudaStreamNonBlocking, greatest);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
     for (int i = 0; e == cudaSuccess && i < 12; i++) e = cudaEventCreate(&ctx->ev[i]);
     // a blocking-wait event for waits off the critical path (the record
@@ -391,6 +423,7 @@ rv_status rv_create(rv_ctx **out, const rv_params *p, int device, size_t hbm_bud
     // on a core the host pool needs
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_block, cudaEventBlockingSync | cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc((void **)&ctx->d_counters, 64 * sizeof(unsigned int));
+    if (e == cudaSuccess) e = cudaHostAlloc((void **)&ctx->h_cnt, 64 * sizeof(unsigned int), cudaHostAllocDefault);
     if (e == cudaSuccess) e = cudaMalloc((void **)&ctx->d_logfact, (size_t)kLogFact * sizeof(double));
     if (e == cudaSuccess) {
         launch_fill_logfact(ctx->d_logfact, ctx->stream);
@@ -455,6 +488,7 @@ void rv_destroy(rv_ctx *ctx) {
     if (ctx->h_mirror) cudaFreeHost(ctx->h_mirror);
     if (ctx->h_mirror_slots) cudaFreeHost(ctx->h_mirror_slots);
     if (ctx->h_fstage) cudaFreeHost(ctx->h_fstage);
+    if (ctx->h_cnt) cudaFreeHost(ctx->h_cnt);
     for (int i = 0; i < 12; i++)
         if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
     if (ctx->ev_block) cudaEventDestroy(ctx->ev_block);
@@ -798,6 +832,12 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
         ctx->wide_cap = 0;
         RV_CUDA(cudaMalloc((void **)&ctx->d_wide, 2 * (size_t)want_wide * sizeof(WidePos)));
         ctx->wide_cap = want_wide;
+        // the two lists' scratch offsets (k_wide_offsets)
+        if (ctx->d_wide_off) cudaFree(ctx->d_wide_off);
+        ctx->d_wide_off = nullptr;
+        ctx->cap_wide_off = 0;
+        RV_CUDA(cudaMalloc((void **)&ctx->d_wide_off, 2 * ((size_t)want_wide + 1) * sizeof(int64_t)));
+        ctx->cap_wide_off = 2 * ((size_t)want_wide + 1);
     }
     // candidates: a few per candidate position; pileup mode scores every position
     const int64_t cand_est = ctx->dp.do_pileup ? 2 * score + 65536 : score / 4 + 1024;
@@ -838,7 +878,7 @@ namespace {
 
 // The memsets and kernels of one pileup, queued on s; `marks` records the
 // per-stage events (left out when the chain is captured into a graph).
-rv_status queue_pileup_chain(rv_ctx *ctx, cudaStream_t s, int grid, int variant, bool marks) {
+rv_status queue_pileup_chain(rv_ctx *ctx, cudaStream_t s, int resident, int variant, bool marks) {
     size_t cap = ctx->cap_cells;
     RV_CUDA(cudaMemsetAsync(ctx->d_cellmem, 0, cap * (8 * 16 + 4 + 1), s));
     RV_CUDA(cudaMemsetAsync(ctx->d_head, 0xFF, cap * 8, s));
@@ -854,7 +894,7 @@ rv_status queue_pileup_chain(rv_ctx *ctx, cudaStream_t s, int grid, int variant,
     launch_region_reset(st, s);
     launch_edge_detect(st, ctx->dp, s);
     if (marks) RV_CUDA(cudaEventRecord(ctx->ev[5], s));
-    RV_CUDA(launch_pileup(st, ctx->dp, grid, s, variant));
+    RV_CUDA(launch_pileup(st, ctx->dp, resident, s, variant, ctx->low_priority));
     if (marks) RV_CUDA(cudaEventRecord(ctx->ev[6], s));
     launch_serial(st, ctx->dp, s);
     if (marks) RV_CUDA(cudaEventRecord(ctx->ev[7], s));
@@ -870,10 +910,10 @@ rv_status queue_pileup_chain(rv_ctx *ctx, cudaStream_t s, int grid, int variant,
 // applied to the graph of the previous batch by cudaGraphExecUpdate (kernel
 // arguments, grids and memset sizes may change between batches), instantiated
 // again when the update is refused, then launched on s.
-rv_status launch_pileup_graph(rv_ctx *ctx, cudaStream_t s, int grid, int variant) {
+rv_status launch_pileup_graph(rv_ctx *ctx, cudaStream_t s, int resident, int variant) {
     cudaGraph_t g = nullptr;
     RV_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
-    rv_status st = queue_pileup_chain(ctx, s, grid, variant, false);
+    rv_status st = queue_pileup_chain(ctx, s, resident, variant, false);
     cudaError_t e = cudaStreamEndCapture(s, &g);
     if (st != RV_OK) {
         if (g) cudaGraphDestroy(g);
@@ -917,7 +957,8 @@ rv_status pileup_launch(rv_ctx *ctx, cudaStream_t s) {
     int variant;
     const char *pin = getenv("RV_PILEUP_VARIANT");
     const bool pinned = pin && *pin;
-    auto grid_of = [&](int v) {
+    // blocks of the variant resident at once (sets the tile kernel's per-block quota)
+    auto resident_of = [&](int v) {
         const int per_sm = std::max(1, pileup_blocks_per_sm(v));
         return std::max(1, std::min<int>((int)ctx->tiles.size(), per_sm * ctx->sm_count));
     };
@@ -926,7 +967,7 @@ rv_status pileup_launch(rv_ctx *ctx, cudaStream_t s) {
     } else {
         if (ctx->variant_runs < nvar && !ctx->tiles.empty()) {
             for (int v = 0; v < nvar; v++) {
-                rv_status ts = queue_pileup_chain(ctx, s, grid_of(v), v, true);
+                rv_status ts = queue_pileup_chain(ctx, s, resident_of(v), v, true);
                 if (ts != RV_OK) return ts;
                 RV_CUDA(cudaStreamSynchronize(s));
                 float m = 0;
@@ -940,12 +981,12 @@ rv_status pileup_launch(rv_ctx *ctx, cudaStream_t s) {
             if (ctx->variant_ms[v] < ctx->variant_ms[variant]) variant = v;
     }
     ctx->variant = variant;
-    const int grid = grid_of(variant);
+    const int resident = resident_of(variant);
     // the legacy default stream cannot be captured
     const bool graphed = ctx->use_graph && s != nullptr;
     RV_CUDA(cudaEventRecord(ctx->ev[0], s));
-    rv_status qs = graphed ? launch_pileup_graph(ctx, s, grid, variant)
-                           : queue_pileup_chain(ctx, s, grid, variant, true);
+    rv_status qs = graphed ? launch_pileup_graph(ctx, s, resident, variant)
+                           : queue_pileup_chain(ctx, s, resident, variant, true);
     if (qs != RV_OK) return qs;
     RV_CUDA(cudaEventRecord(ctx->ev[1], s));
     ctx->pileup_graphed = graphed;
@@ -1061,67 +1102,61 @@ rv_status rv_realign(rv_ctx *ctx, void *stream) {
     return RV_OK;
 }
 
-static rv_status score_impl(rv_ctx *ctx, void *stream, const DevParams &dp) {
-    if (!ctx) return RV_ERR_ARG;
+// The score stage in two steps, so that the two samples of a pair queue
+// their kernels together and share one wait (while another batch's tile
+// kernel holds the SMs, a wait lasts until one of its chunks ends).
+// score_a queues everything: counters, the insertion adjustments and their
+// wide pass, the score kernel and its wide pass, and the counter words'
+// copy to the context's pinned words.
+static rv_status score_a(rv_ctx *ctx, cudaStream_t s, const DevParams &dp) {
     if (ctx->stage < 2) { ctx->err = "rv_score before rv_pileup"; return RV_ERR_STATE; }
     if (ctx->stage >= 4) { ctx->err = "this batch was already scored (submit it again)"; return RV_ERR_STATE; }
     RV_CUDA(cudaSetDevice(ctx->device));
-    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
     DevState st = ctx->state();
     RV_CUDA(cudaEventRecord(ctx->ev[2], s));
     RV_CUDA(cudaMemsetAsync(ctx->d_counters + CNT_CAND, 0, 4, s));
     RV_CUDA(cudaMemsetAsync(ctx->d_counters + CNT_WIDE_INS, 0, 4, s));
     RV_CUDA(cudaMemsetAsync(ctx->d_counters + CNT_WIDE_SCORE, 0, 4, s));
     launch_ins_adjust(st, s);
-    {
-        // positions with more insertion keys than the kernel's arrays: their
-        // adjustments must land before any position is scored
-        unsigned int nw = 0;
-        RV_CUDA(cudaMemcpyAsync(&nw, ctx->d_counters + CNT_WIDE_INS, 4, cudaMemcpyDeviceToHost, s));
-        RV_CUDA(cudaStreamSynchronize(s));
-        rv_status ws = run_wide(ctx, 0, nw, s);
-        if (ws) return ws;
-    }
+    // positions with more insertion keys than the kernel's arrays: their
+    // adjustments land before any position is scored
+    queue_wide(ctx, 0, dp, s);
     RV_CUDA(cudaEventRecord(ctx->ev[8], s));
     launch_score(st, dp, s);
+    queue_wide(ctx, 1, dp, s);
     RV_CUDA(cudaGetLastError());
-    unsigned int hdr[12];
-    RV_CUDA(cudaMemcpyAsync(hdr, ctx->d_counters, sizeof hdr, cudaMemcpyDeviceToHost, s));
-    RV_CUDA(cudaStreamSynchronize(s));
-    if (hdr[CNT_WIDE_SCORE] && !(hdr[CNT_ERR] & ERR_CAND_FULL)) {
-        rv_status ws = run_wide(ctx, 1, hdr[CNT_WIDE_SCORE], s);
-        if (ws) return ws;
-        RV_CUDA(cudaMemcpyAsync(hdr, ctx->d_counters, sizeof hdr, cudaMemcpyDeviceToHost, s));
-        RV_CUDA(cudaStreamSynchronize(s));
-    }
     RV_CUDA(cudaEventRecord(ctx->ev[3], s));
-    if (hdr[CNT_ERR] & ERR_CAND_FULL) {
-        // more scored alleles than the buffer holds: grow it to the count
-        // the run reached and score again (the kernel only reads the maps)
-        const unsigned long long need = hdr[CNT_CAND];
-        if (ctx->d_cand) cudaFree(ctx->d_cand);
-        ctx->d_cand = nullptr;
-        ctx->cand_cap = 0;
-        const unsigned int cap = (unsigned int)std::min<unsigned long long>(INT32_MAX, need + need / 4 + 65536);
-        RV_CUDA(cudaMalloc((void **)&ctx->d_cand, (size_t)cap * sizeof(CandVar)));
-        ctx->cand_cap = cap;
-        st = ctx->state();
+    RV_CUDA(cudaMemcpyAsync(ctx->h_cnt, ctx->d_counters, kHdrWords * 4, cudaMemcpyDeviceToHost, s));
+    ctx->kernels += 2;
+    return RV_OK;
+}
+
+// score_c, after score_a's copy has landed: what overflowed (the candidate
+// buffer, the wide scratch) is grown and scored again, then the error bits
+// and the candidates to the host.
+static rv_status score_c(rv_ctx *ctx, cudaStream_t s, const DevParams &dp) {
+    unsigned int hdr[kHdrWords];
+    std::memcpy(hdr, ctx->h_cnt, sizeof hdr);
+    for (int attempt = 0; attempt < 3 && (hdr[CNT_ERR] & kScoreRetryBits); attempt++) {
+        rv_status g;
+        if ((hdr[CNT_ERR] & ERR_CAND_FULL) && (g = grow_cand(ctx, hdr[CNT_CAND]))) return g;
+        if ((hdr[CNT_ERR] & (ERR_WIDE_INS_SCRATCH | ERR_WIDE_SCORE_SCRATCH)) && (g = grow_wide_scratch(ctx, s)))
+            return g;
+        DevState st = ctx->state();
+        // the insertion pass that did nothing runs now (its offsets stand);
+        // the score kernel only reads the maps, so it runs again whole
+        if (hdr[CNT_ERR] & ERR_WIDE_INS_SCRATCH)
+            launch_ins_adjust_wide(st, wide_off(ctx, 0), ctx->d_wide_scratch, wide_entries(ctx), s);
         RV_CUDA(cudaMemsetAsync(ctx->d_counters + CNT_CAND, 0, 4, s));
         RV_CUDA(cudaMemsetAsync(ctx->d_counters + CNT_WIDE_SCORE, 0, 4, s));
-        launch_clear_err_bits(st, ~ERR_CAND_FULL, s);
+        launch_clear_err_bits(st, ~kScoreRetryBits, s);
         launch_score(st, dp, s);
+        queue_wide(ctx, 1, dp, s);
         RV_CUDA(cudaGetLastError());
+        RV_CUDA(cudaEventRecord(ctx->ev[3], s));
         RV_CUDA(cudaMemcpyAsync(hdr, ctx->d_counters, sizeof hdr, cudaMemcpyDeviceToHost, s));
         RV_CUDA(cudaStreamSynchronize(s));
-        if (hdr[CNT_WIDE_SCORE]) {
-            rv_status ws = run_wide(ctx, 1, hdr[CNT_WIDE_SCORE], s);
-            if (ws) return ws;
-            RV_CUDA(cudaMemcpyAsync(hdr, ctx->d_counters, sizeof hdr, cudaMemcpyDeviceToHost, s));
-            RV_CUDA(cudaStreamSynchronize(s));
-        }
-        RV_CUDA(cudaEventRecord(ctx->ev[3], s));
-        RV_CUDA(cudaStreamSynchronize(s));
-        ctx->kernels += 2;
+        ctx->kernels += 3;
     }
     float ms = 0;
     cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]);
@@ -1130,32 +1165,34 @@ static rv_status score_impl(rv_ctx *ctx, void *stream, const DevParams &dp) {
     ctx->stage_ms[5] = ms;
     cudaEventElapsedTime(&ms, ctx->ev[8], ctx->ev[3]);
     ctx->stage_ms[6] = ms;
-    ctx->kernels += 2;
-    unsigned int n = hdr[CNT_CAND];
-    if (n > ctx->cand_cap || (hdr[CNT_ERR] & ERR_CAND_FULL)) {
-        ctx->err = "candidate buffer overflow";
-        return RV_ERR_CAPACITY;
-    }
-    if (hdr[CNT_ERR] & ERR_WIDE_FULL) {
-        ctx->err = "more positions with many alleles than the wide list holds";
-        return RV_ERR_CAPACITY;
-    }
-    if (hdr[CNT_ERR] & (ERR_UNSUPPORTED | ERR_CELL_RANGE)) {
-        char buf[96];
-        snprintf(buf, sizeof buf, "score device error bits 0x%x", hdr[CNT_ERR]);
-        ctx->err = buf;
-        return RV_ERR_UNSUPPORTED;
-    }
+    const unsigned int n = hdr[CNT_CAND];
+    rv_status e = score_errors(ctx, hdr, n);
+    if (e) return e;
+    // (copies on the context's stream: a legacy-stream copy was measured to
+    // wait for another batch's pileup queued on the other streams)
     ctx->h_cand.resize(n);
-    if (n) RV_CUDA(cudaMemcpy(ctx->h_cand.data(), ctx->d_cand, (size_t)n * sizeof(CandVar), cudaMemcpyDeviceToHost));
+    if (n)
+        RV_CUDA(cudaMemcpyAsync(ctx->h_cand.data(), ctx->d_cand, (size_t)n * sizeof(CandVar), cudaMemcpyDeviceToHost,
+                                s));
     unsigned long long used = 0;
-    RV_CUDA(cudaMemcpy(&used, ctx->d_counters + 8, 8, cudaMemcpyDeviceToHost));
+    RV_CUDA(cudaMemcpyAsync(&used, ctx->d_counters + 8, 8, cudaMemcpyDeviceToHost, s));
+    RV_CUDA(cudaStreamSynchronize(s));
     used = std::min<unsigned long long>(used, ctx->arena_cap);
     ctx->h_arena.resize(used);
-    if (used) RV_CUDA(cudaMemcpy(ctx->h_arena.data(), ctx->d_arena, used, cudaMemcpyDeviceToHost));
+    if (used) RV_CUDA(cudaMemcpyAsync(ctx->h_arena.data(), ctx->d_arena, used, cudaMemcpyDeviceToHost, s));
+    RV_CUDA(cudaStreamSynchronize(s));
     ctx->io_d2h += (int64_t)sizeof hdr + (int64_t)n * (int64_t)sizeof(CandVar) + 8 + (int64_t)used;
     ctx->stage = 4;
     return RV_OK;
+}
+
+static rv_status score_impl(rv_ctx *ctx, void *stream, const DevParams &dp) {
+    if (!ctx) return RV_ERR_ARG;
+    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+    rv_status st;
+    if ((st = score_a(ctx, s, dp))) return st;
+    RV_CUDA(cudaStreamSynchronize(s));
+    return score_c(ctx, s, dp);
 }
 
 rv_status rv_score(rv_ctx *ctx, void *stream) {
@@ -1277,14 +1314,40 @@ rv_status rv_score_pair(rv_ctx *tumor, rv_ctx *normal) {
     }
     rv_status s;
     PhaseTimer tm("score_pair");
-    if ((s = rv_score(tumor, nullptr))) return s;
-    if ((s = rv_score(normal, nullptr))) { tumor->err = normal->err; return s; }
-    tm.lap("score");
+    // each step is queued for both samples before either is waited for
+    rv_ctx *both[2] = {tumor, normal};
+    auto each = [&](const std::function<rv_status(rv_ctx *)> &f) -> rv_status {
+        for (rv_ctx *c : both) {
+            rv_status r = f(c);
+            if (r) {
+                if (c != tumor) tumor->err = c->err;
+                return r;
+            }
+        }
+        return (rv_status)RV_OK;
+    };
+    auto wait = [&](rv_ctx *c) -> rv_status {
+        cudaError_t e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) { c->err = std::string("cudaStreamSynchronize: ") + cudaGetErrorString(e); return RV_ERR_CUDA; }
+        return (rv_status)RV_OK;
+    };
+    tumor->dp.dataset_min = normal->dp.dataset_min = 0;
+    if ((s = each([](rv_ctx *c) { return score_a(c, c->stream, c->dp); }))) return s;
+    tm.lap("queue");
+    if ((s = wait(tumor))) return s;
+    tm.lap("wait_tumor");
+    if ((s = wait(normal))) { tumor->err = normal->err; return s; }
+    tm.lap("wait_normal");
+    if ((s = each([](rv_ctx *c) { return score_c(c, c->stream, c->dp); }))) return s;
+    tm.lap("collect");
     // every position where one sample has a candidate is needed in both
     std::vector<int2> pt = positions_of(tumor), pn = positions_of(normal);
     tm.lap("positions");
-    if ((s = score_list(tumor, missing(pn, pt)))) return s;
-    if ((s = score_list(normal, missing(pt, pn)))) { tumor->err = normal->err; return s; }
+    const std::vector<int2> lt = missing(pn, pt), ln = missing(pt, pn);
+    if ((s = score_list_a(tumor, lt))) return s;
+    if ((s = score_list_a(normal, ln))) { tumor->err = normal->err; return s; }
+    if ((s = score_list_b(tumor, lt))) return s;
+    if ((s = score_list_b(normal, ln))) { tumor->err = normal->err; return s; }
     tm.lap("score_list");
     return RV_OK;
 }
@@ -1293,13 +1356,13 @@ namespace {
 
 // Queues both samples' pileups (and, with -k 1, their realigner mirrors)
 // without waiting.  The tumor's mirror kernels go before the normal's
-// pileup, whose persistent blocks would otherwise hold every SM until they
-// finish; the mirror's copies then overlap the normal's kernels.  On an
-// error nothing stays in flight.
+// pileup, so the tumor's realigner can start as soon as they end; the
+// mirror's copies then overlap the normal's kernels.  On an error nothing
+// stays in flight.
 rv_status pair_launch(rv_ctx *tumor, rv_ctx *normal, cudaEvent_t after = nullptr) {
     rv_status s;
     // `after`: the pileups queue behind that event (another pair's pileup),
-    // so the two pairs' persistent tile kernels do not share the SMs
+    // so the two pairs' tile kernels do not share the SMs
     if (after) {
         cudaError_t e = cudaStreamWaitEvent(tumor->stream, after, 0);
         if (e != cudaSuccess) {

@@ -17,7 +17,9 @@ void launch_init_slots(Slot *slots, unsigned long long n, cudaStream_t s);
 void launch_clear_used(Slot *slots, const uint32_t *used, const unsigned int *n_used, unsigned long long cap,
                        cudaStream_t s);
 void launch_region_reset(const DevState &st, cudaStream_t s);
-cudaError_t launch_pileup(const DevState &st, const DevParams &P, int grid, cudaStream_t s, int variant);
+cudaError_t launch_pileup(const DevState &st, const DevParams &P, int resident_blocks, cudaStream_t s, int variant,
+                          int priority);
+int tile_quota(int64_t n_tiles, int resident_blocks);
 int pileup_variants();
 void launch_serial(const DevState &st, const DevParams &P, cudaStream_t s);
 void launch_edge_detect(const DevState &st, const DevParams &P, cudaStream_t s);
@@ -31,8 +33,9 @@ void launch_ins_adjust(const DevState &st, cudaStream_t s);
 void launch_score(const DevState &st, const DevParams &P, cudaStream_t s);
 void launch_clear_err_bits(const DevState &st, unsigned int keep, cudaStream_t s);
 size_t wide_entry_bytes();
-void launch_ins_adjust_wide(const DevState &st, const int64_t *off, void *scratch, int64_t total, cudaStream_t s);
-void launch_score_wide(const DevState &st, const DevParams &P, const int64_t *off, void *scratch, int64_t total,
+void launch_wide_offsets(const DevState &st, int list, int64_t *off, cudaStream_t s);
+void launch_ins_adjust_wide(const DevState &st, const int64_t *off, void *scratch, int64_t entries, cudaStream_t s);
+void launch_score_wide(const DevState &st, const DevParams &P, const int64_t *off, void *scratch, int64_t entries,
                        cudaStream_t s);
 void launch_fisher(const int32_t *tab, int64_t n, double *p2, double *ratio, cudaStream_t s,
                    const double *lf = nullptr);
@@ -189,9 +192,10 @@ struct rv_ctx {
     size_t cap_wide_scratch = 0;
     int32_t max_lq = 0;   // longest read of the batch
 
-    // small counters: tile_counter, n_deferred, n_used, err, n_cand, pad, n_ofix, n_wide_ins,
-    // arena_used (64-bit, words 8-9), n_wide_score
+    // small counters (64 words): n_deferred, n_used, err, n_cand, aux, n_ofix, n_wide_ins,
+    // arena_used (64-bit, words 8-9), n_wide_score, tile counter (word 32)
     unsigned int *d_counters = nullptr;
+    unsigned int *h_cnt = nullptr;  // pinned host copy of the counter words (asynchronous reads)
 
     // scratch for the realigner boundary (grown on demand, owned by the context)
     uint32_t *d_tmp_idx = nullptr;
@@ -250,6 +254,7 @@ struct rv_ctx {
     int variant = -1;
     double variant_ms[8] = {};
     int variant_runs = 0;
+    int low_priority = 0;    // the device's lowest stream priority (the tile kernel's)
     bool pileup_pin = false;       // RV_PILEUP_VARIANT pinned the variant of the pileup in flight
     bool pileup_pending = false;   // pileup queued, not yet finished
     // pileup chain as a CUDA graph (rv_set_pileup_graph): each batch's chain

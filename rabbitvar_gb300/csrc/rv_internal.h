@@ -190,6 +190,8 @@ enum : uint32_t {
     ERR_FIX_FULL = 256u,     // more order-dependent entries than the OrderFix list holds
     ERR_CAND_FULL = 512u,    // more scored alleles than the candidate buffer holds
     ERR_WIDE_FULL = 1024u,   // more wide positions than the WidePos lists hold
+    ERR_WIDE_INS_SCRATCH = 2048u,    // the wide insertion pass needs more scratch (it did nothing)
+    ERR_WIDE_SCORE_SCRATCH = 4096u,  // the wide score pass needs more scratch (it did nothing)
 };
 
 // One scored allele at a candidate position, handed to the host for the

@@ -1,8 +1,8 @@
 // Pileup kernels: the record filter, the per-read CIGAR walk and the
 // allele-count maps (CigarParser::process, src/parseCigar.cpp:410-974).
 //
-//  * k_pileup_tiles: persistent blocks pull tiles (a region's consecutive
-//    reads) from a device work queue; each thread walks one read; A/C/G/T
+//  * k_pileup_tiles: blocks pull tiles (a region's consecutive reads) from a
+//    device work queue, a few each; each thread walks one read; A/C/G/T
 //    observations go into a shared-memory histogram covering the tile's
 //    window (kTileW positions), flushed to the per-position global cells once
 //    per tile; string-keyed alleles (MNV, indels, soft clips) go to a global
@@ -15,6 +15,8 @@
 //    getVariationMaybe lookup of src/parseCigar.cpp:1475) by re-walking the
 //    same and earlier reads, then applies it.
 #include <cuda_runtime.h>
+
+#include <algorithm>
 
 #include "rv_walk.cuh"
 
@@ -579,7 +581,7 @@ __global__ void k_region_reset(DevState st) {
 }
 
 template <int TW, int MINB, bool AGG>
-__global__ void __launch_bounds__(kPileupThreads, MINB) k_pileup_tiles(DevState st, DevParams P) {
+__global__ void __launch_bounds__(kPileupThreads, MINB) k_pileup_tiles(DevState st, DevParams P, int quota) {
     extern __shared__ __align__(16) unsigned char smem[];
     uint32_t *w0 = (uint32_t *)smem;
     uint32_t *w1 = w0 + 4 * TW;
@@ -587,7 +589,7 @@ __global__ void __launch_bounds__(kPileupThreads, MINB) k_pileup_tiles(DevState 
     uint32_t *first = w2 + 4 * TW;
     __shared__ int s_tile;
     __shared__ char s_ref[TW];
-    for (;;) {
+    for (int done = 0; done < quota; done++) {
         if (threadIdx.x == 0) s_tile = (int)atomicAdd(st.tile_counter, 1u);
         __syncthreads();
         int t = s_tile;
@@ -860,7 +862,7 @@ size_t pileup_smem_bytes() { return (size_t)kTileW * 4 * 4 * 4; }
 // histogram updates; the autotuner times them and keeps the fastest
 // (RV_PILEUP_VARIANT pins one, 0..5: 0-2 direct updates with 2/3/4 blocks
 // per SM, 3-5 the same with warp aggregation).
-using PileupKernel = void (*)(DevState, DevParams);
+using PileupKernel = void (*)(DevState, DevParams, int);
 static PileupKernel pileup_variant(int v) {
     switch (v) {
     case 0: return k_pileup_tiles<kTileW, 2, false>;
@@ -873,14 +875,44 @@ static PileupKernel pileup_variant(int v) {
 }
 int pileup_variants() { return 6; }
 
-cudaError_t launch_pileup(const DevState &st, const DevParams &P, int grid, cudaStream_t s, int variant) {
+// Blocks of the tile kernel are not persistent: each pulls at most `quota`
+// tiles from the shared counter and exits, so the grid is ceil(tiles /
+// quota) blocks and block slots free up continuously.  The launch carries
+// stream priority `priority` (the device's lowest): the blocks of a
+// higher-priority kernel queued meanwhile (another batch's realigner pass,
+// its scoring kernels, each dependent on the one before) take the next free
+// slots instead of waiting for the whole pileup.  Tiles are independent
+// (every histogram update is an atomic or an order-free merge), so neither
+// the quota nor the interleaving changes a result.
+int tile_quota(int64_t n_tiles, int resident_blocks) {
+    // at most 4 tiles per block (about a millisecond on a deep batch), and
+    // at least 32 waves of resident blocks' worth
+    const int64_t per = (int64_t)std::max(1, resident_blocks) * 32;
+    return (int)std::max<int64_t>(1, std::min<int64_t>(4, n_tiles / per));
+}
+
+cudaError_t launch_pileup(const DevState &st, const DevParams &P, int resident_blocks, cudaStream_t s, int variant,
+                          int priority) {
     size_t smem = pileup_smem_bytes();
     PileupKernel k = pileup_variant(variant);
     // (a larger shared-memory carveout was measured slower: the walker's
     // local-memory state lives in L1)
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k<<<grid, kPileupThreads, smem, s>>>(st, P);
+    if (st.n_tiles <= 0) return cudaSuccess;
+    const int quota = tile_quota(st.n_tiles, resident_blocks);
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributePriority;
+    attr[0].val.priority = priority;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(((int64_t)st.n_tiles + quota - 1) / quota));
+    cfg.blockDim = dim3(kPileupThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    e = cudaLaunchKernelEx(&cfg, k, st, P, quota);
+    if (e != cudaSuccess) return e;
     return cudaGetLastError();
 }
 

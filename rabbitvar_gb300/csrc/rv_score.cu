@@ -315,11 +315,59 @@ __global__ void k_ins_adjust(DevState st) {
     }
 }
 
+// Scratch offsets of a wide list: off[i] = the sum over j < i of
+// max(1, need_j) + 8 (entry j's alleles and insertion keys), off[n] the
+// total.  One block; the wide kernels queued behind it read them, so the
+// wide passes need no host round trip.
+__global__ void k_wide_offsets(const WidePos *list, const unsigned int *n_ptr, unsigned int cap, int64_t *off) {
+    __shared__ int64_t warp_sum[32];
+    __shared__ int64_t carry;
+    unsigned int n = *n_ptr;
+    if (n > cap) n = cap;
+    if (threadIdx.x == 0) {
+        carry = 0;
+        off[0] = 0;
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (unsigned int base = 0; base < n; base += blockDim.x) {
+        const unsigned int i = base + threadIdx.x;
+        int64_t v = i < n ? (int64_t)max(1, list[i].need) + 8 : 0;
+        for (int d = 1; d < 32; d <<= 1) {
+            const int64_t t = __shfl_up_sync(0xffffffffu, v, d);
+            if (lane >= d) v += t;
+        }
+        if (lane == 31) warp_sum[wid] = v;
+        __syncthreads();
+        if (wid == 0) {
+            int64_t w = lane < nw ? warp_sum[lane] : 0;
+            for (int d = 1; d < 32; d <<= 1) {
+                const int64_t t = __shfl_up_sync(0xffffffffu, w, d);
+                if (lane >= d) w += t;
+            }
+            if (lane < nw) warp_sum[lane] = w;
+        }
+        __syncthreads();
+        const int64_t incl = carry + (wid ? warp_sum[wid - 1] : 0) + v;
+        if (i < n) off[i + 1] = incl;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry = incl;
+        __syncthreads();
+    }
+}
+
 // The same for the queued wide positions, one thread each, with their
-// insertion keys in global scratch (off[i]: first scratch entry of entry i).
-__global__ void k_ins_adjust_wide(DevState st, const int64_t *off, uint32_t *ins_scratch) {
+// insertion keys in global scratch (off[i]: first scratch entry of entry i,
+// from k_wide_offsets).  Scratch of fewer than off[n] entries: nothing is
+// done and the error word says so (the host grows it and runs this again).
+__global__ void k_ins_adjust_wide(DevState st, const int64_t *off, uint32_t *ins_scratch, int64_t scratch_cap) {
     unsigned int n = *st.n_wide_ins;
     if (n > st.wide_cap) n = st.wide_cap;
+    if (n == 0) return;
+    if (off[n] > scratch_cap) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(st.err, ERR_WIDE_INS_SCRATCH);
+        return;
+    }
     for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const WidePos w = st.wide_ins[i];
         const Region &R = st.regions[w.region];
@@ -668,10 +716,18 @@ __global__ void k_score_list(DevState st, DevParams P, const int2 *list, int n) 
 }
 
 // The queued wide positions, one thread each, with their alleles and
-// insertion keys in global scratch (off[i]: first scratch entry of entry i).
-__global__ void k_score_wide(DevState st, DevParams P, const int64_t *off, V *v_scratch, uint32_t *ins_scratch) {
+// insertion keys in global scratch (off[i]: first scratch entry of entry i,
+// from k_wide_offsets; the alleles in the first scratch_cap entries, the
+// insertion keys after them).  Too little scratch: as k_ins_adjust_wide.
+__global__ void k_score_wide(DevState st, DevParams P, const int64_t *off, V *v_scratch, uint32_t *ins_scratch,
+                             int64_t scratch_cap) {
     unsigned int n = *st.n_wide_score;
     if (n > st.wide_cap) n = st.wide_cap;
+    if (n == 0) return;
+    if (off[n] > scratch_cap) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(st.err, ERR_WIDE_SCORE_SCRATCH);
+        return;
+    }
     for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const WidePos w = st.wide_score[i];
         const int cap = (int)(off[i + 1] - off[i]);
@@ -681,16 +737,21 @@ __global__ void k_score_wide(DevState st, DevParams P, const int64_t *off, V *v_
 
 size_t wide_entry_bytes() { return sizeof(V) + sizeof(uint32_t); }
 
-void launch_ins_adjust_wide(const DevState &st, const int64_t *off, void *scratch, int64_t total, cudaStream_t s) {
-    (void)total;
-    k_ins_adjust_wide<<<64, 64, 0, s>>>(st, off, (uint32_t *)scratch);
+void launch_wide_offsets(const DevState &st, int list, int64_t *off, cudaStream_t s) {
+    k_wide_offsets<<<1, 1024, 0, s>>>(list == 0 ? st.wide_ins : st.wide_score,
+                                      list == 0 ? st.n_wide_ins : st.n_wide_score, st.wide_cap, off);
 }
 
-void launch_score_wide(const DevState &st, const DevParams &P, const int64_t *off, void *scratch, int64_t total,
+// scratch: `entries` wide entries (wide_entry_bytes each)
+void launch_ins_adjust_wide(const DevState &st, const int64_t *off, void *scratch, int64_t entries, cudaStream_t s) {
+    k_ins_adjust_wide<<<64, 64, 0, s>>>(st, off, (uint32_t *)scratch, scratch ? entries : 0);
+}
+
+void launch_score_wide(const DevState &st, const DevParams &P, const int64_t *off, void *scratch, int64_t entries,
                        cudaStream_t s) {
     V *vs = (V *)scratch;
-    uint32_t *ins = (uint32_t *)(vs + total);
-    k_score_wide<<<64, 64, 0, s>>>(st, P, off, vs, ins);
+    uint32_t *ins = scratch ? (uint32_t *)(vs + entries) : nullptr;
+    k_score_wide<<<64, 64, 0, s>>>(st, P, off, vs, ins, scratch ? entries : 0);
 }
 
 // Features of the learned filter: 40 floats per candidate allele, from its
