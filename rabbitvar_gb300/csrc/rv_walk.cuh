@@ -150,6 +150,48 @@ struct Walker {
         __device__ int q(int i) const { return w->rv.q(i); }
         __device__ int lseq() const { return w->rv.lseq; }
     };
+    // CigarModifier (src/parseCigar.cpp:547-571) of a read whose CIGAR is
+    // one M op of length L >= 8 (most reads): no indel rule applies, so the
+    // rewrite is the two end scans, captureMisSoftly3Mismatches (:531-566)
+    // and then combineBeginDigM (:412-439), with the same reference lookups as
+    // rewrite_cigar and no token lists; at most 3 bases become a soft clip at
+    // either end.
+    __device__ __forceinline__ void rewrite_single_m(int L, int &position) {
+        int mch = L, tail = 0, head = 0;
+        {
+            // back_scan(L, position + L, L)
+            const int refoff = position + L;
+            int rn = 0, rrn = 0, rmch = 0;
+            while (rrn < mch && rn < mch) {
+                const int p = refoff - rrn - 1;
+                if (!has(p)) break;
+                if (at(p) != rv.base(L - rrn - 1)) { rn = rrn + 1; rmch = 0; }
+                else rmch++;
+                rrn++;
+                if (rmch >= 3) break;
+            }
+            if (rn > 0 && rn <= 3) { mch -= rn; tail = rn; }
+        }
+        {
+            int rn = 0, rrn = 0, rmch = 0;
+            while (rrn < mch && rn < mch) {
+                const int p = position + rrn;
+                if (!has(p)) break;
+                if (at(p) != rv.base(rrn)) { rn = rrn + 1; rmch = 0; }
+                else rmch++;
+                rrn++;
+                if (rmch >= 3) break;
+            }
+            if (rn > 0 && rn <= 3) { mch -= rn; head = rn; position += rn; }
+        }
+        if (!head && !tail) return;
+        int k = 0;
+        if (head) mod_w[k++] = ((uint32_t)head << 4) | 4u;
+        mod_w[k++] = (uint32_t)mch << 4;
+        if (tail) mod_w[k++] = ((uint32_t)tail << 4) | 4u;
+        mod_n = k;
+        n_cigar = k;
+    }
     // CigarModifier (src/parseCigar.cpp:547-571); false when the read is not supported
     __device__ __noinline__ bool rewrite_cigar(int idl, int &position) {
         const int n0 = rv.n_cigar;
@@ -743,9 +785,14 @@ struct Walker {
         int mapq = B.mapq[r];
         int position = B.pos[r] + 1;
         rpis = rpes = 0;
-        if (P.local_realign && !rewrite_cigar(idl, position)) {
-            S.error(ERR_UNSUPPORTED);
-            return;
+        if (P.local_realign) {
+            const uint32_t w0 = __ldg(rv.cig);
+            if (n_cigar == 1 && cig_op(w0) == 0 && cig_len(w0) >= 8 && cig_len(w0) == rv.lseq) {
+                rewrite_single_m(cig_len(w0), position);
+            } else if (!rewrite_cigar(idl, position)) {
+                S.error(ERR_UNSUPPORTED);
+                return;
+            }
         }
         // cleanupCigar (src/parseCigar.cpp:1858-1892), applied on read by W()
         lead_end = n_cigar;
