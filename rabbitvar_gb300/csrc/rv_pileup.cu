@@ -201,6 +201,7 @@ struct SinkBase {
     const DevParams *P;
     const Region *R;
     int region_idx;
+    __device__ bool done() const { return false; }  // the walk may stop early (no: every observation counts)
     __device__ void error(unsigned int bits) { set_err(st->err, bits); }
     __device__ void cov(int p, int n) {
         if (p < R->clo || p > R->chi) { error(ERR_CELL_RANGE); return; }
@@ -435,6 +436,8 @@ struct ProbeSink {
     int64_t stop_read;
     int stop_ci;
     bool stopped, found;
+    // the answer is known once the key was seen or the asking insertion reached
+    __device__ bool done() const { return found || stopped; }
     __device__ bool phantom(int) const { return false; }
     __device__ void touch_phantom(int) {}
     __device__ void error(unsigned int) {}
@@ -457,6 +460,7 @@ struct DetectSink {
     __device__ Fast fast() const { return Fast(); }
     const Region *R;
     int *hit;
+    __device__ bool done() const { return false; }
     __device__ bool phantom(int) const { return false; }
     __device__ void touch_phantom(int p) {
         if (p > R->we) atomicExch(hit, 1);
@@ -488,6 +492,7 @@ struct OrderSink {
     int pp;
     double pq;
     bool pstd, qstd;
+    __device__ bool done() const { return false; }
     __device__ bool phantom(int p) const {
         if (!track) return false;
         if (p > R->we) { int d = p - R->we - 1; return d < SerialSink::kPh && ((ph_hi[d >> 5] >> (d & 31)) & 1u); }

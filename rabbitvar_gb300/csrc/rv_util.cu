@@ -247,108 +247,143 @@ __device__ __forceinline__ int clip_rank_d(char c) {
     }
 }
 
-__global__ void k_clip_consensus(const Slot *list, const uint32_t *off, int64_t n_cells, const uint8_t *arena,
-                                 const unsigned long long *arena_used, uint32_t *meta, uint8_t *cons) {
+// One warp per cell: the lanes zero the cell's meta words and look for clip
+// aggregates together (most cells have none); for each aggregate, in list
+// order, the lanes gather its per-offset base counts into shared memory
+// (list order kept by ballot prefixes), rank them by (offset, base rank) —
+// each lane places its entries by counting smaller keys, ties by list
+// order, which is the stable order — and lane 0 walks the ranked counts.
+constexpr int kConsWarps = 4;
+__global__ void __launch_bounds__(32 * kConsWarps)
+    k_clip_consensus(const Slot *list, const uint32_t *off, int64_t n_cells, const uint8_t *arena,
+                     const unsigned long long *arena_used, uint32_t *meta, uint8_t *cons) {
+    __shared__ uint32_t s_key[kConsWarps][kMaxNt];  // offset << 9 | base rank
+    __shared__ int s_cnt[kConsWarps][kMaxNt];
+    __shared__ double s_q[kConsWarps][kMaxNt];
+    __shared__ char s_ch[kConsWarps][kMaxNt];
+    __shared__ uint16_t s_ord[kConsWarps][kMaxNt];  // ranked position -> gathered entry
+    const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+    uint32_t *key = s_key[wl];
+    int *cnt = s_cnt[wl];
+    double *q = s_q[wl];
+    char *ch = s_ch[wl];
+    uint16_t *ord = s_ord[wl];
     const unsigned long long used_bytes = *arena_used;
-    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n_cells; c += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t warps = (int64_t)gridDim.x * kConsWarps;
+    for (int64_t c = blockIdx.x * (int64_t)kConsWarps + wl; c < n_cells; c += warps) {
         const uint32_t b = off[c], e = off[c + 1];
+        bool any = false;
+        for (uint32_t i = b + lane; i < e; i += 32) {
+            meta[i] = 0u;
+            const int k = list[i].kind;
+            any |= k == KIND_SC5 || k == KIND_SC3;
+        }
+        if (!__any_sync(0xffffffffu, any)) continue;
+        __syncwarp();
         uint32_t written = 0;
         for (uint32_t i = b; i < e; i++) {
             const int kind = list[i].kind;
-            meta[i] = 0u;
             if (kind != KIND_SC5 && kind != KIND_SC3) continue;
             const int seqk = kind == KIND_SC3 ? KIND_SC3_SEQ : KIND_SC5_SEQ;
             const int agg_cnt = list[i].fwd + list[i].rev;
-            int idx[kMaxNt], cnt[kMaxNt], rk[kMaxNt];
-            char ch[kMaxNt];
-            double q[kMaxNt];
             int n = 0;
-            bool over = false;
-            for (uint32_t j = b; j < e; j++) {
-                const Slot &t = list[j];
-                if (t.kind != seqk || t.klen != 3 || (unsigned long long)t.koff + 3 > used_bytes) continue;
-                if (n == kMaxNt) { over = true; break; }
-                const uint8_t *kb = arena + t.koff;
-                idx[n] = kb[0] | (kb[1] << 8);
-                ch[n] = (char)kb[2];
-                rk[n] = clip_rank_d(ch[n]);
-                cnt[n] = t.obs;
-                q[n] = t.q_sum;
-                n++;
-            }
-            if (over) continue;
-            // order by (offset, rank)
-            for (int x = 1; x < n; x++) {
-                int ix = idx[x], rx = rk[x], cx = cnt[x];
-                char hx = ch[x];
-                double qx = q[x];
-                int y = x - 1;
-                while (y >= 0 && (idx[y] > ix || (idx[y] == ix && rk[y] > rx))) {
-                    idx[y + 1] = idx[y]; rk[y + 1] = rk[y]; cnt[y + 1] = cnt[y]; ch[y + 1] = ch[y]; q[y + 1] = q[y];
-                    y--;
+            for (uint32_t j0 = b; j0 < e; j0 += 32) {
+                const uint32_t j = j0 + lane;
+                bool m = false;
+                if (j < e) {
+                    const Slot &t = list[j];
+                    m = t.kind == seqk && t.klen == 3 && (unsigned long long)t.koff + 3 <= used_bytes;
                 }
-                idx[y + 1] = ix; rk[y + 1] = rx; cnt[y + 1] = cx; ch[y + 1] = hx; q[y + 1] = qx;
+                const unsigned bal = __ballot_sync(0xffffffffu, m);
+                const int pos = n + __popc(bal & ((1u << lane) - 1u));
+                if (m && pos < kMaxNt) {
+                    const Slot &t = list[j];
+                    const uint8_t *kb = arena + t.koff;
+                    const char c2 = (char)kb[2];
+                    key[pos] = ((uint32_t)(kb[0] | (kb[1] << 8)) << 9) | (uint32_t)clip_rank_d(c2);
+                    ch[pos] = c2;
+                    cnt[pos] = t.obs;
+                    q[pos] = t.q_sum;
+                }
+                n += __popc(bal);
             }
-            int nts = 0;
-            for (int x = 0; x < n; x++)
-                if (x == 0 || idx[x] != idx[x - 1]) nts++;
-            // the consensus characters go straight to this clip's output range
-            if (written > 16383u) continue;
-            uint8_t *out = cons + b + written;
-            int total = 0, match = 0, sl = 0;
-            bool flag = false;
-            for (int x = 0; x < n;) {
-                int y = x;
-                while (y < n && idx[y] == idx[x]) y++;
-                int maxc = 0, tt = 0;
-                double maxq = 0;
-                char chosen = 0;
-                for (int k = x; k < y; k++) {
-                    tt += cnt[k];
-                    if (cnt[k] > maxc || q[k] > maxq) {
-                        maxc = cnt[k];
-                        chosen = ch[k];
-                        maxq = q[k];
+            // more per-offset counts than the arrays hold: left to the host
+            if (n > kMaxNt) continue;
+            __syncwarp();
+            for (int x = lane; x < n; x += 32) {
+                const uint32_t kx = key[x];
+                int r = 0;
+                for (int y = 0; y < n; y++) {
+                    const uint32_t ky = key[y];
+                    r += ky < kx || (ky == kx && y < x);
+                }
+                ord[r] = (uint16_t)x;
+            }
+            __syncwarp();
+            if (lane == 0 && written <= 16383u) {
+                int nts = 0;
+                for (int x = 0; x < n; x++)
+                    if (x == 0 || (key[ord[x]] >> 9) != (key[ord[x - 1]] >> 9)) nts++;
+                // the consensus characters go straight to this clip's output range
+                uint8_t *out = cons + b + written;
+                int total = 0, match = 0, sl = 0;
+                bool flag = false;
+                for (int x = 0; x < n;) {
+                    const uint32_t ix = key[ord[x]] >> 9;
+                    int y = x;
+                    while (y < n && (key[ord[y]] >> 9) == ix) y++;
+                    int maxc = 0, tt = 0;
+                    double maxq = 0;
+                    char chosen = 0;
+                    for (int k = x; k < y; k++) {
+                        const int o = ord[k];
+                        tt += cnt[o];
+                        if (cnt[o] > maxc || q[o] > maxq) {
+                            maxc = cnt[o];
+                            chosen = ch[o];
+                            maxq = q[o];
+                        }
                     }
+                    if (ix == 3 && nts >= 6 && tt / (double)agg_cnt < 0.2 && tt <= 2) break;
+                    if ((tt - maxc > 2 || maxc <= tt - maxc) && maxc / (double)tt < 0.8) {
+                        if (flag) break;
+                        flag = true;
+                    }
+                    total += tt;
+                    match += maxc;
+                    if (chosen != 0) out[sl++] = (uint8_t)chosen;
+                    x = y;
                 }
-                if (idx[x] == 3 && nts >= 6 && tt / (double)agg_cnt < 0.2 && tt <= 2) break;
-                if ((tt - maxc > 2 || maxc <= tt - maxc) && maxc / (double)tt < 0.8) {
-                    if (flag) break;
-                    flag = true;
+                bool keep = total != 0 && match / (double)total > 0.9 && sl / 1.5 > nts - sl &&
+                            (sl / (double)nts > 0.8 || nts - sl < 10 || sl > 25);
+                int len = sl;
+                if (!keep) {
+                    out[0] = (uint8_t)' ';
+                    len = 1;
                 }
-                total += tt;
-                match += maxc;
-                if (chosen != 0) out[sl++] = (uint8_t)chosen;
-                x = y;
+                bool used = false;
+                if (len > 12) {
+                    bool a7 = true, t7 = true;
+                    for (int k = 1; k < 8; k++) {
+                        a7 = a7 && out[k] == 'A';
+                        t7 = t7 && out[k] == 'T';
+                    }
+                    if (a7 || t7) used = true;
+                    const char bases[4] = {'A', 'T', 'G', 'C'};
+                    int kinds = 0;
+                    bool low = false;
+                    for (int m = 0; m < 4; m++) {
+                        int cc = 0;
+                        for (int k = 0; k < len; k++) cc += out[k] == (uint8_t)bases[m];
+                        if (cc > 0) kinds++;
+                        if (cc / (double)len > 0.75) low = true;
+                    }
+                    if (low || kinds < 3) used = true;
+                }
+                meta[i] = (1u << 31) | (used ? (1u << 30) : 0u) | (written << 16) | (uint32_t)len;
+                written += (uint32_t)len;
             }
-            bool keep = total != 0 && match / (double)total > 0.9 && sl / 1.5 > nts - sl &&
-                        (sl / (double)nts > 0.8 || nts - sl < 10 || sl > 25);
-            int len = sl;
-            if (!keep) {
-                out[0] = (uint8_t)' ';
-                len = 1;
-            }
-            bool used = false;
-            if (len > 12) {
-                bool a7 = true, t7 = true;
-                for (int k = 1; k < 8; k++) {
-                    a7 = a7 && out[k] == 'A';
-                    t7 = t7 && out[k] == 'T';
-                }
-                if (a7 || t7) used = true;
-                const char bases[4] = {'A', 'T', 'G', 'C'};
-                int kinds = 0;
-                bool low = false;
-                for (int m = 0; m < 4; m++) {
-                    int cc = 0;
-                    for (int k = 0; k < len; k++) cc += out[k] == (uint8_t)bases[m];
-                    if (cc > 0) kinds++;
-                    if (cc / (double)len > 0.75) low = true;
-                }
-                if (low || kinds < 3) used = true;
-            }
-            meta[i] = (1u << 31) | (used ? (1u << 30) : 0u) | (written << 16) | (uint32_t)len;
-            written += (uint32_t)len;
+            written = __shfl_sync(0xffffffffu, written, 0);
         }
     }
 }
@@ -357,8 +392,8 @@ void launch_clip_consensus(const DevState &st, const uint32_t *off, const Slot *
                            cudaStream_t s) {
     const int64_t n = st.cells.n_cells;
     if (n > 0)
-        k_clip_consensus<<<(int)std::min<int64_t>((n + 127) / 128, 4096), 128, 0, s>>>(
-            list, off, n, st.hash.arena, st.hash.arena_used, meta, cons);
+        k_clip_consensus<<<(int)std::min<int64_t>((n + kConsWarps - 1) / kConsWarps, 152 * 32), 32 * kConsWarps, 0,
+                           s>>>(list, off, n, st.hash.arena, st.hash.arena_used, meta, cons);
 }
 
 // MNP keys (A/C/G/T '&' A/C/G/T...) that the realigner's adjustMNP visits.

@@ -841,6 +841,7 @@ struct Walker {
         const int goodq = P.goodq_i;  // integer qualities: q >= goodq_i exactly when q >= goodq
         const int ttr = P.trim_bases_after;
         for (int ci = 0; ci < n_cigar; ++ci) {
+            if (S.done()) return;
             int c_op = cop(ci);
             cel = clen(ci);
             if ((ci == 0 || ci == n_cigar - 1) && c_op == 1) c_op = 4;
@@ -900,6 +901,7 @@ struct Walker {
                             o.dir = dir; o.tp = tp; o.q = (double)q0; o.mapq = mapq; o.nm = nom - nmoff;
                             o.std_rel = true; o.creates = true;
                             S.single(st, b, o, read_idx);
+                            if (S.done()) return;
                         }
                     }
                     st++; rp++; rq++;
