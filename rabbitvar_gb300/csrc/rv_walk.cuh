@@ -756,6 +756,40 @@ struct Walker {
             if (c_op != 2) { rpis++; rpes++; }
             }
 
+    // The MNV growth loop of src/parseCigar.cpp:711-767, entered at a
+    // high-quality mismatch (read base rp against reference position st,
+    // base i of an M op of cel bases, no indel within vext after it): true
+    // when the loop ends in its first iteration without growing the key, so
+    // the allele is the single read base (the general path would emit it
+    // exactly as a match is emitted).  False when the key grows, and when
+    // the answer needs a reference lookup outside the window (the general
+    // path then decides, with the map's insert-on-lookup semantics).
+    __device__ __forceinline__ bool snv_stays_single(const typename Sink::Fast &fe, int rp, int st, int i, int cel,
+                                                     int goodq) const {
+        if (rv.q(rp + 1) < goodq + 5) return true;  // integer q: q < goodq + 5 exactly when q < goodq_i + 5
+        const char nuc = rv.base(rp + 1);
+        if (nuc == 'N') return true;
+        const int p1 = st + 1;
+        if (p1 < R.ws || p1 > R.we) return false;
+        const char r1 = fe.ref(ref, p1);
+        if (r1 == 'N') return true;
+        if (r1 != nuc) return false;  // the next base mismatches too: an MNV
+        int ssn = 0;
+        for (int ssi = 1; ssi <= P.vext; ssi++) {
+            if (i + 1 + ssi >= cel) break;
+            if (rp + 1 + ssi < rv.lseq) {
+                const int p = p1 + ssi;
+                if (p < R.ws || p > R.we) return false;
+                if (fe.ref(ref, p) != rv.base(rp + 1 + ssi)) {
+                    ssn = ssi + 1;
+                    break;
+                }
+            }
+        }
+        if (ssn == 0) return true;
+        return rv.q(rp + ssn) < goodq + 5;
+    }
+
     // parseCigar: src/parseCigar.cpp:497-974
     __device__ void walk(const Batch &B, int64_t r) {
         read_idx = r;
@@ -890,8 +924,11 @@ struct Walker {
                 const bool hs = st >= ws && st <= we;
                 const char rc = hs ? fe.ref(refp, st) : (char)0;
                 const bool mm = hs && base_index(rc) != b;
-                const bool slow = b < 0 || i >= tail_from ||
-                                  (mm && q0 >= goodq && st + 1 >= rs && st + 1 <= re && i + 1 < celr && rc != 'N');
+                bool slow = b < 0 || i >= tail_from;
+                // a high-quality mismatch enters the MNV growth; most end
+                // there as the single base and are emitted like a match
+                if (!slow && mm && q0 >= goodq && st + 1 >= rs && st + 1 <= re && i + 1 < celr && rc != 'N')
+                    slow = !snv_stays_single(fe, rp, st, i, celr, goodq);
                 if (!slow) {
                     const bool tr = ttr != 0 && (dir ? tlen - rp > ttr : rp > ttr);
                     if (!tr && st >= rs && st <= re) {
