@@ -123,6 +123,7 @@ DevState rv_ctx::state() const {
     s.n_regions = (int32_t)regions.size();
     s.tiles = d_tiles;
     s.n_tiles = (int32_t)tiles.size();
+    s.tile_reads = d_tile_reads;
     s.tile_counter = d_counters + CNT_TILE;
     s.cells = cells;
     s.hash.slots = d_slots;
@@ -482,7 +483,7 @@ void rv_destroy(rv_ctx *ctx) {
                     ctx->d_ftab, ctx->d_logfact, ctx->d_skip, ctx->d_patches, ctx->d_patch_keys,
                     ctx->d_list_off, ctx->d_list_bsum, ctx->d_list_idx, ctx->d_list_slots,
                     ctx->d_cons_meta, ctx->d_cons, ctx->d_ofix, ctx->d_used, ctx->d_wide, ctx->d_wide_off,
-                    ctx->d_wide_scratch, ctx->d_f35};
+                    ctx->d_wide_scratch, ctx->d_f35, ctx->d_tile_reads};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (ctx->h_mirror) cudaFreeHost(ctx->h_mirror);
@@ -535,6 +536,7 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
         std::vector<uint8_t> bad((size_t)nch, 0);
         ctx->h_span_lo.resize((size_t)n);
         ctx->h_span_hi.resize((size_t)n);
+        ctx->h_simple.resize((size_t)n);
         const bool widen = ctx->params.local_realign != 0;
         parallel_chunks(n, 1 << 16, [&](int64_t k, int64_t a, int64_t e) {
             int msp = 1, mlq = 1;
@@ -556,6 +558,7 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
                     if ((c[nc - 1] & 15) == 4 || (c[nc - 1] & 15) == 1) clip3 = (int)(c[nc - 1] >> 4);
                 }
                 if (!widen) ins = 0;
+                ctx->h_simple[i] = (uint8_t)(nc == 1 && (c[0] & 15) == 0);
                 const int pos1 = b->pos[i] + 1;
                 ctx->h_span_lo[i] = pos1 - clip5 - 1 - ins;
                 ctx->h_span_hi[i] = pos1 + sp + clip3 + ins;
@@ -634,7 +637,8 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
     ctx->regions.clear();
     ctx->tiles.clear();
     ctx->score_base.clear();
-    std::vector<int64_t> tile_begin;
+    std::vector<int64_t> list_begin;  // per region: its first entry in the tile read list
+    int64_t list_total = 0;
     int64_t cell_base = 0, score = 0;
     for (int r = 0; r < n_regions; r++) {
         Region R;
@@ -657,33 +661,50 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
         R.r0 = std::lower_bound(b->pos, b->pos + n, lo_pos) - b->pos;
         R.r1 = std::lower_bound(b->pos, b->pos + n, R.end) - b->pos;
         ctx->regions.push_back(R);
-        tile_begin.push_back((int64_t)ctx->tiles.size());
+        list_begin.push_back(list_total);
+        list_total += R.r1 - R.r0;
         ctx->score_base.push_back(score);
         score += R.end - R.start + 1;
-        // tiles of consecutive reads sized so a tile's window fits kTileW positions
-        int64_t nr = R.r1 - R.r0;
-        if (nr > 0) {
-            double dens = nr / (double)(R.end - R.start + 1 + 2 * max_lq);
-            double usable = (double)kTileW - max_span - max_lq - 16.0;  // window = start span + read extent
-            int64_t tr = (int64_t)std::max(32.0, std::min((double)kTileReads, usable * dens));
-            for (int64_t a = R.r0; a < R.r1; a += tr) {
-                Tile t;
-                t.region = r;
-                t.r0 = a;
-                t.r1 = std::min(R.r1, a + tr);
-                t.wlo = 0;  // set below from the read spans
-                ctx->tiles.push_back(t);
-            }
-        }
     }
-    tile_begin.push_back((int64_t)ctx->tiles.size());
-    // per region, from the read spans: the reads' reach, the edge-read flag
-    // and each tile's window start (the lowest span start of its non-edge
-    // reads); regions on host threads
+    list_begin.push_back(list_total);
+    if (n > (int64_t)UINT32_MAX) { ctx->err = "more than 2^32 reads in one batch"; return RV_ERR_ARG; }
+    ctx->tile_reads.resize((size_t)list_total);
+    std::vector<std::vector<Tile>> rtiles((size_t)n_regions);
+    // per region, on host threads: its read list (the reads whose CIGAR is
+    // one M op, then the others, file order within each: a tile of the first
+    // kind holds reads of equal walk cost, so its threads reach the tile's
+    // end together), its tiles over that list, sized so a tile's window fits
+    // kTileW positions, and from the read spans: the reads' reach, the
+    // edge-read flag and each tile's window start (the lowest span start of
+    // its non-edge reads)
     std::atomic<int> span_bad{0};
     parallel_for(n_regions, [&](int64_t r) {
         Region &R = ctx->regions[r];
         if (R.r1 <= R.r0) return;
+        uint32_t *list = ctx->tile_reads.data() + list_begin[r];
+        int64_t n_simple = 0;
+        for (int64_t i = R.r0; i < R.r1; i++)
+            if (ctx->h_simple[i]) list[n_simple++] = (uint32_t)i;
+        int64_t k = n_simple;
+        for (int64_t i = R.r0; i < R.r1; i++)
+            if (!ctx->h_simple[i]) list[k++] = (uint32_t)i;
+        const double len = (double)(R.end - R.start + 1 + 2 * max_lq);
+        const double usable = (double)kTileW - max_span - max_lq - 16.0;  // window = start span + read extent
+        std::vector<Tile> &tl = rtiles[(size_t)r];
+        for (int part = 0; part < 2; part++) {
+            const int64_t a0 = part ? n_simple : 0, a1 = part ? R.r1 - R.r0 : n_simple;
+            if (a1 <= a0) continue;
+            const double dens = (a1 - a0) / len;
+            const int64_t tr = (int64_t)std::max(32.0, std::min((double)kTileReads, usable * dens));
+            for (int64_t a = a0; a < a1; a += tr) {
+                Tile t;
+                t.region = (int32_t)r;
+                t.r0 = list_begin[r] + a;
+                t.r1 = list_begin[r] + std::min(a1, a + tr);
+                t.wlo = 0;
+                tl.push_back(t);
+            }
+        }
         int lo = INT32_MAX, hi = INT32_MIN, reach = 0;
         for (int64_t i = R.r0; i < R.r1; i++) {
             lo = std::min(lo, std::max(ctx->h_span_lo[i], 1));
@@ -695,14 +716,16 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
         R.reach = reach;
         R.serial = hi + kEdgeMargin > R.we ? 1 : 0;
         if (lo < R.clo || hi > R.chi) span_bad.store(1);
-        for (int64_t k = tile_begin[r]; k < tile_begin[r + 1]; k++) {
-            Tile &t = ctx->tiles[k];
+        for (Tile &t : tl) {
             int wlo = INT32_MAX;
-            for (int64_t i = t.r0; i < t.r1; i++)
+            for (int64_t e = t.r0; e < t.r1; e++) {
+                const uint32_t i = ctx->tile_reads[e];
                 if (ctx->h_span_hi[i] + kEdgeMargin <= R.we) wlo = std::min(wlo, ctx->h_span_lo[i]);
+            }
             t.wlo = std::max(wlo, R.clo);
         }
     });
+    for (const std::vector<Tile> &tl : rtiles) ctx->tiles.insert(ctx->tiles.end(), tl.begin(), tl.end());
     if (span_bad.load()) { ctx->err = "read span outside the region's cell range"; return RV_ERR_UNSUPPORTED; }
     ctx->n_score = score;
     ctx->n_cells = cell_base + 4;
@@ -772,6 +795,15 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
     if (!ctx->tiles.empty())
         RV_CUDA(cudaMemcpyAsync(ctx->d_tiles, ctx->tiles.data(), ctx->tiles.size() * sizeof(Tile),
                                 cudaMemcpyHostToDevice, s));
+    {
+        size_t cl = ctx->cap_tile_reads;
+        if ((st = grow(ctx, ctx->d_tile_reads, cl, ctx->tile_reads.size() + 1))) return st;
+        ctx->cap_tile_reads = cl;
+        if (!ctx->tile_reads.empty())
+            RV_CUDA(cudaMemcpyAsync(ctx->d_tile_reads, ctx->tile_reads.data(), ctx->tile_reads.size() * 4,
+                                    cudaMemcpyHostToDevice, s));
+        ctx->io_h2d += (int64_t)ctx->tile_reads.size() * 4;
+    }
     // cells: 7 x 4 words + first (4 words) per position, plus cov, kflags, head
     size_t need_cells = (size_t)ctx->n_cells;
     if (need_cells > ctx->cap_cells || !ctx->d_cellmem) {

@@ -142,13 +142,17 @@ struct rv_ctx {
     std::vector<uint16_t> h_flag, h_ncig;
     std::vector<uint32_t> h_cigoff, h_cigar;
     std::vector<int32_t> h_span_lo, h_span_hi;  // per read: the span the tile windows cover
+    std::vector<uint8_t> h_simple;              // per read: its CIGAR is one M op
 
     // regions / tiles
     std::vector<rv::Region> regions;
     std::vector<rv::Tile> tiles;
+    std::vector<uint32_t> tile_reads;  // per region: its one-op reads, then the others (the tiles' read lists)
     std::vector<int64_t> score_base;
     rv::Region *d_regions = nullptr;
     rv::Tile *d_tiles = nullptr;
+    uint32_t *d_tile_reads = nullptr;
+    size_t cap_tile_reads = 0;
     int64_t *d_score_base = nullptr;
     size_t cap_regions = 0, cap_tiles = 0;
     int64_t n_score = 0;

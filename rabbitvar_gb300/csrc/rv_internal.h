@@ -78,7 +78,7 @@ struct Region {
 struct Tile {
     int32_t region;
     int32_t wlo;             // first position of the tile's shared-memory window (host-computed)
-    int64_t r0, r1;          // reads [r0, r1) of the batch
+    int64_t r0, r1;          // entries [r0, r1) of the tile read list (DevState::tile_reads)
 };
 
 // A read is an edge read of a region when its span reaches within this many
@@ -213,6 +213,7 @@ struct DevState {
     int32_t n_regions;
     Tile *tiles;
     int32_t n_tiles;
+    const uint32_t *tile_reads;  // per region, its reads with a one-op M CIGAR and then the others (file order each)
     unsigned int *tile_counter;
     Cells cells;
     Hash hash;

@@ -627,7 +627,8 @@ __global__ void __launch_bounds__(kPileupThreads, MINB) k_pileup_tiles(DevState 
             // and would hit the same histogram words together)
             static_assert(kTileReads == 256 && kPileupThreads == 256, "tile read permutation");
             const int64_t k = (int64_t)((threadIdx.x & 31u) * 8u + (threadIdx.x >> 5));
-            for (int64_t r = tile.r0 + k; r < tile.r1; r += blockDim.x) {
+            for (int64_t e = tile.r0 + k; e < tile.r1; e += blockDim.x) {
+                const int64_t r = st.tile_reads[e];
                 if (!read_passes(st.batch, P, R, r)) continue;
                 if (R.serial && R.edge_hit) {
                     int a, b;
