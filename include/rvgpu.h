@@ -125,7 +125,11 @@ rv_status rv_upload_reference(rv_ctx *ctx, const char *chr, const char *bases, i
 
 /* Replaces the record iterator (sam_itr_querys + next_record,
  * src/recordPreprocessor.cpp:101-180) for a batch of regions: copies the
- * host batch to the device on `stream` (cudaStream_t, NULL = default). */
+ * host batch to the device on `stream` (cudaStream_t, NULL = default).
+ * With local realignment (-k 1) rv_realign reads the batch's host arrays
+ * pos, flag, n_cigar, cig_off and cigar again (the reference's realigner
+ * re-reads the records of a region): they must stay valid and unchanged
+ * until rv_realign of this batch returns. */
 rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *reads, const rv_region *regions, int n_regions,
                           void *stream);
 

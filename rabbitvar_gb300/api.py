@@ -232,6 +232,9 @@ class Context:
         self._check(self.L.rv_upload_reference(self.h, chr_name.encode(), bases, len(bases)))
 
     def submit(self, batch: Batch, regions: list[tuple[int, int]]):
+        # the batch's arrays stay referenced until the next submit: with -k 1
+        # the realigner reads the alignments again from them
+        self._batch = batch
         self._batch_struct = batch.struct()
         self._regions = (Region * max(len(regions), 1))(*[Region(a, b) for a, b in regions])
         self._check(self.L.rv_submit_batch(self.h, C.byref(self._batch_struct), self._regions, len(regions), None))

@@ -50,6 +50,18 @@ rv_status grow(rv_ctx *ctx, T *&p, size_t &cap, size_t need) {
     return RV_OK;
 }
 
+// Pinned host buffer of at least `need` bytes (grown with headroom).
+rv_status ensure_pinned(rv_ctx *ctx, void **p, size_t &cap, size_t need) {
+    if (need <= cap && *p) return RV_OK;
+    if (*p) cudaFreeHost(*p);
+    *p = nullptr;
+    cap = 0;
+    const size_t n = std::max<size_t>(need + need / 4, 4096);
+    RV_CUDA(cudaHostAlloc(p, n, cudaHostAllocDefault));
+    cap = n;
+    return RV_OK;
+}
+
 unsigned long long next_pow2(unsigned long long x) {
     unsigned long long p = 1;
     while (p < x) p <<= 1;
@@ -490,6 +502,8 @@ void rv_destroy(rv_ctx *ctx) {
     if (ctx->h_mirror_slots) cudaFreeHost(ctx->h_mirror_slots);
     if (ctx->h_fstage) cudaFreeHost(ctx->h_fstage);
     if (ctx->h_cnt) cudaFreeHost(ctx->h_cnt);
+    if (ctx->h_tile_reads) cudaFreeHost(ctx->h_tile_reads);
+    if (ctx->h_meta) cudaFreeHost(ctx->h_meta);
     for (int i = 0; i < 12; i++)
         if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
     if (ctx->ev_block) cudaEventDestroy(ctx->ev_block);
@@ -536,7 +550,7 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
         std::vector<uint8_t> bad((size_t)nch, 0);
         ctx->h_span_lo.resize((size_t)n);
         ctx->h_span_hi.resize((size_t)n);
-        ctx->h_simple.resize((size_t)n);
+        ctx->h_cost.resize((size_t)n);
         const bool widen = ctx->params.local_realign != 0;
         parallel_chunks(n, 1 << 16, [&](int64_t k, int64_t a, int64_t e) {
             int msp = 1, mlq = 1;
@@ -558,7 +572,14 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
                     if ((c[nc - 1] & 15) == 4 || (c[nc - 1] & 15) == 1) clip3 = (int)(c[nc - 1] >> 4);
                 }
                 if (!widen) ins = 0;
-                ctx->h_simple[i] = (uint8_t)(nc == 1 && (c[0] & 15) == 0);
+                // walk-cost class: one M op; soft clips around one M op; anything else
+                uint8_t cls = 2;
+                if (nc == 1 && (c[0] & 15) == 0) cls = 0;
+                else if (nc == 2 && (((c[0] & 15) == 4 && (c[1] & 15) == 0) || ((c[0] & 15) == 0 && (c[1] & 15) == 4)))
+                    cls = 1;
+                else if (nc == 3 && (c[0] & 15) == 4 && (c[1] & 15) == 0 && (c[2] & 15) == 4)
+                    cls = 1;
+                ctx->h_cost[i] = cls;
                 const int pos1 = b->pos[i] + 1;
                 ctx->h_span_lo[i] = pos1 - clip5 - 1 - ins;
                 ctx->h_span_hi[i] = pos1 + sp + clip3 + ins;
@@ -576,6 +597,7 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
         }
     }
     if (misaligned) { ctx->err = "base_off must be a multiple of 32"; return RV_ERR_ARG; }
+    tm.lap("spans");
     ctx->n_reads = n;
     ctx->max_lq = max_lq;
     ctx->n_cigar_words = b->n_cigar_words;
@@ -608,30 +630,14 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
     }
     ctx->io_d2h = 0;
     tm.lap("prep+alloc");
-    // -k 1: the alignment spans stay on the host for noPassingReads
-    if (ctx->params.local_realign) {
-        // copied in chunks on the host threads (tens of MB for a deep batch)
-        ctx->h_pos.resize((size_t)n);
-        ctx->h_flag.resize((size_t)n);
-        ctx->h_ncig.resize((size_t)n);
-        ctx->h_cigoff.resize((size_t)n);
-        ctx->h_cigar.resize((size_t)b->n_cigar_words);
-        parallel_chunks(n, 1 << 16, [&](int64_t, int64_t a, int64_t e) {
-            std::copy(b->pos + a, b->pos + e, ctx->h_pos.data() + a);
-            std::copy(b->flag + a, b->flag + e, ctx->h_flag.data() + a);
-            std::copy(b->n_cigar + a, b->n_cigar + e, ctx->h_ncig.data() + a);
-            std::copy(b->cig_off + a, b->cig_off + e, ctx->h_cigoff.data() + a);
-        });
-        parallel_chunks(b->n_cigar_words, 1 << 18, [&](int64_t, int64_t a, int64_t e) {
-            std::copy(b->cigar + a, b->cigar + e, ctx->h_cigar.data() + a);
-        });
-    } else {
-        ctx->h_pos.clear();
-        ctx->h_flag.clear();
-        ctx->h_ncig.clear();
-        ctx->h_cigoff.clear();
-        ctx->h_cigar.clear();
-    }
+    // -k 1: the realigner reads the batch's alignments again from the
+    // caller's arrays (noPassingReads)
+    ctx->hb_n = ctx->params.local_realign ? n : 0;
+    ctx->hb_pos = b->pos;
+    ctx->hb_flag = b->flag;
+    ctx->hb_ncig = b->n_cigar;
+    ctx->hb_cigoff = b->cig_off;
+    ctx->hb_cigar = b->cigar;
     const int pad = max_span + max_lq + 4;
     const rv_params &P = ctx->params;
     ctx->regions.clear();
@@ -668,12 +674,15 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
     }
     list_begin.push_back(list_total);
     if (n > (int64_t)UINT32_MAX) { ctx->err = "more than 2^32 reads in one batch"; return RV_ERR_ARG; }
-    ctx->tile_reads.resize((size_t)list_total);
+    if ((st = ensure_pinned(ctx, (void **)&ctx->h_tile_reads, ctx->cap_h_tile_reads, (size_t)list_total * 4)))
+        return st;
+    ctx->n_tile_reads = (size_t)list_total;
     std::vector<std::vector<Tile>> rtiles((size_t)n_regions);
     // per region, on host threads: its read list (the reads whose CIGAR is
-    // one M op, then the others, file order within each: a tile of the first
-    // kind holds reads of equal walk cost, so its threads reach the tile's
-    // end together), its tiles over that list, sized so a tile's window fits
+    // one M op, then those with soft clips around one M op, then the others,
+    // file order within each: a tile holds reads of one kind, of about equal
+    // walk cost, so its threads reach the tile's end together), its tiles
+    // over that list, sized so a tile's window fits
     // kTileW positions, and from the read spans: the reads' reach, the
     // edge-read flag and each tile's window start (the lowest span start of
     // its non-edge reads)
@@ -681,18 +690,19 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
     parallel_for(n_regions, [&](int64_t r) {
         Region &R = ctx->regions[r];
         if (R.r1 <= R.r0) return;
-        uint32_t *list = ctx->tile_reads.data() + list_begin[r];
-        int64_t n_simple = 0;
-        for (int64_t i = R.r0; i < R.r1; i++)
-            if (ctx->h_simple[i]) list[n_simple++] = (uint32_t)i;
-        int64_t k = n_simple;
-        for (int64_t i = R.r0; i < R.r1; i++)
-            if (!ctx->h_simple[i]) list[k++] = (uint32_t)i;
+        uint32_t *list = ctx->h_tile_reads + list_begin[r];
+        int64_t bound[4] = {0, 0, 0, 0};
+        for (int cls = 0; cls < 3; cls++) {
+            int64_t k = bound[cls];
+            for (int64_t i = R.r0; i < R.r1; i++)
+                if (ctx->h_cost[i] == cls) list[k++] = (uint32_t)i;
+            bound[cls + 1] = k;
+        }
         const double len = (double)(R.end - R.start + 1 + 2 * max_lq);
         const double usable = (double)kTileW - max_span - max_lq - 16.0;  // window = start span + read extent
         std::vector<Tile> &tl = rtiles[(size_t)r];
-        for (int part = 0; part < 2; part++) {
-            const int64_t a0 = part ? n_simple : 0, a1 = part ? R.r1 - R.r0 : n_simple;
+        for (int part = 0; part < 3; part++) {
+            const int64_t a0 = bound[part], a1 = bound[part + 1];
             if (a1 <= a0) continue;
             const double dens = (a1 - a0) / len;
             const int64_t tr = (int64_t)std::max(32.0, std::min((double)kTileReads, usable * dens));
@@ -719,13 +729,14 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
         for (Tile &t : tl) {
             int wlo = INT32_MAX;
             for (int64_t e = t.r0; e < t.r1; e++) {
-                const uint32_t i = ctx->tile_reads[e];
+                const uint32_t i = ctx->h_tile_reads[e];
                 if (ctx->h_span_hi[i] + kEdgeMargin <= R.we) wlo = std::min(wlo, ctx->h_span_lo[i]);
             }
             t.wlo = std::max(wlo, R.clo);
         }
     });
     for (const std::vector<Tile> &tl : rtiles) ctx->tiles.insert(ctx->tiles.end(), tl.begin(), tl.end());
+    tm.lap("regions+tiles");
     if (span_bad.load()) { ctx->err = "read span outside the region's cell range"; return RV_ERR_UNSUPPORTED; }
     ctx->n_score = score;
     ctx->n_cells = cell_base + 4;
@@ -786,24 +797,36 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
         return st;
     ctx->cap_regions = creg;
     ctx->cap_tiles = ct;
-    if (!ctx->regions.empty()) {
-        RV_CUDA(cudaMemcpyAsync(ctx->d_regions, ctx->regions.data(), ctx->regions.size() * sizeof(Region),
-                                cudaMemcpyHostToDevice, s));
-        RV_CUDA(cudaMemcpyAsync(ctx->d_score_base, ctx->score_base.data(), ctx->score_base.size() * 8,
-                                cudaMemcpyHostToDevice, s));
+    {
+        // regions, score bases and tiles through the context's pinned staging
+        auto up16 = [](size_t x) { return (x + 15) & ~(size_t)15; };
+        const size_t b_reg = up16(ctx->regions.size() * sizeof(Region)), b_sb = up16(ctx->score_base.size() * 8);
+        const size_t b_tl = up16(ctx->tiles.size() * sizeof(Tile));
+        if ((st = ensure_pinned(ctx, (void **)&ctx->h_meta, ctx->cap_meta, b_reg + b_sb + b_tl + 16))) return st;
+        char *h = ctx->h_meta;
+        if (!ctx->regions.empty()) {
+            memcpy(h, ctx->regions.data(), ctx->regions.size() * sizeof(Region));
+            memcpy(h + b_reg, ctx->score_base.data(), ctx->score_base.size() * 8);
+            RV_CUDA(cudaMemcpyAsync(ctx->d_regions, h, ctx->regions.size() * sizeof(Region), cudaMemcpyHostToDevice, s));
+            RV_CUDA(cudaMemcpyAsync(ctx->d_score_base, h + b_reg, ctx->score_base.size() * 8, cudaMemcpyHostToDevice,
+                                    s));
+        }
+        if (!ctx->tiles.empty()) {
+            memcpy(h + b_reg + b_sb, ctx->tiles.data(), ctx->tiles.size() * sizeof(Tile));
+            RV_CUDA(cudaMemcpyAsync(ctx->d_tiles, h + b_reg + b_sb, ctx->tiles.size() * sizeof(Tile),
+                                    cudaMemcpyHostToDevice, s));
+        }
     }
-    if (!ctx->tiles.empty())
-        RV_CUDA(cudaMemcpyAsync(ctx->d_tiles, ctx->tiles.data(), ctx->tiles.size() * sizeof(Tile),
-                                cudaMemcpyHostToDevice, s));
     {
         size_t cl = ctx->cap_tile_reads;
-        if ((st = grow(ctx, ctx->d_tile_reads, cl, ctx->tile_reads.size() + 1))) return st;
+        if ((st = grow(ctx, ctx->d_tile_reads, cl, ctx->n_tile_reads + 1))) return st;
         ctx->cap_tile_reads = cl;
-        if (!ctx->tile_reads.empty())
-            RV_CUDA(cudaMemcpyAsync(ctx->d_tile_reads, ctx->tile_reads.data(), ctx->tile_reads.size() * 4,
+        if (ctx->n_tile_reads)
+            RV_CUDA(cudaMemcpyAsync(ctx->d_tile_reads, ctx->h_tile_reads, ctx->n_tile_reads * 4,
                                     cudaMemcpyHostToDevice, s));
-        ctx->io_h2d += (int64_t)ctx->tile_reads.size() * 4;
+        ctx->io_h2d += (int64_t)ctx->n_tile_reads * 4;
     }
+    tm.lap("region+tile copies");
     // cells: 7 x 4 words + first (4 words) per position, plus cov, kflags, head
     size_t need_cells = (size_t)ctx->n_cells;
     if (need_cells > ctx->cap_cells || !ctx->d_cellmem) {
@@ -833,6 +856,7 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
         C.kflags = (uint8_t *)m;
         C.n_cells = ctx->n_cells;
     }
+    tm.lap("cells");
     // hash table / arena / deferred / order-fix list sized from the batch (or
     // the capacities rv_set_capacities forced for this batch); every table
     // grows when a pileup overflows it (pileup_finish runs the pileup again)
@@ -857,6 +881,7 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
         ctx->force_hash = ctx->force_arena = 0;
         ctx->force_deferred = ctx->force_fix = 0;
     }
+    tm.lap("tables");
     unsigned int want_wide = (unsigned int)std::min<int64_t>(INT32_MAX / 2, score / 8 + 4096);
     if (want_wide > ctx->wide_cap || !ctx->d_wide) {
         if (ctx->d_wide) cudaFree(ctx->d_wide);
@@ -880,7 +905,7 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
         RV_CUDA(cudaMalloc((void **)&ctx->d_cand, (size_t)want_cand * sizeof(CandVar)));
         ctx->cand_cap = want_cand;
     }
-    tm.lap("regions+dedup+buffers");
+    tm.lap("wide+candidates");
     // the read arrays last: the small pageable copies above are staged before
     // these large pinned copies are queued, so none of them waits on the batch
     // upload

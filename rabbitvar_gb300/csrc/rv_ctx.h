@@ -137,17 +137,25 @@ struct rv_ctx {
     uint8_t *d_skip = nullptr;  // -t duplicate flags
     size_t cap_skip = 0;
     bool use_skip = false;
-    // -k 1: alignment spans of the batch kept on the host (noPassingReads)
-    std::vector<int32_t> h_pos;
-    std::vector<uint16_t> h_flag, h_ncig;
-    std::vector<uint32_t> h_cigoff, h_cigar;
+    // -k 1: the submitted batch's host arrays, read again by the realigner
+    // (noPassingReads); the caller keeps them until rv_realign returns
+    const int32_t *hb_pos = nullptr;
+    const uint16_t *hb_flag = nullptr, *hb_ncig = nullptr;
+    const uint32_t *hb_cigoff = nullptr, *hb_cigar = nullptr;
+    int64_t hb_n = 0;
     std::vector<int32_t> h_span_lo, h_span_hi;  // per read: the span the tile windows cover
-    std::vector<uint8_t> h_simple;              // per read: its CIGAR is one M op
+    std::vector<uint8_t> h_cost;                // per read: walk-cost class (0 one M op, 1 clips around one M, 2 other)
 
     // regions / tiles
     std::vector<rv::Region> regions;
     std::vector<rv::Tile> tiles;
-    std::vector<uint32_t> tile_reads;  // per region: its one-op reads, then the others (the tiles' read lists)
+    // pinned host staging of the batch's tile read lists (per region: its
+    // reads by walk-cost class) and of the region and tile records, so their
+    // copies queue without waiting behind the previous batch's uploads
+    uint32_t *h_tile_reads = nullptr;
+    size_t cap_h_tile_reads = 0, n_tile_reads = 0;
+    char *h_meta = nullptr;
+    size_t cap_meta = 0;
     std::vector<int64_t> score_base;
     rv::Region *d_regions = nullptr;
     rv::Tile *d_tiles = nullptr;

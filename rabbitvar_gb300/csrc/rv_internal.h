@@ -213,7 +213,7 @@ struct DevState {
     int32_t n_regions;
     Tile *tiles;
     int32_t n_tiles;
-    const uint32_t *tile_reads;  // per region, its reads with a one-op M CIGAR and then the others (file order each)
+    const uint32_t *tile_reads;  // per region, its reads grouped by CIGAR shape (one M op; clips around one M op; other)
     unsigned int *tile_counter;
     Cells cells;
     Hash hash;

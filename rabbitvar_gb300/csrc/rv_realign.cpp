@@ -606,22 +606,23 @@ struct RegionRealigner {
         const rv_ctx *c = ctx;
         int cnt = 0;
         const uint32_t dlen = ((uint32_t)(end - start) << 4) | 2u;
-        const int64_t n = (int64_t)c->h_pos.size();
-        int64_t lo = std::lower_bound(c->h_pos.begin(), c->h_pos.end(), start - 1 - 4096) - c->h_pos.begin();
-        for (int64_t i = lo; i < n && c->h_pos[i] < end; i++) {
-            const uint32_t *cg = c->h_cigar.data() + c->h_cigoff[i];
+        const int64_t n = c->hb_n;
+        const int32_t *pos = c->hb_pos;
+        int64_t lo = std::lower_bound(pos, pos + n, start - 1 - 4096) - pos;
+        for (int64_t i = lo; i < n && pos[i] < end; i++) {
+            const uint32_t *cg = c->hb_cigar + c->hb_cigoff[i];
             int span = 0, aligned = 0;
             bool has_d = false;
-            for (int k = 0; k < c->h_ncig[i]; k++) {
+            for (int k = 0; k < c->hb_ncig[i]; k++) {
                 int o = cg[k] & 15;
                 if (o == 0 || o == 2 || o == 3 || o == 7 || o == 8) span += (int)(cg[k] >> 4);
                 if (o == 0 || o == 2) aligned += (int)(cg[k] >> 4);
                 if (cg[k] == dlen) has_d = true;
             }
-            int endpos = ((c->h_flag[i] & 4) || span == 0) ? c->h_pos[i] + 1 : c->h_pos[i] + span;
+            int endpos = ((c->hb_flag[i] & 4) || span == 0) ? pos[i] + 1 : pos[i] + span;
             if (endpos <= start - 1) continue;
             if (has_d) continue;
-            int rs0 = c->h_pos[i] + 1, re0 = rs0 + aligned;
+            int rs0 = pos[i] + 1, re0 = rs0 + aligned;
             if (re0 > end + 2 && rs0 < start - 2) cnt++;
         }
         return cnt <= 0;
