@@ -108,20 +108,26 @@ __device__ __forceinline__ void stage_tile(unsigned char *dst, const bf16 *src, 
 }
 
 // C tile = A[m0.., k-range] * B[0..N, k-range]^T, accumulated in TMEM, then the epilogue.
-// grid.x: M tiles; grid.y: K splits of `kper` columns each.
+// grid.x: M tiles; grid.y: K splits of `kper` columns each.  The operands of
+// 64-column chunks are staged in two shared-memory buffers: while the tensor
+// core multiplies chunk i out of one, the threads stage chunk i + 1 into the
+// other (after the MMAs of chunk i - 1, which read it, have completed: each
+// buffer's commits arrive on its own mbarrier).
 template <int N, int EPI>
 __global__ void __launch_bounds__(128, 1) k_umma(const bf16 *A, int lda, const bf16 *B, int ldb, int kper, Epi e) {
     extern __shared__ __align__(1024) unsigned char smem[];
-    unsigned char *sa = smem;                  // 128 x 64 bf16 = 16 KB
-    unsigned char *sb = smem + 16384;          // N x 64 bf16
-    __shared__ __align__(8) uint64_t bar;
+    constexpr int kStage = 16384 + N * kChunkK * 2;  // one buffer: A 128 x 64, B N x 64 (bf16)
+    static_assert(2 * kStage <= kGemmSmem, "two staging buffers");
+    __shared__ __align__(8) uint64_t bar[2];
     __shared__ uint32_t s_tmem;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int m0 = blockIdx.x * kTileM;
     const int kb = blockIdx.y * kper;
-    const uint32_t bar_a = smem_u32(&bar);
+    const int nk = (kper + kChunkK - 1) / kChunkK;
+    const uint32_t bar0 = smem_u32(&bar[0]);
     if (threadIdx.x == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_a) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0 + 8) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
@@ -130,22 +136,25 @@ __global__ void __launch_bounds__(128, 1) k_umma(const bf16 *A, int lda, const b
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
+    if (nk > 0) {
+        stage_tile<kTileM>(smem, A, lda, m0, kb);
+        stage_tile<N>(smem + 16384, B, ldb, 0, kb);
+    }
+    // generic-proxy shared-memory writes -> visible to the tensor core
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = s_tmem;
     const uint32_t idesc = make_idesc(kTileM, N);
     bool ok = true;
-    int it = 0;
-    for (int k0 = kb; k0 < kb + kper; k0 += kChunkK, ++it) {
-        stage_tile<kTileM>(sa, A, lda, m0, k0);
-        stage_tile<N>(sb, B, ldb, 0, k0);
-        // generic-proxy shared-memory writes -> visible to the tensor core
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
+    int committed = -1;  // last chunk whose MMAs were committed
+    for (int it = 0; it < nk; ++it) {
+        const int buf = it & 1;
+        unsigned char *sa = smem + buf * kStage;
         if (threadIdx.x == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t a0 = smem_u32(sa), b0 = smem_u32(sb);
+            const uint32_t a0 = smem_u32(sa), b0 = a0 + 16384;
 #pragma unroll
             for (int kk = 0; kk < kChunkK / 16; kk++) {
                 uint64_t ad = make_desc(a0 + kk * 256, 128, 1024);
@@ -158,15 +167,32 @@ __global__ void __launch_bounds__(128, 1) k_umma(const bf16 *A, int lda, const b
                     "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
                     : "memory");
             }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar_a)
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             bar0 + 8 * buf)
                          : "memory");
         }
-        // every thread waits; the outcome is made uniform before anyone leaves
-        const bool done = mbar_wait(bar_a, (uint32_t)(it & 1));
-        if (!__syncthreads_and(done)) {
-            ok = false;
-            break;
+        committed = it;
+        if (it + 1 < nk) {
+            // the other buffer was read by chunk it - 1: wait for its MMAs
+            // (the (it - 1) / 2-th phase of that buffer's barrier)
+            bool done = true;
+            if (it >= 1) done = mbar_wait(bar0 + 8 * (buf ^ 1), (uint32_t)(((it - 1) >> 1) & 1));
+            if (!__syncthreads_and(done)) {
+                ok = false;
+                break;
+            }
+            unsigned char *na = smem + (buf ^ 1) * kStage;
+            stage_tile<kTileM>(na, A, lda, m0, kb + (it + 1) * kChunkK);
+            stage_tile<N>(na + 16384, B, ldb, 0, kb + (it + 1) * kChunkK);
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncthreads();
         }
+    }
+    // the last commit tracks every MMA issued before it; after a timeout the
+    // MMAs already committed are waited for (bounded) before TMEM is freed
+    if (committed >= 0) {
+        const bool done = mbar_wait(bar0 + 8 * (committed & 1), (uint32_t)((committed >> 1) & 1));
+        if (!__syncthreads_and(done)) ok = false;
     }
     if (!ok) {
         if (threadIdx.x == 0) atomicOr(e.err, 1u);
