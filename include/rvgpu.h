@@ -124,8 +124,14 @@ const char *rv_last_error(const rv_ctx *ctx);
 rv_status rv_upload_reference(rv_ctx *ctx, const char *chr, const char *bases, int64_t n);
 
 /* Replaces the record iterator (sam_itr_querys + next_record,
- * src/recordPreprocessor.cpp:101-180) for a batch of regions: copies the
- * host batch to the device on `stream` (cudaStream_t, NULL = default).
+ * src/recordPreprocessor.cpp:101-180) for a batch of regions: queues the
+ * copy of the host batch to the device on `stream` (cudaStream_t, NULL =
+ * default) and the batch's preparation there (read spans, region bounds,
+ * the tiles of the pileup), without waiting for either; the host arrays
+ * must stay unchanged until the following rv_pileup has returned.  A CIGAR
+ * outside the batch's words is refused here; the device's record checks
+ * (base_off a multiple of 32, bases inside the batch's bases) are reported
+ * by that rv_pileup.
  * With local realignment (-k 1) rv_realign reads the batch's host arrays
  * pos, flag, n_cigar, cig_off and cigar again (the reference's realigner
  * re-reads the records of a region): they must stay valid and unchanged

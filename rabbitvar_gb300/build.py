@@ -16,7 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "librvgpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU = ["rv_pileup.cu", "rv_score.cu", "rv_util.cu", "rv_noalloc.cu", "rv_mlp.cu", "rv_bgzf.cu"]
+CU = ["rv_pileup.cu", "rv_score.cu", "rv_util.cu", "rv_prep.cu", "rv_noalloc.cu", "rv_mlp.cu", "rv_bgzf.cu"]
 CPP = ["rv_capi.cpp", "rv_host.cpp", "rv_realign.cpp", "rv_records.cpp", "rv_somatic.cpp", "rv_bam.cpp", "rv_pool.cpp"]
 # the native generator of the large synthetic workloads (host only, its own library)
 SYNTH_SRC = "rv_synth.cpp"

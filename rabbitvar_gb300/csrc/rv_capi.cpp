@@ -134,7 +134,7 @@ DevState rv_ctx::state() const {
     s.regions = d_regions;
     s.n_regions = (int32_t)regions.size();
     s.tiles = d_tiles;
-    s.n_tiles = (int32_t)tiles.size();
+    s.n_tiles = (int32_t)n_tiles;
     s.tile_reads = d_tile_reads;
     s.tile_counter = d_counters + CNT_TILE;
     s.cells = cells;
@@ -429,6 +429,8 @@ rv_status rv_create(rv_ctx **out, const rv_params *p, int device, size_t hbm_bud
     if (e == cudaSuccess) e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
     ctx->low_priority = least;
     if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&ctx->stream, cudaStreamNonBlocking, greatest);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_up, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
     for (int i = 0; e == cudaSuccess && i < 12; i++) e = cudaEventCreate(&ctx->ev[i]);
     // a blocking-wait event for waits off the critical path (the record
@@ -437,6 +439,8 @@ rv_status rv_create(rv_ctx **out, const rv_params *p, int device, size_t hbm_bud
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_block, cudaEventBlockingSync | cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc((void **)&ctx->d_counters, 64 * sizeof(unsigned int));
     if (e == cudaSuccess) e = cudaHostAlloc((void **)&ctx->h_cnt, 64 * sizeof(unsigned int), cudaHostAllocDefault);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&ctx->d_prep, PREP_WORDS * sizeof(int));
+    if (e == cudaSuccess) e = cudaHostAlloc((void **)&ctx->h_prep, PREP_WORDS * sizeof(unsigned int), cudaHostAllocDefault);
     if (e == cudaSuccess) e = cudaMalloc((void **)&ctx->d_logfact, (size_t)kLogFact * sizeof(double));
     if (e == cudaSuccess) {
         launch_fill_logfact(ctx->d_logfact, ctx->stream);
@@ -495,19 +499,23 @@ void rv_destroy(rv_ctx *ctx) {
                     ctx->d_ftab, ctx->d_logfact, ctx->d_skip, ctx->d_patches, ctx->d_patch_keys,
                     ctx->d_list_off, ctx->d_list_bsum, ctx->d_list_idx, ctx->d_list_slots,
                     ctx->d_cons_meta, ctx->d_cons, ctx->d_ofix, ctx->d_used, ctx->d_wide, ctx->d_wide_off,
-                    ctx->d_wide_scratch, ctx->d_f35, ctx->d_tile_reads};
+                    ctx->d_wide_scratch, ctx->d_f35, ctx->d_tile_reads, ctx->d_span_lo, ctx->d_span_hi,
+                    ctx->d_cost, ctx->d_list_begin, ctx->d_rtiles, ctx->d_prep};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (ctx->h_mirror) cudaFreeHost(ctx->h_mirror);
     if (ctx->h_mirror_slots) cudaFreeHost(ctx->h_mirror_slots);
     if (ctx->h_fstage) cudaFreeHost(ctx->h_fstage);
     if (ctx->h_cnt) cudaFreeHost(ctx->h_cnt);
-    if (ctx->h_tile_reads) cudaFreeHost(ctx->h_tile_reads);
+    if (ctx->h_prep) cudaFreeHost(ctx->h_prep);
     if (ctx->h_meta) cudaFreeHost(ctx->h_meta);
     for (int i = 0; i < 12; i++)
         if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
     if (ctx->ev_block) cudaEventDestroy(ctx->ev_block);
     if (ctx->pileup_exec) cudaGraphExecDestroy(ctx->pileup_exec);
+    if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
+    if (ctx->ev_up) cudaEventDestroy(ctx->ev_up);
+    if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -531,77 +539,18 @@ rv_status rv_upload_reference(rv_ctx *ctx, const char *chr, const char *bases, i
     return RV_OK;
 }
 
-rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *regs, int n_regions,
-                          void *stream) {
-    if (!ctx || !b || (!regs && n_regions > 0) || n_regions < 0) return RV_ERR_ARG;
-    if (!ctx->d_ref) { ctx->err = "reference not uploaded"; return RV_ERR_STATE; }
-    RV_CUDA(cudaSetDevice(ctx->device));
-    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+namespace {
+
+// rv_submit_batch in two steps, so that a tumor/normal pair prepares both
+// samples before either's bulk upload is queued (one host-to-device copy
+// engine serves both: a sample's preparation would otherwise wait behind
+// the other's bases and qualities).  submit_prepare: the arrays the
+// preparation reads, its kernels (spans, classes, region bounds, read
+// lists, tiles) and the context's tables; submit_upload: the rest of the
+// batch, and the preparation's results.
+// The device read buffers sized for batch b.
+rv_status grow_reads(rv_ctx *ctx, const rv_read_batch *b) {
     const int64_t n = b->n_reads;
-    if (n < 0 || b->n_cigar_words < 0 || b->n_bases < 0) return RV_ERR_ARG;
-    PhaseTimer tm("submit");
-    // batch-wide bounds used to size the per-region cell ranges, and the
-    // base_off alignment check (host threads over chunks of reads)
-    int max_span = 1, max_lq = 1;
-    bool misaligned = false;
-    {
-        const int64_t nch = chunks_for(n, 1 << 16);
-        std::vector<int> ms((size_t)nch, 1), ml((size_t)nch, 1);
-        std::vector<uint8_t> bad((size_t)nch, 0);
-        ctx->h_span_lo.resize((size_t)n);
-        ctx->h_span_hi.resize((size_t)n);
-        ctx->h_cost.resize((size_t)n);
-        const bool widen = ctx->params.local_realign != 0;
-        parallel_chunks(n, 1 << 16, [&](int64_t k, int64_t a, int64_t e) {
-            int msp = 1, mlq = 1;
-            uint8_t bd = 0;
-            for (int64_t i = a; i < e; i++) {
-                bd |= (uint8_t)((b->base_off[i] & 31) != 0);
-                const uint32_t *c = b->cigar + b->cig_off[i];
-                const int nc = b->n_cigar[i];
-                int sp = 0, ins = 0, clip5 = 0, clip3 = 0;
-                for (int q = 0; q < nc; q++) {
-                    int o = c[q] & 15;
-                    if (o == 0 || o == 2 || o == 3 || o == 7 || o == 8) sp += (int)(c[q] >> 4);
-                    if (o == 1) ins += (int)(c[q] >> 4);
-                }
-                // the read's span as the tile windows see it (the device's
-                // read_span): soft clips and edge insertions widen it
-                if (nc > 0) {
-                    if ((c[0] & 15) == 4 || (c[0] & 15) == 1) clip5 = (int)(c[0] >> 4);
-                    if ((c[nc - 1] & 15) == 4 || (c[nc - 1] & 15) == 1) clip3 = (int)(c[nc - 1] >> 4);
-                }
-                if (!widen) ins = 0;
-                // walk-cost class: one M op; soft clips around one M op; anything else
-                uint8_t cls = 2;
-                if (nc == 1 && (c[0] & 15) == 0) cls = 0;
-                else if (nc == 2 && (((c[0] & 15) == 4 && (c[1] & 15) == 0) || ((c[0] & 15) == 0 && (c[1] & 15) == 4)))
-                    cls = 1;
-                else if (nc == 3 && (c[0] & 15) == 4 && (c[1] & 15) == 0 && (c[2] & 15) == 4)
-                    cls = 1;
-                ctx->h_cost[i] = cls;
-                const int pos1 = b->pos[i] + 1;
-                ctx->h_span_lo[i] = pos1 - clip5 - 1 - ins;
-                ctx->h_span_hi[i] = pos1 + sp + clip3 + ins;
-                msp = std::max(msp, sp);
-                mlq = std::max(mlq, (int)b->l_qseq[i]);
-            }
-            ms[k] = msp;
-            ml[k] = mlq;
-            bad[k] = bd;
-        });
-        for (int64_t k = 0; k < nch; k++) {
-            max_span = std::max(max_span, ms[k]);
-            max_lq = std::max(max_lq, ml[k]);
-            misaligned |= bad[k] != 0;
-        }
-    }
-    if (misaligned) { ctx->err = "base_off must be a multiple of 32"; return RV_ERR_ARG; }
-    tm.lap("spans");
-    ctx->n_reads = n;
-    ctx->max_lq = max_lq;
-    ctx->n_cigar_words = b->n_cigar_words;
-    ctx->n_bases = b->n_bases;
     size_t cr = ctx->cap_reads, cr2 = cr, cr3 = cr, cr4 = cr, cr5 = cr, cr6 = cr, cr7 = cr, cr8 = cr, cr9 = cr;
     rv_status st;
     size_t need = (size_t)std::max<int64_t>(n, 1);
@@ -620,6 +569,73 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
         (st = grow(ctx, ctx->d_seq, cb2, (size_t)std::max<int64_t>(b->n_bases, 32) / 2 + 64)))
         return st;
     ctx->cap_bases = cb;
+    return RV_OK;
+}
+
+// The arrays of batch b that the preparation reads, or the rest of it, on stream s.
+rv_status copy_reads(rv_ctx *ctx, const rv_read_batch *b, cudaStream_t s, bool prep_part) {
+    const int64_t n = b->n_reads;
+    if (n <= 0) return RV_OK;
+    if (prep_part) {
+        RV_CUDA(cudaMemcpyAsync(ctx->d_pos, b->pos, n * 4, cudaMemcpyHostToDevice, s));
+        RV_CUDA(cudaMemcpyAsync(ctx->d_lq, b->l_qseq, n * 4, cudaMemcpyHostToDevice, s));
+        RV_CUDA(cudaMemcpyAsync(ctx->d_ncig, b->n_cigar, n * 2, cudaMemcpyHostToDevice, s));
+        RV_CUDA(cudaMemcpyAsync(ctx->d_cigoff, b->cig_off, n * 4, cudaMemcpyHostToDevice, s));
+        RV_CUDA(cudaMemcpyAsync(ctx->d_boff, b->base_off, n * 8, cudaMemcpyHostToDevice, s));
+        RV_CUDA(cudaMemcpyAsync(ctx->d_cigar, b->cigar, b->n_cigar_words * 4, cudaMemcpyHostToDevice, s));
+    } else {
+        // bases and qualities may already be on the device (a batch of a BAM
+        // decoded there by rv_bam_read_gpu): the copy direction follows the pointers
+        RV_CUDA(cudaMemcpyAsync(ctx->d_mpos, b->mpos, n * 4, cudaMemcpyHostToDevice, s));
+        RV_CUDA(cudaMemcpyAsync(ctx->d_nm, b->nm, n * 4, cudaMemcpyHostToDevice, s));
+        RV_CUDA(cudaMemcpyAsync(ctx->d_flag, b->flag, n * 2, cudaMemcpyHostToDevice, s));
+        RV_CUDA(cudaMemcpyAsync(ctx->d_mapq, b->mapq, n, cudaMemcpyHostToDevice, s));
+        RV_CUDA(cudaMemcpyAsync(ctx->d_seq, b->seq, (size_t)(b->n_bases + 1) / 2, cudaMemcpyDefault, s));
+        RV_CUDA(cudaMemcpyAsync(ctx->d_qual, b->qual, (size_t)b->n_bases, cudaMemcpyDefault, s));
+    }
+    return RV_OK;
+}
+
+// Queues the whole of batch b into the context's read buffers on its copy
+// stream, behind the context's last pileup chain (ev[1]): the read arrays
+// are not read again after that chain (the realigner, the scoring and the
+// formatting of the batch in flight use the maps, and the host arrays), so
+// the next batch's upload overlaps them.  The next rv_submit_batch of b on
+// this context waits for it instead of copying.
+rv_status early_upload(rv_ctx *ctx, const rv_read_batch *b) {
+    if (!b || b->n_reads < 0 || b->n_cigar_words < 0 || b->n_bases < 0) return RV_OK;
+    rv_status st = grow_reads(ctx, b);
+    if (st) return st;
+    RV_CUDA(cudaStreamWaitEvent(ctx->copy_stream, ctx->ev[1], 0));
+    if ((st = copy_reads(ctx, b, ctx->copy_stream, true)) || (st = copy_reads(ctx, b, ctx->copy_stream, false)))
+        return st;
+    RV_CUDA(cudaEventRecord(ctx->ev_up, ctx->copy_stream));
+    ctx->early_batch = b;
+    return RV_OK;
+}
+
+rv_status submit_prepare(rv_ctx *ctx, const rv_read_batch *b, const rv_region *regs, int n_regions,
+                         cudaStream_t s) {
+    if (!ctx || !b || (!regs && n_regions > 0) || n_regions < 0) return RV_ERR_ARG;
+    if (!ctx->d_ref) { ctx->err = "reference not uploaded"; return RV_ERR_STATE; }
+    RV_CUDA(cudaSetDevice(ctx->device));
+    const int64_t n = b->n_reads;
+    if (n < 0 || b->n_cigar_words < 0 || b->n_bases < 0) return RV_ERR_ARG;
+    ctx->stage = 0;
+    PhaseTimer tm("submit");
+    ctx->n_reads = n;
+    ctx->n_cigar_words = b->n_cigar_words;
+    ctx->n_bases = b->n_bases;
+    rv_status st;
+    ctx->batch_early = ctx->early_batch == b;
+    ctx->early_batch = nullptr;
+    if ((st = grow_reads(ctx, b))) return st;
+    size_t need = (size_t)std::max<int64_t>(n, 1);
+    size_t cp = ctx->cap_prep, cp2 = cp, cp3 = cp;
+    if ((st = grow(ctx, ctx->d_span_lo, cp, need)) || (st = grow(ctx, ctx->d_span_hi, cp2, need)) ||
+        (st = grow(ctx, ctx->d_cost, cp3, need)))
+        return st;
+    ctx->cap_prep = std::min(cp, std::min(cp2, cp3));
     ctx->io_h2d = n * (4 + 4 + 4 + 4 + 2 + 2 + 1 + 4 + 8) + b->n_cigar_words * 4;
     {
         cudaPointerAttributes pa;
@@ -629,7 +645,82 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
         if (!dev_bases) ctx->io_h2d += (b->n_bases + 1) / 2 + b->n_bases;
     }
     ctx->io_d2h = 0;
-    tm.lap("prep+alloc");
+    // the arrays the batch's preparation reads go up first (the rest is
+    // queued behind the preparation's kernels), unless the whole batch was
+    // queued early on the copy stream
+    if (ctx->batch_early) RV_CUDA(cudaStreamWaitEvent(s, ctx->ev_up, 0));
+    else if ((st = copy_reads(ctx, b, s, true))) return st;
+    // the batch's longest reference span and read (the region records'
+    // bounds) on host threads, and each read's CIGAR inside the batch's
+    // words; every other per-read step is the device's
+    int max_span = 1, max_lq = 1;
+    {
+        const int64_t nch = chunks_for(n, 1 << 16);
+        std::vector<int> ms((size_t)nch, 1), ml((size_t)nch, 1);
+        std::vector<uint8_t> bad((size_t)nch, 0);
+        parallel_chunks(n, 1 << 16, [&](int64_t k, int64_t a, int64_t e) {
+            int msp = 1, mlq = 1;
+            uint8_t bd = 0;
+            for (int64_t i = a; i < e; i++) {
+                const int nc = b->n_cigar[i];
+                if ((int64_t)b->cig_off[i] + nc > b->n_cigar_words) {
+                    bd = 1;
+                    continue;
+                }
+                const uint32_t *c = b->cigar + b->cig_off[i];
+                int sp = 0;
+                for (int q = 0; q < nc; q++) {
+                    const uint32_t o = c[q] & 15u;
+                    if (o == 0 || o == 2 || o == 3 || o == 7 || o == 8) sp += (int)(c[q] >> 4);
+                }
+                msp = std::max(msp, sp);
+                mlq = std::max(mlq, (int)b->l_qseq[i]);
+            }
+            ms[k] = msp;
+            ml[k] = mlq;
+            bad[k] = bd;
+        });
+        bool cig_bad = false;
+        for (int64_t k = 0; k < nch; k++) {
+            max_span = std::max(max_span, ms[k]);
+            max_lq = std::max(max_lq, ml[k]);
+            cig_bad |= bad[k] != 0;
+        }
+        if (cig_bad) { ctx->err = "a read's CIGAR lies outside the batch's CIGAR words"; return RV_ERR_ARG; }
+    }
+    // per read on the device: its span, walk-cost class and the record
+    // checks (read back with the tile count before the pileup)
+    RV_CUDA(cudaMemsetAsync(ctx->d_prep, 0, PREP_WORDS * 4, s));
+    {
+        ReadPrepIn in;
+        in.n = n;
+        in.pos = ctx->d_pos;
+        in.l_qseq = ctx->d_lq;
+        in.n_cigar = ctx->d_ncig;
+        in.cig_off = ctx->d_cigoff;
+        in.cigar = ctx->d_cigar;
+        in.base_off = ctx->d_boff;
+        in.n_cigar_words = b->n_cigar_words;
+        in.n_bases = b->n_bases;
+        in.widen = ctx->params.local_realign != 0;
+        ReadPrepOut out;
+        out.span_lo = ctx->d_span_lo;
+        out.span_hi = ctx->d_span_hi;
+        out.cost = ctx->d_cost;
+        out.words = ctx->d_prep;
+        // every buffer the kernel touches exists and holds the batch
+        if (n > 0 && (!in.pos || !in.l_qseq || !in.n_cigar || !in.cig_off || !in.cigar || !in.base_off ||
+                      !out.span_lo || !out.span_hi || !out.cost || !out.words || ctx->cap_prep < (size_t)n ||
+                      ctx->cap_reads < (size_t)n || ctx->cap_cigar < (size_t)b->n_cigar_words)) {
+            ctx->err = "batch preparation buffers missing";
+            return RV_ERR_STATE;
+        }
+        launch_read_prep(in, out, ctx->sm_count, s);
+        RV_CUDA(cudaGetLastError());
+    }
+    ctx->max_span = max_span;
+    ctx->max_lq = max_lq;
+    tm.lap("read prep");
     // -k 1: the realigner reads the batch's alignments again from the
     // caller's arrays (noPassingReads)
     ctx->hb_n = ctx->params.local_realign ? n : 0;
@@ -641,7 +732,7 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
     const int pad = max_span + max_lq + 4;
     const rv_params &P = ctx->params;
     ctx->regions.clear();
-    ctx->tiles.clear();
+    ctx->n_tiles = 0;
     ctx->score_base.clear();
     std::vector<int64_t> list_begin;  // per region: its first entry in the tile read list
     int64_t list_total = 0;
@@ -674,70 +765,8 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
     }
     list_begin.push_back(list_total);
     if (n > (int64_t)UINT32_MAX) { ctx->err = "more than 2^32 reads in one batch"; return RV_ERR_ARG; }
-    if ((st = ensure_pinned(ctx, (void **)&ctx->h_tile_reads, ctx->cap_h_tile_reads, (size_t)list_total * 4)))
-        return st;
     ctx->n_tile_reads = (size_t)list_total;
-    std::vector<std::vector<Tile>> rtiles((size_t)n_regions);
-    // per region, on host threads: its read list (the reads whose CIGAR is
-    // one M op, then those with soft clips around one M op, then the others,
-    // file order within each: a tile holds reads of one kind, of about equal
-    // walk cost, so its threads reach the tile's end together), its tiles
-    // over that list, sized so a tile's window fits
-    // kTileW positions, and from the read spans: the reads' reach, the
-    // edge-read flag and each tile's window start (the lowest span start of
-    // its non-edge reads)
-    std::atomic<int> span_bad{0};
-    parallel_for(n_regions, [&](int64_t r) {
-        Region &R = ctx->regions[r];
-        if (R.r1 <= R.r0) return;
-        uint32_t *list = ctx->h_tile_reads + list_begin[r];
-        int64_t bound[4] = {0, 0, 0, 0};
-        for (int cls = 0; cls < 3; cls++) {
-            int64_t k = bound[cls];
-            for (int64_t i = R.r0; i < R.r1; i++)
-                if (ctx->h_cost[i] == cls) list[k++] = (uint32_t)i;
-            bound[cls + 1] = k;
-        }
-        const double len = (double)(R.end - R.start + 1 + 2 * max_lq);
-        const double usable = (double)kTileW - max_span - max_lq - 16.0;  // window = start span + read extent
-        std::vector<Tile> &tl = rtiles[(size_t)r];
-        for (int part = 0; part < 3; part++) {
-            const int64_t a0 = bound[part], a1 = bound[part + 1];
-            if (a1 <= a0) continue;
-            const double dens = (a1 - a0) / len;
-            const int64_t tr = (int64_t)std::max(32.0, std::min((double)kTileReads, usable * dens));
-            for (int64_t a = a0; a < a1; a += tr) {
-                Tile t;
-                t.region = (int32_t)r;
-                t.r0 = list_begin[r] + a;
-                t.r1 = list_begin[r] + std::min(a1, a + tr);
-                t.wlo = 0;
-                tl.push_back(t);
-            }
-        }
-        int lo = INT32_MAX, hi = INT32_MIN, reach = 0;
-        for (int64_t i = R.r0; i < R.r1; i++) {
-            lo = std::min(lo, std::max(ctx->h_span_lo[i], 1));
-            hi = std::max(hi, ctx->h_span_hi[i]);
-            reach = std::max(reach, ctx->h_span_hi[i] - (b->pos[i] + 1));
-        }
-        R.span_lo = lo;
-        R.span_hi = hi;
-        R.reach = reach;
-        R.serial = hi + kEdgeMargin > R.we ? 1 : 0;
-        if (lo < R.clo || hi > R.chi) span_bad.store(1);
-        for (Tile &t : tl) {
-            int wlo = INT32_MAX;
-            for (int64_t e = t.r0; e < t.r1; e++) {
-                const uint32_t i = ctx->h_tile_reads[e];
-                if (ctx->h_span_hi[i] + kEdgeMargin <= R.we) wlo = std::min(wlo, ctx->h_span_lo[i]);
-            }
-            t.wlo = std::max(wlo, R.clo);
-        }
-    });
-    for (const std::vector<Tile> &tl : rtiles) ctx->tiles.insert(ctx->tiles.end(), tl.begin(), tl.end());
-    tm.lap("regions+tiles");
-    if (span_bad.load()) { ctx->err = "read span outside the region's cell range"; return RV_ERR_UNSUPPORTED; }
+    size_t &tile_bound = ctx->tile_bound;
     ctx->n_score = score;
     ctx->n_cells = cell_base + 4;
     // -t: RecordPreprocessor::next_record's duplicate filter
@@ -790,43 +819,75 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
         ctx->io_h2d += n;
         ctx->use_skip = true;
     }
-    size_t creg = ctx->cap_regions, ct = ctx->cap_tiles, creg2 = ctx->cap_regions;
-    if ((st = grow(ctx, ctx->d_regions, creg, ctx->regions.size() + 1)) ||
-        (st = grow(ctx, ctx->d_score_base, creg2, ctx->regions.size() + 1)) ||
-        (st = grow(ctx, ctx->d_tiles, ct, ctx->tiles.size() + 1)))
-        return st;
-    ctx->cap_regions = creg;
-    ctx->cap_tiles = ct;
+    // region records, score bases and list starts through the context's
+    // pinned staging; then per region on the device: its bounds, read list
+    // (reads grouped by walk-cost class: one M op, soft clips around one M
+    // op, the rest; file order within each, so a tile holds reads of about
+    // equal walk cost and its threads reach the tile's end together) and
+    // tiles over that list, sized so a tile's window fits kTileW positions,
+    // each tile's window starting at the lowest span start of its non-edge
+    // reads
     {
-        // regions, score bases and tiles through the context's pinned staging
+        size_t creg = ctx->cap_regions, creg2 = ctx->cap_regions, creg3 = ctx->cap_regions, creg4 = ctx->cap_regions;
+        const size_t nr1 = ctx->regions.size() + 1;
+        if ((st = grow(ctx, ctx->d_regions, creg, nr1)) || (st = grow(ctx, ctx->d_score_base, creg2, nr1)) ||
+            (st = grow(ctx, ctx->d_list_begin, creg3, nr1)) || (st = grow(ctx, ctx->d_rtiles, creg4, nr1)))
+            return st;
+        ctx->cap_regions = std::min(std::min(creg, creg2), std::min(creg3, creg4));
+        // tiles: at most one per 32 reads of each class segment, plus one per segment
+        tile_bound = (size_t)list_total / 32 + 3 * ctx->regions.size() + 1;
+        size_t ct = ctx->cap_tiles, cl = ctx->cap_tile_reads;
+        if ((st = grow(ctx, ctx->d_tiles, ct, tile_bound)) ||
+            (st = grow(ctx, ctx->d_tile_reads, cl, (size_t)list_total + 1)))
+            return st;
+        ctx->cap_tiles = ct;
+        ctx->cap_tile_reads = cl;
         auto up16 = [](size_t x) { return (x + 15) & ~(size_t)15; };
         const size_t b_reg = up16(ctx->regions.size() * sizeof(Region)), b_sb = up16(ctx->score_base.size() * 8);
-        const size_t b_tl = up16(ctx->tiles.size() * sizeof(Tile));
-        if ((st = ensure_pinned(ctx, (void **)&ctx->h_meta, ctx->cap_meta, b_reg + b_sb + b_tl + 16))) return st;
+        const size_t b_lb = up16(list_begin.size() * 8);
+        if ((st = ensure_pinned(ctx, (void **)&ctx->h_meta, ctx->cap_meta, b_reg + b_sb + b_lb + 16))) return st;
         char *h = ctx->h_meta;
         if (!ctx->regions.empty()) {
             memcpy(h, ctx->regions.data(), ctx->regions.size() * sizeof(Region));
             memcpy(h + b_reg, ctx->score_base.data(), ctx->score_base.size() * 8);
+            memcpy(h + b_reg + b_sb, list_begin.data(), list_begin.size() * 8);
             RV_CUDA(cudaMemcpyAsync(ctx->d_regions, h, ctx->regions.size() * sizeof(Region), cudaMemcpyHostToDevice, s));
             RV_CUDA(cudaMemcpyAsync(ctx->d_score_base, h + b_reg, ctx->score_base.size() * 8, cudaMemcpyHostToDevice,
                                     s));
-        }
-        if (!ctx->tiles.empty()) {
-            memcpy(h + b_reg + b_sb, ctx->tiles.data(), ctx->tiles.size() * sizeof(Tile));
-            RV_CUDA(cudaMemcpyAsync(ctx->d_tiles, h + b_reg + b_sb, ctx->tiles.size() * sizeof(Tile),
+            RV_CUDA(cudaMemcpyAsync(ctx->d_list_begin, h + b_reg + b_sb, list_begin.size() * 8,
                                     cudaMemcpyHostToDevice, s));
+            if (!ctx->d_regions || !ctx->d_rtiles || !ctx->d_list_begin || !ctx->d_tiles || !ctx->d_tile_reads ||
+                !ctx->d_span_lo || !ctx->d_span_hi || !ctx->d_cost || !ctx->d_prep || !ctx->d_pos) {
+                ctx->err = "batch preparation buffers missing";
+                return RV_ERR_STATE;
+            }
+            RegionPrepArgs ra;
+            ra.regions = ctx->d_regions;
+            ra.span_lo = ctx->d_span_lo;
+            ra.span_hi = ctx->d_span_hi;
+            ra.pos = ctx->d_pos;
+            ra.cost = ctx->d_cost;
+            ra.max_span = max_span;
+            ra.max_lq = max_lq;
+            ra.rtiles = ctx->d_rtiles;
+            ra.words = ctx->d_prep;
+            launch_region_prep(ra, (int)ctx->regions.size(), s);
+            RegionFillArgs fa;
+            fa.regions = ctx->d_regions;
+            fa.rtiles = ctx->d_rtiles;
+            fa.list_begin = ctx->d_list_begin;
+            fa.span_lo = ctx->d_span_lo;
+            fa.span_hi = ctx->d_span_hi;
+            fa.cost = ctx->d_cost;
+            fa.list = ctx->d_tile_reads;
+            fa.tiles = ctx->d_tiles;
+            launch_region_fill(fa, (int)ctx->regions.size(), s);
+            RV_CUDA(cudaGetLastError());
         }
+        RV_CUDA(cudaMemcpyAsync(ctx->h_prep, ctx->d_prep, PREP_WORDS * 4, cudaMemcpyDeviceToHost, s));
+        RV_CUDA(cudaEventRecord(ctx->ev[10], s));
     }
-    {
-        size_t cl = ctx->cap_tile_reads;
-        if ((st = grow(ctx, ctx->d_tile_reads, cl, ctx->n_tile_reads + 1))) return st;
-        ctx->cap_tile_reads = cl;
-        if (ctx->n_tile_reads)
-            RV_CUDA(cudaMemcpyAsync(ctx->d_tile_reads, ctx->h_tile_reads, ctx->n_tile_reads * 4,
-                                    cudaMemcpyHostToDevice, s));
-        ctx->io_h2d += (int64_t)ctx->n_tile_reads * 4;
-    }
-    tm.lap("region+tile copies");
+    tm.lap("regions+tiles");
     // cells: 7 x 4 words + first (4 words) per position, plus cov, kflags, head
     size_t need_cells = (size_t)ctx->n_cells;
     if (need_cells > ctx->cap_cells || !ctx->d_cellmem) {
@@ -906,29 +967,72 @@ rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *
         ctx->cand_cap = want_cand;
     }
     tm.lap("wide+candidates");
-    // the read arrays last: the small pageable copies above are staged before
-    // these large pinned copies are queued, so none of them waits on the batch
-    // upload
-    if (n > 0) {
-        RV_CUDA(cudaMemcpyAsync(ctx->d_pos, b->pos, n * 4, cudaMemcpyHostToDevice, s));
-        RV_CUDA(cudaMemcpyAsync(ctx->d_mpos, b->mpos, n * 4, cudaMemcpyHostToDevice, s));
-        RV_CUDA(cudaMemcpyAsync(ctx->d_nm, b->nm, n * 4, cudaMemcpyHostToDevice, s));
-        RV_CUDA(cudaMemcpyAsync(ctx->d_lq, b->l_qseq, n * 4, cudaMemcpyHostToDevice, s));
-        RV_CUDA(cudaMemcpyAsync(ctx->d_flag, b->flag, n * 2, cudaMemcpyHostToDevice, s));
-        RV_CUDA(cudaMemcpyAsync(ctx->d_ncig, b->n_cigar, n * 2, cudaMemcpyHostToDevice, s));
-        RV_CUDA(cudaMemcpyAsync(ctx->d_mapq, b->mapq, n, cudaMemcpyHostToDevice, s));
-        RV_CUDA(cudaMemcpyAsync(ctx->d_cigoff, b->cig_off, n * 4, cudaMemcpyHostToDevice, s));
-        RV_CUDA(cudaMemcpyAsync(ctx->d_boff, b->base_off, n * 8, cudaMemcpyHostToDevice, s));
-        RV_CUDA(cudaMemcpyAsync(ctx->d_cigar, b->cigar, b->n_cigar_words * 4, cudaMemcpyHostToDevice, s));
-        // bases and qualities may already be on the device (a batch of a
-        // BAM decoded there, rv_bam_read_gpu): the copy direction follows
-        // the pointers
-        RV_CUDA(cudaMemcpyAsync(ctx->d_seq, b->seq, (size_t)(b->n_bases + 1) / 2, cudaMemcpyDefault, s));
-        RV_CUDA(cudaMemcpyAsync(ctx->d_qual, b->qual, (size_t)b->n_bases, cudaMemcpyDefault, s));
+    return RV_OK;
+}
+
+rv_status submit_upload(rv_ctx *ctx, const rv_read_batch *b, cudaStream_t s) {
+    const int64_t n = b->n_reads;
+    // the rest of the batch (the bases and qualities are most of it) after
+    // the preparation's kernels
+    if (!ctx->batch_early) {
+        rv_status st = copy_reads(ctx, b, s, false);
+        if (st) return st;
     }
-    tm.lap("queue copies");
+    ctx->prep_pending = true;
     ctx->stage = 1;
     return RV_OK;
+}
+
+}  // namespace
+
+// The batch preparation's results, queued by rv_submit_batch and waited for
+// here, before the first kernel that needs them (the pileup): the device's
+// record checks and the tile count.
+rv_status prep_finish(rv_ctx *ctx) {
+    if (!ctx->prep_pending) return RV_OK;
+    ctx->prep_pending = false;
+    RV_CUDA(cudaEventSynchronize(ctx->ev[10]));
+    const unsigned int *w = ctx->h_prep;
+    rv_status st = RV_OK;
+    if (w[PREP_MISALIGNED] & 1u) { ctx->err = "base_off must be a multiple of 32"; st = RV_ERR_ARG; }
+    else if (w[PREP_MISALIGNED] & 2u) { ctx->err = "a read's CIGAR lies outside the batch's CIGAR words"; st = RV_ERR_ARG; }
+    else if (w[PREP_MISALIGNED] & 4u) { ctx->err = "a read's bases lie outside the batch's bases"; st = RV_ERR_ARG; }
+    else if ((int)w[PREP_MAX_SPAN] > ctx->max_span || (int)w[PREP_MAX_LQ] > ctx->max_lq) {
+        ctx->err = "the device's read spans disagree with the host's";
+        st = RV_ERR_UNSUPPORTED;
+    } else if (w[PREP_SPAN_BAD]) {
+        ctx->err = "read span outside the region's cell range";
+        st = RV_ERR_UNSUPPORTED;
+    }
+    if (!st) {
+        ctx->n_tiles = ctx->regions.empty() ? 0 : (int64_t)w[PREP_N_TILES];
+        if ((size_t)ctx->n_tiles > ctx->tile_bound) { ctx->err = "tile count above its bound"; st = RV_ERR_UNSUPPORTED; }
+    }
+    if (st) ctx->stage = 0;
+    return st;
+}
+
+namespace {
+
+// Both samples of a pair: both preparations, then both uploads.
+rv_status submit_pair(rv_ctx *tumor, rv_ctx *normal, const rv_read_batch *bt, const rv_read_batch *bn,
+                      const rv_region *regs, int n_regions) {
+    rv_status s = submit_prepare(tumor, bt, regs, n_regions, tumor->stream);
+    if (!s && (s = submit_prepare(normal, bn, regs, n_regions, normal->stream))) tumor->err = normal->err;
+    if (!s) s = submit_upload(tumor, bt, tumor->stream);
+    if (!s && (s = submit_upload(normal, bn, normal->stream))) tumor->err = normal->err;
+    return s;
+}
+
+}  // namespace
+
+rv_status rv_submit_batch(rv_ctx *ctx, const rv_read_batch *b, const rv_region *regs, int n_regions,
+                          void *stream) {
+    if (!ctx || !b) return RV_ERR_ARG;
+    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+    rv_status st = submit_prepare(ctx, b, regs, n_regions, s);
+    if (st) return st;
+    return submit_upload(ctx, b, s);
 }
 
 namespace {
@@ -1006,6 +1110,8 @@ rv_status launch_pileup_graph(rv_ctx *ctx, cudaStream_t s, int resident, int var
 rv_status pileup_launch(rv_ctx *ctx, cudaStream_t s) {
     if (ctx->stage < 1) { ctx->err = "rv_pileup before rv_submit_batch"; return RV_ERR_STATE; }
     RV_CUDA(cudaSetDevice(ctx->device));
+    rv_status ps = prep_finish(ctx);
+    if (ps) return ps;
     // autotuner: unless RV_PILEUP_VARIANT pins one, the first batch of the
     // context runs the whole pileup chain once with every tile-kernel variant
     // (register budget x warp aggregation), timing the tile kernel of each;
@@ -1017,12 +1123,12 @@ rv_status pileup_launch(rv_ctx *ctx, cudaStream_t s) {
     // blocks of the variant resident at once (sets the tile kernel's per-block quota)
     auto resident_of = [&](int v) {
         const int per_sm = std::max(1, pileup_blocks_per_sm(v));
-        return std::max(1, std::min<int>((int)ctx->tiles.size(), per_sm * ctx->sm_count));
+        return (int)std::max<int64_t>(1, std::min<int64_t>(ctx->n_tiles, (int64_t)per_sm * ctx->sm_count));
     };
     if (pinned) {
         variant = std::max(0, std::min(nvar - 1, atoi(pin)));
     } else {
-        if (ctx->variant_runs < nvar && !ctx->tiles.empty()) {
+        if (ctx->variant_runs < nvar && ctx->n_tiles > 0) {
             for (int v = 0; v < nvar; v++) {
                 rv_status ts = queue_pileup_chain(ctx, s, resident_of(v), v, true);
                 if (ts != RV_OK) return ts;
@@ -1459,8 +1565,11 @@ rv_status pair_launch(rv_ctx *tumor, rv_ctx *normal, cudaEvent_t after = nullptr
 // Waits for the tumor's pileup and realigns it on the host (while the
 // normal's kernels run), then the normal's.  `between` runs after the
 // tumor's pileup finished and before its realigner (the stream uses it to
-// queue the next batch's pileups behind this one's).
-rv_status pair_finish(rv_ctx *tumor, rv_ctx *normal, const std::function<rv_status()> &between) {
+// queue the next batch's pileups behind this one's, and the upload of the
+// tumor's batch after next); `after_normal` after the normal's pileup
+// finished (the upload of the normal's batch after next).
+rv_status pair_finish(rv_ctx *tumor, rv_ctx *normal, const std::function<rv_status()> &between,
+                      const std::function<rv_status()> &after_normal = nullptr) {
     rv_status st = pileup_finish(tumor, tumor->stream);
     if (st) {
         pileup_finish(normal, normal->stream);
@@ -1475,6 +1584,7 @@ rv_status pair_finish(rv_ctx *tumor, rv_ctx *normal, const std::function<rv_stat
         return st;
     }
     if ((st = pileup_finish(normal, normal->stream))) { tumor->err = normal->err; return st; }
+    if (after_normal && (st = after_normal())) return st;
     if ((st = rv_realign(normal, nullptr))) { tumor->err = normal->err; return st; }
     return RV_OK;
 }
@@ -1526,9 +1636,9 @@ rv_status rv_call_somatic_stream(rv_ctx *tumor0, rv_ctx *normal0, rv_ctx *tumor1
     auto submit = [&](int pi, int64_t k) -> rv_status {
         const rv_somatic_job &j = jobs[k];
         if (!j.tumor && !j.normal) return resident(pi);
-        rv_status s = rv_submit_batch(T[pi], j.tumor, j.regions, j.n_regions, nullptr);
-        if (!s && (s = rv_submit_batch(N[pi], j.normal, j.regions, j.n_regions, nullptr))) T[pi]->err = N[pi]->err;
-        return s;
+        // both samples prepared before either's bulk upload
+        return (j.tumor && j.normal) ? submit_pair(T[pi], N[pi], j.tumor, j.normal, j.regions, j.n_regions)
+                                     : (rv_status)RV_ERR_ARG;
     };
     rv_status s = RV_OK;
     int bad = 0;  // the pair whose context holds the error message
@@ -1573,9 +1683,25 @@ rv_status rv_call_somatic_stream(rv_ctx *tumor0, rv_ctx *normal0, rv_ctx *tumor1
                 }
                 next_in_flight = true;
             }
+            // job k + 2 runs on this pair: its tumor reads go up now (the
+            // tumor's pileup chain is done with the read buffers)
+            if (k + 2 < n_jobs && jobs[k + 2].tumor && jobs[k + 2].normal) {
+                rv_status u = early_upload(T[pi], jobs[k + 2].tumor);
+                if (u) return u;
+            }
             return (rv_status)RV_OK;
         };
-        if ((s = pair_finish(T[pi], N[pi], between))) break;
+        auto after_normal = [&]() -> rv_status {
+            if (k + 2 < n_jobs && jobs[k + 2].tumor && jobs[k + 2].normal) {
+                rv_status u = early_upload(N[pi], jobs[k + 2].normal);
+                if (u) {
+                    T[pi]->err = N[pi]->err;
+                    return u;
+                }
+            }
+            return (rv_status)RV_OK;
+        };
+        if ((s = pair_finish(T[pi], N[pi], between, after_normal))) break;
         tm.lap("realign");
         if ((s = rv_score_pair(T[pi], N[pi]))) break;
         tm.lap("score");
@@ -1588,9 +1714,9 @@ rv_status rv_call_somatic_stream(rv_ctx *tumor0, rv_ctx *normal0, rv_ctx *tumor1
             rv_status st = rv_format_somatic(t, n, j->sample, j->gene, nullptr, nullptr, nullptr);
             // the records stay in t->text until this pair is formatted again
             if (!st && next && (next->tumor || next->normal)) {
-                st = rv_submit_batch(t, next->tumor, next->regions, next->n_regions, nullptr);
-                if (!st && (st = rv_submit_batch(n, next->normal, next->regions, next->n_regions, nullptr)))
-                    t->err = n->err;
+                st = (next->tumor && next->normal)
+                         ? submit_pair(t, n, next->tumor, next->normal, next->regions, next->n_regions)
+                         : (rv_status)RV_ERR_ARG;
             }
             *out = st;
         });
@@ -1606,6 +1732,8 @@ rv_status rv_call_somatic_stream(rv_ctx *tumor0, rv_ctx *normal0, rv_ctx *tumor1
         s = finish(bad, n_jobs - 1);
     }
     join_all();
+    // an upload queued for a job that did not run stays unused
+    for (rv_ctx *c : all) c->early_batch = nullptr;
     if (s && bad != 0) T[0]->err = T[bad]->err;
     return s;
 }
@@ -1631,8 +1759,8 @@ rv_status rv_call_somatic(rv_ctx *tumor, rv_ctx *normal, const rv_read_batch *tu
                           int64_t *n_records) {
     if (!tumor || !normal) return RV_ERR_ARG;
     rv_status s;
-    if ((s = rv_submit_batch(tumor, tumor_reads, regions, n_regions, nullptr))) return s;
-    if ((s = rv_submit_batch(normal, normal_reads, regions, n_regions, nullptr))) { tumor->err = normal->err; return s; }
+    if (!tumor_reads || !normal_reads) return RV_ERR_ARG;
+    if ((s = submit_pair(tumor, normal, tumor_reads, normal_reads, regions, n_regions))) return s;
     if ((s = rv_pileup_realign_pair(tumor, normal))) return s;
     if ((s = rv_score_pair(tumor, normal))) return s;
     return rv_format_somatic(tumor, normal, sample, gene, text, text_len, n_records);

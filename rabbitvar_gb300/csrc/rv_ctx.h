@@ -20,6 +20,9 @@ void launch_region_reset(const DevState &st, cudaStream_t s);
 cudaError_t launch_pileup(const DevState &st, const DevParams &P, int resident_blocks, cudaStream_t s, int variant,
                           int priority);
 int tile_quota(int64_t n_tiles, int resident_blocks);
+void launch_read_prep(const ReadPrepIn &in, const ReadPrepOut &out, int sm_count, cudaStream_t s);
+void launch_region_prep(const RegionPrepArgs &a, int n_regions, cudaStream_t s);
+void launch_region_fill(const RegionFillArgs &a, int n_regions, cudaStream_t s);
 int pileup_variants();
 void launch_serial(const DevState &st, const DevParams &P, cudaStream_t s);
 void launch_edge_detect(const DevState &st, const DevParams &P, cudaStream_t s);
@@ -143,19 +146,33 @@ struct rv_ctx {
     const uint16_t *hb_flag = nullptr, *hb_ncig = nullptr;
     const uint32_t *hb_cigoff = nullptr, *hb_cigar = nullptr;
     int64_t hb_n = 0;
-    std::vector<int32_t> h_span_lo, h_span_hi;  // per read: the span the tile windows cover
-    std::vector<uint8_t> h_cost;                // per read: walk-cost class (0 one M op, 1 clips around one M, 2 other)
 
     // regions / tiles
     std::vector<rv::Region> regions;
-    std::vector<rv::Tile> tiles;
-    // pinned host staging of the batch's tile read lists (per region: its
-    // reads by walk-cost class) and of the region and tile records, so their
-    // copies queue without waiting behind the previous batch's uploads
-    uint32_t *h_tile_reads = nullptr;
-    size_t cap_h_tile_reads = 0, n_tile_reads = 0;
+    int64_t n_tiles = 0;
+    size_t tile_bound = 0;    // tiles the device list holds (the preparation's bound)
+    // pinned host staging of the region records, score bases and list
+    // starts, so their copies queue without waiting behind other uploads
     char *h_meta = nullptr;
     size_t cap_meta = 0;
+    size_t n_tile_reads = 0;
+    // batch preparation on the device: per read its span and walk-cost
+    // class; per region its list start and tile segments
+    int32_t *d_span_lo = nullptr, *d_span_hi = nullptr;
+    uint8_t *d_cost = nullptr;
+    size_t cap_prep = 0;
+    int64_t *d_list_begin = nullptr;
+    rv::RegionTiles *d_rtiles = nullptr;
+    // a stream of batches uploads the next batch's reads on the copy stream
+    // as soon as the last pileup chain no longer reads them (early_upload)
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_up = nullptr;                 // that upload's end
+    const rv_read_batch *early_batch = nullptr;  // the batch it carries
+    bool batch_early = false;                    // the submitted batch came that way
+    int *d_prep = nullptr;                // the preparation's result words (PREP_*)
+    unsigned int *h_prep = nullptr;       // their pinned host copy
+    bool prep_pending = false;            // results queued, not yet read (read before the pileup)
+    int max_span = 1;                     // the batch's longest reference span (host scan)
     std::vector<int64_t> score_base;
     rv::Region *d_regions = nullptr;
     rv::Tile *d_tiles = nullptr;

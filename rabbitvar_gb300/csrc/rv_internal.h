@@ -85,6 +85,50 @@ struct Tile {
 // positions of the reference window's end.
 constexpr int kEdgeMargin = 8;
 
+// Batch preparation on the device (rv_prep.cu): result words
+// (PREP_MISALIGNED bits: 1 base_off not a multiple of 32, 2 CIGAR outside the
+// batch's words, 4 bases outside the batch's bases)
+enum { PREP_MAX_SPAN = 0, PREP_MAX_LQ = 1, PREP_MISALIGNED = 2, PREP_SPAN_BAD = 3, PREP_N_TILES = 4, PREP_WORDS = 8 };
+
+struct ReadPrepIn {
+    int64_t n;
+    const int32_t *pos, *l_qseq;
+    const uint16_t *n_cigar;
+    const uint32_t *cig_off, *cigar;
+    const uint64_t *base_off;
+    int64_t n_cigar_words, n_bases;  // bounds of every read's CIGAR and bases (checked)
+    int widen;               // -k 1: edge insertions widen the span
+};
+struct ReadPrepOut {
+    int32_t *span_lo, *span_hi;
+    uint8_t *cost;           // walk-cost class: 0 one M op, 1 soft clips around one M op, 2 other
+    int *words;
+};
+// Per region: its read list's class segments and their tiles.
+struct RegionTiles {
+    long long start[3], count[3];  // list segment of each class (relative to the region's list start)
+    long long per[3];              // reads per tile of each class
+    int tile0[3];                  // first tile of each class (relative to base)
+    int n_tiles, base;             // tiles of the region; its first tile in the batch's list
+};
+struct RegionPrepArgs {
+    Region *regions;
+    const int32_t *span_lo, *span_hi, *pos;
+    const uint8_t *cost;
+    int max_span, max_lq;
+    RegionTiles *rtiles;
+    int *words;
+};
+struct RegionFillArgs {
+    const Region *regions;
+    const RegionTiles *rtiles;
+    const int64_t *list_begin;
+    const int32_t *span_lo, *span_hi;
+    const uint8_t *cost;
+    uint32_t *list;
+    Tile *tiles;
+};
+
 // Device copy of rv_params plus derived values.
 struct DevParams {
     double goodq, freq, qratio, mapq_filter, lofreq, bias;

@@ -64,9 +64,11 @@ def test_somatic_tiles_match_golden():
 
 
 def test_somatic_stream_matches_calls():
-    """rv_call_somatic_stream over three batches (two context pairs, records
-    formatted on a host thread while the next batch is piled up) gives the
-    records of one call per batch, in order."""
+    """rv_call_somatic_stream over five batches (two context pairs, records
+    formatted on a host thread while the next batch is piled up, a batch's
+    reads uploaded while the batch before it on the same pair is realigned;
+    batches of different sizes, so an early upload replaces a larger or
+    smaller batch) gives the records of one call per batch, in order."""
     from rabbitvar_gb300 import api, synth
     g, _, t, n = synth.somatic_mix(0x5EED0051)
     regions = [[(1, g.shape[0])], [(1, 3000), (3001, 9000), (9001, g.shape[0])], [(8001, 20000)]]
@@ -74,11 +76,17 @@ def test_somatic_stream_matches_calls():
     pair = api.SomaticPair(api.default_params(**params))
     pair.upload_reference(t.contig, synth.genome_str(g).encode())
     bt, bn = api.Batch.from_readset(t), api.Batch.from_readset(n)
-    want = [pair.call(bt, bn, rg, "T", t.contig) for rg in regions]
+    # the first half of each sample's reads as a second batch
+    ht = api.Batch.from_readset(synth.read_range(t, 0, t.n // 2))
+    hn = api.Batch.from_readset(synth.read_range(n, 0, n.n // 2))
+    jobs = [(bt, bn, regions[0]), (bt, bn, regions[1]), (ht, hn, regions[0]), (bt, bn, regions[2]),
+            (bt, bn, regions[0])]
+    want = [pair.call(a, b, rg, "T", t.contig) for a, b, rg in jobs]
     pair.close()
     stream = api.SomaticStream(api.default_params(**params))
     stream.upload_reference(t.contig, synth.genome_str(g).encode())
-    got = stream.run([(bt, bn, rg) for rg in regions + regions[:1]], "T", t.contig)
+    got = stream.run(jobs, "T", t.contig)
     stream.close()
-    assert got == want + want[:1]
+    assert got == want
     assert all(len(w.splitlines()) > 10 for w in want)
+    assert want[2] != want[0]
