@@ -891,10 +891,11 @@ int pileup_variants() { return 6; }
 // (every histogram update is an atomic or an order-free merge), so neither
 // the quota nor the interleaving changes a result.
 int tile_quota(int64_t n_tiles, int resident_blocks) {
-    // at most 4 tiles per block (about a millisecond on a deep batch), and
-    // at least 32 waves of resident blocks' worth
-    const int64_t per = (int64_t)std::max(1, resident_blocks) * 32;
-    return (int)std::max<int64_t>(1, std::min<int64_t>(4, n_tiles / per));
+    // at most 16 tiles per block (a few milliseconds on a deep batch; a
+    // block's exit writes its threads' local-memory state back), and at
+    // least 8 waves of resident blocks' worth
+    const int64_t per = (int64_t)std::max(1, resident_blocks) * 8;
+    return (int)std::max<int64_t>(1, std::min<int64_t>(16, n_tiles / per));
 }
 
 cudaError_t launch_pileup(const DevState &st, const DevParams &P, int resident_blocks, cudaStream_t s, int variant,

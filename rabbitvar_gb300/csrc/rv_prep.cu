@@ -218,15 +218,19 @@ __global__ void __launch_bounds__(kPrepThreads) k_region_fill(RegionFillArgs a) 
             if (lane == 0) s_cnt[cc][w] = __popc(m[cc]);
         }
         __syncthreads();
+        // the warp's lanes of one tile (consecutive entries of a class)
+        // lower its window start with one atomic
+        int jt = -1, v = INT_MAX;
         if (c < 3) {
             long long p = next[c] + __popc(m[c] & lt);
             for (int k = 0; k < w; k++) p += s_cnt[c][k];
             a.list[lb + p] = (uint32_t)i;
-            if (a.span_hi[i] + kEdgeMargin <= R.we) {
-                const long long j = (p - t.start[c]) / t.per[c];
-                atomicMin(&a.tiles[t.base + t.tile0[c] + j].wlo, a.span_lo[i]);
-            }
+            jt = t.tile0[c] + (int)((p - t.start[c]) / t.per[c]);
+            if (a.span_hi[i] + kEdgeMargin <= R.we) v = a.span_lo[i];
         }
+        const unsigned peers = __match_any_sync(0xffffffffu, jt);
+        v = __reduce_min_sync(peers, v);
+        if (jt >= 0 && v != INT_MAX && lane == __ffs(peers) - 1) atomicMin(&a.tiles[t.base + jt].wlo, v);
         for (int cc = 0; cc < 3; cc++)
             for (int k = 0; k < kPrepWarps; k++) next[cc] += s_cnt[cc][k];
         __syncthreads();
