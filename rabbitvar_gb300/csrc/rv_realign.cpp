@@ -23,6 +23,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <deque>
 #include <memory>
 #include <mutex>
 #include <set>
@@ -224,7 +225,37 @@ struct RegionRealigner {
         int seq_kind = 0;
         bool loaded = false;
     };
-    std::map<int, Clip> sc5, sc3;
+    // The soft-clip aggregates by position (the reference's position-keyed
+    // maps, filled in position order by load_lists): an index per position
+    // of the region's cell range into a deque (stable references), and the
+    // filled positions in ascending order for the walks over all of them.
+    struct ClipMap {
+        int lo = 0;
+        std::vector<int32_t> idx;  // per position from lo: index into clips, -1 = absent
+        std::deque<Clip> clips;
+        std::vector<int> pos;      // position of each clip, ascending
+        void init(int clo, int chi) {
+            lo = clo;
+            idx.assign((size_t)std::max(0, chi - clo + 1), -1);
+            clips.clear();
+            pos.clear();
+        }
+        Clip &insert(int p) {
+            int32_t &k = idx[(size_t)(p - lo)];
+            if (k < 0) {
+                k = (int32_t)clips.size();
+                clips.emplace_back();
+                pos.push_back(p);
+            }
+            return clips[(size_t)k];
+        }
+        Clip *find(int p) {
+            const int64_t i = (int64_t)p - lo;
+            if (i < 0 || i >= (int64_t)idx.size() || idx[(size_t)i] < 0) return nullptr;
+            return &clips[(size_t)idx[(size_t)i]];
+        }
+    };
+    ClipMap sc5, sc3;
 
     RegionRealigner(Mirror &m, rv_ctx *c, int r)
         : mir(m), ctx(c), P(c->params), region(r), Rg(m.regions[r]), max_rl(m.regions[r].max_read_len),
@@ -311,10 +342,7 @@ struct RegionRealigner {
         return j == m.keys.end() ? nullptr : &j->second;
     }
 
-    Clip *clip(std::map<int, Clip> &sc, int p) {
-        auto it = sc.find(p);
-        return it == sc.end() ? nullptr : &it->second;
-    }
+    Clip *clip(ClipMap &sc, int p) { return sc.find(p); }
     double *prof = nullptr;  // per-region phase times (trace)
     const string &consensus(Clip &k) {
         if (!k.loaded && k.agg >= 0 && (mir.cmeta[k.agg] >> 31)) {
@@ -372,13 +400,15 @@ struct RegionRealigner {
                     std::map<int, std::map<string, int>> &inscnt) {
         const uint8_t *arena = ctx->h_arena.data();
         const size_t arena_n = ctx->h_arena.size();
+        sc5.init(Rg.clo, Rg.chi);
+        sc3.init(Rg.clo, Rg.chi);
         for (int p = Rg.clo; p <= Rg.chi; p++) {
             const int64_t c = cell_of(p);
             const uint32_t e = mir.off[c + 1];
             for (uint32_t i = mir.off[c]; i < e; i++) {
                 const Slot &s = mir.slots[i];
                 if (s.kind == KIND_SC5 || s.kind == KIND_SC3) {
-                    Clip &k = (s.kind == KIND_SC3 ? sc3 : sc5)[p];
+                    Clip &k = (s.kind == KIND_SC3 ? sc3 : sc5).insert(p);
                     k.c.agg = from_slot(s, mir.sidx[i]);
                     k.cell = c;
                     k.agg = i;
@@ -950,10 +980,14 @@ struct RegionRealigner {
     // by position with their rank in t3.
     struct LgT { int pos; Clip *c; int cnt; };
     void lgins_lists(std::vector<LgT> &t5, std::vector<LgT> &t3, std::vector<std::pair<int, int>> &by_pos) {
-        for (auto &e : sc5)
-            if (!(e.first < Rg.start - 5000 || e.first > Rg.end + 5000)) t5.push_back({e.first, &e.second, e.second.c.agg.cnt});
-        for (auto &e : sc3)
-            if (!(e.first < Rg.start - 5000 || e.first > Rg.end + 5000)) t3.push_back({e.first, &e.second, e.second.c.agg.cnt});
+        for (size_t k = 0; k < sc5.clips.size(); k++) {
+            const int p = sc5.pos[k];
+            if (!(p < Rg.start - 5000 || p > Rg.end + 5000)) t5.push_back({p, &sc5.clips[k], sc5.clips[k].c.agg.cnt});
+        }
+        for (size_t k = 0; k < sc3.clips.size(); k++) {
+            const int p = sc3.pos[k];
+            if (!(p < Rg.start - 5000 || p > Rg.end + 5000)) t3.push_back({p, &sc3.clips[k], sc3.clips[k].c.agg.cnt});
+        }
         auto by_cnt = [](const LgT &a, const LgT &b) { return a.cnt != b.cnt ? a.cnt > b.cnt : a.pos < b.pos; };
         std::sort(t5.begin(), t5.end(), by_cnt);
         std::sort(t3.begin(), t3.end(), by_cnt);
