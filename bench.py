@@ -675,21 +675,23 @@ def measure_pair(g, tumor, normal, regions, args, dist, clocks, device: int, wor
     sites = 2 * sum(b - a + 1 for a, b in regions)
     score_stage_ms = (host_ms["score"] + host_ms["format"]) / args.steps
     out["sites_per_s"] = sites / (score_stage_ms * 1e-3)
+    # the tumor's k_pileup_tiles launch, timed alone right after the timed
+    # region on the same batch (in the timed steps both samples' kernels
+    # share the GPU, one stream each)
+    tile_ms_shared = statistics.mean(s_["pileup_tiles"] for s_ in stages[0::2])
+    solo = []
+    for _ in range(3):
+        pair.tumor.pileup()
+        solo.append(pair.tumor.stage_times()["pileup_tiles"])
+    tile_ms = statistics.mean(solo)
+    cells = sum(b - a + 1 for a, b in regions)
+    window = sum(b - a + 1 + 2 * 1200 for a, b in regions)
+    per_launch_bytes = read_alg_bytes(tumor) + cells * 256 + window  # reads + site records + reference windows
+    achieved = per_launch_bytes / (tile_ms * 1e-3) / 1e9
+    peak, peak_kind = measured_peak_hbm()
+    out["tumor_tile_launch"] = {"launch_ms": tile_ms, "reads": int(tumor.n), "achieved_gbs": achieved,
+                                "frac": achieved / peak, "peak_kind": peak_kind}
     if roofline:
-        # the tumor's k_pileup_tiles launch, timed alone right after the timed
-        # region on the same batch (in the timed steps both samples' kernels
-        # share the GPU, one stream each)
-        tile_ms_shared = statistics.mean(s_["pileup_tiles"] for s_ in stages[0::2])
-        solo = []
-        for _ in range(3):
-            pair.tumor.pileup()
-            solo.append(pair.tumor.stage_times()["pileup_tiles"])
-        tile_ms = statistics.mean(solo)
-        cells = sum(b - a + 1 for a, b in regions)
-        window = sum(b - a + 1 + 2 * 1200 for a, b in regions)
-        per_launch_bytes = read_alg_bytes(tumor) + cells * 256 + window  # reads + site records + reference windows
-        achieved = per_launch_bytes / (tile_ms * 1e-3) / 1e9
-        peak, peak_kind = measured_peak_hbm()
         traffic = PILEUP_TRAFFIC_PER_READ * tumor.n if PILEUP_TRAFFIC_PER_READ else None
         out["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                            "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
@@ -712,7 +714,8 @@ def pair_1mb_leg(args, device: int) -> dict:
     r = measure_pair(g, tumor, normal, regions, args, None, clocks, device, 1, roofline=False)
     out = {"workload": workload(args.local_realign), "value": r["value"], "e2e": r["e2e"]["value"],
            "unit": "reads/s", "ms_per_step": r["ms_per_step"], "reads_per_step": r["reads_per_step"],
-           "records_per_step": r["records_per_step"], "host_call_ms_per_step": r["host_call_ms_per_step"]}
+           "records_per_step": r["records_per_step"], "host_call_ms_per_step": r["host_call_ms_per_step"],
+           "tumor_tile_launch": r["tumor_tile_launch"]}
     if not args.no_bam:
         out["e2e_from_bam"] = bam_leg(g, tumor, normal, regions, args.local_realign, args.steps, args.warmup,
                                       device, r["text"])
