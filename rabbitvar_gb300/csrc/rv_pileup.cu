@@ -260,12 +260,18 @@ template <bool AGG>
 struct TileFast {
     uint32_t w_s;       // shared-space address of the word arrays (w0 | w1 | w2 | first, 4*kTileW words each)
     uint32_t ref_s;     // shared-space address of the reference bases wlo .. wlo + kTileW - 1
+    uint32_t code_s;    // and of their codes (ref_code_of)
     int wlo;
     int goodq;          // integer quality threshold (DevParams::goodq_i)
     // reference base at p (inside the region's window): from the tile's shared copy
     __device__ __forceinline__ char ref(const char *refp, int p) const {
         unsigned d = (unsigned)(p - wlo);
         return d < (unsigned)kTileW ? (char)shared_ld_u8(ref_s + d) : __ldg(refp + p - 1);
+    }
+    // its code (ref_code_of), from the tile's shared copy of the codes
+    __device__ __forceinline__ int ref_code(const char *refp, int p) const {
+        unsigned d = (unsigned)(p - wlo);
+        return d < (unsigned)kTileW ? (int)shared_ld_u8(code_s + d) : ref_code_of(__ldg(refp + p - 1));
     }
     __device__ __forceinline__ bool emit(int p, int b, int dir, int tp, int q, int mapq, int nm) const {
         if (AGG) return emit_warp(p, b, dir, tp, q, mapq, nm);
@@ -594,6 +600,7 @@ __global__ void __launch_bounds__(kPileupThreads, MINB) k_pileup_tiles(DevState 
     uint32_t *first = w2 + 4 * TW;
     __shared__ int s_tile;
     __shared__ char s_ref[TW];
+    __shared__ uint8_t s_code[TW];
     for (int done = 0; done < quota; done++) {
         if (threadIdx.x == 0) s_tile = (int)atomicAdd(st.tile_counter, 1u);
         __syncthreads();
@@ -607,7 +614,9 @@ __global__ void __launch_bounds__(kPileupThreads, MINB) k_pileup_tiles(DevState 
         for (int i = threadIdx.x; i < 4 * 4 * TW; i += blockDim.x) w0[i] = 0u;
         for (int i = threadIdx.x; i < TW; i += blockDim.x) {
             const int64_t p = (int64_t)wlo + i;  // 1-based; the walk reads it only inside [ws, we]
-            s_ref[i] = (p >= 1 && p <= st.ref_len) ? st.ref[p - 1] : (char)0;
+            const char c = (p >= 1 && p <= st.ref_len) ? st.ref[p - 1] : (char)0;
+            s_ref[i] = c;
+            s_code[i] = (uint8_t)ref_code_of(c);
         }
         __syncthreads();
         TileSink<AGG> sink;
@@ -618,6 +627,7 @@ __global__ void __launch_bounds__(kPileupThreads, MINB) k_pileup_tiles(DevState 
         sink.f.w_s = (uint32_t)__cvta_generic_to_shared(w0);
         sink.f.wlo = wlo;
         sink.f.ref_s = (uint32_t)__cvta_generic_to_shared(s_ref);
+        sink.f.code_s = (uint32_t)__cvta_generic_to_shared(s_code);
         sink.f.goodq = P.goodq_i;
         {
             Walker<TileSink<AGG>> w(P, sink, R, st.ref, st.ref_len);

@@ -82,12 +82,21 @@ __device__ __forceinline__ uint32_t pick_word(const uint4 &v, int k) {
 
 // BAM 4-bit code -> 0..3 for A/C/G/T, -1 otherwise
 __device__ __forceinline__ int code_base(int code) {
-    return code == 1 ? 0 : (code == 2 ? 1 : (code == 4 ? 2 : (code == 8 ? 3 : -1)));
+    // the one-bit codes 1, 2, 4, 8 are A, C, G, T
+    return __popc((unsigned)code) == 1 ? __ffs(code) - 1 : -1;
 }
 
 // Sinks without an inline fast path for single-base observations.
+// Reference base code for the per-base loop: 0-3 for A/C/G/T (base_index),
+// 5 for 'N', 4 for anything else.
+__device__ __forceinline__ int ref_code_of(char c) {
+    const int b = base_index(c);
+    return b >= 0 ? b : (c == 'N' ? 5 : 4);
+}
+
 struct NoFast {
     __device__ __forceinline__ char ref(const char *refp, int p) const { return __ldg(refp + p - 1); }
+    __device__ __forceinline__ int ref_code(const char *refp, int p) const { return ref_code_of(__ldg(refp + p - 1)); }
     __device__ __forceinline__ bool emit(int, int, int, int, int, int, int) const { return false; }
 };
 
@@ -922,12 +931,14 @@ struct Walker {
                 const int q0 = (int)((pick_word(qw, (rp & 15) >> 2) >> ((rp & 3) * 8)) & 255u);
                 const int b = code_base(code);
                 const bool hs = st >= ws && st <= we;
-                const char rc = hs ? fe.ref(refp, st) : (char)0;
-                const bool mm = hs && base_index(rc) != b;
+                // the reference base's code (ref_code_of): a mismatch is any
+                // code but the read base's, 'N' is code 5
+                const int rcode = hs ? fe.ref_code(refp, st) : 4;
+                const bool mm = hs && rcode != b;
                 bool slow = b < 0 || i >= tail_from;
                 // a high-quality mismatch enters the MNV growth; most end
                 // there as the single base and are emitted like a match
-                if (!slow && mm && q0 >= goodq && st + 1 >= rs && st + 1 <= re && i + 1 < celr && rc != 'N')
+                if (!slow && mm && q0 >= goodq && st + 1 >= rs && st + 1 <= re && i + 1 < celr && rcode != 5)
                     slow = !snv_stays_single(fe, rp, st, i, celr, goodq);
                 if (!slow) {
                     const bool tr = ttr != 0 && (dir ? tlen - rp > ttr : rp > ttr);
