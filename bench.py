@@ -173,9 +173,9 @@ REF_REGIONS = list(range(0, PANEL_REGIONS, 25))
 CPU_TILES = 40   # 1 Mb pair: CPU sample of 40 of the 100 tiles
 # DRAM bytes (read + write) per read of one k_pileup_tiles launch, from one
 # ncu capture of a tumor launch of the deep panel on a 16-region slice
-# (2.67 M reads, 1563.6 MB read + 1369.3 MB written); the headline launch's
+# (2.67 M reads, 1541.7 MB read + 1368.3 MB written); the headline launch's
 # traffic is this times its reads
-PILEUP_TRAFFIC_PER_READ = (1563.6e6 + 1369.3e6) / 2666656
+PILEUP_TRAFFIC_PER_READ = (1541.7e6 + 1368.3e6) / 2666656
 
 
 def deep_workload(rank: int = 0, world: int = 1, only=None):
