@@ -486,8 +486,8 @@ def panel_leg(n_reg: int, k: int, steps: int, warmup: int, device: int = 0, per_
     """Batched amplicon panel (config 2's shape: n_reg regions of U(100, 2000)
     bp, depth log-normal median 500x, amplicon reads with 0.5% exact
     duplicates, -t -u, simple mode), from pinned host batches through the C
-    ABI.  Batched: all regions in one submit and one persistent pileup
-    launch (the pileup chain as a CUDA graph); region by region: one submit
+    ABI.  Batched: all regions in one submit and one pileup launch (the
+    pileup chain as a CUDA graph); region by region: one submit
     and pipeline per region (the reference's per-region stage sequence), on
     the first `per_region_sample` regions, whose records must equal the
     batched run's records for them."""

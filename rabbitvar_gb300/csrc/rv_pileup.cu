@@ -584,8 +584,8 @@ __device__ void read_span(const Batch &B, int64_t r, int &lo, int &hi, bool wide
 // ---------------------------------------------------------------------------
 // kernels
 // ---------------------------------------------------------------------------
-// The region fields the host computed from the read spans (span_lo/hi,
-// serial) stay; only the per-launch edge flag is reset.
+// The region fields the batch preparation computed from the read spans
+// (span_lo/hi, serial) stay; only the per-launch edge flag is reset.
 __global__ void k_region_reset(DevState st) {
     int reg = blockIdx.x * blockDim.x + threadIdx.x;
     if (reg < st.n_regions) st.regions[reg].edge_hit = 0;
@@ -609,7 +609,7 @@ __global__ void __launch_bounds__(kPileupThreads, MINB) k_pileup_tiles(DevState 
         const Tile tile = st.tiles[t];
         const Region &R = st.regions[tile.region];
         // window start: the lowest span start of the tile's non-edge reads
-        // (computed on the host from the same CIGAR arithmetic as read_span)
+        // (computed by the batch preparation from the same CIGAR arithmetic as read_span)
         const int wlo = tile.wlo;
         for (int i = threadIdx.x; i < 4 * 4 * TW; i += blockDim.x) w0[i] = 0u;
         for (int i = threadIdx.x; i < TW; i += blockDim.x) {
