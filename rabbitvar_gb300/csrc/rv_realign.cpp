@@ -980,6 +980,8 @@ struct RegionRealigner {
     // by position with their rank in t3.
     struct LgT { int pos; Clip *c; int cnt; };
     void lgins_lists(std::vector<LgT> &t5, std::vector<LgT> &t3, std::vector<std::pair<int, int>> &by_pos) {
+        t5.clear();
+        t3.clear();
         for (size_t k = 0; k < sc5.clips.size(); k++) {
             const int p = sc5.pos[k];
             if (!(p < Rg.start - 5000 || p > Rg.end + 5000)) t5.push_back({p, &sc5.clips[k], sc5.clips[k].c.agg.cnt});
@@ -1001,10 +1003,17 @@ struct RegionRealigner {
     // `used` marks, which only skip pairs, are left out).  Appends each pair
     // as four int32 (offset and length of the 5' and of the 3' consensus in
     // `strs`) and records its index for find35.
+    // the lists of the last lgins_lists call (collect_lgins_pairs builds them;
+    // no clip count changes before realignlgins30 reads them)
+    std::vector<LgT> lg_t5, lg_t3;
+    std::vector<std::pair<int, int>> lg_by_pos;
+    bool lg_ready = false;
+
     void collect_lgins_pairs(std::vector<int32_t> &pairs, string &strs) {
-        std::vector<LgT> t5, t3;
-        std::vector<std::pair<int, int>> by_pos;
-        lgins_lists(t5, t3, by_pos);
+        lgins_lists(lg_t5, lg_t3, lg_by_pos);
+        lg_ready = true;
+        std::vector<LgT> &t5 = lg_t5, &t3 = lg_t3;
+        const std::vector<std::pair<int, int>> &by_pos = lg_by_pos;
         // every 3' clip's consensus length; the "long" ones (more than 10
         // characters) by position with their rank in t3.  A 3' clip of 10 or
         // fewer characters does nothing in realignlgins30's loop: its
@@ -1058,13 +1067,14 @@ struct RegionRealigner {
     // insert stay local), the nested realignins/realigndel use the shared one
     void realignlgins30() {
         PRef RL = R;
-        std::vector<LgT> t5, t3;
         // the 3' clips by position (with their rank in t3): a 5' clip only
         // pairs with 3' clips in [p5 - 2.5 max_rl, p5 + max_rl - 10], and the
         // reference's loop over t3 does nothing else for the others, so the
         // pass visits just those, in t3 order
-        std::vector<std::pair<int, int>> by_pos;
-        lgins_lists(t5, t3, by_pos);
+        if (!lg_ready) lgins_lists(lg_t5, lg_t3, lg_by_pos);
+        lg_ready = false;
+        std::vector<LgT> &t5 = lg_t5, &t3 = lg_t3;
+        const std::vector<std::pair<int, int>> &by_pos = lg_by_pos;
         const bool dev = f35_res != nullptr;  // device results for the listed pairs
         std::vector<int> near_host;
         for (size_t ia = 0; ia < t5.size(); ia++) {
