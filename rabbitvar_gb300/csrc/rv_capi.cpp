@@ -53,7 +53,11 @@ rv_status grow(rv_ctx *ctx, T *&p, size_t &cap, size_t need) {
 // Pinned host buffer of at least `need` bytes (grown with headroom).
 rv_status ensure_pinned(rv_ctx *ctx, void **p, size_t &cap, size_t need) {
     if (need <= cap && *p) return RV_OK;
-    if (*p) cudaFreeHost(*p);
+    // a copy queued from the old buffer may still be running
+    if (*p) {
+        RV_CUDA(cudaDeviceSynchronize());
+        cudaFreeHost(*p);
+    }
     *p = nullptr;
     cap = 0;
     const size_t n = std::max<size_t>(need + need / 4, 4096);
